@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark of the dense-BEM hot path on GB300: frequency-solves/sec (and panel-pairs/sec).
+
+Workload (one "step"): the 2000-panel truncated vertical cylinder (r = 5 m,
+draft 10 m; side 40 x 40 + bottom 10 x 40 panels), 30 wave frequencies uniform
+in [0.2, 3.0] rad/s, 6 rigid-body dofs about the origin radiating + 1 heading
+(beta = 0) diffracting, the default Green functions (Rankine + image + GFWu),
+direct BEM, infinite depth, rho = 1025, g = 9.81.  One frequency-solve = one
+(body, omega): assemble S and D, factorize, solve all 7 right-hand sides,
+integrate forces.  Synthetic mesh (no dataset).
+
+  value  -- inputs resident in HBM (mesh handle, dof fields, device outputs)
+  e2e    -- the public C-ABI call with host buffers: mesh upload, dof upload,
+            sweep, coefficient read-back, all inside the timed region
+  --impl reference -- the CPU oracle (C restatement of the reference) on the
+            host cores, same workload and metric, a bounded sample per step
+
+Multi-GPU (torchrun): every rank runs the same per-GPU workload on its own GPU
+(independent (body, omega) units, no collective on the data path; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_OMEGA = 30
+OMEGAS = np.linspace(0.2, 3.0, N_OMEGA)
+RHO, G = 1025.0, 9.81
+DOFS = ["Surge", "Sway", "Heave", "Roll", "Pitch", "Yaw"]
+BETAS = [0.0]
+WORKLOAD = ("vertical cylinder r=5 m draft=10 m, 2000 panels (side 40x40 + bottom 10x40), 30 omega uniform "
+            "[0.2,3.0] rad/s, 6 rigid dofs radiating + 1 heading, Rankine+image+GFWu, direct BEM, infinite depth")
+METRIC = "frequency-solves/sec"
+UNIT = "frequency-solves/s"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def build_workload(mh):
+    mesh = mh.config2_cylinder()
+    body = mh.FloatingBody(mesh, DOFS, rotation_center=(0.0, 0.0, 0.0), body_name="cylinder")
+    return mesh, body
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the oracle on the host cores
+# ---------------------------------------------------------------------------
+def cpu_frequency_solves(mesh, body, n_omega, oracle):
+    """Run the oracle's frequency-solves for the first n_omega frequencies; returns seconds."""
+    t0 = time.perf_counter()
+    for om in OMEGAS[:n_omega]:
+        oracle.hydro_one_frequency(mesh, body.dofs, float(om), rho=RHO, g=G, betas=BETAS, lapack=True)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(mesh, body, oracle, budget_s=12.0):
+    """Bounded sample: as many frequencies as fit in ~budget_s (at least 2)."""
+    t_one = cpu_frequency_solves(mesh, body, 1, oracle)
+    n = int(max(2, min(N_OMEGA, budget_s // max(t_one, 1e-3))))
+    t = cpu_frequency_solves(mesh, body, n, oracle)
+    return {"value": n / t, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n} of the 30 frequencies of the same workload (N=2000), oracle C assembly with OpenMP on "
+                      f"{os.cpu_count()} threads + LAPACK zgesv (numpy) for the 7 right-hand sides"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    from __graft_entry__ import load_package
+    mh = load_package()
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.build()
+    mesh, body = build_workload(mh)
+    per_step = 2
+    for _ in range(args.warmup):
+        cpu_frequency_solves(mesh, body, 1, oracle)
+    times = [cpu_frequency_solves(mesh, body, per_step, oracle) for _ in range(args.steps)]
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "step": f"{per_step} of the 30 frequency-solves (bounded CPU sample)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{per_step} frequencies per step of the N=2000 workload; oracle C assembly "
+                                       f"(OpenMP, {os.cpu_count()} threads) + LAPACK zgesv"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        smax = max(float(r[2]) for r in rows)
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3] not in ("", "[N/A]"))}
+
+
+def lu_gemm_flops(n, nb=32):
+    """Algorithmic real flops of the trailing updates of one n x n complex LU (8 per complex MAC)."""
+    f = 0
+    for k in range(0, n, nb):
+        kb = min(nb, n - k)
+        rest = n - k - kb
+        f += 8 * rest * rest * kb
+    return f
+
+
+def run_gpu(args):
+    import ctypes
+
+    import torch
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from __graft_entry__ import load_package
+    mh = load_package()
+    from marinehydro_gb300 import _lib
+
+    ctx = mh.Context(local)
+    mesh, body = build_workload(mh)
+    n = mesh.nfaces
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    names = list(body.dofs)
+    dofs_h = body.dof_array(names)
+    dofs_d = torch.from_numpy(dofs_h).to(dev)
+    rad = np.arange(len(DOFS), dtype=np.int32)
+    inf = np.arange(len(DOFS), dtype=np.int32)
+    om = np.ascontiguousarray(OMEGAS)
+    be = np.asarray(BETAS, dtype=np.float64)
+    gfs = mh.gf_flags(mh.default_greens_functions("Wu"))
+    nr, ni, nb, nw = len(rad), len(inf), len(be), N_OMEGA
+    outs_d = [torch.empty(ni * nr * nw, dtype=torch.float64, device=dev) for _ in range(2)] + \
+             [torch.empty(ni * nw * nb * 2, dtype=torch.float64, device=dev) for _ in range(3)]
+    dmesh = mesh.device_mesh(ctx)
+    L = ctx._L
+
+    def step_device(precision):
+        ctx.check(L.mh_hydrodynamic_coefficients(
+            ctx.handle, dmesh.handle, nw, om.ctypes.data, RHO, G, gfs, 1, len(names), dofs_d.data_ptr(), nr,
+            rad.ctypes.data, ni, inf.ctypes.data, nb, be.ctypes.data, precision,
+            *[o.data_ptr() for o in outs_d], _lib.MH_MEM_DEVICE), "sweep")
+
+    # e2e: pinned host inputs and outputs through the same C-ABI
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    V_h, C_h, N_h = pin(mesh.panel_vertices), pin(mesh.centers), pin(mesh.normals)
+    A_h, R_h, dofs_hp = pin(mesh.areas), pin(mesh.radii), pin(dofs_h)
+    outs_h = [pin(np.empty(ni * nr * nw)) for _ in range(2)] + [pin(np.empty(ni * nw * nb * 2)) for _ in range(3)]
+
+    def step_e2e(precision):
+        h = ctypes.c_void_p()
+        ctx.check(L.mh_mesh_create(ctx.handle, n, V_h.ctypes.data, C_h.ctypes.data, N_h.ctypes.data,
+                                   A_h.ctypes.data, R_h.ctypes.data, _lib.MH_MEM_HOST, ctypes.byref(h)), "mesh")
+        try:
+            ctx.check(L.mh_hydrodynamic_coefficients(
+                ctx.handle, h, nw, om.ctypes.data, RHO, G, gfs, 1, len(names), dofs_hp.ctypes.data, nr,
+                rad.ctypes.data, ni, inf.ctypes.data, nb, be.ctypes.data, precision,
+                *[o.ctypes.data for o in outs_h], _lib.MH_MEM_HOST), "sweep")
+        finally:
+            L.mh_mesh_destroy(h)
+
+    nsmall = 2 * nw + nb + (nr + ni + 1) // 2 + 1 + 8
+    h2d = 8 * (V_h.size + C_h.size + N_h.size + A_h.size + R_h.size + dofs_hp.size) + 8 * nsmall
+    d2h = 16 * nw * ni * (nr + nb) + 16 * nw * ni * nb + 4 * nw
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, steps, warmup, profile=False):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            dist.barrier()
+        if profile:
+            ctx.profile_reset()
+            ctx.profile(True)
+        l0 = ctx.launch_count()
+        tot = 0.0
+        wall0 = time.perf_counter()
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)  # L2 flush between timed steps (outside the event pair)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1) / 1e3
+        wall = time.perf_counter() - wall0
+        launches = ctx.launch_count() - l0
+        prof = None
+        if profile:
+            prof = ctx.profile_read()
+            ctx.profile(False)
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            t = torch.tensor([tot], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+            dist.barrier()
+        return tot, wall, launches, prof
+
+    peak64, peak32 = ctx.probe_fma_peaks()
+    with ClockSampler(local) as clk:
+        t_dev, wall_dev, launches, prof = timed(lambda: step_device(_lib.MH_PREC_FP64), args.steps, args.warmup,
+                                                profile=True)
+    clocks = clk.summary()
+    res64 = [o.cpu().numpy().copy() for o in outs_d]
+    t_e2e, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_FP64), max(2, args.steps // 2), 1)
+    e2e_steps = max(2, args.steps // 2)
+    t_mix, _, _, prof_mix = timed(lambda: step_device(_lib.MH_PREC_MIXED), args.steps, 1, profile=True)
+    resmx = [o.cpu().numpy() for o in outs_d]
+    dev_mix = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(resmx, res64))
+    t_e2e_mix, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_MIXED), e2e_steps, 1)
+
+    units = N_OMEGA * args.steps * ws
+    value = units / t_dev
+    ms_step = 1e3 * t_dev / args.steps
+
+    # roofline of the dominant kernel group (FP64 FMA bound)
+    total_ms = sum(v[0] for v in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    top_name, (top_ms, top_launches) = top
+    share = {k: round(v[0] / total_ms, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    pairs_per_step = N_OMEGA * n * n
+    asm_ms = sum(v[0] for k, v in prof.items() if k.startswith("assemble"))
+    roof = None
+    if top_name == "lu_gemm_f64":
+        flops_per_launch = lu_gemm_flops(n) * N_OMEGA / (top_launches / args.steps)
+        achieved = flops_per_launch / (top_ms / top_launches * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": top_name, "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                "frac": achieved / peak64, "traffic": None,
+                "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks (MEASURED_PEAKS.json "
+                               "has no FP64 figure)",
+                "work": "8 real flops per complex multiply-add of the trailing update, summed over panel steps"}
+    else:
+        roof = {"bound": "fp64", "kernel": top_name, "achieved": None, "peak": peak64, "unit": "TFLOP/s",
+                "frac": None, "traffic": None}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "panels": n, "omegas": N_OMEGA, "rhs_per_omega": len(DOFS) + len(BETAS),
+                   "precision": "fp64 (LU, pivoting and substitution in FP64)",
+                   "l2": "flushed before every timed step (256 MiB write); per-step working set 3.8 GB > L2"},
+        "panel_pairs_per_sec": pairs_per_step * args.steps * ws / (asm_ms * 1e-3) if asm_ms > 0 else None,
+        "gpu_launches": launches,
+        "e2e": {"value": N_OMEGA * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof,
+        "kernel_time_share": share,
+        "clocks": clocks,
+        "variants": {"mixed_precision_ir": {
+            "value": N_OMEGA * args.steps * ws / t_mix, "unit": UNIT,
+            "e2e": N_OMEGA * e2e_steps * ws / t_e2e_mix,
+            "max_rel_dev_vs_fp64": dev_mix,
+            "note": "FP32 LU factors + FP64 iterative refinement to FP64 accuracy; same assembly",
+            "kernel_time_share": {k: round(v[0] / sum(x[0] for x in prof_mix.values()), 4)
+                                  for k, v in sorted(prof_mix.items(), key=lambda kv: -kv[1][0])}}},
+        "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        oracle.build()
+        line["cpu_baseline"] = cpu_baseline(mesh, body, oracle)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,179 @@
+/*
+ * marinehydro_gb300.h -- C-ABI of libmarinehydro_cuda.so, the GB300 (sm_103a)
+ * implementation of MarineHydro.jl's dense boundary-element hot path:
+ * influence-matrix assembly (Birk / Delhommeau Rankine panel integrals and their
+ * free-surface image, the Wu and exact Guevel-Delhommeau infinite-depth wave
+ * Green functions) and the complex linear solve that turns S and D into added
+ * mass, radiation damping and excitation forces.
+ *
+ * Every entry point names the reference (MarineHydro.jl) interface it replaces,
+ * as file:line in the MarineHydro.jl tree.  The reference-side ccall bindings are
+ * listed in INTEGRATION.md.
+ *
+ * Conventions
+ *   - All arithmetic on the plain path is FP64.
+ *   - Complex numbers are interleaved (re, im) doubles, i.e. the memory layout of
+ *     Julia's ComplexF64, C99 double _Complex and cuDoubleComplex.
+ *   - Matrices are column-major (Julia's layout): entry (i, j) at [i + j*n].
+ *   - A mesh is passed per panel ("gathered" vertices), so no face-index base
+ *     (Julia 1-based vs Capytaine 0-based) crosses the ABI:
+ *       vertices n x 4 x 3 (panel, corner, xyz), centers n x 3, normals n x 3,
+ *       areas n, radii n  (meshes.jl:42-51, 255-277).
+ *   - Buffers are owned by the caller.  `mem` says where they live:
+ *     MH_MEM_HOST (pageable or pinned host memory; the library copies) or
+ *     MH_MEM_DEVICE (device pointers on the context's device).
+ *   - Calls are synchronous: on return, outputs are complete in the caller's
+ *     buffers.  A context is not thread-safe; use one context per host thread.
+ *   - Every function returns an mh_status; mh_last_error() describes the last
+ *     failure on a context.  No C++ exception crosses the ABI.
+ */
+#ifndef MARINEHYDRO_GB300_H
+#define MARINEHYDRO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MH_ABI_VERSION 1
+
+typedef enum {
+    MH_OK = 0,
+    MH_ERR_ARG = 1,           /* bad argument (maps to ArgumentError / DimensionMismatch) */
+    MH_ERR_UNSUPPORTED = 2,   /* unsupported combination (ArgumentError) */
+    MH_ERR_SINGULAR = 3,      /* exactly zero pivot (LinearAlgebra.SingularException) */
+    MH_ERR_CUDA = 4,          /* CUDA runtime error */
+    MH_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+    MH_ERR_NOT_CONVERGED = 6, /* mixed-precision refinement did not converge */
+    MH_ERR_NOMEM = 7          /* device allocation failed */
+} mh_status;
+
+/* Green-function selection: a bit set mirroring the reference's GF tuples
+   (formulations.jl:5-37; green_functions/*.jl).  The default formulation
+   (Rankine(), RankineReflected(), GFWu()) is MH_GF_DEFAULT_WU. */
+#define MH_GF_RANKINE                        1u  /* Birk vectorized Rankine (rankine_vectorized.jl) */
+#define MH_GF_RANKINE_REFLECTED              2u  /* its free-surface image (rankine_reflected.jl) */
+#define MH_GF_RANKINE_REFLECTED_NEGATIVE     4u  /* minus the image (rankine_reflected_negative.jl) */
+#define MH_GF_DELHOMMEAU_RANKINE             8u  /* Capytaine-style Rankine (rankine.jl) */
+#define MH_GF_DELHOMMEAU_RANKINE_REFLECTED  16u  /* its image */
+#define MH_GF_WU                            32u  /* GFWu (wu.jl) */
+#define MH_GF_EXACT_DELHOMMEAU              64u  /* ExactGuevelDelhommeau (exact_Guevel_Delhommeau.jl) */
+#define MH_GF_DEFAULT_WU  (MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_WU)
+#define MH_GF_DEFAULT_EGD (MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_EXACT_DELHOMMEAU)
+
+#define MH_MEM_HOST 0
+#define MH_MEM_DEVICE 1
+
+/* Linear-solve precision.  MH_PREC_FP64: LU, pivoting and substitution in FP64
+   (the reference's arithmetic).  MH_PREC_MIXED: LU factors in FP32 with FP64
+   partial pivoting decisions on FP32 data, then FP64 iterative refinement of
+   every right-hand side to a backward error below 1e-14 (falls back to FP64 LU
+   when refinement stalls). */
+#define MH_PREC_FP64 0
+#define MH_PREC_MIXED 1
+
+typedef struct mh_context mh_context;
+typedef struct mh_mesh mh_mesh;
+
+/* ---- context ---------------------------------------------------------- */
+int mh_abi_version(void);
+/* Creates a context on CUDA device `device` with its own stream. */
+int mh_create(int device, mh_context** out);
+int mh_destroy(mh_context* ctx);
+/* Text of the last error on this context ("" if none).  Never NULL. */
+const char* mh_last_error(const mh_context* ctx);
+/* The cudaStream_t the context launches on (as void*).  mh_set_stream(ctx, NULL)
+   restores the context's own stream. */
+int mh_get_stream(mh_context* ctx, void** stream);
+int mh_set_stream(mh_context* ctx, void* stream);
+int mh_synchronize(mh_context* ctx);
+/* Number of kernels this context has launched since creation. */
+int64_t mh_launch_count(const mh_context* ctx);
+/* Device bytes currently held by the context's workspaces. */
+int64_t mh_workspace_bytes(const mh_context* ctx);
+
+/* ---- mesh --------------------------------------------------------------- */
+/* Replaces StaticArraysMesh(...) + element(mesh, j) (meshes.jl:42-51, 255-277):
+   uploads one body's panels and precomputes the per-panel Birk frame
+   (birk_panel_geometry, rankine_vectorized.jl:129-137). */
+int mh_mesh_create(mh_context* ctx, int64_t n_panels, const double* vertices, const double* centers,
+                   const double* normals, const double* areas, const double* radii, int mem, mh_mesh** out);
+int mh_mesh_destroy(mh_mesh* mesh);
+int64_t mh_mesh_panels(const mh_mesh* mesh);
+
+/* ---- assembly ----------------------------------------------------------- */
+/* Replaces assemble_matrices(green_functions, mesh::StaticArraysMesh, k;
+   direct, include_identity, all_normals) -> (S, D)   (matrix_assembly.jl:167-222,
+   274-369, 70-88).  S, D: n x n complex, column-major.  fixed_normal: NULL or
+   3 doubles (the reference's `all_normals`, e.g. [1,0,0] for forward speed).
+   The wavenumber-independent Rankine part is cached on the mesh per
+   (gfs, direct, include_identity, fixed_normal) and reused across wavenumbers. */
+int mh_assemble_matrices(mh_context* ctx, mh_mesh* mesh, double wavenumber, uint32_t gfs, int direct,
+                         int include_identity, const double* fixed_normal, double* S, double* D, int mem);
+
+/* ---- dense complex solves ------------------------------------------------ */
+/* Replaces linsolve(A, b) / _linearsolve / gpu_linsolve (matrix_assembly.jl:396-434):
+   X = A \ B, A n x n, B and X n x nrhs complex.  X may alias B. */
+int mh_linsolve(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const double* B, double* X,
+                int precision, int mem);
+/* Replaces solve(D, S, bc; direct) -> (phi, sources) (matrix_assembly.jl:436-449).
+   direct: phi = D \ (S bc), `sources` untouched (may be NULL).
+   indirect: sources = D \ bc (D is K), phi = S sources. */
+int mh_solve(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const double* S, const double* bc,
+             int direct, double* phi, double* sources, int precision, int mem);
+/* The adjoint solve of the IFT rule for _linearsolve / gpu_linsolve
+   (ad_rules.jl:360-414): lambda = A^H \ ybar. */
+int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const double* Ybar,
+                        double* Lambda, int precision, int mem);
+
+/* ---- hydrodynamic coefficients over a frequency sweep ------------------- */
+/* Replaces hydrodynamic_coefficients(body, params, formulation)
+   (problems_and_results.jl:464-495) with _hydro_one_frequency (:472-478) for a
+   zero-forward-speed body: for every omega, S and D are assembled once and all
+   radiation and diffraction right-hand sides are solved together.
+     dofs:      n_dofs x n x 3 dof fields (bodies.jl:382-426), [d][i][xyz]
+     rad_idx:   n_rad indices into dofs (radiating_dofs)
+     inf_idx:   n_inf indices into dofs (influenced_dofs)
+     betas:     n_beta wave directions (wave_directions)
+   Outputs (column-major, like the reference's arrays with n_U = 1):
+     added_mass, radiation_damping: n_inf x n_rad x n_omega doubles
+     diffraction_force, froude_krylov_force, excitation_force:
+                                    n_inf x n_omega x n_beta complex
+   Any output may be NULL when its group is empty. */
+int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas,
+                                 double rho, double g, uint32_t gfs, int direct, int64_t n_dofs,
+                                 const double* dofs, int64_t n_rad, const int32_t* rad_idx, int64_t n_inf,
+                                 const int32_t* inf_idx, int64_t n_beta, const double* betas, int precision,
+                                 double* added_mass, double* radiation_damping, double* diffraction_force,
+                                 double* froude_krylov_force, double* excitation_force, int mem);
+
+/* ---- wave-term evaluators (kernel-level parity entry points) ------------- */
+/* _wu_wave_term_and_derivs(hh, vv) (wu.jl:28-37) for m points: out 3 complex
+   per point (GF, dGF/dhh, dGF/dvv), i.e. 6 doubles. */
+int mh_wu_wave_terms(mh_context* ctx, int64_t m, const double* hh, const double* vv, double* out, int mem);
+/* _dimless_wave_term and _d_dimless_wave_term_dr (exact_Guevel_Delhommeau.jl:15-46)
+   for m points: out 2 complex per point; rtol/atol: adaptive Gauss-Kronrod
+   tolerances (the reference's Integrals.jl call uses its defaults). */
+int mh_exact_wave_terms(mh_context* ctx, int64_t m, const double* r, const double* z, double rtol, double atol,
+                        double* out, int mem);
+/* Tolerances used by assembly with MH_GF_EXACT_DELHOMMEAU (default 1e-12, 1e-14). */
+int mh_set_quadrature_tolerance(mh_context* ctx, double rtol, double atol);
+
+/* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* Per-kernel-group device timing with CUDA events on the launching stream.
+   mh_profile_read fills up to `capacity` groups: names (32 chars each, NUL
+   padded), total milliseconds and launch counts; *n_groups = groups recorded. */
+int mh_profile_enable(mh_context* ctx, int enable);
+int mh_profile_reset(mh_context* ctx);
+int mh_profile_read(mh_context* ctx, int64_t capacity, char* names, double* total_ms, int64_t* launches,
+                    int64_t* n_groups);
+/* Measured FP64 / FP32 fused-multiply-add throughput of the device (TFLOP/s),
+   the denominators of the FP64-bound kernels' roofline. */
+int mh_probe_fma_peaks(mh_context* ctx, double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARINEHYDRO_GB300_H */

@@ -1,0 +1,26 @@
+"""marinehydro_gb300 -- GB300 (sm_103a) implementation of MarineHydro.jl's dense-BEM hot path.
+
+The Python surface mirrors the reference's Julia API; assembly, dense solves and
+the frequency sweep run in libmarinehydro_cuda.so (hand-written CUDA, FP64 plain
+path) behind the C-ABI declared in include/marinehydro_gb300.h.  The directory
+name is not a Python identifier; load it with ``load_package()`` below or
+``importlib`` under the name ``marinehydro_gb300``.
+"""
+from ._lib import (Context, MarineHydroError, default_context, load as load_library)  # noqa: F401
+from .api import (airy_bc, airy_pressure, assemble_matrices, assemble_matrix_wu, calculate_radiation_forces,  # noqa
+                  compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
+                  gpu_linsolve, hydrodynamic_coefficients, integrate_pressure, linsolve, linsolve_adjoint,
+                  problems_from_data, radiation_bc, solve, solve_linear, solve_problem)
+from .bodies import FloatingBody, combine_floatingbodies, rotational_dofs, translational_dofs  # noqa: F401
+from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineReflected, DirectBEM,  # noqa: F401
+                           ExactGuevelDelhommeau, GFWu, GreensFunction, IndirectBEM, Rankine, RankineReflected,
+                           RankineReflectedNegative, bem_formulation, default_greens_functions, gf_flags, is_direct,
+                           partition_greens_functions)
+from .meshes import (Mesh, StaticArraysMesh, barge_mesh, combine_meshes, config1_hemisphere,  # noqa: F401
+                     config2_cylinder, hemisphere_mesh, random_body, smesh, tiny_static_mesh, vertical_cylinder_mesh)
+from .problems import (SETTINGS, DiffractionProblem, DiffractionResult, RadiationProblem,  # noqa: F401
+                       RadiationResult, added_mass, compute_encountered_values, compute_wavenumber,
+                       diffraction_force, make_result, radiation_coefficients, radiation_damping, remake, set_g,
+                       set_rho)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

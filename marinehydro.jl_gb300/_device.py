@@ -1,0 +1,156 @@
+"""Device-side handles and thin wrappers over the C-ABI calls."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import MH_MEM_DEVICE, MH_MEM_HOST, ptr_and_mem
+
+
+class DeviceMesh:
+    """An mh_mesh: one body's panels resident on the device of `ctx`."""
+
+    def __init__(self, ctx: _lib.Context, mesh):
+        self.ctx = ctx
+        self.n = mesh.nfaces
+        V = np.ascontiguousarray(mesh.panel_vertices, dtype=np.float64)
+        C = np.ascontiguousarray(mesh.centers, dtype=np.float64)
+        N = np.ascontiguousarray(mesh.normals, dtype=np.float64)
+        A = np.ascontiguousarray(mesh.areas, dtype=np.float64)
+        R = np.ascontiguousarray(mesh.radii, dtype=np.float64)
+        h = ctypes.c_void_p()
+        ctx.check(ctx._L.mh_mesh_create(ctx.handle, self.n, V.ctypes.data, C.ctypes.data, N.ctypes.data,
+                                        A.ctypes.data, R.ctypes.data, MH_MEM_HOST, ctypes.byref(h)),
+                  "mh_mesh_create")
+        self._h = h
+
+    @classmethod
+    def from_device_arrays(cls, ctx, n, V, C, N, A, R):
+        """Build from device buffers (objects with __cuda_array_interface__)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.n = int(n)
+        ptrs = [ptr_and_mem(x) for x in (V, C, N, A, R)]
+        if any(m != MH_MEM_DEVICE for _, m in ptrs):
+            raise TypeError("from_device_arrays needs device arrays")
+        h = ctypes.c_void_p()
+        ctx.check(ctx._L.mh_mesh_create(ctx.handle, self.n, *[p for p, _ in ptrs], MH_MEM_DEVICE, ctypes.byref(h)),
+                  "mh_mesh_create")
+        self._h = h
+        return self
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.ctx._L.mh_mesh_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _c128(a, shape=None, order="F"):
+    a = np.asarray(a, dtype=np.complex128)
+    if shape is not None:
+        a = a.reshape(shape, order=order)
+    return np.asfortranarray(a)
+
+
+def assemble(ctx, dmesh: DeviceMesh, k: float, gfs: int, direct: bool, include_identity: bool, fixed_normal=None):
+    n = dmesh.n
+    S = np.empty((n, n), dtype=np.complex128, order="F")
+    D = np.empty((n, n), dtype=np.complex128, order="F")
+    fx = None
+    if fixed_normal is not None:
+        fx = np.ascontiguousarray(np.asarray(fixed_normal, dtype=np.float64).reshape(3))
+    ctx.check(ctx._L.mh_assemble_matrices(ctx.handle, dmesh.handle, float(k), int(gfs), int(bool(direct)),
+                                          int(bool(include_identity)), fx.ctypes.data if fx is not None else None,
+                                          S.ctypes.data, D.ctypes.data, MH_MEM_HOST), "assemble_matrices")
+    return S, D
+
+
+def linsolve(ctx, A, B, precision=_lib.MH_PREC_FP64, adjoint=False):
+    A = _c128(A)
+    n = A.shape[0]
+    if A.shape != (n, n):
+        raise ValueError(f"A must be square, got {A.shape}")
+    Bv = np.asarray(B, dtype=np.complex128)
+    vec = Bv.ndim == 1
+    if Bv.shape[0] != n:
+        raise ValueError(f"dimension mismatch: A is {n}x{n}, b has {Bv.shape[0]} rows")
+    Bm = np.asfortranarray(Bv.reshape(n, -1, order="F"))
+    X = np.empty_like(Bm, order="F")
+    fn = ctx._L.mh_linsolve_adjoint if adjoint else ctx._L.mh_linsolve
+    ctx.check(fn(ctx.handle, n, Bm.shape[1], A.ctypes.data, Bm.ctypes.data, X.ctypes.data, int(precision),
+                 MH_MEM_HOST), "linsolve")
+    return X[:, 0].copy() if vec else X
+
+
+def solve_linear(ctx, D, S, bc, direct=True, precision=_lib.MH_PREC_FP64):
+    D = _c128(D)
+    S = _c128(S)
+    n = D.shape[0]
+    b = np.asarray(bc, dtype=np.complex128)
+    vec = b.ndim == 1
+    if b.shape[0] != n or S.shape != (n, n) or D.shape != (n, n):
+        raise ValueError("dimension mismatch between D, S and bc")
+    B = np.asfortranarray(b.reshape(n, -1, order="F"))
+    phi = np.empty_like(B, order="F")
+    src = None if direct else np.empty_like(B, order="F")
+    ctx.check(ctx._L.mh_solve(ctx.handle, n, B.shape[1], D.ctypes.data, S.ctypes.data, B.ctypes.data,
+                              int(bool(direct)), phi.ctypes.data, None if direct else src.ctypes.data,
+                              int(precision), MH_MEM_HOST), "solve")
+    if vec:
+        return phi[:, 0].copy(), (None if direct else src[:, 0].copy())
+    return phi, src
+
+
+def wu_wave_terms(ctx, hh, vv):
+    hh = np.ascontiguousarray(np.asarray(hh, dtype=np.float64).ravel())
+    vv = np.ascontiguousarray(np.asarray(vv, dtype=np.float64).ravel())
+    m = hh.size
+    out = np.empty((m, 3), dtype=np.complex128)
+    ctx.check(ctx._L.mh_wu_wave_terms(ctx.handle, m, hh.ctypes.data, vv.ctypes.data, out.ctypes.data, MH_MEM_HOST),
+              "wu wave terms")
+    return out
+
+
+def exact_wave_terms(ctx, r, z, rtol=1e-12, atol=1e-14):
+    r = np.ascontiguousarray(np.asarray(r, dtype=np.float64).ravel())
+    z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).ravel())
+    m = r.size
+    out = np.empty((m, 2), dtype=np.complex128)
+    ctx.check(ctx._L.mh_exact_wave_terms(ctx.handle, m, r.ctypes.data, z.ctypes.data, float(rtol), float(atol),
+                                         out.ctypes.data, MH_MEM_HOST), "exact wave terms")
+    return out
+
+
+def hydro_sweep(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, direct, dofs, rad_idx, inf_idx, betas,
+                precision=_lib.MH_PREC_FP64, out=None):
+    """mh_hydrodynamic_coefficients with host buffers; returns the five arrays."""
+    om = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
+    be = np.ascontiguousarray(np.asarray(betas, dtype=np.float64).ravel())
+    dofs = np.ascontiguousarray(np.asarray(dofs, dtype=np.float64))
+    ri = np.ascontiguousarray(np.asarray(rad_idx, dtype=np.int32).ravel())
+    ii = np.ascontiguousarray(np.asarray(inf_idx, dtype=np.int32).ravel())
+    nw, nb, nr, ni = om.size, be.size, ri.size, ii.size
+    nd = dofs.shape[0] if dofs.size else 0
+    A = np.empty((ni, nr, nw), dtype=np.float64, order="F")
+    B = np.empty_like(A)
+    Fd = np.empty((ni, nw, nb), dtype=np.complex128, order="F")
+    Fk = np.empty_like(Fd)
+    Fe = np.empty_like(Fd)
+    p = lambda a: a.ctypes.data if a.size else None
+    ctx.check(ctx._L.mh_hydrodynamic_coefficients(
+        ctx.handle, dmesh.handle, nw, om.ctypes.data, float(rho), float(g), int(gfs), int(bool(direct)), nd,
+        p(dofs), nr, p(ri), ni, p(ii), nb, p(be), int(precision), p(A), p(B), p(Fd), p(Fk), p(Fe), MH_MEM_HOST),
+        "hydrodynamic_coefficients")
+    return A, B, Fd, Fk, Fe

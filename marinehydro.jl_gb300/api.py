@@ -1,0 +1,256 @@
+"""The reference's public solve path, re-targeted at libmarinehydro_cuda.so.
+
+Mirrors (names, argument meaning, errors):
+  assemble_matrices(gfs, mesh, k; direct, include_identity, all_normals)   matrix_assembly.jl:164-222
+  linsolve(A, b) / gpu_linsolve                                            matrix_assembly.jl:396-434
+  solve(D, S, bc; direct) -> (phi, sources)                                matrix_assembly.jl:436-449
+  solve(problem, formulation)                                              solve.jl:183-214
+  radiation_bc / airy_bc / integrate_pressure / froude_krylov_force       waves.jl:154-303
+  problems_from_data / hydrodynamic_coefficients                          problems_and_results.jl:242-495
+Assembly and dense solves always run on the GPU; there is no CPU fallback.  The
+O(N) boundary conditions and force sums of `solve(problem, ...)` run in numpy
+exactly where the reference runs them on the host; `hydrodynamic_coefficients`
+keeps everything on the device.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _device, _lib
+from .bodies import FloatingBody, evaluate_gradient_of_motion
+from .formulations import BEMFormulation, DirectBEM, bem_formulation, gf_flags, is_direct
+from .meshes import StaticArraysMesh
+from .problems import (DiffractionProblem, DiffractionResult, RadiationProblem, RadiationResult, SETTINGS,
+                       compute_wavenumber, make_result)
+
+
+def _ctx(ctx=None):
+    return ctx if ctx is not None else _lib.default_context(0)
+
+
+def _prec(precision):
+    if precision in (None, "fp64", _lib.MH_PREC_FP64):
+        return _lib.MH_PREC_FP64
+    if precision in ("mixed", _lib.MH_PREC_MIXED):
+        return _lib.MH_PREC_MIXED
+    raise ValueError('precision must be "fp64" or "mixed"')
+
+
+# ---------------------------------------------------------------------------
+# matrix level
+# ---------------------------------------------------------------------------
+def assemble_matrices(green_functions, mesh: StaticArraysMesh, wavenumber, direct=True, include_identity=True,
+                      all_normals=None, ctx=None):
+    """(S, D) influence matrices, n x n complex (matrix_assembly.jl:167-222)."""
+    c = _ctx(ctx)
+    return _device.assemble(c, mesh.device_mesh(c), wavenumber, gf_flags(green_functions), direct,
+                            include_identity, all_normals)
+
+
+def assemble_matrix_wu(mesh, wavenumber, direct=True, all_normals=None, ctx=None):
+    """assemble_matrix_wu (matrix_assembly.jl:372-374)."""
+    from .formulations import GFWu, Rankine, RankineReflected
+
+    return assemble_matrices((Rankine(), RankineReflected(), GFWu()), mesh, wavenumber, direct=direct,
+                             all_normals=all_normals, ctx=ctx)
+
+
+def linsolve(A, b, precision="fp64", ctx=None):
+    """A \\ b (matrix_assembly.jl:396-416); raises numpy.linalg.LinAlgError on an exactly singular A."""
+    return _device.linsolve(_ctx(ctx), A, b, _prec(precision))
+
+
+gpu_linsolve = linsolve
+
+
+def linsolve_adjoint(A, ybar, precision="fp64", ctx=None):
+    """lambda = A^H \\ ybar, the adjoint solve of the IFT rule (ad_rules.jl:360-414)."""
+    return _device.linsolve(_ctx(ctx), A, ybar, _prec(precision), adjoint=True)
+
+
+def solve_linear(D, S, bc, direct=True, precision="fp64", ctx=None):
+    """solve(D, S, bc; direct) -> (phi, sources) (matrix_assembly.jl:436-449)."""
+    return _device.solve_linear(_ctx(ctx), D, S, bc, direct, _prec(precision))
+
+
+# ---------------------------------------------------------------------------
+# physics around the solve (waves.jl)
+# ---------------------------------------------------------------------------
+def _normal_displacement(mesh, dof):
+    return np.einsum("ij,ij->i", mesh.normals, dof)
+
+
+def radiation_bc(problem: RadiationProblem) -> np.ndarray:
+    """radiation_bc(problem) (waves.jl:183-199)."""
+    mesh = problem.floatingbody.mesh
+    dof = problem.floatingbody.dofs[problem.radiating_dof]
+    bc = (-1j * problem.encountered_omega) * _normal_displacement(mesh, dof)
+    if problem.forward_speed != 0:
+        ddx = evaluate_gradient_of_motion(mesh, problem.radiating_dof)
+        bc = bc + problem.forward_speed * _normal_displacement(mesh, ddx)
+    return bc
+
+
+def _airy_vel(centers, problem):
+    """_airy_vel (waves.jl:266-273)."""
+    k = problem.wavenumber
+    wbar = centers[:, 0] * np.cos(problem.encountered_beta) + centers[:, 1] * np.sin(problem.encountered_beta)
+    cih = np.exp(k * centers[:, 2])
+    amp = problem.g * k / problem.omega * np.exp(1j * k * wbar)
+    return np.stack([amp * np.cos(problem.beta) * cih, amp * np.sin(problem.beta) * cih, -1j * amp * cih], axis=1)
+
+
+def airy_bc(problem: DiffractionProblem) -> np.ndarray:
+    """_airy_bc(::StaticArraysMesh) (waves.jl:275-282)."""
+    mesh = problem.floatingbody.mesh
+    v = _airy_vel(mesh.centers, problem)
+    n = mesh.normals
+    return -(v[:, 0] * n[:, 0] + v[:, 1] * n[:, 1] + v[:, 2] * n[:, 2])
+
+
+def compute_bc(problem):
+    return radiation_bc(problem) if isinstance(problem, RadiationProblem) else airy_bc(problem)
+
+
+def airy_pressure(problem: DiffractionProblem) -> np.ndarray:
+    """_airy_pressure(::StaticArraysMesh) (waves.jl:259-264, 301-303)."""
+    c = problem.floatingbody.mesh.centers
+    k = problem.wavenumber
+    wbar = c[:, 0] * np.cos(problem.encountered_beta) + c[:, 1] * np.sin(problem.encountered_beta)
+    phi = -1j * problem.g / problem.omega * np.exp(k * c[:, 2]) * np.exp(1j * k * wbar)
+    return 1j * problem.omega * problem.rho * phi
+
+
+def integrate_pressure(body: FloatingBody, influenced_dofs, pressure) -> dict:
+    """integrate_pressure (waves.jl:154-178): {dof: sum p_i * -(dof_i . n_i) * a_i}."""
+    mesh = body.mesh
+    out = {}
+    for d in influenced_dofs:
+        disp = _normal_displacement(mesh, body.dofs[d])
+        out[d] = complex(np.sum(pressure * -disp * mesh.areas))
+    return out
+
+
+def froude_krylov_force(problem_or_result, influenced_dofs=None) -> dict:
+    """froude_krylov_force (waves.jl:294-298; problems_and_results.jl:216-217)."""
+    prob = problem_or_result.problem if isinstance(problem_or_result, DiffractionResult) else problem_or_result
+    inf = prob.influenced_dofs if influenced_dofs is None else influenced_dofs
+    return integrate_pressure(prob.floatingbody, inf, airy_pressure(prob))
+
+
+def excitation_force(res: DiffractionResult) -> dict:
+    """diffraction + Froude-Krylov (problems_and_results.jl:218-219)."""
+    fk = froude_krylov_force(res)
+    return {k: v + fk[k] for k, v in res.forces.items()}
+
+
+# ---------------------------------------------------------------------------
+# problem level
+# ---------------------------------------------------------------------------
+def solve(problem, formulation: BEMFormulation | None = None, ctx=None):
+    """solve(problem, formulation) (solve.jl:195-201) or, for arrays, solve(D, S, bc; direct)."""
+    if isinstance(problem, (list, tuple)):
+        return [solve(p, formulation, ctx=ctx) for p in problem]
+    if isinstance(problem, np.ndarray):
+        raise TypeError("use solve_linear(D, S, bc, direct=...) for the matrix-level solve")
+    f = formulation or DirectBEM()
+    c = _ctx(ctx)
+    direct = is_direct(f)
+    omega = problem.omega if problem.forward_speed == 0 else problem.encountered_omega
+    k = problem.wavenumber if problem.forward_speed == 0 else problem.encountered_wavenumber
+    mesh = problem.floatingbody.mesh
+    bc = compute_bc(problem)
+    S, D = assemble_matrices(f.greens, mesh, k, direct=direct, ctx=c)
+    potential, sources = _device.solve_linear(c, D, S, bc, direct, f.precision_code)
+    pressure = 1j * problem.rho * omega * potential
+    if problem.forward_speed != 0:
+        # _maybe_forward_speed_pressure (solve.jl:171-181)
+        if direct:
+            raise ValueError("nonzero forward speed is not supported with the direct method; use IndirectBEM "
+                             "(direct = false)")
+        _, K = assemble_matrices(f.greens, mesh, k, direct=False, all_normals=[1.0, 0.0, 0.0], ctx=c)
+        pressure = pressure + problem.rho * problem.forward_speed * (K @ sources)
+    return make_result(problem, integrate_pressure(problem.floatingbody, problem.influenced_dofs, pressure))
+
+
+def solve_problem(problem, formulation=None, direct=True, gf="Wu", greens_functions=None, ctx=None):
+    return solve(problem, bem_formulation(formulation, direct, gf, greens_functions), ctx=ctx)
+
+
+def problems_from_data(parameters: dict, body: FloatingBody) -> dict:
+    """problems_from_data (problems_and_results.jl:242-283)."""
+    oms = np.atleast_1d(np.asarray(parameters["wave_frequencies"], dtype=float))
+    inf = list(parameters.get("influenced_dofs", list(body.dofs)))
+    Us = list(parameters.get("forward_speeds", [0.0]))
+    rad = []
+    if "radiating_dofs" in parameters:
+        betas = parameters.get("wave_directions", [0.0]) if "forward_speeds" in parameters else [0.0]
+        for U in Us:
+            for om in oms:
+                for d in parameters["radiating_dofs"]:
+                    for b in betas:
+                        rad.append(RadiationProblem(body, om, d, inf, beta=b if U != 0 else None, forward_speed=U,
+                                                    rho=parameters.get("rho"), g=parameters.get("g")))
+    dif = []
+    if "wave_directions" in parameters:
+        for U in Us:
+            for om in oms:
+                for b in parameters["wave_directions"]:
+                    dif.append(DiffractionProblem(body, om, b, inf, forward_speed=U, rho=parameters.get("rho"),
+                                                  g=parameters.get("g")))
+    return {"radiation": rad, "diffraction": dif}
+
+
+def hydrodynamic_coefficients(body: FloatingBody, parameters: dict, formulation: BEMFormulation | None = None,
+                              ctx=None, rho=None, g=None) -> dict:
+    """hydrodynamic_coefficients (problems_and_results.jl:464-495) for zero forward speed.
+
+    Returns numpy arrays with the reference's shapes (n_U = 1):
+      added_mass, radiation_damping: (n_inf, n_rad, n_omega, 1)
+      diffraction_force, Froude_Krylov_force, excitation_force: (n_inf, n_omega, n_beta, 1)
+    One assembly of S and D and one factorization per frequency serve every
+    radiation and diffraction right-hand side.
+    """
+    f = formulation or DirectBEM()
+    if any(u != 0 for u in parameters.get("forward_speeds", [0.0])):
+        raise ValueError("hydrodynamic_coefficients on the GPU sweep supports forward_speeds = [0] only; "
+                         "use solve(RadiationProblem(..., forward_speed=U), IndirectBEM())")
+    c = _ctx(ctx)
+    oms = np.atleast_1d(np.asarray(parameters["wave_frequencies"], dtype=float))
+    names = list(body.dofs)
+    inf = list(parameters.get("influenced_dofs", names))
+    rad = list(parameters.get("radiating_dofs", []))
+    betas = list(parameters.get("wave_directions", []))
+    idx = {n: i for i, n in enumerate(names)}
+    dofs = body.dof_array(names)
+    rho = parameters.get("rho", SETTINGS["rho"]) if rho is None else rho
+    g = parameters.get("g", SETTINGS["g"]) if g is None else g
+    A, B, Fd, Fk, Fe = _device.hydro_sweep(c, body.mesh.device_mesh(c), oms, rho, g, gf_flags(f.greens),
+                                           is_direct(f), dofs, [idx[d] for d in rad], [idx[d] for d in inf], betas,
+                                           f.precision_code)
+    return {
+        "added_mass": A[..., None] if rad else np.zeros(0),
+        "radiation_damping": B[..., None] if rad else np.zeros(0),
+        "diffraction_force": Fd[..., None] if betas else np.zeros(0),
+        "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
+        "excitation_force": Fe[..., None] if betas else np.zeros(0),
+    }
+
+
+def compute_hydrodynamic_coefficients(parameters, body, formulation=None, direct=True, gf="Wu",
+                                      greens_functions=None, ctx=None):
+    return hydrodynamic_coefficients(body, parameters, bem_formulation(formulation, direct, gf, greens_functions),
+                                     ctx=ctx)
+
+
+def calculate_radiation_forces(mesh, dof, omega, rho=None, g=None, ctx=None):
+    """calculate_radiation_forces (waves.jl:47-55): [A, B] for a uniform dof vector."""
+    rho = SETTINGS["rho"] if rho is None else rho
+    g = SETTINGS["g"] if g is None else g
+    k = compute_wavenumber(omega, g)
+    S, D = assemble_matrix_wu(mesh, k, ctx=ctx)
+    bc = -1j * omega * (mesh.normals @ np.asarray(dof, dtype=float))
+    phi, _ = solve_linear(D, S, bc, ctx=ctx)
+    p = 1j * rho * omega * phi
+    F = np.sum(p * -(mesh.normals @ np.asarray(dof, dtype=float)) * mesh.areas)
+    return [F.real / omega ** 2, F.imag / omega]

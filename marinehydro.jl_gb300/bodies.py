@@ -1,0 +1,105 @@
+"""Floating bodies and rigid-body dof fields (bodies.jl)."""
+from __future__ import annotations
+
+import numpy as np
+
+from .meshes import StaticArraysMesh, combine_meshes
+
+TRANSLATIONS = ("Surge", "Sway", "Heave")
+ROTATIONS = ("Roll", "Pitch", "Yaw")
+
+
+def translational_dofs(mesh: StaticArraysMesh, name: str) -> np.ndarray:
+    """translational_dofs (bodies.jl:382-394): a unit vector on every panel."""
+    dof = np.zeros((mesh.nfaces, 3))
+    dof[:, TRANSLATIONS.index(name)] = 1.0
+    return dof
+
+
+def rotational_dofs(mesh: StaticArraysMesh, name: str, rotation_center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """rotational_dofs (bodies.jl:411-426): axis x (center_i - rotation_center)."""
+    if name not in ROTATIONS:
+        raise ValueError(f"unknown rotational dof {name}")
+    axis = np.zeros(3)
+    axis[ROTATIONS.index(name)] = 1.0
+    return np.cross(axis, mesh.centers - np.asarray(rotation_center, dtype=float))
+
+
+def evaluate_gradient_of_motion(mesh: StaticArraysMesh, name: str) -> np.ndarray:
+    """evaluate_gradient_of_motion (bodies.jl:363-374), forward-speed problems only."""
+    if name not in TRANSLATIONS + ROTATIONS:
+        raise ValueError("forward speed problems are only developed for rigid body dofs")
+    d = np.zeros((mesh.nfaces, 3))
+    if name == "Pitch":
+        d[:, 2] = 1.0
+    elif name == "Yaw":
+        d[:, 1] = -1.0
+    return d
+
+
+class FloatingBody:
+    """FloatingBody (bodies.jl:9-51): mesh, optional lid, named dof fields (n x 3)."""
+
+    def __init__(self, mesh: StaticArraysMesh, dofs=None, rotation_center=None, body_name: str = "body",
+                 lid_mesh=None):
+        if lid_mesh is not None:
+            raise ValueError("lid meshes (irregular-frequency removal) are not supported by the GPU path")
+        self.mesh = mesh
+        self.lid_mesh = None
+        self.body_name = body_name
+        if dofs is None:
+            dofs = {}
+        if isinstance(dofs, dict):
+            self.dofs = {str(k): np.ascontiguousarray(np.asarray(v, dtype=float)) for k, v in dofs.items()}
+        else:  # rigid dof names
+            rc = (0.0, 0.0, 0.0) if rotation_center is None else rotation_center
+            self.dofs = {}
+            for name in dofs:
+                name = str(name)
+                self.dofs[name] = (translational_dofs(mesh, name) if name in TRANSLATIONS
+                                   else rotational_dofs(mesh, name, rc))
+        for k, v in self.dofs.items():
+            if v.shape != (mesh.nfaces, 3):
+                raise ValueError(f"dof {k} must have shape ({mesh.nfaces}, 3)")
+
+    def __add__(self, other):
+        return combine_floatingbodies([self, other])
+
+    def dof_array(self, names=None) -> np.ndarray:
+        names = list(self.dofs) if names is None else list(names)
+        return np.ascontiguousarray(np.stack([self.dofs[n] for n in names])) if names else np.zeros((0, 0, 3))
+
+
+def _unique_names(names):
+    """make_body_name_list_unique (bodies.jl:446-469)."""
+    seen, out = {}, []
+    for s in names:
+        if s not in seen:
+            out.append(s)
+            seen[s] = 2
+        else:
+            c = seen[s]
+            new = f"{s}_{c}"
+            while new in seen or new in names:
+                c += 1
+                new = f"{s}_{c}"
+            out.append(new)
+            seen[s] = c + 1
+            seen[new] = 1
+    return out
+
+
+def combine_floatingbodies(bodies, new_body_name: str | None = None) -> FloatingBody:
+    """combine_floatingbodies (bodies.jl:473-525): one mesh, dofs named body__dof, zero on other bodies."""
+    names = _unique_names([b.body_name.replace(" ", "_") for b in bodies])
+    mesh = combine_meshes([b.mesh for b in bodies])
+    total = mesh.nfaces
+    dofs = {}
+    off = 0
+    for b, nm in zip(bodies, names):
+        for k, v in b.dofs.items():
+            d = np.zeros((total, 3))
+            d[off:off + b.mesh.nfaces] = v
+            dofs[f"{nm}__{k}"] = d
+        off += b.mesh.nfaces
+    return FloatingBody(mesh, dofs, body_name=new_body_name or "+".join(names))

@@ -1,0 +1,361 @@
+// mh_assembly.cu -- influence-matrix assembly kernels (sm_103a, FP64).
+//
+// Replaces the reference's StaticArraysMesh assembly (matrix_assembly.jl:167-369)
+// and its GPU broadcast / KernelAbstractions kernels (matrix_assembly.jl:56-128).
+//
+// Layout: S and D are n x n column-major.  A CTA owns 128 consecutive rows i
+// (one thread per row, so the complex stores of a column are coalesced) and
+// kColsPerCta consecutive columns j; the source-panel records of its columns are
+// staged in shared memory and read as warp-wide broadcasts, the field-panel data
+// of its row stays in registers.
+//
+// The wavenumber-independent part (Rankine + image, and the identity jump) is a
+// separate kernel writing real n x n arrays, so a frequency sweep computes it
+// once per mesh (the reference re-assembles it for every problem; the sum
+// S = S_static + S_wave is the reference's own split, matrix_assembly.jl:183-208).
+#include <cuda_runtime.h>
+
+#include "mh_greens.cuh"
+#include "mh_internal.cuh"
+
+namespace mh {
+
+namespace {
+
+constexpr int kRowsPerCta = 128;
+constexpr int kColsPerCta = 8;
+
+constexpr uint32_t kBirkKinds = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE;
+constexpr uint32_t kDelhKinds = MH_GF_DELHOMMEAU_RANKINE | MH_GF_DELHOMMEAU_RANKINE_REFLECTED;
+
+// birk_panel_geometry (rankine_vectorized.jl:79-137) for every panel, plus the
+// mesh's own center / normal / area / radius.
+__global__ void panel_geometry_kernel(int64_t n, const double* __restrict__ V, const double* __restrict__ C,
+                                      const double* __restrict__ N, const double* __restrict__ A,
+                                      const double* __restrict__ R, PanelRec* __restrict__ out) {
+  int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double* v = V + 12 * j;
+  double mid[4][3], mgc[3], s[3], tt[3], nn[3], t[3];
+  for (int i = 0; i < 4; ++i) {
+    int ip = (i + 1) & 3;
+    for (int c = 0; c < 3; ++c) mid[i][c] = (v[3 * i + c] + v[3 * ip + c]) / 2;
+  }
+  for (int c = 0; c < 3; ++c) {
+    mgc[c] = (mid[1][c] + mid[3][c]) / 2;
+    s[c] = mid[1][c] - mid[3][c];
+    tt[c] = mid[2][c] - mid[0][c];
+  }
+  double ns = sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+  for (int c = 0; c < 3; ++c) s[c] /= ns;
+  nn[0] = s[1] * tt[2] - s[2] * tt[1];
+  nn[1] = s[2] * tt[0] - s[0] * tt[2];
+  nn[2] = s[0] * tt[1] - s[1] * tt[0];
+  double nl = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+  for (int c = 0; c < 3; ++c) nn[c] /= nl;
+  t[0] = nn[1] * s[2] - nn[2] * s[1];
+  t[1] = nn[2] * s[0] - nn[0] * s[2];
+  t[2] = nn[0] * s[1] - nn[1] * s[0];
+  double tl = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+  for (int c = 0; c < 3; ++c) t[c] /= tl;
+  double tc[4][2];
+  for (int k = 0; k < 4; ++k) {
+    double d0 = v[3 * k] - mgc[0], d1 = v[3 * k + 1] - mgc[1], d2 = v[3 * k + 2] - mgc[2];
+    tc[k][0] = d0 * s[0] + d1 * s[1] + d2 * s[2];
+    tc[k][1] = d0 * t[0] + d1 * t[1] + d2 * t[2];
+  }
+  double Ar = 0.0, Mx = 0.0, My = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    int kn = (k + 1) & 3;
+    double xk = tc[k][0], yk = tc[k][1], xk1 = tc[kn][0], yk1 = tc[kn][1];
+    Ar += (yk1 - yk) * (xk + xk1) / 2;
+    Mx += (xk1 - xk) * (yk * yk + yk * yk1 + yk1 * yk1) / 6;
+    My += (yk1 - yk) * (xk * xk + xk * xk1 + xk1 * xk1) / 6;
+  }
+  double clx = My / Ar, cly = -Mx / Ar;
+  PanelRec P;
+  for (int c = 0; c < 3; ++c) {
+    P.T[c] = s[c];
+    P.T[3 + c] = t[c];
+    P.T[6 + c] = nn[c];
+    P.qgc[c] = mgc[c] + clx * s[c] + cly * t[c];
+    P.c[c] = C[3 * j + c];
+    P.n[c] = N[3 * j + c];
+  }
+  for (int k = 0; k < 4; ++k) {
+    P.lc[2 * k] = tc[k][0] - clx;
+    P.lc[2 * k + 1] = tc[k][1] - cly;
+  }
+  P.area = A[j];
+  P.radius = R[j];
+  P.pad[0] = P.pad[1] = P.pad[2] = P.pad[3] = 0.0;
+  out[j] = P;
+}
+
+__device__ __forceinline__ void stage_panels(PanelRec* sp, const PanelRec* __restrict__ P, int64_t j0, int64_t n) {
+  // kColsPerCta records of 16 double2 each
+  const double2* src = reinterpret_cast<const double2*>(P + j0);
+  double2* dst = reinterpret_cast<double2*>(sp);
+  int64_t avail = n - j0;
+  int cnt = (int)(avail < kColsPerCta ? avail : kColsPerCta) * 16;
+  for (int q = threadIdx.x; q < cnt; q += blockDim.x) dst[q] = __ldg(src + q);
+}
+
+template <bool DIRECT>
+__device__ __forceinline__ void pick_normal(const AssemblyParams& p, const PanelRec& Pj, const double ni[3],
+                                            double nv[3]) {
+  // _panel_or_fixed (matrix_assembly.jl:228-230)
+  if (p.has_fixed) { nv[0] = p.fixed[0]; nv[1] = p.fixed[1]; nv[2] = p.fixed[2]; }
+  else if (DIRECT) { nv[0] = Pj.n[0]; nv[1] = Pj.n[1]; nv[2] = Pj.n[2]; }
+  else { nv[0] = ni[0]; nv[1] = ni[1]; nv[2] = ni[2]; }
+}
+
+__device__ __forceinline__ double identity_jump(const AssemblyParams& p, const double ni[3]) {
+  // _add_identity! (matrix_assembly.jl:234-245)
+  if (p.has_fixed) return 0.5 * (p.fixed[0] * ni[0] + p.fixed[1] * ni[1] + p.fixed[2] * ni[2]);
+  return 0.5;
+}
+
+// Static (Rankine-family) part.  BIRK: assemble_birk_rankine (matrix_assembly.jl:274-331);
+// otherwise the broadcasting sum over the static tuple (matrix_assembly.jl:70-88).
+template <bool DIRECT, bool BIRK>
+__global__ void __launch_bounds__(kRowsPerCta) static_kernel(AssemblyParams p, double* __restrict__ SR,
+                                                             double* __restrict__ DR) {
+  __shared__ PanelRec sp[kColsPerCta];
+  const int64_t n = p.n;
+  const int64_t i = blockIdx.x * (int64_t)kRowsPerCta + threadIdx.x;
+  const int64_t j0 = blockIdx.y * (int64_t)kColsPerCta;
+  stage_panels(sp, p.P, j0, n);
+  __syncthreads();
+  if (i >= n) return;
+  double ci[3], ni[3];
+  for (int c = 0; c < 3; ++c) { ci[c] = __ldg(&p.P[i].c[c]); ni[c] = __ldg(&p.P[i].n[c]); }
+  const bool need_R = (p.gfs & MH_GF_RANKINE) != 0;
+  const bool need_I = (p.gfs & MH_GF_RANKINE_REFLECTED) != 0;
+  const bool need_N = (p.gfs & MH_GF_RANKINE_REFLECTED_NEGATIVE) != 0;
+  const double image_sign = (need_I ? 1.0 : 0.0) + (need_N ? -1.0 : 0.0);
+  const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  for (int jj = 0; jj < jmax; ++jj) {
+    const int64_t j = j0 + jj;
+    const PanelRec& Pj = sp[jj];
+    double nv[3];
+    pick_normal<DIRECT>(p, Pj, ni, nv);
+    double s = 0.0, d = 0.0;
+    if (BIRK) {
+      double phi, g[3];
+      if (need_R) {
+        vrankine_from_geom(ci, Pj, phi, g);
+        if (!DIRECT) { g[0] = -g[0]; g[1] = -g[1]; g[2] = -g[2]; }
+        s += phi;
+        d += nv[0] * g[0] + nv[1] * g[1] + nv[2] * g[2];
+      }
+      if (need_I || need_N) {
+        double cr[3] = {ci[0], ci[1], -ci[2]};
+        vrankine_from_geom(cr, Pj, phi, g);
+        if (!DIRECT) { g[0] = -g[0]; g[1] = -g[1]; }  // vertical_reflection(-g)
+        s += image_sign * phi;
+        d += image_sign * (nv[0] * g[0] + nv[1] * g[1] + nv[2] * g[2]);
+      }
+    } else {
+      // canonical tuple order: Rankine, RankineReflected, RankineReflectedNegative,
+      // DelhommeauRankine, DelhommeauRankineReflected
+      const double* vj = p.V + 12 * j;
+      double v12[12];
+      for (int q = 0; q < 12; ++q) v12[q] = __ldg(vj + q);
+      double gs[3] = {0.0, 0.0, 0.0};
+      const uint32_t kinds[5] = {MH_GF_RANKINE, MH_GF_RANKINE_REFLECTED, MH_GF_RANKINE_REFLECTED_NEGATIVE,
+                                 MH_GF_DELHOMMEAU_RANKINE, MH_GF_DELHOMMEAU_RANKINE_REFLECTED};
+      for (int q = 0; q < 5; ++q) {
+        const uint32_t kd = kinds[q];
+        if (!(p.gfs & kd)) continue;
+        const bool refl = kd == MH_GF_RANKINE_REFLECTED || kd == MH_GF_RANKINE_REFLECTED_NEGATIVE ||
+                          kd == MH_GF_DELHOMMEAU_RANKINE_REFLECTED;
+        double pt[3] = {ci[0], ci[1], refl ? -ci[2] : ci[2]};
+        double I, g[3];
+        if (kd & kBirkKinds) {
+          vrankine_from_geom(pt, Pj, I, g);
+          if (!DIRECT) { g[0] = -g[0]; g[1] = -g[1]; g[2] = -g[2]; }
+        } else {
+          delhommeau_rankine(pt, Pj, v12, !DIRECT, I, g);
+        }
+        if (refl && !DIRECT) g[2] = -g[2];
+        if (kd == MH_GF_RANKINE_REFLECTED_NEGATIVE) { I = -I; g[0] = -g[0]; g[1] = -g[1]; g[2] = -g[2]; }
+        s += I;
+        gs[0] += g[0]; gs[1] += g[1]; gs[2] += g[2];
+      }
+      d = nv[0] * gs[0] + nv[1] * gs[1] + nv[2] * gs[2];
+    }
+    double sv = kMinusInv4Pi * s, dv = kMinusInv4Pi * d;
+    if (p.include_identity && i == j) dv += identity_jump(p, ni);
+    SR[i + j * n] = sv;
+    DR[i + j * n] = dv;
+  }
+}
+
+// Wave part for a batch of wavenumbers (blockIdx.z), added to the cached static
+// part.  WU: the fused centres loop (matrix_assembly.jl:343-369, wu.jl:104-127);
+// EGD (or Wu + EGD): broadcasting sum over the wave tuple (matrix_assembly.jl:70-88).
+template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both
+__global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, const double* __restrict__ SR,
+                                                           const double* __restrict__ DR,
+                                                           const double* __restrict__ ks, double2* __restrict__ S,
+                                                           double2* __restrict__ D, int64_t sstride,
+                                                           int wave_identity) {
+  __shared__ PanelRec sp[kColsPerCta];
+  const int64_t n = p.n;
+  const int64_t i = blockIdx.x * (int64_t)kRowsPerCta + threadIdx.x;
+  const int64_t j0 = blockIdx.y * (int64_t)kColsPerCta;
+  const double k = ks[blockIdx.z];
+  double2* Sb = S + blockIdx.z * sstride;
+  double2* Db = D + blockIdx.z * sstride;
+  stage_panels(sp, p.P, j0, n);
+  __syncthreads();
+  if (i >= n) return;
+  double ci[3], ni[3];
+  for (int c = 0; c < 3; ++c) { ci[c] = __ldg(&p.P[i].c[c]); ni[c] = __ldg(&p.P[i].n[c]); }
+  const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  for (int jj = 0; jj < jmax; ++jj) {
+    const int64_t j = j0 + jj;
+    const PanelRec& Pj = sp[jj];
+    double nv[3];
+    pick_normal<DIRECT>(p, Pj, ni, nv);
+    double2 s, d;
+    if (WMODE == 1) {
+      const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+      const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+      wu_sd(ci, Pj.c, nv, Pj.area, k, dx1, dx2, s, d);
+    } else {
+      double2 I = make_double2(0.0, 0.0), gs[3] = {I, I, I};
+      if (WMODE & 1) {
+        double hh, vv;
+        reduced_coords(ci, Pj.c, k, hh, vv);
+        double2 GF, Gh, Gv;
+        wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+        double d1 = 0.0, d2 = 0.0;
+        if (fabs(hh) > 1e-6) {
+          d1 = k * k / hh * (DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0]);
+          d2 = k * k / hh * (DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1]);
+        }
+        I = make_double2((k * GF.x) * Pj.area, (k * GF.y) * Pj.area);
+        gs[0] = make_double2(k * (d1 * Gh.x) * Pj.area, k * (d1 * Gh.y) * Pj.area);
+        gs[1] = make_double2(k * (d2 * Gh.x) * Pj.area, k * (d2 * Gh.y) * Pj.area);
+        gs[2] = make_double2(k * (k * Gv.x) * Pj.area, k * (k * Gv.y) * Pj.area);
+      }
+      if (WMODE & 2) {
+        double2 Ie, ge[3];
+        egd_integrals(ci, Pj.c, k, Pj.area, !DIRECT, p.quad_rtol, p.quad_atol, Ie, ge);
+        I = zadd(I, Ie);
+        gs[0] = zadd(gs[0], ge[0]);
+        gs[1] = zadd(gs[1], ge[1]);
+        gs[2] = zadd(gs[2], ge[2]);
+      }
+      s = I;
+      d = make_double2(nv[0] * gs[0].x + nv[1] * gs[1].x + nv[2] * gs[2].x,
+                       nv[0] * gs[0].y + nv[1] * gs[1].y + nv[2] * gs[2].y);
+    }
+    double2 sv = make_double2(kMinusInv4Pi * s.x, kMinusInv4Pi * s.y);
+    double2 dv = make_double2(kMinusInv4Pi * d.x, kMinusInv4Pi * d.y);
+    if (wave_identity && i == j) dv.x += identity_jump(p, ni);
+    const int64_t idx = i + j * n;
+    if (SR) {
+      sv.x = SR[idx] + sv.x;
+      dv.x = DR[idx] + dv.x;
+    }
+    Sb[idx] = sv;
+    Db[idx] = dv;
+  }
+}
+
+__global__ void static_only_kernel(int64_t count, const double* __restrict__ SR, const double* __restrict__ DR,
+                                   double2* __restrict__ S, double2* __restrict__ D) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= count) return;
+  S[q] = make_double2(SR[q], 0.0);
+  D[q] = make_double2(DR[q], 0.0);
+}
+
+__global__ void wu_points_kernel(int64_t m, const double* __restrict__ hh, const double* __restrict__ vv,
+                                 double2* __restrict__ out) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  double2 a, b, c;
+  wu_wave_term_and_derivs(hh[q], vv[q], a, b, c);
+  out[3 * q] = a;
+  out[3 * q + 1] = b;
+  out[3 * q + 2] = c;
+}
+
+__global__ void exact_points_kernel(int64_t m, const double* __restrict__ r, const double* __restrict__ z,
+                                    double rtol, double atol, double2* __restrict__ out) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  out[2 * q] = egd_adaptive<false>(r[q], z[q], rtol, atol);
+  out[2 * q + 1] = egd_adaptive<true>(r[q], z[q], rtol, atol);
+}
+
+}  // namespace
+
+void launch_panel_geometry(cudaStream_t st, LaunchCounter lc, int64_t n, const double* V, const double* C,
+                           const double* N, const double* A, const double* R, PanelRec* out) {
+  if (n <= 0) return;
+  MH_LAUNCH(lc, st, "panel_geometry",
+            panel_geometry_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, V, C, N, A, R, out));
+}
+
+void launch_assemble_static(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double* SR, double* DR) {
+  if (p.n <= 0) return;
+  dim3 grid((unsigned)((p.n + kRowsPerCta - 1) / kRowsPerCta), (unsigned)((p.n + kColsPerCta - 1) / kColsPerCta));
+  const bool birk = (p.gfs & kDelhKinds) == 0;
+  lc.pre(st);
+  if (p.direct) {
+    if (birk) static_kernel<true, true><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR);
+    else static_kernel<true, false><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR);
+  } else {
+    if (birk) static_kernel<false, true><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR);
+    else static_kernel<false, false><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR);
+  }
+  lc.post(st, "assemble_static");
+}
+
+void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
+                          const double* DR, int nk, const double* ks_dev, double2* S, double2* D, int64_t sstride,
+                          int wave_identity) {
+  if (p.n <= 0 || nk <= 0) return;
+  const uint32_t wv = p.gfs & (MH_GF_WU | MH_GF_EXACT_DELHOMMEAU);
+  if (!wv) {
+    // static only: widen to complex for every requested wavenumber
+    int64_t count = p.n * p.n;
+    for (int b = 0; b < nk; ++b) {
+      MH_LAUNCH(lc, st, "assemble_static_widen",
+                static_only_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(count, SR, DR, S + b * sstride,
+                                                                                     D + b * sstride));
+    }
+    return;
+  }
+  dim3 grid((unsigned)((p.n + kRowsPerCta - 1) / kRowsPerCta), (unsigned)((p.n + kColsPerCta - 1) / kColsPerCta),
+            (unsigned)nk);
+  const int mode = (wv == MH_GF_WU) ? 1 : (wv == MH_GF_EXACT_DELHOMMEAU ? 2 : 3);
+  lc.pre(st);
+#define MH_WAVE(DIR, MODE) wave_kernel<DIR, MODE><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity)
+  if (p.direct) {
+    if (mode == 1) MH_WAVE(true, 1); else if (mode == 2) MH_WAVE(true, 2); else MH_WAVE(true, 3);
+  } else {
+    if (mode == 1) MH_WAVE(false, 1); else if (mode == 2) MH_WAVE(false, 2); else MH_WAVE(false, 3);
+  }
+#undef MH_WAVE
+  lc.post(st, mode == 1 ? "assemble_wave_wu" : "assemble_wave_exact");
+}
+
+void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out) {
+  if (m <= 0) return;
+  MH_LAUNCH(lc, st, "wu_points", wu_points_kernel<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(m, hh, vv, out));
+}
+
+void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* r, const double* z, double rtol,
+                         double atol, double2* out) {
+  if (m <= 0) return;
+  MH_LAUNCH(lc, st, "exact_points",
+            exact_points_kernel<<<(unsigned)((m + 63) / 64), 64, 0, st>>>(m, r, z, rtol, atol, out));
+}
+
+}  // namespace mh

@@ -1,0 +1,450 @@
+// mh_greens.cuh -- device Green-function kernels of the MarineHydro.jl hot path (FP64).
+//
+// Each function restates the reference function cited beside it (paths within the
+// MarineHydro.jl tree).  Special functions are CUDA's (j0, j1, y0, y1, exp, log,
+// atan2, sqrt, hypot, sincos); the complex exponential integral and the
+// Gauss-Kronrod rule are written from their published definitions (DLMF 6.6.2 /
+// 6.9.1; Kronrod's 15-point nodes, QUADPACK qk15).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mh_internal.cuh"
+
+namespace mh {
+
+// ------------------------------- complex ------------------------------------
+__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ double zabs(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ double2 zdiv(double2 a, double2 b) {
+  // Smith's algorithm (scaled) for a / b
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, den = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  } else {
+    double r = b.x / b.y, den = b.y + b.x * r;
+    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+  }
+}
+__device__ __forceinline__ double2 zexp(double2 a) {
+  double s, c;
+  sincos(a.y, &s, &c);
+  double e = exp(a.x);
+  return make_double2(e * c, e * s);
+}
+__device__ __forceinline__ double2 zlog(double2 a) { return make_double2(log(hypot(a.x, a.y)), atan2(a.y, a.x)); }
+
+// ------------------------------- Birk Rankine -------------------------------
+constexpr double kBirkZTol = 1e-14;   // rankine_vectorized.jl:24
+constexpr double kBirkDkTol = 1e-14;  // rankine_vectorized.jl:25
+
+// _abs_ad (rankine_vectorized.jl:30): -0.0 stays -0.0
+__device__ __forceinline__ double abs_ad(double x) { return x < 0.0 ? -x : x; }
+// _atan_ratio (rankine_vectorized.jl:42-45)
+__device__ __forceinline__ double atan_ratio(double num, double den) {
+  double flipped = den < 0.0 ? -num : num;
+  return atan2(flipped, abs_ad(den));
+}
+
+// birk_phi_and_velocity (rankine_vectorized.jl:241-267); lc = 4 local corners (x, y)
+__device__ inline void birk_phi_and_velocity(double x, double y, double z, const double* lc, double& phi,
+                                             double v[3]) {
+  double sx[4], sy[4], r[4], e[4], h[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    sx[k] = x - lc[2 * k];
+    sy[k] = y - lc[2 * k + 1];
+    r[k] = sqrt(sx[k] * sx[k] + sy[k] * sy[k] + z * z);
+    e[k] = sx[k] * sx[k] + z * z;
+    h[k] = sx[k] * sy[k];
+  }
+  const bool inplane = fabs(z) <= kBirkZTol;  // _inplane_atan (:49-54)
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int kn = (k + 1) & 3;
+    double dx = lc[2 * kn] - lc[2 * k];
+    double dy = lc[2 * kn + 1] - lc[2 * k + 1];
+    double dk = hypot(dx, dy);
+    if (!(dk <= kBirkDkTol)) {
+      double rsum = r[k] + r[kn];
+      double log_term = log((rsum - dk) / (rsum + dk));
+      double lt_dk = log_term / dk;
+      double vzk = 0.0;
+      if (!inplane)
+        vzk = atan_ratio(dy * e[k] - dx * h[k], dx * z * r[k]) - atan_ratio(dy * e[kn] - dx * h[kn], dx * z * r[kn]);
+      s0 += (sx[k] * dy - sy[k] * dx) * lt_dk + z * vzk;
+      s1 += dy * lt_dk;
+      s2 += -dx * lt_dk;
+      s3 += vzk;
+    }
+  }
+  phi = kMinusInv4Pi * s0;
+  v[0] = kMinusInv4Pi * s1;
+  v[1] = kMinusInv4Pi * s2;
+  v[2] = kMinusInv4Pi * s3;
+}
+
+// _vrankine_from_geom (rankine_vectorized.jl:273-287): integral of 1/r over panel P
+// seen from `pt`, and its gradient with respect to the source.
+__device__ inline void vrankine_from_geom(const double pt[3], const PanelRec& P, double& phi, double g[3]) {
+  double rb0 = pt[0] - P.c[0], rb1 = pt[1] - P.c[1], rb2 = pt[2] - P.c[2];
+  double r = sqrt(rb0 * rb0 + rb1 * rb1 + rb2 * rb2);
+  if (r > 7 * P.radius) {
+    double r3 = r * r * r;
+    phi = P.area / r;
+    g[0] = (rb0 / r3) * P.area;
+    g[1] = (rb1 / r3) * P.area;
+    g[2] = (rb2 / r3) * P.area;
+    return;
+  }
+  double d0 = pt[0] - P.qgc[0], d1 = pt[1] - P.qgc[1], d2 = pt[2] - P.qgc[2];
+  double fx = P.T[0] * d0 + P.T[1] * d1 + P.T[2] * d2;
+  double fy = P.T[3] * d0 + P.T[4] * d1 + P.T[5] * d2;
+  double fz = P.T[6] * d0 + P.T[7] * d1 + P.T[8] * d2;
+  double phb, vl[3];
+  birk_phi_and_velocity(fx, fy, fz, P.lc, phb, vl);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g[i] = kFourPi * (P.T[i] * vl[0] + P.T[3 + i] * vl[1] + P.T[6 + i] * vl[2]);
+  phi = -kFourPi * phb;
+}
+
+// ---------------------------- Delhommeau Rankine ----------------------------
+__device__ __forceinline__ double sign_ad(double x) { return x < 0.0 ? -1.0 : 1.0; }
+
+// integral(::DelhommeauRankine) (rankine.jl:33-71) and the gradient of
+// both_integral_and_integral_gradient (rankine.jl:73-131); v12: 4 raw corners.
+__device__ inline void delhommeau_rankine(const double pt[3], const PanelRec& P, const double* v12, int wrt_first,
+                                          double& integral, double g[3]) {
+  double rb[3] = {pt[0] - P.c[0], pt[1] - P.c[1], pt[2] - P.c[2]};
+  double r = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+  const double* nrm = P.n;
+  if (r > 7 * P.radius) {
+    double r3 = r * r * r;
+    integral = P.area / r;
+    for (int c = 0; c < 3; ++c) g[c] = (1 / r3 * rb[c]) * P.area;
+  } else {
+    integral = 0.0;
+    g[0] = g[1] = g[2] = 0.0;
+    double GZ = rb[0] * nrm[0] + rb[1] * nrm[1] + rb[2] * nrm[2];
+    double RR[4], DRX[4][3];
+    for (int i = 0; i < 4; ++i) {
+      double d[3] = {pt[0] - v12[3 * i], pt[1] - v12[3 * i + 1], pt[2] - v12[3 * i + 2]};
+      RR[i] = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      for (int c = 0; c < 3; ++c) DRX[i][c] = d[c] / RR[i];
+    }
+    for (int iv = 0; iv < 4; ++iv) {
+      int in = (iv + 1) & 3;
+      double ctn[3] = {v12[3 * in] - v12[3 * iv], v12[3 * in + 1] - v12[3 * iv + 1], v12[3 * in + 2] - v12[3 * iv + 2]};
+      double seg = sqrt(ctn[0] * ctn[0] + ctn[1] * ctn[1] + ctn[2] * ctn[2]);
+      if (!(seg >= 1e-3 * P.radius)) continue;
+      double u[3] = {ctn[0] / seg, ctn[1] / seg, ctn[2] / seg};
+      double GYX[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2], nrm[0] * u[1] - nrm[1] * u[0]};
+      double pv[3] = {pt[0] - v12[3 * iv], pt[1] - v12[3 * iv + 1], pt[2] - v12[3 * iv + 2]};
+      double GY = pv[0] * GYX[0] + pv[1] * GYX[1] + pv[2] * GYX[2];
+      double ANT = 2 * GY * seg;
+      double rs = RR[in] + RR[iv];
+      double DNT = rs * rs - seg * seg + 2 * abs_ad(GZ) * rs;
+      double ANL = rs + seg, DNL = rs - seg;
+      double ALDEN = log(ANL / DNL);
+      double AT = fabs(GZ) >= 1e-4 * P.radius ? atan2(ANT, DNT) : 0.0;  // _delhommeau_atan
+      integral -= 2 * abs_ad(GZ) * AT;
+      if (fabs(GY) > 1e-5) integral += GY * ALDEN;
+      double q1 = GY * (DNL - ANL), q2 = 2 * abs_ad(GZ), den2 = ANT * ANT + DNT * DNT;
+      for (int c = 0; c < 3; ++c) {
+        double ANLX = DRX[in][c] + DRX[iv][c];
+        double ANTX = 2 * seg * GYX[c];
+        double DNTX = 2 * (rs + abs_ad(GZ)) * ANLX + 2 * sign_ad(GZ) * rs * nrm[c];
+        double term = ALDEN * GYX[c] - 2 * sign_ad(GZ) * AT * nrm[c] + q1 / (ANL * DNL) * ANLX -
+                      q2 * (ANTX * DNT - DNTX * ANT) / den2;
+        g[c] = g[c] - term;
+      }
+    }
+  }
+  if (wrt_first) { g[0] = -g[0]; g[1] = -g[1]; g[2] = -g[2]; }
+}
+
+// ------------------------------------ Wu -----------------------------------
+// Polynomial fits A-D and dA-dC of Liang, Wu & Noblesse (wu.jl:131-197, 235-329).
+__device__ __forceinline__ double wu_dC(double t) {
+  double v = (3168.35 + -1590.27 * t) * t;
+  v = (-2318.58 + v) * t; v = (847.8 + v) * t; v = (-148.24 + v) * t;
+  return 14.19 + v;
+}
+__device__ __forceinline__ double wu_dB(double t) {
+  double v = (-76209.82 + 19923.28 * t) * t;
+  v = (118879.26 + v) * t; v = (-97014.11 + v) * t; v = (44270.15 + v) * t; v = (-11336.19 + v) * t;
+  v = (1565.35 + v) * t; v = (-76.765 + v) * t; v = (2.894 + v) * t;
+  return 1.11 + v;
+}
+__device__ __forceinline__ double wu_dA(double t) {
+  double v = (-46688.0 + 12622.25 * t) * t;
+  v = (68220.87 + v) * t; v = (-48811.41 + v) * t; v = (16370.75 + v) * t; v = (-1187.71 + v) * t;
+  v = (-754.85 + v) * t; v = (249.69 + v) * t; v = (-24.53 + v) * t;
+  return 2.948 + v;
+}
+__device__ __forceinline__ double wu_D(double t) {
+  double v = (128170.2 + -33744.6 * t) * t;
+  v = (-205690.43 + v) * t; v = (181856.75 + v) * t; v = (-96293.05 + v) * t; v = (31127.39 + v) * t;
+  v = (-6072.07 + v) * t; v = (667.16 + v) * t; v = (-40.97 + v) * t;
+  return 0.632 + v;
+}
+__device__ __forceinline__ double wu_C(double t) {
+  double v = (9136.4 + -3272.62 * t) * t;
+  v = (-9844.35 + v) * t; v = (5155.67 + v) * t; v = (-1397.89 + v) * t; v = (209.653 + v) * t;
+  v = (-9.747 + v) * t;
+  return 1.268 + v;
+}
+__device__ __forceinline__ double wu_B(double t) {
+  double v = (-29030.24 + 7671.22 * t) * t;
+  v = (44894.06 + v) * t; v = (-36618.81 + v) * t; v = (17137.74 + v) * t; v = (-4780.77 + v) * t;
+  v = (796.534 + v) * t; v = (-67.92 + v) * t; v = (5.737 + v) * t;
+  return 0.938 + v;
+}
+__device__ __forceinline__ double wu_A(double t) {
+  double v = (21859.0 + -4838.6 * t) * t;
+  v = (-41592.9 + v) * t; v = (42002.57 + v) * t; v = (-24314.21 + v) * t; v = (8418.94 + v) * t;
+  v = (-1763.96 + v) * t; v = (215.896 + v) * t; v = (-13.328 + v) * t;
+  return 1.21 + v;
+}
+
+// StruveH0 and StruveH1 fits (wu.jl:368-435); also returns J0/J1 so that the
+// Bessel calls are issued together.
+__device__ inline void struve_bessel(double xx, double& H0, double& H1, double& J0, double& J1) {
+  J0 = j0(xx);
+  J1 = j1(xx);
+  if (xx <= 3.0) {
+    double yy = (xx / 3.0) * (xx / 3.0);
+    double h0 = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
+    H0 = h0 * (xx / 3.0);
+    H1 = (1.909859286 + (-1.145914713 + (0.294656958 + (-0.042070508 + (0.003785727 + -0.000207183 * yy) * yy) * yy) * yy) * yy) * yy;
+  } else {
+    double yy = (3.0 / xx) * (3.0 / xx);
+    double c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
+    double c2 = kPi * xx * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
+    H0 = c1 / c2 + y0(xx);
+    double d1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
+    double d2 = kPi * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
+    H1 = d1 / d2 + y1(xx);
+  }
+}
+
+// _wu_wave_term_and_derivs (wu.jl:28-37) with GF_Func_L0/Lp/W/Ls/Lsp/Wh (wu.jl:201-366)
+__device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv) {
+  double dd = sqrt(hh * hh + vv * vv);
+  double alpha = -vv / dd;
+  double beta = hh / dd;
+  double rho = dd / (1 + dd);
+  double dd2 = dd * dd, dd3 = dd * dd * dd;
+  double omr = 1.0 - rho;
+  double omr3 = omr * omr * omr;
+  double ev = exp(vv);
+  double H0, H1, J0, J1;
+  struve_bessel(hh, H0, H1, J0, J1);
+  // GF_Func_Lp
+  double RR = (1.0 - beta) * wu_A(rho);
+  RR -= beta * wu_B(rho);
+  RR -= alpha * wu_C(rho) / (1.0 + 6.0 * alpha * rho * (1.0 - rho));
+  RR += beta * (1.0 - beta) * wu_D(rho);
+  double Lp = rho * omr3 * RR;
+  // GF_Func_L0
+  const double gama = 0.5772156649;
+  double PP = log(0.5 * (dd - vv)) + gama - 2.0 * dd2;
+  PP = ev * PP;
+  PP = PP + dd2 - vv;
+  double L0 = 2.0 * PP / (1.0 + dd3) + 2.0 * Lp;
+  const double twopi = 2 * kPi;
+  GF = make_double2(-L0 - (twopi * H0) * ev, -((twopi * -J0) * ev));
+  // GF_Func_Lsp
+  double RS = beta * wu_dA(rho);
+  RS -= (1.0 - alpha) * wu_dB(rho);
+  RS += beta * (1.0 - beta) * rho * (1.0 - 2.0 * rho) * wu_dC(rho);
+  double Lsp = rho * omr3 * RS;
+  // GF_Func_Ls
+  double PS = (beta + hh) / (dd - vv);
+  PS = PS - 2.0 * beta + 2.0 * ev * dd - hh;
+  double QS = exp(-dd) * (1.0 - beta);
+  QS = QS * (1.0 + dd / (1.0 + dd3));
+  double Ls = 2.0 * PS / (1.0 + dd3) - 4.0 * QS + 2.0 * Lsp;
+  dGh = make_double2(-Ls - (twopi * (2 / kPi - H1)) * ev, -((twopi * J1) * ev));
+  dGv = make_double2(GF.x + 2 / dd, GF.y);
+}
+
+// _wu_reduced_hh_vv (wu.jl:7-18) == with_reduced_coordinates (abstract_greens_function.jl:192-213)
+__device__ __forceinline__ void reduced_coords(const double x[3], const double xi[3], double k, double& hh,
+                                               double& vv) {
+  double d2 = (x[0] - xi[0]) * (x[0] - xi[0]) + (x[1] - xi[1]) * (x[1] - xi[1]);
+  const double purt = 1e-18;
+  double dis = (d2 == 0) ? sqrt(d2 + purt * purt) - purt : sqrt(d2);
+  hh = k * dis;
+  vv = k * (x[2] + xi[2]);
+}
+
+// _wu_sd (wu.jl:112-127): s, d for one pair before the -1/4pi scale
+__device__ inline void wu_sd(const double x[3], const double xi[3], const double nv[3], double area2, double k,
+                             double dx1, double dx2, double2& s, double2& d) {
+  double hh, vv;
+  reduced_coords(x, xi, k, hh, vv);
+  double2 GF, Gh, Gv;
+  wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+  double dr1 = 0.0, dr2 = 0.0;
+  if (fabs(hh) > 1e-6) {
+    dr1 = k * k / hh * dx1;
+    dr2 = k * k / hh * dx2;
+  }
+  double g0r = k * (dr1 * Gh.x), g0i = k * (dr1 * Gh.y);
+  double g1r = k * (dr2 * Gh.x), g1i = k * (dr2 * Gh.y);
+  double g2r = k * (k * Gv.x), g2i = k * (k * Gv.y);
+  s = make_double2((k * GF.x) * area2, (k * GF.y) * area2);
+  d = make_double2((nv[0] * g0r + nv[1] * g1r + nv[2] * g2r) * area2, (nv[0] * g0i + nv[1] * g1i + nv[2] * g2i) * area2);
+}
+
+// ------------------------- exact Guevel-Delhommeau --------------------------
+// e^z E1(z): power series of E1 (DLMF 6.6.2) where its cancellation loss
+// exp(|z| + Re z) is below e^4, else the even continued fraction of DLMF 6.9.1
+// by the modified Lentz method.  Iteration counts are bounded.
+__device__ inline double2 exp_e1(double2 z) {
+  double az = hypot(z.x, z.y);
+  if (az + z.x < 4.0) {
+    double2 term = make_double2(1.0, 0.0), sum = make_double2(0.0, 0.0);
+    double2 mz = make_double2(-z.x, -z.y);
+    for (int n = 1; n < 400; ++n) {
+      term = zscale(1.0 / (double)n, zmul(term, mz));
+      double2 add = zscale(1.0 / (double)n, term);
+      sum = zadd(sum, add);
+      if (hypot(add.x, add.y) <= 1e-17 * hypot(sum.x, sum.y)) break;
+    }
+    const double euler_gamma = 0.57721566490153286061;
+    double2 lz = zlog(z);
+    double2 e1 = make_double2(-euler_gamma - lz.x - sum.x, -lz.y - sum.y);
+    return zmul(zexp(z), e1);
+  }
+  const double tiny = 1e-300;
+  double2 b = make_double2(z.x + 1.0, z.y);
+  double2 f = b;
+  double2 C = f, D = make_double2(0.0, 0.0);
+  for (int i = 1; i < 400; ++i) {
+    double a = -(double)i * (double)i;
+    b.x += 2.0;
+    D = make_double2(b.x + a * D.x, b.y + a * D.y);
+    if (hypot(D.x, D.y) < tiny) D = make_double2(tiny, 0.0);
+    double2 q = zdiv(make_double2(a, 0.0), C);
+    C = make_double2(b.x + q.x, b.y + q.y);
+    if (hypot(C.x, C.y) < tiny) C = make_double2(tiny, 0.0);
+    D = zdiv(make_double2(1.0, 0.0), D);
+    double2 delta = zmul(C, D);
+    f = zmul(f, delta);
+    if (hypot(delta.x - 1.0, delta.y) < 1e-16) break;
+  }
+  return zdiv(make_double2(1.0, 0.0), f);
+}
+
+// integrands of _dimless_wave_term / _d_dimless_wave_term_dr
+// (exact_Guevel_Delhommeau.jl:16-23, 36-43)
+template <bool DR>
+__device__ __forceinline__ double2 egd_integrand(double theta, double r, double z) {
+  double ct = cos(theta);
+  double2 zeta = make_double2(z, r * ct);
+  double2 ez = zexp(zeta);
+  double2 g = exp_e1(zeta);
+  // j = e^zeta (E1(zeta)/pi + i) = g/pi + i e^zeta
+  double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
+  if (!DR) return make_double2(j.x, ez.x);
+  double2 inv = zdiv(make_double2(1.0, 0.0), make_double2(kPi * zeta.x, kPi * zeta.y));
+  double2 w = make_double2(j.x - inv.x, j.y - inv.y);
+  // Re(i ct w) = -ct Im(w); Re(i ct e^zeta) = -ct Im(e^zeta)
+  return make_double2(-ct * w.y, -ct * ez.y);
+}
+
+__constant__ static const double kGKx[8] = {0.991455371120812639206854697526329, 0.949107912342758524526189684047851,
+                                           0.864864423359769072789712788640926, 0.741531185599394439863864773280788,
+                                           0.586087235467691130294144845693013, 0.405845151377397166906606412076961,
+                                           0.207784955007898467600689403773245, 0.0};
+__constant__ static const double kGKwk[8] = {0.022935322010529224963732008058970, 0.063092092629978553290700663189204,
+                                            0.104790010322250183839876322541518, 0.140653259715525918745189590510238,
+                                            0.169004726639267902826583426598550, 0.190350578064785409913256402421014,
+                                            0.204432940075298892414161999234649, 0.209482141084727828012999174891714};
+__constant__ static const double kGKwg[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
+                                            0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
+
+template <bool DR>
+__device__ inline void gk15(double a, double b, double r, double z, double2& val, double& err) {
+  double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  double2 fc = egd_integrand<DR>(c, r, z);
+  double2 Ik = zscale(kGKwk[7], fc), Ig = zscale(kGKwg[3], fc);
+#pragma unroll 1
+  for (int j = 0; j < 7; ++j) {
+    double dx = h * kGKx[j];
+    double2 f1 = egd_integrand<DR>(c - dx, r, z), f2 = egd_integrand<DR>(c + dx, r, z);
+    double2 fs = zadd(f1, f2);
+    Ik = zadd(Ik, zscale(kGKwk[j], fs));
+    if (j & 1) Ig = zadd(Ig, zscale(kGKwg[j >> 1], fs));
+  }
+  val = zscale(h, Ik);
+  double2 dif = zsub(Ik, Ig);
+  err = hypot(dif.x * h, dif.y * h);
+}
+
+constexpr int kGKMaxSeg = 64;
+
+// 4 * adaptive GK(7,15) over [0, pi/2] (exact_Guevel_Delhommeau.jl:8-13, 25, 45):
+// bisection of the worst segment until total error <= max(atol, rtol |I|)
+template <bool DR>
+__device__ inline double2 egd_adaptive(double r, double z, double rtol, double atol) {
+  double sa[kGKMaxSeg], sb[kGKMaxSeg], serr[kGKMaxSeg];
+  double2 sval[kGKMaxSeg];
+  int ns = 1;
+  sa[0] = 0.0;
+  sb[0] = kPi / 2;
+  gk15<DR>(sa[0], sb[0], r, z, sval[0], serr[0]);
+  double2 tot = sval[0];
+  double E = serr[0];
+  while (E > fmax(atol, rtol * hypot(tot.x, tot.y)) && ns < kGKMaxSeg) {
+    int w = 0;
+    for (int i = 1; i < ns; ++i) if (serr[i] > serr[w]) w = i;
+    double a = sa[w], b = sb[w], m = 0.5 * (a + b);
+    double2 oldv = sval[w];
+    double olde = serr[w];
+    double2 v1, v2;
+    double e1, e2;
+    gk15<DR>(a, m, r, z, v1, e1);
+    gk15<DR>(m, b, r, z, v2, e2);
+    sa[w] = a; sb[w] = m; sval[w] = v1; serr[w] = e1;
+    sa[ns] = m; sb[ns] = b; sval[ns] = v2; serr[ns] = e2;
+    ++ns;
+    tot = zadd(tot, zsub(zadd(v1, v2), oldv));
+    E += (e1 + e2) - olde;
+  }
+  double2 s = make_double2(0.0, 0.0);
+  for (int i = 0; i < ns; ++i) s = zadd(s, sval[i]);
+  return zscale(4.0, s);
+}
+
+// both_greens_and_gradient_greens(::ExactGuevelDelhommeau) with
+// with_reduced_coordinates_derivative (exact_Guevel_Delhommeau.jl:52-59;
+// abstract_greens_function.jl:215-260); outputs already multiplied by the area
+// (integral / integral_gradient, exact_Guevel_Delhommeau.jl:61-69).
+__device__ inline void egd_integrals(const double x[3], const double xi[3], double k, double area, int wrt_first,
+                                     double rtol, double atol, double2& I, double2 g[3]) {
+  double r, z;
+  reduced_coords(x, xi, k, r, z);
+  double2 GF = egd_adaptive<false>(r, z, rtol, atol);
+  double2 dGdr = egd_adaptive<true>(r, z, rtol, atol);
+  double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
+  double d1 = 0.0, d2 = 0.0;
+  if (fabs(r) > 1e-6) {
+    if (wrt_first) { d1 = k * k / r * (x[0] - xi[0]); d2 = k * k / r * (x[1] - xi[1]); }
+    else { d1 = k * k / r * (xi[0] - x[0]); d2 = k * k / r * (xi[1] - x[1]); }
+  }
+  I = make_double2((k * GF.x) * area, (k * GF.y) * area);
+  g[0] = make_double2((k * (d1 * dGdr.x)) * area, (k * (d1 * dGdr.y)) * area);
+  g[1] = make_double2((k * (d2 * dGdr.x)) * area, (k * (d2 * dGdr.y)) * area);
+  g[2] = make_double2((k * (k * dGdz.x)) * area, (k * (k * dGdz.y)) * area);
+}
+
+}  // namespace mh

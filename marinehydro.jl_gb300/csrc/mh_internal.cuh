@@ -1,0 +1,147 @@
+// mh_internal.cuh -- shared declarations of libmarinehydro_cuda.so (not part of the C-ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/marinehydro_gb300.h"
+
+namespace mh {
+
+// ---------------------------------------------------------------------------
+// constants (values as Julia evaluates them in the reference)
+// ---------------------------------------------------------------------------
+constexpr double kPi = 3.141592653589793;
+constexpr double kFourPi = 12.566370614359172;        // 4pi
+constexpr double kMinusInv4Pi = -0.07957747154594767;  // -1/4pi
+
+// Per-panel record staged in shared memory by the assembly kernels (32 doubles,
+// 256 B, 16-byte aligned so it moves with double2 loads).
+struct __align__(16) PanelRec {
+  double T[9];      // Birk local frame, column-major (s, t, n)      rankine_vectorized.jl:80-89
+  double qgc[3];    // Birk area centroid                             :118-122
+  double lc[8];     // local corners (x, y) relative to qgc           :125-127
+  double c[3];      // mesh center (element center)                   meshes.jl:42-51
+  double n[3];      // mesh normal
+  double area;      // mesh area
+  double radius;    // mesh radius
+  double pad[4];
+};
+static_assert(sizeof(PanelRec) == 256, "PanelRec layout");
+
+// ---------------------------------------------------------------------------
+// complex helpers (interleaved re, im)
+// ---------------------------------------------------------------------------
+template <typename T> struct cplx_t;
+template <> struct cplx_t<double> { using type = double2; };
+template <> struct cplx_t<float> { using type = float2; };
+
+__host__ __device__ inline double2 cmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ inline float2 cmk(float r, float i) { return make_float2(r, i); }
+
+// ---------------------------------------------------------------------------
+// host-side kernel launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+// Counts kernel launches and, when profiling is on, brackets each launch with a
+// pair of CUDA events attributed to a named kernel group (see mh_profile_*).
+struct Profiler;
+struct LaunchCounter {
+  int64_t* count;
+  Profiler* prof;
+  void pre(cudaStream_t st) const;
+  void post(cudaStream_t st, const char* group) const;
+};
+
+#define MH_LAUNCH(lc, st, group, ...) \
+  do {                                \
+    (lc).pre(st);                     \
+    __VA_ARGS__;                      \
+    (lc).post((st), (group));         \
+  } while (0)
+
+// assembly (mh_assembly.cu)
+void launch_panel_geometry(cudaStream_t st, LaunchCounter lc, int64_t n, const double* V, const double* C,
+                           const double* N, const double* A, const double* R, PanelRec* out);
+
+struct AssemblyParams {
+  int64_t n;
+  const PanelRec* P;
+  const double* V;        // n x 12 raw vertices (Delhommeau Rankine near field)
+  uint32_t gfs;
+  int direct;
+  int include_identity;
+  int has_fixed;
+  double fixed[3];
+  double k;
+  double quad_rtol, quad_atol;
+};
+
+// Static (wavenumber-independent) part into real n x n arrays SR, DR (identity included when asked).
+void launch_assemble_static(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double* SR, double* DR);
+// S = SR + S_wave(k), D = DR + D_wave(k) (complex); SR/DR may be null (no static part).
+// batch: `nk` wavenumbers ks[b], output b at S + b*sstride (complex elements).
+void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
+                          const double* DR, int nk, const double* ks_dev, double2* S, double2* D, int64_t sstride,
+                          int wave_identity);
+// point evaluators
+void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out);
+void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* r, const double* z, double rtol,
+                         double atol, double2* out);
+
+// dense linear algebra (mh_lu.cu)
+struct BatchDesc {
+  int64_t n;        // order
+  int64_t batch;    // number of matrices
+  int64_t stride;   // complex elements between matrices
+};
+template <typename T>
+int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
+                      int32_t* ipiv, int32_t* info);
+template <typename T>
+void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
+                      const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,
+                      bool adjoint);
+// Y_b = A_b X_b (n x n times n x nrhs), batched, FP64; partial sums in `work`
+void zgemm_nn_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                      int64_t nrhs, int64_t xstride, double2* Y, double2* work);
+size_t zgemm_work_elems(int64_t n, int64_t nrhs, int64_t batch);
+void convert_z_to_c(cudaStream_t st, LaunchCounter lc, const double2* src, float2* dst, int64_t count);
+// R = B - A X (FP64), then C = (float) R ; returns nothing, norms into `norms` (per rhs: |R|_inf, |X|_inf)
+void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                      const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work, bool adjoint);
+void ir_update(cudaStream_t st, LaunchCounter lc, int64_t count, double2* X, const float2* C);
+void widen_c_to_z(cudaStream_t st, LaunchCounter lc, const float2* src, double2* dst, int64_t count);
+void inf_norms_batched(cudaStream_t st, LaunchCounter lc, int64_t n, int64_t ncols, const double2* X,
+                       double* out);
+
+// epilogue (mh_epilogue.cu)
+struct EpilogueGeom {
+  int64_t n;
+  const double* C;   // centers n x 3
+  const double* N;   // normals n x 3
+  const double* A;   // areas
+  const double* dofs;  // n_dofs x n x 3
+};
+void launch_build_rhs(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int nw, const double* omegas_dev,
+                      double gacc, int n_rad, const int32_t* rad_idx_dev, int n_beta, const double* betas_dev,
+                      double2* Bmat, int64_t bstride);
+void launch_forces(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int nw, const double* omegas_dev,
+                   double rho, double gacc, int nrhs, const double2* Phi, int64_t pstride, int n_inf,
+                   const int32_t* inf_idx_dev, int n_beta, const double* betas_dev, double2* F /*nw x n_inf x nrhs*/,
+                   double2* FK /*nw x n_inf x n_beta*/);
+
+// profiling (mh_profile.cu)
+Profiler* profiler_create();
+void profiler_destroy(Profiler* p);
+void profiler_enable(Profiler* p, bool on);
+void profiler_reset(Profiler* p);
+int profiler_read(Profiler* p, int64_t capacity, char* names, double* total_ms, int64_t* launches, int64_t* n);
+int probe_fma_peaks(cudaStream_t st, double* fp64_tflops, double* fp32_tflops);
+
+// misc
+void launch_combine_real_to_complex(cudaStream_t st, LaunchCounter lc, int64_t count, const double* re,
+                                    double2* out);
+
+}  // namespace mh

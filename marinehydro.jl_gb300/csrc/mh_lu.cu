@@ -1,0 +1,599 @@
+// mh_lu.cu -- batched dense complex LU with partial pivoting and multi-RHS solves.
+//
+// Replaces linsolve / _linearsolve / gpu_linsolve (matrix_assembly.jl:396-434),
+// whose CPU path is LinearSolve LUFactorization -> LAPACK zgetrf/zgetrs and whose
+// CUDA path is cuSOLVER through `\` on a CuArray.  Same semantics as zgetrf:
+// right-looking blocked LU, pivot = first row of maximal |re|+|im| (izamax), rows
+// swapped across the whole matrix, info = index of the first exactly-zero pivot.
+//
+// Work split per panel step k (nb = 32 columns):
+//   panel_kernel   one CTA per matrix: pivot search, row swap, scaling and the
+//                  rank-1 updates inside the panel (L2-resident, latency-bound;
+//                  many matrices run side by side in a frequency sweep)
+//   trsm_kernel    U12 = L11^-1 A12, one thread per column, L11 in shared memory
+//   gemm_kernel    A22 -= L21 U12, 64x64 tiles, 4x4 complex outputs per thread
+// Templated on the real type: double (the plain FP64 path) and float (the factor
+// used by mixed-precision iterative refinement).
+#include <cuda_runtime.h>
+
+#include "mh_internal.cuh"
+
+namespace mh {
+
+namespace {
+
+constexpr int kNB = 32;
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+// c - a*b with fused multiply-adds
+template <typename C> __device__ __forceinline__ C cfms(C c, C a, C b) {
+  C r;
+  r.x = fma(-a.x, b.x, c.x); r.x = fma(a.y, b.y, r.x);
+  r.y = fma(-a.x, b.y, c.y); r.y = fma(-a.y, b.x, r.y);
+  return r;
+}
+// c + a*b
+template <typename C> __device__ __forceinline__ C cfma(C c, C a, C b) {
+  C r;
+  r.x = fma(a.x, b.x, c.x); r.x = fma(-a.y, b.y, r.x);
+  r.y = fma(a.x, b.y, c.y); r.y = fma(a.y, b.x, r.y);
+  return r;
+}
+template <typename C> __device__ __forceinline__ C crecip(C a) {
+  // 1 / a (Smith)
+  C r;
+  if (fabs(a.x) >= fabs(a.y)) {
+    auto q = a.y / a.x; auto den = a.x + a.y * q;
+    r.x = 1 / den; r.y = -q / den;
+  } else {
+    auto q = a.x / a.y; auto den = a.y + a.x * q;
+    r.x = q / den; r.y = -1 / den;
+  }
+  return r;
+}
+template <typename C> __device__ __forceinline__ C cdiv(C a, C b) { return cmul(a, crecip(b)); }
+template <typename C> __device__ __forceinline__ C czero() { C r; r.x = 0; r.y = 0; return r; }
+
+// ------------------------------- panel ---------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) panel_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                    int32_t* __restrict__ ipiv_all, int32_t* __restrict__ info_all,
+                                                    int64_t k) {
+  using C = typename cplx_t<T>::type;
+  __shared__ T wv[16];
+  __shared__ int wi[16];
+  __shared__ int s_piv;
+  __shared__ T s_best;
+  const int64_t n = d.n;
+  C* A = Aall + blockIdx.x * d.stride;
+  int32_t* ipiv = ipiv_all + blockIdx.x * n;
+  const int64_t kend = (k + kNB < n) ? k + kNB : n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  for (int64_t j = k; j < kend; ++j) {
+    T best = -1;
+    int bi = (int)n;
+    for (int64_t i = j + tid; i < n; i += blockDim.x) {
+      C a = A[i + j * n];
+      T v = fabs(a.x) + fabs(a.y);
+      if (v > best) { best = v; bi = (int)i; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      T ob = __shfl_down_sync(0xffffffffu, best, off);
+      int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { wv[warp] = best; wi[warp] = bi; }
+    __syncthreads();
+    if (warp == 0) {
+      best = lane < nwarp ? wv[lane] : (T)-1;
+      bi = lane < nwarp ? wi[lane] : (int)n;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_down_sync(0xffffffffu, best, off);
+        int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) { s_piv = bi; s_best = best; }
+    }
+    __syncthreads();
+    const int64_t p = s_piv;
+    if (tid == 0) ipiv[j] = (int32_t)p;
+    if (!(s_best > 0)) {
+      // exactly zero column: zgetf2 records info and moves on
+      if (tid == 0 && info_all[blockIdx.x] == 0) info_all[blockIdx.x] = (int32_t)(j + 1);
+      if (tid == 0) ipiv[j] = (int32_t)j;
+      __syncthreads();
+      continue;
+    }
+    if (p != j) {
+      for (int64_t c = tid; c < n; c += blockDim.x) {
+        C t = A[j + c * n];
+        A[j + c * n] = A[p + c * n];
+        A[p + c * n] = t;
+      }
+    }
+    __syncthreads();
+    const C inv = crecip(A[j + j * n]);
+    for (int64_t i = j + 1 + tid; i < n; i += blockDim.x) A[i + j * n] = cmul(A[i + j * n], inv);
+    __syncthreads();
+    const int64_t m = n - j - 1, w = kend - j - 1;
+    if (w > 0) {
+      for (int64_t idx = tid; idx < m * w; idx += blockDim.x) {
+        int64_t r = idx % m, c = idx / m;
+        int64_t i = j + 1 + r, cc = j + 1 + c;
+        A[i + cc * n] = cfms(A[i + cc * n], A[i + j * n], A[j + cc * n]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------- U12 -----------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) trsm_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                   int64_t k) {
+  using C = typename cplx_t<T>::type;
+  __shared__ C sL[kNB][kNB + 1];
+  const int64_t n = d.n;
+  C* A = Aall + blockIdx.y * d.stride;
+  const int kb = (int)((k + kNB < n) ? kNB : n - k);
+  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+    int r = idx % kb, q = idx / kb;
+    sL[r][q] = A[(k + r) + (k + q) * n];
+  }
+  __syncthreads();
+  const int64_t c = k + kb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  C x[kNB];
+#pragma unroll
+  for (int r = 0; r < kNB; ++r) x[r] = (r < kb) ? A[(k + r) + c * n] : czero<C>();
+#pragma unroll
+  for (int r = 1; r < kNB; ++r) {
+#pragma unroll
+    for (int q = 0; q < r; ++q) x[r] = cfms(x[r], sL[r][q], x[q]);
+  }
+#pragma unroll
+  for (int r = 0; r < kNB; ++r)
+    if (r < kb) A[(k + r) + c * n] = x[r];
+}
+
+// ------------------------------ trailing update -------------------------------
+constexpr int kTM = 64, kTN = 64, kKC = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                   int64_t k) {
+  using C = typename cplx_t<T>::type;
+  __shared__ C sA[kKC][kTM + 1];
+  __shared__ C sB[kKC][kTN + 1];
+  const int64_t n = d.n;
+  C* A = Aall + blockIdx.z * d.stride;
+  const int kb = (int)((k + kNB < n) ? kNB : n - k);
+  const int64_t base = k + kb;
+  const int64_t row0 = base + blockIdx.x * (int64_t)kTM;
+  const int64_t col0 = base + blockIdx.y * (int64_t)kTN;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  C acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = czero<C>();
+  for (int k0 = 0; k0 < kb; k0 += kKC) {
+    for (int idx = threadIdx.x; idx < kKC * kTM; idx += 256) {
+      int r = idx % kTM, q = idx / kTM;
+      int64_t gi = row0 + r;
+      int kk = k0 + q;
+      sA[q][r] = (gi < n && kk < kb) ? A[gi + (k + kk) * n] : czero<C>();
+    }
+    for (int idx = threadIdx.x; idx < kKC * kTN; idx += 256) {
+      int q = idx % kKC, c = idx / kKC;
+      int64_t gc = col0 + c;
+      int kk = k0 + q;
+      sB[q][c] = (gc < n && kk < kb) ? A[(k + kk) + gc * n] : czero<C>();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kKC; ++q) {
+      C a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = sA[q][tx + 16 * r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = sB[q][ty + 16 * c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = cfma(acc[r][c], a[r], b[c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    int64_t gc = col0 + ty + 16 * c;
+    if (gc >= n) continue;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int64_t gi = row0 + tx + 16 * r;
+      if (gi < n) {
+        C v = A[gi + gc * n];
+        v.x -= acc[r][c].x;
+        v.y -= acc[r][c].y;
+        A[gi + gc * n] = v;
+      }
+    }
+  }
+}
+
+// ------------------------------ substitution ---------------------------------
+// One CTA per (group of right-hand sides, matrix); the group's vectors live in
+// shared memory.  Forward: unit lower L; backward: upper U; both in 32-column
+// blocks (warp 0 solves the diagonal block, all threads update the rest).
+// ADJ: solves A^H x = b = U^H L^H P^T x.
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(256) solve_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
+                                                    const int32_t* __restrict__ ipiv_all,
+                                                    typename cplx_t<T>::type* __restrict__ Xall, int64_t nrhs,
+                                                    int64_t xstride, int group) {
+  using C = typename cplx_t<T>::type;
+  extern __shared__ unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);
+  const int64_t n = d.n;
+  const C* LU = LUall + blockIdx.y * d.stride;
+  const int32_t* ipiv = ipiv_all + blockIdx.y * n;
+  C* X = Xall + blockIdx.y * xstride;
+  const int64_t r0 = blockIdx.x * (int64_t)group;
+  const int g = (int)((r0 + group <= nrhs) ? group : nrhs - r0);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int64_t idx = tid; idx < g * n; idx += blockDim.x) {
+    int64_t r = idx / n, i = idx % n;
+    xs[r * n + i] = X[i + (r0 + r) * n];
+  }
+  __syncthreads();
+  if (!ADJ) {
+    if (tid < g) {  // apply the row interchanges in order (zgetrs / zlaswp)
+      C* x = xs + tid * n;
+      for (int64_t j = 0; j < n; ++j) {
+        int64_t p = ipiv[j];
+        if (p != j) { C t = x[j]; x[j] = x[p]; x[p] = t; }
+      }
+    }
+    __syncthreads();
+    // L y = b
+    for (int64_t jb = 0; jb < n; jb += 32) {
+      const int64_t je = (jb + 32 < n) ? jb + 32 : n;
+      if (warp == 0) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          for (int64_t j = jb; j < je; ++j) {
+            C xj = x[j];
+            __syncwarp();
+            int64_t i = jb + lane;
+            if (i > j && i < je) x[i] = cfms(x[i], LU[i + j * n], xj);
+            __syncwarp();
+          }
+        }
+      }
+      __syncthreads();
+      for (int64_t i = je + tid; i < n; i += blockDim.x) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          C acc = czero<C>();
+          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, LU[i + j * n], x[j]);
+          x[i] = csub(x[i], acc);
+        }
+      }
+      __syncthreads();
+    }
+    // U x = y
+    const int64_t nblk = (n + 31) / 32;
+    for (int64_t bI = nblk - 1; bI >= 0; --bI) {
+      const int64_t jb = bI * 32, je = (jb + 32 < n) ? jb + 32 : n;
+      if (warp == 0) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          for (int64_t j = je - 1; j >= jb; --j) {
+            if (lane == 0) x[j] = cdiv(x[j], LU[j + j * n]);
+            __syncwarp();
+            C xj = x[j];
+            int64_t i = jb + lane;
+            if (i < j) x[i] = cfms(x[i], LU[i + j * n], xj);
+            __syncwarp();
+          }
+        }
+      }
+      __syncthreads();
+      for (int64_t i = tid; i < jb; i += blockDim.x) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          C acc = czero<C>();
+          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, LU[i + j * n], x[j]);
+          x[i] = csub(x[i], acc);
+        }
+      }
+      __syncthreads();
+    }
+  } else {
+    // U^H w = b (lower triangular, conj(U) transposed)
+    for (int64_t jb = 0; jb < n; jb += 32) {
+      const int64_t je = (jb + 32 < n) ? jb + 32 : n;
+      if (warp == 0) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          for (int64_t j = jb; j < je; ++j) {
+            if (lane == 0) x[j] = cdiv(x[j], cconj(LU[j + j * n]));
+            __syncwarp();
+            C xj = x[j];
+            int64_t i = jb + lane;
+            if (i > j && i < je) x[i] = cfms(x[i], cconj(LU[j + i * n]), xj);
+            __syncwarp();
+          }
+        }
+      }
+      __syncthreads();
+      for (int64_t i = je + tid; i < n; i += blockDim.x) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          C acc = czero<C>();
+          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, cconj(LU[j + i * n]), x[j]);
+          x[i] = csub(x[i], acc);
+        }
+      }
+      __syncthreads();
+    }
+    // L^H v = w (upper, unit diagonal)
+    const int64_t nblk = (n + 31) / 32;
+    for (int64_t bI = nblk - 1; bI >= 0; --bI) {
+      const int64_t jb = bI * 32, je = (jb + 32 < n) ? jb + 32 : n;
+      if (warp == 0) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          for (int64_t j = je - 1; j >= jb; --j) {
+            C xj = x[j];
+            __syncwarp();
+            int64_t i = jb + lane;
+            if (i < j) x[i] = cfms(x[i], cconj(LU[j + i * n]), xj);
+            __syncwarp();
+          }
+        }
+      }
+      __syncthreads();
+      for (int64_t i = tid; i < jb; i += blockDim.x) {
+        for (int r = 0; r < g; ++r) {
+          C* x = xs + r * n;
+          C acc = czero<C>();
+          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, cconj(LU[j + i * n]), x[j]);
+          x[i] = csub(x[i], acc);
+        }
+      }
+      __syncthreads();
+    }
+    if (tid < g) {  // x = P v: undo the interchanges in reverse order
+      C* x = xs + tid * n;
+      for (int64_t j = n - 1; j >= 0; --j) {
+        int64_t p = ipiv[j];
+        if (p != j) { C t = x[j]; x[j] = x[p]; x[p] = t; }
+      }
+    }
+    __syncthreads();
+  }
+  for (int64_t idx = tid; idx < g * n; idx += blockDim.x) {
+    int64_t r = idx / n, i = idx % n;
+    X[i + (r0 + r) * n] = xs[r * n + i];
+  }
+}
+
+// ------------------------------ Y = A X (FP64) --------------------------------
+constexpr int kGemvRows = 128;
+constexpr int kGemvNR = 8;
+
+// partial[js][b][r][i] = sum_{j in chunk js} A_b[i, j] X_b[j, r]  (ADJ: A^H)
+template <bool ADJ>
+__global__ void __launch_bounds__(kGemvRows) zgemm_partial_kernel(BatchDesc d, const double2* __restrict__ Aall,
+                                                                  const double2* __restrict__ Xall, int64_t nrhs,
+                                                                  int64_t xstride, int64_t jchunk, int r0,
+                                                                  double2* __restrict__ part) {
+  const int64_t n = d.n;
+  const int64_t i = blockIdx.x * (int64_t)kGemvRows + threadIdx.x;
+  const int64_t js = blockIdx.y;
+  const int64_t b = blockIdx.z;
+  const double2* A = Aall + b * d.stride;
+  const double2* X = Xall + b * xstride;
+  const int64_t ja = js * jchunk, jbnd = (ja + jchunk < n) ? ja + jchunk : n;
+  const int g = (int)((r0 + kGemvNR <= nrhs) ? kGemvNR : nrhs - r0);
+  double2 acc[kGemvNR];
+#pragma unroll
+  for (int r = 0; r < kGemvNR; ++r) acc[r] = make_double2(0.0, 0.0);
+  if (i < n) {
+    for (int64_t j = ja; j < jbnd; ++j) {
+      double2 a = ADJ ? cconj(__ldg(A + j + i * n)) : __ldg(A + i + j * n);
+#pragma unroll
+      for (int r = 0; r < kGemvNR; ++r)
+        if (r < g) acc[r] = cfma(acc[r], a, __ldg(X + j + (r0 + r) * n));
+    }
+    double2* P = part + ((js * d.batch + b) * nrhs) * n;
+#pragma unroll
+    for (int r = 0; r < kGemvNR; ++r)
+      if (r < g) P[(r0 + r) * n + i] = acc[r];
+  }
+}
+
+__global__ void zgemm_reduce_kernel(BatchDesc d, int64_t nrhs, int64_t nsplit, const double2* __restrict__ part,
+                                    double2* __restrict__ Yall, int64_t ystride, const double2* __restrict__ Ball,
+                                    int subtract_from_b) {
+  const int64_t n = d.n;
+  const int64_t per = nrhs * n;
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= per * d.batch) return;
+  const int64_t b = q / per, e = q % per;
+  double2 s = make_double2(0.0, 0.0);
+  for (int64_t js = 0; js < nsplit; ++js) {
+    double2 v = part[(js * d.batch + b) * per + e];
+    s.x += v.x;
+    s.y += v.y;
+  }
+  if (subtract_from_b) {
+    double2 bb = Ball[b * ystride + e];
+    s = make_double2(bb.x - s.x, bb.y - s.y);
+  }
+  Yall[b * ystride + e] = s;
+}
+
+int64_t gemm_split(int64_t n, int64_t batch) {
+  int64_t rows = (n + kGemvRows - 1) / kGemvRows;
+  int64_t want = (4 * 152 + rows * batch - 1) / (rows * batch);
+  int64_t maxs = (n + 63) / 64;
+  if (want < 1) want = 1;
+  if (want > maxs) want = maxs;
+  return want;
+}
+
+__global__ void z_to_c_kernel(const double2* __restrict__ s, float2* __restrict__ d, int64_t count) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < count) d[q] = make_float2((float)s[q].x, (float)s[q].y);
+}
+
+__global__ void c_to_z_kernel(const float2* __restrict__ s, double2* __restrict__ d, int64_t count) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < count) d[q] = make_double2((double)s[q].x, (double)s[q].y);
+}
+
+__global__ void ir_update_kernel(double2* __restrict__ X, const float2* __restrict__ Cc, int64_t count) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < count) { X[q].x += (double)Cc[q].x; X[q].y += (double)Cc[q].y; }
+}
+
+// out[col] = max_i |re| + |im|  over column col of an n x ncols array
+__global__ void col_inf_norm_kernel(int64_t n, const double2* __restrict__ X, double* __restrict__ out) {
+  const int64_t col = blockIdx.x;
+  double m = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 v = X[i + col * n];
+    double a = fabs(v.x) + fabs(v.y);
+    m = a > m ? a : m;
+  }
+  __shared__ double red[8];
+  for (int off = 16; off > 0; off >>= 1) { double o = __shfl_down_sync(0xffffffffu, m, off); m = o > m ? o : m; }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = red[w] > r ? red[w] : r;
+    out[col] = r;
+  }
+}
+
+
+}  // namespace
+
+template <typename T>
+int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
+                      int32_t* ipiv, int32_t* info) {
+  const int64_t n = d.n;
+  if (n <= 0 || d.batch <= 0) return 0;
+  cudaMemsetAsync(info, 0, sizeof(int32_t) * d.batch, st);
+  for (int64_t k = 0; k < n; k += kNB) {
+    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
+              panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
+    const int64_t kb = (k + kNB < n) ? kNB : n - k;
+    const int64_t rest = n - k - kb;
+    if (rest <= 0) continue;
+    dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
+    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
+    dim3 gg((unsigned)((rest + kTM - 1) / kTM), (unsigned)((rest + kTN - 1) / kTN), (unsigned)d.batch);
+    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_gemm_f64" : "lu_gemm_f32", gemm_kernel<T><<<gg, 256, 0, st>>>(d, A, k));
+  }
+  return 0;
+}
+
+template <typename T>
+void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
+                      const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,
+                      bool adjoint) {
+  using C = typename cplx_t<T>::type;
+  const int64_t n = d.n;
+  if (n <= 0 || nrhs <= 0 || d.batch <= 0) return;
+  const size_t max_smem = 200 * 1024;
+  int64_t group = (int64_t)(max_smem / (sizeof(C) * n));
+  if (group < 1) group = 1;
+  if (group > nrhs) group = nrhs;
+  const size_t smem = sizeof(C) * n * group;
+  dim3 grid((unsigned)((nrhs + group - 1) / group), (unsigned)d.batch);
+  lc.pre(st);
+  if (adjoint) {
+    cudaFuncSetAttribute(solve_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+    solve_kernel<T, true><<<grid, 256, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+  } else {
+    cudaFuncSetAttribute(solve_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+    solve_kernel<T, false><<<grid, 256, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+  }
+  lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
+}
+
+template int lu_factor_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, double2*, int32_t*, int32_t*);
+template int lu_factor_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, float2*, int32_t*, int32_t*);
+template void lu_solve_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, const double2*,
+                                       const int32_t*, double2*, int64_t, int64_t, bool);
+template void lu_solve_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, const float2*, const int32_t*,
+                                      float2*, int64_t, int64_t, bool);
+
+size_t zgemm_work_elems(int64_t n, int64_t nrhs, int64_t batch) {
+  return (size_t)gemm_split(n, batch) * (size_t)batch * (size_t)nrhs * (size_t)n;
+}
+
+static void zgemm_impl(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                       int64_t nrhs, int64_t xstride, double2* Y, double2* work, const double2* B, bool adjoint) {
+  const int64_t n = d.n;
+  if (n <= 0 || nrhs <= 0 || d.batch <= 0) return;
+  const int64_t ns = gemm_split(n, d.batch);
+  const int64_t jchunk = (n + ns - 1) / ns;
+  dim3 grid((unsigned)((n + kGemvRows - 1) / kGemvRows), (unsigned)ns, (unsigned)d.batch);
+  for (int r0 = 0; r0 < nrhs; r0 += kGemvNR) {
+    lc.pre(st);
+    if (adjoint) zgemm_partial_kernel<true><<<grid, kGemvRows, 0, st>>>(d, A, X, nrhs, xstride, jchunk, r0, work);
+    else zgemm_partial_kernel<false><<<grid, kGemvRows, 0, st>>>(d, A, X, nrhs, xstride, jchunk, r0, work);
+    lc.post(st, "zgemm_rhs");
+  }
+  const int64_t tot = nrhs * n * d.batch;
+  MH_LAUNCH(lc, st, "zgemm_rhs_reduce",
+            zgemm_reduce_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(d, nrhs, ns, work, Y, xstride, B,
+                                                                                B != nullptr));
+}
+
+void zgemm_nn_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                      int64_t nrhs, int64_t xstride, double2* Y, double2* work) {
+  zgemm_impl(st, lc, d, A, X, nrhs, xstride, Y, work, nullptr, false);
+}
+
+void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                      const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work, bool adjoint) {
+  zgemm_impl(st, lc, d, A, X, nrhs, xstride, R, work, B, adjoint);
+}
+
+void convert_z_to_c(cudaStream_t st, LaunchCounter lc, const double2* src, float2* dst, int64_t count) {
+  if (count <= 0) return;
+  MH_LAUNCH(lc, st, "convert", z_to_c_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(src, dst, count));
+}
+
+
+void ir_update(cudaStream_t st, LaunchCounter lc, int64_t count, double2* X, const float2* Cc) {
+  if (count <= 0) return;
+  MH_LAUNCH(lc, st, "ir_update", ir_update_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(X, Cc, count));
+}
+
+void widen_c_to_z(cudaStream_t st, LaunchCounter lc, const float2* src, double2* dst, int64_t count) {
+  if (count <= 0) return;
+  MH_LAUNCH(lc, st, "convert", c_to_z_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(src, dst, count));
+}
+
+void inf_norms_batched(cudaStream_t st, LaunchCounter lc, int64_t n, int64_t ncols, const double2* X, double* out) {
+  if (ncols <= 0) return;
+  MH_LAUNCH(lc, st, "ir_norms", col_inf_norm_kernel<<<(unsigned)ncols, 256, 0, st>>>(n, X, out));
+}
+
+
+}  // namespace mh

@@ -1,0 +1,152 @@
+// mh_profile.cu -- launch accounting, per-kernel-group CUDA-event timing and FMA peak probes.
+//
+// When profiling is enabled on a context, every kernel launch is bracketed by two
+// CUDA events recorded on the launching stream; mh_profile_read() resolves them
+// into total device time and launch count per kernel group.  The probes measure
+// the FP64 and FP32 fused-multiply-add throughput of the device (the roofline
+// denominators of the FP64-bound assembly / LU kernels).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mh_internal.cuh"
+
+namespace mh {
+
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  cudaEvent_t pending = nullptr;
+  struct Rec { int group; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<int64_t> count;
+
+  cudaEvent_t take() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  int group_index(const char* g) {
+    for (size_t i = 0; i < names.size(); ++i)
+      if (names[i] == g) return (int)i;
+    names.emplace_back(g);
+    ms.push_back(0.0);
+    count.push_back(0);
+    return (int)names.size() - 1;
+  }
+  // requires the stream(s) to be synchronized
+  void resolve() {
+    for (const Rec& r : recs) {
+      float t = 0.f;
+      if (r.a && r.b && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) ms[r.group] += t;
+      count[r.group] += 1;
+    }
+    recs.clear();
+    used = 0;
+  }
+  void reset() {
+    recs.clear();
+    used = 0;
+    names.clear();
+    ms.clear();
+    count.clear();
+  }
+  ~Profiler() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+
+void LaunchCounter::pre(cudaStream_t st) const {
+  if (prof && prof->on) {
+    prof->pending = prof->take();
+    if (prof->pending) cudaEventRecord(prof->pending, st);
+  }
+}
+
+void LaunchCounter::post(cudaStream_t st, const char* group) const {
+  if (count) *count += 1;
+  if (prof && prof->on) {
+    cudaEvent_t e = prof->take();
+    if (e) cudaEventRecord(e, st);
+    prof->recs.push_back(Profiler::Rec{prof->group_index(group), prof->pending, e});
+    prof->pending = nullptr;
+  }
+}
+
+Profiler* profiler_create() { return new Profiler(); }
+void profiler_destroy(Profiler* p) { delete p; }
+void profiler_enable(Profiler* p, bool on) { p->on = on; }
+void profiler_reset(Profiler* p) { p->reset(); }
+int profiler_read(Profiler* p, int64_t capacity, char* names, double* total_ms, int64_t* launches, int64_t* n) {
+  p->resolve();
+  *n = (int64_t)p->names.size();
+  for (int64_t i = 0; i < *n && i < capacity; ++i) {
+    if (names) {
+      std::memset(names + 32 * i, 0, 32);
+      std::strncpy(names + 32 * i, p->names[i].c_str(), 31);
+    }
+    if (total_ms) total_ms[i] = p->ms[i];
+    if (launches) launches[i] = p->count[i];
+  }
+  return 0;
+}
+
+namespace {
+
+template <typename T>
+__global__ void fma_probe_kernel(int iters, T a, T b, T* out) {
+  T x0 = (T)threadIdx.x * (T)1e-3, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+  T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == (T)-1.2345) out[0] = s;  // keeps the chains live
+}
+
+template <typename T>
+double run_probe(cudaStream_t st, int iters, T* scratch) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fma_probe_kernel<T><<<blocks, threads, 0, st>>>(16, (T)0.999999, (T)1e-7, scratch);  // warm-up
+  cudaEventRecord(a, st);
+  fma_probe_kernel<T><<<blocks, threads, 0, st>>>(iters, (T)0.999999, (T)1e-7, scratch);
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const double flops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+}
+
+}  // namespace
+
+int probe_fma_peaks(cudaStream_t st, double* fp64_tflops, double* fp32_tflops) {
+  double* scratch = nullptr;
+  if (cudaMallocAsync((void**)&scratch, 64, st) != cudaSuccess) return MH_ERR_NOMEM;
+  double p64 = run_probe<double>(st, 1 << 13, scratch);
+  double p32 = run_probe<float>(st, 1 << 16, (float*)scratch);
+  cudaFreeAsync(scratch, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (fp64_tflops) *fp64_tflops = p64;
+  if (fp32_tflops) *fp32_tflops = p32;
+  return e == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+}  // namespace mh
