@@ -259,41 +259,40 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
     // x0 = LU32 \ b
     convert_z_to_c(ctx->stream, ctx->lc(), B0, X32, xstride * d.batch);
     lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
-    MH_CUDA(ctx, cudaMemsetAsync(X, 0, sizeof(double2) * xstride * d.batch, ctx->stream));
-    ir_update(ctx->stream, ctx->lc(), xstride * d.batch, X, X32);
-    // refinement: r = b - A x (FP64); c = LU32 \ r; x += c
+    widen_c_to_z(ctx->stream, ctx->lc(), X32, X, xstride * d.batch);
+    // Refinement with LAPACK zcgesv's stopping rule: accept x when
+    // |b - A x|_inf <= sqrt(n) eps |A|_inf |x|_inf for every column, at most 30 sweeps.
     const int64_t ncols = nrhs * d.batch;
     double* norms;
-    MH_TRY(ws_get_t(ctx, kSlotNorm, (size_t)(2 * ncols), &norms));
+    MH_TRY(ws_get_t(ctx, kSlotNorm, (size_t)(2 * ncols + d.batch), &norms));
+    double* anrm_d = norms + 2 * ncols;
+    matrix_inf_norms(ctx->stream, ctx->lc(), d, Adev, anrm_d);
     double* hn;
-    MH_TRY(pinned_get(ctx, sizeof(double) * 2 * ncols + 64, &hn));
+    MH_TRY(pinned_get(ctx, sizeof(double) * (2 * ncols + d.batch) + 64, &hn));
+    const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
     bool converged = false;
-    double prev = 1e300;
-    for (int it = 0; it < 30; ++it) {
-      // r = b - A x (FP64); c = LU32 \ r (FP32); x += c
+    for (int it = 0; it <= 30; ++it) {
       residual_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, adjoint);
-      convert_z_to_c(ctx->stream, ctx->lc(), R, X32, xstride * d.batch);
-      lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
-      ir_update(ctx->stream, ctx->lc(), xstride * d.batch, X, X32);
-      // convergence test on the correction just applied: max_col |c|_inf / |x|_inf
-      widen_c_to_z(ctx->stream, ctx->lc(), X32, R, xstride * d.batch);
       for (int64_t b = 0; b < d.batch; ++b) {
         inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, R + b * xstride, norms + b * nrhs);
         inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, X + b * xstride, norms + ncols + b * nrhs);
       }
       MH_TRY(check_launch(ctx, "refinement"));
-      MH_CUDA(ctx, cudaMemcpyAsync(hn, norms, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, ctx->stream));
+      MH_CUDA(ctx, cudaMemcpyAsync(hn, norms, sizeof(double) * (2 * ncols + d.batch), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
       MH_TRY(sync(ctx, "refinement norms"));
-      double worst = 0.0;
-      for (int64_t c = 0; c < ncols; ++c) {
-        double xn = hn[ncols + c];
-        double rel = xn > 0 ? hn[c] / xn : hn[c];
-        if (!(rel == rel)) rel = 1e300;  // NaN
-        worst = std::max(worst, rel);
+      bool ok = true;
+      for (int64_t c = 0; c < ncols && ok; ++c) {
+        const double anrm = hn[2 * ncols + c / nrhs];
+        const double rn = hn[c], xn = hn[ncols + c];
+        if (!(rn <= cte * anrm * xn)) ok = false;  // also false for NaN
       }
-      if (worst <= 4e-16) { converged = true; break; }
-      if (it >= 3 && worst > 0.5 * prev) break;  // stalled
-      prev = worst;
+      if (ok) { converged = true; break; }
+      if (it == 30) break;
+      // c = LU32 \ r ; x += c
+      convert_z_to_c(ctx->stream, ctx->lc(), R, X32, xstride * d.batch);
+      lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
+      ir_update(ctx->stream, ctx->lc(), xstride * d.batch, X, X32);
     }
     if (!converged) {
       // fall back to the FP64 factorization

@@ -113,6 +113,7 @@ void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
                       const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work, bool adjoint);
 void ir_update(cudaStream_t st, LaunchCounter lc, int64_t count, double2* X, const float2* C);
 void widen_c_to_z(cudaStream_t st, LaunchCounter lc, const float2* src, double2* dst, int64_t count);
+void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out);
 void inf_norms_batched(cudaStream_t st, LaunchCounter lc, int64_t n, int64_t ncols, const double2* X,
                        double* out);
 

@@ -488,7 +488,25 @@ __global__ void col_inf_norm_kernel(int64_t n, const double2* __restrict__ X, do
 }
 
 
+// out[b] = max_i sum_j |re|+|im| of matrix b (|.|_inf, order independent via atomicMax on the bits
+// of a non-negative double); out must be zeroed first
+__global__ void mat_inf_norm_kernel(BatchDesc d, const double2* __restrict__ A, unsigned long long* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t b = blockIdx.y;
+  if (i >= d.n) return;
+  const double2* Ab = A + b * d.stride;
+  double s = 0.0;
+  for (int64_t j = 0; j < d.n; ++j) { double2 v = Ab[i + j * d.n]; s += fabs(v.x) + fabs(v.y); }
+  atomicMax(out + b, (unsigned long long)__double_as_longlong(s));
+}
+
 }  // namespace
+
+void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out) {
+  cudaMemsetAsync(out, 0, sizeof(double) * d.batch, st);
+  dim3 grid((unsigned)((d.n + 127) / 128), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "ir_norms", mat_inf_norm_kernel<<<grid, 128, 0, st>>>(d, A, (unsigned long long*)out));
+}
 
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,

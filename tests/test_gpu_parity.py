@@ -45,9 +45,13 @@ def test_wu_wave_terms(mh, oracle, ctx):
     vv = -np.concatenate([[0.5, 1.0, 2.0, 0.1, 5.0], rng.uniform(1e-3, 30, 300), 10 ** rng.uniform(-3, 1.3, 200)])
     got = mh._device.wu_wave_terms(ctx, hh, vv)
     ref = np.array([oracle.wu_wave_term_and_derivs(h, v) for h, v in zip(hh, vv)])
+    # The polynomial fits A-D of wu.jl:131-329 have coefficients up to 2e5 with
+    # alternating signs evaluated at rho in (0, 1): a last-bit difference (the GPU
+    # fuses multiply-adds, the reference does not) is amplified to ~1e-11 absolute.
     for c in range(3):
         err = np.abs(got[:, c] - ref[:, c]) / np.maximum(np.abs(ref[:, c]), 1.0)
-        assert err.max() < 1e-12, (c, err.max())
+        assert err.max() < 1e-10, (c, err.max())
+        assert np.median(err) < 1e-14, (c, np.median(err))
 
 
 def test_exact_wave_terms(mh, oracle, ctx):
