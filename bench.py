@@ -36,6 +36,15 @@ sys.path.insert(0, REPO)
 
 N_OMEGA = 30
 OMEGAS = np.linspace(0.2, 3.0, N_OMEGA)
+
+
+def set_omegas(count):
+    """Use the first `count` frequencies of the 30 (a smaller case for ncu captures)."""
+    global N_OMEGA, OMEGAS
+    N_OMEGA = int(count)
+    OMEGAS = np.linspace(0.2, 3.0, 30)[:N_OMEGA]
+
+
 RHO, G = 1025.0, 9.81
 DOFS = ["Surge", "Sway", "Heave", "Roll", "Pitch", "Yaw"]
 BETAS = [0.0]
@@ -272,6 +281,13 @@ def run_gpu(args):
             dist.barrier()
         return tot, wall, launches, prof
 
+    if args.profile_only:
+        # a small, self-contained case for ncu: W untimed sweeps + one sweep, nothing else
+        for _ in range(args.warmup + 1):
+            step_device(_lib.MH_PREC_MIXED if args.precision == "mixed" else _lib.MH_PREC_FP64)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile_only": True, "omegas": N_OMEGA, "launches": ctx.launch_count()}))
+        return 0
     peak64, peak32 = ctx.probe_fma_peaks()
     with ClockSampler(local) as clk:
         t_dev, wall_dev, launches, prof = timed(lambda: step_device(_lib.MH_PREC_FP64), args.steps, args.warmup,
@@ -350,8 +366,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
+    ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="for --profile-only")
     args = ap.parse_args()
-    if args.warmup < 3:
+    set_omegas(args.omegas)
+    if args.warmup < 3 and not args.profile_only:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
