@@ -128,6 +128,32 @@ int mh_solve(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const do
 int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const double* Ybar,
                         double* Lambda, int precision, int mem);
 
+/* Influence-matrix assembly that allocates no device memory.  No counterpart in
+   the reference.  For callers that cannot call cudaMalloc: code running under a
+   device-memory pool that already owns the GPU's memory (a Julia CUDA.jl session,
+   a framework with its own caching allocator) or code that must not allocate once
+   initialised.  Same result as mh_assemble_matrices for gfs made of
+   MH_GF_RANKINE, MH_GF_RANKINE_REFLECTED, MH_GF_RANKINE_REFLECTED_NEGATIVE and
+   MH_GF_WU (other kinds: MH_ERR_UNSUPPORTED).
+     - vertices, centers, normals, areas, radii, S, D: DEVICE pointers on the
+       current device, laid out as for mh_mesh_create / mh_assemble_matrices;
+       fixed_normal: NULL or 3 doubles in host memory.
+     - The per-panel scratch is a fixed file-scope device array of 8192 panel
+       records (2 MiB) that every GPU loading the library keeps until exit:
+       n_panels > 8192 is rejected with MH_ERR_ARG.  Calls share the array and it
+       keeps the last call's contents (each call rewrites its own panels first);
+       calls whose work overlaps on the GPU (other streams or host threads) race.
+     - The first call on a device looks up the array's device address (setup);
+       make that first call before any stream capture.
+     - Stream-ordered: kernels are queued on `stream` (a cudaStream_t, NULL = the
+       default stream) and the call returns without synchronizing; S and D are
+       complete when the stream reaches that point.  No cudaMalloc, cudaFree or
+       allocating library routine is called. */
+int mh_assemble_matrices_noalloc(void* stream, int64_t n_panels, const double* vertices, const double* centers,
+                                 const double* normals, const double* areas, const double* radii, double wavenumber,
+                                 uint32_t gfs, int direct, int include_identity, const double* fixed_normal,
+                                 double* S, double* D);
+
 /* ---- hydrodynamic coefficients over a frequency sweep ------------------- */
 /* Replaces hydrodynamic_coefficients(body, params, formulation)
    (problems_and_results.jl:464-495) with _hydro_one_frequency (:472-478) for a
