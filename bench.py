@@ -61,6 +61,21 @@ def dist_info():
     return ws, rank, local
 
 
+def batch_workload(mh, seed=2026, n_bodies=64, n_omega=16):
+    """64 seeded bodies (spheres r in [0.5,5] m, vertical cylinders, barges L/B in [2,6]), panel counts
+    log-uniform in [300, 4000], 16 frequencies log-uniform in [0.3, 2.5] rad/s each, heave + pitch."""
+    rng = np.random.default_rng(seed)
+    bodies, params = [], []
+    for b in range(n_bodies):
+        target = int(round(np.exp(rng.uniform(np.log(300), np.log(4000)))))
+        _, mesh = mh.random_body(rng, target)
+        bodies.append(mh.FloatingBody(mesh, ["Heave", "Pitch"], rotation_center=(0.0, 0.0, 0.0), body_name=f"b{b}"))
+        oms = np.sort(np.exp(rng.uniform(np.log(0.3), np.log(2.5), n_omega)))
+        params.append({"wave_frequencies": oms, "radiating_dofs": ["Heave", "Pitch"],
+                       "influenced_dofs": ["Heave", "Pitch"]})
+    return bodies, params
+
+
 def build_workload(mh):
     mesh = mh.config2_cylinder()
     body = mh.FloatingBody(mesh, DOFS, rotation_center=(0.0, 0.0, 0.0), body_name="cylinder")
@@ -301,6 +316,10 @@ def run_gpu(args):
     dev_mix = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(resmx, res64))
     t_e2e_mix, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_MIXED), e2e_steps, 1)
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch_variant(mh, ctx, stream, dev, torch, timed)
+
     units = N_OMEGA * args.steps * ws
     value = units / t_dev
     ms_step = 1e3 * t_dev / args.steps
@@ -347,6 +366,8 @@ def run_gpu(args):
                                   for k, v in sorted(prof_mix.items(), key=lambda kv: -kv[1][0])}}},
         "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32},
     }
+    if batch is not None:
+        line["variants"]["batched_64_bodies"] = batch
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle
@@ -359,6 +380,34 @@ def run_gpu(args):
     return 0
 
 
+def run_batch_variant(mh, ctx, stream, dev, torch, timed):
+    """The many-body batching workload through mh_batch_hydrodynamic_coefficients (one CUDA graph)."""
+    bodies, params = batch_workload(mh)
+    units = sum(len(p["wave_frequencies"]) for p in params)
+    pairs = sum(b.mesh.nfaces ** 2 * len(p["wave_frequencies"]) for b, p in zip(bodies, params))
+    out = {"workload": "64 seeded bodies (sphere/cylinder/barge), N log-uniform [300,4000] (sum N = "
+                       f"{sum(b.mesh.nfaces for b in bodies)}), 16 omega log-uniform [0.3,2.5] each, heave+pitch "
+                       "radiation, Rankine+image+GFWu direct; one CUDA graph over 4 streams",
+           "units": units, "panel_pairs": pairs, "unit": UNIT}
+    results = {}
+    for prec in ("fp64", "mixed"):
+        F = mh.DirectBEM(precision=prec)
+        # first call: graph capture + instantiation + one run (untimed warm-up, also the results)
+        results[prec] = mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO, g=G)
+        steps = 1
+        t, _, launches, _ = timed(lambda: mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO,
+                                                                             g=G), steps, 0)
+        out[prec] = {"value": units * steps / t, "ms_per_step": 1e3 * t / steps, "gpu_launches": launches}
+        ctx._L.mh_batch_release(ctx.handle)
+    dev_max = 0.0
+    for a, b in zip(results["mixed"], results["fp64"]):
+        for key in ("added_mass", "radiation_damping"):
+            dev_max = max(dev_max, float(np.abs(a[key] - b[key]).max() / np.abs(b[key]).max()))
+    out["mixed"]["max_rel_dev_vs_fp64"] = dev_max
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,6 +415,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-body batching variant")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
     ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")

@@ -175,6 +175,30 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* mesh, int64_t n_omega
                                  double* added_mass, double* radiation_damping, double* diffraction_force,
                                  double* froude_krylov_force, double* excitation_force, int mem);
 
+/* Replaces a loop of hydrodynamic_coefficients over many bodies
+   (problems_and_results.jl:464-495): body b is meshes[b] with n_omega[b]
+   frequencies (omegas holds them concatenated in body order); every body has the
+   same dof names, dofs[b] is its n_dofs x n_b x 3 field block.  Outputs are the
+   per-body arrays of mh_hydrodynamic_coefficients concatenated along the
+   frequency axis in body order (body b's block starts at the sum of the earlier
+   bodies' n_omega).  The whole schedule -- every body's static and wave assembly,
+   factorization, refinement, solves and forces -- is captured into ONE CUDA graph
+   over n_streams streams (0 = 4), bodies placed longest-first on the least-loaded
+   stream; the instantiated graph and its buffers are cached on the context and
+   reused while the bodies, frequency counts and options are unchanged (omegas,
+   betas and dof values may change between calls).  Mixed precision runs two
+   refinement sweeps inside the graph and finishes any right-hand side that has
+   not met the backward-error test on the host afterwards. */
+int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mesh* const* meshes,
+                                       const int64_t* n_omega, const double* omegas, double rho, double g,
+                                       uint32_t gfs, int direct, int64_t n_dofs, const double* const* dofs,
+                                       int64_t n_rad, const int32_t* rad_idx, int64_t n_inf, const int32_t* inf_idx,
+                                       int64_t n_beta, const double* betas, int precision, int n_streams,
+                                       double* added_mass, double* radiation_damping, double* diffraction_force,
+                                       double* froude_krylov_force, double* excitation_force, int mem);
+/* Frees the cached batch graph and its device buffers. */
+int mh_batch_release(mh_context* ctx);
+
 /* ---- wave-term evaluators (kernel-level parity entry points) ------------- */
 /* _wu_wave_term_and_derivs(hh, vv) (wu.jl:28-37) for m points: out 3 complex
    per point (GF, dGF/dhh, dGF/dvv), i.e. 6 doubles. */

@@ -7,7 +7,8 @@ name is not a Python identifier; load it with ``load_package()`` below or
 ``importlib`` under the name ``marinehydro_gb300``.
 """
 from ._lib import (Context, MarineHydroError, default_context, load as load_library)  # noqa: F401
-from .api import (airy_bc, airy_pressure, assemble_matrices, assemble_matrix_wu, calculate_radiation_forces,  # noqa
+from .api import (airy_bc, airy_pressure, assemble_matrices, assemble_matrix_wu, batch_hydrodynamic_coefficients,  # noqa
+                  calculate_radiation_forces,
                   compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
                   gpu_linsolve, hydrodynamic_coefficients, integrate_pressure, linsolve, linsolve_adjoint,
                   problems_from_data, radiation_bc, solve, solve_linear, solve_problem)

@@ -154,3 +154,40 @@ def hydro_sweep(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, direct, dofs, rad_i
         p(dofs), nr, p(ri), ni, p(ii), nb, p(be), int(precision), p(A), p(B), p(Fd), p(Fk), p(Fe), MH_MEM_HOST),
         "hydrodynamic_coefficients")
     return A, B, Fd, Fk, Fe
+
+
+def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_body, rad_idx, inf_idx, betas,
+                precision=_lib.MH_PREC_FP64, n_streams=0):
+    """mh_batch_hydrodynamic_coefficients with host buffers; returns per-body lists of the five arrays."""
+    nb_ = len(dmeshes)
+    nws = np.asarray([len(o) for o in omegas_per_body], dtype=np.int64)
+    om = np.ascontiguousarray(np.concatenate([np.asarray(o, dtype=np.float64) for o in omegas_per_body]))
+    be = np.ascontiguousarray(np.asarray(betas, dtype=np.float64).ravel())
+    ri = np.ascontiguousarray(np.asarray(rad_idx, dtype=np.int32).ravel())
+    ii = np.ascontiguousarray(np.asarray(inf_idx, dtype=np.int32).ravel())
+    dofs = [np.ascontiguousarray(np.asarray(d, dtype=np.float64)) for d in dofs_per_body]
+    nd = dofs[0].shape[0] if dofs and dofs[0].size else 0
+    mesh_arr = (ctypes.c_void_p * nb_)(*[m.handle.value for m in dmeshes])
+    dof_arr = (ctypes.c_void_p * nb_)(*[d.ctypes.data for d in dofs])
+    W, nr, ni, nbeta = int(nws.sum()), ri.size, ii.size, be.size
+    A = np.empty(ni * nr * W)
+    B = np.empty_like(A)
+    Fd = np.empty(ni * W * nbeta, dtype=np.complex128)
+    Fk = np.empty_like(Fd)
+    Fe = np.empty_like(Fd)
+    p = lambda a: a.ctypes.data if a.size else None
+    ctx.check(ctx._L.mh_batch_hydrodynamic_coefficients(
+        ctx.handle, nb_, mesh_arr, nws.ctypes.data, om.ctypes.data, float(rho), float(g), int(gfs), int(bool(direct)),
+        nd, dof_arr, nr, p(ri), ni, p(ii), nbeta, p(be), int(precision), int(n_streams), p(A), p(B), p(Fd), p(Fk),
+        p(Fe), MH_MEM_HOST), "batch_hydrodynamic_coefficients")
+    out = []
+    w0 = 0
+    for nw in nws:
+        nw = int(nw)
+        a = A[ni * nr * w0:ni * nr * (w0 + nw)].reshape((ni, nr, nw), order="F")
+        b = B[ni * nr * w0:ni * nr * (w0 + nw)].reshape((ni, nr, nw), order="F")
+        sl = slice(ni * nbeta * w0, ni * nbeta * (w0 + nw))
+        fd, fk, fe = (x[sl].reshape((ni, nw, nbeta), order="F") for x in (Fd, Fk, Fe))
+        out.append((a, b, fd, fk, fe))
+        w0 += nw
+    return out

@@ -36,7 +36,7 @@ EXPORTS = (
     "mh_mesh_panels", "mh_assemble_matrices", "mh_linsolve", "mh_solve", "mh_linsolve_adjoint",
     "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
-    "mh_assemble_matrices_noalloc",
+    "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
 )
 
 
@@ -94,6 +94,9 @@ def load(path: str | None = None):
         L.mh_profile_reset.argtypes = [vp]
         L.mh_profile_read.argtypes = [vp, i64, vp, vp, vp, ctypes.POINTER(i64)]
         L.mh_probe_fma_peaks.argtypes = [vp, ctypes.POINTER(D), ctypes.POINTER(D)]
+        L.mh_batch_hydrodynamic_coefficients.argtypes = [vp, i64, vp, vp, vp, D, D, u32, I, i64, vp, i64, vp, i64,
+                                                         vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
+        L.mh_batch_release.argtypes = [vp]
         L.mh_assemble_matrices_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, D, u32, I, I, vp, vp, vp]
         for name in EXPORTS:
             getattr(L, name)  # AttributeError if the build lacks a declared entry point

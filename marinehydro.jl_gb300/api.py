@@ -237,6 +237,42 @@ def hydrodynamic_coefficients(body: FloatingBody, parameters: dict, formulation:
     }
 
 
+def batch_hydrodynamic_coefficients(bodies, parameters_per_body, formulation: BEMFormulation | None = None,
+                                    ctx=None, rho=None, g=None, n_streams=0) -> list:
+    """hydrodynamic_coefficients for many bodies at once (one CUDA graph over several streams).
+
+    Every body must have the same dof names; `parameters_per_body[b]` gives body b's
+    wave_frequencies (radiating_dofs / influenced_dofs / wave_directions are taken
+    from the first entry).  Returns one result dict per body, as hydrodynamic_coefficients.
+    """
+    f = formulation or DirectBEM()
+    c = _ctx(ctx)
+    p0 = parameters_per_body[0]
+    names = list(bodies[0].dofs)
+    for b in bodies:
+        if list(b.dofs) != names:
+            raise ValueError("every body of a batch must have the same dof names")
+    inf = list(p0.get("influenced_dofs", names))
+    rad = list(p0.get("radiating_dofs", []))
+    betas = list(p0.get("wave_directions", []))
+    idx = {n: i for i, n in enumerate(names)}
+    rho = p0.get("rho", SETTINGS["rho"]) if rho is None else rho
+    g = p0.get("g", SETTINGS["g"]) if g is None else g
+    res = _device.batch_hydro(c, [b.mesh.device_mesh(c) for b in bodies],
+                              [np.atleast_1d(np.asarray(p["wave_frequencies"], dtype=float)) for p in
+                               parameters_per_body], rho, g, gf_flags(f.greens), is_direct(f),
+                              [b.dof_array(names) for b in bodies], [idx[d] for d in rad], [idx[d] for d in inf],
+                              betas, f.precision_code, n_streams)
+    out = []
+    for A, B, Fd, Fk, Fe in res:
+        out.append({"added_mass": A[..., None] if rad else np.zeros(0),
+                    "radiation_damping": B[..., None] if rad else np.zeros(0),
+                    "diffraction_force": Fd[..., None] if betas else np.zeros(0),
+                    "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
+                    "excitation_force": Fe[..., None] if betas else np.zeros(0)})
+    return out
+
+
 def compute_hydrodynamic_coefficients(parameters, body, formulation=None, direct=True, gf="Wu",
                                       greens_functions=None, ctx=None):
     return hydrodynamic_coefficients(body, parameters, bem_formulation(formulation, direct, gf, greens_functions),

@@ -195,6 +195,74 @@ __global__ void __launch_bounds__(kRowsPerCta) static_kernel(AssemblyParams p, d
 // Wave part for a batch of wavenumbers (blockIdx.z), added to the cached static
 // part.  WU: the fused centres loop (matrix_assembly.jl:343-369, wu.jl:104-127);
 // EGD (or Wu + EGD): broadcasting sum over the wave tuple (matrix_assembly.jl:70-88).
+//
+// The wave term depends on the pair only through hh = k |x_h - xi_h| and
+// vv = k (z + zeta), both symmetric in (i, j) in IEEE arithmetic, so each
+// unordered pair {i, j} evaluates the special functions once and writes both
+// S/D entries: for (j, i) the horizontal gradient factors are the exact negations
+// of those of (i, j) and the area / normal are swapped.  The result is the same
+// as evaluating every ordered pair.  CTAs whose tile lies strictly below the
+// diagonal exit at once; within a tile, a thread handles the pairs with i <= j.
+struct WaveTerms {
+  double2 I;       // integral before the -1/4pi scale, without the source area
+  double2 gh[2];   // horizontal gradient components for the (i, j) orientation, without area
+  double2 gz;      // vertical gradient component, without area
+};
+
+template <bool DIRECT, int WMODE>
+__device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
+                                           WaveTerms& w) {
+  w.I = make_double2(0.0, 0.0);
+  w.gh[0] = w.gh[1] = w.gz = w.I;
+  // (i, j) orientation: gradient w.r.t. the source (direct) or the field point (indirect)
+  const double dx1 = DIRECT ? cj[0] - ci[0] : ci[0] - cj[0];
+  const double dx2 = DIRECT ? cj[1] - ci[1] : ci[1] - cj[1];
+  if (WMODE & 1) {  // _wu_sd (wu.jl:112-127)
+    double hh, vv;
+    reduced_coords(ci, cj, k, hh, vv);
+    double2 GF, Gh, Gv;
+    wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+    double dr1 = 0.0, dr2 = 0.0;
+    if (fabs(hh) > 1e-6) {
+      dr1 = k * k / hh * dx1;
+      dr2 = k * k / hh * dx2;
+    }
+    w.I = make_double2(k * GF.x, k * GF.y);
+    w.gh[0] = make_double2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
+    w.gh[1] = make_double2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));
+    w.gz = make_double2(k * (k * Gv.x), k * (k * Gv.y));
+  }
+  if (WMODE & 2) {  // both_greens_and_gradient_greens(::ExactGuevelDelhommeau)
+    double r, z;
+    reduced_coords(ci, cj, k, r, z);
+    double2 GF = egd_adaptive<false>(r, z, p.quad_rtol, p.quad_atol);
+    double2 dGdr = egd_adaptive<true>(r, z, p.quad_rtol, p.quad_atol);
+    double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
+    double d1 = 0.0, d2 = 0.0;
+    if (fabs(r) > 1e-6) {
+      d1 = k * k / r * dx1;
+      d2 = k * k / r * dx2;
+    }
+    w.I = zadd(w.I, make_double2(k * GF.x, k * GF.y));
+    w.gh[0] = zadd(w.gh[0], make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y)));
+    w.gh[1] = zadd(w.gh[1], make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y)));
+    w.gz = zadd(w.gz, make_double2(k * (k * dGdz.x), k * (k * dGdz.y)));
+  }
+}
+
+// S and D entries (before adding the static part) from the wave terms; `sgn` = -1
+// gives the mirrored (j, i) orientation, `area` and `nv` are that entry's.
+__device__ __forceinline__ void wave_entry(const WaveTerms& w, double sgn, double area, const double nv[3],
+                                           double2& sv, double2& dv) {
+  const double2 g0 = make_double2(sgn * w.gh[0].x, sgn * w.gh[0].y);
+  const double2 g1 = make_double2(sgn * w.gh[1].x, sgn * w.gh[1].y);
+  const double2 s = make_double2(w.I.x * area, w.I.y * area);
+  const double2 d = make_double2((nv[0] * g0.x + nv[1] * g1.x + nv[2] * w.gz.x) * area,
+                                 (nv[0] * g0.y + nv[1] * g1.y + nv[2] * w.gz.y) * area);
+  sv = make_double2(kMinusInv4Pi * s.x, kMinusInv4Pi * s.y);
+  dv = make_double2(kMinusInv4Pi * d.x, kMinusInv4Pi * d.y);
+}
+
 template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both
 __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, const double* __restrict__ SR,
                                                            const double* __restrict__ DR,
@@ -203,8 +271,10 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
                                                            int wave_identity) {
   __shared__ PanelRec sp[kColsPerCta];
   const int64_t n = p.n;
-  const int64_t i = blockIdx.x * (int64_t)kRowsPerCta + threadIdx.x;
+  const int64_t i0 = blockIdx.x * (int64_t)kRowsPerCta;
   const int64_t j0 = blockIdx.y * (int64_t)kColsPerCta;
+  if (i0 > j0 + kColsPerCta - 1) return;  // tile strictly below the diagonal
+  const int64_t i = i0 + threadIdx.x;
   const double k = ks[blockIdx.z];
   double2* Sb = S + blockIdx.z * sstride;
   double2* Db = D + blockIdx.z * sstride;
@@ -213,48 +283,19 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
   if (i >= n) return;
   double ci[3], ni[3];
   for (int c = 0; c < 3; ++c) { ci[c] = __ldg(&p.P[i].c[c]); ni[c] = __ldg(&p.P[i].n[c]); }
+  const double ai = __ldg(&p.P[i].area);
   const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
   for (int jj = 0; jj < jmax; ++jj) {
     const int64_t j = j0 + jj;
+    if (i > j) continue;
     const PanelRec& Pj = sp[jj];
+    WaveTerms w;
+    wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
+    // (i, j): source j
     double nv[3];
     pick_normal<DIRECT>(p, Pj, ni, nv);
-    double2 s, d;
-    if (WMODE == 1) {
-      const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
-      const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
-      wu_sd(ci, Pj.c, nv, Pj.area, k, dx1, dx2, s, d);
-    } else {
-      double2 I = make_double2(0.0, 0.0), gs[3] = {I, I, I};
-      if (WMODE & 1) {
-        double hh, vv;
-        reduced_coords(ci, Pj.c, k, hh, vv);
-        double2 GF, Gh, Gv;
-        wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
-        double d1 = 0.0, d2 = 0.0;
-        if (fabs(hh) > 1e-6) {
-          d1 = k * k / hh * (DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0]);
-          d2 = k * k / hh * (DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1]);
-        }
-        I = make_double2((k * GF.x) * Pj.area, (k * GF.y) * Pj.area);
-        gs[0] = make_double2(k * (d1 * Gh.x) * Pj.area, k * (d1 * Gh.y) * Pj.area);
-        gs[1] = make_double2(k * (d2 * Gh.x) * Pj.area, k * (d2 * Gh.y) * Pj.area);
-        gs[2] = make_double2(k * (k * Gv.x) * Pj.area, k * (k * Gv.y) * Pj.area);
-      }
-      if (WMODE & 2) {
-        double2 Ie, ge[3];
-        egd_integrals(ci, Pj.c, k, Pj.area, !DIRECT, p.quad_rtol, p.quad_atol, Ie, ge);
-        I = zadd(I, Ie);
-        gs[0] = zadd(gs[0], ge[0]);
-        gs[1] = zadd(gs[1], ge[1]);
-        gs[2] = zadd(gs[2], ge[2]);
-      }
-      s = I;
-      d = make_double2(nv[0] * gs[0].x + nv[1] * gs[1].x + nv[2] * gs[2].x,
-                       nv[0] * gs[0].y + nv[1] * gs[1].y + nv[2] * gs[2].y);
-    }
-    double2 sv = make_double2(kMinusInv4Pi * s.x, kMinusInv4Pi * s.y);
-    double2 dv = make_double2(kMinusInv4Pi * d.x, kMinusInv4Pi * d.y);
+    double2 sv, dv;
+    wave_entry(w, 1.0, Pj.area, nv, sv, dv);
     if (wave_identity && i == j) dv.x += identity_jump(p, ni);
     const int64_t idx = i + j * n;
     if (SR) {
@@ -263,6 +304,21 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
     }
     Sb[idx] = sv;
     Db[idx] = dv;
+    if (i == j) continue;
+    // (j, i): source i, field j -- normal of the source (direct) / field (indirect) swaps
+    double nm[3];
+    if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
+    else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
+    else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
+    double2 sm, dm;
+    wave_entry(w, -1.0, ai, nm, sm, dm);
+    const int64_t mdx = j + i * n;
+    if (SR) {
+      sm.x = SR[mdx] + sm.x;
+      dm.x = DR[mdx] + dm.x;
+    }
+    Sb[mdx] = sm;
+    Db[mdx] = dm;
   }
 }
 

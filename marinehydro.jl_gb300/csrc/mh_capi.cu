@@ -27,6 +27,38 @@ struct DevBuf {
 
 }  // namespace
 
+struct BodyPlan {
+  mh_mesh* m = nullptr;
+  int64_t n = 0, nw = 0, w_off = 0, out_off = 0;
+  int stream = 0;
+  double cost = 0.0;
+  double *SR = nullptr, *DR = nullptr, *params = nullptr, *dofs = nullptr, *norms = nullptr;
+  double2 *S = nullptr, *D = nullptr, *B = nullptr, *X = nullptr, *B0 = nullptr, *R = nullptr, *work = nullptr;
+  double2 *F = nullptr, *FK = nullptr;
+  float2 *LU32 = nullptr, *X32 = nullptr;
+  int32_t *ipiv = nullptr, *info = nullptr;
+  double2 *hF = nullptr, *hFK = nullptr;
+  int32_t* hinfo = nullptr;
+  double *hnorms = nullptr, *hparams = nullptr, *hdofs = nullptr;
+  size_t nparams = 0;
+};
+
+struct BatchCache {
+  std::vector<double> key;
+  std::vector<BodyPlan> bodies;
+  void* arena = nullptr;
+  char* pinned = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_kernels = 0;
+  int device = 0;
+  ~BatchCache() {
+    cudaSetDevice(device);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (arena) cudaFree(arena);
+    if (pinned) cudaFreeHost(pinned);
+  }
+};
+
 struct mh_context {
   int device = 0;
   cudaStream_t own = nullptr;
@@ -38,6 +70,8 @@ struct mh_context {
   double* pinned = nullptr;  // small pinned staging buffer for scalars / norms
   size_t pinned_bytes = 0;
   Profiler* prof = nullptr;
+  std::vector<cudaStream_t> side;  // extra streams of the many-body batch schedule
+  BatchCache* batch = nullptr;
   LaunchCounter lc() { return LaunchCounter{&launches, prof}; }
 };
 
@@ -63,7 +97,8 @@ namespace {
 
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
-  kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotCount
+  kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
+  kSlotGrad, kSlotLam, kSlotT, kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...) {
@@ -172,6 +207,10 @@ int put_out(mh_context* ctx, void* dst, const void* src_host, size_t bytes, int 
   MH_CUDA(ctx, cudaMemcpyAsync(dst, src_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
   return sync(ctx, "result upload");
 }
+
+// The substitution kernel keeps one right-hand side (n complex doubles) plus a
+// 32 x 33 block in shared memory (<= 227 KB per CTA).
+constexpr int64_t kMaxOrder = 12000;
 
 constexpr uint32_t kStaticKinds = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE |
                                   MH_GF_DELHOMMEAU_RANKINE | MH_GF_DELHOMMEAU_RANKINE_REFLECTED;
@@ -311,6 +350,199 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
   return MH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Many-body batch: every body's sweep is enqueued without host synchronisation on
+// one of several streams (longest-processing-time order), the whole schedule is
+// captured into one CUDA graph, and the instantiated graph is cached for repeated
+// calls with the same bodies and options.
+// ---------------------------------------------------------------------------
+struct BatchOpts {
+  uint32_t gfs;
+  int direct, precision, ir_sweeps;
+  double rho, g;
+  int64_t n_dofs, n_rad, n_inf, n_beta, nrhs;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Lay out (or size, when base == nullptr) the device buffers of one body.
+size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
+  const size_t n = (size_t)b.n, nw = (size_t)b.nw, nn = n * n, nx = n * (size_t)o.nrhs;
+  const bool mixed = o.precision == MH_PREC_MIXED;
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += align256(std::max<size_t>(bytes, 8));
+    return p;
+  };
+  b.SR = (double*)take(nn * 8);
+  b.DR = (double*)take(nn * 8);
+  b.S = (double2*)take(nw * nn * 16);
+  b.D = (double2*)take(nw * nn * 16);
+  b.B = (double2*)take(nw * nx * 16);
+  b.X = (double2*)take(nw * nx * 16);
+  b.B0 = mixed ? (double2*)take(nw * nx * 16) : nullptr;
+  b.R = mixed ? (double2*)take(nw * nx * 16) : nullptr;
+  b.work = (double2*)take(zgemm_work_elems(b.n, o.nrhs, b.nw) * 16);
+  b.LU32 = mixed ? (float2*)take(nw * nn * 8) : nullptr;
+  b.X32 = mixed ? (float2*)take(nw * nx * 8) : nullptr;
+  b.ipiv = (int32_t*)take(nw * n * 4);
+  b.info = (int32_t*)take(nw * 4);
+  b.norms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
+  b.F = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
+  b.FK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
+  b.nparams = 2 * nw + (size_t)o.n_beta + (size_t)(o.n_rad + o.n_inf + 1) / 2 + 2;
+  b.params = (double*)take(b.nparams * 8);
+  b.dofs = (double*)take((size_t)o.n_dofs * n * 3 * 8);
+  return off;
+}
+
+size_t pinned_body(BodyPlan& b, const BatchOpts& o, char* base) {
+  const size_t nw = (size_t)b.nw;
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += align256(std::max<size_t>(bytes, 8));
+    return p;
+  };
+  b.hF = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
+  b.hFK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
+  b.hinfo = (int32_t*)take(nw * 4);
+  b.hnorms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
+  b.hparams = (double*)take(b.nparams * 8);
+  b.hdofs = (double*)take((size_t)o.n_dofs * (size_t)b.n * 3 * 8);
+  return off;
+}
+
+// One body's whole sweep, enqueued on `st` with no host synchronisation.
+void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& b, const BatchOpts& o) {
+  const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs;
+  const double* om_d = b.params;
+  const double* ks_d = b.params + nw;
+  const double* beta_d = b.params + 2 * nw;
+  const int32_t* rad_d = (const int32_t*)(b.params + 2 * nw + o.n_beta);
+  const int32_t* inf_d = rad_d + o.n_rad;
+  const uint32_t st_kinds = o.gfs & kStaticKinds;
+  AssemblyParams p = make_params(ctx, b.m, o.gfs, o.direct, 1, nullptr);
+  if (st_kinds) {
+    AssemblyParams ps = make_params(ctx, b.m, st_kinds, o.direct, 1, nullptr);
+    launch_assemble_static(st, lc, ps, b.SR, b.DR);
+  }
+  launch_assemble_wave(st, lc, p, st_kinds ? b.SR : nullptr, st_kinds ? b.DR : nullptr, (int)nw, ks_d, b.S, b.D,
+                       nn, st_kinds ? 0 : 1);
+  EpilogueGeom eg{n, b.m->C, b.m->N, b.m->A, b.dofs};
+  launch_build_rhs(st, lc, eg, (int)nw, om_d, o.g, (int)o.n_rad, rad_d, (int)o.n_beta, beta_d, b.B, bstride);
+  BatchDesc d{n, nw, nn};
+  if (o.direct) zgemm_nn_batched(st, lc, d, b.S, b.B, o.nrhs, bstride, b.X, b.work);
+  else cudaMemcpyAsync(b.X, b.B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
+  if (o.precision == MH_PREC_FP64) {
+    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info);
+    lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
+  } else {
+    BatchDesc d32{n, nw, nn};
+    cudaMemcpyAsync(b.B0, b.X, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
+    convert_z_to_c(st, lc, b.D, b.LU32, nn * nw);
+    lu_factor_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.info);
+    convert_z_to_c(st, lc, b.B0, b.X32, bstride * nw);
+    lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
+    widen_c_to_z(st, lc, b.X32, b.X, bstride * nw);
+    const int64_t ncols = o.nrhs * nw;
+    matrix_inf_norms(st, lc, d, b.D, b.norms + 2 * ncols);
+    for (int it = 0; it < o.ir_sweeps; ++it) {
+      residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
+      convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
+      lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
+      ir_update(st, lc, bstride * nw, b.X, b.X32);
+    }
+    // the residual of the returned x, judged on the host after the graph
+    residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
+    for (int64_t w = 0; w < nw; ++w) {
+      inf_norms_batched(st, lc, n, o.nrhs, b.R + w * bstride, b.norms + w * o.nrhs);
+      inf_norms_batched(st, lc, n, o.nrhs, b.X + w * bstride, b.norms + ncols + w * o.nrhs);
+    }
+    cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * (2 * ncols + nw), cudaMemcpyDeviceToHost, st);
+  }
+  double2* phi = b.X;
+  if (!o.direct) {
+    zgemm_nn_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work);
+    phi = b.B;
+  }
+  if (o.n_inf > 0)
+    launch_forces(st, lc, eg, (int)nw, om_d, o.rho, o.g, (int)o.nrhs, phi, bstride, (int)o.n_inf, inf_d,
+                  (int)o.n_beta, beta_d, b.F, b.FK);
+  cudaMemcpyAsync(b.hinfo, b.info, sizeof(int32_t) * nw, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(b.hF, b.F, sizeof(double2) * nw * std::max<int64_t>(o.n_inf, 1) * o.nrhs,
+                  cudaMemcpyDeviceToHost, st);
+  if (o.n_beta > 0)
+    cudaMemcpyAsync(b.hFK, b.FK, sizeof(double2) * nw * std::max<int64_t>(o.n_inf, 1) * o.n_beta,
+                    cudaMemcpyDeviceToHost, st);
+}
+
+// Host-side completion of one body after the graph: singular check, refinement
+// convergence (extra sweeps or the FP64 fallback on the context stream).
+int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
+  for (int64_t w = 0; w < b.nw; ++w)
+    if (b.hinfo[w] != 0)
+      return fail(ctx, MH_ERR_SINGULAR, "body with %lld panels, frequency %lld: zero pivot in column %d",
+                  (long long)b.n, (long long)w, b.hinfo[w]);
+  if (o.precision != MH_PREC_MIXED) return MH_OK;
+  const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs, ncols = o.nrhs * nw;
+  const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
+  auto converged = [&]() {
+    for (int64_t c = 0; c < ncols; ++c) {
+      const double anrm = b.hnorms[2 * ncols + c / o.nrhs];
+      if (!(b.hnorms[c] <= cte * anrm * b.hnorms[ncols + c])) return false;
+    }
+    return true;
+  };
+  if (converged()) return MH_OK;
+  cudaStream_t st = ctx->stream;
+  const LaunchCounter lc = ctx->lc();
+  BatchDesc d{n, nw, nn};
+  bool ok = false;
+  for (int it = 0; it < 30 && !ok; ++it) {
+    convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
+    lu_solve_batched<float>(st, lc, d, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
+    ir_update(st, lc, bstride * nw, b.X, b.X32);
+    residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
+    for (int64_t w = 0; w < nw; ++w) {
+      inf_norms_batched(st, lc, n, o.nrhs, b.R + w * bstride, b.norms + w * o.nrhs);
+      inf_norms_batched(st, lc, n, o.nrhs, b.X + w * bstride, b.norms + ncols + w * o.nrhs);
+    }
+    MH_CUDA(ctx, cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * (2 * ncols + nw), cudaMemcpyDeviceToHost, st));
+    MH_TRY(sync(ctx, "batch refinement"));
+    ok = converged();
+  }
+  if (!ok) {
+    MH_CUDA(ctx, cudaMemcpyAsync(b.X, b.B0, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st));
+    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info);
+    lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
+  }
+  // forces of the corrected solution
+  const double* om_d = b.params;
+  const double* beta_d = b.params + 2 * nw;
+  const int32_t* inf_d = (const int32_t*)(b.params + 2 * nw + o.n_beta) + o.n_rad;
+  EpilogueGeom eg{n, b.m->C, b.m->N, b.m->A, b.dofs};
+  double2* phi = b.X;
+  if (!o.direct) {
+    zgemm_nn_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work);
+    phi = b.B;
+  }
+  if (o.n_inf > 0)
+    launch_forces(st, lc, eg, (int)nw, om_d, o.rho, o.g, (int)o.nrhs, phi, bstride, (int)o.n_inf, inf_d,
+                  (int)o.n_beta, beta_d, b.F, b.FK);
+  MH_CUDA(ctx, cudaMemcpyAsync(b.hF, b.F, sizeof(double2) * nw * std::max<int64_t>(o.n_inf, 1) * o.nrhs,
+                               cudaMemcpyDeviceToHost, st));
+  if (o.n_beta > 0)
+    MH_CUDA(ctx, cudaMemcpyAsync(b.hFK, b.FK, sizeof(double2) * nw * std::max<int64_t>(o.n_inf, 1) * o.n_beta,
+                                 cudaMemcpyDeviceToHost, st));
+  MH_CUDA(ctx, cudaMemcpyAsync(b.hinfo, b.info, sizeof(int32_t) * nw, cudaMemcpyDeviceToHost, st));
+  MH_TRY(sync(ctx, "batch fallback"));
+  for (int64_t w = 0; w < nw; ++w)
+    if (b.hinfo[w] != 0) return fail(ctx, MH_ERR_SINGULAR, "singular matrix in the batch");
+  return MH_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -347,6 +579,8 @@ int mh_destroy(mh_context* ctx) {
     if (b.p) cudaFreeAsync(b.p, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  delete ctx->batch;
+  for (cudaStream_t st : ctx->side) cudaStreamDestroy(st);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   profiler_destroy(ctx->prof);
   delete ctx;
@@ -496,6 +730,7 @@ int mh_linsolve(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const
   if (!A || !B || !X) return fail(ctx, MH_ERR_ARG, "A, B and X must not be NULL");
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
   const size_t nn = (size_t)n * (size_t)n, nx = (size_t)n * (size_t)nrhs;
   double2 *Ad, *Xd;
@@ -516,6 +751,7 @@ int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* 
   if (!A || !Ybar || !Lambda) return fail(ctx, MH_ERR_ARG, "A, Ybar and Lambda must not be NULL");
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
   const size_t nn = (size_t)n * (size_t)n, nx = (size_t)n * (size_t)nrhs;
   double2 *Ad, *Xd;
@@ -537,6 +773,7 @@ int mh_solve(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const do
   if (!direct && !sources) return fail(ctx, MH_ERR_ARG, "the indirect method needs a `sources` buffer");
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
   const size_t nn = (size_t)n * (size_t)n, nx = (size_t)n * (size_t)nrhs;
   double2 *Ad, *Sd, *Bd, *Xd, *work;
@@ -588,6 +825,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
     if (rad_idx[q] < 0 || rad_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "radiating dof index out of range");
   for (int64_t q = 0; q < n_inf; ++q)
     if (inf_idx[q] < 0 || inf_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "influenced dof index out of range");
+  if (m->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "mesh of %lld panels exceeds the supported %lld", (long long)m->n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
   const int64_t n = m->n;
   const size_t nn = (size_t)n * (size_t)n;
@@ -790,6 +1028,328 @@ int mh_probe_fma_peaks(mh_context* ctx, double* fp64_tflops, double* fp32_tflops
   return MH_OK;
 }
 
+int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mesh* const* meshes,
+                                       const int64_t* n_omega, const double* omegas, double rho, double g,
+                                       uint32_t gfs, int direct, int64_t n_dofs, const double* const* dofs,
+                                       int64_t n_rad, const int32_t* rad_idx, int64_t n_inf, const int32_t* inf_idx,
+                                       int64_t n_beta, const double* betas, int precision, int n_streams,
+                                       double* added_mass, double* radiation_damping, double* diffraction_force,
+                                       double* froude_krylov_force, double* excitation_force, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (n_bodies <= 0 || !meshes || !n_omega || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one body");
+  if (n_rad < 0 || n_inf < 0 || n_beta < 0 || n_dofs < 0) return fail(ctx, MH_ERR_ARG, "negative counts");
+  if (n_rad + n_beta == 0) return fail(ctx, MH_ERR_ARG, "nothing to solve: no radiating dof and no wave direction");
+  if ((n_rad > 0 || n_inf > 0) && (!dofs || n_dofs <= 0)) return fail(ctx, MH_ERR_ARG, "dof fields required");
+  if (gfs == 0 || (gfs & ~kAllKinds)) return fail(ctx, MH_ERR_ARG, "bad Green-function set 0x%x", gfs);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
+  for (int64_t q = 0; q < n_rad; ++q)
+    if (rad_idx[q] < 0 || rad_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "radiating dof index out of range");
+  for (int64_t q = 0; q < n_inf; ++q)
+    if (inf_idx[q] < 0 || inf_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "influenced dof index out of range");
+  int64_t total_w = 0;
+  for (int64_t b = 0; b < n_bodies; ++b) {
+    if (!meshes[b] || meshes[b]->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh %lld does not belong to this context", (long long)b);
+    if (n_omega[b] <= 0) return fail(ctx, MH_ERR_ARG, "body %lld has no wave frequency", (long long)b);
+    if (meshes[b]->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "body %lld exceeds %lld panels", (long long)b, (long long)kMaxOrder);
+    total_w += n_omega[b];
+  }
+  for (int64_t w = 0; w < total_w; ++w)
+    if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive");
+  MH_TRY(set_device(ctx));
+  const int S = n_streams > 0 ? (int)std::min(n_streams, 16) : 4;
+  BatchOpts o{gfs, direct ? 1 : 0, precision, 2, rho, g, n_dofs, n_rad, n_inf, n_beta, n_rad + n_beta};
+
+  // cache key: everything the captured graph bakes in
+  std::vector<double> key = {(double)n_bodies, (double)gfs, (double)o.direct, (double)precision, (double)S, rho, g,
+                             (double)n_dofs, (double)n_rad, (double)n_inf, (double)n_beta, ctx->quad_rtol,
+                             ctx->quad_atol};
+  for (int64_t b = 0; b < n_bodies; ++b) {
+    key.push_back((double)(uintptr_t)meshes[b]);
+    key.push_back((double)n_omega[b]);
+  }
+  for (int64_t q = 0; q < n_rad; ++q) key.push_back(rad_idx[q]);
+  for (int64_t q = 0; q < n_inf; ++q) key.push_back(inf_idx[q]);
+  BatchCache* bc = ctx->batch;
+  if (!bc || bc->key != key) {
+    delete bc;
+    ctx->batch = nullptr;
+    bc = new BatchCache();
+    bc->device = ctx->device;
+    bc->key = key;
+    bc->bodies.resize(n_bodies);
+    int64_t w_off = 0;
+    for (int64_t b = 0; b < n_bodies; ++b) {
+      BodyPlan& p = bc->bodies[b];
+      p.m = meshes[b];
+      p.n = meshes[b]->n;
+      p.nw = n_omega[b];
+      p.w_off = w_off;
+      w_off += p.nw;
+      const double n = (double)p.n;
+      p.cost = (double)p.nw * (precision == MH_PREC_FP64 ? n * n * n : n * n * n / 20.0 + 60.0 * n * n);
+    }
+    // longest processing time first onto the least-loaded stream
+    std::vector<int64_t> order(n_bodies);
+    for (int64_t b = 0; b < n_bodies; ++b) order[b] = b;
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return bc->bodies[a].cost > bc->bodies[c].cost; });
+    std::vector<double> load(S, 0.0);
+    for (int64_t b : order) {
+      int best = 0;
+      for (int q = 1; q < S; ++q) if (load[q] < load[best]) best = q;
+      bc->bodies[b].stream = best;
+      load[best] += bc->bodies[b].cost;
+    }
+    size_t dev_bytes = 0, host_bytes = 0;
+    std::vector<size_t> doff(n_bodies), hoff(n_bodies);
+    for (int64_t b = 0; b < n_bodies; ++b) {
+      doff[b] = dev_bytes;
+      dev_bytes += layout_body(bc->bodies[b], o, nullptr);
+      hoff[b] = host_bytes;
+      host_bytes += pinned_body(bc->bodies[b], o, nullptr);
+    }
+    size_t free_b = 0, total_b = 0;
+    MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    if (dev_bytes > (size_t)(0.8 * (double)free_b)) {
+      delete bc;
+      return fail(ctx, MH_ERR_NOMEM, "batch needs %.1f GB of device memory, %.1f GB free", dev_bytes / 1e9,
+                  free_b / 1e9);
+    }
+    MH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (cudaMalloc(&bc->arena, dev_bytes) != cudaSuccess || cudaMallocHost((void**)&bc->pinned, host_bytes) != cudaSuccess) {
+      delete bc;
+      return fail(ctx, MH_ERR_NOMEM, "batch allocation of %.1f GB failed", dev_bytes / 1e9);
+    }
+    for (int64_t b = 0; b < n_bodies; ++b) {
+      layout_body(bc->bodies[b], o, (char*)bc->arena + doff[b]);
+      pinned_body(bc->bodies[b], o, bc->pinned + hoff[b]);
+    }
+    while ((int)ctx->side.size() < S - 1) {
+      cudaStream_t st;
+      MH_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      ctx->side.push_back(st);
+    }
+    // capture the schedule
+    cudaStream_t s0 = ctx->stream;
+    std::vector<cudaEvent_t> ev(S);
+    for (auto& e : ev) MH_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    LaunchCounter cap{&bc->graph_kernels, nullptr};
+    MH_CUDA(ctx, cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
+    cudaEventRecord(ev[0], s0);
+    for (int q = 1; q < S; ++q) cudaStreamWaitEvent(ctx->side[q - 1], ev[0], 0);
+    for (int64_t b : order) {
+      BodyPlan& p = bc->bodies[b];
+      enqueue_body(ctx, cap, p.stream == 0 ? s0 : ctx->side[p.stream - 1], p, o);
+    }
+    for (int q = 1; q < S; ++q) {
+      cudaEventRecord(ev[q], ctx->side[q - 1]);
+      cudaStreamWaitEvent(s0, ev[q], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s0, &graph);
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (ce != cudaSuccess || !graph) {
+      delete bc;
+      return fail(ctx, MH_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(&bc->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      delete bc;
+      return fail(ctx, MH_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce));
+    }
+    ctx->batch = bc;
+  }
+  // per-call parameters -> the bodies' device buffers (outside the graph)
+  for (int64_t b = 0; b < n_bodies; ++b) {
+    BodyPlan& p = bc->bodies[b];
+    double* hp = p.hparams;
+    std::memcpy(hp, omegas + p.w_off, sizeof(double) * p.nw);
+    for (int64_t w = 0; w < p.nw; ++w) hp[p.nw + w] = omegas[p.w_off + w] * omegas[p.w_off + w] / g;
+    if (n_beta) std::memcpy(hp + 2 * p.nw, betas, sizeof(double) * n_beta);
+    int32_t* hi = (int32_t*)(hp + 2 * p.nw + n_beta);
+    for (int64_t q = 0; q < n_rad; ++q) hi[q] = rad_idx[q];
+    for (int64_t q = 0; q < n_inf; ++q) hi[n_rad + q] = inf_idx[q];
+    MH_CUDA(ctx, cudaMemcpyAsync(p.params, hp, sizeof(double) * p.nparams, cudaMemcpyHostToDevice, ctx->stream));
+    if (n_dofs > 0) {
+      const size_t db = sizeof(double) * n_dofs * p.n * 3;
+      if (mem == MH_MEM_HOST) {
+        std::memcpy(p.hdofs, dofs[b], db);
+        MH_CUDA(ctx, cudaMemcpyAsync(p.dofs, p.hdofs, db, cudaMemcpyHostToDevice, ctx->stream));
+      } else {
+        MH_CUDA(ctx, cudaMemcpyAsync(p.dofs, dofs[b], db, cudaMemcpyDeviceToDevice, ctx->stream));
+      }
+    }
+  }
+  MH_CUDA(ctx, cudaGraphLaunch(bc->exec, ctx->stream));
+  ctx->launches += bc->graph_kernels;
+  MH_TRY(sync(ctx, "batch graph"));
+  for (auto& p : bc->bodies) MH_TRY(finish_body(ctx, p, o));
+  // pack per body (n_U = 1), bodies concatenated along the frequency axis
+  std::vector<double> hA((size_t)(n_inf * n_rad * total_w)), hB(hA.size());
+  std::vector<double2> hd((size_t)(n_inf * total_w * n_beta)), hk(hd.size()), he(hd.size());
+  for (auto& p : bc->bodies) {
+    for (int64_t w = 0; w < p.nw; ++w) {
+      const double om = omegas[p.w_off + w];
+      for (int64_t i = 0; i < n_inf; ++i) {
+        for (int64_t r = 0; r < n_rad; ++r) {
+          double2 f = p.hF[(w * n_inf + i) * o.nrhs + r];
+          hA[(size_t)(n_inf * n_rad * p.w_off) + i + n_inf * (r + n_rad * w)] = f.x / (om * om);
+          hB[(size_t)(n_inf * n_rad * p.w_off) + i + n_inf * (r + n_rad * w)] = f.y / om;
+        }
+        for (int64_t bb = 0; bb < n_beta; ++bb) {
+          double2 fd = p.hF[(w * n_inf + i) * o.nrhs + n_rad + bb];
+          double2 fk = p.hFK[(w * n_inf + i) * n_beta + bb];
+          size_t q = (size_t)(n_inf * n_beta * p.w_off) + (size_t)(i + n_inf * (w + p.nw * bb));
+          hd[q] = fd;
+          hk[q] = fk;
+          he[q] = make_double2(fd.x + fk.x, fd.y + fk.y);
+        }
+      }
+    }
+  }
+  MH_TRY(put_out(ctx, added_mass, hA.data(), hA.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, radiation_damping, hB.data(), hB.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, diffraction_force, hd.data(), hd.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, froude_krylov_force, hk.data(), hk.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, excitation_force, he.data(), he.size() * sizeof(double2), mem));
+  return sync(ctx, "batch outputs");
+}
+
+int mh_batch_release(mh_context* ctx) {
+  if (!ctx) return MH_ERR_ARG;
+  MH_TRY(set_device(ctx));
+  MH_TRY(sync(ctx, "batch release"));
+  delete ctx->batch;
+  ctx->batch = nullptr;
+  return MH_OK;
+}
+
+int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
+                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
+                      double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                      double* grad_vertices, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
+  if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
+  if (n_obj <= 0 || n_obj > 4 || !obj_idx) return fail(ctx, MH_ERR_ARG, "objective needs 1..4 dofs");
+  if (!dofs || n_dofs <= 0) return fail(ctx, MH_ERR_ARG, "dof fields required");
+  const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU;
+  if (gfs == 0 || (gfs & ~allowed))
+    return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint covers the Birk Rankine family and GFWu (got 0x%x)", gfs);
+  if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
+  for (int64_t q = 0; q < n_obj; ++q)
+    if (obj_idx[q] < 0 || obj_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "objective dof index out of range");
+  for (int64_t w = 0; w < n_omega; ++w)
+    if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive");
+  if (m->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "mesh exceeds %lld panels", (long long)kMaxOrder);
+  MH_TRY(set_device(ctx));
+  const int64_t n = m->n, nh = n_obj;
+  const size_t nn = (size_t)n * n;
+  cudaStream_t st = ctx->stream;
+  const LaunchCounter lc = ctx->lc();
+  double *SR, *DR, *RS, *RD, *grad, *small, *dofs_d;
+  double2 *S, *D, *B, *X, *lam, *t, *work, *F, *FK;
+  int32_t *ipiv, *info;
+  MH_TRY(ws_get_t(ctx, kSlotSR, nn, &SR));
+  MH_TRY(ws_get_t(ctx, kSlotDR, nn, &DR));
+  MH_TRY(ws_get_t(ctx, kSlotRS, nn, &RS));
+  MH_TRY(ws_get_t(ctx, kSlotRD, nn, &RD));
+  MH_TRY(ws_get_t(ctx, kSlotS, nn, &S));
+  MH_TRY(ws_get_t(ctx, kSlotD, nn, &D));
+  MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)(n * nh), &B));
+  MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(n * nh), &X));
+  MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(n * nh), &lam));
+  MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(n * nh), &t));
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nh, 1), &work));
+  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(nh * nh), &F));
+  MH_TRY(ws_get_t(ctx, kSlotFK, 4, &FK));
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
+  MH_TRY(ws_get_t(ctx, kSlotInfo, 1, &info));
+  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)(19 * n), &grad));
+  MH_TRY(ws_get_t(ctx, kSlotIdx, 8, &small));
+  if (mem == MH_MEM_DEVICE) {
+    dofs_d = (double*)dofs;
+  } else {
+    MH_TRY(ws_get_t(ctx, kSlotDofs, (size_t)(n_dofs * n * 3), &dofs_d));
+    MH_TRY(copy_in(ctx, dofs_d, dofs, sizeof(double) * n_dofs * n * 3, MH_MEM_HOST));
+  }
+  double* gc = grad;
+  double* gn = grad + 3 * n;
+  double* ga = grad + 6 * n;
+  double* gv = grad + 7 * n;
+  MH_CUDA(ctx, cudaMemsetAsync(grad, 0, sizeof(double) * 19 * n, st));
+  MH_CUDA(ctx, cudaMemsetAsync(RS, 0, sizeof(double) * nn, st));
+  MH_CUDA(ctx, cudaMemsetAsync(RD, 0, sizeof(double) * nn, st));
+  const uint32_t stk = gfs & kStaticKinds;
+  AssemblyParams pst = make_params(ctx, m, stk, 1, 1, nullptr);
+  if (stk) {
+    launch_assemble_static(st, lc, pst, SR, DR);
+    MH_TRY(check_launch(ctx, "static assembly"));
+  }
+  AssemblyParams p = make_params(ctx, m, gfs, 1, 1, nullptr);
+  // staging: [omega, k, obj idx]
+  double* hs;
+  MH_TRY(pinned_get(ctx, 64 + sizeof(double2) * (size_t)(nh * nh), &hs));
+  int32_t* hobj = (int32_t*)(hs + 4);
+  for (int64_t q = 0; q < nh; ++q) hobj[q] = obj_idx[q];
+  double2* hF = (double2*)(hs + 8);
+  double Jsum = 0.0;
+  BatchDesc d{n, 1, (int64_t)nn};
+  EpilogueGeom eg{n, m->C, m->N, m->A, dofs_d};
+  const int32_t* obj_d = (const int32_t*)(small + 4);
+  for (int64_t w = 0; w < n_omega; ++w) {
+    const double om = omegas[w], k = om * om / g;
+    hs[0] = om;
+    hs[1] = k;
+    MH_CUDA(ctx, cudaMemcpyAsync(small, hs, sizeof(double) * 8, cudaMemcpyHostToDevice, st));
+    launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, 1, small + 1, S, D, (int64_t)nn,
+                         stk ? 0 : 1);
+    launch_build_rhs(st, lc, eg, 1, small, g, (int)nh, obj_d, 0, nullptr, B, n * nh);
+    zgemm_nn_batched(st, lc, d, S, B, nh, n * nh, X, work);
+    lu_factor_batched<double>(st, lc, d, D, ipiv, info);
+    lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, n * nh, false);        // X = phi
+    launch_forces(st, lc, eg, 1, small, rho, g, (int)nh, X, n * nh, (int)nh, obj_d, 0, nullptr, F, FK);
+    launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, lam);
+    lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, n * nh, true);       // mu = D^-H conj(w)
+    zgemm_adj_batched(st, lc, d, S, lam, nh, n * nh, t, work);                 // S^H mu
+    launch_conj(st, lc, n * nh, t);                                            // t = S^T lam
+    launch_conj(st, lc, n * nh, lam);                                          // lam = D^-T w
+    const double2 c = make_double2(1.0 / (om * om), -1.0 / om);
+    if (gfs & MH_GF_WU) {
+      launch_wave_adjoint(st, lc, p, k, lam, B, X, (int)nh, c, gc, gn, ga, RS, RD);
+    } else {
+      // static-only objective: accumulate the weights without a wave term
+      AssemblyParams pz = p;
+      pz.gfs = 0;
+      launch_wave_adjoint(st, lc, pz, k, lam, B, X, (int)nh, c, gc, gn, ga, RS, RD);
+    }
+    launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, c, X, t, gn, ga);
+    MH_TRY(check_launch(ctx, "gradient frequency"));
+    int32_t hinfo = 0;
+    MH_CUDA(ctx, cudaMemcpyAsync(hF, F, sizeof(double2) * nh * nh, cudaMemcpyDeviceToHost, st));
+    MH_CUDA(ctx, cudaMemcpyAsync(&hinfo, info, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    MH_TRY(sync(ctx, "gradient frequency"));
+    if (hinfo) return fail(ctx, MH_ERR_SINGULAR, "singular D at omega %g", om);
+    for (int64_t h = 0; h < nh; ++h) {
+      const double2 f = hF[h * nh + h];  // influenced dof h, right-hand side h
+      Jsum += f.x / (om * om) + f.y / om;
+    }
+  }
+  if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
+  MH_TRY(check_launch(ctx, "static adjoint"));
+  if (J) *J = Jsum;
+  MH_TRY(copy_out(ctx, grad_centers, gc, sizeof(double) * 3 * n, mem));
+  MH_TRY(copy_out(ctx, grad_normals, gn, sizeof(double) * 3 * n, mem));
+  MH_TRY(copy_out(ctx, grad_areas, ga, sizeof(double) * n, mem));
+  MH_TRY(copy_out(ctx, grad_vertices, gv, sizeof(double) * 12 * n, mem));
+  return sync(ctx, "gradient");
+}
+
 }  // extern "C"
+
+
 
 

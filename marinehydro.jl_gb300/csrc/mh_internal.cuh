@@ -107,6 +107,9 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
 void zgemm_nn_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
                       int64_t nrhs, int64_t xstride, double2* Y, double2* work);
 size_t zgemm_work_elems(int64_t n, int64_t nrhs, int64_t batch);
+// Y_b = A_b^H X_b
+void zgemm_adj_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                       int64_t nrhs, int64_t xstride, double2* Y, double2* work);
 void convert_z_to_c(cudaStream_t st, LaunchCounter lc, const double2* src, float2* dst, int64_t count);
 // R = B - A X (FP64), then C = (float) R ; returns nothing, norms into `norms` (per rhs: |R|_inf, |X|_inf)
 void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
@@ -132,6 +135,19 @@ void launch_forces(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int
                    double rho, double gacc, int nrhs, const double2* Phi, int64_t pstride, int n_inf,
                    const int32_t* inf_idx_dev, int n_beta, const double* betas_dev, double2* F /*nw x n_inf x nrhs*/,
                    double2* FK /*nw x n_inf x n_beta*/);
+
+// adjoint (mh_adjoint.cu)
+void launch_static_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* RS,
+                           const double* RD, double* gc, double* gn, double* ga, double* gv);
+void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lam,
+                         const double2* b, const double2* phi, int nh, double2 c, double* gc, double* gn, double* ga,
+                         double* RS, double* RD);
+void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
+                        const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2 c,
+                        const double2* phi, const double2* t, double* gn, double* ga);
+void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
+                          const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2* wconj);
+void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x);
 
 // profiling (mh_profile.cu)
 Profiler* profiler_create();

@@ -164,60 +164,67 @@ __global__ void __launch_bounds__(128) trsm_kernel(BatchDesc d, typename cplx_t<
 }
 
 // ------------------------------ trailing update -------------------------------
-constexpr int kTM = 64, kTN = 64, kKC = 16;
+// Tile shapes per precision: FP64 is FP64-pipe bound already with 64x64 CTA tiles
+// and 4x4 complex outputs per thread; FP32 needs 8x8 outputs per thread (128x128
+// CTA tiles) so that the shared-memory loads keep up with the FP32 FMA rate.
+template <typename T> struct GemmTile;
+template <> struct GemmTile<double> { static constexpr int RM = 4, TM = 64, KC = 16; };
+template <> struct GemmTile<float> { static constexpr int RM = 8, TM = 128, KC = 32; };  // whole panel depth
 
 template <typename T>
 __global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
                                                    int64_t k) {
   using C = typename cplx_t<T>::type;
-  __shared__ C sA[kKC][kTM + 1];
-  __shared__ C sB[kKC][kTN + 1];
+  constexpr int RM = GemmTile<T>::RM, TM = GemmTile<T>::TM, KC = GemmTile<T>::KC;
+  extern __shared__ unsigned char gemm_smem[];
+  C (*sA)[TM + 1] = reinterpret_cast<C (*)[TM + 1]>(gemm_smem);
+  C (*sB)[TM + 1] = reinterpret_cast<C (*)[TM + 1]>(gemm_smem + sizeof(C) * KC * (TM + 1));
   const int64_t n = d.n;
   C* A = Aall + blockIdx.z * d.stride;
   const int kb = (int)((k + kNB < n) ? kNB : n - k);
   const int64_t base = k + kb;
-  const int64_t row0 = base + blockIdx.x * (int64_t)kTM;
-  const int64_t col0 = base + blockIdx.y * (int64_t)kTN;
+  const int64_t row0 = base + blockIdx.x * (int64_t)TM;
+  const int64_t col0 = base + blockIdx.y * (int64_t)TM;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  C acc[4][4];
+  C acc[RM][RM];
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < RM; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) acc[r][c] = czero<C>();
-  for (int k0 = 0; k0 < kb; k0 += kKC) {
-    for (int idx = threadIdx.x; idx < kKC * kTM; idx += 256) {
-      int r = idx % kTM, q = idx / kTM;
+    for (int c = 0; c < RM; ++c) acc[r][c] = czero<C>();
+  for (int k0 = 0; k0 < kb; k0 += KC) {
+    for (int idx = threadIdx.x; idx < KC * TM; idx += 256) {
+      int r = idx % TM, q = idx / TM;
       int64_t gi = row0 + r;
       int kk = k0 + q;
       sA[q][r] = (gi < n && kk < kb) ? A[gi + (k + kk) * n] : czero<C>();
     }
-    for (int idx = threadIdx.x; idx < kKC * kTN; idx += 256) {
-      int q = idx % kKC, c = idx / kKC;
+    for (int idx = threadIdx.x; idx < KC * TM; idx += 256) {
+      int q = idx % KC, c = idx / KC;
       int64_t gc = col0 + c;
       int kk = k0 + q;
       sB[q][c] = (gc < n && kk < kb) ? A[(k + kk) + gc * n] : czero<C>();
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < kKC; ++q) {
-      C a[4], b[4];
+    for (int q = 0; q < KC; ++q) {
+      C a[RM], b[RM];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = sA[q][tx + 16 * r];
+      for (int r = 0; r < RM; ++r) a[r] = sA[q][tx + 16 * r];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = sB[q][ty + 16 * c];
+      for (int c = 0; c < RM; ++c) b[c] = sB[q][ty + 16 * c];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int r = 0; r < RM; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = cfma(acc[r][c], a[r], b[c]);
+        for (int c = 0; c < RM; ++c) acc[r][c] = cfma(acc[r][c], a[r], b[c]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
+  for (int c = 0; c < RM; ++c) {
     int64_t gc = col0 + ty + 16 * c;
     if (gc >= n) continue;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < RM; ++r) {
       int64_t gi = row0 + tx + 16 * r;
       if (gi < n) {
         C v = A[gi + gc * n];
@@ -230,18 +237,101 @@ __global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<
 }
 
 // ------------------------------ substitution ---------------------------------
+// x_r[i] -= sum_{j in [jb, je)} M[i, j] x_r[j] for the g right-hand sides of the
+// group (M = the stored factor, or its conjugate transpose when CT); every matrix
+// element is loaded once and applied to up to kSG vectors held in registers.
+constexpr int kSG = 8;
+
+__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ float2 shfl_c(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// Diagonal 32x32 block solves done by one warp: the block sits in shared memory
+// (blk, 32 x 33 padded, blk[l*33+q] = M[jb+l, jb+q] as stored), lane l owns
+// entry jb+l of the solution, and solved entries travel by shuffle.
+// KIND 0: unit lower L; 1: upper U; 2: lower U^H; 3: unit upper L^H.
+template <typename C>
+__device__ __forceinline__ void load_diag_block(const C* __restrict__ LU, int64_t n, int64_t jb, int bw, C* blk) {
+  for (int idx = threadIdx.x; idx < bw * bw; idx += blockDim.x) {
+    int r = idx % bw, q = idx / bw;
+    blk[r * 33 + q] = LU[(jb + r) + (jb + q) * n];
+  }
+}
+
+template <typename C, int KIND>
+__device__ __forceinline__ void diag_block_solve(const C* blk, int64_t n, int64_t jb, int bw, C* xs, int g,
+                                                 int lane) {
+  for (int r = 0; r < g; ++r) {
+    C* x = xs + (int64_t)r * n;
+    C xl = lane < bw ? x[jb + lane] : czero<C>();
+    if (KIND == 0 || KIND == 2) {
+#pragma unroll 4
+      for (int q = 0; q < bw; ++q) {
+        C m = (KIND == 0) ? blk[lane * 33 + q] : cconj(blk[q * 33 + lane]);
+        if (KIND == 2 && lane == q) xl = cdiv(xl, m);
+        C xq = shfl_c(xl, q);
+        if (lane > q && lane < bw) xl = cfms(xl, m, xq);
+      }
+    } else {
+#pragma unroll 4
+      for (int q = bw - 1; q >= 0; --q) {
+        C m = (KIND == 1) ? blk[lane * 33 + q] : cconj(blk[q * 33 + lane]);
+        if (KIND == 1 && lane == q) xl = cdiv(xl, m);
+        C xq = shfl_c(xl, q);
+        if (lane < q) xl = cfms(xl, m, xq);
+      }
+    }
+    if (lane < bw) x[jb + lane] = xl;
+  }
+}
+
+template <typename C, bool CT>
+__device__ __forceinline__ void update_row(const C* __restrict__ LU, int64_t n, int64_t i, int64_t jb, int64_t je,
+                                           C* xs, int g) {
+  for (int r0 = 0; r0 < g; r0 += kSG) {
+    C acc[kSG];
+#pragma unroll
+    for (int r = 0; r < kSG; ++r) acc[r] = czero<C>();
+    const int gr = (g - r0 < kSG) ? g - r0 : kSG;
+    if (je - jb == 32) {
+#pragma unroll 8
+      for (int jj = 0; jj < 32; ++jj) {
+        const int64_t j = jb + jj;
+        C m = CT ? cconj(LU[j + i * n]) : LU[i + j * n];
+#pragma unroll
+        for (int r = 0; r < kSG; ++r)
+          if (r < gr) acc[r] = cfma(acc[r], m, xs[(r0 + r) * n + j]);
+      }
+    } else {
+      for (int64_t j = jb; j < je; ++j) {
+        C m = CT ? cconj(LU[j + i * n]) : LU[i + j * n];
+#pragma unroll
+        for (int r = 0; r < kSG; ++r)
+          if (r < gr) acc[r] = cfma(acc[r], m, xs[(r0 + r) * n + j]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kSG; ++r)
+      if (r < gr) xs[(r0 + r) * n + i] = csub(xs[(r0 + r) * n + i], acc[r]);
+  }
+}
+
 // One CTA per (group of right-hand sides, matrix); the group's vectors live in
 // shared memory.  Forward: unit lower L; backward: upper U; both in 32-column
 // blocks (warp 0 solves the diagonal block, all threads update the rest).
 // ADJ: solves A^H x = b = U^H L^H P^T x.
 template <typename T, bool ADJ>
-__global__ void __launch_bounds__(256) solve_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
+__global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
                                                     const int32_t* __restrict__ ipiv_all,
                                                     typename cplx_t<T>::type* __restrict__ Xall, int64_t nrhs,
                                                     int64_t xstride, int group) {
   using C = typename cplx_t<T>::type;
   extern __shared__ unsigned char smem_raw[];
-  C* xs = reinterpret_cast<C*>(smem_raw);
+  C* blk = reinterpret_cast<C*>(smem_raw);
+  C* xs = blk + 32 * 33;
   const int64_t n = d.n;
   const C* LU = LUall + blockIdx.y * d.stride;
   const int32_t* ipiv = ipiv_all + blockIdx.y * n;
@@ -266,110 +356,44 @@ __global__ void __launch_bounds__(256) solve_kernel(BatchDesc d, const typename 
     // L y = b
     for (int64_t jb = 0; jb < n; jb += 32) {
       const int64_t je = (jb + 32 < n) ? jb + 32 : n;
-      if (warp == 0) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          for (int64_t j = jb; j < je; ++j) {
-            C xj = x[j];
-            __syncwarp();
-            int64_t i = jb + lane;
-            if (i > j && i < je) x[i] = cfms(x[i], LU[i + j * n], xj);
-            __syncwarp();
-          }
-        }
-      }
+      load_diag_block(LU, n, jb, (int)(je - jb), blk);
       __syncthreads();
-      for (int64_t i = je + tid; i < n; i += blockDim.x) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          C acc = czero<C>();
-          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, LU[i + j * n], x[j]);
-          x[i] = csub(x[i], acc);
-        }
-      }
+      if (warp == 0) diag_block_solve<C, 0>(blk, n, jb, (int)(je - jb), xs, g, lane);
+      __syncthreads();
+      for (int64_t i = je + tid; i < n; i += blockDim.x) update_row<C, false>(LU, n, i, jb, je, xs, g);
       __syncthreads();
     }
     // U x = y
     const int64_t nblk = (n + 31) / 32;
     for (int64_t bI = nblk - 1; bI >= 0; --bI) {
       const int64_t jb = bI * 32, je = (jb + 32 < n) ? jb + 32 : n;
-      if (warp == 0) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          for (int64_t j = je - 1; j >= jb; --j) {
-            if (lane == 0) x[j] = cdiv(x[j], LU[j + j * n]);
-            __syncwarp();
-            C xj = x[j];
-            int64_t i = jb + lane;
-            if (i < j) x[i] = cfms(x[i], LU[i + j * n], xj);
-            __syncwarp();
-          }
-        }
-      }
+      load_diag_block(LU, n, jb, (int)(je - jb), blk);
       __syncthreads();
-      for (int64_t i = tid; i < jb; i += blockDim.x) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          C acc = czero<C>();
-          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, LU[i + j * n], x[j]);
-          x[i] = csub(x[i], acc);
-        }
-      }
+      if (warp == 0) diag_block_solve<C, 1>(blk, n, jb, (int)(je - jb), xs, g, lane);
+      __syncthreads();
+      for (int64_t i = tid; i < jb; i += blockDim.x) update_row<C, false>(LU, n, i, jb, je, xs, g);
       __syncthreads();
     }
   } else {
     // U^H w = b (lower triangular, conj(U) transposed)
     for (int64_t jb = 0; jb < n; jb += 32) {
       const int64_t je = (jb + 32 < n) ? jb + 32 : n;
-      if (warp == 0) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          for (int64_t j = jb; j < je; ++j) {
-            if (lane == 0) x[j] = cdiv(x[j], cconj(LU[j + j * n]));
-            __syncwarp();
-            C xj = x[j];
-            int64_t i = jb + lane;
-            if (i > j && i < je) x[i] = cfms(x[i], cconj(LU[j + i * n]), xj);
-            __syncwarp();
-          }
-        }
-      }
+      load_diag_block(LU, n, jb, (int)(je - jb), blk);
       __syncthreads();
-      for (int64_t i = je + tid; i < n; i += blockDim.x) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          C acc = czero<C>();
-          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, cconj(LU[j + i * n]), x[j]);
-          x[i] = csub(x[i], acc);
-        }
-      }
+      if (warp == 0) diag_block_solve<C, 2>(blk, n, jb, (int)(je - jb), xs, g, lane);
+      __syncthreads();
+      for (int64_t i = je + tid; i < n; i += blockDim.x) update_row<C, true>(LU, n, i, jb, je, xs, g);
       __syncthreads();
     }
     // L^H v = w (upper, unit diagonal)
     const int64_t nblk = (n + 31) / 32;
     for (int64_t bI = nblk - 1; bI >= 0; --bI) {
       const int64_t jb = bI * 32, je = (jb + 32 < n) ? jb + 32 : n;
-      if (warp == 0) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          for (int64_t j = je - 1; j >= jb; --j) {
-            C xj = x[j];
-            __syncwarp();
-            int64_t i = jb + lane;
-            if (i < j) x[i] = cfms(x[i], cconj(LU[j + i * n]), xj);
-            __syncwarp();
-          }
-        }
-      }
+      load_diag_block(LU, n, jb, (int)(je - jb), blk);
       __syncthreads();
-      for (int64_t i = tid; i < jb; i += blockDim.x) {
-        for (int r = 0; r < g; ++r) {
-          C* x = xs + r * n;
-          C acc = czero<C>();
-          for (int64_t j = jb; j < je; ++j) acc = cfma(acc, cconj(LU[j + i * n]), x[j]);
-          x[i] = csub(x[i], acc);
-        }
-      }
+      if (warp == 0) diag_block_solve<C, 3>(blk, n, jb, (int)(je - jb), xs, g, lane);
+      __syncthreads();
+      for (int64_t i = tid; i < jb; i += blockDim.x) update_row<C, true>(LU, n, i, jb, je, xs, g);
       __syncthreads();
     }
     if (tid < g) {  // x = P v: undo the interchanges in reverse order
@@ -514,6 +538,11 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
   const int64_t n = d.n;
   if (n <= 0 || d.batch <= 0) return 0;
   cudaMemsetAsync(info, 0, sizeof(int32_t) * d.batch, st);
+  {
+    constexpr int TM = GemmTile<T>::TM;
+    constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
+    cudaFuncSetAttribute(gemm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
+  }
   for (int64_t k = 0; k < n; k += kNB) {
     MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
               panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
@@ -522,8 +551,11 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     if (rest <= 0) continue;
     dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
     MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
-    dim3 gg((unsigned)((rest + kTM - 1) / kTM), (unsigned)((rest + kTN - 1) / kTN), (unsigned)d.batch);
-    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_gemm_f64" : "lu_gemm_f32", gemm_kernel<T><<<gg, 256, 0, st>>>(d, A, k));
+    constexpr int TM = GemmTile<T>::TM;
+    dim3 gg((unsigned)((rest + TM - 1) / TM), (unsigned)((rest + TM - 1) / TM), (unsigned)d.batch);
+    constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
+    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_gemm_f64" : "lu_gemm_f32",
+              gemm_kernel<T><<<gg, 256, gsmem, st>>>(d, A, k));
   }
   return 0;
 }
@@ -536,18 +568,28 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   const int64_t n = d.n;
   if (n <= 0 || nrhs <= 0 || d.batch <= 0) return;
   const size_t max_smem = 200 * 1024;
-  int64_t group = (int64_t)(max_smem / (sizeof(C) * n));
+  const size_t blk_bytes = sizeof(C) * 32 * 33;
+  int64_t group = (int64_t)((max_smem - blk_bytes) / (sizeof(C) * n));
+  // Enough CTAs to occupy every SM twice: each CTA streams the factor once for
+  // its group of right-hand sides, so fewer RHS per CTA trades factor re-reads
+  // (from L2 / HBM) for parallelism.
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want_ctas = 2 * (int64_t)sms;
+  const int64_t g_par = (nrhs * d.batch + want_ctas - 1) / want_ctas;
+  if (group > g_par) group = g_par;
   if (group < 1) group = 1;
   if (group > nrhs) group = nrhs;
-  const size_t smem = sizeof(C) * n * group;
+  const size_t smem = blk_bytes + sizeof(C) * n * group;
   dim3 grid((unsigned)((nrhs + group - 1) / group), (unsigned)d.batch);
   lc.pre(st);
   if (adjoint) {
     cudaFuncSetAttribute(solve_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
-    solve_kernel<T, true><<<grid, 256, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+    solve_kernel<T, true><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
   } else {
     cudaFuncSetAttribute(solve_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
-    solve_kernel<T, false><<<grid, 256, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+    solve_kernel<T, false><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
   }
   lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
 }
@@ -585,6 +627,11 @@ static void zgemm_impl(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, co
 void zgemm_nn_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
                       int64_t nrhs, int64_t xstride, double2* Y, double2* work) {
   zgemm_impl(st, lc, d, A, X, nrhs, xstride, Y, work, nullptr, false);
+}
+
+void zgemm_adj_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                       int64_t nrhs, int64_t xstride, double2* Y, double2* work) {
+  zgemm_impl(st, lc, d, A, X, nrhs, xstride, Y, work, nullptr, true);
 }
 
 void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,

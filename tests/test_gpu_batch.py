@@ -1,0 +1,50 @@
+"""Many-body batch (one CUDA graph over several streams) vs per-body sweeps.
+
+The per-body sweep (mh_hydrodynamic_coefficients) is checked against the oracle in
+test_gpu_parity.py; here the batched schedule must reproduce it for bodies of
+uneven panel counts and frequency counts, on the first call (capture) and on a
+second call with new frequencies (cached graph, new parameters).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+def _bodies(mh):
+    meshes = [mh.hemisphere_mesh(1.0, 6, 12), mh.vertical_cylinder_mesh(2.0, 3.0, 16, 4, 3),
+              mh.barge_mesh(12.0, 4.0, 2.0, 8, 3, 2)]
+    return [mh.FloatingBody(m, ["Heave", "Pitch"], rotation_center=(0.0, 0.0, 0.0), body_name=f"b{i}")
+            for i, m in enumerate(meshes)]
+
+
+def _check(res, ref):
+    for key in ("added_mass", "radiation_damping", "excitation_force", "diffraction_force", "Froude_Krylov_force"):
+        a, b = np.asarray(res[key]), np.asarray(ref[key])
+        assert a.shape == b.shape, key
+        assert np.abs(a - b).max() <= REL * max(np.abs(b).max(), 1e-30), key
+
+
+@pytest.mark.parametrize("direct", [True, False])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_per_body(mh, ctx, direct, precision):
+    bodies = _bodies(mh)
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)(precision=precision)
+    rng = np.random.default_rng(5)
+    for call in range(2):  # second call: cached graph, new frequencies
+        params = [{"wave_frequencies": np.sort(rng.uniform(0.3, 2.5, nw)), "radiating_dofs": ["Heave", "Pitch"],
+                   "influenced_dofs": ["Heave", "Pitch"], "wave_directions": [0.0, 0.7]} for nw in (3, 2, 4)]
+        out = mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=1025.0, n_streams=2)
+        for body, p, res in zip(bodies, params, out):
+            ref = mh.hydrodynamic_coefficients(body, p, F, ctx=ctx, rho=1025.0)
+            _check(res, ref)
+
+
+def test_batch_rejects_mixed_dof_names(mh, ctx):
+    b = _bodies(mh)
+    b[1] = mh.FloatingBody(b[1].mesh, ["Heave"], body_name="other")
+    with pytest.raises(ValueError):
+        mh.batch_hydrodynamic_coefficients(b, [{"wave_frequencies": [1.0], "radiating_dofs": ["Heave"]}] * 3,
+                                           ctx=ctx)
