@@ -199,6 +199,33 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
 /* Frees the cached batch graph and its device buffers. */
 int mh_batch_release(mh_context* ctx);
 
+/* ---- reverse-mode gradient (hand-written adjoint) ------------------------ */
+/* Replaces a reverse-mode gradient through assemble_matrices -> _mulvec ->
+   _linearsolve -> force integration: the rules of ad_rules.jl:300-414
+   (_mulvec: dS = ybar bc^H, dbc = S^H ybar; _linearsolve: lambda = A^-H ybar,
+   dA = -lambda y^H) and the Birk kernel rules (ad_rules.jl:79-294), applied
+   to the objective
+       J = sum_omega sum_h ( A_hh(omega) + B_hh(omega) ),  h over obj_idx
+   (added mass plus radiation damping of the objective dofs, the direct
+   formulation, zero forward speed).  Each frequency reuses its LU factors for
+   one adjoint solve; no N^2 cotangent is stored: the pair derivatives are
+   recomputed tile by tile and contracted with rank-n_obj weights, the
+   frequency-independent Rankine part once with frequency-summed weights.
+     gfs:       Birk Rankine kinds (MH_GF_RANKINE*) and/or MH_GF_WU
+     dofs:      n_dofs x n x 3 dof fields, held fixed
+     obj_idx:   1..4 indices into dofs
+   Outputs (any may be NULL):
+     J                   the objective
+     grad_centers[n][3], grad_normals[n][3], grad_areas[n]: dJ w.r.t. the
+                         panel fields passed to mh_mesh_create
+     grad_vertices[n][12]: dJ w.r.t. the 4 corners (Birk near-field terms)
+     grad_dofs[n_obj][n][3]: dJ w.r.t. the objective dof fields
+   The caller chains these through its mesh and dof construction. */
+int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
+                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
+                      double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                      double* grad_vertices, double* grad_dofs, int mem);
+
 /* ---- wave-term evaluators (kernel-level parity entry points) ------------- */
 /* _wu_wave_term_and_derivs(hh, vv) (wu.jl:28-37) for m points: out 3 complex
    per point (GF, dGF/dhh, dGF/dvv), i.e. 6 doubles. */

@@ -191,3 +191,26 @@ def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_bod
         out.append((a, b, fd, fk, fe))
         w0 += nw
     return out
+
+
+def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx):
+    """mh_hydro_gradient with host buffers.
+
+    Returns (J, gc (n,3), gn (n,3), ga (n,), gv (n,4,3), gd (n_obj,n,3)): the objective
+    J = sum_omega sum_h A_hh + B_hh and its gradient w.r.t. the panel fields, the Birk
+    corners and the objective dof fields."""
+    om = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
+    dofs = np.ascontiguousarray(np.asarray(dofs, dtype=np.float64))
+    oi = np.ascontiguousarray(np.asarray(obj_idx, dtype=np.int32).ravel())
+    n = dmesh.n
+    J = ctypes.c_double()
+    gc = np.empty((n, 3))
+    gn = np.empty((n, 3))
+    ga = np.empty(n)
+    gv = np.empty((n, 4, 3))
+    gd = np.empty((oi.size, n, 3))
+    ctx.check(ctx._L.mh_hydro_gradient(
+        ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), dofs.shape[0],
+        dofs.ctypes.data, oi.size, oi.ctypes.data, ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data,
+        gv.ctypes.data, gd.ctypes.data, MH_MEM_HOST), "hydro_gradient")
+    return J.value, gc, gn, ga, gv, gd

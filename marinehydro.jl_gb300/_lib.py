@@ -37,6 +37,7 @@ EXPORTS = (
     "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
+    "mh_hydro_gradient",
 )
 
 
@@ -97,6 +98,7 @@ def load(path: str | None = None):
         L.mh_batch_hydrodynamic_coefficients.argtypes = [vp, i64, vp, vp, vp, D, D, u32, I, i64, vp, i64, vp, i64,
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
+        L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, I]
         L.mh_assemble_matrices_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, D, u32, I, I, vp, vp, vp]
         for name in EXPORTS:
             getattr(L, name)  # AttributeError if the build lacks a declared entry point

@@ -19,7 +19,7 @@ import numpy as np
 from . import _device, _lib
 from .bodies import FloatingBody, evaluate_gradient_of_motion
 from .formulations import BEMFormulation, DirectBEM, bem_formulation, gf_flags, is_direct
-from .meshes import StaticArraysMesh
+from .meshes import StaticArraysMesh, face_fields, face_fields_jacobian
 from .problems import (DiffractionProblem, DiffractionResult, RadiationProblem, RadiationResult, SETTINGS,
                        compute_wavenumber, make_result)
 
@@ -271,6 +271,65 @@ def batch_hydrodynamic_coefficients(bodies, parameters_per_body, formulation: BE
                     "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
                     "excitation_force": Fe[..., None] if betas else np.zeros(0)})
     return out
+
+
+def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formulation: BEMFormulation | None = None,
+                   ctx=None, rho=None, g=None, return_panel_terms=False):
+    """Reverse-mode gradient of J = sum over wave_frequencies and objective_dofs h of
+    added_mass[h, h] + radiation_damping[h, h], w.r.t. every mesh vertex.
+
+    This is the quantity the reference obtains by differentiating
+    hydrodynamic_coefficients with Zygote / Enzyme through the rules of
+    ad_rules.jl:79-414 (Birk kernels, _mulvec, _linearsolve); here the adjoint is
+    hand-written on the device (mh_hydro_gradient): one adjoint solve per frequency
+    reusing the LU factors, pair derivatives recomputed instead of taped.
+
+    The panel centres, normals and areas must be those meshes.face_fields derives from
+    the vertices (they are differentiated through it); rigid rotation dofs follow the
+    panel centres and are chained through them, other dof fields are held fixed.
+    DirectBEM with the Birk Rankine family and GFWu, zero forward speed, FP64.
+
+    Returns (J, dJ/dvertices as an (nvertices, 3) array); with return_panel_terms the
+    raw per-panel terms of the C-ABI come back as a third item (a dict).
+    """
+    f = formulation or DirectBEM()
+    if not is_direct(f):
+        raise ValueError("hydro_gradient differentiates the direct formulation")
+    if f.precision != "fp64":
+        raise ValueError("hydro_gradient runs in FP64")
+    mesh = body.mesh
+    c, nrm, a, _ = face_fields(mesh.vertices, mesh.faces - 1)
+    if not (np.allclose(c, mesh.centers, rtol=0, atol=1e-12) and np.allclose(nrm, mesh.normals, rtol=0, atol=1e-12)
+            and np.allclose(a, mesh.areas, rtol=1e-12, atol=0)):
+        raise ValueError("the vertex gradient needs panel fields derived from the vertices (meshes.face_fields)")
+    ctx_ = _ctx(ctx)
+    names = list(body.dofs)
+    idx = {n: i for i, n in enumerate(names)}
+    obj = list(objective_dofs)
+    rho = SETTINGS["rho"] if rho is None else rho
+    g = SETTINGS["g"] if g is None else g
+    oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
+    J, gc, gn, ga, gv, gd = _device.hydro_gradient(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
+                                                    body.dof_array(names), [idx[d] for d in obj])
+    gc = gc.copy()
+    # rotation dof field axis x (c - rc) on its panels: d/dc of gd . (axis x c) = gd x axis
+    rot = getattr(body, "rotations", {})
+    for h, name in enumerate(obj):
+        if name in rot:
+            ax, _, p0, p1 = rot[name]
+            e = np.zeros(3)
+            e[ax] = 1.0
+            gc[p0:p1] += np.cross(gd[h, p0:p1], e)
+    dC, dN, dA = face_fields_jacobian(mesh.panel_vertices)
+    corner = (np.einsum("ik,ikq->iq", gc, dC) + np.einsum("ik,ikq->iq", gn, dN) + ga[:, None] * dA
+              + gv.reshape(-1, 12))
+    grad = np.zeros_like(mesh.vertices)
+    faces0 = mesh.faces - 1
+    for q in range(4):
+        np.add.at(grad, faces0[:, q], corner[:, 3 * q:3 * q + 3])
+    if return_panel_terms:
+        return J, grad, {"centers": gc, "normals": gn, "areas": ga, "corners": gv, "dofs": gd}
+    return J, grad
 
 
 def compute_hydrodynamic_coefficients(parameters, body, formulation=None, direct=True, gf="Wu",

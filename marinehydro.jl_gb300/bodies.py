@@ -47,6 +47,9 @@ class FloatingBody:
         self.mesh = mesh
         self.lid_mesh = None
         self.body_name = body_name
+        # rigid rotation dofs: name -> (axis index, rotation centre, first panel, end panel); their
+        # fields follow the panel centres, which the gradient chain needs
+        self.rotations = {}
         if dofs is None:
             dofs = {}
         if isinstance(dofs, dict):
@@ -58,6 +61,8 @@ class FloatingBody:
                 name = str(name)
                 self.dofs[name] = (translational_dofs(mesh, name) if name in TRANSLATIONS
                                    else rotational_dofs(mesh, name, rc))
+                if name in ROTATIONS:
+                    self.rotations[name] = (ROTATIONS.index(name), tuple(float(x) for x in rc), 0, mesh.nfaces)
         for k, v in self.dofs.items():
             if v.shape != (mesh.nfaces, 3):
                 raise ValueError(f"dof {k} must have shape ({mesh.nfaces}, 3)")
@@ -94,12 +99,16 @@ def combine_floatingbodies(bodies, new_body_name: str | None = None) -> Floating
     names = _unique_names([b.body_name.replace(" ", "_") for b in bodies])
     mesh = combine_meshes([b.mesh for b in bodies])
     total = mesh.nfaces
-    dofs = {}
+    dofs, rotations = {}, {}
     off = 0
     for b, nm in zip(bodies, names):
         for k, v in b.dofs.items():
             d = np.zeros((total, 3))
             d[off:off + b.mesh.nfaces] = v
             dofs[f"{nm}__{k}"] = d
+        for k, (ax, rc, p0, p1) in getattr(b, "rotations", {}).items():
+            rotations[f"{nm}__{k}"] = (ax, rc, off + p0, off + p1)
         off += b.mesh.nfaces
-    return FloatingBody(mesh, dofs, body_name=new_body_name or "+".join(names))
+    out = FloatingBody(mesh, dofs, body_name=new_body_name or "+".join(names))
+    out.rotations = rotations
+    return out

@@ -191,7 +191,7 @@ int copy_in(mh_context* ctx, void* dst, const void* src, size_t bytes, int mem) 
 }
 
 int copy_out(mh_context* ctx, void* dst, const void* src, size_t bytes, int mem) {
-  if (bytes == 0) return MH_OK;
+  if (!dst || bytes == 0) return MH_OK;  // NULL destination skips
   MH_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, mem == MH_MEM_HOST ? cudaMemcpyDeviceToHost
                                                                    : cudaMemcpyDeviceToDevice, ctx->stream));
   return MH_OK;
@@ -1229,7 +1229,7 @@ int mh_batch_release(mh_context* ctx) {
 int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       double* J, double* grad_centers, double* grad_normals, double* grad_areas,
-                      double* grad_vertices, int mem) {
+                      double* grad_vertices, double* grad_dofs, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
@@ -1250,6 +1250,14 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   const size_t nn = (size_t)n * n;
   cudaStream_t st = ctx->stream;
   const LaunchCounter lc = ctx->lc();
+  // frequencies are processed in chunks sized by free memory, like the sweep: assembly,
+  // factorization and both solves run batched over a chunk, the adjoint kernels per frequency
+  size_t free_b = 0, total_b = 0;
+  MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+  const size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nh * sizeof(double2) * 6;
+  const size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
+  const int64_t chunk = std::min<int64_t>(n_omega, (int64_t)std::max<size_t>(1, budget / per_w));
+  const int64_t bstride = n * nh;
   double *SR, *DR, *RS, *RD, *grad, *small, *dofs_d;
   double2 *S, *D, *B, *X, *lam, *t, *work, *F, *FK;
   int32_t *ipiv, *info;
@@ -1257,19 +1265,21 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   MH_TRY(ws_get_t(ctx, kSlotDR, nn, &DR));
   MH_TRY(ws_get_t(ctx, kSlotRS, nn, &RS));
   MH_TRY(ws_get_t(ctx, kSlotRD, nn, &RD));
-  MH_TRY(ws_get_t(ctx, kSlotS, nn, &S));
-  MH_TRY(ws_get_t(ctx, kSlotD, nn, &D));
-  MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)(n * nh), &B));
-  MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(n * nh), &X));
-  MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(n * nh), &lam));
-  MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(n * nh), &t));
-  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nh, 1), &work));
-  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(nh * nh), &F));
+  MH_TRY(ws_get_t(ctx, kSlotS, nn * chunk, &S));
+  MH_TRY(ws_get_t(ctx, kSlotD, nn * chunk, &D));
+  MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)(bstride * chunk), &B));
+  MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(bstride * chunk), &X));
+  MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(bstride * chunk), &lam));
+  MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(bstride * chunk), &t));
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nh, chunk), &work));
+  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(nh * nh * n_omega), &F));
   MH_TRY(ws_get_t(ctx, kSlotFK, 4, &FK));
-  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
-  MH_TRY(ws_get_t(ctx, kSlotInfo, 1, &info));
-  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)(19 * n), &grad));
-  MH_TRY(ws_get_t(ctx, kSlotIdx, 8, &small));
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * chunk), &ipiv));
+  MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)chunk, &info));
+  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)((19 + 3 * nh) * n), &grad));
+  // small device block: [omegas | wavenumbers | objective dof indices (int32)]
+  const size_t nsmall = (size_t)(2 * n_omega) + 4;
+  MH_TRY(ws_get_t(ctx, kSlotIdx, nsmall, &small));
   if (mem == MH_MEM_DEVICE) {
     dofs_d = (double*)dofs;
   } else {
@@ -1280,7 +1290,8 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   double* gn = grad + 3 * n;
   double* ga = grad + 6 * n;
   double* gv = grad + 7 * n;
-  MH_CUDA(ctx, cudaMemsetAsync(grad, 0, sizeof(double) * 19 * n, st));
+  double* gd = grad + 19 * n;
+  MH_CUDA(ctx, cudaMemsetAsync(grad, 0, sizeof(double) * (19 + 3 * nh) * n, st));
   MH_CUDA(ctx, cudaMemsetAsync(RS, 0, sizeof(double) * nn, st));
   MH_CUDA(ctx, cudaMemsetAsync(RD, 0, sizeof(double) * nn, st));
   const uint32_t stk = gfs & kStaticKinds;
@@ -1290,61 +1301,72 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     MH_TRY(check_launch(ctx, "static assembly"));
   }
   AssemblyParams p = make_params(ctx, m, gfs, 1, 1, nullptr);
-  // staging: [omega, k, obj idx]
   double* hs;
-  MH_TRY(pinned_get(ctx, 64 + sizeof(double2) * (size_t)(nh * nh), &hs));
-  int32_t* hobj = (int32_t*)(hs + 4);
-  for (int64_t q = 0; q < nh; ++q) hobj[q] = obj_idx[q];
-  double2* hF = (double2*)(hs + 8);
-  double Jsum = 0.0;
-  BatchDesc d{n, 1, (int64_t)nn};
-  EpilogueGeom eg{n, m->C, m->N, m->A, dofs_d};
-  const int32_t* obj_d = (const int32_t*)(small + 4);
+  MH_TRY(pinned_get(ctx, sizeof(double) * nsmall + sizeof(double2) * (size_t)(nh * nh * n_omega) +
+                             sizeof(int32_t) * (size_t)chunk + 64, &hs));
   for (int64_t w = 0; w < n_omega; ++w) {
-    const double om = omegas[w], k = om * om / g;
-    hs[0] = om;
-    hs[1] = k;
-    MH_CUDA(ctx, cudaMemcpyAsync(small, hs, sizeof(double) * 8, cudaMemcpyHostToDevice, st));
-    launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, 1, small + 1, S, D, (int64_t)nn,
+    hs[w] = omegas[w];
+    hs[n_omega + w] = omegas[w] * omegas[w] / g;
+  }
+  int32_t* hobj = (int32_t*)(hs + 2 * n_omega);
+  for (int64_t q = 0; q < nh; ++q) hobj[q] = obj_idx[q];
+  double2* hF = (double2*)(hs + nsmall);
+  int32_t* hinfo = (int32_t*)(hF + nh * nh * n_omega);
+  MH_CUDA(ctx, cudaMemcpyAsync(small, hs, sizeof(double) * nsmall, cudaMemcpyHostToDevice, st));
+  const double* om_d = small;
+  const double* ks_d = small + n_omega;
+  const int32_t* obj_d = (const int32_t*)(small + 2 * n_omega);
+  EpilogueGeom eg{n, m->C, m->N, m->A, dofs_d};
+  for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
+    const int64_t nw = std::min<int64_t>(chunk, n_omega - w0);
+    BatchDesc d{n, nw, (int64_t)nn};
+    launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, (int)nw, ks_d + w0, S, D, (int64_t)nn,
                          stk ? 0 : 1);
-    launch_build_rhs(st, lc, eg, 1, small, g, (int)nh, obj_d, 0, nullptr, B, n * nh);
-    zgemm_nn_batched(st, lc, d, S, B, nh, n * nh, X, work);
+    launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nh, obj_d, 0, nullptr, B, bstride);
+    zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
     lu_factor_batched<double>(st, lc, d, D, ipiv, info);
-    lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, n * nh, false);        // X = phi
-    launch_forces(st, lc, eg, 1, small, rho, g, (int)nh, X, n * nh, (int)nh, obj_d, 0, nullptr, F, FK);
-    launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, lam);
-    lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, n * nh, true);       // mu = D^-H conj(w)
-    zgemm_adj_batched(st, lc, d, S, lam, nh, n * nh, t, work);                 // S^H mu
-    launch_conj(st, lc, n * nh, t);                                            // t = S^T lam
-    launch_conj(st, lc, n * nh, lam);                                          // lam = D^-T w
-    const double2 c = make_double2(1.0 / (om * om), -1.0 / om);
-    if (gfs & MH_GF_WU) {
-      launch_wave_adjoint(st, lc, p, k, lam, B, X, (int)nh, c, gc, gn, ga, RS, RD);
-    } else {
-      // static-only objective: accumulate the weights without a wave term
-      AssemblyParams pz = p;
-      pz.gfs = 0;
-      launch_wave_adjoint(st, lc, pz, k, lam, B, X, (int)nh, c, gc, gn, ga, RS, RD);
+    lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, bstride, false);       // X = phi
+    launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nh, X, bstride, (int)nh, obj_d, 0, nullptr,
+                  F + w0 * nh * nh, FK);
+    for (int64_t w = 0; w < nw; ++w)
+      launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, omegas[w0 + w], rho, lam + w * bstride);
+    lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, bstride, true);      // mu = D^-H conj(w)
+    zgemm_adj_batched(st, lc, d, S, lam, nh, bstride, t, work);                // S^H mu
+    launch_conj(st, lc, nw * bstride, t);                                      // t = S^T lam
+    launch_conj(st, lc, nw * bstride, lam);                                    // lam = D^-T w
+    for (int64_t w = 0; w < nw; ++w) {
+      const double om = omegas[w0 + w], k = om * om / g;
+      const double2 c = make_double2(1.0 / (om * om), -1.0 / om);
+      // wave-term gradient (GFWu only) and the frequency-summed Rankine weights
+      launch_wave_adjoint(st, lc, p, k, lam + w * bstride, B + w * bstride, X + w * bstride, (int)nh, c, gc, gn, ga,
+                          RS, RD);
+      launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, c, X + w * bstride,
+                         t + w * bstride, gn, ga, gd);
     }
-    launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, c, X, t, gn, ga);
-    MH_TRY(check_launch(ctx, "gradient frequency"));
-    int32_t hinfo = 0;
-    MH_CUDA(ctx, cudaMemcpyAsync(hF, F, sizeof(double2) * nh * nh, cudaMemcpyDeviceToHost, st));
-    MH_CUDA(ctx, cudaMemcpyAsync(&hinfo, info, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    MH_TRY(sync(ctx, "gradient frequency"));
-    if (hinfo) return fail(ctx, MH_ERR_SINGULAR, "singular D at omega %g", om);
+    MH_TRY(check_launch(ctx, "gradient frequencies"));
+    MH_CUDA(ctx, cudaMemcpyAsync(hinfo, info, sizeof(int32_t) * nw, cudaMemcpyDeviceToHost, st));
+    MH_TRY(sync(ctx, "gradient frequencies"));
+    for (int64_t w = 0; w < nw; ++w)
+      if (hinfo[w]) return fail(ctx, MH_ERR_SINGULAR, "singular D at omega %g", omegas[w0 + w]);
+  }
+  MH_CUDA(ctx, cudaMemcpyAsync(hF, F, sizeof(double2) * nh * nh * n_omega, cudaMemcpyDeviceToHost, st));
+  if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
+  MH_TRY(check_launch(ctx, "static adjoint"));
+  MH_TRY(sync(ctx, "forces"));
+  double Jsum = 0.0;
+  for (int64_t w = 0; w < n_omega; ++w) {
+    const double om = omegas[w];
     for (int64_t h = 0; h < nh; ++h) {
-      const double2 f = hF[h * nh + h];  // influenced dof h, right-hand side h
+      const double2 f = hF[(w * nh + h) * nh + h];  // influenced dof h, right-hand side h
       Jsum += f.x / (om * om) + f.y / om;
     }
   }
-  if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
-  MH_TRY(check_launch(ctx, "static adjoint"));
   if (J) *J = Jsum;
   MH_TRY(copy_out(ctx, grad_centers, gc, sizeof(double) * 3 * n, mem));
   MH_TRY(copy_out(ctx, grad_normals, gn, sizeof(double) * 3 * n, mem));
   MH_TRY(copy_out(ctx, grad_areas, ga, sizeof(double) * n, mem));
   MH_TRY(copy_out(ctx, grad_vertices, gv, sizeof(double) * 12 * n, mem));
+  MH_TRY(copy_out(ctx, grad_dofs, gd, sizeof(double) * 3 * nh * n, mem));
   return sync(ctx, "gradient");
 }
 

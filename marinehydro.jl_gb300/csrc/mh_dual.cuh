@@ -1,0 +1,135 @@
+// mh_dual.cuh -- forward-mode dual numbers for the reverse (adjoint) kernels.
+//
+// Dn<M> carries a value and M partial derivatives.  The adjoint kernels evaluate
+// the pair Green functions on Dn to obtain the exact derivatives of the code path
+// the primal kernels run (the Wu polynomial/Struve fits, the Birk panel
+// integral), the way the reference differentiates them with ForwardDiff / Enzyme
+// (ad_rules.jl:79-294).  Derivatives of the special functions:
+//   d j0 = -j1, d j1 = j0 - j1/x, d y0 = -y1, d y1 = y0 - y1/x,
+//   d atan2(y, x) = (x dy - y dx) / (x^2 + y^2).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mh {
+
+template <int M>
+struct Dn {
+  double v;
+  double d[M];
+  __device__ Dn() : v(0.0) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) d[q] = 0.0;
+  }
+  __device__ Dn(double x) : v(x) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) d[q] = 0.0;
+  }
+  __device__ static Dn var(double x, int slot) {
+    Dn r(x);
+    if (slot >= 0 && slot < M) r.d[slot] = 1.0;
+    return r;
+  }
+};
+
+template <int M> __device__ __forceinline__ double val(const Dn<M>& a) { return a.v; }
+__device__ __forceinline__ double val(double a) { return a; }
+
+// double overloads, so that templated code written for Dn also compiles for double
+// (and unqualified calls inside namespace mh keep finding the CUDA math functions)
+__device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+__device__ __forceinline__ double log(double x) { return ::log(x); }
+__device__ __forceinline__ double exp(double x) { return ::exp(x); }
+__device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
+__device__ __forceinline__ double hypot(double x, double y) { return ::hypot(x, y); }
+__device__ __forceinline__ double j0(double x) { return ::j0(x); }
+__device__ __forceinline__ double j1(double x) { return ::j1(x); }
+__device__ __forceinline__ double y0(double x) { return ::y0(x); }
+__device__ __forceinline__ double y1(double x) { return ::y1(x); }
+
+// chain: r = f(a) with f'(a) = s
+template <int M> __device__ __forceinline__ Dn<M> chain1(const Dn<M>& a, double fv, double s) {
+  Dn<M> r(fv);
+#pragma unroll
+  for (int q = 0; q < M; ++q) r.d[q] = s * a.d[q];
+  return r;
+}
+
+template <int M> __device__ __forceinline__ Dn<M> operator+(const Dn<M>& a, const Dn<M>& b) {
+  Dn<M> r(a.v + b.v);
+#pragma unroll
+  for (int q = 0; q < M; ++q) r.d[q] = a.d[q] + b.d[q];
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> operator-(const Dn<M>& a, const Dn<M>& b) {
+  Dn<M> r(a.v - b.v);
+#pragma unroll
+  for (int q = 0; q < M; ++q) r.d[q] = a.d[q] - b.d[q];
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> operator-(const Dn<M>& a) { return chain1(a, -a.v, -1.0); }
+template <int M> __device__ __forceinline__ Dn<M> operator*(const Dn<M>& a, const Dn<M>& b) {
+  Dn<M> r(a.v * b.v);
+#pragma unroll
+  for (int q = 0; q < M; ++q) r.d[q] = a.d[q] * b.v + a.v * b.d[q];
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> operator/(const Dn<M>& a, const Dn<M>& b) {
+  const double inv = 1.0 / b.v, rv = a.v * inv;
+  Dn<M> r(a.v / b.v);
+#pragma unroll
+  for (int q = 0; q < M; ++q) r.d[q] = (a.d[q] - rv * b.d[q]) * inv;
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> operator+(const Dn<M>& a, double b) { return chain1(a, a.v + b, 1.0); }
+template <int M> __device__ __forceinline__ Dn<M> operator+(double b, const Dn<M>& a) { return chain1(a, b + a.v, 1.0); }
+template <int M> __device__ __forceinline__ Dn<M> operator-(const Dn<M>& a, double b) { return chain1(a, a.v - b, 1.0); }
+template <int M> __device__ __forceinline__ Dn<M> operator-(double b, const Dn<M>& a) { return chain1(a, b - a.v, -1.0); }
+template <int M> __device__ __forceinline__ Dn<M> operator*(const Dn<M>& a, double b) { return chain1(a, a.v * b, b); }
+template <int M> __device__ __forceinline__ Dn<M> operator*(double b, const Dn<M>& a) { return chain1(a, b * a.v, b); }
+template <int M> __device__ __forceinline__ Dn<M> operator/(const Dn<M>& a, double b) { return chain1(a, a.v / b, 1.0 / b); }
+template <int M> __device__ __forceinline__ Dn<M> operator/(double b, const Dn<M>& a) {
+  return chain1(a, b / a.v, -b / (a.v * a.v));
+}
+template <int M> __device__ __forceinline__ Dn<M>& operator+=(Dn<M>& a, const Dn<M>& b) { a = a + b; return a; }
+template <int M> __device__ __forceinline__ Dn<M>& operator-=(Dn<M>& a, const Dn<M>& b) { a = a - b; return a; }
+
+template <int M> __device__ __forceinline__ Dn<M> sqrt(const Dn<M>& a) {
+  const double s = ::sqrt(a.v);
+  return chain1(a, s, s > 0.0 ? 0.5 / s : 0.0);
+}
+template <int M> __device__ __forceinline__ Dn<M> log(const Dn<M>& a) { return chain1(a, ::log(a.v), 1.0 / a.v); }
+template <int M> __device__ __forceinline__ Dn<M> exp(const Dn<M>& a) {
+  const double e = ::exp(a.v);
+  return chain1(a, e, e);
+}
+template <int M> __device__ __forceinline__ Dn<M> atan2(const Dn<M>& y, const Dn<M>& x) {
+  const double den = x.v * x.v + y.v * y.v;
+  Dn<M> r(::atan2(y.v, x.v));
+  if (den > 0.0) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) r.d[q] = (x.v * y.d[q] - y.v * x.d[q]) / den;
+  }
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> hypot(const Dn<M>& x, const Dn<M>& y) {
+  const double h = ::hypot(x.v, y.v);
+  Dn<M> r(h);
+  if (h > 0.0) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) r.d[q] = (x.v * x.d[q] + y.v * y.d[q]) / h;
+  }
+  return r;
+}
+template <int M> __device__ __forceinline__ Dn<M> j0(const Dn<M>& a) { return chain1(a, ::j0(a.v), -::j1(a.v)); }
+template <int M> __device__ __forceinline__ Dn<M> j1(const Dn<M>& a) {
+  const double x = a.v, J1 = ::j1(x);
+  return chain1(a, J1, x != 0.0 ? ::j0(x) - J1 / x : 0.5);
+}
+template <int M> __device__ __forceinline__ Dn<M> y0(const Dn<M>& a) { return chain1(a, ::y0(a.v), -::y1(a.v)); }
+template <int M> __device__ __forceinline__ Dn<M> y1(const Dn<M>& a) {
+  const double x = a.v, Y1 = ::y1(x);
+  return chain1(a, Y1, ::y0(x) - Y1 / x);
+}
+
+}  // namespace mh

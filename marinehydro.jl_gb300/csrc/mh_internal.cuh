@@ -144,7 +144,7 @@ void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams
                          double* RS, double* RD);
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
                         const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2 c,
-                        const double2* phi, const double2* t, double* gn, double* ga);
+                        const double2* phi, const double2* t, double* gn, double* ga, double* gd);
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
                           const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2* wconj);
 void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x);

@@ -96,6 +96,40 @@ def face_fields(vertices: np.ndarray, faces0: np.ndarray):
     return center, nrm, area1 + area2, radius
 
 
+def _corner_fields(a, b, c, d, degenerate2):
+    """face_fields on corner arrays, written with analytic operations only (no abs), so
+    that a complex step through it differentiates it.  A triangle stored as a quad
+    (c == d) has a second triangle of area 0 whatever the shared vertex does: such
+    panels (``degenerate2``) keep area2 = 0 instead of differentiating |0|."""
+    def norm(x):
+        return np.sqrt(np.sum(x * x, axis=-1))
+    nrm = np.cross(b - a, c - a)
+    area1 = 0.5 * norm(nrm)
+    area2 = np.where(degenerate2, 0.0, 0.5 * norm(np.cross(c - a, d - a)))
+    center = (((a + b + c) / 3) * area1[:, None] + ((a + c + d) / 3) * area2[:, None]) / (area1 + area2)[:, None]
+    return center, nrm / norm(nrm)[:, None], area1 + area2
+
+
+def face_fields_jacobian(panel_vertices: np.ndarray, step: float = 1e-30):
+    """Jacobians of (center, normal, area) w.r.t. the 12 corner coordinates of each panel
+    (corner q, axis x -> column 3q + x), by complex step: exact to rounding.
+    Returns dC (n,3,12), dN (n,3,12), dA (n,12)."""
+    V = np.asarray(panel_vertices, dtype=np.float64)
+    n = V.shape[0]
+    dC = np.empty((n, 3, 12))
+    dN = np.empty((n, 3, 12))
+    dA = np.empty((n, 12))
+    deg2 = np.all(np.cross(V[:, 2] - V[:, 0], V[:, 3] - V[:, 0]) == 0.0, axis=-1)
+    for col in range(12):
+        Vc = V.astype(np.complex128)
+        Vc[:, col // 3, col % 3] += 1j * step
+        c, nv, ar = _corner_fields(Vc[:, 0], Vc[:, 1], Vc[:, 2], Vc[:, 3], deg2)
+        dC[:, :, col] = c.imag / step
+        dN[:, :, col] = nv.imag / step
+        dA[:, col] = ar.imag / step
+    return dC, dN, dA
+
+
 def combine_meshes(meshes) -> StaticArraysMesh:
     """combine_meshes (meshes.jl:56-92): concatenate, offsetting face indices."""
     verts, faces, cs, ns, as_, rs = [], [], [], [], [], []

@@ -1,0 +1,147 @@
+"""Reverse-mode gradient (mh_hydro_gradient) against central finite differences.
+
+Two truncated cylinders side by side; the objective is the summed diagonal added
+mass + radiation damping of the objective dofs over a few frequencies.  The
+finite differences use the device sweep (itself pinned against the oracle) with
+h = 1e-6 along per-body affine vertex moves.  Affine moves keep every panel
+planar: the Birk self term zeroes the solid-angle part of an in-plane field
+point, so along a move that bends a panel out of its plane the primal is not
+smooth at h = 0 and no derivative exists to compare with.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-6
+OMEGAS = (0.6, 1.1, 1.7)
+RTOL = 1e-6  # central differences at h = 1e-6 carry ~1e-9 relative rounding and h^2 truncation
+
+
+def _geometry(mh):
+    m1 = mh.vertical_cylinder_mesh(1.0, 1.6, 10, 4, 2)
+    m2 = mh.vertical_cylinder_mesh(1.0, 1.6, 10, 4, 2, center=(4.0, 0.5))
+    return m1, m2
+
+
+def _body(mh, V1, V2, m1, m2, dofs):
+    b1 = mh.FloatingBody(mh.StaticArraysMesh(V1, m1.faces), dofs, rotation_center=(0.0, 0.0, -0.5), body_name="c1")
+    b2 = mh.FloatingBody(mh.StaticArraysMesh(V2, m2.faces), dofs, rotation_center=(4.0, 0.5, -0.5),
+                         body_name="c2")
+    return b1 + b2
+
+
+def _objective(mh, ctx, body, obj, F):
+    r = mh.hydrodynamic_coefficients(body, {"wave_frequencies": OMEGAS, "radiating_dofs": obj,
+                                            "influenced_dofs": obj}, F, ctx=ctx, rho=1025.0, g=9.81)
+    A, B = r["added_mass"][..., 0], r["radiation_damping"][..., 0]
+    return sum(A[h, h, w] + B[h, h, w] for h in range(len(obj)) for w in range(len(OMEGAS)))
+
+
+def _affine_moves(V1, V2, rng):
+    """Per-body affine vertex moves that keep z = 0 at z = 0 (no panel leaves the water)."""
+    moves = []
+    for which in (0, 1):
+        M = rng.standard_normal((3, 3))
+        M[2, :2] = 0.0
+        t = np.array([rng.standard_normal(), rng.standard_normal(), 0.0])
+        d1 = V1 @ M.T + t if which == 0 else np.zeros_like(V1)
+        d2 = V2 @ M.T + t if which == 1 else np.zeros_like(V2)
+        moves.append((d1, d2))
+    moves.append((np.zeros_like(V1), np.tile([1.0, 0.0, 0.0], (len(V2), 1))))  # spacing
+    moves.append((V1 * [0.0, 0.0, 1.0], np.zeros_like(V2)))                      # draft of body 1
+    return moves
+
+
+@pytest.mark.parametrize("gf,obj", [("wu_heave", ["c1__Heave", "c2__Heave"]),
+                                    ("wu_pitch", ["c1__Pitch", "c2__Heave"]),
+                                    ("rankine", ["c1__Heave"])])
+def test_gradient_matches_finite_differences(mh, ctx, gf, obj):
+    F = mh.DirectBEM() if gf.startswith("wu") else mh.DirectBEM((mh.Rankine(), mh.RankineReflectedNegative()))
+    m1, m2 = _geometry(mh)
+    dofs = ["Heave", "Pitch"]
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
+    J, grad = mh.hydro_gradient(body, OMEGAS, obj, F, ctx=ctx, rho=1025.0, g=9.81)
+    J_sweep = _objective(mh, ctx, body, obj, F)
+    assert abs(J - J_sweep) <= 1e-12 * abs(J_sweep)
+    n1 = m1.nvertices
+    rng = np.random.default_rng(11)
+    for d1, d2 in _affine_moves(m1.vertices, m2.vertices, rng):
+        jp = _objective(mh, ctx, _body(mh, m1.vertices + H * d1, m2.vertices + H * d2, m1, m2, dofs), obj, F)
+        jm = _objective(mh, ctx, _body(mh, m1.vertices - H * d1, m2.vertices - H * d2, m1, m2, dofs), obj, F)
+        fd = (jp - jm) / (2 * H)
+        ad = float(np.sum(grad[:n1] * d1) + np.sum(grad[n1:] * d2))
+        scale = np.abs(grad).sum() * max(np.abs(d1).max(), np.abs(d2).max())
+        assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
+
+
+def test_gradient_rejects_unsupported(mh, ctx):
+    m1, m2 = _geometry(mh)
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave"])
+    with pytest.raises(ValueError):
+        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.IndirectBEM(), ctx=ctx)
+    with pytest.raises(ValueError):
+        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.DirectBEM("ExactGuevelDelhommeau"), ctx=ctx)
+
+
+def _soup(mh, V4, C, N, A, R):
+    """A mesh whose panels own their corners and carry the given (independent) fields."""
+    n = len(C)
+    return mh.StaticArraysMesh(V4.reshape(-1, 3), np.arange(4 * n).reshape(n, 4) + 1, C, N, A, R)
+
+
+def _inplane(v, N):
+    """Component of v (n, ..., 3) orthogonal to each panel normal N (n, 3)."""
+    if v.ndim == 3:
+        return v - np.einsum("iqk,ik->iq", v, N)[..., None] * N[:, None, :]
+    return v - np.sum(v * N, axis=1)[:, None] * N
+
+
+@pytest.mark.parametrize("wu", [True, False])
+def test_panel_terms_match_finite_differences(mh, ctx, wu):
+    """Each per-panel term of mh_hydro_gradient alone: areas, normals, in-plane centre
+    moves, in-plane corner moves and dof fields, perturbed independently.  In-plane
+    moves keep every self and coplanar pair in the plane of its panel; a triangle's
+    repeated corner moves with its twin (moved apart, the zero-length edge the Birk
+    integral skips would open: a kink, not a derivative)."""
+    from importlib import import_module
+    dev = import_module("marinehydro_gb300._device")
+    m1, m2 = _geometry(mh)
+    mesh = m1 + m2
+    body = mh.FloatingBody(mesh, ["Heave", "Pitch"], rotation_center=(0.0, 0.0, -0.5))
+    dofs = body.dof_array(["Heave", "Pitch"])
+    obj = [0, 1]
+    gfs = mh.gf_flags((mh.Rankine(), mh.RankineReflected()) + ((mh.GFWu(),) if wu else ()))
+    V4, C, N, A, R = mesh.panel_vertices, mesh.centers, mesh.normals, mesh.areas, mesh.radii
+
+    def J(V4_, C_, N_, A_, dofs_):
+        sm = _soup(mh, V4_, C_, N_, A_, R)
+        a, b, *_ = dev.hydro_sweep(ctx, sm.device_mesh(ctx), OMEGAS, 1025.0, 9.81, gfs, True, dofs_, obj, obj, [])
+        return sum(a[h, h, w] + b[h, h, w] for h in range(2) for w in range(len(OMEGAS)))
+
+    sm0 = _soup(mh, V4, C, N, A, R)
+    J0, gc, gn, ga, gv, gd = dev.hydro_gradient(ctx, sm0.device_mesh(ctx), OMEGAS, 1025.0, 9.81, gfs, dofs, obj)
+    assert abs(J0 - J(V4, C, N, A, dofs)) <= 1e-12 * abs(J0)
+    rng = np.random.default_rng(17)
+    z = np.zeros_like
+    dAr = rng.standard_normal(A.shape) * A
+    dN = rng.standard_normal(N.shape)
+    dC = _inplane(rng.standard_normal(C.shape), N)
+    dV = _inplane(rng.standard_normal(V4.shape), N)
+    tri = np.all(V4[:, 3] == V4[:, 2], axis=1)  # a triangle's repeated corner moves with its twin
+    dV[tri, 3] = dV[tri, 2]
+    dD = np.zeros_like(dofs)
+    dD[obj] = rng.standard_normal(dofs[obj].shape)
+    cases = {"areas": ((z(V4), z(C), z(N), dAr, z(dofs)), np.sum(ga * dAr)),
+             "normals": ((z(V4), z(C), dN, z(A), z(dofs)), np.sum(gn * dN)),
+             "centers": ((z(V4), dC, z(N), z(A), z(dofs)), np.sum(gc * dC)),
+             "corners": ((dV, z(C), z(N), z(A), z(dofs)), np.sum(gv * dV)),
+             "dofs": ((z(V4), z(C), z(N), z(A), dD), np.sum(gd * dD[obj]))}
+    bad = {}
+    for name, (d, ad) in cases.items():
+        plus = [x + H * dx for x, dx in zip((V4, C, N, A, dofs), d)]
+        minus = [x - H * dx for x, dx in zip((V4, C, N, A, dofs), d)]
+        fd = (J(*plus) - J(*minus)) / (2 * H)
+        if not abs(ad - fd) <= RTOL * max(abs(fd), 1e-6 * abs(J0)):
+            bad[name] = (ad, fd)
+    assert not bad, bad
