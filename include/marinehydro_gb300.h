@@ -214,6 +214,9 @@ int mh_batch_release(mh_context* ctx);
      gfs:       Birk Rankine kinds (MH_GF_RANKINE*) and/or MH_GF_WU
      dofs:      n_dofs x n x 3 dof fields, held fixed
      obj_idx:   1..4 indices into dofs
+     precision: MH_PREC_FP64, or MH_PREC_MIXED: FP32 factors with both the forward and
+                the adjoint solve refined to the FP64 backward-error test (a frequency
+                chunk that does not converge is redone with FP64 factors)
    Outputs (any may be NULL):
      J                   the objective
      grad_centers[n][3], grad_normals[n][3], grad_areas[n]: dJ w.r.t. the
@@ -223,7 +226,7 @@ int mh_batch_release(mh_context* ctx);
    The caller chains these through its mesh and dof construction. */
 int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
-                      double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                      int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem);
 
 /* ---- wave-term evaluators (kernel-level parity entry points) ------------- */

@@ -193,7 +193,7 @@ def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_bod
     return out
 
 
-def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx):
+def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx, precision=_lib.MH_PREC_FP64):
     """mh_hydro_gradient with host buffers.
 
     Returns (J, gc (n,3), gn (n,3), ga (n,), gv (n,4,3), gd (n_obj,n,3)): the objective
@@ -211,6 +211,6 @@ def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx):
     gd = np.empty((oi.size, n, 3))
     ctx.check(ctx._L.mh_hydro_gradient(
         ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), dofs.shape[0],
-        dofs.ctypes.data, oi.size, oi.ctypes.data, ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data,
+        dofs.ctypes.data, oi.size, oi.ctypes.data, int(precision), ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data,
         gv.ctypes.data, gd.ctypes.data, MH_MEM_HOST), "hydro_gradient")
     return J.value, gc, gn, ga, gv, gd

@@ -98,7 +98,7 @@ def load(path: str | None = None):
         L.mh_batch_hydrodynamic_coefficients.argtypes = [vp, i64, vp, vp, vp, D, D, u32, I, i64, vp, i64, vp, i64,
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
-        L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, vp, vp, vp, vp, vp, vp, I]
+        L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, I, vp, vp, vp, vp, vp, vp, I]
         L.mh_assemble_matrices_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, D, u32, I, I, vp, vp, vp]
         for name in EXPORTS:
             getattr(L, name)  # AttributeError if the build lacks a declared entry point

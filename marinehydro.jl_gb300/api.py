@@ -287,7 +287,9 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     The panel centres, normals and areas must be those meshes.face_fields derives from
     the vertices (they are differentiated through it); rigid rotation dofs follow the
     panel centres and are chained through them, other dof fields are held fixed.
-    DirectBEM with the Birk Rankine family and GFWu, zero forward speed, FP64.
+    DirectBEM with the Birk Rankine family and GFWu, zero forward speed, FP64
+    arithmetic; formulation precision "mixed" factors in FP32 and refines both the
+    forward and the adjoint solve to the FP64 backward-error test.
 
     Returns (J, dJ/dvertices as an (nvertices, 3) array); with return_panel_terms the
     raw per-panel terms of the C-ABI come back as a third item (a dict).
@@ -295,8 +297,6 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     f = formulation or DirectBEM()
     if not is_direct(f):
         raise ValueError("hydro_gradient differentiates the direct formulation")
-    if f.precision != "fp64":
-        raise ValueError("hydro_gradient runs in FP64")
     mesh = body.mesh
     c, nrm, a, _ = face_fields(mesh.vertices, mesh.faces - 1)
     if not (np.allclose(c, mesh.centers, rtol=0, atol=1e-12) and np.allclose(nrm, mesh.normals, rtol=0, atol=1e-12)
@@ -310,7 +310,7 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     g = SETTINGS["g"] if g is None else g
     oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
     J, gc, gn, ga, gv, gd = _device.hydro_gradient(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
-                                                    body.dof_array(names), [idx[d] for d in obj])
+                                                    body.dof_array(names), [idx[d] for d in obj], f.precision_code)
     gc = gc.copy()
     # rotation dof field axis x (c - rc) on its panels: d/dc of gd . (axis x c) = gd x axis
     rot = getattr(body, "rotations", {})

@@ -266,9 +266,100 @@ int ensure_static_cache(mh_context* ctx, mh_mesh* m, uint32_t gfs, int direct, i
 }
 
 // --- dense solve core on device arrays ------------------------------------------
+// FP32 copy of the batch `Adev` (left intact for the FP64 residuals), factored in place.
+int factor_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, float2** LU32_out) {
+  const int64_t n = d.n, nn = n * n;
+  int32_t *ipiv, *info;
+  float2* LU32;
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * d.batch), &ipiv));
+  MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)d.batch, &info));
+  MH_TRY(ws_get_t(ctx, kSlotLU32, (size_t)(nn * d.batch), &LU32));
+  BatchDesc d32 = d;
+  d32.stride = nn;
+  for (int64_t b = 0; b < d.batch; ++b) convert_z_to_c(ctx->stream, ctx->lc(), Adev + b * d.stride, LU32 + b * nn, nn);
+  lu_factor_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, info);
+  MH_TRY(check_launch(ctx, "lu factor fp32"));
+  *LU32_out = LU32;
+  return MH_OK;
+}
+
+// Solve A x = b (or A^H x = b) with the FP32 factors of factor_mixed and FP64 iterative
+// refinement under LAPACK zcgesv's stopping rule: accept x when
+// |b - A x|_inf <= sqrt(n) eps |A|_inf |x|_inf for every column, at most 30 sweeps.
+// X holds b on entry and x on exit; *converged reports whether every column met the test
+// (when it did not, X holds the last iterate and the caller falls back to FP64).
+int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const float2* LU32, double2* X,
+                 int64_t nrhs, int64_t xstride, bool adjoint, bool* converged, double2** B0_out) {
+  const int64_t n = d.n, nn = n * n;
+  int32_t* ipiv;
+  float2* X32;
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * d.batch), &ipiv));
+  MH_TRY(ws_get_t(ctx, kSlotX32, (size_t)(xstride * d.batch), &X32));
+  BatchDesc d32 = d;
+  d32.stride = nn;
+  double2 *B0, *R, *work;
+  MH_TRY(ws_get_t(ctx, kSlotB, (size_t)(xstride * d.batch), &B0));
+  MH_TRY(ws_get_t(ctx, kSlotR, (size_t)(xstride * d.batch), &R));
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, d.batch), &work));
+  MH_CUDA(ctx, cudaMemcpyAsync(B0, X, sizeof(double2) * xstride * d.batch, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (B0_out) *B0_out = B0;
+  // x0 = LU32 \ b
+  convert_z_to_c(ctx->stream, ctx->lc(), B0, X32, xstride * d.batch);
+  lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
+  widen_c_to_z(ctx->stream, ctx->lc(), X32, X, xstride * d.batch);
+  const int64_t ncols = nrhs * d.batch;
+  double* norms;
+  MH_TRY(ws_get_t(ctx, kSlotNorm, (size_t)(2 * ncols + d.batch), &norms));
+  double* anrm_d = norms + 2 * ncols;
+  matrix_inf_norms(ctx->stream, ctx->lc(), d, Adev, anrm_d);
+  double* hn;
+  MH_TRY(pinned_get(ctx, sizeof(double) * (2 * ncols + d.batch) + 64, &hn));
+  const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
+  *converged = false;
+  for (int it = 0; it <= 30; ++it) {
+    residual_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, adjoint);
+    for (int64_t b = 0; b < d.batch; ++b) {
+      inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, R + b * xstride, norms + b * nrhs);
+      inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, X + b * xstride, norms + ncols + b * nrhs);
+    }
+    MH_TRY(check_launch(ctx, "refinement"));
+    MH_CUDA(ctx, cudaMemcpyAsync(hn, norms, sizeof(double) * (2 * ncols + d.batch), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    MH_TRY(sync(ctx, "refinement norms"));
+    bool ok = true;
+    for (int64_t c = 0; c < ncols && ok; ++c) {
+      const double anrm = hn[2 * ncols + c / nrhs];
+      const double rn = hn[c], xn = hn[ncols + c];
+      if (!(rn <= cte * anrm * xn)) ok = false;  // also false for NaN
+    }
+    if (ok) { *converged = true; break; }
+    if (it == 30) break;
+    // c = LU32 \ r ; x += c
+    convert_z_to_c(ctx->stream, ctx->lc(), R, X32, xstride * d.batch);
+    lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
+    ir_update(ctx->stream, ctx->lc(), xstride * d.batch, X, X32);
+  }
+  return MH_OK;
+}
+
+// Reads the per-matrix pivot status of the last factorization; MH_ERR_SINGULAR on a zero pivot.
+int check_pivots(mh_context* ctx, const BatchDesc& d, int64_t first_index) {
+  int32_t* info;
+  MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)d.batch, &info));
+  std::vector<int32_t> hinfo(d.batch);
+  MH_CUDA(ctx, cudaMemcpyAsync(hinfo.data(), info, sizeof(int32_t) * d.batch, cudaMemcpyDeviceToHost, ctx->stream));
+  MH_TRY(sync(ctx, "lu"));
+  for (int64_t b = 0; b < d.batch; ++b)
+    if (hinfo[b] != 0)
+      return fail(ctx, MH_ERR_SINGULAR, "matrix %lld is singular: zero pivot in column %d",
+                  (long long)(first_index + b), hinfo[b]);
+  return MH_OK;
+}
+
 // Factor the batch of matrices `Adev` (overwritten with LU factors in FP64 mode)
 // and solve for X (in/out: rhs on entry).  In mixed mode `Adev` is left intact
-// (used for the FP64 residuals) and an FP32 copy is factored.
+// (used for the FP64 residuals) and an FP32 copy is factored; when refinement does
+// not converge, the FP64 factorization is used instead.
 int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, int64_t nrhs, int64_t xstride,
                int precision, bool adjoint) {
   const int64_t n = d.n;
@@ -281,58 +372,11 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
     lu_solve_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, X, nrhs, xstride, adjoint);
     MH_TRY(check_launch(ctx, "lu solve"));
   } else {
-    const int64_t nn = n * n;
-    float2 *LU32, *X32;
-    MH_TRY(ws_get_t(ctx, kSlotLU32, (size_t)(nn * d.batch), &LU32));
-    MH_TRY(ws_get_t(ctx, kSlotX32, (size_t)(xstride * d.batch), &X32));
-    BatchDesc d32 = d;
-    d32.stride = nn;
-    for (int64_t b = 0; b < d.batch; ++b) convert_z_to_c(ctx->stream, ctx->lc(), Adev + b * d.stride, LU32 + b * nn, nn);
-    lu_factor_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, info);
-    MH_TRY(check_launch(ctx, "lu factor fp32"));
-    double2 *B0, *R, *work;
-    MH_TRY(ws_get_t(ctx, kSlotB, (size_t)(xstride * d.batch), &B0));
-    MH_TRY(ws_get_t(ctx, kSlotR, (size_t)(xstride * d.batch), &R));
-    MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, d.batch), &work));
-    MH_CUDA(ctx, cudaMemcpyAsync(B0, X, sizeof(double2) * xstride * d.batch, cudaMemcpyDeviceToDevice, ctx->stream));
-    // x0 = LU32 \ b
-    convert_z_to_c(ctx->stream, ctx->lc(), B0, X32, xstride * d.batch);
-    lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
-    widen_c_to_z(ctx->stream, ctx->lc(), X32, X, xstride * d.batch);
-    // Refinement with LAPACK zcgesv's stopping rule: accept x when
-    // |b - A x|_inf <= sqrt(n) eps |A|_inf |x|_inf for every column, at most 30 sweeps.
-    const int64_t ncols = nrhs * d.batch;
-    double* norms;
-    MH_TRY(ws_get_t(ctx, kSlotNorm, (size_t)(2 * ncols + d.batch), &norms));
-    double* anrm_d = norms + 2 * ncols;
-    matrix_inf_norms(ctx->stream, ctx->lc(), d, Adev, anrm_d);
-    double* hn;
-    MH_TRY(pinned_get(ctx, sizeof(double) * (2 * ncols + d.batch) + 64, &hn));
-    const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
+    float2* LU32;
+    MH_TRY(factor_mixed(ctx, d, Adev, &LU32));
     bool converged = false;
-    for (int it = 0; it <= 30; ++it) {
-      residual_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, adjoint);
-      for (int64_t b = 0; b < d.batch; ++b) {
-        inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, R + b * xstride, norms + b * nrhs);
-        inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, X + b * xstride, norms + ncols + b * nrhs);
-      }
-      MH_TRY(check_launch(ctx, "refinement"));
-      MH_CUDA(ctx, cudaMemcpyAsync(hn, norms, sizeof(double) * (2 * ncols + d.batch), cudaMemcpyDeviceToHost,
-                                   ctx->stream));
-      MH_TRY(sync(ctx, "refinement norms"));
-      bool ok = true;
-      for (int64_t c = 0; c < ncols && ok; ++c) {
-        const double anrm = hn[2 * ncols + c / nrhs];
-        const double rn = hn[c], xn = hn[ncols + c];
-        if (!(rn <= cte * anrm * xn)) ok = false;  // also false for NaN
-      }
-      if (ok) { converged = true; break; }
-      if (it == 30) break;
-      // c = LU32 \ r ; x += c
-      convert_z_to_c(ctx->stream, ctx->lc(), R, X32, xstride * d.batch);
-      lu_solve_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, X32, nrhs, xstride, adjoint);
-      ir_update(ctx->stream, ctx->lc(), xstride * d.batch, X, X32);
-    }
+    double2* B0 = nullptr;
+    MH_TRY(refine_mixed(ctx, d, Adev, LU32, X, nrhs, xstride, adjoint, &converged, &B0));
     if (!converged) {
       // fall back to the FP64 factorization
       MH_CUDA(ctx, cudaMemcpyAsync(X, B0, sizeof(double2) * xstride * d.batch, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -341,13 +385,7 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
       MH_TRY(check_launch(ctx, "lu fp64 fallback"));
     }
   }
-  std::vector<int32_t> hinfo(d.batch);
-  MH_CUDA(ctx, cudaMemcpyAsync(hinfo.data(), info, sizeof(int32_t) * d.batch, cudaMemcpyDeviceToHost, ctx->stream));
-  MH_TRY(sync(ctx, "lu"));
-  for (int64_t b = 0; b < d.batch; ++b)
-    if (hinfo[b] != 0)
-      return fail(ctx, MH_ERR_SINGULAR, "matrix %lld is singular: zero pivot in column %d", (long long)b, hinfo[b]);
-  return MH_OK;
+  return check_pivots(ctx, d, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1228,7 +1266,7 @@ int mh_batch_release(mh_context* ctx) {
 
 int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
-                      double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                      int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
@@ -1239,6 +1277,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   if (gfs == 0 || (gfs & ~allowed))
     return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint covers the Birk Rankine family and GFWu (got 0x%x)", gfs);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
   for (int64_t q = 0; q < n_obj; ++q)
     if (obj_idx[q] < 0 || obj_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "objective dof index out of range");
@@ -1254,7 +1293,8 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   // factorization and both solves run batched over a chunk, the adjoint kernels per frequency
   size_t free_b = 0, total_b = 0;
   MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-  const size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nh * sizeof(double2) * 6;
+  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nh * sizeof(double2) * 6;
+  if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * nh * sizeof(double2) * 3;
   const size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
   const int64_t chunk = std::min<int64_t>(n_omega, (int64_t)std::max<size_t>(1, budget / per_w));
   const int64_t bstride = n * nh;
@@ -1301,18 +1341,16 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     MH_TRY(check_launch(ctx, "static assembly"));
   }
   AssemblyParams p = make_params(ctx, m, gfs, 1, 1, nullptr);
-  double* hs;
-  MH_TRY(pinned_get(ctx, sizeof(double) * nsmall + sizeof(double2) * (size_t)(nh * nh * n_omega) +
-                             sizeof(int32_t) * (size_t)chunk + 64, &hs));
+  // host staging in pageable memory (the mixed solver owns the pinned block)
+  std::vector<double> hsmall(nsmall, 0.0);
   for (int64_t w = 0; w < n_omega; ++w) {
-    hs[w] = omegas[w];
-    hs[n_omega + w] = omegas[w] * omegas[w] / g;
+    hsmall[w] = omegas[w];
+    hsmall[n_omega + w] = omegas[w] * omegas[w] / g;
   }
-  int32_t* hobj = (int32_t*)(hs + 2 * n_omega);
+  int32_t* hobj = (int32_t*)(hsmall.data() + 2 * n_omega);
   for (int64_t q = 0; q < nh; ++q) hobj[q] = obj_idx[q];
-  double2* hF = (double2*)(hs + nsmall);
-  int32_t* hinfo = (int32_t*)(hF + nh * nh * n_omega);
-  MH_CUDA(ctx, cudaMemcpyAsync(small, hs, sizeof(double) * nsmall, cudaMemcpyHostToDevice, st));
+  MH_CUDA(ctx, cudaMemcpyAsync(small, hsmall.data(), sizeof(double) * nsmall, cudaMemcpyHostToDevice, st));
+  std::vector<double2> hF((size_t)(nh * nh * n_omega));
   const double* om_d = small;
   const double* ks_d = small + n_omega;
   const int32_t* obj_d = (const int32_t*)(small + 2 * n_omega);
@@ -1323,14 +1361,37 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, (int)nw, ks_d + w0, S, D, (int64_t)nn,
                          stk ? 0 : 1);
     launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nh, obj_d, 0, nullptr, B, bstride);
-    zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
-    lu_factor_batched<double>(st, lc, d, D, ipiv, info);
-    lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, bstride, false);       // X = phi
-    launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nh, X, bstride, (int)nh, obj_d, 0, nullptr,
-                  F + w0 * nh * nh, FK);
-    for (int64_t w = 0; w < nw; ++w)
-      launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, omegas[w0 + w], rho, lam + w * bstride);
-    lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, bstride, true);      // mu = D^-H conj(w)
+    // phi = D^-1 S b, forces, and mu = D^-H conj(w) for the force weights w
+    auto forces_and_weights = [&]() {
+      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nh, X, bstride, (int)nh, obj_d, 0, nullptr,
+                    F + w0 * nh * nh, FK);
+      for (int64_t w = 0; w < nw; ++w)
+        launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, omegas[w0 + w], rho, lam + w * bstride);
+    };
+    bool done = false;
+    if (precision == MH_PREC_MIXED) {
+      // FP32 factors, both solves refined to FP64 backward error; any column that does not
+      // converge sends the whole chunk to the FP64 factorization below (D is left intact)
+      float2* LU32;
+      MH_TRY(factor_mixed(ctx, d, D, &LU32));
+      zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
+      bool ok_fwd = false, ok_adj = false;
+      MH_TRY(refine_mixed(ctx, d, D, LU32, X, nh, bstride, false, &ok_fwd, nullptr));
+      if (ok_fwd) {
+        forces_and_weights();
+        MH_TRY(refine_mixed(ctx, d, D, LU32, lam, nh, bstride, true, &ok_adj, nullptr));
+      }
+      done = ok_fwd && ok_adj;
+    }
+    if (!done) {
+      zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
+      lu_factor_batched<double>(st, lc, d, D, ipiv, info);
+      lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, bstride, false);     // X = phi
+      forces_and_weights();
+      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, bstride, true);    // mu = D^-H conj(w)
+    }
+    MH_TRY(check_launch(ctx, "gradient solves"));
+    MH_TRY(check_pivots(ctx, d, w0));
     zgemm_adj_batched(st, lc, d, S, lam, nh, bstride, t, work);                // S^H mu
     launch_conj(st, lc, nw * bstride, t);                                      // t = S^T lam
     launch_conj(st, lc, nw * bstride, lam);                                    // lam = D^-T w
@@ -1344,12 +1405,8 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
                          t + w * bstride, gn, ga, gd);
     }
     MH_TRY(check_launch(ctx, "gradient frequencies"));
-    MH_CUDA(ctx, cudaMemcpyAsync(hinfo, info, sizeof(int32_t) * nw, cudaMemcpyDeviceToHost, st));
-    MH_TRY(sync(ctx, "gradient frequencies"));
-    for (int64_t w = 0; w < nw; ++w)
-      if (hinfo[w]) return fail(ctx, MH_ERR_SINGULAR, "singular D at omega %g", omegas[w0 + w]);
   }
-  MH_CUDA(ctx, cudaMemcpyAsync(hF, F, sizeof(double2) * nh * nh * n_omega, cudaMemcpyDeviceToHost, st));
+  MH_CUDA(ctx, cudaMemcpyAsync(hF.data(), F, sizeof(double2) * nh * nh * n_omega, cudaMemcpyDeviceToHost, st));
   if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
   MH_TRY(check_launch(ctx, "static adjoint"));
   MH_TRY(sync(ctx, "forces"));

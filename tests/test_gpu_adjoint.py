@@ -145,3 +145,14 @@ def test_panel_terms_match_finite_differences(mh, ctx, wu):
         if not abs(ad - fd) <= RTOL * max(abs(fd), 1e-6 * abs(J0)):
             bad[name] = (ad, fd)
     assert not bad, bad
+
+
+def test_mixed_precision_gradient_matches_fp64(mh, ctx):
+    """FP32 factors + refinement of both solves: J and the gradient agree with FP64."""
+    m1, m2 = _geometry(mh)
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave", "Pitch"])
+    obj = ["c1__Heave", "c2__Pitch"]
+    J64, g64 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(), ctx=ctx, rho=1025.0)
+    J32, g32 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(precision="mixed"), ctx=ctx, rho=1025.0)
+    assert abs(J32 - J64) <= 1e-12 * abs(J64)
+    assert np.abs(g32 - g64).max() <= 1e-10 * np.abs(g64).max()
