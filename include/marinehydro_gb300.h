@@ -60,6 +60,9 @@ typedef enum {
 #define MH_GF_DELHOMMEAU_RANKINE_REFLECTED  16u  /* its image */
 #define MH_GF_WU                            32u  /* GFWu (wu.jl) */
 #define MH_GF_EXACT_DELHOMMEAU              64u  /* ExactGuevelDelhommeau (exact_Guevel_Delhommeau.jl) */
+#define MH_GF_SURROGATE                    128u  /* learned approximation of ExactGuevelDelhommeau
+                                                    (mh_surrogate_train / mh_surrogate_set); no
+                                                    counterpart in the reference */
 #define MH_GF_DEFAULT_WU  (MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_WU)
 #define MH_GF_DEFAULT_EGD (MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_EXACT_DELHOMMEAU)
 
@@ -228,6 +231,39 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const dou
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem);
+
+/* ---- learned wave-term surrogate (no counterpart in the reference) --------- */
+/* A 2 -> 64 -> 64 -> 64 -> 6 tanh network with BF16 weights and FP32 arithmetic that
+   corrects the Wu fits (wu.jl:28-37) toward the exact Guevel-Delhommeau wave term
+   (exact_Guevel_Delhommeau.jl:15-46).  Inputs u = log10(r)/3, v = z/25 + 1 in the
+   reduced coordinates (r, z) = (k |x_h - xi_h|, k (z + zeta)); outputs (1 + d)^2 times
+   the real and imaginary parts of G_exact - G_Wu, its r-derivative and its
+   z-derivative, d = sqrt(r^2 + z^2).  Used inside r in [1e-3, 1e3], z in [-50, 0];
+   assembly with MH_GF_SURROGATE recomputes every pair outside that box with the
+   exact kernel.  Parameters are packed as W1[64][2], b1, W2[64][64], b2, W3[64][64],
+   b3, W4[6][64], b4 (mh_surrogate_param_count() floats). */
+int mh_surrogate_param_count(void);
+/* Trains on the device: n_samples points drawn with `seed` (r log-uniform, z uniform
+   in the box), targets from the exact kernel at the context's quadrature
+   tolerances; Adam with cosine-decayed learning rate from lr, `epochs` passes in
+   batches of `batch`, BF16-rounded forward weights.  Installs the result on the
+   context and writes it to params_out (may be NULL).  report (may be NULL), 10
+   doubles: final mean squared error; RMS and max relative error of G over held-out
+   points for the surrogate, then for the Wu fits; max relative error of dG/dr,
+   surrogate then Wu; seconds of sample generation; seconds of training; number of
+   held-out points. */
+int mh_surrogate_train(mh_context* ctx, int64_t n_samples, uint64_t seed, int epochs, int batch, double lr,
+                       float* params_out, double* report);
+/* Installs parameters (rounded to BF16) on the context. */
+int mh_surrogate_set(mh_context* ctx, const float* params);
+/* Surrogate GF, dGF/dr, dGF/dz at m points (3 complex per point, the layout of
+   mh_wu_wave_terms); points outside the training box take the exact kernel. */
+int mh_surrogate_wave_terms(mh_context* ctx, int64_t m, const double* r, const double* z, double* out, int mem);
+/* Mean squared error of the network (parameters rounded to BF16) on m samples
+   (inputs m x 2 as (u, v), targets m x 6) and its gradient with respect to the
+   parameters, computed by the training kernels.  Host buffers, m <= 2^20. */
+int mh_surrogate_loss_grad(mh_context* ctx, const float* params, int64_t m, const float* inputs, const float* targets,
+                           float* grad, double* loss);
 
 /* ---- wave-term evaluators (kernel-level parity entry points) ------------- */
 /* _wu_wave_term_and_derivs(hh, vv) (wu.jl:28-37) for m points: out 3 complex

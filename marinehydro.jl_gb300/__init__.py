@@ -10,12 +10,12 @@ from ._lib import (Context, MarineHydroError, default_context, load as load_libr
 from .api import (airy_bc, airy_pressure, assemble_matrices, assemble_matrix_wu, batch_hydrodynamic_coefficients,  # noqa
                   calculate_radiation_forces,
                   compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
-                  gpu_linsolve, hydro_gradient, hydrodynamic_coefficients, integrate_pressure, linsolve, linsolve_adjoint,
+                  gpu_linsolve, hydro_gradient, hydrodynamic_coefficients, set_surrogate, surrogate_wave_terms, train_surrogate, integrate_pressure, linsolve, linsolve_adjoint,
                   problems_from_data, radiation_bc, solve, solve_linear, solve_problem)
 from .bodies import FloatingBody, combine_floatingbodies, rotational_dofs, translational_dofs  # noqa: F401
 from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineReflected, DirectBEM,  # noqa: F401
                            ExactGuevelDelhommeau, GFWu, GreensFunction, IndirectBEM, Rankine, RankineReflected,
-                           RankineReflectedNegative, bem_formulation, default_greens_functions, gf_flags, is_direct,
+                           RankineReflectedNegative, SurrogateDelhommeau, bem_formulation, default_greens_functions, gf_flags, is_direct,
                            partition_greens_functions)
 from .meshes import (Mesh, StaticArraysMesh, barge_mesh, combine_meshes, config1_hemisphere,  # noqa: F401
                      config2_cylinder, face_fields, face_fields_jacobian, hemisphere_mesh, random_body, smesh, tiny_static_mesh, vertical_cylinder_mesh)

@@ -28,6 +28,7 @@ GF_DELHOMMEAU_RANKINE = 8
 GF_DELHOMMEAU_RANKINE_REFLECTED = 16
 GF_WU = 32
 GF_EXACT_DELHOMMEAU = 64
+GF_SURROGATE = 128
 
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = (
@@ -37,7 +38,8 @@ EXPORTS = (
     "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
-    "mh_hydro_gradient",
+    "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
+    "mh_surrogate_wave_terms", "mh_surrogate_loss_grad",
 )
 
 
@@ -99,6 +101,11 @@ def load(path: str | None = None):
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
         L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, I, vp, vp, vp, vp, vp, vp, I]
+        L.mh_surrogate_param_count.restype = I
+        L.mh_surrogate_train.argtypes = [vp, i64, ctypes.c_uint64, I, I, D, vp, vp]
+        L.mh_surrogate_set.argtypes = [vp, vp]
+        L.mh_surrogate_wave_terms.argtypes = [vp, i64, vp, vp, vp, I]
+        L.mh_surrogate_loss_grad.argtypes = [vp, vp, i64, vp, vp, vp, ctypes.POINTER(D)]
         L.mh_assemble_matrices_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, D, u32, I, I, vp, vp, vp]
         for name in EXPORTS:
             getattr(L, name)  # AttributeError if the build lacks a declared entry point
@@ -173,6 +180,36 @@ class Context:
             nm = names.raw[32 * i:32 * (i + 1)].split(b"\0", 1)[0].decode()
             out[nm] = (ms[i], int(cnt[i]))
         return out
+
+    def surrogate_train(self, n_samples=10_000_000, seed=2026, epochs=8, batch=8192, lr=3e-3):
+        """mh_surrogate_train: trains the learned wave-term surrogate on this context's device
+        and installs it.  Returns (params float32 array, report dict)."""
+        n = int(self._L.mh_surrogate_param_count())
+        params = np.empty(n, dtype=np.float32)
+        rep = np.zeros(10)
+        self.check(self._L.mh_surrogate_train(self._h, int(n_samples), int(seed), int(epochs), int(batch), float(lr),
+                                               params.ctypes.data, rep.ctypes.data), "mh_surrogate_train")
+        keys = ("final_mse", "rms_rel_err_G", "max_rel_err_G", "wu_rms_rel_err_G", "wu_max_rel_err_G",
+                "max_rel_err_dGdr", "wu_max_rel_err_dGdr", "sample_seconds", "train_seconds", "validation_points")
+        return params, dict(zip(keys, rep.tolist()))
+
+    def surrogate_set(self, params):
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).ravel())
+        n = int(self._L.mh_surrogate_param_count())
+        if p.size != n:
+            raise ValueError(f"the surrogate takes {n} parameters, got {p.size}")
+        self.check(self._L.mh_surrogate_set(self._h, p.ctypes.data), "mh_surrogate_set")
+
+    def surrogate_loss_grad(self, params, inputs, targets):
+        """Loss and gradient from the training kernels (for checking them)."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).ravel())
+        x = np.ascontiguousarray(np.asarray(inputs, dtype=np.float32).reshape(-1, 2))
+        y = np.ascontiguousarray(np.asarray(targets, dtype=np.float32).reshape(-1, 6))
+        g = np.empty_like(p)
+        loss = ctypes.c_double()
+        self.check(self._L.mh_surrogate_loss_grad(self._h, p.ctypes.data, x.shape[0], x.ctypes.data, y.ctypes.data,
+                                                  g.ctypes.data, ctypes.byref(loss)), "mh_surrogate_loss_grad")
+        return loss.value, g
 
     def probe_fma_peaks(self):
         """(fp64, fp32) FMA throughput in TFLOP/s measured on this device."""

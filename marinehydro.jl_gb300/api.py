@@ -332,6 +332,30 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     return J, grad
 
 
+def train_surrogate(n_samples=10_000_000, seed=2026, epochs=8, batch=8192, lr=3e-3, ctx=None):
+    """Train the learned Delhommeau wave-term surrogate on the device and install it on
+    the context (mh_surrogate_train).  Returns (params, report)."""
+    return _ctx(ctx).surrogate_train(n_samples, seed, epochs, batch, lr)
+
+
+def set_surrogate(params, ctx=None):
+    """Install surrogate parameters (as returned by train_surrogate) on the context."""
+    _ctx(ctx).surrogate_set(params)
+
+
+def surrogate_wave_terms(r, z, ctx=None):
+    """Surrogate (GF, dGF/dr, dGF/dz) at reduced coordinates (r, z): (m, 3) complex."""
+    c = _ctx(ctx)
+    r = np.ascontiguousarray(np.asarray(r, dtype=np.float64).ravel())
+    z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).ravel())
+    if r.shape != z.shape:
+        raise ValueError("r and z must have the same length")
+    out = np.empty((r.size, 3), dtype=np.complex128)
+    c.check(c._L.mh_surrogate_wave_terms(c.handle, r.size, r.ctypes.data, z.ctypes.data, out.ctypes.data,
+                                         _lib.MH_MEM_HOST), "surrogate wave terms")
+    return out
+
+
 def compute_hydrodynamic_coefficients(parameters, body, formulation=None, direct=True, gf="Wu",
                                       greens_functions=None, ctx=None):
     return hydrodynamic_coefficients(body, parameters, bem_formulation(formulation, direct, gf, greens_functions),

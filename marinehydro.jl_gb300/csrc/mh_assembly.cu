@@ -17,6 +17,7 @@
 
 #include "mh_greens.cuh"
 #include "mh_internal.cuh"
+#include "mh_mlp.cuh"
 
 namespace mh {
 
@@ -209,19 +210,37 @@ struct WaveTerms {
   double2 gz;      // vertical gradient component, without area
 };
 
+// dynamic shared memory of the surrogate mode: the packed MLP parameters
+extern __shared__ float4 mh_wave_dyn_smem[];
+
+// WMODE bits: 1 = Wu, 2 = exact Delhommeau, 4 = learned surrogate (Wu + MLP correction).
+// Returns true when the pair lies outside the surrogate's training box (the terms
+// then hold the plain Wu values and the caller queues the pair for the exact kernel).
 template <bool DIRECT, int WMODE>
-__device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
+__device__ __forceinline__ bool wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
                                            WaveTerms& w) {
   w.I = make_double2(0.0, 0.0);
   w.gh[0] = w.gh[1] = w.gz = w.I;
   // (i, j) orientation: gradient w.r.t. the source (direct) or the field point (indirect)
   const double dx1 = DIRECT ? cj[0] - ci[0] : ci[0] - cj[0];
   const double dx2 = DIRECT ? cj[1] - ci[1] : ci[1] - cj[1];
-  if (WMODE & 1) {  // _wu_sd (wu.jl:112-127)
+  bool fallback = false;
+  if (WMODE & 5) {  // _wu_sd (wu.jl:112-127); the surrogate adds its learned correction
     double hh, vv;
     reduced_coords(ci, cj, k, hh, vv);
     double2 GF, Gh, Gv;
     wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+    if (WMODE & 4) {
+      if (surrogate_in_box(hh, vv)) {
+        double2 dG, dGr, dGz;
+        surrogate_correction(reinterpret_cast<const float*>(mh_wave_dyn_smem), hh, vv, dG, dGr, dGz);
+        GF = zadd(GF, dG);
+        Gh = zadd(Gh, dGr);
+        Gv = zadd(Gv, dGz);
+      } else {
+        fallback = true;
+      }
+    }
     double dr1 = 0.0, dr2 = 0.0;
     if (fabs(hh) > 1e-6) {
       dr1 = k * k / hh * dx1;
@@ -248,6 +267,7 @@ __device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double
     w.gh[1] = zadd(w.gh[1], make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y)));
     w.gz = zadd(w.gz, make_double2(k * (k * dGdz.x), k * (k * dGdz.y)));
   }
+  return fallback;
 }
 
 // S and D entries (before adding the static part) from the wave terms; `sgn` = -1
@@ -263,7 +283,44 @@ __device__ __forceinline__ void wave_entry(const WaveTerms& w, double sgn, doubl
   dv = make_double2(kMinusInv4Pi * d.x, kMinusInv4Pi * d.y);
 }
 
-template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both
+// writes the (i, j) entry and, for i != j, the mirrored (j, i) entry of one unordered pair
+template <bool DIRECT>
+__device__ __forceinline__ void store_pair(const AssemblyParams& p, const WaveTerms& w, int64_t i, int64_t j,
+                                           const double ni[3], double ai, const PanelRec& Pj,
+                                           const double* __restrict__ SR, const double* __restrict__ DR,
+                                           double2* __restrict__ Sb, double2* __restrict__ Db, int wave_identity) {
+  const int64_t n = p.n;
+  // (i, j): source j
+  double nv[3];
+  pick_normal<DIRECT>(p, Pj, ni, nv);
+  double2 sv, dv;
+  wave_entry(w, 1.0, Pj.area, nv, sv, dv);
+  if (wave_identity && i == j) dv.x += identity_jump(p, ni);
+  const int64_t idx = i + j * n;
+  if (SR) {
+    sv.x = SR[idx] + sv.x;
+    dv.x = DR[idx] + dv.x;
+  }
+  Sb[idx] = sv;
+  Db[idx] = dv;
+  if (i == j) return;
+  // (j, i): source i, field j -- normal of the source (direct) / field (indirect) swaps
+  double nm[3];
+  if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
+  else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
+  else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
+  double2 sm, dm;
+  wave_entry(w, -1.0, ai, nm, sm, dm);
+  const int64_t mdx = j + i * n;
+  if (SR) {
+    sm.x = SR[mdx] + sm.x;
+    dm.x = DR[mdx] + dm.x;
+  }
+  Sb[mdx] = sm;
+  Db[mdx] = dm;
+}
+
+template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both, 4 = surrogate
 __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, const double* __restrict__ SR,
                                                            const double* __restrict__ DR,
                                                            const double* __restrict__ ks, double2* __restrict__ S,
@@ -279,6 +336,10 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
   double2* Sb = S + blockIdx.z * sstride;
   double2* Db = D + blockIdx.z * sstride;
   stage_panels(sp, p.P, j0, n);
+  if (WMODE & 4) {
+    const float4* src = reinterpret_cast<const float4*>(p.mlp);
+    for (int q = threadIdx.x; q < kMlpParamsPadded / 4; q += blockDim.x) mh_wave_dyn_smem[q] = __ldg(src + q);
+  }
   __syncthreads();
   if (i >= n) return;
   double ci[3], ni[3];
@@ -290,35 +351,38 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
     if (i > j) continue;
     const PanelRec& Pj = sp[jj];
     WaveTerms w;
-    wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
-    // (i, j): source j
-    double nv[3];
-    pick_normal<DIRECT>(p, Pj, ni, nv);
-    double2 sv, dv;
-    wave_entry(w, 1.0, Pj.area, nv, sv, dv);
-    if (wave_identity && i == j) dv.x += identity_jump(p, ni);
-    const int64_t idx = i + j * n;
-    if (SR) {
-      sv.x = SR[idx] + sv.x;
-      dv.x = DR[idx] + dv.x;
+    const bool fb = wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
+    if ((WMODE & 4) && (fb || i == j)) {
+      // outside the training box, and the self pairs: queued for the exact kernel (the
+      // entries written here are replaced)
+      const unsigned long long slot = atomicAdd(p.fb_state, 1ull);
+      if ((int64_t)slot < p.fb_cap) p.fb_list[slot] = make_int4((int)i, (int)j, (int)blockIdx.z, 0);
     }
-    Sb[idx] = sv;
-    Db[idx] = dv;
-    if (i == j) continue;
-    // (j, i): source i, field j -- normal of the source (direct) / field (indirect) swaps
-    double nm[3];
-    if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
-    else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
-    else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
-    double2 sm, dm;
-    wave_entry(w, -1.0, ai, nm, sm, dm);
-    const int64_t mdx = j + i * n;
-    if (SR) {
-      sm.x = SR[mdx] + sm.x;
-      dm.x = DR[mdx] + dm.x;
-    }
-    Sb[mdx] = sm;
-    Db[mdx] = dm;
+    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
+  }
+}
+
+// Exact Delhommeau terms for the pairs the surrogate queued (one thread per pair).
+template <bool DIRECT>
+__global__ void __launch_bounds__(64) surrogate_fallback_kernel(AssemblyParams p, const double* __restrict__ SR,
+                                                                const double* __restrict__ DR,
+                                                                const double* __restrict__ ks,
+                                                                double2* __restrict__ S, double2* __restrict__ D,
+                                                                int64_t sstride, int wave_identity) {
+  const unsigned long long queued = p.fb_state[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (int64_t)queued > p.fb_cap) p.fb_state[1] = 1ull;  // sticky overflow
+  const int64_t count = (int64_t)queued < p.fb_cap ? (int64_t)queued : p.fb_cap;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+    const int4 e = p.fb_list[q];
+    const int64_t i = e.x, j = e.y;
+    const double k = ks[e.z];
+    double ci[3], ni[3];
+    for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
+    const double ai = p.P[i].area;
+    const PanelRec& Pj = p.P[j];
+    WaveTerms w;
+    wave_terms<DIRECT, 2>(p, ci, Pj.c, k, w);
+    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, S + e.z * sstride, D + e.z * sstride, wave_identity);
   }
 }
 
@@ -377,7 +441,7 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
                           const double* DR, int nk, const double* ks_dev, double2* S, double2* D, int64_t sstride,
                           int wave_identity) {
   if (p.n <= 0 || nk <= 0) return;
-  const uint32_t wv = p.gfs & (MH_GF_WU | MH_GF_EXACT_DELHOMMEAU);
+  const uint32_t wv = p.gfs & (MH_GF_WU | MH_GF_EXACT_DELHOMMEAU | MH_GF_SURROGATE);
   if (!wv) {
     // static only: widen to complex for every requested wavenumber
     int64_t count = p.n * p.n;
@@ -390,6 +454,21 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
   }
   dim3 grid((unsigned)((p.n + kRowsPerCta - 1) / kRowsPerCta), (unsigned)((p.n + kColsPerCta - 1) / kColsPerCta),
             (unsigned)nk);
+  if (wv & MH_GF_SURROGATE) {
+    // Wu + learned correction; pairs outside the training box are queued and then
+    // recomputed by the exact kernel (the caller validates that no other wave kind is set)
+    const size_t smem = sizeof(float) * kMlpParamsPadded;
+    lc.pre(st);
+    cudaMemsetAsync(p.fb_state, 0, sizeof(unsigned long long), st);
+    if (p.direct) wave_kernel<true, 4><<<grid, kRowsPerCta, smem, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    else wave_kernel<false, 4><<<grid, kRowsPerCta, smem, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    lc.post(st, "assemble_wave_surrogate");
+    lc.pre(st);
+    if (p.direct) surrogate_fallback_kernel<true><<<4 * 152, 64, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    else surrogate_fallback_kernel<false><<<4 * 152, 64, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    lc.post(st, "assemble_wave_fallback");
+    return;
+  }
   const int mode = (wv == MH_GF_WU) ? 1 : (wv == MH_GF_EXACT_DELHOMMEAU ? 2 : 3);
   lc.pre(st);
 #define MH_WAVE(DIR, MODE) wave_kernel<DIR, MODE><<<grid, kRowsPerCta, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity)

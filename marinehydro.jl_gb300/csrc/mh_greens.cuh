@@ -390,39 +390,70 @@ __device__ inline void gk15(double a, double b, double r, double z, double2& val
   err = hypot(dif.x * h, dif.y * h);
 }
 
-constexpr int kGKMaxSeg = 64;
+constexpr int kGKStack = 48;        // depth-first refinement stack (segments)
+constexpr int kGKMaxEvals = 8192;   // GK15 evaluations per integral, a hard bound
 
-// 4 * adaptive GK(7,15) over [0, pi/2] (exact_Guevel_Delhommeau.jl:8-13, 25, 45):
-// bisection of the worst segment until total error <= max(atol, rtol |I|)
+// 4 * adaptive GK(7,15) over [0, pi/2] (exact_Guevel_Delhommeau.jl:8-13, 25, 45) to a
+// total error estimate <= max(atol, rtol |I|).  The phase r cos(theta) of the integrand
+// turns through r radians over the interval, so the interval is first cut into
+// ceil(r / 4) equal segments (at most 1024, about 2/3 of an oscillation each); each is
+// then refined depth-first by bisection until its GK error estimate is below its
+// share of the tolerance, tol * length / (pi/2), with tol from a first pass over the
+// initial segments.  The per-thread state is a short stack, so large r costs time,
+// not memory.
 template <bool DR>
 __device__ inline double2 egd_adaptive(double r, double z, double rtol, double atol) {
-  double sa[kGKMaxSeg], sb[kGKMaxSeg], serr[kGKMaxSeg];
-  double2 sval[kGKMaxSeg];
-  int ns = 1;
-  sa[0] = 0.0;
-  sb[0] = kPi / 2;
-  gk15<DR>(sa[0], sb[0], r, z, sval[0], serr[0]);
-  double2 tot = sval[0];
-  double E = serr[0];
-  while (E > fmax(atol, rtol * hypot(tot.x, tot.y)) && ns < kGKMaxSeg) {
-    int w = 0;
-    for (int i = 1; i < ns; ++i) if (serr[i] > serr[w]) w = i;
-    double a = sa[w], b = sb[w], m = 0.5 * (a + b);
-    double2 oldv = sval[w];
-    double olde = serr[w];
-    double2 v1, v2;
-    double e1, e2;
-    gk15<DR>(a, m, r, z, v1, e1);
-    gk15<DR>(m, b, r, z, v2, e2);
-    sa[w] = a; sb[w] = m; sval[w] = v1; serr[w] = e1;
-    sa[ns] = m; sb[ns] = b; sval[ns] = v2; serr[ns] = e2;
-    ++ns;
-    tot = zadd(tot, zsub(zadd(v1, v2), oldv));
-    E += (e1 + e2) - olde;
+  const double L = kPi / 2;
+  const int m0 = (int)fmin(1024.0, fmax(1.0, ceil(r / 4.0)));
+  const double h0 = L / m0;
+  // first pass: the integral and the tolerance it implies
+  double2 coarse = make_double2(0.0, 0.0);
+  double v0e = 0.0;
+  double2 v0 = make_double2(0.0, 0.0);
+  for (int s = 0; s < m0; ++s) {
+    double2 v;
+    double e;
+    gk15<DR>(s * h0, s == m0 - 1 ? L : (s + 1) * h0, r, z, v, e);
+    coarse = zadd(coarse, v);
+    if (s == 0) { v0 = v; v0e = e; }
   }
-  double2 s = make_double2(0.0, 0.0);
-  for (int i = 0; i < ns; ++i) s = zadd(s, sval[i]);
-  return zscale(4.0, s);
+  int evals = m0;
+  const double tol = fmax(atol, rtol * hypot(coarse.x, coarse.y));
+  double2 total = make_double2(0.0, 0.0);
+  double sa[kGKStack], sb[kGKStack], se[kGKStack];
+  double2 sv[kGKStack];
+  for (int s = 0; s < m0; ++s) {
+    int top = 0;
+    sa[0] = s * h0;
+    sb[0] = s == m0 - 1 ? L : (s + 1) * h0;
+    if (m0 == 1) {
+      sv[0] = v0;
+      se[0] = v0e;
+    } else {
+      gk15<DR>(sa[0], sb[0], r, z, sv[0], se[0]);
+      ++evals;
+    }
+    top = 1;
+    while (top > 0) {
+      --top;
+      const double a = sa[top], b = sb[top];
+      const double2 v = sv[top];
+      const double e = se[top];
+      if (e <= tol * (b - a) / L || top + 2 > kGKStack || evals + 2 > kGKMaxEvals) {
+        total = zadd(total, v);
+        continue;
+      }
+      const double mid = 0.5 * (a + b);
+      double2 v1, v2;
+      double e1, e2;
+      gk15<DR>(a, mid, r, z, v1, e1);
+      gk15<DR>(mid, b, r, z, v2, e2);
+      evals += 2;
+      sa[top] = mid; sb[top] = b; sv[top] = v2; se[top] = e2; ++top;
+      sa[top] = a; sb[top] = mid; sv[top] = v1; se[top] = e1; ++top;
+    }
+  }
+  return zscale(4.0, total);
 }
 
 // both_greens_and_gradient_greens(::ExactGuevelDelhommeau) with

@@ -76,6 +76,12 @@ struct AssemblyParams {
   double fixed[3];
   double k;
   double quad_rtol, quad_atol;
+  // learned surrogate (MH_GF_SURROGATE): packed BF16-rounded MLP parameters, and the list
+  // of pairs outside its training box that the exact kernel recomputes
+  const float* mlp;
+  int4* fb_list;                 // (i, j, wavenumber index, 0), i <= j
+  unsigned long long* fb_state;  // [0] entries appended by the current launch, [1] sticky overflow
+  int64_t fb_cap;
 };
 
 // Static (wavenumber-independent) part into real n x n arrays SR, DR (identity included when asked).
@@ -85,6 +91,26 @@ void launch_assemble_static(cudaStream_t st, LaunchCounter lc, const AssemblyPar
 void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
                           const double* DR, int nk, const double* ks_dev, double2* S, double2* D, int64_t sstride,
                           int wave_identity);
+// learned surrogate (mh_surrogate.cu)
+void launch_surrogate_points(cudaStream_t st, LaunchCounter lc, const float* mlp, int64_t m, const double* r,
+                             const double* z, double rtol, double atol, double2* out);
+// training samples [offset, offset + count) of the M samples of `seed`: inputs X (u, v),
+// scaled targets Y8 (8 floats per sample, 6 used), optionally (r, z) in FP64 into R2
+void launch_surrogate_samples(cudaStream_t st, LaunchCounter lc, uint64_t seed, int64_t M, int64_t offset,
+                              int64_t count, double rtol, double atol, float2* X, float* Y8, double* R2);
+// floats of the per-step activation buffer for a batch of B samples
+int64_t mlp_act_floats(int B);
+// one Adam step (t >= 1) over samples ((base + b) mod M) * prime mod M, b < B; the mean
+// squared error of the batch is added to *loss
+void launch_mlp_train_step(cudaStream_t st, LaunchCounter lc, float* theta, float* qparams, float* grad, float* m1,
+                           float* m2, const float2* X, const float* Y8, int64_t M, int64_t base, int64_t prime, int B,
+                           float* acts, double* loss, float lr, int t);
+// mean squared error into *loss and its gradient into grad (accumulated) for the BF16
+// parameters qparams over samples ((base + b) mod M) * prime mod M, b < B
+void launch_mlp_loss_grad(cudaStream_t st, LaunchCounter lc, const float* qparams, const float2* X, const float* Y8,
+                          int64_t M, int64_t base, int64_t prime, int B, float* acts, double* loss, float* grad);
+// out = BF16-rounded copy of the packed parameters (padding zeroed)
+void launch_round_bf16(cudaStream_t st, LaunchCounter lc, const float* in, float* out);
 // point evaluators
 void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out);
 void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* r, const double* z, double rtol,

@@ -1,0 +1,126 @@
+// mh_mlp.cuh -- the learned Delhommeau wave-term surrogate: a 2 -> 64 -> 64 -> 64 -> 6
+// multilayer perceptron with tanh hidden units, BF16 weights (held as BF16-rounded
+// FP32 values) and FP32 arithmetic.  No counterpart in the reference.
+//
+// What it learns.  The exact Guevel-Delhommeau wave term G(r, z) and dG/dr
+// (exact_Guevel_Delhommeau.jl:15-46) differ from the Wu fits (wu.jl:28-37) by a
+// smooth remainder: the imaginary parts agree exactly (both are 2 pi e^z J0(r) and
+// -2 pi e^z J1(r)), and dG/dz - G = 2/sqrt(r^2 + z^2) holds for both.  The network
+// therefore predicts the remainder
+//   y = [s Re dG, s Im dG, s_r Re dGr, s_r Im dGr, s Re dGz, s Im dGz],
+//   dG = G_exact - G_Wu,  dGr = dG/dr_exact - dG/dr_Wu,  dGz = dG/dz_exact - dG/dz_Wu,
+//   s = (1 + d)^2,  s_r = (1 + d)^2 (1 + r) / r,  d = sqrt(r^2 + z^2),
+// from the inputs u = log10(r) / 3 and v = z / 25 + 1 (both in [-1, 1] over the
+// training box r in [1e-3, 1e3], z in [-50, 0]).  The scales make every target O(0.1):
+// the remainder decays like 1/d^2, and dGr vanishes like r at r = 0, where the
+// assembly divides it by r (the horizontal gradient k^2/r dx dG/dr).
+// The surrogate applies outputs 0 and 2: G = G_Wu + y0 / s, dG/dr = dG/dr_Wu + y2 / s_r
+// and dG/dz = G + 2/d as for both kernels.  Outputs 1, 3 and 5 (imaginary parts, zero
+// for the exact remainder) and 4 (equal to output 0) are trained as consistency checks
+// and not applied.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mh {
+
+constexpr int kMlpIn = 2, kMlpH = 64, kMlpOut = 6;
+// packed parameter layout (row-major weights: W[out][in])
+constexpr int kMlpW1 = 0;                          // 64 x 2
+constexpr int kMlpB1 = kMlpW1 + kMlpH * kMlpIn;    // 64
+constexpr int kMlpW2 = kMlpB1 + kMlpH;             // 64 x 64
+constexpr int kMlpB2 = kMlpW2 + kMlpH * kMlpH;     // 64
+constexpr int kMlpW3 = kMlpB2 + kMlpH;             // 64 x 64
+constexpr int kMlpB3 = kMlpW3 + kMlpH * kMlpH;     // 64
+constexpr int kMlpW4 = kMlpB3 + kMlpH;             // 6 x 64
+constexpr int kMlpB4 = kMlpW4 + kMlpOut * kMlpH;   // 6
+constexpr int kMlpParams = kMlpB4 + kMlpOut;       // 8902
+constexpr int kMlpParamsPadded = (kMlpParams + 3) & ~3;
+
+// training box of the surrogate; pairs outside it take the exact kernel
+constexpr double kSurrRMin = 1e-3, kSurrRMax = 1e3, kSurrZMin = -50.0;
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ void mlp_inputs(double r, double z, float& u, float& v) {
+  u = (float)(log10(r) * (1.0 / 3.0));
+  v = (float)(z * (1.0 / 25.0) + 1.0);
+}
+
+// one dense tanh layer of 64 outputs from `nin` inputs held in registers
+template <int NIN>
+__device__ __forceinline__ void mlp_layer_tanh(const float* __restrict__ W, const float* __restrict__ b,
+                                               const float (&x)[NIN], float (&y)[kMlpH]) {
+#pragma unroll
+  for (int j = 0; j < kMlpH; ++j) {
+    float acc = b[j];
+    if constexpr (NIN % 4 == 0) {
+      const float4* w4 = reinterpret_cast<const float4*>(W + j * NIN);
+#pragma unroll
+      for (int i = 0; i < NIN / 4; ++i) {
+        const float4 w = w4[i];
+        acc = fmaf(w.x, x[4 * i], acc);
+        acc = fmaf(w.y, x[4 * i + 1], acc);
+        acc = fmaf(w.z, x[4 * i + 2], acc);
+        acc = fmaf(w.w, x[4 * i + 3], acc);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) acc = fmaf(W[j * NIN + i], x[i], acc);
+    }
+    y[j] = tanh_fast(acc);
+  }
+}
+
+// forward pass; `P` points at the packed parameters (shared or global memory,
+// 16-byte aligned)
+__device__ __forceinline__ void mlp_forward(const float* __restrict__ P, float u, float v, float (&out)[kMlpOut]) {
+  const float x[kMlpIn] = {u, v};
+  float h1[kMlpH], h2[kMlpH];
+  mlp_layer_tanh<kMlpIn>(P + kMlpW1, P + kMlpB1, x, h1);
+  mlp_layer_tanh<kMlpH>(P + kMlpW2, P + kMlpB2, h1, h2);
+  mlp_layer_tanh<kMlpH>(P + kMlpW3, P + kMlpB3, h2, h1);
+  const float4* w4 = reinterpret_cast<const float4*>(P + kMlpW4);
+#pragma unroll
+  for (int q = 0; q < kMlpOut; ++q) {
+    float acc = P[kMlpB4 + q];
+#pragma unroll
+    for (int i = 0; i < kMlpH / 4; ++i) {
+      const float4 w = w4[q * (kMlpH / 4) + i];
+      acc = fmaf(w.x, h1[4 * i], acc);
+      acc = fmaf(w.y, h1[4 * i + 1], acc);
+      acc = fmaf(w.z, h1[4 * i + 2], acc);
+      acc = fmaf(w.w, h1[4 * i + 3], acc);
+    }
+    out[q] = acc;
+  }
+}
+
+// the surrogate's correction to the Wu terms at (r, z): dGF, dGh, dGv (complex) to add
+// to wu_wave_term_and_derivs' GF, Gh, Gv.  Below r = 1e-3 the network is read at
+// r = 1e-3: the remainder is even in r (its r-derivative vanishes like r), so its
+// value there differs from the r -> 0 limit by O(1e-6) of its size, and the dG/dr
+// correction keeps its factor r.
+__device__ __forceinline__ void surrogate_correction(const float* __restrict__ P, double r, double z, double2& dG,
+                                                     double2& dGr, double2& dGz) {
+  float u, v, y[kMlpOut];
+  mlp_inputs(fmax(r, kSurrRMin), z, u, v);
+  mlp_forward(P, u, v, y);
+  const double d = sqrt(r * r + z * z);
+  const double inv = 1.0 / ((1.0 + d) * (1.0 + d));
+  dG = make_double2(y[0] * inv, 0.0);
+  dGr = make_double2(y[2] * inv * (r / (1.0 + r)), 0.0);
+  dGz = dG;
+}
+
+// where the surrogate is used: r up to the top of the training box (below it, see
+// surrogate_correction) and z within it; elsewhere the exact kernel
+__device__ __forceinline__ bool surrogate_in_box(double r, double z) {
+  return r <= kSurrRMax && z >= kSurrZMin && z <= 0.0;
+}
+
+}  // namespace mh

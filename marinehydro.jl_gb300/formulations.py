@@ -64,6 +64,14 @@ class ExactGuevelDelhommeau(GreensFunction):
     flag = _lib.GF_EXACT_DELHOMMEAU
 
 
+class SurrogateDelhommeau(GreensFunction):
+    """Learned approximation of ExactGuevelDelhommeau: the Wu fits plus a BF16 MLP
+    correction, exact kernel outside the training box (no counterpart in the
+    reference; train with ``train_surrogate`` or install parameters with
+    ``set_surrogate`` first)."""
+    flag = _lib.GF_SURROGATE
+
+
 def partition_greens_functions(gfs):
     """partition_greens_functions (abstract_greens_function.jl:8-22)."""
     gfs = tuple(gfs)
@@ -91,6 +99,8 @@ def default_greens_functions(gf: str = "Wu"):
         wave = GFWu()
     elif gf == "ExactGuevelDelhommeau":
         wave = ExactGuevelDelhommeau()
+    elif gf == "Surrogate":
+        wave = SurrogateDelhommeau()
     else:
         raise ValueError(f'unknown Green\'s function "{gf}"; use "Wu" or "ExactGuevelDelhommeau"')
     return (Rankine(), RankineReflected(), wave)

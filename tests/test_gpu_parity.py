@@ -55,8 +55,9 @@ def test_wu_wave_terms(mh, oracle, ctx):
 
 
 def test_exact_wave_terms(mh, oracle, ctx):
-    rs = np.array([0.0, 1e-4, 0.3, 1.0, 2.5, 7.0, 40.0, 300.0])
-    zs = -np.array([1.0, 0.05, 0.8, 1.0, 3.0, 0.4, 20.0, 49.0])
+    # includes large r with small |z|: hundreds of oscillations of the integrand
+    rs = np.array([0.0, 1e-4, 0.3, 1.0, 2.5, 7.0, 40.0, 300.0, 300.0, 950.0, 120.0])
+    zs = -np.array([1.0, 0.05, 0.8, 1.0, 3.0, 0.4, 20.0, 49.0, 0.5, 2.0, 0.02])
     got = mh._device.exact_wave_terms(ctx, rs, zs, rtol=1e-12, atol=1e-14)
     for i, (r, z) in enumerate(zip(rs, zs)):
         G = oracle.egd_dimless(r, z, 1e-12, 1e-14)

@@ -1,0 +1,171 @@
+"""Learned Delhommeau wave-term surrogate: training kernels against a PyTorch fp32
+reference, training quality against the Wu fits, the exact fallback, and assembly.
+
+The surrogate corrects the Wu fits toward the exact Guevel-Delhommeau term; its
+target and network are described in csrc/mh_mlp.cuh.  The exact kernel it is
+measured against is itself pinned to the oracle in test_gpu_parity.py.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N_PARAMS = 8902
+
+
+def _torch_loss_grad(params, x, y):
+    """Plain PyTorch fp32 forward/backward of the same network (exact tanh)."""
+    torch = pytest.importorskip("torch")
+    p = torch.tensor(params, dtype=torch.float32, requires_grad=True)
+    o = 0
+    def take(n):
+        nonlocal o
+        t = p[o:o + n]
+        o += n
+        return t
+    W1 = take(128).view(64, 2); b1 = take(64)
+    W2 = take(4096).view(64, 64); b2 = take(64)
+    W3 = take(4096).view(64, 64); b3 = take(64)
+    W4 = take(384).view(6, 64); b4 = take(6)
+    X = torch.tensor(x, dtype=torch.float32)
+    Y = torch.tensor(y, dtype=torch.float32)
+    h = torch.tanh(X @ W1.T + b1)
+    h = torch.tanh(h @ W2.T + b2)
+    h = torch.tanh(h @ W3.T + b3)
+    out = h @ W4.T + b4
+    loss = ((out - Y) ** 2).mean()
+    loss.backward()
+    return float(loss), p.grad.numpy().astype(np.float64)
+
+
+def _bf16(a):
+    """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    u = np.asarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def test_training_kernels_match_torch(ctx):
+    rng = np.random.default_rng(4)
+    params = np.zeros(N_PARAMS, dtype=np.float32)
+    for off, fo, fi in ((0, 64, 2), (192, 64, 64), (4352, 64, 64), (8512, 6, 64)):
+        a = np.sqrt(6.0 / (fo + fi))
+        params[off:off + fo * fi] = rng.uniform(-a, a, fo * fi)
+    params[128:192] = rng.normal(0, 0.1, 64)
+    params = _bf16(params)
+    x = rng.uniform(-1, 1, (1000, 2)).astype(np.float32)
+    y = rng.normal(0, 0.2, (1000, 6)).astype(np.float32)
+    loss, g = ctx.surrogate_loss_grad(params, x, y)
+    tl, tg = _torch_loss_grad(params, x, y)
+    # tanh.approx.f32 (max relative error 2^-11) against torch's exact tanh
+    assert abs(loss - tl) <= 5e-3 * tl
+    assert np.linalg.norm(g - tg) <= 1e-2 * np.linalg.norm(tg)
+
+
+@pytest.fixture(scope="module")
+def trained(mh, ctx):
+    params, report = ctx.surrogate_train(n_samples=1 << 18, seed=7, epochs=24, batch=2048, lr=3e-3)
+    return params, report
+
+
+def test_training_beats_wu(trained):
+    _, rep = trained
+    assert rep["validation_points"] >= 1024
+    assert np.isfinite(rep["final_mse"]) and rep["final_mse"] < 1e-2
+    # the corrected term is closer to the exact kernel than the Wu fits it starts from
+    assert rep["rms_rel_err_G"] < 0.5 * rep["wu_rms_rel_err_G"]
+
+
+def test_points_fallback_and_correction(mh, ctx, trained):
+    params, _ = trained
+    ctx.surrogate_set(params)
+    rng = np.random.default_rng(9)
+    r_in = 10 ** rng.uniform(-2, 2, 64)
+    z_in = rng.uniform(-20, -0.1, 64)
+    r_out = np.array([2e3, 0.5, 1.5e3])
+    z_out = np.array([-2.0, -60.0, -0.3])
+    r = np.concatenate([r_in, r_out])
+    z = np.concatenate([z_in, z_out])
+    sur = mh.surrogate_wave_terms(r, z, ctx=ctx)
+    ex = _exact(mh, ctx, r, z)
+    wu = _wu(mh, ctx, r, z)
+    # outside the box: the exact kernel itself
+    k = len(r_in)
+    assert np.array_equal(sur[k:, 0], ex[k:, 0]) and np.array_equal(sur[k:, 1], ex[k:, 1])
+    # below r = 1e-3 the network is read at r = 1e-3: still close to exact, and exact in Im
+    r0 = np.array([0.0, 1e-5, 5e-4])
+    z0 = np.array([-0.4, -3.0, -12.0])
+    s0, e0 = mh.surrogate_wave_terms(r0, z0, ctx=ctx), _exact(mh, ctx, r0, z0)
+    assert np.all(np.abs(s0[:, 0] - e0[:, 0]) <= 1e-2 * np.abs(e0[:, 0]))
+    # inside: closer to exact than Wu on average
+    e_s = np.abs(sur[:k, 0] - ex[:k, 0]) / np.abs(ex[:k, 0])
+    e_w = np.abs(wu[:k, 0] - ex[:k, 0]) / np.abs(ex[:k, 0])
+    assert np.sqrt(np.mean(e_s ** 2)) < np.sqrt(np.mean(e_w ** 2))
+    # imaginary parts are the exact J0 / J1 terms in both kernels; the surrogate keeps Wu's
+    assert np.array_equal(sur[:k, 0].imag, wu[:k, 0].imag)
+    assert np.abs(sur[:k, 0].imag - ex[:k, 0].imag).max() < 1e-9
+
+
+def _exact(mh, ctx, r, z):
+    out = np.empty((len(r), 2), dtype=np.complex128)
+    ctx.check(ctx._L.mh_exact_wave_terms(ctx.handle, len(r), np.ascontiguousarray(r).ctypes.data,
+                                         np.ascontiguousarray(z).ctypes.data, 1e-12, 1e-14, out.ctypes.data, 0), "exact")
+    return out
+
+
+def _wu(mh, ctx, r, z):
+    out = np.empty((len(r), 3), dtype=np.complex128)
+    ctx.check(ctx._L.mh_wu_wave_terms(ctx.handle, len(r), np.ascontiguousarray(r).ctypes.data,
+                                      np.ascontiguousarray(z).ctypes.data, out.ctypes.data, 0), "wu")
+    return out
+
+
+@pytest.mark.parametrize("direct", [True, False])
+def test_assembly_between_wu_and_exact(mh, ctx, trained, direct):
+    params, _ = trained
+    ctx.surrogate_set(params)
+    mesh = mh.hemisphere_mesh(1.0, 8, 16)
+    k = 0.7
+    S_s, D_s = mh.assemble_matrices((mh.Rankine(), mh.RankineReflected(), mh.SurrogateDelhommeau()), mesh, k,
+                                    direct=direct, ctx=ctx)
+    S_e, D_e = mh.assemble_matrices((mh.Rankine(), mh.RankineReflected(), mh.ExactGuevelDelhommeau()), mesh, k,
+                                    direct=direct, ctx=ctx)
+    S_w, D_w = mh.assemble_matrices((mh.Rankine(), mh.RankineReflected(), mh.GFWu()), mesh, k, direct=direct,
+                                    ctx=ctx)
+    # self pairs (r = 0) lie outside the training box: recomputed by the exact kernel
+    di = np.arange(mesh.nfaces)
+    assert np.array_equal(S_s[di, di], S_e[di, di]) and np.array_equal(D_s[di, di], D_e[di, di])
+    for A_s, A_e, A_w in ((S_s, S_e, S_w), (D_s, D_e, D_w)):
+        err_s = np.linalg.norm(A_s - A_e) / np.linalg.norm(A_e)
+        err_w = np.linalg.norm(A_w - A_e) / np.linalg.norm(A_e)
+        assert err_s < err_w
+
+
+def test_surrogate_sweep_and_errors(mh, ctx, trained):
+    params, _ = trained
+    ctx.surrogate_set(params)
+    body = mh.FloatingBody(mh.hemisphere_mesh(1.0, 6, 12), ["Heave", "Surge"])
+    p = {"wave_frequencies": [0.6, 1.2, 2.0], "radiating_dofs": ["Heave", "Surge"], "wave_directions": [0.0]}
+    res = {}
+    for name, gf in (("s", mh.SurrogateDelhommeau()), ("e", mh.ExactGuevelDelhommeau()), ("w", mh.GFWu())):
+        res[name] = mh.hydrodynamic_coefficients(body, p, mh.DirectBEM((mh.Rankine(), mh.RankineReflected(), gf)),
+                                                 ctx=ctx, rho=1025.0)
+    for key in ("added_mass", "radiation_damping", "excitation_force"):
+        e = np.abs(res["s"][key] - res["e"][key]).max() / np.abs(res["e"][key]).max()
+        w = np.abs(res["w"][key] - res["e"][key]).max() / np.abs(res["e"][key]).max()
+        assert e < w, key
+    with pytest.raises(ValueError):
+        mh.hydrodynamic_coefficients(body, p, mh.DirectBEM((mh.Rankine(), mh.GFWu(), mh.SurrogateDelhommeau())),
+                                     ctx=ctx)
+    with pytest.raises(ValueError):
+        mh.batch_hydrodynamic_coefficients([body], [p], mh.DirectBEM("Surrogate"), ctx=ctx)
+
+
+def test_surrogate_needs_parameters(mh):
+    fresh = mh.Context(0)
+    try:
+        with pytest.raises(ValueError):
+            mh.assemble_matrices((mh.Rankine(), mh.SurrogateDelhommeau()), mh.hemisphere_mesh(1.0, 4, 8), 0.5,
+                                 ctx=fresh)
+    finally:
+        fresh.close() if hasattr(fresh, "close") else None
