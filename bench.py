@@ -319,6 +319,15 @@ def run_gpu(args):
     batch = None
     if not args.no_batch:
         batch = run_batch_variant(mh, ctx, stream, dev, torch, timed)
+    extra = {}
+    if not args.no_variants and ws == 1:
+        for name, fn in (("config2_kernels", lambda: run_kernel_variants(mh, ctx)),
+                         ("config4_surrogate", lambda: run_surrogate_variant(mh, ctx, args.surrogate_exact)),
+                         ("config5_adjoint", lambda: run_adjoint_variant(mh, ctx))):
+            try:
+                extra[name] = fn()
+            except Exception as exc:  # a failed variant is reported, the headline still prints
+                extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
 
     units = N_OMEGA * args.steps * ws
     value = units / t_dev
@@ -368,6 +377,7 @@ def run_gpu(args):
     }
     if batch is not None:
         line["variants"]["batched_64_bodies"] = batch
+    line["variants"].update(extra)
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle
@@ -408,6 +418,135 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
     return out
 
 
+def _profiled(ctx, fn):
+    """Run fn once with the per-kernel-group profiler; returns (seconds, {group: ms})."""
+    ctx.synchronize()
+    ctx.profile_reset()
+    ctx.profile(True)
+    t0 = time.perf_counter()
+    out = fn()
+    ctx.synchronize()
+    t = time.perf_counter() - t0
+    prof = {k: v[0] for k, v in ctx.profile_read().items()}
+    ctx.profile(False)
+    return t, prof, out
+
+
+def run_kernel_variants(mh, ctx):
+    """Config 2 with the exact Guevel-Delhommeau kernel (a subset of the frequencies) and the
+    indirect formulation; timed once each, host-to-host through the public API."""
+    mesh, body = build_workload(mh)
+    n = mesh.nfaces
+    out = {}
+    sub = OMEGAS[[0, len(OMEGAS) // 2, len(OMEGAS) - 1]] if len(OMEGAS) >= 3 else OMEGAS
+    p = {"wave_frequencies": sub, "radiating_dofs": DOFS, "wave_directions": BETAS}
+    t, prof, _ = _profiled(ctx, lambda: mh.hydrodynamic_coefficients(
+        body, p, mh.DirectBEM("ExactGuevelDelhommeau"), ctx=ctx, rho=RHO, g=G))
+    asm = sum(v for k, v in prof.items() if k.startswith("assemble"))
+    out["exact_delhommeau_direct"] = {
+        "omegas": [float(x) for x in sub], "value": len(sub) / t, "unit": UNIT,
+        "panel_pairs_per_sec": len(sub) * n * n / (asm * 1e-3),
+        "note": "per pair two adaptive Gauss-Kronrod (7,15) integrals of e^zeta E1(zeta) to 1e-12 relative"}
+    p = {"wave_frequencies": OMEGAS, "radiating_dofs": DOFS, "wave_directions": BETAS}
+    t, prof, _ = _profiled(ctx, lambda: mh.hydrodynamic_coefficients(body, p, mh.IndirectBEM(), ctx=ctx, rho=RHO,
+                                                                      g=G))
+    out["wu_indirect"] = {"value": len(OMEGAS) / t, "unit": UNIT,
+                          "note": "IndirectBEM: sources = K^-1 bc, phi = S sources; same Green functions"}
+    return out
+
+
+def run_surrogate_variant(mh, ctx, exact_omegas=1):
+    """Config 4: the learned surrogate on the 8000-panel barge (100 x 20 x 10 m), 40 omega uniform in
+    [0.2, 3.0]; errors against the exact kernel on `exact_omegas` of the frequencies."""
+    params = mh.load_surrogate(ctx=ctx)
+    meta_path = os.path.join(REPO, "marinehydro.jl_gb300", "data", "surrogate_delhommeau.json")
+    meta = json.load(open(meta_path)) if os.path.exists(meta_path) else {}
+    mesh = mh.barge_mesh(100.0, 20.0, 10.0, 100, 20, 25)
+    body = mh.FloatingBody(mesh, ["Surge", "Heave", "Pitch"], rotation_center=(0.0, 0.0, 0.0))
+    n = mesh.nfaces
+    oms = np.linspace(0.2, 3.0, 40)
+    gfs_s = (mh.Rankine(), mh.RankineReflected(), mh.SurrogateDelhommeau())
+    prm = {"wave_frequencies": oms, "radiating_dofs": ["Surge", "Heave", "Pitch"], "wave_directions": [0.0]}
+    out = {"workload": "barge 100x20x10 m, 8000 panels (bottom 100x20, sides 100x25, ends 20x25), 40 omega uniform "
+                       "[0.2,3.0], surge/heave/pitch + 1 heading, Rankine+image+surrogate, direct",
+           "panels": n, "params": len(params), "training": meta}
+    mh.hydrodynamic_coefficients(body, {**prm, "wave_frequencies": oms[:2]}, mh.DirectBEM(gfs_s, precision="mixed"),
+                                 ctx=ctx, rho=RHO, g=G)  # warm-up
+    for prec in ("mixed",):
+        t, prof, _ = _profiled(ctx, lambda: mh.hydrodynamic_coefficients(
+            body, prm, mh.DirectBEM(gfs_s, precision=prec), ctx=ctx, rho=RHO, g=G))
+        wave = prof.get("assemble_wave_surrogate", 0.0) + prof.get("assemble_wave_fallback", 0.0)
+        out[prec] = {"value": len(oms) / t, "unit": UNIT, "seconds": t,
+                     "surrogate_pairs_per_sec": len(oms) * n * n / (wave * 1e-3) if wave else None,
+                     "fallback_ms": prof.get("assemble_wave_fallback", 0.0),
+                     "kernel_ms": {k: round(v, 1) for k, v in sorted(prof.items(), key=lambda kv: -kv[1])[:6]}}
+    if exact_omegas > 0:
+        sub = oms[:exact_omegas]
+        ps = {**prm, "wave_frequencies": sub}
+        res = {}
+        times = {}
+        for name, gf in (("surrogate", mh.SurrogateDelhommeau()), ("exact", mh.ExactGuevelDelhommeau()),
+                         ("wu", mh.GFWu())):
+            t0 = time.perf_counter()
+            res[name] = mh.hydrodynamic_coefficients(body, ps, mh.DirectBEM((mh.Rankine(), mh.RankineReflected(), gf),
+                                                                            precision="mixed"), ctx=ctx, rho=RHO, g=G)
+            times[name] = time.perf_counter() - t0
+        errs = {}
+        for key in ("added_mass", "radiation_damping", "excitation_force"):
+            ref = res["exact"][key]
+            scale = float(np.abs(ref).max())
+            errs[key] = {"surrogate": float(np.abs(res["surrogate"][key] - ref).max() / scale),
+                         "wu": float(np.abs(res["wu"][key] - ref).max() / scale)}
+        out["vs_exact"] = {"omegas": [float(x) for x in sub], "max_abs_err_over_max_abs": errs,
+                           "seconds": {k: round(v, 3) for k, v in times.items()},
+                           "exact_over_surrogate_time": times["exact"] / times["surrogate"]}
+    return out
+
+
+def run_adjoint_variant(mh, ctx):
+    """Config 5: gradient of J = sum over 20 omega of heave added mass + damping of two cylinders
+    (r = 3 m, draft 6 m, 3000 panels each, 30 m apart) w.r.t. every vertex coordinate."""
+    m1 = mh.vertical_cylinder_mesh(3.0, 6.0, 60, 40, 10)
+    m2 = mh.vertical_cylinder_mesh(3.0, 6.0, 60, 40, 10, center=(30.0, 0.0))
+    def bodies(V1, V2):
+        b1 = mh.FloatingBody(mh.StaticArraysMesh(V1, m1.faces), ["Heave"], body_name="c1")
+        b2 = mh.FloatingBody(mh.StaticArraysMesh(V2, m2.faces), ["Heave"], body_name="c2")
+        return b1 + b2
+    body = bodies(m1.vertices, m2.vertices)
+    oms = np.linspace(0.4, 2.0, 20)
+    obj = ["c1__Heave", "c2__Heave"]
+    out = {"workload": "two vertical cylinders r=3 m draft 6 m, 3000 panels each (60 x (40+10)), 30 m apart, 20 omega "
+                       "uniform [0.4,2.0]; J = sum_omega (A+B) of both heave diagonal entries; d J / d vertices",
+           "panels": body.mesh.nfaces, "vertex_coordinates": int(body.mesh.vertices.size)}
+    def sweep(b, prec):
+        r = mh.hydrodynamic_coefficients(b, {"wave_frequencies": oms, "radiating_dofs": obj, "influenced_dofs": obj},
+                                         mh.DirectBEM(precision=prec), ctx=ctx, rho=RHO, g=G)
+        A, B = r["added_mass"][..., 0], r["radiation_damping"][..., 0]
+        return float(sum(A[h, h, w] + B[h, h, w] for h in range(2) for w in range(len(oms))))
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        J, grad = mh.hydro_gradient(body, oms, obj, mh.DirectBEM(precision=prec), ctx=ctx, rho=RHO, g=G)
+        tg = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        Js = sweep(body, prec)
+        tf = time.perf_counter() - t0
+        out[prec] = {"gradient_seconds": tg, "forward_sweep_seconds": tf, "J": J, "J_sweep": Js,
+                     "gradient_over_forward": tg / tf}
+        if prec == "fp64":
+            g64 = grad
+    # central differences (h = 1e-6) along the radial scaling of cylinder 1 (an affine move:
+    # panels stay planar), with FP64-accurate mixed-precision sweeps
+    d1 = m1.vertices * [1.0, 1.0, 0.0]
+    h = 1e-6
+    jp = sweep(bodies(m1.vertices + h * d1, m2.vertices), "mixed")
+    jm = sweep(bodies(m1.vertices - h * d1, m2.vertices), "mixed")
+    fd = (jp - jm) / (2 * h)
+    ad = float(np.sum(g64[:m1.nvertices] * d1))
+    out["fd_check"] = {"direction": "radial scaling of cylinder 1", "adjoint": ad, "central_difference": fd,
+                       "rel_err": abs(ad - fd) / abs(fd)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -416,6 +555,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-body batching variant")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the exact-kernel, surrogate and adjoint variants")
+    ap.add_argument("--surrogate-exact", type=int, default=1,
+                    help="frequencies of the surrogate workload also run with the exact kernel for its errors")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
     ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")

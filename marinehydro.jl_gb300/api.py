@@ -14,6 +14,8 @@ keeps everything on the device.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from . import _device, _lib
@@ -341,6 +343,17 @@ def train_surrogate(n_samples=10_000_000, seed=2026, epochs=8, batch=8192, lr=3e
 def set_surrogate(params, ctx=None):
     """Install surrogate parameters (as returned by train_surrogate) on the context."""
     _ctx(ctx).surrogate_set(params)
+
+
+SURROGATE_PARAMS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_delhommeau.npy")
+
+
+def load_surrogate(path=None, ctx=None):
+    """Install the shipped surrogate parameters (data/surrogate_delhommeau.npy, made by
+    data/train_surrogate.py) or those in `path` on the context; returns them."""
+    params = np.load(path or SURROGATE_PARAMS)
+    set_surrogate(params, ctx)
+    return params
 
 
 def surrogate_wave_terms(r, z, ctx=None):
