@@ -297,11 +297,16 @@ def run_gpu(args):
         return tot, wall, launches, prof
 
     if args.profile_only:
-        # a small, self-contained case for ncu: W untimed sweeps + one sweep, nothing else
+        # a small, self-contained case for ncu: W untimed runs + one run, nothing else
+        run = {"cylinder": lambda: step_device(_lib.MH_PREC_MIXED if args.precision == "mixed" else _lib.MH_PREC_FP64),
+               "surrogate": lambda: _profile_case_surrogate(mh, ctx),
+               "adjoint": lambda: _profile_case_adjoint(mh, ctx),
+               "exact": lambda: _profile_case_exact(mh, ctx, body)}[args.case]
         for _ in range(args.warmup + 1):
-            step_device(_lib.MH_PREC_MIXED if args.precision == "mixed" else _lib.MH_PREC_FP64)
+            run()
         torch.cuda.synchronize(dev)
-        print(json.dumps({"profile_only": True, "omegas": N_OMEGA, "launches": ctx.launch_count()}))
+        print(json.dumps({"profile_only": True, "case": args.case, "omegas": N_OMEGA,
+                          "launches": ctx.launch_count()}))
         return 0
     peak64, peak32 = ctx.probe_fma_peaks()
     with ClockSampler(local) as clk:
@@ -430,6 +435,31 @@ def _profiled(ctx, fn):
     prof = {k: v[0] for k, v in ctx.profile_read().items()}
     ctx.profile(False)
     return t, prof, out
+
+
+def _profile_case_surrogate(mh, ctx):
+    """Small surrogate case: barge 100 x 20 x 10 m with 4400 panels, 2 frequencies."""
+    mh.load_surrogate(ctx=ctx)
+    mesh = mh.barge_mesh(100.0, 20.0, 10.0, 100, 20, 10)
+    body = mh.FloatingBody(mesh, ["Heave"])
+    gf = (mh.Rankine(), mh.RankineReflected(), mh.SurrogateDelhommeau())
+    mh.hydrodynamic_coefficients(body, {"wave_frequencies": [0.8, 2.0], "radiating_dofs": ["Heave"]},
+                                 mh.DirectBEM(gf, precision="mixed"), ctx=ctx, rho=RHO, g=G)
+
+
+def _profile_case_adjoint(mh, ctx):
+    """Small adjoint case: two cylinders of 3000 panels each, 2 frequencies."""
+    m1 = mh.vertical_cylinder_mesh(3.0, 6.0, 60, 40, 10)
+    m2 = mh.vertical_cylinder_mesh(3.0, 6.0, 60, 40, 10, center=(30.0, 0.0))
+    body = mh.FloatingBody(m1, ["Heave"], body_name="c1") + mh.FloatingBody(m2, ["Heave"], body_name="c2")
+    mh.hydro_gradient(body, [0.8, 1.6], ["c1__Heave", "c2__Heave"], mh.DirectBEM(precision="mixed"), ctx=ctx,
+                      rho=RHO, g=G)
+
+
+def _profile_case_exact(mh, ctx, body):
+    """Exact Guevel-Delhommeau kernel on the 2000-panel cylinder, 1 frequency."""
+    mh.hydrodynamic_coefficients(body, {"wave_frequencies": [1.6], "radiating_dofs": ["Heave"]},
+                                 mh.DirectBEM("ExactGuevelDelhommeau", precision="mixed"), ctx=ctx, rho=RHO, g=G)
 
 
 def run_kernel_variants(mh, ctx):
@@ -563,6 +593,8 @@ def main():
                     help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
     ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="for --profile-only")
+    ap.add_argument("--case", default="cylinder", choices=["cylinder", "surrogate", "adjoint", "exact"],
+                    help="for --profile-only: the headline sweep, or a small surrogate / adjoint / exact-kernel case")
     args = ap.parse_args()
     set_omegas(args.omegas)
     if args.warmup < 3 and not args.profile_only:
