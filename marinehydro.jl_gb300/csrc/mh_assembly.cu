@@ -15,6 +15,8 @@
 // S = S_static + S_wave is the reference's own split, matrix_assembly.jl:183-208).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mh_greens.cuh"
 #include "mh_internal.cuh"
 #include "mh_mlp.cuh"
@@ -362,27 +364,83 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
   }
 }
 
-// Exact Delhommeau terms for the pairs the surrogate queued (one thread per pair).
+// The exact Delhommeau terms of one unordered pair {i, j} at wavenumber k, computed by the
+// whole warp (egd_warp); lane 0 writes both S/D entries.
 template <bool DIRECT>
-__global__ void __launch_bounds__(64) surrogate_fallback_kernel(AssemblyParams p, const double* __restrict__ SR,
-                                                                const double* __restrict__ DR,
-                                                                const double* __restrict__ ks,
-                                                                double2* __restrict__ S, double2* __restrict__ D,
-                                                                int64_t sstride, int wave_identity) {
+__device__ __forceinline__ void exact_pair_warp(const AssemblyParams& p, int64_t i, int64_t j, double k, double* sw,
+                                                const double* __restrict__ SR, const double* __restrict__ DR,
+                                                double2* __restrict__ Sb, double2* __restrict__ Db, int wave_identity) {
+  const PanelRec& Pi = p.P[i];
+  const PanelRec& Pj = p.P[j];
+  const double ci[3] = {Pi.c[0], Pi.c[1], Pi.c[2]};
+  double r, z;
+  reduced_coords(ci, Pj.c, k, r, z);
+  double2 GF, dGdr;
+  egd_warp(r, z, p.quad_rtol, p.quad_atol, sw, GF, dGdr);
+  if ((threadIdx.x & 31) != 0) return;
+  // both_greens_and_gradient_greens + with_reduced_coordinates_derivative, as wave_terms<., 2>
+  const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+  const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+  const double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
+  double d1 = 0.0, d2 = 0.0;
+  if (fabs(r) > 1e-6) {
+    d1 = k * k / r * dx1;
+    d2 = k * k / r * dx2;
+  }
+  WaveTerms w;
+  w.I = make_double2(k * GF.x, k * GF.y);
+  w.gh[0] = make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y));
+  w.gh[1] = make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y));
+  w.gz = make_double2(k * (k * dGdz.x), k * (k * dGdz.y));
+  const double ni[3] = {Pi.n[0], Pi.n[1], Pi.n[2]};
+  store_pair<DIRECT>(p, w, i, j, ni, Pi.area, Pj, SR, DR, Sb, Db, wave_identity);
+}
+
+constexpr int kExactWarps = 4;  // warps per CTA of the warp-per-pair exact kernels
+
+// Exact Delhommeau wave part: one warp per unordered pair {i <= j}, pairs in column-major
+// upper-triangle order q = j (j + 1) / 2 + i, grid-strided; blockIdx.y = wavenumber.
+template <bool DIRECT>
+__global__ void __launch_bounds__(32 * kExactWarps) exact_wave_warp_kernel(AssemblyParams p,
+                                                                            const double* __restrict__ SR,
+                                                                            const double* __restrict__ DR,
+                                                                            const double* __restrict__ ks,
+                                                                            double2* __restrict__ S,
+                                                                            double2* __restrict__ D, int64_t sstride,
+                                                                            int wave_identity) {
+  __shared__ double sw[kExactWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5;
+  const int64_t npairs = p.n * (p.n + 1) / 2;
+  const double k = ks[blockIdx.y];
+  double2* Sb = S + blockIdx.y * sstride;
+  double2* Db = D + blockIdx.y * sstride;
+  for (int64_t q = blockIdx.x * (int64_t)kExactWarps + warp; q < npairs; q += (int64_t)gridDim.x * kExactWarps) {
+    int64_t j = (int64_t)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while (j * (j + 1) / 2 > q) --j;
+    while ((j + 1) * (j + 2) / 2 <= q) ++j;
+    const int64_t i = q - j * (j + 1) / 2;
+    exact_pair_warp<DIRECT>(p, i, j, k, sw[warp], SR, DR, Sb, Db, wave_identity);
+  }
+}
+
+// Exact Delhommeau terms for the pairs the surrogate queued (one warp per pair).
+template <bool DIRECT>
+__global__ void __launch_bounds__(32 * kExactWarps) surrogate_fallback_kernel(AssemblyParams p,
+                                                                               const double* __restrict__ SR,
+                                                                               const double* __restrict__ DR,
+                                                                               const double* __restrict__ ks,
+                                                                               double2* __restrict__ S,
+                                                                               double2* __restrict__ D,
+                                                                               int64_t sstride, int wave_identity) {
+  __shared__ double sw[kExactWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5;
   const unsigned long long queued = p.fb_state[0];
   if (blockIdx.x == 0 && threadIdx.x == 0 && (int64_t)queued > p.fb_cap) p.fb_state[1] = 1ull;  // sticky overflow
   const int64_t count = (int64_t)queued < p.fb_cap ? (int64_t)queued : p.fb_cap;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t q = blockIdx.x * (int64_t)kExactWarps + warp; q < count; q += (int64_t)gridDim.x * kExactWarps) {
     const int4 e = p.fb_list[q];
-    const int64_t i = e.x, j = e.y;
-    const double k = ks[e.z];
-    double ci[3], ni[3];
-    for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
-    const double ai = p.P[i].area;
-    const PanelRec& Pj = p.P[j];
-    WaveTerms w;
-    wave_terms<DIRECT, 2>(p, ci, Pj.c, k, w);
-    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, S + e.z * sstride, D + e.z * sstride, wave_identity);
+    exact_pair_warp<DIRECT>(p, e.x, e.y, ks[e.z], sw[warp], SR, DR, S + e.z * sstride, D + e.z * sstride,
+                            wave_identity);
   }
 }
 
@@ -405,12 +463,20 @@ __global__ void wu_points_kernel(int64_t m, const double* __restrict__ hh, const
   out[3 * q + 2] = c;
 }
 
-__global__ void exact_points_kernel(int64_t m, const double* __restrict__ r, const double* __restrict__ z,
-                                    double rtol, double atol, double2* __restrict__ out) {
-  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= m) return;
-  out[2 * q] = egd_adaptive<false>(r[q], z[q], rtol, atol);
-  out[2 * q + 1] = egd_adaptive<true>(r[q], z[q], rtol, atol);
+// one warp per point
+__global__ void __launch_bounds__(32 * kExactWarps) exact_points_kernel(int64_t m, const double* __restrict__ r,
+                                                                         const double* __restrict__ z, double rtol,
+                                                                         double atol, double2* __restrict__ out) {
+  __shared__ double sw[kExactWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5;
+  const int64_t q = blockIdx.x * (int64_t)kExactWarps + warp;
+  if (q >= m) return;  // warp-uniform
+  double2 G, Gr;
+  egd_warp(r[q], z[q], rtol, atol, sw[warp], G, Gr);
+  if ((threadIdx.x & 31) == 0) {
+    out[2 * q] = G;
+    out[2 * q + 1] = Gr;
+  }
 }
 
 }  // namespace
@@ -464,9 +530,21 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
     else wave_kernel<false, 4><<<grid, kRowsPerCta, smem, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
     lc.post(st, "assemble_wave_surrogate");
     lc.pre(st);
-    if (p.direct) surrogate_fallback_kernel<true><<<4 * 152, 64, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
-    else surrogate_fallback_kernel<false><<<4 * 152, 64, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    const int fbg = 8 * 152;
+    if (p.direct) surrogate_fallback_kernel<true><<<fbg, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    else surrogate_fallback_kernel<false><<<fbg, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
     lc.post(st, "assemble_wave_fallback");
+    return;
+  }
+  if (wv == MH_GF_EXACT_DELHOMMEAU) {
+    // one warp per unordered pair; enough CTAs for several resident per SM
+    const int64_t npairs = p.n * (p.n + 1) / 2;
+    const int64_t want = (npairs + kExactWarps - 1) / kExactWarps;
+    dim3 g((unsigned)std::min<int64_t>(want, 152 * 16), (unsigned)nk);
+    lc.pre(st);
+    if (p.direct) exact_wave_warp_kernel<true><<<g, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    else exact_wave_warp_kernel<false><<<g, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    lc.post(st, "assemble_wave_exact");
     return;
   }
   const int mode = (wv == MH_GF_WU) ? 1 : (wv == MH_GF_EXACT_DELHOMMEAU ? 2 : 3);
@@ -490,7 +568,8 @@ void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const dou
                          double atol, double2* out) {
   if (m <= 0) return;
   MH_LAUNCH(lc, st, "exact_points",
-            exact_points_kernel<<<(unsigned)((m + 63) / 64), 64, 0, st>>>(m, r, z, rtol, atol, out));
+            exact_points_kernel<<<(unsigned)((m + kExactWarps - 1) / kExactWarps), 32 * kExactWarps, 0, st>>>(
+                m, r, z, rtol, atol, out));
 }
 
 }  // namespace mh

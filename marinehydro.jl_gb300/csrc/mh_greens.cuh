@@ -456,6 +456,161 @@ __device__ inline double2 egd_adaptive(double r, double z, double rtol, double a
   return zscale(4.0, total);
 }
 
+// ---- warp-cooperative form: one warp per (r, z), both integrals at once -------------
+// The same quadrature rule and tolerance test, organised for the SIMT machine: the 15
+// Kronrod nodes of two segments run on 30 lanes, G and dG/dr come from the same
+// exp(zeta), E1(zeta) evaluation at each node, and the depth-first refinement stack
+// lives in shared memory, written by lane 0 and read by the whole warp.  A segment is
+// accepted when both integrals meet their share of the tolerance.
+constexpr int kGKWarpStack = 48;   // entries of 8 doubles: a, b, G (2), dG/dr (2), err G, err dG/dr
+
+// both integrands at theta (the two egd_integrand<> forms sharing E1)
+__device__ __forceinline__ void egd_integrands(double theta, double r, double z, double f[4]) {
+  const double ct = cos(theta);
+  const double2 zeta = make_double2(z, r * ct);
+  const double2 ez = zexp(zeta);
+  const double2 g = exp_e1(zeta);
+  const double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
+  f[0] = j.x;
+  f[1] = ez.x;
+  const double2 inv = zdiv(make_double2(1.0, 0.0), make_double2(kPi * zeta.x, kPi * zeta.y));
+  const double2 w = make_double2(j.x - inv.x, j.y - inv.y);
+  f[2] = -ct * w.y;
+  f[3] = -ct * ez.y;
+}
+
+// Kronrod node, Kronrod weight and Gauss weight of this lane (lanes 15 and 31 idle)
+__device__ __forceinline__ void gk_lane_node(int lane, double& t, double& wk, double& wg) {
+  const int j = lane & 15;
+  t = 0.0; wk = 0.0; wg = 0.0;
+  if (j == 15) return;
+  if (j < 7) {
+    t = -kGKx[j]; wk = kGKwk[j]; wg = (j & 1) ? kGKwg[j >> 1] : 0.0;
+  } else if (j == 7) {
+    wk = kGKwk[7]; wg = kGKwg[3];
+  } else {
+    const int m = 14 - j;
+    t = kGKx[m]; wk = kGKwk[m]; wg = (m & 1) ? kGKwg[m >> 1] : 0.0;
+  }
+}
+
+// GK(7,15) of both integrands over [aA, bA] (lanes 0-15) and [aB, bB] (lanes 16-31);
+// every lane returns both results
+__device__ __forceinline__ void gk15_pair_warp(double aA, double bA, double aB, double bB, double r, double z,
+                                               double vA[4], double& eGA, double& eRA, double vB[4], double& eGB,
+                                               double& eRB) {
+  const int lane = threadIdx.x & 31;
+  double t, wk, wg;
+  gk_lane_node(lane, t, wk, wg);
+  const double a = lane < 16 ? aA : aB, b = lane < 16 ? bA : bB;
+  const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  double f[4];
+  egd_integrands(c + h * t, r, z, f);
+  double K[4], Gs[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) { K[q] = wk * f[q]; Gs[q] = wg * f[q]; }
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      K[q] += __shfl_xor_sync(0xffffffffu, K[q], off);
+      Gs[q] += __shfl_xor_sync(0xffffffffu, Gs[q], off);
+    }
+  }
+  double KA[4], GA[4], KB[4], GB[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    KA[q] = __shfl_sync(0xffffffffu, K[q], 0);
+    GA[q] = __shfl_sync(0xffffffffu, Gs[q], 0);
+    KB[q] = __shfl_sync(0xffffffffu, K[q], 16);
+    GB[q] = __shfl_sync(0xffffffffu, Gs[q], 16);
+  }
+  const double hA = 0.5 * (bA - aA), hB = 0.5 * (bB - aB);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) { vA[q] = hA * KA[q]; vB[q] = hB * KB[q]; }
+  eGA = hypot(hA * (KA[0] - GA[0]), hA * (KA[1] - GA[1]));
+  eRA = hypot(hA * (KA[2] - GA[2]), hA * (KA[3] - GA[3]));
+  eGB = hypot(hB * (KB[0] - GB[0]), hB * (KB[1] - GB[1]));
+  eRB = hypot(hB * (KB[2] - GB[2]), hB * (KB[3] - GB[3]));
+}
+
+// G = _dimless_wave_term(r, z) and dG/dr = _d_dimless_wave_term_dr(r, z) by the whole warp
+// (all 32 lanes call it with the same r, z; `sw` is this warp's 8 * kGKWarpStack doubles of
+// shared memory).  Same segmentation and tolerance rule as egd_adaptive.
+__device__ inline void egd_warp(double r, double z, double rtol, double atol, double* sw, double2& G, double2& Gr) {
+  const int lane = threadIdx.x & 31;
+  const double L = kPi / 2;
+  const int m0 = (int)fmin(1024.0, fmax(1.0, ceil(r / 4.0)));
+  const double h0 = L / m0;
+  // first pass: the integrals over the initial segments and the tolerances they imply
+  double cg[4] = {0.0, 0.0, 0.0, 0.0};
+  double v1[4] = {0.0, 0.0, 0.0, 0.0}, e1G = 0.0, e1R = 0.0;
+  int evals = 0;
+  for (int s = 0; s < m0; s += 2) {
+    const int s2 = s + 1 < m0 ? s + 1 : s;
+    double vA[4], vB[4], eGA, eRA, eGB, eRB;
+    gk15_pair_warp(s * h0, s == m0 - 1 ? L : (s + 1) * h0, s2 * h0, s2 == m0 - 1 ? L : (s2 + 1) * h0, r, z, vA, eGA,
+                   eRA, vB, eGB, eRB);
+    ++evals;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cg[q] += vA[q] + (s2 != s ? vB[q] : 0.0);
+    if (s == 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v1[q] = vA[q];
+      e1G = eGA;
+      e1R = eRA;
+    }
+  }
+  const double tolG = fmax(atol, rtol * hypot(cg[0], cg[1]));
+  const double tolR = fmax(atol, rtol * hypot(cg[2], cg[3]));
+  double tot[4] = {0.0, 0.0, 0.0, 0.0};
+  int top = 0;
+  auto push = [&](double a, double b, const double v[4], double eG, double eR) {
+    if (lane == 0) {
+      double* e = sw + 8 * top;
+      e[0] = a; e[1] = b; e[2] = v[0]; e[3] = v[1]; e[4] = v[2]; e[5] = v[3]; e[6] = eG; e[7] = eR;
+    }
+    ++top;
+  };
+  for (int s = 0; s < m0; s += 2) {
+    const int s2 = s + 1 < m0 ? s + 1 : s;
+    if (m0 == 1) {
+      push(0.0, L, v1, e1G, e1R);
+    } else {
+      double vA[4], vB[4], eGA, eRA, eGB, eRB;
+      const double aA = s * h0, bA = s == m0 - 1 ? L : (s + 1) * h0;
+      const double aB = s2 * h0, bB = s2 == m0 - 1 ? L : (s2 + 1) * h0;
+      gk15_pair_warp(aA, bA, aB, bB, r, z, vA, eGA, eRA, vB, eGB, eRB);
+      ++evals;
+      if (s2 != s) push(aB, bB, vB, eGB, eRB);
+      push(aA, bA, vA, eGA, eRA);
+    }
+    __syncwarp();
+    while (top > 0) {
+      --top;
+      const double* e = sw + 8 * top;
+      const double a = e[0], b = e[1], eG = e[6], eR = e[7];
+      const double v[4] = {e[2], e[3], e[4], e[5]};
+      __syncwarp();  // every lane has read the entry before it can be overwritten
+      const double frac = (b - a) / L;
+      if ((eG <= tolG * frac && eR <= tolR * frac) || top + 2 > kGKWarpStack || evals + 1 > kGKMaxEvals) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tot[q] += v[q];
+        continue;
+      }
+      const double mid = 0.5 * (a + b);
+      double vA[4], vB[4], eGA, eRA, eGB, eRB;
+      gk15_pair_warp(a, mid, mid, b, r, z, vA, eGA, eRA, vB, eGB, eRB);
+      ++evals;
+      push(mid, b, vB, eGB, eRB);
+      push(a, mid, vA, eGA, eRA);  // the left half is refined first
+      __syncwarp();
+    }
+  }
+  G = make_double2(4.0 * tot[0], 4.0 * tot[1]);
+  Gr = make_double2(4.0 * tot[2], 4.0 * tot[3]);
+}
+
 // both_greens_and_gradient_greens(::ExactGuevelDelhommeau) with
 // with_reduced_coordinates_derivative (exact_Guevel_Delhommeau.jl:52-59;
 // abstract_greens_function.jl:215-260); outputs already multiplied by the area

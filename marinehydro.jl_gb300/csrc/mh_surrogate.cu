@@ -50,16 +50,25 @@ __device__ __forceinline__ void sample_point(uint64_t seed, uint64_t q, uint64_t
   z = -50.0 * u01(h2);
 }
 
-__global__ void surrogate_samples_kernel(uint64_t seed, int64_t M, int64_t offset, int64_t count, double rtol,
-                                         double atol, float2* __restrict__ X, float* __restrict__ Y8,
-                                         double* __restrict__ R2) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= count) return;
+constexpr int kSampleWarps = 4;
+
+// one warp per sample (the exact kernel's warp-cooperative quadrature); lane 0 writes
+__global__ void __launch_bounds__(32 * kSampleWarps) surrogate_samples_kernel(uint64_t seed, int64_t M,
+                                                                               int64_t offset, int64_t count,
+                                                                               double rtol, double atol,
+                                                                               float2* __restrict__ X,
+                                                                               float* __restrict__ Y8,
+                                                                               double* __restrict__ R2) {
+  __shared__ double sw[kSampleWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5;
+  const int64_t t = blockIdx.x * (int64_t)kSampleWarps + warp;
+  if (t >= count) return;  // warp-uniform
   const int64_t q = offset + t;
   double r, z;
   sample_point(seed, (uint64_t)q, (uint64_t)M, r, z);
-  const double2 G = egd_adaptive<false>(r, z, rtol, atol);
-  const double2 Gr = egd_adaptive<true>(r, z, rtol, atol);
+  double2 G, Gr;
+  egd_warp(r, z, rtol, atol, sw[warp], G, Gr);
+  if ((threadIdx.x & 31) != 0) return;
   double2 GF, Gh, Gv;
   wu_wave_term_and_derivs(r, z, GF, Gh, Gv);
   const double d = sqrt(r * r + z * z);
@@ -275,20 +284,25 @@ __global__ void round_bf16_kernel(const float* __restrict__ in, float* __restric
   out[p] = p < count ? __bfloat162float(__float2bfloat16_rn(in[p])) : 0.0f;
 }
 
-// surrogate GF, Gh, Gv at points (r, z) (the layout of the Wu point evaluator); points
-// outside the training box take the exact kernel, as in assembly
-__global__ void __launch_bounds__(64) surrogate_points_kernel(const float* __restrict__ mlp, int64_t m,
-                                                              const double* __restrict__ r,
-                                                              const double* __restrict__ z, double rtol,
-                                                              double atol, double2* __restrict__ out) {
+// surrogate GF, Gh, Gv at points (r, z) (the layout of the Wu point evaluator), one warp per
+// point; points outside the training box take the exact kernel (warp-cooperative, as in
+// assembly), inside it lane 0 evaluates the Wu terms and the network
+__global__ void __launch_bounds__(32 * kSampleWarps) surrogate_points_kernel(const float* __restrict__ mlp, int64_t m,
+                                                                              const double* __restrict__ r,
+                                                                              const double* __restrict__ z,
+                                                                              double rtol, double atol,
+                                                                              double2* __restrict__ out) {
   extern __shared__ float4 spp4[];
+  __shared__ double sw[kSampleWarps][8 * kGKWarpStack];
   load_params(spp4, mlp);
   __syncthreads();
-  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q >= m) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t q = blockIdx.x * (int64_t)kSampleWarps + warp;
+  if (q >= m) return;  // warp-uniform
   const double rq = r[q], zq = z[q];
   double2 GF, Gh, Gv;
   if (surrogate_in_box(rq, zq)) {
+    if (lane != 0) return;
     wu_wave_term_and_derivs(rq, zq, GF, Gh, Gv);
     double2 dG, dGr, dGz;
     surrogate_correction(reinterpret_cast<const float*>(spp4), rq, zq, dG, dGr, dGz);
@@ -296,8 +310,8 @@ __global__ void __launch_bounds__(64) surrogate_points_kernel(const float* __res
     Gh = zadd(Gh, dGr);
     Gv = zadd(Gv, dGz);
   } else {
-    GF = egd_adaptive<false>(rq, zq, rtol, atol);
-    Gh = egd_adaptive<true>(rq, zq, rtol, atol);
+    egd_warp(rq, zq, rtol, atol, sw[warp], GF, Gh);
+    if (lane != 0) return;
     Gv = make_double2(GF.x + 2.0 / hypot(rq, zq), GF.y);
   }
   out[3 * q] = GF;
@@ -313,8 +327,8 @@ void launch_surrogate_samples(cudaStream_t st, LaunchCounter lc, uint64_t seed, 
                               int64_t count, double rtol, double atol, float2* X, float* Y8, double* R2) {
   if (count <= 0) return;
   MH_LAUNCH(lc, st, "surrogate_samples",
-            surrogate_samples_kernel<<<(unsigned)((count + 63) / 64), 64, 0, st>>>(seed, M, offset, count, rtol,
-                                                                                  atol, X, Y8, R2));
+            surrogate_samples_kernel<<<(unsigned)((count + kSampleWarps - 1) / kSampleWarps), 32 * kSampleWarps, 0,
+                                       st>>>(seed, M, offset, count, rtol, atol, X, Y8, R2));
 }
 
 void launch_mlp_loss_grad(cudaStream_t st, LaunchCounter lc, const float* qparams, const float2* X, const float* Y8,
@@ -350,7 +364,8 @@ void launch_surrogate_points(cudaStream_t st, LaunchCounter lc, const float* mlp
   if (m <= 0) return;
   const size_t psmem = sizeof(float) * kMlpParamsPadded;
   MH_LAUNCH(lc, st, "surrogate_points",
-            surrogate_points_kernel<<<(unsigned)((m + 63) / 64), 64, psmem, st>>>(mlp, m, r, z, rtol, atol, out));
+            surrogate_points_kernel<<<(unsigned)((m + kSampleWarps - 1) / kSampleWarps), 32 * kSampleWarps, psmem,
+                                      st>>>(mlp, m, r, z, rtol, atol, out));
 }
 
 }  // namespace mh
