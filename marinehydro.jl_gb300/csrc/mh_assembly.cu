@@ -20,6 +20,7 @@
 #include "mh_greens.cuh"
 #include "mh_internal.cuh"
 #include "mh_mlp.cuh"
+#include "mh_tc.cuh"
 
 namespace mh {
 
@@ -364,6 +365,201 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Surrogate wave assembly with the network's two 64 x 64 layers on the tensor cores.
+//
+// The CTA's 128 threads own 128 rows i; for each of its kColsPerCta columns j the 128 pairs
+// (i, j) form one M = 128 batch: every thread evaluates its pair's Wu terms (FP64) and the
+// first layer (2 -> 64, CUDA cores) into row i of a BF16 activation tile in shared memory,
+// thread 0 issues tcgen05.mma (M = 128, N = 64, K = 64 in four K = 16 steps) against the
+// BF16 weight tile, the FP32 result lands in tensor memory, and each thread reads its row
+// back (tcgen05.ld), applies bias and tanh, and writes the next layer's activations; the
+// last layer (64 -> 6, of which outputs 0 and 2 are used) runs on the CUDA cores.
+// Shared memory: W2, W3 (64 x 64 BF16, 8 KB each), the activation tile (128 x 64 BF16,
+// 16 KB), and the FP32 first/last-layer parameters.  Tensor memory: 64 columns.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 64;                  // TMEM columns (FP32 accumulator, N = 64)
+constexpr uint32_t kTcWaitPolls = 1u << 24;       // bounded mbarrier wait
+constexpr int kTcSmemW2 = 0, kTcSmemW3 = 8192, kTcSmemA = 16384, kTcSmemF = 32768;
+constexpr int kTcSmemFloats = 128 + 64 + 64 + 64 + 128 + 2;  // W1, b1, b2, b3, W4 rows 0 and 2, b4[0], b4[2]
+constexpr int kTcSmemBytes = kTcSmemF + 4 * kTcSmemFloats;
+
+template <bool DIRECT>
+__device__ __forceinline__ void wu_to_wave_terms(double hh, double k, double dx1, double dx2, double2 GF, double2 Gh,
+                                                 double2 Gv, WaveTerms& w) {
+  double dr1 = 0.0, dr2 = 0.0;
+  if (fabs(hh) > 1e-6) {
+    dr1 = k * k / hh * dx1;
+    dr2 = k * k / hh * dx2;
+  }
+  w.I = make_double2(k * GF.x, k * GF.y);
+  w.gh[0] = make_double2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
+  w.gh[1] = make_double2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));
+  w.gz = make_double2(k * (k * Gv.x), k * (k * Gv.y));
+}
+
+template <bool DIRECT>
+__global__ void __launch_bounds__(kTcRows) wave_kernel_tc(AssemblyParams p, const double* __restrict__ SR,
+                                                          const double* __restrict__ DR,
+                                                          const double* __restrict__ ks, double2* __restrict__ S,
+                                                          double2* __restrict__ D, int64_t sstride,
+                                                          int wave_identity) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ PanelRec sp[kColsPerCta];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int64_t n = p.n;
+  const int64_t i0 = blockIdx.x * (int64_t)kTcRows;
+  const int64_t j0 = blockIdx.y * (int64_t)kColsPerCta;
+  if (i0 > j0 + kColsPerCta - 1) return;  // tile strictly below the diagonal (whole CTA)
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int64_t i = i0 + tid;
+  const double k = ks[blockIdx.z];
+  double2* Sb = S + blockIdx.z * sstride;
+  double2* Db = D + blockIdx.z * sstride;
+  unsigned char* W2s = tsm + kTcSmemW2;
+  unsigned char* W3s = tsm + kTcSmemW3;
+  unsigned char* As = tsm + kTcSmemA;
+  float* F = reinterpret_cast<float*>(tsm + kTcSmemF);
+  float* W1f = F;            // 64 x 2
+  float* b1f = F + 128;
+  float* b2f = F + 192;
+  float* b3f = F + 256;
+  float* W4f = F + 320;      // rows 0 and 2 of W4, 2 x 64
+  float* b4f = F + 448;      // b4[0], b4[2]
+  stage_panels(sp, p.P, j0, n);
+  // weights: W2, W3 as BF16 in the canonical K-major layout (row = output, K = input)
+  for (int q = tid; q < kMlpH * kMlpH; q += kTcRows) {
+    const int r = q / kMlpH, c = q % kMlpH;
+    *reinterpret_cast<__nv_bfloat16*>(W2s + tc::kmajor_offset(r, c, kMlpH)) = __float2bfloat16_rn(p.mlp[kMlpW2 + q]);
+    *reinterpret_cast<__nv_bfloat16*>(W3s + tc::kmajor_offset(r, c, kMlpH)) = __float2bfloat16_rn(p.mlp[kMlpW3 + q]);
+  }
+  for (int q = tid; q < 128; q += kTcRows) W1f[q] = p.mlp[kMlpW1 + q];
+  for (int q = tid; q < 64; q += kTcRows) {
+    b1f[q] = p.mlp[kMlpB1 + q];
+    b2f[q] = p.mlp[kMlpB2 + q];
+    b3f[q] = p.mlp[kMlpB3 + q];
+    W4f[q] = p.mlp[kMlpW4 + 0 * kMlpH + q];
+    W4f[64 + q] = p.mlp[kMlpW4 + 2 * kMlpH + q];
+  }
+  if (tid == 0) {
+    b4f[0] = p.mlp[kMlpB4 + 0];
+    b4f[1] = p.mlp[kMlpB4 + 2];
+    tc::mbar_init(&mbar, 1);
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kTcCols);
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 TMEM lanes
+  const uint32_t idesc = tc::idesc_bf16_f32(kTcRows, kMlpH);
+  const uint32_t a_base = tc::smem_u32(As), w2_base = tc::smem_u32(W2s), w3_base = tc::smem_u32(W3s);
+  const bool row_ok = i < n;
+  double ci[3] = {0, 0, 0}, ni[3] = {0, 0, 1};
+  double ai = 0.0;
+  if (row_ok) {
+    for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
+    ai = p.P[i].area;
+  }
+  uint32_t phase = 0;
+  bool timed_out = false;
+  const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  for (int jj = 0; jj < jmax && !timed_out; ++jj) {
+    const int64_t j = j0 + jj;
+    const bool active = row_ok && i <= j;
+    const PanelRec& Pj = sp[jj];
+    double hh = 1.0, vv = -1.0;
+    double2 GF = make_double2(0, 0), Gh = GF, Gv = GF;
+    if (active) {
+      reduced_coords(ci, Pj.c, k, hh, vv);
+      wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+    }
+    // first layer (CUDA cores) -> BF16 activation row `tid`
+    float u, v;
+    mlp_inputs(fmax(hh, kSurrRMin), fmax(vv, kSurrZMin), u, v);
+#pragma unroll 8
+    for (int q = 0; q < kMlpH; ++q) {
+      const float h = tanh_fast(fmaf(W1f[2 * q], u, fmaf(W1f[2 * q + 1], v, b1f[q])));
+      *reinterpret_cast<__nv_bfloat16*>(As + tc::kmajor_offset(tid, q, kMlpH)) = __float2bfloat16_rn(h);
+    }
+    float y0 = b4f[0], y2 = b4f[1];
+    for (int layer = 0; layer < 2 && !timed_out; ++layer) {
+      // make the activation tile visible to the tensor cores, then one thread issues
+      tc::fence_proxy_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t w_base = layer == 0 ? w2_base : w3_base;
+#pragma unroll
+        for (int kk = 0; kk < kMlpH / 16; ++kk) {
+          const uint64_t ad = tc::smem_desc(a_base + kk * 256, 128, (kMlpH / 8) * 128);
+          const uint64_t bd = tc::smem_desc(w_base + kk * 256, 128, (kMlpH / 8) * 128);
+          tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+        }
+        tc::mma_commit(&mbar);
+      }
+      const bool ok = tc::mbar_wait(&mbar, phase, kTcWaitPolls);
+      phase ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        timed_out = true;
+        break;
+      }
+      tc::fence_after_sync();
+      const float* bl = layer == 0 ? b2f : b3f;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float acc[32];
+        tc::tmem_ld32(trow + half * 32, acc);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int c = half * 32 + q;
+          const float h = tanh_fast(acc[q] + bl[c]);
+          if (layer == 0) {
+            *reinterpret_cast<__nv_bfloat16*>(As + tc::kmajor_offset(tid, c, kMlpH)) = __float2bfloat16_rn(h);
+          } else {
+            y0 = fmaf(W4f[c], h, y0);
+            y2 = fmaf(W4f[64 + c], h, y2);
+          }
+        }
+      }
+    }
+    if (timed_out) break;
+    // all TMEM reads of this batch are done before the next batch's MMA overwrites it
+    tc::fence_before_sync();
+    __syncthreads();
+    if (!active) continue;
+    const bool in_box = surrogate_in_box(hh, vv) && i != j;
+    if (in_box) {
+      double2 dG, dGr, dGz;
+      surrogate_apply(y0, y2, hh, vv, dG, dGr, dGz);
+      GF = zadd(GF, dG);
+      Gh = zadd(Gh, dGr);
+      Gv = zadd(Gv, dGz);
+    } else {
+      // outside the training box, and the self pairs: queued for the exact kernel
+      const unsigned long long slot = atomicAdd(p.fb_state, 1ull);
+      if ((int64_t)slot < p.fb_cap) p.fb_list[slot] = make_int4((int)i, (int)j, (int)blockIdx.z, 0);
+    }
+    const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+    const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+    WaveTerms w;
+    wu_to_wave_terms<DIRECT>(hh, k, dx1, dx2, GF, Gh, Gv, w);
+    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
+  }
+  if (timed_out) {
+    // reported by the host as a timeout; let the MMAs in flight finish (bounded) before the
+    // tensor memory is released
+    if (tid == 0) atomicExch(p.fb_state + 2, 1ull);
+    tc::mbar_wait(&mbar, phase ^ 1u, kTcWaitPolls);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTcCols);
+}
+
 // The exact Delhommeau terms of one unordered pair {i, j} at wavenumber k, computed by the
 // whole warp (egd_warp); lane 0 writes both S/D entries.
 template <bool DIRECT>
@@ -523,11 +719,11 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
   if (wv & MH_GF_SURROGATE) {
     // Wu + learned correction; pairs outside the training box are queued and then
     // recomputed by the exact kernel (the caller validates that no other wave kind is set)
-    const size_t smem = sizeof(float) * kMlpParamsPadded;
     lc.pre(st);
     cudaMemsetAsync(p.fb_state, 0, sizeof(unsigned long long), st);
-    if (p.direct) wave_kernel<true, 4><<<grid, kRowsPerCta, smem, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
-    else wave_kernel<false, 4><<<grid, kRowsPerCta, smem, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    static_assert(kTcRows == kRowsPerCta, "tensor-core tile rows");
+    if (p.direct) wave_kernel_tc<true><<<grid, kTcRows, kTcSmemBytes, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
+    else wave_kernel_tc<false><<<grid, kTcRows, kTcSmemBytes, st>>>(p, SR, DR, ks_dev, S, D, sstride, wave_identity);
     lc.post(st, "assemble_wave_surrogate");
     lc.pre(st);
     const int fbg = 8 * 152;

@@ -259,17 +259,19 @@ int prepare_surrogate(mh_context* ctx, AssemblyParams& p, int64_t nk) {
   p.mlp = ctx->mlp;
   p.fb_cap = std::max<int64_t>((int64_t)1 << 20, p.n * (nk + 64));
   MH_TRY(ws_get_t(ctx, kSlotFb, (size_t)p.fb_cap, &p.fb_list));
-  MH_TRY(ws_get_t(ctx, kSlotFbState, 2, &p.fb_state));
-  MH_CUDA(ctx, cudaMemsetAsync(p.fb_state, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  MH_TRY(ws_get_t(ctx, kSlotFbState, 4, &p.fb_state));
+  MH_CUDA(ctx, cudaMemsetAsync(p.fb_state, 0, 4 * sizeof(unsigned long long), ctx->stream));
   return MH_OK;
 }
 
 // after a synchronisation: did any surrogate launch queue more pairs than the list holds?
 int check_surrogate(mh_context* ctx, const AssemblyParams& p) {
   if (!(p.gfs & MH_GF_SURROGATE)) return MH_OK;
-  unsigned long long st[2] = {0, 0};
+  unsigned long long st[3] = {0, 0, 0};
   MH_CUDA(ctx, cudaMemcpyAsync(st, p.fb_state, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
   MH_TRY(sync(ctx, "surrogate state"));
+  if (st[2])
+    return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the surrogate assembly gave up");
   if (st[1])
     return fail(ctx, MH_ERR_UNSUPPORTED, "more than %lld panel pairs per launch lie outside the surrogate's training "
                                          "box; use ExactGuevelDelhommeau for this mesh", (long long)p.fb_cap);

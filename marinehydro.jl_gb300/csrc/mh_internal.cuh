@@ -80,7 +80,8 @@ struct AssemblyParams {
   // of pairs outside its training box that the exact kernel recomputes
   const float* mlp;
   int4* fb_list;                 // (i, j, wavenumber index, 0), i <= j
-  unsigned long long* fb_state;  // [0] entries appended by the current launch, [1] sticky overflow
+  unsigned long long* fb_state;  // [0] entries appended by the current launch, [1] sticky overflow,
+                                 // [2] sticky tensor-core wait timeout
   int64_t fb_cap;
 };
 

@@ -20,6 +20,7 @@
 // and not applied.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace mh {
@@ -46,13 +47,18 @@ __device__ __forceinline__ float tanh_fast(float x) {
   return y;
 }
 
+// the hidden activations that feed a 64 x 64 layer are BF16 (the tensor cores' operand
+// type); all paths (training, point evaluation, tensor-core assembly) round them alike
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
 __device__ __forceinline__ void mlp_inputs(double r, double z, float& u, float& v) {
   u = (float)(log10(r) * (1.0 / 3.0));
   v = (float)(z * (1.0 / 25.0) + 1.0);
 }
 
-// one dense tanh layer of 64 outputs from `nin` inputs held in registers
-template <int NIN>
+// one dense tanh layer of 64 outputs from `nin` inputs held in registers; ROUND: the outputs
+// are rounded to BF16 (they feed a 64 x 64 layer)
+template <int NIN, bool ROUND>
 __device__ __forceinline__ void mlp_layer_tanh(const float* __restrict__ W, const float* __restrict__ b,
                                                const float (&x)[NIN], float (&y)[kMlpH]) {
 #pragma unroll
@@ -72,7 +78,7 @@ __device__ __forceinline__ void mlp_layer_tanh(const float* __restrict__ W, cons
 #pragma unroll
       for (int i = 0; i < NIN; ++i) acc = fmaf(W[j * NIN + i], x[i], acc);
     }
-    y[j] = tanh_fast(acc);
+    y[j] = ROUND ? bf16r(tanh_fast(acc)) : tanh_fast(acc);
   }
 }
 
@@ -81,9 +87,9 @@ __device__ __forceinline__ void mlp_layer_tanh(const float* __restrict__ W, cons
 __device__ __forceinline__ void mlp_forward(const float* __restrict__ P, float u, float v, float (&out)[kMlpOut]) {
   const float x[kMlpIn] = {u, v};
   float h1[kMlpH], h2[kMlpH];
-  mlp_layer_tanh<kMlpIn>(P + kMlpW1, P + kMlpB1, x, h1);
-  mlp_layer_tanh<kMlpH>(P + kMlpW2, P + kMlpB2, h1, h2);
-  mlp_layer_tanh<kMlpH>(P + kMlpW3, P + kMlpB3, h2, h1);
+  mlp_layer_tanh<kMlpIn, true>(P + kMlpW1, P + kMlpB1, x, h1);
+  mlp_layer_tanh<kMlpH, true>(P + kMlpW2, P + kMlpB2, h1, h2);
+  mlp_layer_tanh<kMlpH, false>(P + kMlpW3, P + kMlpB3, h2, h1);
   const float4* w4 = reinterpret_cast<const float4*>(P + kMlpW4);
 #pragma unroll
   for (int q = 0; q < kMlpOut; ++q) {
@@ -100,6 +106,16 @@ __device__ __forceinline__ void mlp_forward(const float* __restrict__ P, float u
   }
 }
 
+// the correction from the network outputs y0 (Re dG) and y2 (Re dGr) at (r, z)
+__device__ __forceinline__ void surrogate_apply(float y0, float y2, double r, double z, double2& dG, double2& dGr,
+                                                double2& dGz) {
+  const double d = sqrt(r * r + z * z);
+  const double inv = 1.0 / ((1.0 + d) * (1.0 + d));
+  dG = make_double2(y0 * inv, 0.0);
+  dGr = make_double2(y2 * inv * (r / (1.0 + r)), 0.0);
+  dGz = dG;
+}
+
 // the surrogate's correction to the Wu terms at (r, z): dGF, dGh, dGv (complex) to add
 // to wu_wave_term_and_derivs' GF, Gh, Gv.  Below r = 1e-3 the network is read at
 // r = 1e-3: the remainder is even in r (its r-derivative vanishes like r), so its
@@ -110,11 +126,7 @@ __device__ __forceinline__ void surrogate_correction(const float* __restrict__ P
   float u, v, y[kMlpOut];
   mlp_inputs(fmax(r, kSurrRMin), z, u, v);
   mlp_forward(P, u, v, y);
-  const double d = sqrt(r * r + z * z);
-  const double inv = 1.0 / ((1.0 + d) * (1.0 + d));
-  dG = make_double2(y[0] * inv, 0.0);
-  dGr = make_double2(y[2] * inv * (r / (1.0 + r)), 0.0);
-  dGz = dG;
+  surrogate_apply(y[0], y[2], r, z, dG, dGr, dGz);
 }
 
 // where the surrogate is used: r up to the top of the training box (below it, see

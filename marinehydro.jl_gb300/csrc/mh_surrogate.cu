@@ -10,7 +10,8 @@
 // and the Wu fits (wu_wave_term_and_derivs).
 //
 // Training step (batch B, one thread per sample):
-//   mlp_fwd_bwd_kernel: forward with the BF16-rounded parameters, mean-squared
+//   mlp_fwd_bwd_kernel: forward with the BF16-rounded parameters (and BF16 activations into
+//     the 64 x 64 layers, as the tensor-core assembly computes them), mean-squared
 //     error, and back-propagation of the per-sample deltas (stored feature-major);
 //   mlp_wgrad_kernel:   weight gradients dW = sum_b delta_b a_b^T per layer (chunks
 //     of 256 samples staged in shared memory, atomically summed);
@@ -136,7 +137,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_fwd_bwd_kernel(const float*
   __syncthreads();
   // forward: ha = h1, hb = h2, ha = h3
   for (int j = 0; j < kMlpH; ++j) {
-    const float v = tanh_fast(fmaf(P[kMlpW1 + 2 * j], x.x, fmaf(P[kMlpW1 + 2 * j + 1], x.y, P[kMlpB1 + j])));
+    const float v = bf16r(tanh_fast(fmaf(P[kMlpW1 + 2 * j], x.x, fmaf(P[kMlpW1 + 2 * j + 1], x.y, P[kMlpB1 + j]))));
     ha[j * kTrainThreads + t] = v;
     if (active) H1[j * Bl + b] = v;
   }
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_fwd_bwd_kernel(const float*
     float acc = P[kMlpB2 + j];
 #pragma unroll 16
     for (int i = 0; i < kMlpH; ++i) acc = fmaf(P[kMlpW2 + j * kMlpH + i], ha[i * kTrainThreads + t], acc);
-    const float v = tanh_fast(acc);
+    const float v = bf16r(tanh_fast(acc));
     hb[j * kTrainThreads + t] = v;
     if (active) H2[j * Bl + b] = v;
   }
