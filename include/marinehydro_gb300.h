@@ -73,9 +73,16 @@ typedef enum {
    (the reference's arithmetic).  MH_PREC_MIXED: LU factors in FP32 with FP64
    partial pivoting decisions on FP32 data, then FP64 iterative refinement of
    every right-hand side to a backward error below 1e-14 (falls back to FP64 LU
-   when refinement stalls). */
+   when refinement stalls).  MH_PREC_FP64_TC: the FP64 LU with its trailing
+   update on the BF16 tensor cores by Ozaki splitting (each row / column scaled
+   by a power of two, cut into eight 7-bit digits, digit products summed exactly
+   in FP32 and recombined in 64-bit integers): FP64 results to within the
+   rounding of the row and column scales; panel, pivoting and substitution as
+   MH_PREC_FP64.  Accepted by mh_linsolve, mh_solve, mh_linsolve_adjoint and
+   mh_hydrodynamic_coefficients. */
 #define MH_PREC_FP64 0
 #define MH_PREC_MIXED 1
+#define MH_PREC_FP64_TC 2
 
 typedef struct mh_context mh_context;
 typedef struct mh_mesh mh_mesh;

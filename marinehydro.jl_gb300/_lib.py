@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(PKG_DIR, "_build", "libmarinehydro_cuda.so")
 MH_OK, MH_ERR_ARG, MH_ERR_UNSUPPORTED, MH_ERR_SINGULAR, MH_ERR_CUDA, MH_ERR_TIMEOUT, MH_ERR_NOT_CONVERGED, \
     MH_ERR_NOMEM = range(8)
 MH_MEM_HOST, MH_MEM_DEVICE = 0, 1
-MH_PREC_FP64, MH_PREC_MIXED = 0, 1
+MH_PREC_FP64, MH_PREC_MIXED, MH_PREC_FP64_TC = 0, 1, 2
 
 GF_RANKINE = 1
 GF_RANKINE_REFLECTED = 2

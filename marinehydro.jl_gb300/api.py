@@ -35,7 +35,9 @@ def _prec(precision):
         return _lib.MH_PREC_FP64
     if precision in ("mixed", _lib.MH_PREC_MIXED):
         return _lib.MH_PREC_MIXED
-    raise ValueError('precision must be "fp64" or "mixed"')
+    if precision in ("fp64_tc", _lib.MH_PREC_FP64_TC):
+        return _lib.MH_PREC_FP64_TC
+    raise ValueError('precision must be "fp64", "mixed" or "fp64_tc"')
 
 
 # ---------------------------------------------------------------------------

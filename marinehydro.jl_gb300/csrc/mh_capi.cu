@@ -101,7 +101,7 @@ namespace {
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
   kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
-  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotCount
+  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...) {
@@ -415,6 +415,20 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
     MH_TRY(check_launch(ctx, "lu factor"));
     lu_solve_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, X, nrhs, xstride, adjoint);
     MH_TRY(check_launch(ctx, "lu solve"));
+  } else if (precision == MH_PREC_FP64_TC) {
+    unsigned char* ws;
+    const size_t wsb = ozaki_workspace_bytes(n, d.batch);
+    MH_TRY(ws_get_t(ctx, kSlotOzaki, wsb + 256, &ws));
+    int* flag = reinterpret_cast<int*>(ws + wsb);
+    MH_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+    lu_factor_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, info, ws, flag);
+    MH_TRY(check_launch(ctx, "lu factor (tensor-core update)"));
+    lu_solve_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, X, nrhs, xstride, adjoint);
+    MH_TRY(check_launch(ctx, "lu solve"));
+    int hflag = 0;
+    MH_CUDA(ctx, cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MH_TRY(sync(ctx, "tensor-core update"));
+    if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
   } else {
     float2* LU32;
     MH_TRY(factor_mixed(ctx, d, Adev, &LU32));
@@ -838,7 +852,7 @@ int mh_linsolve(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const
   if (!ctx) return MH_ERR_ARG;
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!A || !B || !X) return fail(ctx, MH_ERR_ARG, "A, B and X must not be NULL");
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
@@ -859,7 +873,7 @@ int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* 
   if (!ctx) return MH_ERR_ARG;
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!A || !Ybar || !Lambda) return fail(ctx, MH_ERR_ARG, "A, Ybar and Lambda must not be NULL");
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
@@ -881,7 +895,7 @@ int mh_solve(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const do
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!D || !S || !bc || !phi) return fail(ctx, MH_ERR_ARG, "D, S, bc and phi must not be NULL");
   if (!direct && !sources) return fail(ctx, MH_ERR_ARG, "the indirect method needs a `sources` buffer");
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
@@ -926,7 +940,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
   if (n_rad + n_beta == 0) return fail(ctx, MH_ERR_ARG, "nothing to solve: no radiating dof and no wave direction");
   if ((n_rad > 0 || n_inf > 0) && (!dofs || n_dofs <= 0)) return fail(ctx, MH_ERR_ARG, "dof fields required");
   MH_TRY(check_gfs(ctx, gfs));
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
   for (int64_t w = 0; w < n_omega; ++w)

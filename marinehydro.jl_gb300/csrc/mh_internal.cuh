@@ -125,7 +125,12 @@ struct BatchDesc {
 };
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
-                      int32_t* ipiv, int32_t* info);
+                      int32_t* ipiv, int32_t* info, void* emu_ws = nullptr, int* emu_flag = nullptr);
+// FP64 trailing update A22 -= L21 U12 of panel step k on the BF16 tensor cores (mh_ozaki.cu);
+// emu_ws: ozaki_workspace_bytes(n, batch) bytes; *timeout_flag set if a completion wait gave up
+size_t ozaki_workspace_bytes(int64_t n, int64_t batch);
+void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
+                           void* ws, int* timeout_flag);
 template <typename T>
 void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
                       const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,

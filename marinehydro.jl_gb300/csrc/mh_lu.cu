@@ -534,7 +534,7 @@ void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
 
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
-                      int32_t* ipiv, int32_t* info) {
+                      int32_t* ipiv, int32_t* info, void* emu_ws, int* emu_flag) {
   const int64_t n = d.n;
   if (n <= 0 || d.batch <= 0) return 0;
   cudaMemsetAsync(info, 0, sizeof(int32_t) * d.batch, st);
@@ -551,6 +551,12 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     if (rest <= 0) continue;
     dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
     MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
+    if constexpr (sizeof(T) == 8) {
+      if (emu_ws) {  // FP64 update on the BF16 tensor cores (mh_ozaki.cu)
+        ozaki_trailing_update(st, lc, d, A, k, (int)kb, emu_ws, emu_flag);
+        continue;
+      }
+    }
     constexpr int TM = GemmTile<T>::TM;
     dim3 gg((unsigned)((rest + TM - 1) / TM), (unsigned)((rest + TM - 1) / TM), (unsigned)d.batch);
     constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
@@ -594,8 +600,10 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
 }
 
-template int lu_factor_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, double2*, int32_t*, int32_t*);
-template int lu_factor_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, float2*, int32_t*, int32_t*);
+template int lu_factor_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, double2*, int32_t*, int32_t*,
+                                       void*, int*);
+template int lu_factor_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, float2*, int32_t*, int32_t*,
+                                      void*, int*);
 template void lu_solve_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, const double2*,
                                        const int32_t*, double2*, int64_t, int64_t, bool);
 template void lu_solve_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, const float2*, const int32_t*,

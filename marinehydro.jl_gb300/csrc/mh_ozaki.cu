@@ -1,0 +1,277 @@
+// mh_ozaki.cu -- the FP64 complex LU trailing update on the BF16 tensor cores (Ozaki splitting).
+//
+// The blocked LU's update A22 -= L21 U12 (K = 32 complex columns per panel step) is the
+// dominant FP64 work of the plain path, and GB300's FP64 rate is ~1/1500 of its BF16 tensor
+// rate.  Each row i of L21 is scaled by 2^-e_i (e_i: the exponent of the row's largest
+// |re|, |im|) and each column j of U12 by 2^-f_j; a scaled value is rounded to a 55-bit
+// fixed-point integer (54 significant bits for the row's largest entry, more than FP64's 53)
+// and cut into eight balanced base-128 digits, each in [-64, 64] and exact in BF16:
+//     x = 2^e sum_p x_p 2^(-7 p - 6),   p = 0 (most significant) .. 7.
+// Then L21 U12 = 2^(e_i + f_j - 12) sum_d 2^(-7 d) T_d with T_d = sum_{p+q=d} X_p Y_q (complex),
+// and every T_d is an integer below 2^21 in magnitude, so the tensor cores accumulate it
+// exactly in FP32 (K = 32, at most 8 digit pairs and 2 real products per complex term).
+// Terms with p + q > 7 are dropped: they are below 2^-55 of the row/column scale product, the
+// size of FP64 rounding.  The T_d are combined exactly in 64-bit integers (d = 0..3 and
+// 4..7 separately, each below 2^43), converted once to FP64, scaled by the power of two and
+// subtracted from A22 -- a handful of FP64 operations per element instead of the 128 FMAs
+// of the FP64 update.
+//
+// Kernels per panel step (all batched over the matrices of the sweep):
+//   ozaki_split_rows: L21 -> digit tiles A[row tile][digit][re/im] (128 x 32 BF16 each, in the
+//     canonical no-swizzle K-major layout) and the row exponents;
+//   ozaki_split_cols: U12 -> digit tiles B[col tile][digit][re/im] (32 x 32 BF16) and the
+//     column exponents;
+//   ozaki_gemm: one CTA per 128 x 32 output tile: 16 + 16 digit tiles in shared memory
+//     (160 KB), 288 tcgen05.mma (M = 128, N = 32, K = 16) into 8 x (Re, Im) FP32 accumulators
+//     filling the 512 TMEM columns, one commit, then the exact integer combination and the
+//     FP64 subtraction.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include "mh_internal.cuh"
+#include "mh_tc.cuh"
+
+namespace mh {
+
+namespace {
+
+constexpr int kOzDigits = 8;
+constexpr int kOzK = 32;            // panel width (the LU's kNB)
+constexpr int kOzRows = 128;        // output rows per CTA (MMA M)
+constexpr int kOzCols = 32;         // output columns per CTA (MMA N)
+constexpr int kOzATile = kOzRows * kOzK * 2;    // bytes of one A digit tile (128 x 32 BF16)
+constexpr int kOzBTile = kOzCols * kOzK * 2;    // bytes of one B digit tile (32 x 32 BF16)
+constexpr int kOzABytes = kOzDigits * 2 * kOzATile;   // 128 KB per row tile
+constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 32 KB per column tile
+constexpr uint32_t kOzTmemCols = 512;
+constexpr uint32_t kOzWaitPolls = 1u << 26;
+
+// exponent e with |v| < 2^e for the largest |v| of a row / column (0 for all-zero)
+__device__ __forceinline__ int scale_exponent(double maxabs) {
+  if (!(maxabs > 0.0)) return 0;
+  int e;
+  frexp(maxabs, &e);
+  return e;
+}
+
+// balanced base-128 digits of round(v 2^(55 - e)), most significant first; |v| < 2^e keeps
+// |X| < 2^55, so the leading digit is in [-64, 64] as well
+__device__ __forceinline__ void digits8(double v, int e, int (&dg)[kOzDigits]) {
+  long long X = llrint(ldexp(v, 55 - e));
+#pragma unroll
+  for (int p = kOzDigits - 1; p > 0; --p) {
+    const long long t = ((X + 64) & 127) - 64;
+    dg[p] = (int)t;
+    X = (X - t) >> 7;
+  }
+  dg[0] = (int)X;
+}
+
+// L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32)
+__global__ void ozaki_split_rows_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k, int kb, int64_t rest,
+                                        int64_t nrt, unsigned char* __restrict__ digA, int* __restrict__ rowexp) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded row of the trailing block
+  const int64_t b = blockIdx.y;
+  if (r >= nrt * kOzRows) return;
+  const int64_t n = d.n;
+  const double2* Ab = A + b * d.stride;
+  const bool live = r < rest;
+  double mx = 0.0;
+  if (live)
+    for (int kk = 0; kk < kb; ++kk) {
+      const double2 v = Ab[(k + kb + r) + (k + kk) * n];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+  const int e = scale_exponent(mx);
+  if (live) rowexp[b * rest + r] = e;
+  unsigned char* tiles = digA + ((b * nrt + r / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
+  const int rr = (int)(r % kOzRows);
+  for (int kk = 0; kk < kOzK; ++kk) {
+    double2 v = make_double2(0.0, 0.0);
+    if (live && kk < kb) v = Ab[(k + kb + r) + (k + kk) * n];
+    int dre[kOzDigits], dim[kOzDigits];
+    digits8(v.x, e, dre);
+    digits8(v.y, e, dim);
+    const uint32_t off = tc::kmajor_offset(rr, kk, kOzK);
+#pragma unroll
+    for (int p = 0; p < kOzDigits; ++p) {
+      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p) * kOzATile + off) = __float2bfloat16_rn((float)dre[p]);
+      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p + 1) * kOzATile + off) = __float2bfloat16_rn((float)dim[p]);
+    }
+  }
+}
+
+// U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1
+__global__ void ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k, int kb, int64_t rest,
+                                        int64_t nct, unsigned char* __restrict__ digB, int* __restrict__ colexp) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded column of the trailing block
+  const int64_t b = blockIdx.y;
+  if (c >= nct * kOzCols) return;
+  const int64_t n = d.n;
+  const double2* Ab = A + b * d.stride;
+  const bool live = c < rest;
+  double mx = 0.0;
+  if (live)
+    for (int kk = 0; kk < kb; ++kk) {
+      const double2 v = Ab[(k + kk) + (k + kb + c) * n];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+  const int e = scale_exponent(mx);
+  if (live) colexp[b * rest + c] = e;
+  unsigned char* tiles = digB + ((b * nct + c / kOzCols) * kOzDigits * 2) * (int64_t)kOzBTile;
+  const int cc = (int)(c % kOzCols);
+  for (int kk = 0; kk < kOzK; ++kk) {
+    double2 v = make_double2(0.0, 0.0);
+    if (live && kk < kb) v = Ab[(k + kk) + (k + kb + c) * n];
+    int dre[kOzDigits], dim[kOzDigits];
+    digits8(v.x, e, dre);
+    digits8(v.y, e, dim);
+    const uint32_t off = tc::kmajor_offset(cc, kk, kOzK);
+#pragma unroll
+    for (int p = 0; p < kOzDigits; ++p) {
+      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p) * kOzBTile + off) = __float2bfloat16_rn((float)dre[p]);
+      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p + 1) * kOzBTile + off) = __float2bfloat16_rn((float)dim[p]);
+    }
+  }
+}
+
+// 2^s as a double, s in the normal range
+__device__ __forceinline__ double pow2(int s) { return __longlong_as_double((long long)(s + 1023) << 52); }
+
+__global__ void __launch_bounds__(kOzRows) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
+                                                              int64_t rest, int64_t nrt, int64_t nct,
+                                                              const unsigned char* __restrict__ digA,
+                                                              const unsigned char* __restrict__ digB,
+                                                              const int* __restrict__ rowexp,
+                                                              const int* __restrict__ colexp,
+                                                              int* __restrict__ timeout_flag) {
+  extern __shared__ __align__(1024) unsigned char osm[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int64_t rt = blockIdx.x, ct = blockIdx.y, b = blockIdx.z;
+  const int64_t n = d.n;
+  unsigned char* As = osm;
+  unsigned char* Bs = osm + kOzABytes;
+  // digit tiles: contiguous kOzABytes / kOzBBytes blocks in global memory
+  {
+    const int4* srcA = reinterpret_cast<const int4*>(digA + (b * nrt + rt) * (int64_t)kOzABytes);
+    const int4* srcB = reinterpret_cast<const int4*>(digB + (b * nct + ct) * (int64_t)kOzBBytes);
+    int4* dA = reinterpret_cast<int4*>(As);
+    int4* dB = reinterpret_cast<int4*>(Bs);
+    for (int q = tid; q < kOzABytes / 16; q += kOzRows) dA[q] = __ldg(srcA + q);
+    for (int q = tid; q < kOzBBytes / 16; q += kOzRows) dB[q] = __ldg(srcB + q);
+  }
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kOzTmemCols);
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16_f32(kOzRows, kOzCols);
+    const uint32_t idesc_neg = tc::idesc_bf16_f32_nega(kOzRows, kOzCols);
+    const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
+    constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
+    for (int dd = 0; dd < kOzDigits; ++dd) {
+      const uint32_t t_re = tmem + (uint32_t)(dd * 2 * kOzCols), t_im = t_re + kOzCols;
+      for (int p = 0; p <= dd; ++p) {
+        const int q = dd - p;
+        const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
+        const uint32_t br = b0 + (uint32_t)(2 * q) * kOzBTile, bi = br + kOzBTile;
+#pragma unroll
+        for (int kk = 0; kk < kOzK / 16; ++kk) {
+          const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
+          const uint32_t first = (p == 0 && kk == 0) ? 0u : 1u;
+          tc::mma_bf16(t_re, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, first);
+          tc::mma_bf16(t_re, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc_neg, 1u);
+          tc::mma_bf16(t_im, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc, first);
+          tc::mma_bf16(t_im, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, 1u);
+        }
+      }
+    }
+    tc::mma_commit(&mbar);
+  }
+  const bool ok = tc::mbar_wait(&mbar, 0, kOzWaitPolls);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) atomicExch(timeout_flag, 1);
+    tc::mbar_wait(&mbar, 0, kOzWaitPolls);  // let the MMAs in flight finish before freeing TMEM
+  } else {
+    tc::fence_after_sync();
+    const int64_t r = rt * kOzRows + tid;  // row of the trailing block
+    const bool row_live = r < rest;
+    const int er = row_live ? rowexp[b * rest + r] : 0;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    double2* Ab = A + b * d.stride;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kOzCols; c0 += 8) {
+      long long hr[8], lr[8], hi[8], li[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { hr[q] = 0; lr[q] = 0; hi[q] = 0; li[q] = 0; }
+#pragma unroll
+      for (int dd = 0; dd < kOzDigits; ++dd) {
+        float vr[8], vi[8];
+        tc::tmem_ld8(trow + (uint32_t)(dd * 2 * kOzCols + c0), vr);
+        tc::tmem_ld8(trow + (uint32_t)(dd * 2 * kOzCols + kOzCols + c0), vi);
+        const int sh = dd < 4 ? 7 * (3 - dd) : 7 * (7 - dd);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const long long tr = (long long)__float2int_rn(vr[q]) << sh;
+          const long long ti = (long long)__float2int_rn(vi[q]) << sh;
+          if (dd < 4) { hr[q] += tr; hi[q] += ti; } else { lr[q] += tr; li[q] += ti; }
+        }
+      }
+      if (row_live) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int64_t c = ct * kOzCols + c0 + q;
+          if (c >= rest) continue;
+          // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
+          const double s = pow2(er + colexp[b * rest + c] - 33);
+          const double xr = fma((double)lr[q], 0x1p-28, (double)hr[q]);
+          const double xi = fma((double)li[q], 0x1p-28, (double)hi[q]);
+          double2* dst = Ab + (k + kb + r) + (k + kb + c) * n;
+          double2 v = *dst;
+          v.x = fma(-xr, s, v.x);
+          v.y = fma(-xi, s, v.y);
+          *dst = v;
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kOzTmemCols);
+}
+
+}  // namespace
+
+size_t ozaki_workspace_bytes(int64_t n, int64_t batch) {
+  const int64_t t = (n + kOzRows - 1) / kOzRows, c = (n + kOzCols - 1) / kOzCols;
+  return (size_t)batch * ((size_t)t * kOzABytes + (size_t)c * kOzBBytes + 2 * sizeof(int) * (size_t)n) + 1024;
+}
+
+void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
+                           void* ws, int* timeout_flag) {
+  const int64_t rest = d.n - k - kb;
+  if (rest <= 0) return;
+  const int64_t nrt = (rest + kOzRows - 1) / kOzRows, nct = (rest + kOzCols - 1) / kOzCols;
+  const int64_t nrt_max = (d.n + kOzRows - 1) / kOzRows, nct_max = (d.n + kOzCols - 1) / kOzCols;
+  unsigned char* digA = static_cast<unsigned char*>(ws);
+  unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
+  int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
+  int* colexp = rowexp + d.batch * d.n;
+  dim3 gr((unsigned)((nrt * kOzRows + 127) / 128), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_rows_kernel<<<gr, 128, 0, st>>>(d, A, k, kb, rest, nrt, digA, rowexp));
+  dim3 gc((unsigned)((nct * kOzCols + 127) / 128), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 128, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
+  const size_t smem = kOzABytes + kOzBBytes;
+  cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 gg((unsigned)nrt, (unsigned)nct, (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_gemm_ozaki",
+            ozaki_gemm_kernel<<<gg, kOzRows, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp,
+                                                          timeout_flag));
+}
+
+}  // namespace mh

@@ -2,8 +2,9 @@
 
 A formulation carries its Green-function tuple; the tuple becomes the bit set the
 C-ABI takes (MH_GF_*).  `precision` selects the linear-solve arithmetic of the
-GPU path: "fp64" (the reference's arithmetic) or "mixed" (FP32 LU factors with
-FP64 iterative refinement to FP64 accuracy).
+GPU path: "fp64" (the reference's arithmetic), "mixed" (FP32 LU factors with
+FP64 iterative refinement to FP64 accuracy) or "fp64_tc" (the FP64 LU with its
+trailing update on the BF16 tensor cores by Ozaki splitting).
 """
 from __future__ import annotations
 
@@ -116,13 +117,13 @@ class BEMFormulation:
             greens = default_greens_functions(greens)
         self.greens = tuple(greens) if not isinstance(greens, GreensFunction) else (greens,)
         gf_flags(self.greens)
-        if precision not in ("fp64", "mixed"):
-            raise ValueError('precision must be "fp64" or "mixed"')
+        if precision not in ("fp64", "mixed", "fp64_tc"):
+            raise ValueError('precision must be "fp64", "mixed" or "fp64_tc"')
         self.precision = precision
 
     @property
     def precision_code(self) -> int:
-        return _lib.MH_PREC_FP64 if self.precision == "fp64" else _lib.MH_PREC_MIXED
+        return {"fp64": _lib.MH_PREC_FP64, "mixed": _lib.MH_PREC_MIXED, "fp64_tc": _lib.MH_PREC_FP64_TC}[self.precision]
 
     def __repr__(self):
         return f"{type(self).__name__}({self.greens!r}, precision={self.precision!r})"

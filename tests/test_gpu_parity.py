@@ -134,7 +134,7 @@ def _well_conditioned(n, nrhs, seed):
 
 
 @pytest.mark.parametrize("n,nrhs", [(1, 1), (7, 3), (33, 1), (64, 2), (200, 7), (531, 9)])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
 def test_linsolve(mh, ctx, n, nrhs, precision):
     A, B = _well_conditioned(n, nrhs, n)
     X = mh.linsolve(A, B, precision=precision, ctx=ctx)
@@ -252,3 +252,19 @@ def test_config2_scale_properties(mh, oracle, ctx):
         X = mh.linsolve(D, B, precision=precision, ctx=ctx)
         r = np.linalg.norm(D @ X - B) / (np.linalg.norm(D) * np.linalg.norm(X))
         assert r < 1e-15
+
+
+@pytest.mark.parametrize("direct", [True, False])
+def test_sweep_tensor_core_fp64_update(mh, ctx, direct):
+    """The FP64 LU with its trailing update on the BF16 tensor cores (Ozaki splitting) gives
+    the FP64 path's coefficients to FP64 rounding (two panel steps and ragged tiles: N = 300)."""
+    body = mh.FloatingBody(mh.vertical_cylinder_mesh(2.0, 3.0, 20, 10, 5), ["Heave", "Surge", "Pitch"],
+                           rotation_center=(0.0, 0.0, 0.0))
+    p = {"wave_frequencies": [0.5, 1.1, 2.3], "radiating_dofs": ["Heave", "Surge", "Pitch"],
+         "wave_directions": [0.0, 0.4]}
+    F = mh.DirectBEM if direct else mh.IndirectBEM
+    r64 = mh.hydrodynamic_coefficients(body, p, F(precision="fp64"), ctx=ctx, rho=1025.0)
+    rtc = mh.hydrodynamic_coefficients(body, p, F(precision="fp64_tc"), ctx=ctx, rho=1025.0)
+    for key in ("added_mass", "radiation_damping", "excitation_force"):
+        a, b = rtc[key], r64[key]
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), key
