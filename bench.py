@@ -298,7 +298,8 @@ def run_gpu(args):
 
     if args.profile_only:
         # a small, self-contained case for ncu: W untimed runs + one run, nothing else
-        run = {"cylinder": lambda: step_device(_lib.MH_PREC_MIXED if args.precision == "mixed" else _lib.MH_PREC_FP64),
+        prec = {"fp64": _lib.MH_PREC_FP64, "mixed": _lib.MH_PREC_MIXED, "fp64_tc": _lib.MH_PREC_FP64_TC}[args.precision]
+        run = {"cylinder": lambda: step_device(prec),
                "surrogate": lambda: _profile_case_surrogate(mh, ctx),
                "adjoint": lambda: _profile_case_adjoint(mh, ctx),
                "exact": lambda: _profile_case_exact(mh, ctx, body)}[args.case]
@@ -605,7 +606,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
     ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="for --profile-only")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp64_tc"], help="for --profile-only")
     ap.add_argument("--case", default="cylinder", choices=["cylinder", "surrogate", "adjoint", "exact"],
                     help="for --profile-only: the headline sweep, or a small surrogate / adjoint / exact-kernel case")
     args = ap.parse_args()

@@ -21,10 +21,11 @@
 //     canonical no-swizzle K-major layout) and the row exponents;
 //   ozaki_split_cols: U12 -> digit tiles B[col tile][digit][re/im] (32 x 32 BF16) and the
 //     column exponents;
-//   ozaki_gemm: one CTA per 128 x 32 output tile: 16 + 16 digit tiles in shared memory
-//     (160 KB), 288 tcgen05.mma (M = 128, N = 32, K = 16) into 8 x (Re, Im) FP32 accumulators
-//     filling the 512 TMEM columns, one commit, then the exact integer combination and the
-//     FP64 subtraction.
+//   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 16 A digit
+//     tiles (128 KB) and double-buffered 16 B digit tiles (2 x 32 KB) arrive in shared memory
+//     by TMA bulk copies; per column tile 288 tcgen05.mma (M = 128, N = 32, K = 16) into
+//     8 x (Re, Im) FP32 accumulators filling the 512 TMEM columns, one commit, then the
+//     exact integer combination and the FP64 subtraction while the next B tile loads.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -138,7 +139,14 @@ __global__ void ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__
 // 2^s as a double, s in the normal range
 __device__ __forceinline__ double pow2(int s) { return __longlong_as_double((long long)(s + 1023) << 52); }
 
-__global__ void __launch_bounds__(kOzRows) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
+constexpr int kOzGroup = 4;    // column tiles per CTA (the A tiles are loaded once for all of them)
+constexpr int kOzThreads = 256; // two threads per output row: warps w and w + 4 share TMEM lanes
+                                // 32 (w % 4) .. and take one half of the 32 columns each
+
+// One CTA per (row tile, group of kOzGroup column tiles, matrix).  The A digit tiles and the
+// first B tile arrive by TMA bulk copies on one mbarrier; the B tiles are double-buffered,
+// the next one prefetched while the current tile's products and epilogue run.
+__global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
                                                               int64_t rest, int64_t nrt, int64_t nct,
                                                               const unsigned char* __restrict__ digA,
                                                               const unsigned char* __restrict__ digB,
@@ -146,66 +154,87 @@ __global__ void __launch_bounds__(kOzRows) ozaki_gemm_kernel(BatchDesc d, double
                                                               const int* __restrict__ colexp,
                                                               int* __restrict__ timeout_flag) {
   extern __shared__ __align__(1024) unsigned char osm[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar_load[2];
+  __shared__ __align__(8) uint64_t mbar_mma;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int64_t rt = blockIdx.x, ct = blockIdx.y, b = blockIdx.z;
+  const int64_t rt = blockIdx.x, b = blockIdx.z;
+  const int64_t ct0 = blockIdx.y * (int64_t)kOzGroup;
+  const int ntile = (int)((nct - ct0) < kOzGroup ? (nct - ct0) : kOzGroup);
   const int64_t n = d.n;
   unsigned char* As = osm;
-  unsigned char* Bs = osm + kOzABytes;
-  // digit tiles: contiguous kOzABytes / kOzBBytes blocks in global memory
-  {
-    const int4* srcA = reinterpret_cast<const int4*>(digA + (b * nrt + rt) * (int64_t)kOzABytes);
-    const int4* srcB = reinterpret_cast<const int4*>(digB + (b * nct + ct) * (int64_t)kOzBBytes);
-    int4* dA = reinterpret_cast<int4*>(As);
-    int4* dB = reinterpret_cast<int4*>(Bs);
-    for (int q = tid; q < kOzABytes / 16; q += kOzRows) dA[q] = __ldg(srcA + q);
-    for (int q = tid; q < kOzBBytes / 16; q += kOzRows) dB[q] = __ldg(srcB + q);
+  unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
+  const unsigned char* srcA = digA + (b * nrt + rt) * (int64_t)kOzABytes;
+  auto srcB = [&](int64_t ct) { return digB + (b * nct + ct) * (int64_t)kOzBBytes; };
+  if (tid == 0) {
+    tc::mbar_init(&mbar_load[0], 1);
+    tc::mbar_init(&mbar_load[1], 1);
+    tc::mbar_init(&mbar_mma, 1);
   }
-  if (tid == 0) tc::mbar_init(&mbar, 1);
   if (warp == 0) tc::tmem_alloc(&tmem_base, kOzTmemCols);
-  tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
   if (tid == 0) {
-    const uint32_t idesc = tc::idesc_bf16_f32(kOzRows, kOzCols);
-    const uint32_t idesc_neg = tc::idesc_bf16_f32_nega(kOzRows, kOzCols);
-    const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
-    constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
-    for (int dd = 0; dd < kOzDigits; ++dd) {
-      const uint32_t t_re = tmem + (uint32_t)(dd * 2 * kOzCols), t_im = t_re + kOzCols;
-      for (int p = 0; p <= dd; ++p) {
-        const int q = dd - p;
-        const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
-        const uint32_t br = b0 + (uint32_t)(2 * q) * kOzBTile, bi = br + kOzBTile;
+    tc::mbar_arrive_expect_tx(&mbar_load[0], kOzABytes + kOzBBytes);
+    for (int q = 0; q < kOzABytes; q += 32768) tc::bulk_g2s(As + q, srcA + q, 32768, &mbar_load[0]);
+    tc::bulk_g2s(Bs[0], srcB(ct0), kOzBBytes, &mbar_load[0]);
+    if (ntile > 1) {
+      tc::mbar_arrive_expect_tx(&mbar_load[1], kOzBBytes);
+      tc::bulk_g2s(Bs[1], srcB(ct0 + 1), kOzBBytes, &mbar_load[1]);
+    }
+  }
+  const uint32_t idesc = tc::idesc_bf16_f32(kOzRows, kOzCols);
+  const uint32_t idesc_neg = tc::idesc_bf16_f32_nega(kOzRows, kOzCols);
+  constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
+  const int lrow = tid & (kOzRows - 1), half = tid >> 7;  // TMEM lane (output row) and column half
+  const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
+  const bool row_live = r < rest;
+  const int er = row_live ? rowexp[b * rest + r] : 0;
+  const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  double2* Ab = A + b * d.stride;
+  bool failed = false;
+  int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
+  for (int t = 0; t < ntile; ++t) {
+    const int buf = t & 1;
+    const int64_t ct = ct0 + t;
+    bool ok = tc::mbar_wait(&mbar_load[buf], (uint32_t)((t >> 1) & 1), kOzWaitPolls);
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+    --outstanding_load;
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs[buf]);
+      for (int dd = 0; dd < kOzDigits; ++dd) {
+        const uint32_t t_re = tmem + (uint32_t)(dd * 2 * kOzCols), t_im = t_re + kOzCols;
+        for (int p = 0; p <= dd; ++p) {
+          const int q = dd - p;
+          const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
+          const uint32_t br = b0 + (uint32_t)(2 * q) * kOzBTile, bi = br + kOzBTile;
 #pragma unroll
-        for (int kk = 0; kk < kOzK / 16; ++kk) {
-          const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
-          const uint32_t first = (p == 0 && kk == 0) ? 0u : 1u;
-          tc::mma_bf16(t_re, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, first);
-          tc::mma_bf16(t_re, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc_neg, 1u);
-          tc::mma_bf16(t_im, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc, first);
-          tc::mma_bf16(t_im, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, 1u);
+          for (int kk = 0; kk < kOzK / 16; ++kk) {
+            const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
+            const uint32_t first = (p == 0 && kk == 0) ? 0u : 1u;
+            tc::mma_bf16(t_re, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, first);
+            tc::mma_bf16(t_re, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc_neg, 1u);
+            tc::mma_bf16(t_im, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc, first);
+            tc::mma_bf16(t_im, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, 1u);
+          }
         }
       }
+      tc::mma_commit(&mbar_mma);
     }
-    tc::mma_commit(&mbar);
-  }
-  const bool ok = tc::mbar_wait(&mbar, 0, kOzWaitPolls);
-  if (__syncthreads_or(!ok)) {
-    if (tid == 0) atomicExch(timeout_flag, 1);
-    tc::mbar_wait(&mbar, 0, kOzWaitPolls);  // let the MMAs in flight finish before freeing TMEM
-  } else {
+    ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
+    if (__syncthreads_or(!ok)) { failed = true; break; }
     tc::fence_after_sync();
-    const int64_t r = rt * kOzRows + tid;  // row of the trailing block
-    const bool row_live = r < rest;
-    const int er = row_live ? rowexp[b * rest + r] : 0;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    double2* Ab = A + b * d.stride;
+    // this B buffer is free again: prefetch tile t + 2 into it
+    if (tid == 0 && t + 2 < ntile) {
+      tc::mbar_arrive_expect_tx(&mbar_load[buf], kOzBBytes);
+      tc::bulk_g2s(Bs[buf], srcB(ct + 2), kOzBBytes, &mbar_load[buf]);
+    }
+    if (t + 2 < ntile) ++outstanding_load;
 #pragma unroll 1
-    for (int c0 = 0; c0 < kOzCols; c0 += 8) {
+    for (int c0 = half * (kOzCols / 2); c0 < (half + 1) * (kOzCols / 2); c0 += 8) {
       long long hr[8], lr[8], hi[8], li[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) { hr[q] = 0; lr[q] = 0; hi[q] = 0; li[q] = 0; }
@@ -239,6 +268,20 @@ __global__ void __launch_bounds__(kOzRows) ozaki_gemm_kernel(BatchDesc d, double
         }
       }
     }
+    // every TMEM read of this tile is done before the next tile's products overwrite it
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (failed) {
+    // reported by the host as a timeout; drain the products and copies in flight (bounded)
+    // before the tensor memory and shared memory are released
+    if (tid == 0) atomicExch(timeout_flag, 1);
+    tc::mbar_wait(&mbar_mma, 0, kOzWaitPolls);
+    tc::mbar_wait(&mbar_mma, 1, kOzWaitPolls);
+    if (outstanding_load > 0) {
+      tc::mbar_wait(&mbar_load[0], 0, kOzWaitPolls);
+      tc::mbar_wait(&mbar_load[1], 0, kOzWaitPolls);
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -266,11 +309,11 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_rows_kernel<<<gr, 128, 0, st>>>(d, A, k, kb, rest, nrt, digA, rowexp));
   dim3 gc((unsigned)((nct * kOzCols + 127) / 128), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 128, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
-  const size_t smem = kOzABytes + kOzBBytes;
+  const size_t smem = kOzABytes + 2 * kOzBBytes;
   cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 gg((unsigned)nrt, (unsigned)nct, (unsigned)d.batch);
+  dim3 gg((unsigned)nrt, (unsigned)((nct + kOzGroup - 1) / kOzGroup), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_ozaki",
-            ozaki_gemm_kernel<<<gg, kOzRows, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp,
+            ozaki_gemm_kernel<<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp,
                                                           timeout_flag));
 }
 
