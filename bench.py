@@ -419,7 +419,7 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
                        "radiation, Rankine+image+GFWu direct; one CUDA graph over 4 streams",
            "units": units, "panel_pairs": pairs, "unit": UNIT}
     results = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "fp64_tc"):
         F = mh.DirectBEM(precision=prec)
         # first call: graph capture + instantiation + one run (untimed warm-up, also the results)
         results[prec] = mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO, g=G)
@@ -433,7 +433,13 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
         for key in ("added_mass", "radiation_damping"):
             dev_max = max(dev_max, float(np.abs(a[key] - b[key]).max() / np.abs(b[key]).max()))
     out["mixed"]["max_rel_dev_vs_fp64"] = dev_max
+    dev_tc = 0.0
+    for a, b in zip(results["fp64_tc"], results["fp64"]):
+        for key in ("added_mass", "radiation_damping"):
+            dev_tc = max(dev_tc, float(np.abs(a[key] - b[key]).max() / np.abs(b[key]).max()))
+    out["fp64_tc"]["max_rel_dev_vs_fp64"] = dev_tc
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["fp64_tc_over_fp64"] = out["fp64_tc"]["value"] / out["fp64"]["value"]
     return out
 
 
@@ -567,7 +573,7 @@ def run_adjoint_variant(mh, ctx):
                                          mh.DirectBEM(precision=prec), ctx=ctx, rho=RHO, g=G)
         A, B = r["added_mass"][..., 0], r["radiation_damping"][..., 0]
         return float(sum(A[h, h, w] + B[h, h, w] for h in range(2) for w in range(len(oms))))
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "mixed", "fp64_tc"):
         t0 = time.perf_counter()
         J, grad = mh.hydro_gradient(body, oms, obj, mh.DirectBEM(precision=prec), ctx=ctx, rho=RHO, g=G)
         tg = time.perf_counter() - t0

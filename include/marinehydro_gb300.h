@@ -78,8 +78,7 @@ typedef enum {
    by a power of two, cut into eight 7-bit digits, digit products summed exactly
    in FP32 and recombined in 64-bit integers): FP64 results to within the
    rounding of the row and column scales; panel, pivoting and substitution as
-   MH_PREC_FP64.  Accepted by mh_linsolve, mh_solve, mh_linsolve_adjoint and
-   mh_hydrodynamic_coefficients. */
+   MH_PREC_FP64.  Accepted by every entry point that takes a precision. */
 #define MH_PREC_FP64 0
 #define MH_PREC_MIXED 1
 #define MH_PREC_FP64_TC 2

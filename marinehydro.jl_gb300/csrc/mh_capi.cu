@@ -39,6 +39,8 @@ struct BodyPlan {
   double2 *F = nullptr, *FK = nullptr;
   float2 *LU32 = nullptr, *X32 = nullptr;
   int32_t *ipiv = nullptr, *info = nullptr;
+  void* oz = nullptr;       // tensor-core FP64 update workspace (MH_PREC_FP64_TC)
+  int* ozflag = nullptr;    // its timeout flag
   double2 *hF = nullptr, *hFK = nullptr;
   int32_t* hinfo = nullptr;
   double *hnorms = nullptr, *hparams = nullptr, *hdofs = nullptr;
@@ -485,6 +487,10 @@ size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
   b.ipiv = (int32_t*)take(nw * n * 4);
   b.info = (int32_t*)take(nw * 4);
   b.norms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
+  if (o.precision == MH_PREC_FP64_TC) {
+    b.oz = take(ozaki_workspace_bytes(b.n, b.nw));
+    b.ozflag = (int*)take(64);
+  }
   b.F = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
   b.FK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
   b.nparams = 2 * nw + (size_t)o.n_beta + (size_t)(o.n_rad + o.n_inf + 1) / 2 + 2;
@@ -531,8 +537,9 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   BatchDesc d{n, nw, nn};
   if (o.direct) zgemm_nn_batched(st, lc, d, b.S, b.B, o.nrhs, bstride, b.X, b.work);
   else cudaMemcpyAsync(b.X, b.B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
-  if (o.precision == MH_PREC_FP64) {
-    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info);
+  if (o.precision == MH_PREC_FP64 || o.precision == MH_PREC_FP64_TC) {
+    if (b.ozflag) cudaMemsetAsync(b.ozflag, 0, sizeof(int), st);
+    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info, b.oz, b.ozflag);
     lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
   } else {
     BatchDesc d32{n, nw, nn};
@@ -581,6 +588,11 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
     if (b.hinfo[w] != 0)
       return fail(ctx, MH_ERR_SINGULAR, "body with %lld panels, frequency %lld: zero pivot in column %d",
                   (long long)b.n, (long long)w, b.hinfo[w]);
+  if (b.ozflag) {
+    int flag = 0;
+    MH_CUDA(ctx, cudaMemcpy(&flag, b.ozflag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+  }
   if (o.precision != MH_PREC_MIXED) return MH_OK;
   const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs, ncols = o.nrhs * nw;
   const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
@@ -1170,7 +1182,7 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
   if (gfs & MH_GF_SURROGATE)
     return fail(ctx, MH_ERR_UNSUPPORTED, "the many-body batch does not take the learned surrogate; use "
                                          "mh_hydrodynamic_coefficients per body");
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
   for (int64_t q = 0; q < n_rad; ++q)
@@ -1368,7 +1380,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   if (gfs == 0 || (gfs & ~allowed))
     return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint covers the Birk Rankine family and GFWu (got 0x%x)", gfs);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
-  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
   for (int64_t q = 0; q < n_obj; ++q)
     if (obj_idx[q] < 0 || obj_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "objective dof index out of range");
@@ -1408,6 +1420,16 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * chunk), &ipiv));
   MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)chunk, &info));
   MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)((19 + 3 * nh) * n), &grad));
+  void* oz_ws = nullptr;  // FP64 LU update on the tensor cores (MH_PREC_FP64_TC)
+  int* oz_flag = nullptr;
+  if (precision == MH_PREC_FP64_TC) {
+    unsigned char* w;
+    const size_t wsb = ozaki_workspace_bytes(n, chunk);
+    MH_TRY(ws_get_t(ctx, kSlotOzaki, wsb + 256, &w));
+    oz_ws = w;
+    oz_flag = reinterpret_cast<int*>(w + wsb);
+    MH_CUDA(ctx, cudaMemsetAsync(oz_flag, 0, sizeof(int), st));
+  }
   // small device block: [omegas | wavenumbers | objective dof indices (int32)]
   const size_t nsmall = (size_t)(2 * n_omega) + 4;
   MH_TRY(ws_get_t(ctx, kSlotIdx, nsmall, &small));
@@ -1476,7 +1498,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     }
     if (!done) {
       zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
-      lu_factor_batched<double>(st, lc, d, D, ipiv, info);
+      lu_factor_batched<double>(st, lc, d, D, ipiv, info, oz_ws, oz_flag);
       lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, bstride, false);     // X = phi
       forces_and_weights();
       lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, bstride, true);    // mu = D^-H conj(w)
@@ -1501,6 +1523,11 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
   MH_TRY(check_launch(ctx, "static adjoint"));
   MH_TRY(sync(ctx, "forces"));
+  if (oz_flag) {
+    int flag = 0;
+    MH_CUDA(ctx, cudaMemcpy(&flag, oz_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+  }
   double Jsum = 0.0;
   for (int64_t w = 0; w < n_omega; ++w) {
     const double om = omegas[w];

@@ -147,12 +147,14 @@ def test_panel_terms_match_finite_differences(mh, ctx, wu):
     assert not bad, bad
 
 
-def test_mixed_precision_gradient_matches_fp64(mh, ctx):
-    """FP32 factors + refinement of both solves: J and the gradient agree with FP64."""
+@pytest.mark.parametrize("precision", ["mixed", "fp64_tc"])
+def test_other_precisions_match_fp64(mh, ctx, precision):
+    """FP32 factors + refinement of both solves, or the FP64 LU with its update on the tensor
+    cores: J and the gradient agree with the FP64 path."""
     m1, m2 = _geometry(mh)
     body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave", "Pitch"])
     obj = ["c1__Heave", "c2__Pitch"]
     J64, g64 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(), ctx=ctx, rho=1025.0)
-    J32, g32 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(precision="mixed"), ctx=ctx, rho=1025.0)
+    J32, g32 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(precision=precision), ctx=ctx, rho=1025.0)
     assert abs(J32 - J64) <= 1e-12 * abs(J64)
     assert np.abs(g32 - g64).max() <= 1e-10 * np.abs(g64).max()

@@ -28,7 +28,7 @@ def _check(res, ref):
 
 
 @pytest.mark.parametrize("direct", [True, False])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
 def test_batch_matches_per_body(mh, ctx, direct, precision):
     bodies = _bodies(mh)
     F = (mh.DirectBEM if direct else mh.IndirectBEM)(precision=precision)
