@@ -7,14 +7,23 @@
 // swapped across the whole matrix, info = index of the first exactly-zero pivot.
 //
 // Work split per panel step k (nb = 32 columns):
-//   panel_kernel   one CTA per matrix: pivot search, row swap, scaling and the
-//                  rank-1 updates inside the panel (L2-resident, latency-bound;
-//                  many matrices run side by side in a frequency sweep)
+//   panel_cluster_kernel  a thread-block cluster of P CTAs per matrix: the panel's
+//                  rows are split over the P CTAs and held in shared memory; pivot
+//                  candidates and the pivot row travel through distributed shared
+//                  memory with two cluster barriers per column, so the panel's FP64
+//                  rank-1 updates run on P SMs instead of one
+//   panel_kernel   the same on one CTA straight from global memory, for panels too
+//                  tall for the cluster's shared memory
+//   laswp_kernel   the panel's row interchanges applied to every column outside it,
+//                  as one permutation of at most 64 rows (a warp per column)
 //   trsm_kernel    U12 = L11^-1 A12, one thread per column, L11 in shared memory
 //   gemm_kernel    A22 -= L21 U12, 64x64 tiles, 4x4 complex outputs per thread
 // Templated on the real type: double (the plain FP64 path) and float (the factor
 // used by mixed-precision iterative refinement).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "mh_internal.cuh"
 
@@ -58,6 +67,13 @@ template <typename C> __device__ __forceinline__ C crecip(C a) {
 }
 template <typename C> __device__ __forceinline__ C cdiv(C a, C b) { return cmul(a, crecip(b)); }
 template <typename C> __device__ __forceinline__ C czero() { C r; r.x = 0; r.y = 0; return r; }
+
+__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ float2 shfl_c(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
 
 // ------------------------------- panel ---------------------------------------
 template <typename T>
@@ -111,8 +127,8 @@ __global__ void __launch_bounds__(512) panel_kernel(BatchDesc d, typename cplx_t
       __syncthreads();
       continue;
     }
-    if (p != j) {
-      for (int64_t c = tid; c < n; c += blockDim.x) {
+    if (p != j) {  // inside the panel; laswp_kernel moves the rest of the rows
+      for (int64_t c = k + tid; c < kend; c += blockDim.x) {
         C t = A[j + c * n];
         A[j + c * n] = A[p + c * n];
         A[p + c * n] = t;
@@ -131,6 +147,244 @@ __global__ void __launch_bounds__(512) panel_kernel(BatchDesc d, typename cplx_t
       }
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------- panel on a cluster -------------------------------
+constexpr int kPanelThreads = 512;
+// panel rows one CTA holds in shared memory (32 complex columns each, < 227 KB)
+template <typename T> struct PanelRows;
+template <> struct PanelRows<double> { static constexpr int value = 432; };
+template <> struct PanelRows<float> { static constexpr int value = 864; };
+
+// (value, row) of the larger |re| + |im|; ties go to the smaller row (izamax's first maximum)
+template <typename T> __device__ __forceinline__ void argmax_merge(T& v, int& i, T ov, int oi) {
+  if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
+}
+template <typename T> __device__ __forceinline__ void warp_argmax(T& v, int& i) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) argmax_merge(v, i, __shfl_xor_sync(0xffffffffu, v, off),
+                                                       __shfl_xor_sync(0xffffffffu, i, off));
+}
+
+// split cluster barrier: arrive (releasing this thread's writes), later wait (acquiring
+// every thread's writes before their arrive)
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire;" ::: "memory"); }
+
+// Rows k .. n-1 of the panel (m = n - k panel rows, panel row r = matrix row k + r) are
+// split into chunks of `chunk` rows, chunk >= kb, so CTA 0 holds the kb diagonal rows.
+// Thread t of a CTA owns its chunk's rows t, t + 512, ...: it alone writes them in shared
+// memory.  Rows cross CTAs only as copies in double-buffered publication slots, one split
+// cluster barrier per column.  Step j (after the barrier of column j):
+//   warp 0 reduces the P posted candidates and fetches the posted copies of the pivot row
+//   and row j through distributed shared memory;
+//   the owners write the interchanged rows; every thread scales its rows' entry j and
+//   updates column j+1 only (look-ahead), searching it;
+//   the CTA's best row for column j+1 and (CTA 0) row j+1 are copied by their owner
+//   threads, the candidate posted, and every thread arrives at the barrier;
+//   then columns j+2 .. kb-1 are updated while the barrier completes, and the thread waits.
+// A posted copy therefore still lacks step j's update of columns j+2 ..; its reader applies
+// it (copy[c] - copy[j] urow[c], the FMA the owner applies), so the completed copy is
+// bitwise the owner's row.  Same arithmetic, in the same order, as panel_kernel.
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                                     int32_t* __restrict__ ipiv_all,
+                                                                     int32_t* __restrict__ info_all, int64_t k,
+                                                                     int chunk) {
+  using C = typename cplx_t<T>::type;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char panel_smem[];
+  C* sp = reinterpret_cast<C*>(panel_smem);  // chunk x kb, column-major (leading dimension chunk)
+  __shared__ C pub_row[2][kNB];               // this CTA's candidate row, by column parity
+  __shared__ C pub_j[2][kNB];                 // CTA 0: row j
+  __shared__ T cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ C urow[kNB], jrow[kNB];          // the pivot row and row j of the current step
+  __shared__ T red_v[kPanelThreads / 32];
+  __shared__ int red_i[kPanelThreads / 32];
+  __shared__ int s_piv;
+  __shared__ C s_inv;
+  const int P = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t n = d.n, bmat = blockIdx.y;
+  C* A = Aall + bmat * d.stride;
+  const int64_t m = n - k;
+  const int kb = (int)(m < kNB ? m : kNB);
+  const int r0 = rank * chunk;  // first panel row of this CTA
+  const int rows = (int)((m - r0) < chunk ? ((m - r0) > 0 ? (m - r0) : 0) : chunk);
+
+  // posts this CTA's candidate for column jj: every warp reduces the per-warp partials, the
+  // owner threads of the best row and (CTA 0) of row jj copy their rows
+  auto post = [&](int jj, T bv, int bix) {
+    warp_argmax(bv, bix);
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bix; }
+    __syncthreads();
+    bv = lane < kPanelThreads / 32 ? red_v[lane] : (T)-1;
+    bix = lane < kPanelThreads / 32 ? red_i[lane] : INT_MAX;
+    warp_argmax(bv, bix);
+    const int par = jj & 1;
+    if (tid == 0) { cand_v[par] = bv; cand_i[par] = bix; }
+    if (bix != INT_MAX && tid == (bix - r0) % kPanelThreads)
+      for (int c = 0; c < kb; ++c) pub_row[par][c] = sp[c * chunk + (bix - r0)];
+    if (rank == 0 && tid == jj)
+      for (int c = 0; c < kb; ++c) pub_j[par][c] = sp[c * chunk + jj];
+  };
+
+  for (int c = 0; c < kb; ++c)
+    for (int i = tid; i < rows; i += kPanelThreads) sp[c * chunk + i] = A[(k + r0 + i) + (k + c) * n];
+  {
+    T best = -1;
+    int bi = INT_MAX;
+    for (int i = tid; i < rows; i += kPanelThreads) {
+      const C a = sp[i];
+      argmax_merge(best, bi, fabs(a.x) + fabs(a.y), r0 + i);
+    }
+    post(0, best, bi);
+  }
+  cluster_arrive();
+  cluster_wait();
+  for (int j = 0; j < kb; ++j) {
+    const int par = j & 1;
+    __syncthreads();  // every thread is done with the previous step's urow
+    if (warp == 0) {
+      T v = -1;
+      int vi = INT_MAX;
+      if (lane < P) {
+        v = *cl.map_shared_rank(&cand_v[par], (unsigned)lane);
+        vi = *cl.map_shared_rank(&cand_i[par], (unsigned)lane);
+      }
+      warp_argmax(v, vi);
+      const bool zero = !(v > 0);
+      const int p = zero ? j : vi;  // panel row of the pivot
+      const int owner = p / chunk;
+      C rj = czero<C>(), rp = czero<C>();
+      if (lane < kb) {
+        rj = cl.map_shared_rank(&pub_j[par][0], 0u)[lane];
+        rp = (p == j) ? rj : cl.map_shared_rank(&pub_row[par][0], (unsigned)owner)[lane];
+      }
+      if (j > 0) {  // the copies still lack step j-1's update of columns j+1 ..
+        const C lj = shfl_c(rj, j - 1), lpv = shfl_c(rp, j - 1);
+        if (lane > j && lane < kb) {
+          const C u = urow[lane];
+          rj = cfms(rj, lj, u);
+          rp = cfms(rp, lpv, u);
+        }
+      }
+      if (lane < kb) { urow[lane] = rp; jrow[lane] = rj; }
+      if (lane == j) s_inv = zero ? czero<C>() : crecip(rp);
+      if (lane == 0) {
+        s_piv = p;
+        if (rank == 0) {
+          ipiv_all[bmat * n + k + j] = (int32_t)(k + p);
+          if (zero && info_all[bmat] == 0) info_all[bmat] = (int32_t)(k + j + 1);
+        }
+      }
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p != j) {
+      if (rank == 0 && tid == j)
+        for (int c = 0; c < kb; ++c) sp[c * chunk + j] = urow[c];
+      const int owner = p / chunk, lp = p - owner * chunk;
+      if (rank == owner && tid == lp % kPanelThreads)
+        for (int c = 0; c < kb; ++c) sp[c * chunk + lp] = jrow[c];
+    }
+    const C inv = s_inv;
+    // look-ahead: scale column j and update column j+1 only
+    T best = -1;
+    int bi = INT_MAX;
+    for (int i = tid; i < rows; i += kPanelThreads) {
+      const int pr = r0 + i;
+      if (pr <= j) continue;
+      const C l = cmul(sp[j * chunk + i], inv);
+      sp[j * chunk + i] = l;
+      if (j + 1 < kb) {
+        const C v = cfms(sp[(j + 1) * chunk + i], l, urow[j + 1]);
+        sp[(j + 1) * chunk + i] = v;
+        argmax_merge(best, bi, fabs(v.x) + fabs(v.y), pr);
+      }
+    }
+    if (j + 1 < kb) {
+      post(j + 1, best, bi);
+      cluster_arrive();
+    }
+    for (int i = tid; i < rows; i += kPanelThreads) {
+      const int pr = r0 + i;
+      if (pr <= j) continue;
+      const C l = sp[j * chunk + i];
+      for (int c = j + 2; c < kb; ++c) sp[c * chunk + i] = cfms(sp[c * chunk + i], l, urow[c]);
+    }
+    if (j + 1 < kb) cluster_wait();
+  }
+  // other CTAs may still read this CTA's slots of the last column: wait for them
+  cl.sync();
+  for (int c = 0; c < kb; ++c)
+    for (int i = tid; i < rows; i += kPanelThreads) A[(k + r0 + i) + (k + c) * n] = sp[c * chunk + i];
+}
+
+// The interchanges of panel step k as one permutation: final row dst = original row src for
+// at most 64 (dst, src) pairs (-1: none).  Slot s < 32 is panel row s, slot 32 + q is the
+// row below the diagonal block that step q chose first.  Runs on warp 0.
+__device__ void panel_permutation(const int32_t* __restrict__ ipiv, int64_t k, int kb, int* s_slot,
+                                  int* s_content, int* s_dst, int* s_src) {
+  const int lane = threadIdx.x & 31;
+  const int p = lane < kb ? (int)(ipiv[k + lane] - k) : lane;  // panel row chosen at step lane
+  int first = lane;
+  for (int q = 31; q >= 0; --q) {
+    const int pq = __shfl_sync(0xffffffffu, p, q);
+    if (q < lane && pq == p) first = q;
+  }
+  s_slot[lane] = p < kNB ? p : kNB + first;
+  s_content[lane] = lane;
+  s_content[lane + 32] = lane + 32;
+  __syncwarp();
+  if (lane == 0)
+    for (int j = 0; j < kb; ++j) {
+      const int a = j, b = s_slot[j];
+      const int t = s_content[a];
+      s_content[a] = s_content[b];
+      s_content[b] = t;
+    }
+  __syncwarp();
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int sl = lane + 32 * h;
+    const int src = s_content[sl];
+    const int q = src >= kNB ? src - kNB : 0;
+    const int psrc = __shfl_sync(0xffffffffu, p, q);
+    const bool live = src != sl;
+    s_dst[sl] = live ? (int)(k + (sl < kNB ? sl : p)) : -1;  // slot 32 + lane is the row p of this lane
+    s_src[sl] = live ? (int)(k + (src < kNB ? src : psrc)) : -1;
+  }
+}
+
+// Applies panel step k's interchanges to the columns outside the panel: one warp per
+// column, all loads of a column before its stores.
+constexpr int kSwpCols = 64;  // columns per CTA (the permutation is built once per CTA)
+template <typename T>
+__global__ void __launch_bounds__(256) laswp_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                   const int32_t* __restrict__ ipiv_all, int64_t k, int kb) {
+  using C = typename cplx_t<T>::type;
+  __shared__ int s_slot[32], s_content[64], s_dst[64], s_src[64];
+  const int64_t n = d.n, bmat = blockIdx.y;
+  if (threadIdx.x < 32) panel_permutation(ipiv_all + bmat * n, k, kb, s_slot, s_content, s_dst, s_src);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int d0 = s_dst[lane], s0 = s_src[lane], d1 = s_dst[lane + 32], s1 = s_src[lane + 32];
+  C* A = Aall + bmat * d.stride;
+  const int64_t nout = n - kb;
+  const int64_t q0 = blockIdx.x * (int64_t)kSwpCols;
+  const int64_t q1 = (q0 + kSwpCols < nout) ? q0 + kSwpCols : nout;
+  for (int64_t q = q0 + warp; q < q1; q += 8) {
+    C* col = A + (q < k ? q : q + kb) * n;
+    C v0 = czero<C>(), v1 = czero<C>();
+    if (d0 >= 0) v0 = col[s0];
+    if (d1 >= 0) v1 = col[s1];
+    __syncwarp();
+    if (d0 >= 0) col[d0] = v0;
+    if (d1 >= 0) col[d1] = v1;
   }
 }
 
@@ -242,12 +496,6 @@ __global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<
 // element is loaded once and applied to up to kSG vectors held in registers.
 constexpr int kSG = 8;
 
-__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
-  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-}
-__device__ __forceinline__ float2 shfl_c(float2 v, int src) {
-  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-}
 
 // Diagonal 32x32 block solves done by one warp: the block sits in shared memory
 // (blk, 32 x 33 padded, blk[l*33+q] = M[jb+l, jb+q] as stored), lane l owns
@@ -411,6 +659,199 @@ __global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename 
   }
 }
 
+// ---------------------------- solve on a cluster --------------------------------
+// One cluster of P CTAs per (group of g <= kSG right-hand sides, matrix).  The 32-row
+// blocks of the solution are dealt out cyclically (block b to CTA b % P), each CTA keeps
+// its blocks' entries of the g vectors in shared memory.  The solve is a sequence of
+// 2 nblk block steps (L then U, or U^H then L^H).  At step s the owner of block s has
+// already solved it and posted its entries in a double-buffered slot; every CTA copies
+// the slot through distributed shared memory and subtracts the block's contribution from
+// its own rows.  The owner of block s + 1 first updates that block's rows, solves it (one
+// warp per vector, reciprocals of the diagonal precomputed), posts it and arrives at the
+// split cluster barrier, and only then updates the rest of its rows; every other CTA
+// arrives as soon as it has its copy.  So the barrier waits only for the next block, not
+// for the whole update.  The permutation of the right-hand sides (the LU's row
+// interchanges) is composed once per CTA into an index map: x = b[sigma] before L
+// (forward), x[sigma] = v after L^H (adjoint).
+
+// kind of block step s (KIND of diag_block_solve) and its block index
+template <bool ADJ> __device__ __forceinline__ void solve_step(int s, int nblk, int& kind, int& bI) {
+  if (s < nblk) { kind = ADJ ? 2 : 0; bI = s; }
+  else { kind = ADJ ? 3 : 1; bI = 2 * nblk - 1 - s; }
+}
+
+// one warp solves the block entries x[0 .. bw) of one vector in place; rd: reciprocals of
+// the diagonal (KIND 1, 2)
+template <typename C, int KIND>
+__device__ __forceinline__ void block_solve_slot(const C* blk, const C* rd, int bw, C* x, int lane) {
+  C xl = lane < bw ? x[lane] : czero<C>();
+  if (KIND == 0 || KIND == 2) {
+#pragma unroll 4
+    for (int q = 0; q < bw; ++q) {
+      C m = (KIND == 0) ? blk[lane * 33 + q] : cconj(blk[q * 33 + lane]);
+      if (KIND == 2 && lane == q) xl = cmul(xl, rd[q]);
+      C xq = shfl_c(xl, q);
+      if (lane > q && lane < bw) xl = cfms(xl, m, xq);
+    }
+  } else {
+#pragma unroll 4
+    for (int q = bw - 1; q >= 0; --q) {
+      C m = (KIND == 1) ? blk[lane * 33 + q] : cconj(blk[q * 33 + lane]);
+      if (KIND == 1 && lane == q) xl = cmul(xl, rd[q]);
+      C xq = shfl_c(xl, q);
+      if (lane < q) xl = cfms(xl, m, xq);
+    }
+  }
+  if (lane < bw) x[lane] = xl;
+}
+
+constexpr int kXbStride = 33;  // padded: the g vectors of one row read different banks
+
+// rows of block b2 take the contribution of block bI at this step?
+__device__ __forceinline__ bool step_updates(int kind, int bI, int b2) {
+  return (kind == 0 || kind == 2) ? (b2 > bI) : (b2 < bI);
+}
+
+// x_i -= sum_jj M(i, jb + jj) xb[q][jj] for the local rows li in [l0, l1) that step (kind,
+// bI) updates, skipping local block `skip`; work item = (row, vector) so that one block's
+// 32 rows still spread over the CTA
+template <typename C>
+__device__ __forceinline__ void cluster_update_rows(const C* __restrict__ LU, int64_t n, int kind, int bI, int bw,
+                                                    int P, int rank, int g, int ln, C* xl, const C* xb, int l0, int l1,
+                                                    int skip) {
+  const bool ct = (kind >= 2);
+  const int64_t jb = (int64_t)bI * 32;
+  const int rows = l1 - l0;
+  for (int w = threadIdx.x; w < rows * g; w += blockDim.x) {
+    const int li = l0 + w / g, q = w % g;  // the g vectors of a row on neighbouring threads
+    const int lb = li >> 5;
+    if (lb == skip) continue;
+    const int b2 = rank + lb * P;
+    if (!step_updates(kind, bI, b2)) continue;
+    const int64_t i = (int64_t)b2 * 32 + (li & 31);
+    if (i >= n) continue;
+    C acc = czero<C>();
+    const C* xq = xb + q * kXbStride;
+    if (ct) {
+      const C* col = LU + i * n + jb;  // M(i, j) = conj(LU[j, i]): row i of LU^H is column i of LU
+#pragma unroll 8
+      for (int jj = 0; jj < bw; ++jj) acc = cfma(acc, cconj(col[jj]), xq[jj]);
+    } else {
+      const C* row = LU + i + jb * n;
+#pragma unroll 8
+      for (int jj = 0; jj < bw; ++jj) acc = cfma(acc, row[(int64_t)jj * n], xq[jj]);
+    }
+    xl[(int64_t)q * ln + li] = csub(xl[(int64_t)q * ln + li], acc);
+  }
+}
+
+template <typename C, bool ADJ>
+__device__ __forceinline__ void cluster_solve_block(const C* __restrict__ LU, int64_t n, int kind, int bI, int P,
+                                                    int g, int ln, C* xl, C* blk, C* rd, C* post) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t jb = (int64_t)bI * 32;
+  const int bw = (int)((jb + 32 < n) ? 32 : n - jb);
+  load_diag_block(LU, n, jb, bw, blk);
+  __syncthreads();
+  if (warp == 0 && lane < bw) {
+    const C dgl = blk[lane * 33 + lane];
+    rd[lane] = crecip(kind == 2 ? cconj(dgl) : dgl);
+  }
+  __syncthreads();
+  if (warp < g) {
+    C* x = xl + (int64_t)warp * ln + (bI / P) * 32;
+    switch (kind) {
+      case 0: block_solve_slot<C, 0>(blk, rd, bw, x, lane); break;
+      case 1: block_solve_slot<C, 1>(blk, rd, bw, x, lane); break;
+      case 2: block_solve_slot<C, 2>(blk, rd, bw, x, lane); break;
+      default: block_solve_slot<C, 3>(blk, rd, bw, x, lane); break;
+    }
+    __syncwarp();
+    post[warp * 32 + lane] = lane < bw ? x[lane] : czero<C>();
+  }
+}
+
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(512) solve_cluster_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
+                                                            const int32_t* __restrict__ ipiv_all,
+                                                            typename cplx_t<T>::type* __restrict__ Xall, int64_t nrhs,
+                                                            int64_t xstride, int group, int ln) {
+  using C = typename cplx_t<T>::type;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  C* xl = reinterpret_cast<C*>(solve_smem);                          // g x ln, vector-major
+  int* sig = reinterpret_cast<int*>(xl + (int64_t)group * ln);       // n
+  int* spv = sig + d.n;                                              // n: the pivots
+  __shared__ C blk[32 * 33];
+  __shared__ C rd[32];
+  __shared__ C pub[2][32 * kSG];
+  __shared__ C xb[2][kXbStride * kSG];
+  const int P = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int64_t n = d.n;
+  const int nblk = (int)((n + 31) / 32);
+  const C* LU = LUall + blockIdx.z * d.stride;
+  const int32_t* ipiv = ipiv_all + blockIdx.z * n;
+  C* X = Xall + blockIdx.z * xstride;
+  const int64_t r0 = blockIdx.y * (int64_t)group;
+  const int g = (int)((r0 + group <= nrhs) ? group : nrhs - r0);
+  const int tid = threadIdx.x;
+  // sigma: the row interchanges composed in order (x = b[sigma] applies them to b)
+  for (int64_t i = tid; i < n; i += blockDim.x) { sig[i] = (int)i; spv[i] = ipiv[i]; }
+  __syncthreads();
+  if (tid == 0)
+    for (int64_t j = 0; j < n; ++j) {
+      const int p = spv[j];
+      if (p != j) { const int t = sig[j]; sig[j] = sig[p]; sig[p] = t; }
+    }
+  __syncthreads();
+  const int nlb = (nblk - rank + P - 1) / P;
+  const int nloc = nlb * 32;
+  for (int w = tid; w < nloc * g; w += blockDim.x) {
+    const int li = w % nloc, q = w / nloc;
+    const int64_t i = (int64_t)(rank + (li >> 5) * P) * 32 + (li & 31);
+    if (i < n) xl[(int64_t)q * ln + li] = X[(ADJ ? i : sig[i]) + (r0 + q) * n];
+  }
+  __syncthreads();
+  const int nsteps = 2 * nblk;
+  int kind, bI;
+  solve_step<ADJ>(0, nblk, kind, bI);
+  if (bI % P == rank) cluster_solve_block<C, ADJ>(LU, n, kind, bI, P, g, ln, xl, blk, rd, pub[0]);
+  cluster_arrive();
+  cluster_wait();
+  for (int s = 0; s < nsteps; ++s) {
+    solve_step<ADJ>(s, nblk, kind, bI);
+    const int bw = (int)(((int64_t)bI * 32 + 32 < n) ? 32 : n - (int64_t)bI * 32);
+    C* xs = xb[s & 1];
+    const C* src = cl.map_shared_rank(&pub[s & 1][0], (unsigned)(bI % P));
+    for (int e = tid; e < 32 * g; e += blockDim.x) xs[(e >> 5) * kXbStride + (e & 31)] = src[e];
+    __syncthreads();
+    const bool last = (s + 1 == nsteps);
+    int nkind = 0, nbI = 0, skip = -1;
+    if (!last) {
+      solve_step<ADJ>(s + 1, nblk, nkind, nbI);
+      if (nbI % P == rank) {
+        // the next block first: its rows, its solve, its slot
+        const int lb = nbI / P;
+        if (step_updates(kind, bI, nbI))
+          cluster_update_rows<C>(LU, n, kind, bI, bw, P, rank, g, ln, xl, xs, lb * 32, lb * 32 + 32, -1);
+        __syncthreads();
+        cluster_solve_block<C, ADJ>(LU, n, nkind, nbI, P, g, ln, xl, blk, rd, pub[(s + 1) & 1]);
+        skip = lb;
+      }
+    }
+    cluster_arrive();  // step s + 1 posted (or nothing to post)
+    cluster_update_rows<C>(LU, n, kind, bI, bw, P, rank, g, ln, xl, xs, 0, nloc, skip);
+    cluster_wait();
+  }
+  __syncthreads();
+  for (int w = tid; w < nloc * g; w += blockDim.x) {
+    const int li = w % nloc, q = w / nloc;
+    const int64_t i = (int64_t)(rank + (li >> 5) * P) * 32 + (li & 31);
+    if (i < n) X[(ADJ ? sig[i] : i) + (r0 + q) * n] = xl[(int64_t)q * ln + li];
+  }
+}
+
 // ------------------------------ Y = A X (FP64) --------------------------------
 constexpr int kGemvRows = 128;
 constexpr int kGemvNR = 8;
@@ -532,6 +973,52 @@ void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   MH_LAUNCH(lc, st, "ir_norms", mat_inf_norm_kernel<<<grid, 128, 0, st>>>(d, A, (unsigned long long*)out));
 }
 
+// CTAs per cluster for a panel of m rows in a batch of `batch` matrices: enough to hold
+// the panel in shared memory, and more (up to 8) while all `batch` clusters still fit on
+// the GPU at once (clusters are placed within one GPC, so this is taken from the
+// occupancy query, not from the SM count); 0 when the panel does not fit the largest
+// cluster the GPU can schedule (panel_kernel then runs).
+template <typename T>
+int panel_cluster_size(int64_t m, int64_t batch) {
+  using C = typename cplx_t<T>::type;
+  constexpr int cap = PanelRows<T>::value;
+  struct Table { int resident[17]; };
+  static const Table tab = [] {
+    Table t{};
+    const int smem = cap * kNB * (int)sizeof(C);
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int p = 1; p <= 16; ++p) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)p, 1, 1);
+      cfg.blockDim = dim3(kPanelThreads, 1, 1);
+      cfg.dynamicSmemBytes = (size_t)smem;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)p;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int num = 0;
+      if (cudaOccupancyMaxActiveClusters(&num, panel_cluster_kernel<T>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        num = 0;
+      }
+      t.resident[p] = num;  // clusters of p CTAs resident at once, at the largest chunk
+    }
+    return t;
+  }();
+  int64_t need = (m + cap - 1) / cap;
+  if (need < 1) need = 1;
+  if (need > 16 || tab.resident[need] <= 0) return 0;
+  const int64_t lim = m / kNB > 1 ? m / kNB : 1;  // keeps every chunk >= 32 rows (CTA 0 holds the diagonal block)
+  int64_t p = need;
+  for (int64_t q = need + 1; q <= 8 && q <= lim; ++q)
+    if (tab.resident[q] >= batch) p = q;
+  return (int)p;
+}
+
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
                       int32_t* ipiv, int32_t* info, void* emu_ws, int* emu_flag) {
@@ -544,9 +1031,33 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     cudaFuncSetAttribute(gemm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
   }
   for (int64_t k = 0; k < n; k += kNB) {
-    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
-              panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
     const int64_t kb = (k + kNB < n) ? kNB : n - k;
+    const int P = panel_cluster_size<T>(n - k, d.batch);
+    if (P > 0) {
+      const int chunk = (int)((n - k + P - 1) / P);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)P, (unsigned)d.batch, 1);
+      cfg.blockDim = dim3(kPanelThreads, 1, 1);
+      cfg.dynamicSmemBytes = (size_t)chunk * kNB * sizeof(typename cplx_t<T>::type);
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)P;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
+                cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, d, A, ipiv, info, k, chunk));
+    } else {
+      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
+                panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
+    }
+    if (n - kb > 0) {
+      dim3 sg((unsigned)((n - kb + kSwpCols - 1) / kSwpCols), (unsigned)d.batch);
+      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_laswp_f64" : "lu_laswp_f32",
+                laswp_kernel<T><<<sg, 256, 0, st>>>(d, A, ipiv, k, (int)kb));
+    }
     const int64_t rest = n - k - kb;
     if (rest <= 0) continue;
     dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
@@ -566,6 +1077,66 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
   return 0;
 }
 
+// Cluster size for the solve: the fewest CTAs whose shares of the vectors fit in shared
+// memory, raised (up to 8) while every (matrix, group) cluster is still resident at once.
+// Returns false when even 8 CTAs cannot hold the vectors (the one-CTA kernel then runs).
+template <typename T>
+bool solve_on_cluster(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
+                      const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride, bool adjoint) {
+  using C = typename cplx_t<T>::type;
+  const int64_t n = d.n;
+  const int g = (int)(nrhs < kSG ? nrhs : kSG);
+  const int64_t ngroups = (nrhs + g - 1) / g;
+  const int64_t nblk = (n + 31) / 32;
+  const size_t max_dyn = 190 * 1024;
+  auto dyn_bytes = [&](int p) {
+    const int64_t ln = (nblk + p - 1) / p * 32;
+    return (size_t)ln * g * sizeof(C) + 2 * sizeof(int) * (size_t)n;
+  };
+  const void* fn = adjoint ? (const void*)solve_cluster_kernel<T, true> : (const void*)solve_cluster_kernel<T, false>;
+  static const bool attr_set = [] {
+    cudaFuncSetAttribute(solve_cluster_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 190 * 1024);
+    cudaFuncSetAttribute(solve_cluster_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 190 * 1024);
+    return true;
+  }();
+  (void)attr_set;
+  auto make_cfg = [&](int p, cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)p, (unsigned)ngroups, (unsigned)d.batch);
+    cfg.blockDim = dim3(512, 1, 1);
+    cfg.dynamicSmemBytes = dyn_bytes(p);
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)p;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+  };
+  int need = 0;
+  for (int p = 1; p <= 8 && p <= nblk; ++p)
+    if (dyn_bytes(p) <= max_dyn) { need = p; break; }
+  if (need == 0) return false;
+  int P = need;
+  const int64_t clusters = ngroups * d.batch;
+  for (int p = need + 1; p <= 8 && p <= nblk; ++p) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = make_cfg(p, attr);
+    int num = 0;
+    if (cudaOccupancyMaxActiveClusters(&num, fn, &cfg) != cudaSuccess) { cudaGetLastError(); break; }
+    if (num >= clusters) P = p;
+  }
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = make_cfg(P, attr);
+  const int ln = (int)((nblk + P - 1) / P * 32);
+  lc.pre(st);
+  if (adjoint) cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, true>, d, LU, ipiv, X, nrhs, xstride, g, ln);
+  else cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, false>, d, LU, ipiv, X, nrhs, xstride, g, ln);
+  lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
+  return true;
+}
+
 template <typename T>
 void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
                       const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,
@@ -573,6 +1144,7 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   using C = typename cplx_t<T>::type;
   const int64_t n = d.n;
   if (n <= 0 || nrhs <= 0 || d.batch <= 0) return;
+  if (solve_on_cluster<T>(st, lc, d, LU, ipiv, X, nrhs, xstride, adjoint)) return;
   const size_t max_smem = 200 * 1024;
   const size_t blk_bytes = sizeof(C) * 32 * 33;
   int64_t group = (int64_t)((max_smem - blk_bytes) / (sizeof(C) * n));

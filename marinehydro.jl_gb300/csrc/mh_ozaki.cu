@@ -19,13 +19,18 @@
 // Kernels per panel step (all batched over the matrices of the sweep):
 //   ozaki_split_rows: L21 -> digit tiles A[row tile][digit][re/im] (128 x 32 BF16 each, in the
 //     canonical no-swizzle K-major layout) and the row exponents;
-//   ozaki_split_cols: U12 -> digit tiles B[col tile][digit][re/im] (32 x 32 BF16) and the
-//     column exponents;
+//   ozaki_split_cols: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
+//     column exponents; the eight digit tiles of one part are consecutive, so digits
+//     q .. 7 form one (32 (8 - q)) x 32 operand;
 //   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 16 A digit
-//     tiles (128 KB) and double-buffered 16 B digit tiles (2 x 32 KB) arrive in shared memory
-//     by TMA bulk copies; per column tile 288 tcgen05.mma (M = 128, N = 32, K = 16) into
-//     8 x (Re, Im) FP32 accumulators filling the 512 TMEM columns, one commit, then the
-//     exact integer combination and the FP64 subtraction while the next B tile loads.
+//     tiles (128 KB) and double-buffered B tiles (2 x 32 KB) arrive in shared memory by TMA
+//     bulk copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (8 - p)
+//     multiplies X_p by the stacked Y_0 .. Y_{7-p} and accumulates X_p Y_q into the TMEM
+//     columns of T_{p+q} (Re: 32 d, Im: 256 + 32 d), so 64 MMAs (8 digits x 2 K-steps x 4
+//     real products) cover the 36 digit pairs.  The epilogue converts the exact integers
+//     with magic-number additions (no integer-to-FP64 conversion instructions), combines
+//     them in 32/64-bit integers and applies C -= 2^s (hi + lo 2^-28) with one FP64 add and
+//     two FMAs per real entry; C is prefetched into registers while the MMAs run.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -130,8 +135,8 @@ __global__ void ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__
     const uint32_t off = tc::kmajor_offset(cc, kk, kOzK);
 #pragma unroll
     for (int p = 0; p < kOzDigits; ++p) {
-      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p) * kOzBTile + off) = __float2bfloat16_rn((float)dre[p]);
-      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p + 1) * kOzBTile + off) = __float2bfloat16_rn((float)dim[p]);
+      *reinterpret_cast<__nv_bfloat16*>(tiles + p * kOzBTile + off) = __float2bfloat16_rn((float)dre[p]);
+      *reinterpret_cast<__nv_bfloat16*>(tiles + (kOzDigits + p) * kOzBTile + off) = __float2bfloat16_rn((float)dim[p]);
     }
   }
 }
@@ -185,8 +190,6 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
       tc::bulk_g2s(Bs[1], srcB(ct0 + 1), kOzBBytes, &mbar_load[1]);
     }
   }
-  const uint32_t idesc = tc::idesc_bf16_f32(kOzRows, kOzCols);
-  const uint32_t idesc_neg = tc::idesc_bf16_f32_nega(kOzRows, kOzCols);
   constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
   const int lrow = tid & (kOzRows - 1), half = tid >> 7;  // TMEM lane (output row) and column half
   const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
@@ -194,6 +197,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const int er = row_live ? rowexp[b * rest + r] : 0;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   double2* Ab = A + b * d.stride;
+  double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
   bool failed = false;
   int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
   for (int t = 0; t < ntile; ++t) {
@@ -205,24 +209,37 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
     if (tid == 0) {
       tc::fence_after_sync();
       const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs[buf]);
-      for (int dd = 0; dd < kOzDigits; ++dd) {
-        const uint32_t t_re = tmem + (uint32_t)(dd * 2 * kOzCols), t_im = t_re + kOzCols;
-        for (int p = 0; p <= dd; ++p) {
-          const int q = dd - p;
-          const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
-          const uint32_t br = b0 + (uint32_t)(2 * q) * kOzBTile, bi = br + kOzBTile;
+      const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
+#pragma unroll 1
+      for (int p = 0; p < kOzDigits; ++p) {
+        const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{7-p} stacked along N
+        const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
+        const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
+        const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
 #pragma unroll
-          for (int kk = 0; kk < kOzK / 16; ++kk) {
-            const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
-            const uint32_t first = (p == 0 && kk == 0) ? 0u : 1u;
-            tc::mma_bf16(t_re, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, first);
-            tc::mma_bf16(t_re, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc_neg, 1u);
-            tc::mma_bf16(t_im, tc::smem_desc(ar + ko, 128, sbo), tc::smem_desc(bi + ko, 128, sbo), idesc, first);
-            tc::mma_bf16(t_im, tc::smem_desc(ai + ko, 128, sbo), tc::smem_desc(br + ko, 128, sbo), idesc, 1u);
-          }
+        for (int kk = 0; kk < kOzK / 16; ++kk) {
+          const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
+          const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
+          const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
+          const uint64_t dbr = tc::smem_desc(bre + ko, 128, sbo), dbi = tc::smem_desc(bim + ko, 128, sbo);
+          tc::mma_bf16(t_re, dar, dbr, id, acc);      // Re T += Xre Yre
+          tc::mma_bf16(t_re, dai, dbi, id_neg, 1u);   // Re T -= Xim Yim
+          tc::mma_bf16(t_im, dar, dbi, id, acc);      // Im T += Xre Yim
+          tc::mma_bf16(t_im, dai, dbr, id, 1u);       // Im T += Xim Yre
         }
       }
       tc::mma_commit(&mbar_mma);
+    }
+    // while the products run: this thread's 16 entries of A22 and their column exponents
+    double2 cv[kOzCols / 2];
+    int ce[kOzCols / 2];
+    const int64_t cbase = ct * kOzCols + half * (kOzCols / 2);
+#pragma unroll
+    for (int q = 0; q < kOzCols / 2; ++q) {
+      const int64_t c = cbase + q;
+      const bool live = row_live && c < rest;
+      cv[q] = live ? crow[c * n] : make_double2(0.0, 0.0);
+      ce[q] = live ? colexp[b * rest + c] : 0;
     }
     ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
     if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -233,40 +250,46 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
       tc::bulk_g2s(Bs[buf], srcB(ct + 2), kOzBBytes, &mbar_load[buf]);
     }
     if (t + 2 < ntile) ++outstanding_load;
-#pragma unroll 1
-    for (int c0 = half * (kOzCols / 2); c0 < (half + 1) * (kOzCols / 2); c0 += 8) {
-      long long hr[8], lr[8], hi[8], li[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) { hr[q] = 0; lr[q] = 0; hi[q] = 0; li[q] = 0; }
+    for (int h8 = 0; h8 < 2; ++h8) {
+      const int c0 = half * (kOzCols / 2) + 8 * h8;
+      // T_d as exact integers: (T0 2^7 + T1, T2 2^7 + T3, T4 2^7 + T5, T6 2^7 + T7), re and im
+      int pr[4][8], pi[4][8];
 #pragma unroll
       for (int dd = 0; dd < kOzDigits; ++dd) {
         float vr[8], vi[8];
-        tc::tmem_ld8(trow + (uint32_t)(dd * 2 * kOzCols + c0), vr);
-        tc::tmem_ld8(trow + (uint32_t)(dd * 2 * kOzCols + kOzCols + c0), vi);
-        const int sh = dd < 4 ? 7 * (3 - dd) : 7 * (7 - dd);
+        tc::tmem_ld8(trow + (uint32_t)(dd * kOzCols + c0), vr);
+        tc::tmem_ld8(trow + (uint32_t)(kOzDigits * kOzCols + dd * kOzCols + c0), vi);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const long long tr = (long long)__float2int_rn(vr[q]) << sh;
-          const long long ti = (long long)__float2int_rn(vi[q]) << sh;
-          if (dd < 4) { hr[q] += tr; hi[q] += ti; } else { lr[q] += tr; li[q] += ti; }
+          // |T| < 2^21: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
+          const int ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
+          const int ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
+          if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 128 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 128 + ii; }
+          else { pr[dd >> 1][q] = ir; pi[dd >> 1][q] = ii; }
         }
       }
-      if (row_live) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int64_t c = ct * kOzCols + c0 + q;
-          if (c >= rest) continue;
-          // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
-          const double s = pow2(er + colexp[b * rest + c] - 33);
-          const double xr = fma((double)lr[q], 0x1p-28, (double)hr[q]);
-          const double xi = fma((double)li[q], 0x1p-28, (double)hi[q]);
-          double2* dst = Ab + (k + kb + r) + (k + kb + c) * n;
-          double2 v = *dst;
-          v.x = fma(-xr, s, v.x);
-          v.y = fma(-xi, s, v.y);
-          *dst = v;
-        }
+      for (int q = 0; q < 8; ++q) {
+        const int qq = 8 * h8 + q;
+        // hi = T0..T3 and lo = T4..T7 in base 2^7 (|.| < 2^43); 1.5 2^52 + x as a double is exact
+        const long long kMagic = 0x4338000000000000LL;
+        const long long hr = (long long)pr[0][q] * 16384 + pr[1][q], lr = (long long)pr[2][q] * 16384 + pr[3][q];
+        const long long hi = (long long)pi[0][q] * 16384 + pi[1][q], li = (long long)pi[2][q] * 16384 + pi[3][q];
+        // (1.5 2^52 + lo) 2^-28 + (hi - 1.5 2^24) = hi + lo 2^-28, rounded once
+        constexpr double kBias = 6755399441055744.0 + 25165824.0;  // 1.5 2^52 + 1.5 2^24
+        const double xr = fma(__longlong_as_double(lr + kMagic), 0x1p-28, __longlong_as_double(hr + kMagic) - kBias);
+        const double xi = fma(__longlong_as_double(li + kMagic), 0x1p-28, __longlong_as_double(hi + kMagic) - kBias);
+        // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
+        const double sc = pow2(er + ce[qq] - 33);
+        cv[qq].x = fma(-xr, sc, cv[qq].x);
+        cv[qq].y = fma(-xi, sc, cv[qq].y);
       }
+    }
+    if (row_live) {
+#pragma unroll
+      for (int q = 0; q < kOzCols / 2; ++q)
+        if (cbase + q < rest) crow[(cbase + q) * n] = cv[q];
     }
     // every TMEM read of this tile is done before the next tile's products overwrite it
     tc::fence_before_sync();

@@ -143,9 +143,11 @@ def test_assembly_between_wu_and_exact(mh, ctx, trained, direct):
         assert err_s < err_w
 
 
-def test_surrogate_sweep_and_errors(mh, ctx, trained):
-    params, _ = trained
-    ctx.surrogate_set(params)
+def test_surrogate_sweep_and_errors(mh, ctx):
+    """The shipped network (1e7 exact samples) against the exact kernel and against Wu, the
+    method without it: added mass, damping and excitation all several times closer to the
+    exact Green function (measured on a GB300: 0.17, 0.07, 0.06 of Wu's error here)."""
+    mh.load_surrogate(ctx=ctx)
     body = mh.FloatingBody(mh.hemisphere_mesh(1.0, 6, 12), ["Heave", "Surge"])
     p = {"wave_frequencies": [0.6, 1.2, 2.0], "radiating_dofs": ["Heave", "Surge"], "wave_directions": [0.0]}
     res = {}
@@ -155,7 +157,7 @@ def test_surrogate_sweep_and_errors(mh, ctx, trained):
     for key in ("added_mass", "radiation_damping", "excitation_force"):
         e = np.abs(res["s"][key] - res["e"][key]).max() / np.abs(res["e"][key]).max()
         w = np.abs(res["w"][key] - res["e"][key]).max() / np.abs(res["e"][key]).max()
-        assert e < w, key
+        assert e < 0.35 * w, (key, e, w)
     with pytest.raises(ValueError):
         mh.hydrodynamic_coefficients(body, p, mh.DirectBEM((mh.Rankine(), mh.GFWu(), mh.SurrogateDelhommeau())),
                                      ctx=ctx)
