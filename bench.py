@@ -440,6 +440,44 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
     out["fp64_tc"]["max_rel_dev_vs_fp64"] = dev_tc
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["fp64_tc_over_fp64"] = out["fp64_tc"]["value"] / out["fp64"]["value"]
+
+    # the plain FP64 GPU path: one hydrodynamic_coefficients call per body, no graph
+    F64 = mh.DirectBEM(precision="fp64")
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    plain = [mh.hydrodynamic_coefficients(b, p, F64, ctx=ctx, rho=RHO, g=G) for b, p in zip(bodies, params)]
+    t_plain = time.perf_counter() - t0
+    out["plain_fp64_per_body"] = {"value": units / t_plain, "seconds": t_plain,
+                                  "note": "mh_hydrodynamic_coefficients per body, FP64, Wu, host-synchronised"}
+    dev_plain = max(float(np.abs(a[key] - b[key]).max() / np.abs(b[key]).max())
+                    for a, b in zip(results["fp64"], plain) for key in ("added_mass", "radiation_damping"))
+    out["fp64"]["max_rel_dev_vs_plain"] = dev_plain
+
+    # surrogate + batched: the learned Delhommeau term in the same graph, mixed precision
+    mh.load_surrogate(ctx=ctx)
+    FS = mh.DirectBEM("Surrogate", precision="mixed")
+    res_s = mh.batch_hydrodynamic_coefficients(bodies, params, FS, ctx=ctx, rho=RHO, g=G)
+    t, _, launches, _ = timed(lambda: mh.batch_hydrodynamic_coefficients(bodies, params, FS, ctx=ctx, rho=RHO, g=G),
+                              1, 0)
+    ctx._L.mh_batch_release(ctx.handle)
+    out["surrogate_mixed"] = {"value": units / t, "ms_per_step": 1e3 * t, "gpu_launches": launches,
+                              "note": "Rankine + image + learned surrogate of the exact Delhommeau term (exact "
+                                      "fallback queue per body), FP32 LU + FP64 refinement, one CUDA graph"}
+    # accuracy against the exact Green function (FP64 oracle arithmetic) on the 4 smallest bodies
+    small = sorted(range(len(bodies)), key=lambda q: bodies[q].mesh.nfaces)[:4]
+    FE = mh.DirectBEM("ExactGuevelDelhommeau", precision="fp64")
+    err = {"surrogate_batched": {"added_mass": 0.0, "radiation_damping": 0.0},
+           "wu_fp64": {"added_mass": 0.0, "radiation_damping": 0.0}}
+    for q in small:
+        ex = mh.hydrodynamic_coefficients(bodies[q], params[q], FE, ctx=ctx, rho=RHO, g=G)
+        for key in ("added_mass", "radiation_damping"):
+            scale = np.abs(ex[key]).max()
+            err["surrogate_batched"][key] = max(err["surrogate_batched"][key],
+                                                float(np.abs(res_s[q][key] - ex[key]).max() / scale))
+            err["wu_fp64"][key] = max(err["wu_fp64"][key], float(np.abs(results["fp64"][q][key] - ex[key]).max() / scale))
+    out["vs_exact_green_function"] = {"bodies": [int(bodies[q].mesh.nfaces) for q in small], "max_rel_err": err}
+    out["surrogate_batched_over_plain_fp64"] = out["surrogate_mixed"]["value"] / out["plain_fp64_per_body"]["value"]
+    out["mixed_batched_over_plain_fp64"] = out["mixed"]["value"] / out["plain_fp64_per_body"]["value"]
     return out
 
 

@@ -197,7 +197,10 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* mesh, int64_t n_omega
    reused while the bodies, frequency counts and options are unchanged (omegas,
    betas and dof values may change between calls).  Mixed precision runs two
    refinement sweeps inside the graph and finishes any right-hand side that has
-   not met the backward-error test on the host afterwards. */
+   not met the backward-error test on the host afterwards.  With MH_GF_SURROGATE
+   each body keeps its own queue of pairs for the exact kernel inside the graph
+   (the surrogate parameters are read when the graph runs, so mh_surrogate_set
+   between calls takes effect). */
 int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mesh* const* meshes,
                                        const int64_t* n_omega, const double* omegas, double rho, double g,
                                        uint32_t gfs, int direct, int64_t n_dofs, const double* const* dofs,

@@ -41,6 +41,9 @@ struct BodyPlan {
   int32_t *ipiv = nullptr, *info = nullptr;
   void* oz = nullptr;       // tensor-core FP64 update workspace (MH_PREC_FP64_TC)
   int* ozflag = nullptr;    // its timeout flag
+  int4* fb_list = nullptr;  // learned surrogate: pairs queued for the exact kernel
+  unsigned long long* fb_state = nullptr;  // queue count, overflow and timeout flags
+  int64_t fb_cap = 0;
   double2 *hF = nullptr, *hFK = nullptr;
   int32_t* hinfo = nullptr;
   double *hnorms = nullptr, *hparams = nullptr, *hdofs = nullptr;
@@ -491,6 +494,11 @@ size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
     b.oz = take(ozaki_workspace_bytes(b.n, b.nw));
     b.ozflag = (int*)take(64);
   }
+  if (o.gfs & MH_GF_SURROGATE) {  // every self pair plus room for pairs outside the training box
+    b.fb_cap = b.n * (b.nw + 64) + 4096;
+    b.fb_list = (int4*)take((size_t)b.fb_cap * sizeof(int4));
+    b.fb_state = (unsigned long long*)take(4 * sizeof(unsigned long long));
+  }
   b.F = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
   b.FK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
   b.nparams = 2 * nw + (size_t)o.n_beta + (size_t)(o.n_rad + o.n_inf + 1) / 2 + 2;
@@ -526,6 +534,13 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   const int32_t* inf_d = rad_d + o.n_rad;
   const uint32_t st_kinds = o.gfs & kStaticKinds;
   AssemblyParams p = make_params(ctx, b.m, o.gfs, o.direct, 1, nullptr);
+  if (b.fb_state) {
+    p.mlp = ctx->mlp;
+    p.fb_list = b.fb_list;
+    p.fb_state = b.fb_state;
+    p.fb_cap = b.fb_cap;
+    cudaMemsetAsync(b.fb_state, 0, 4 * sizeof(unsigned long long), st);
+  }
   if (st_kinds) {
     AssemblyParams ps = make_params(ctx, b.m, st_kinds, o.direct, 1, nullptr);
     launch_assemble_static(st, lc, ps, b.SR, b.DR);
@@ -592,6 +607,15 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
     int flag = 0;
     MH_CUDA(ctx, cudaMemcpy(&flag, b.ozflag, sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+  }
+  if (b.fb_state) {
+    unsigned long long fs[3] = {0, 0, 0};
+    MH_CUDA(ctx, cudaMemcpy(fs, b.fb_state, sizeof(fs), cudaMemcpyDeviceToHost));
+    if (fs[2]) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the surrogate assembly gave up");
+    if (fs[1])
+      return fail(ctx, MH_ERR_UNSUPPORTED, "body with %lld panels: more than %lld panel pairs lie outside the "
+                                           "surrogate's training box; use ExactGuevelDelhommeau for it",
+                  (long long)b.n, (long long)b.fb_cap);
   }
   if (o.precision != MH_PREC_MIXED) return MH_OK;
   const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs, ncols = o.nrhs * nw;
@@ -1178,10 +1202,7 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
   if (n_rad < 0 || n_inf < 0 || n_beta < 0 || n_dofs < 0) return fail(ctx, MH_ERR_ARG, "negative counts");
   if (n_rad + n_beta == 0) return fail(ctx, MH_ERR_ARG, "nothing to solve: no radiating dof and no wave direction");
   if ((n_rad > 0 || n_inf > 0) && (!dofs || n_dofs <= 0)) return fail(ctx, MH_ERR_ARG, "dof fields required");
-  if (gfs == 0 || (gfs & ~kAllKinds)) return fail(ctx, MH_ERR_ARG, "bad Green-function set 0x%x", gfs);
-  if (gfs & MH_GF_SURROGATE)
-    return fail(ctx, MH_ERR_UNSUPPORTED, "the many-body batch does not take the learned surrogate; use "
-                                         "mh_hydrodynamic_coefficients per body");
+  MH_TRY(check_gfs(ctx, gfs));
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");

@@ -175,18 +175,20 @@ __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.w
 // Rows k .. n-1 of the panel (m = n - k panel rows, panel row r = matrix row k + r) are
 // split into chunks of `chunk` rows, chunk >= kb, so CTA 0 holds the kb diagonal rows.
 // Thread t of a CTA owns its chunk's rows t, t + 512, ...: it alone writes them in shared
-// memory.  Rows cross CTAs only as copies in double-buffered publication slots, one split
-// cluster barrier per column.  Step j (after the barrier of column j):
-//   warp 0 reduces the P posted candidates and fetches the posted copies of the pivot row
-//   and row j through distributed shared memory;
-//   the owners write the interchanged rows; every thread scales its rows' entry j and
-//   updates column j+1 only (look-ahead), searching it;
-//   the CTA's best row for column j+1 and (CTA 0) row j+1 are copied by their owner
-//   threads, the candidate posted, and every thread arrives at the barrier;
-//   then columns j+2 .. kb-1 are updated while the barrier completes, and the thread waits.
-// A posted copy therefore still lacks step j's update of columns j+2 ..; its reader applies
-// it (copy[c] - copy[j] urow[c], the FMA the owner applies), so the completed copy is
-// bitwise the owner's row.  Same arithmetic, in the same order, as panel_kernel.
+// memory.  Rows cross CTAs only through double-buffered publication slots, so one cluster
+// barrier per column suffices.  Per column j:
+//   every CTA posts its best candidate (value, row) and a copy of that row; CTA 0 also
+//   posts a copy of row j;  cluster barrier
+//   warp 0 of every CTA reduces the P candidates and fetches the pivot row (and, in the
+//   CTA that owns the pivot row, row j) from the winners' slots through distributed
+//   shared memory;  CTA barrier
+//   the owners write the interchanged rows, then every thread scales its rows' entry j and
+//   applies the rank-1 update to columns j+1 .. kb-1, searching column j+1 as it goes.
+// Slots of parity j are rewritten at column j + 2, after every CTA has passed the barrier
+// of column j + 1 and so finished its reads of column j.  (Posting column j+1 before the
+// rest of the update and overlapping that update with a split barrier was measured slower:
+// the extra CTA barriers cost more than the overlap saves.)  Same arithmetic, in the same
+// order, as panel_kernel.
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
                                                                      int32_t* __restrict__ ipiv_all,
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
   __shared__ C pub_j[2][kNB];                 // CTA 0: row j
   __shared__ T cand_v[2];
   __shared__ int cand_i[2];
-  __shared__ C urow[kNB], jrow[kNB];          // the pivot row and row j of the current step
+  __shared__ C urow[kNB], jrow[kNB];
   __shared__ T red_v[kPanelThreads / 32];
   __shared__ int red_i[kPanelThreads / 32];
   __shared__ int s_piv;
@@ -215,39 +217,30 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
   const int r0 = rank * chunk;  // first panel row of this CTA
   const int rows = (int)((m - r0) < chunk ? ((m - r0) > 0 ? (m - r0) : 0) : chunk);
 
-  // posts this CTA's candidate for column jj: every warp reduces the per-warp partials, the
-  // owner threads of the best row and (CTA 0) of row jj copy their rows
-  auto post = [&](int jj, T bv, int bix) {
-    warp_argmax(bv, bix);
-    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bix; }
-    __syncthreads();
-    bv = lane < kPanelThreads / 32 ? red_v[lane] : (T)-1;
-    bix = lane < kPanelThreads / 32 ? red_i[lane] : INT_MAX;
-    warp_argmax(bv, bix);
-    const int par = jj & 1;
-    if (tid == 0) { cand_v[par] = bv; cand_i[par] = bix; }
-    if (bix != INT_MAX && tid == (bix - r0) % kPanelThreads)
-      for (int c = 0; c < kb; ++c) pub_row[par][c] = sp[c * chunk + (bix - r0)];
-    if (rank == 0 && tid == jj)
-      for (int c = 0; c < kb; ++c) pub_j[par][c] = sp[c * chunk + jj];
-  };
-
   for (int c = 0; c < kb; ++c)
     for (int i = tid; i < rows; i += kPanelThreads) sp[c * chunk + i] = A[(k + r0 + i) + (k + c) * n];
-  {
-    T best = -1;
-    int bi = INT_MAX;
-    for (int i = tid; i < rows; i += kPanelThreads) {
-      const C a = sp[i];
-      argmax_merge(best, bi, fabs(a.x) + fabs(a.y), r0 + i);
-    }
-    post(0, best, bi);
+  // candidate for column 0 (each thread reads only its own rows)
+  T best = -1;
+  int bi = INT_MAX;
+  for (int i = tid; i < rows; i += kPanelThreads) {
+    const C a = sp[i];
+    argmax_merge(best, bi, fabs(a.x) + fabs(a.y), r0 + i);
   }
-  cluster_arrive();
-  cluster_wait();
   for (int j = 0; j < kb; ++j) {
     const int par = j & 1;
-    __syncthreads();  // every thread is done with the previous step's urow
+    // post this CTA's candidate for column j with a copy of its row, and (CTA 0) row j
+    warp_argmax(best, bi);
+    if (lane == 0) { red_v[warp] = best; red_i[warp] = bi; }
+    __syncthreads();
+    if (warp == 0) {
+      best = lane < kPanelThreads / 32 ? red_v[lane] : (T)-1;
+      bi = lane < kPanelThreads / 32 ? red_i[lane] : INT_MAX;
+      warp_argmax(best, bi);
+      if (lane == 0) { cand_v[par] = best; cand_i[par] = bi; }
+      if (bi != INT_MAX && lane < kb) pub_row[par][lane] = sp[lane * chunk + (bi - r0)];
+      if (rank == 0 && lane < kb) pub_j[par][lane] = sp[lane * chunk + j];
+    }
+    cl.sync();  // candidates and rows posted
     if (warp == 0) {
       T v = -1;
       int vi = INT_MAX;
@@ -259,21 +252,14 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
       const bool zero = !(v > 0);
       const int p = zero ? j : vi;  // panel row of the pivot
       const int owner = p / chunk;
-      C rj = czero<C>(), rp = czero<C>();
+      C u = czero<C>(), rj = czero<C>();
       if (lane < kb) {
         rj = cl.map_shared_rank(&pub_j[par][0], 0u)[lane];
-        rp = (p == j) ? rj : cl.map_shared_rank(&pub_row[par][0], (unsigned)owner)[lane];
+        u = (p == j) ? rj : cl.map_shared_rank(&pub_row[par][0], (unsigned)owner)[lane];
+        urow[lane] = u;
+        jrow[lane] = rj;
       }
-      if (j > 0) {  // the copies still lack step j-1's update of columns j+1 ..
-        const C lj = shfl_c(rj, j - 1), lpv = shfl_c(rp, j - 1);
-        if (lane > j && lane < kb) {
-          const C u = urow[lane];
-          rj = cfms(rj, lj, u);
-          rp = cfms(rp, lpv, u);
-        }
-      }
-      if (lane < kb) { urow[lane] = rp; jrow[lane] = rj; }
-      if (lane == j) s_inv = zero ? czero<C>() : crecip(rp);
+      if (lane == j) s_inv = zero ? czero<C>() : crecip(u);
       if (lane == 0) {
         s_piv = p;
         if (rank == 0) {
@@ -292,31 +278,19 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
         for (int c = 0; c < kb; ++c) sp[c * chunk + lp] = jrow[c];
     }
     const C inv = s_inv;
-    // look-ahead: scale column j and update column j+1 only
-    T best = -1;
-    int bi = INT_MAX;
+    best = -1;
+    bi = INT_MAX;
     for (int i = tid; i < rows; i += kPanelThreads) {
       const int pr = r0 + i;
       if (pr <= j) continue;
       const C l = cmul(sp[j * chunk + i], inv);
       sp[j * chunk + i] = l;
-      if (j + 1 < kb) {
-        const C v = cfms(sp[(j + 1) * chunk + i], l, urow[j + 1]);
-        sp[(j + 1) * chunk + i] = v;
-        argmax_merge(best, bi, fabs(v.x) + fabs(v.y), pr);
+      for (int c = j + 1; c < kb; ++c) {
+        const C v = cfms(sp[c * chunk + i], l, urow[c]);
+        sp[c * chunk + i] = v;
+        if (c == j + 1) argmax_merge(best, bi, fabs(v.x) + fabs(v.y), pr);
       }
     }
-    if (j + 1 < kb) {
-      post(j + 1, best, bi);
-      cluster_arrive();
-    }
-    for (int i = tid; i < rows; i += kPanelThreads) {
-      const int pr = r0 + i;
-      if (pr <= j) continue;
-      const C l = sp[j * chunk + i];
-      for (int c = j + 2; c < kb; ++c) sp[c * chunk + i] = cfms(sp[c * chunk + i], l, urow[c]);
-    }
-    if (j + 1 < kb) cluster_wait();
   }
   // other CTAs may still read this CTA's slots of the last column: wait for them
   cl.sync();

@@ -161,8 +161,24 @@ def test_surrogate_sweep_and_errors(mh, ctx):
     with pytest.raises(ValueError):
         mh.hydrodynamic_coefficients(body, p, mh.DirectBEM((mh.Rankine(), mh.GFWu(), mh.SurrogateDelhommeau())),
                                      ctx=ctx)
-    with pytest.raises(ValueError):
-        mh.batch_hydrodynamic_coefficients([body], [p], mh.DirectBEM("Surrogate"), ctx=ctx)
+
+
+def test_batch_takes_the_surrogate(mh, ctx):
+    """The many-body graph with the learned surrogate (a fallback queue per body inside the
+    graph) gives the per-body sweep's coefficients."""
+    mh.load_surrogate(ctx=ctx)
+    bodies = [mh.FloatingBody(mh.hemisphere_mesh(1.0, 6, 12), ["Heave", "Surge"]),
+              mh.FloatingBody(mh.vertical_cylinder_mesh(1.0, 2.0, 24, 8, 4), ["Heave", "Surge"])]
+    ps = [{"wave_frequencies": [0.6, 1.2], "radiating_dofs": ["Heave", "Surge"], "wave_directions": [0.0]},
+          {"wave_frequencies": [0.9, 1.5, 2.0], "radiating_dofs": ["Heave", "Surge"], "wave_directions": [0.0]}]
+    for prec in ("fp64", "mixed"):
+        F = mh.DirectBEM("Surrogate", precision=prec)
+        got = mh.batch_hydrodynamic_coefficients(bodies, ps, F, ctx=ctx, rho=1025.0)
+        for b, p, g in zip(bodies, ps, got):
+            ref = mh.hydrodynamic_coefficients(b, p, F, ctx=ctx, rho=1025.0)
+            for key in ("added_mass", "radiation_damping", "excitation_force"):
+                np.testing.assert_allclose(g[key], ref[key], rtol=1e-10, atol=1e-10 * np.abs(ref[key]).max())
+        ctx._L.mh_batch_release(ctx.handle)
 
 
 def test_surrogate_needs_parameters(mh):
