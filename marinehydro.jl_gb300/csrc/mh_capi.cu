@@ -39,7 +39,7 @@ struct BodyPlan {
   double2 *F = nullptr, *FK = nullptr;
   float2 *LU32 = nullptr, *X32 = nullptr;
   int32_t *ipiv = nullptr, *info = nullptr;
-  void* oz = nullptr;       // tensor-core FP64 update workspace (MH_PREC_FP64_TC)
+  void* oz = nullptr;       // tensor-core update workspace (FP64_TC: Ozaki digits; MIXED: BF16 terms)
   int* ozflag = nullptr;    // its timeout flag
   int4* fb_list = nullptr;  // learned surrogate: pairs queued for the exact kernel
   unsigned long long* fb_state = nullptr;  // queue count, overflow and timeout flags
@@ -106,7 +106,7 @@ namespace {
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
   kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
-  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotCount
+  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...) {
@@ -326,8 +326,18 @@ int factor_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, float
   BatchDesc d32 = d;
   d32.stride = nn;
   for (int64_t b = 0; b < d.batch; ++b) convert_z_to_c(ctx->stream, ctx->lc(), Adev + b * d.stride, LU32 + b * nn, nn);
-  lu_factor_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, info);
+  // the trailing updates on the BF16 tensor cores (three-way split, FP32 accuracy)
+  unsigned char* ws;
+  const size_t wsb = bx3_workspace_bytes(n, d.batch);
+  MH_TRY(ws_get_t(ctx, kSlotBx3, wsb + 256, &ws));
+  int* flag = reinterpret_cast<int*>(ws + wsb);
+  MH_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+  lu_factor_batched<float>(ctx->stream, ctx->lc(), d32, LU32, ipiv, info, ws, flag);
   MH_TRY(check_launch(ctx, "lu factor fp32"));
+  int hflag = 0;
+  MH_CUDA(ctx, cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MH_TRY(sync(ctx, "lu factor fp32"));
+  if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
   *LU32_out = LU32;
   return MH_OK;
 }
@@ -363,10 +373,14 @@ int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const
   matrix_inf_norms(ctx->stream, ctx->lc(), d, Adev, anrm_d);
   double* hn;
   MH_TRY(pinned_get(ctx, sizeof(double) * (2 * ncols + d.batch) + 64, &hn));
+  int* tcflag;  // the FP64-accurate residuals run on the tensor cores (forward solves)
+  MH_TRY(ws_get_t(ctx, kSlotTcFlag, 4, &tcflag));
+  MH_CUDA(ctx, cudaMemsetAsync(tcflag, 0, sizeof(int), ctx->stream));
   const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
   *converged = false;
   for (int it = 0; it <= 30; ++it) {
-    residual_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, adjoint);
+    if (adjoint) residual_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, true);
+    else residual_tc_batched(ctx->stream, ctx->lc(), d, Adev, X, B0, nrhs, xstride, R, work, tcflag);
     for (int64_t b = 0; b < d.batch; ++b) {
       inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, R + b * xstride, norms + b * nrhs);
       inf_norms_batched(ctx->stream, ctx->lc(), n, nrhs, X + b * xstride, norms + ncols + b * nrhs);
@@ -374,7 +388,10 @@ int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const
     MH_TRY(check_launch(ctx, "refinement"));
     MH_CUDA(ctx, cudaMemcpyAsync(hn, norms, sizeof(double) * (2 * ncols + d.batch), cudaMemcpyDeviceToHost,
                                  ctx->stream));
+    int* hflag = reinterpret_cast<int*>(hn + 2 * ncols + d.batch);
+    MH_CUDA(ctx, cudaMemcpyAsync(hflag, tcflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MH_TRY(sync(ctx, "refinement norms"));
+    if (*hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the refinement residual gave up");
     bool ok = true;
     for (int64_t c = 0; c < ncols && ok; ++c) {
       const double anrm = hn[2 * ncols + c / nrhs];
@@ -493,6 +510,9 @@ size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
   if (o.precision == MH_PREC_FP64_TC) {
     b.oz = take(ozaki_workspace_bytes(b.n, b.nw));
     b.ozflag = (int*)take(64);
+  } else if (mixed) {
+    b.oz = take(bx3_workspace_bytes(b.n, b.nw));
+    b.ozflag = (int*)take(64);
   }
   if (o.gfs & MH_GF_SURROGATE) {  // every self pair plus room for pairs outside the training box
     b.fb_cap = b.n * (b.nw + 64) + 4096;
@@ -550,30 +570,35 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   EpilogueGeom eg{n, b.m->C, b.m->N, b.m->A, b.dofs};
   launch_build_rhs(st, lc, eg, (int)nw, om_d, o.g, (int)o.n_rad, rad_d, (int)o.n_beta, beta_d, b.B, bstride);
   BatchDesc d{n, nw, nn};
-  if (o.direct) zgemm_nn_batched(st, lc, d, b.S, b.B, o.nrhs, bstride, b.X, b.work);
+  if (b.ozflag) cudaMemsetAsync(b.ozflag, 0, sizeof(int), st);
+  // S products on the tensor cores (FP64-accurate) outside the plain FP64 path
+  auto s_times = [&](const double2* in, double2* out) {
+    if (o.precision == MH_PREC_FP64) zgemm_nn_batched(st, lc, d, b.S, in, o.nrhs, bstride, out, b.work);
+    else zgemm_nn_tc_batched(st, lc, d, b.S, in, o.nrhs, bstride, out, b.work, b.ozflag);
+  };
+  if (o.direct) s_times(b.B, b.X);
   else cudaMemcpyAsync(b.X, b.B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
   if (o.precision == MH_PREC_FP64 || o.precision == MH_PREC_FP64_TC) {
-    if (b.ozflag) cudaMemsetAsync(b.ozflag, 0, sizeof(int), st);
     lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info, b.oz, b.ozflag);
     lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
   } else {
     BatchDesc d32{n, nw, nn};
     cudaMemcpyAsync(b.B0, b.X, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
     convert_z_to_c(st, lc, b.D, b.LU32, nn * nw);
-    lu_factor_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.info);
+    lu_factor_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.info, b.oz, b.ozflag);
     convert_z_to_c(st, lc, b.B0, b.X32, bstride * nw);
     lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
     widen_c_to_z(st, lc, b.X32, b.X, bstride * nw);
     const int64_t ncols = o.nrhs * nw;
     matrix_inf_norms(st, lc, d, b.D, b.norms + 2 * ncols);
     for (int it = 0; it < o.ir_sweeps; ++it) {
-      residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
+      residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
       convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
       lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
       ir_update(st, lc, bstride * nw, b.X, b.X32);
     }
     // the residual of the returned x, judged on the host after the graph
-    residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
+    residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
     for (int64_t w = 0; w < nw; ++w) {
       inf_norms_batched(st, lc, n, o.nrhs, b.R + w * bstride, b.norms + w * o.nrhs);
       inf_norms_batched(st, lc, n, o.nrhs, b.X + w * bstride, b.norms + ncols + w * o.nrhs);
@@ -582,7 +607,7 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   }
   double2* phi = b.X;
   if (!o.direct) {
-    zgemm_nn_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work);
+    s_times(b.X, b.B);
     phi = b.B;
   }
   if (o.n_inf > 0)
@@ -1066,16 +1091,32 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
     MH_TRY(check_launch(ctx, "boundary conditions"));
     BatchDesc d{n, nw, (int64_t)nn};
     MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, nw), &work));
+    // S times a block of vectors: FP64 FMAs in the plain path, the FP64-accurate tensor-core
+    // product in the others
+    int* tcflag;
+    MH_TRY(ws_get_t(ctx, kSlotTcFlag, 4, &tcflag));
+    auto s_times = [&](const double2* in, double2* out) -> int {
+      if (precision == MH_PREC_FP64) {
+        zgemm_nn_batched(ctx->stream, ctx->lc(), d, S, in, nrhs, bstride, out, work);
+        return check_launch(ctx, "S product");
+      }
+      MH_CUDA(ctx, cudaMemsetAsync(tcflag + 2, 0, sizeof(int), ctx->stream));
+      zgemm_nn_tc_batched(ctx->stream, ctx->lc(), d, S, in, nrhs, bstride, out, work, tcflag + 2);
+      MH_TRY(check_launch(ctx, "S product"));
+      int hflag = 0;
+      MH_CUDA(ctx, cudaMemcpyAsync(&hflag, tcflag + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      MH_TRY(sync(ctx, "S product"));
+      if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the S product gave up");
+      return MH_OK;
+    };
     if (direct) {
-      zgemm_nn_batched(ctx->stream, ctx->lc(), d, S, B, nrhs, bstride, X, work);
-      MH_TRY(check_launch(ctx, "S*bc"));
+      MH_TRY(s_times(B, X));
       MH_TRY(solve_core(ctx, d, D, X, nrhs, bstride, precision, false));
     } else {
       MH_CUDA(ctx, cudaMemcpyAsync(X, B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, ctx->stream));
       MH_TRY(solve_core(ctx, d, D, X, nrhs, bstride, precision, false));
       MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, nw), &work));
-      zgemm_nn_batched(ctx->stream, ctx->lc(), d, S, X, nrhs, bstride, B, work);
-      MH_TRY(check_launch(ctx, "S*sources"));
+      MH_TRY(s_times(X, B));
       std::swap(B, X);
     }
     if (n_inf > 0) {

@@ -129,6 +129,11 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
 // FP64 trailing update A22 -= L21 U12 of panel step k on the BF16 tensor cores (mh_ozaki.cu);
 // emu_ws: ozaki_workspace_bytes(n, batch) bytes; *timeout_flag set if a completion wait gave up
 size_t ozaki_workspace_bytes(int64_t n, int64_t batch);
+// FP32 trailing update of the mixed-precision factors on the BF16 tensor cores, three-way
+// split (mh_bf16x3.cu); ws: bx3_workspace_bytes(n, batch) bytes
+size_t bx3_workspace_bytes(int64_t n, int64_t batch);
+void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, float2* A, int64_t k, int kb,
+                         void* ws, int* timeout_flag);
 void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
                            void* ws, int* timeout_flag);
 template <typename T>
@@ -146,6 +151,16 @@ void convert_z_to_c(cudaStream_t st, LaunchCounter lc, const double2* src, float
 // R = B - A X (FP64), then C = (float) R ; returns nothing, norms into `norms` (per rhs: |R|_inf, |X|_inf)
 void residual_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
                       const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work, bool adjoint);
+// The same products on the BF16 tensor cores, FP64-accurate (mh_zgemv_tc.cu); A X only (no
+// adjoint), `work` as for zgemm_nn_batched; *timeout_flag set if a completion wait gave up.
+size_t tc_zgemv_workspace_bytes(int64_t n, int64_t batch);
+void tc_zgemv(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+              int64_t nrhs, int64_t xstride, double2* Y, const double2* B, void* ws, int* timeout_flag);
+void zgemm_nn_tc_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                         int64_t nrhs, int64_t xstride, double2* Y, double2* work, int* timeout_flag);
+void residual_tc_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                         const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work,
+                         int* timeout_flag);
 void ir_update(cudaStream_t st, LaunchCounter lc, int64_t count, double2* X, const float2* C);
 void widen_c_to_z(cudaStream_t st, LaunchCounter lc, const float2* src, double2* dst, int64_t count);
 void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out);

@@ -1036,11 +1036,13 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     if (rest <= 0) continue;
     dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
     MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
-    if constexpr (sizeof(T) == 8) {
-      if (emu_ws) {  // FP64 update on the BF16 tensor cores (mh_ozaki.cu)
+    if (emu_ws) {
+      if constexpr (sizeof(T) == 8) {  // FP64 update on the BF16 tensor cores (mh_ozaki.cu)
         ozaki_trailing_update(st, lc, d, A, k, (int)kb, emu_ws, emu_flag);
-        continue;
+      } else {  // FP32 update on the BF16 tensor cores (mh_bf16x3.cu)
+        bx3_trailing_update(st, lc, d, A, k, (int)kb, emu_ws, emu_flag);
       }
+      continue;
     }
     constexpr int TM = GemmTile<T>::TM;
     dim3 gg((unsigned)((rest + TM - 1) / TM), (unsigned)((rest + TM - 1) / TM), (unsigned)d.batch);
@@ -1156,7 +1158,20 @@ template void lu_solve_batched<float>(cudaStream_t, LaunchCounter, const BatchDe
                                       float2*, int64_t, int64_t, bool);
 
 size_t zgemm_work_elems(int64_t n, int64_t nrhs, int64_t batch) {
-  return (size_t)gemm_split(n, batch) * (size_t)batch * (size_t)nrhs * (size_t)n;
+  const size_t fp64 = (size_t)gemm_split(n, batch) * (size_t)batch * (size_t)nrhs * (size_t)n;
+  const size_t tc = (tc_zgemv_workspace_bytes(n, batch) + sizeof(double2) - 1) / sizeof(double2);
+  return fp64 > tc ? fp64 : tc;
+}
+
+void zgemm_nn_tc_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                         int64_t nrhs, int64_t xstride, double2* Y, double2* work, int* timeout_flag) {
+  tc_zgemv(st, lc, d, A, X, nrhs, xstride, Y, nullptr, work, timeout_flag);
+}
+
+void residual_tc_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
+                         const double2* B, int64_t nrhs, int64_t xstride, double2* R, double2* work,
+                         int* timeout_flag) {
+  tc_zgemv(st, lc, d, A, X, nrhs, xstride, R, B, work, timeout_flag);
 }
 
 static void zgemm_impl(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
