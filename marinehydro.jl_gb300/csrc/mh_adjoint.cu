@@ -84,8 +84,9 @@ template <typename R> __device__ R pdC(R t) {
 template <typename R>
 __device__ void wu_terms_t(R hh, R vv, CR<R>& GF, CR<R>& Gh, CR<R>& Gv) {
   R dd = sqrt(hh * hh + vv * vv);
-  R alpha = -vv / dd;
-  R beta = hh / dd;
+  const R inv_dd = 1.0 / dd;
+  R alpha = -vv * inv_dd;
+  R beta = hh * inv_dd;
   R rho = dd / (1.0 + dd);
   R dd2 = dd * dd, dd3 = dd * dd * dd;
   R omr = 1.0 - rho;
@@ -115,7 +116,8 @@ __device__ void wu_terms_t(R hh, R vv, CR<R>& GF, CR<R>& Gh, CR<R>& Gv) {
   R PP = log(0.5 * (dd - vv)) + gama - 2.0 * dd2;
   PP = ev * PP;
   PP = PP + dd2 - vv;
-  R L0 = 2.0 * PP / (1.0 + dd3) + 2.0 * Lp;
+  const R inv_1dd3 = 1.0 / (1.0 + dd3);
+  R L0 = 2.0 * PP * inv_1dd3 + 2.0 * Lp;
   const double twopi = 2 * kPi;
   GF.x = -L0 - (twopi * H0) * ev;
   GF.y = -((twopi * -J0) * ev);
@@ -126,11 +128,11 @@ __device__ void wu_terms_t(R hh, R vv, CR<R>& GF, CR<R>& Gh, CR<R>& Gv) {
   R PS = (beta + hh) / (dd - vv);
   PS = PS - 2.0 * beta + 2.0 * ev * dd - hh;
   R QS = exp(-dd) * (1.0 - beta);
-  QS = QS * (1.0 + dd / (1.0 + dd3));
-  R Ls = 2.0 * PS / (1.0 + dd3) - 4.0 * QS + 2.0 * Lsp;
+  QS = QS * (1.0 + dd * inv_1dd3);
+  R Ls = 2.0 * PS * inv_1dd3 - 4.0 * QS + 2.0 * Lsp;
   Gh.x = -Ls - (twopi * (2 / kPi - H1)) * ev;
   Gh.y = -((twopi * J1) * ev);
-  Gv.x = GF.x + 2.0 / dd;
+  Gv.x = GF.x + 2.0 * inv_dd;
   Gv.y = GF.y;
 }
 

@@ -235,10 +235,14 @@ __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& 
 }
 
 // _wu_wave_term_and_derivs (wu.jl:28-37) with GF_Func_L0/Lp/W/Ls/Lsp/Wh (wu.jl:201-366)
+// FP64 division is a multi-instruction sequence on GB300's FP64 pipe, which bounds this
+// kernel; 1/dd and 1/(1 + dd^3) are formed once and multiplied (rho stays a true division:
+// it feeds the fits A-D, whose alternating coefficients up to 2e5 amplify its last bit).
 __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv) {
   double dd = sqrt(hh * hh + vv * vv);
-  double alpha = -vv / dd;
-  double beta = hh / dd;
+  const double inv_dd = 1.0 / dd;
+  double alpha = -vv * inv_dd;
+  double beta = hh * inv_dd;
   double rho = dd / (1 + dd);
   double dd2 = dd * dd, dd3 = dd * dd * dd;
   double omr = 1.0 - rho;
@@ -257,7 +261,8 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   double PP = log(0.5 * (dd - vv)) + gama - 2.0 * dd2;
   PP = ev * PP;
   PP = PP + dd2 - vv;
-  double L0 = 2.0 * PP / (1.0 + dd3) + 2.0 * Lp;
+  const double inv_1dd3 = 1.0 / (1.0 + dd3);
+  double L0 = 2.0 * PP * inv_1dd3 + 2.0 * Lp;
   const double twopi = 2 * kPi;
   GF = make_double2(-L0 - (twopi * H0) * ev, -((twopi * -J0) * ev));
   // GF_Func_Lsp
@@ -269,10 +274,10 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   double PS = (beta + hh) / (dd - vv);
   PS = PS - 2.0 * beta + 2.0 * ev * dd - hh;
   double QS = exp(-dd) * (1.0 - beta);
-  QS = QS * (1.0 + dd / (1.0 + dd3));
-  double Ls = 2.0 * PS / (1.0 + dd3) - 4.0 * QS + 2.0 * Lsp;
+  QS = QS * (1.0 + dd * inv_1dd3);
+  double Ls = 2.0 * PS * inv_1dd3 - 4.0 * QS + 2.0 * Lsp;
   dGh = make_double2(-Ls - (twopi * (2 / kPi - H1)) * ev, -((twopi * J1) * ev));
-  dGv = make_double2(GF.x + 2 / dd, GF.y);
+  dGv = make_double2(GF.x + 2 * inv_dd, GF.y);
 }
 
 // _wu_reduced_hh_vv (wu.jl:7-18) == with_reduced_coordinates (abstract_greens_function.jl:192-213)

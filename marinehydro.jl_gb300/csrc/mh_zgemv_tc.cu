@@ -67,6 +67,34 @@ __device__ __forceinline__ long long fixed55(double v, int emax_biased) {
   return bits < 0 ? -X : X;
 }
 
+// the same digits with 32-bit arithmetic: X = hi 2^28 + lo, lo in [0, 2^28) gives digits 7..4
+// and a carry, hi (|hi| < 2^27) digits 3..0
+__device__ __forceinline__ void digits_of32(long long X, int (&dg)[kZvDigits]) {
+  int lo = (int)(X & 0xFFFFFFF);
+  int hi = (int)(X >> 28);
+#pragma unroll
+  for (int p = kZvDigits - 1; p >= 4; --p) {
+    const int c = lo + 64;
+    dg[p] = (c & 127) - 64;
+    lo = c >> 7;
+  }
+  hi += lo;
+#pragma unroll
+  for (int p = 3; p >= 1; --p) {
+    const int c = hi + 64;
+    dg[p] = (c & 127) - 64;
+    hi = c >> 7;
+  }
+  dg[0] = hi;
+}
+
+// two BF16 values (small integers) in one 32-bit word, the first in the low half
+__device__ __forceinline__ uint32_t bf16x2_of_small(int d0, int d1) {
+  const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
+  const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
+  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+}
+
 __device__ __forceinline__ void digits_of(long long X, int (&dg)[kZvDigits]) {
 #pragma unroll
   for (int p = kZvDigits - 1; p > 0; --p) {
@@ -239,14 +267,14 @@ __global__ void __launch_bounds__(kZvThreads) zgemv_tc_kernel(BatchDesc d, const
 #pragma unroll
       for (int c = 0; c < 8; c += 2) {
         int a0[kZvDigits], a1[kZvDigits], b0[kZvDigits], b1[kZvDigits];
-        digits_of(fixed55(vals[c].x, emax), a0);
-        digits_of(fixed55(vals[c + 1].x, emax), a1);
-        digits_of(fixed55(vals[c].y, emax), b0);
-        digits_of(fixed55(vals[c + 1].y, emax), b1);
+        digits_of32(fixed55(vals[c].x, emax), a0);
+        digits_of32(fixed55(vals[c + 1].x, emax), a1);
+        digits_of32(fixed55(vals[c].y, emax), b0);
+        digits_of32(fixed55(vals[c + 1].y, emax), b1);
 #pragma unroll
         for (int p = 0; p < kZvDigits; ++p) {
-          pk[0][p][c >> 1] = bf16_of_small(a0[p]) | (bf16_of_small(a1[p]) << 16);
-          pk[1][p][c >> 1] = bf16_of_small(b0[p]) | (bf16_of_small(b1[p]) << 16);
+          pk[0][p][c >> 1] = bf16x2_of_small(a0[p], a1[p]);
+          pk[1][p][c >> 1] = bf16x2_of_small(b0[p], b1[p]);
         }
       }
       const uint32_t off = tc::kmajor_offset(srow, 8 * sq, kZvK);
