@@ -27,7 +27,9 @@
 //     bulk copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (8 - p)
 //     multiplies X_p by the stacked Y_0 .. Y_{7-p} and accumulates X_p Y_q into the TMEM
 //     columns of T_{p+q} (Re: 32 d, Im: 256 + 32 d), so 64 MMAs (8 digits x 2 K-steps x 4
-//     real products) cover the 36 digit pairs.  The epilogue converts the exact integers
+//     real products) cover the 36 digit pairs.  (16-column tiles, whose two accumulator sets
+//     fit TMEM twice so that the products overlap the epilogue, measured 12 % slower: they
+//     read every A tile twice as often.)  The epilogue converts the exact integers
 //     with magic-number additions (no integer-to-FP64 conversion instructions), combines
 //     them in 32/64-bit integers and applies C -= 2^s (hi + lo 2^-28) with one FP64 add and
 //     two FMAs per real entry; C is prefetched into registers while the MMAs run.
@@ -44,13 +46,12 @@ namespace {
 constexpr int kOzDigits = 8;
 constexpr int kOzK = 32;            // panel width (the LU's kNB)
 constexpr int kOzRows = 128;        // output rows per CTA (MMA M)
-constexpr int kOzCols = 16;         // output columns per column tile
+constexpr int kOzCols = 32;         // output columns per CTA (MMA N)
 constexpr int kOzATile = kOzRows * kOzK * 2;    // bytes of one A digit tile (128 x 32 BF16)
-constexpr int kOzBTile = kOzCols * kOzK * 2;    // bytes of one B digit tile (16 x 32 BF16)
+constexpr int kOzBTile = kOzCols * kOzK * 2;    // bytes of one B digit tile (32 x 32 BF16)
 constexpr int kOzABytes = kOzDigits * 2 * kOzATile;   // 128 KB per row tile
-constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 16 KB per column tile
-constexpr int kOzAcc = 2 * kOzDigits * kOzCols;       // 256 TMEM columns: T_0..7, Re and Im
-constexpr uint32_t kOzTmemCols = 512;                 // two accumulator sets
+constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 32 KB per column tile
+constexpr uint32_t kOzTmemCols = 512;
 constexpr uint32_t kOzWaitPolls = 1u << 26;
 
 // exponent e with |v| < 2^e for the largest |v| of a row / column (0 for all-zero)
@@ -145,14 +146,13 @@ __global__ void ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__
 // 2^s as a double, s in the normal range
 __device__ __forceinline__ double pow2(int s) { return __longlong_as_double((long long)(s + 1023) << 52); }
 
-constexpr int kOzGroup = 8;     // column tiles per CTA (the A tiles are loaded once for all of them)
+constexpr int kOzGroup = 4;    // column tiles per CTA (the A tiles are loaded once for all of them)
 constexpr int kOzThreads = 256; // two threads per output row: warps w and w + 4 share TMEM lanes
-                                // 32 (w % 4) .. and take one half of the 16 columns each
+                                // 32 (w % 4) .. and take one half of the 32 columns each
 
 // One CTA per (row tile, group of kOzGroup column tiles, matrix).  The A digit tiles and the
-// first two B tiles arrive by TMA bulk copies; the B tiles are double-buffered, and so are
-// the accumulators: the products of column tile t run while the epilogue of tile t - 1
-// reads the other accumulator set.
+// first B tile arrive by TMA bulk copies on one mbarrier; the B tiles are double-buffered,
+// the next one prefetched while the current tile's products and epilogue run.
 __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
                                                               int64_t rest, int64_t nrt, int64_t nct,
                                                               const unsigned char* __restrict__ digA,
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
                                                               int* __restrict__ timeout_flag) {
   extern __shared__ __align__(1024) unsigned char osm[];
   __shared__ __align__(8) uint64_t mbar_load[2];
-  __shared__ __align__(8) uint64_t mbar_mma[2];
+  __shared__ __align__(8) uint64_t mbar_mma;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
@@ -176,8 +176,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   if (tid == 0) {
     tc::mbar_init(&mbar_load[0], 1);
     tc::mbar_init(&mbar_load[1], 1);
-    tc::mbar_init(&mbar_mma[0], 1);
-    tc::mbar_init(&mbar_mma[1], 1);
+    tc::mbar_init(&mbar_mma, 1);
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base, kOzTmemCols);
   tc::fence_before_sync();
@@ -199,137 +198,112 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const bool row_live = r < rest;
   const int er = row_live ? rowexp[b * rest + r] : 0;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  double2* crow = A + b * d.stride + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
+  double2* Ab = A + b * d.stride;
+  double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
   bool failed = false;
-  int loads_pending = ntile > 1 ? 2 : 1, mma_pending = 0;
-
-  // the 64 products of column tile t into accumulator set t & 1
-  auto issue = [&](int t) {
-    tc::fence_after_sync();
-    const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs[t & 1]);
-    const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
-    const uint32_t acc0 = tmem + (uint32_t)((t & 1) * kOzAcc);
+  int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
+  for (int t = 0; t < ntile; ++t) {
+    const int buf = t & 1;
+    const int64_t ct = ct0 + t;
+    bool ok = tc::mbar_wait(&mbar_load[buf], (uint32_t)((t >> 1) & 1), kOzWaitPolls);
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+    --outstanding_load;
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs[buf]);
+      const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
 #pragma unroll 1
-    for (int p = 0; p < kOzDigits; ++p) {
-      const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{7-p} stacked along N
-      const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
-      const uint32_t t_re = acc0 + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
-      const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
+      for (int p = 0; p < kOzDigits; ++p) {
+        const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{7-p} stacked along N
+        const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
+        const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
+        const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
 #pragma unroll
-      for (int kk = 0; kk < kOzK / 16; ++kk) {
-        const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
-        const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
-        const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
-        const uint64_t dbr = tc::smem_desc(bre + ko, 128, sbo), dbi = tc::smem_desc(bim + ko, 128, sbo);
-        tc::mma_bf16(t_re, dar, dbr, id, acc);      // Re T += Xre Yre
-        tc::mma_bf16(t_re, dai, dbi, id_neg, 1u);   // Re T -= Xim Yim
-        tc::mma_bf16(t_im, dar, dbi, id, acc);      // Im T += Xre Yim
-        tc::mma_bf16(t_im, dai, dbr, id, 1u);       // Im T += Xim Yre
+        for (int kk = 0; kk < kOzK / 16; ++kk) {
+          const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
+          const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
+          const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
+          const uint64_t dbr = tc::smem_desc(bre + ko, 128, sbo), dbi = tc::smem_desc(bim + ko, 128, sbo);
+          tc::mma_bf16(t_re, dar, dbr, id, acc);      // Re T += Xre Yre
+          tc::mma_bf16(t_re, dai, dbi, id_neg, 1u);   // Re T -= Xim Yim
+          tc::mma_bf16(t_im, dar, dbi, id, acc);      // Im T += Xre Yim
+          tc::mma_bf16(t_im, dai, dbr, id, 1u);       // Im T += Xim Yre
+        }
       }
+      tc::mma_commit(&mbar_mma);
     }
-    tc::mma_commit(&mbar_mma[t & 1]);
-  };
-  // this thread's 8 entries of A22 in column tile t and their column exponents
-  double2 cv[8];
-  int ce[8];
-  auto prefetch = [&](int t) {
-    const int64_t cbase = (ct0 + t) * kOzCols + half * 8;
+    // while the products run: this thread's 16 entries of A22 and their column exponents
+    double2 cv[kOzCols / 2];
+    int ce[kOzCols / 2];
+    const int64_t cbase = ct * kOzCols + half * (kOzCols / 2);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < kOzCols / 2; ++q) {
       const int64_t c = cbase + q;
       const bool live = row_live && c < rest;
       cv[q] = live ? crow[c * n] : make_double2(0.0, 0.0);
       ce[q] = live ? colexp[b * rest + c] : 0;
     }
-  };
-  // A22 -= the accumulators of column tile t
-  auto epilogue = [&](int t) {
-    const uint32_t acc0 = trow + (uint32_t)((t & 1) * kOzAcc) + (uint32_t)(half * 8);
-    // T_d as exact integers: (T0 2^7 + T1, T2 2^7 + T3, T4 2^7 + T5, T6 2^7 + T7), re and im
-    int pr[4][8], pi[4][8];
+    ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+    tc::fence_after_sync();
+    // this B buffer is free again: prefetch tile t + 2 into it
+    if (tid == 0 && t + 2 < ntile) {
+      tc::mbar_arrive_expect_tx(&mbar_load[buf], kOzBBytes);
+      tc::bulk_g2s(Bs[buf], srcB(ct + 2), kOzBBytes, &mbar_load[buf]);
+    }
+    if (t + 2 < ntile) ++outstanding_load;
 #pragma unroll
-    for (int dd = 0; dd < kOzDigits; ++dd) {
-      float vr[8], vi[8];
-      tc::tmem_ld8(acc0 + (uint32_t)(dd * kOzCols), vr);
-      tc::tmem_ld8(acc0 + (uint32_t)(kOzDigits * kOzCols + dd * kOzCols), vi);
+    for (int h8 = 0; h8 < 2; ++h8) {
+      const int c0 = half * (kOzCols / 2) + 8 * h8;
+      // T_d as exact integers: (T0 2^7 + T1, T2 2^7 + T3, T4 2^7 + T5, T6 2^7 + T7), re and im
+      int pr[4][8], pi[4][8];
+#pragma unroll
+      for (int dd = 0; dd < kOzDigits; ++dd) {
+        float vr[8], vi[8];
+        tc::tmem_ld8(trow + (uint32_t)(dd * kOzCols + c0), vr);
+        tc::tmem_ld8(trow + (uint32_t)(kOzDigits * kOzCols + dd * kOzCols + c0), vi);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          // |T| < 2^21: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
+          const int ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
+          const int ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
+          if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 128 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 128 + ii; }
+          else { pr[dd >> 1][q] = ir; pi[dd >> 1][q] = ii; }
+        }
+      }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        // |T| < 2^21: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
-        const int ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
-        const int ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
-        if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 128 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 128 + ii; }
-        else { pr[dd >> 1][q] = ir; pi[dd >> 1][q] = ii; }
+        const int qq = 8 * h8 + q;
+        // hi = T0..T3 and lo = T4..T7 in base 2^7 (|.| < 2^43); 1.5 2^52 + x as a double is exact
+        const long long kMagic = 0x4338000000000000LL;
+        const long long hr = (long long)pr[0][q] * 16384 + pr[1][q], lr = (long long)pr[2][q] * 16384 + pr[3][q];
+        const long long hi = (long long)pi[0][q] * 16384 + pi[1][q], li = (long long)pi[2][q] * 16384 + pi[3][q];
+        // (1.5 2^52 + lo) 2^-28 + (hi - 1.5 2^24) = hi + lo 2^-28, rounded once
+        constexpr double kBias = 6755399441055744.0 + 25165824.0;  // 1.5 2^52 + 1.5 2^24
+        const double xr = fma(__longlong_as_double(lr + kMagic), 0x1p-28, __longlong_as_double(hr + kMagic) - kBias);
+        const double xi = fma(__longlong_as_double(li + kMagic), 0x1p-28, __longlong_as_double(hi + kMagic) - kBias);
+        // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
+        const double sc = pow2(er + ce[qq] - 33);
+        cv[qq].x = fma(-xr, sc, cv[qq].x);
+        cv[qq].y = fma(-xi, sc, cv[qq].y);
       }
-    }
-    const int64_t cbase = (ct0 + t) * kOzCols + half * 8;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      // hi = T0..T3 and lo = T4..T7 in base 2^7 (|.| < 2^43); 1.5 2^52 + x as a double is exact
-      const long long kMagic = 0x4338000000000000LL;
-      const long long hr = (long long)pr[0][q] * 16384 + pr[1][q], lr = (long long)pr[2][q] * 16384 + pr[3][q];
-      const long long hi = (long long)pi[0][q] * 16384 + pi[1][q], li = (long long)pi[2][q] * 16384 + pi[3][q];
-      // (1.5 2^52 + lo) 2^-28 + (hi - 1.5 2^24) = hi + lo 2^-28, rounded once
-      constexpr double kBias = 6755399441055744.0 + 25165824.0;  // 1.5 2^52 + 1.5 2^24
-      const double xr = fma(__longlong_as_double(lr + kMagic), 0x1p-28, __longlong_as_double(hr + kMagic) - kBias);
-      const double xi = fma(__longlong_as_double(li + kMagic), 0x1p-28, __longlong_as_double(hi + kMagic) - kBias);
-      // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
-      const double sc = pow2(er + ce[q] - 33);
-      cv[q].x = fma(-xr, sc, cv[q].x);
-      cv[q].y = fma(-xi, sc, cv[q].y);
     }
     if (row_live) {
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
+      for (int q = 0; q < kOzCols / 2; ++q)
         if (cbase + q < rest) crow[(cbase + q) * n] = cv[q];
     }
-  };
-
-  for (int t = 0; t < ntile && !failed; ++t) {
-    bool ok = tc::mbar_wait(&mbar_load[t & 1], (uint32_t)((t >> 1) & 1), kOzWaitPolls);
-    if (__syncthreads_or(!ok)) { failed = true; break; }
-    --loads_pending;
-    if (tid == 0) issue(t);
-    ++mma_pending;
-    if (t > 0) {
-      prefetch(t - 1);
-      // tile t-1: its products are done, so its B buffer takes tile t+1 and its result is read
-      ok = tc::mbar_wait(&mbar_mma[(t - 1) & 1], (uint32_t)(((t - 1) >> 1) & 1), kOzWaitPolls);
-      if (__syncthreads_or(!ok)) { failed = true; break; }
-      --mma_pending;
-      tc::fence_after_sync();
-      if (t + 1 < ntile) {
-        if (tid == 0) {
-          tc::mbar_arrive_expect_tx(&mbar_load[(t + 1) & 1], kOzBBytes);
-          tc::bulk_g2s(Bs[(t + 1) & 1], srcB(ct0 + t + 1), kOzBBytes, &mbar_load[(t + 1) & 1]);
-        }
-        ++loads_pending;
-      }
-      epilogue(t - 1);
-      // every read of accumulator set (t-1) & 1 is done before tile t+1's products overwrite it
-      tc::fence_before_sync();
-      __syncthreads();
-    }
-  }
-  if (!failed) {
-    const int t = ntile - 1;
-    prefetch(t);
-    const bool ok = tc::mbar_wait(&mbar_mma[t & 1], (uint32_t)((t >> 1) & 1), kOzWaitPolls);
-    if (__syncthreads_or(!ok)) failed = true;
-    else {
-      --mma_pending;
-      tc::fence_after_sync();
-      epilogue(t);
-    }
+    // every TMEM read of this tile is done before the next tile's products overwrite it
+    tc::fence_before_sync();
+    __syncthreads();
   }
   if (failed) {
     // reported by the host as a timeout; drain the products and copies in flight (bounded)
     // before the tensor memory and shared memory are released
     if (tid == 0) atomicExch(timeout_flag, 1);
-    if (mma_pending > 0) {
-      tc::mbar_wait(&mbar_mma[0], 0, kOzWaitPolls);
-      tc::mbar_wait(&mbar_mma[1], 0, kOzWaitPolls);
-    }
-    if (loads_pending > 0) {
+    tc::mbar_wait(&mbar_mma, 0, kOzWaitPolls);
+    tc::mbar_wait(&mbar_mma, 1, kOzWaitPolls);
+    if (outstanding_load > 0) {
       tc::mbar_wait(&mbar_load[0], 0, kOzWaitPolls);
       tc::mbar_wait(&mbar_load[1], 0, kOzWaitPolls);
     }
