@@ -49,49 +49,71 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 (&t)[kBxTerms]) {
   t[2] = __float2bfloat16_rn(r2);
 }
 
-// one 128-row tile of `rows`-major data: element (r, kk) of the tile at plane offset
-__device__ __forceinline__ void store_terms(unsigned char* tile, int r, int kk, float2 v) {
-  __nv_bfloat16 tr[kBxTerms], ti[kBxTerms];
-  split3(v.x, tr);
-  split3(v.y, ti);
-  const uint32_t off = tc::kmajor_offset(r, kk, kBxK);
+// eight consecutive K values of one row of a tile -> six 16-byte chunks (re/im x 3 terms)
+__device__ __forceinline__ void store_terms8(unsigned char* tile, int r, int k8, const float2 (&v)[8]) {
+  uint32_t pk[2][kBxTerms][4];
 #pragma unroll
-  for (int p = 0; p < kBxTerms; ++p) {
-    *reinterpret_cast<__nv_bfloat16*>(tile + p * kBxPlane + off) = tr[p];
-    *reinterpret_cast<__nv_bfloat16*>(tile + (kBxTerms + p) * kBxPlane + off) = ti[p];
+  for (int c = 0; c < 8; c += 2) {
+    __nv_bfloat16 a0[kBxTerms], a1[kBxTerms], b0[kBxTerms], b1[kBxTerms];
+    split3(v[c].x, a0);
+    split3(v[c + 1].x, a1);
+    split3(v[c].y, b0);
+    split3(v[c + 1].y, b1);
+#pragma unroll
+    for (int p = 0; p < kBxTerms; ++p) {
+      pk[0][p][c >> 1] = (uint32_t)__bfloat16_as_ushort(a0[p]) | ((uint32_t)__bfloat16_as_ushort(a1[p]) << 16);
+      pk[1][p][c >> 1] = (uint32_t)__bfloat16_as_ushort(b0[p]) | ((uint32_t)__bfloat16_as_ushort(b1[p]) << 16);
+    }
   }
+  const uint32_t off = tc::kmajor_offset(r, k8, kBxK);
+#pragma unroll
+  for (int part = 0; part < 2; ++part)
+#pragma unroll
+    for (int p = 0; p < kBxTerms; ++p)
+      *reinterpret_cast<uint4*>(tile + (part * kBxTerms + p) * kBxPlane + off) =
+          make_uint4(pk[part][p][0], pk[part][p][1], pk[part][p][2], pk[part][p][3]);
 }
 
-// L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32)
+// L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32); four
+// threads per row, eight columns each
 __global__ void bx3_split_rows_kernel(BatchDesc d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
                                       int64_t ntile, unsigned char* __restrict__ tiles) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded row of the trailing block
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t r = t >> 2;  // padded row of the trailing block
+  const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (r >= ntile * kBxTile) return;
   const int64_t n = d.n;
   const float2* Ab = A + b * d.stride;
-  unsigned char* tile = tiles + (b * ntile + r / kBxTile) * (int64_t)kBxTileBytes;
   const bool live = r < rest;
-  for (int kk = 0; kk < kBxK; ++kk) {
-    const float2 v = (live && kk < kb) ? Ab[(k + kb + r) + (k + kk) * n] : make_float2(0.f, 0.f);
-    store_terms(tile, (int)(r % kBxTile), kk, v);
+  float2 v[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int kk = 8 * kq + c;
+    v[c] = (live && kk < kb) ? Ab[(k + kb + r) + (k + kk) * n] : make_float2(0.f, 0.f);
   }
+  store_terms8(tiles + (b * ntile + r / kBxTile) * (int64_t)kBxTileBytes, (int)(r % kBxTile), 8 * kq, v);
 }
 
-// U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1
+// U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1; four threads per
+// column, eight rows each
 __global__ void bx3_split_cols_kernel(BatchDesc d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
                                       int64_t ntile, unsigned char* __restrict__ tiles) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded column of the trailing block
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = t >> 2;  // padded column of the trailing block
+  const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (c >= ntile * kBxTile) return;
   const int64_t n = d.n;
   const float2* Ab = A + b * d.stride;
-  unsigned char* tile = tiles + (b * ntile + c / kBxTile) * (int64_t)kBxTileBytes;
   const bool live = c < rest;
-  for (int kk = 0; kk < kBxK; ++kk) {
-    const float2 v = (live && kk < kb) ? Ab[(k + kk) + (k + kb + c) * n] : make_float2(0.f, 0.f);
-    store_terms(tile, (int)(c % kBxTile), kk, v);
+  float2 v[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int kk = 8 * kq + q;
+    v[q] = (live && kk < kb) ? Ab[(k + kk) + (k + kb + c) * n] : make_float2(0.f, 0.f);
   }
+  store_terms8(tiles + (b * ntile + c / kBxTile) * (int64_t)kBxTileBytes, (int)(c % kBxTile), 8 * kq, v);
 }
 
 __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float2* __restrict__ A, int64_t k, int kb,
@@ -266,9 +288,9 @@ void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, 
   const int64_t nt = (rest + kBxTile - 1) / kBxTile, nt_max = (d.n + kBxTile - 1) / kBxTile;
   unsigned char* tA = static_cast<unsigned char*>(ws);
   unsigned char* tB = tA + d.batch * nt_max * (int64_t)kBxTileBytes;
-  dim3 gs((unsigned)nt, (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_rows_kernel<<<gs, kBxTile, 0, st>>>(d, A, k, kb, rest, nt, tA));
-  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_cols_kernel<<<gs, kBxTile, 0, st>>>(d, A, k, kb, rest, nt, tB));
+  dim3 gs((unsigned)(nt * 2), (unsigned)d.batch);  // 4 threads per row / column, 256 per CTA
+  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_rows_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, tA));
+  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_cols_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, tB));
   const size_t smem = 3 * (size_t)kBxTileBytes;
   cudaFuncSetAttribute(bx3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 gg((unsigned)nt, (unsigned)((nt + kBxGroup - 1) / kBxGroup), (unsigned)d.batch);

@@ -929,14 +929,28 @@ __global__ void col_inf_norm_kernel(int64_t n, const double2* __restrict__ X, do
 
 // out[b] = max_i sum_j |re|+|im| of matrix b (|.|_inf, order independent via atomicMax on the bits
 // of a non-negative double); out must be zeroed first
-__global__ void mat_inf_norm_kernel(BatchDesc d, const double2* __restrict__ A, unsigned long long* __restrict__ out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// 128 rows x 8 column slices per CTA (more loads in flight than one thread per row); the
+// slices' partial row sums are added in a fixed order
+__global__ void __launch_bounds__(1024) mat_inf_norm_kernel(BatchDesc d, const double2* __restrict__ A,
+                                                            unsigned long long* __restrict__ out) {
+  __shared__ double part[8][128];
+  const int64_t i = blockIdx.x * (int64_t)128 + threadIdx.x;
   const int64_t b = blockIdx.y;
-  if (i >= d.n) return;
+  const int64_t n = d.n;
   const double2* Ab = A + b * d.stride;
+  const int64_t j0 = (n * threadIdx.y) / 8, j1 = (n * (threadIdx.y + 1)) / 8;
   double s = 0.0;
-  for (int64_t j = 0; j < d.n; ++j) { double2 v = Ab[i + j * d.n]; s += fabs(v.x) + fabs(v.y); }
-  atomicMax(out + b, (unsigned long long)__double_as_longlong(s));
+  if (i < n) {
+#pragma unroll 4
+    for (int64_t j = j0; j < j1; ++j) { const double2 v = Ab[i + j * n]; s += fabs(v.x) + fabs(v.y); }
+  }
+  part[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && i < n) {
+    double t = 0.0;
+    for (int y = 0; y < 8; ++y) t += part[y][threadIdx.x];
+    atomicMax(out + b, (unsigned long long)__double_as_longlong(t));
+  }
 }
 
 }  // namespace
@@ -944,7 +958,7 @@ __global__ void mat_inf_norm_kernel(BatchDesc d, const double2* __restrict__ A, 
 void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out) {
   cudaMemsetAsync(out, 0, sizeof(double) * d.batch, st);
   dim3 grid((unsigned)((d.n + 127) / 128), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "ir_norms", mat_inf_norm_kernel<<<grid, 128, 0, st>>>(d, A, (unsigned long long*)out));
+  MH_LAUNCH(lc, st, "ir_norms", mat_inf_norm_kernel<<<grid, dim3(128, 8), 0, st>>>(d, A, (unsigned long long*)out));
 }
 
 // CTAs per cluster for a panel of m rows in a batch of `batch` matrices: enough to hold

@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include "mh_digits.cuh"
 #include "mh_internal.cuh"
 #include "mh_tc.cuh"
 
@@ -54,92 +55,76 @@ constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 32 KB per column tile
 constexpr uint32_t kOzTmemCols = 512;
 constexpr uint32_t kOzWaitPolls = 1u << 26;
 
-// exponent e with |v| < 2^e for the largest |v| of a row / column (0 for all-zero)
-__device__ __forceinline__ int scale_exponent(double maxabs) {
-  if (!(maxabs > 0.0)) return 0;
-  int e;
-  frexp(maxabs, &e);
-  return e;
-}
-
-// balanced base-128 digits of round(v 2^(55 - e)), most significant first; |v| < 2^e keeps
-// |X| < 2^55, so the leading digit is in [-64, 64] as well
-__device__ __forceinline__ void digits8(double v, int e, int (&dg)[kOzDigits]) {
-  long long X = llrint(ldexp(v, 55 - e));
-#pragma unroll
-  for (int p = kOzDigits - 1; p > 0; --p) {
-    const long long t = ((X + 64) & 127) - 64;
-    dg[p] = (int)t;
-    X = (X - t) >> 7;
-  }
-  dg[0] = (int)X;
-}
-
-// L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32)
-__global__ void ozaki_split_rows_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k, int kb, int64_t rest,
-                                        int64_t nrt, unsigned char* __restrict__ digA, int* __restrict__ rowexp) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded row of the trailing block
+// L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32).  Four
+// threads per row, eight columns each: the row's largest exponent by shuffles, then its
+// digits with integer arithmetic (mh_digits.cuh), one 16-byte store per digit plane.
+__global__ void __launch_bounds__(256) ozaki_split_rows_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k,
+                                                               int kb, int64_t rest, int64_t nrt,
+                                                               unsigned char* __restrict__ digA,
+                                                               int* __restrict__ rowexp) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t r = t >> 2;  // padded row of the trailing block
+  const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
-  if (r >= nrt * kOzRows) return;
+  if (r >= nrt * kOzRows) return;  // whole groups of four leave together
   const int64_t n = d.n;
   const double2* Ab = A + b * d.stride;
   const bool live = r < rest;
-  double mx = 0.0;
-  if (live)
-    for (int kk = 0; kk < kb; ++kk) {
-      const double2 v = Ab[(k + kb + r) + (k + kk) * n];
-      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
-    }
-  const int e = scale_exponent(mx);
-  if (live) rowexp[b * rest + r] = e;
-  unsigned char* tiles = digA + ((b * nrt + r / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
-  const int rr = (int)(r % kOzRows);
-  for (int kk = 0; kk < kOzK; ++kk) {
-    double2 v = make_double2(0.0, 0.0);
-    if (live && kk < kb) v = Ab[(k + kb + r) + (k + kk) * n];
-    int dre[kOzDigits], dim[kOzDigits];
-    digits8(v.x, e, dre);
-    digits8(v.y, e, dim);
-    const uint32_t off = tc::kmajor_offset(rr, kk, kOzK);
+  double2 v[8];
+  int emax = 0;
 #pragma unroll
-    for (int p = 0; p < kOzDigits; ++p) {
-      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p) * kOzATile + off) = __float2bfloat16_rn((float)dre[p]);
-      *reinterpret_cast<__nv_bfloat16*>(tiles + (2 * p + 1) * kOzATile + off) = __float2bfloat16_rn((float)dim[p]);
-    }
+  for (int c = 0; c < 8; ++c) {
+    const int kk = 8 * kq + c;
+    v[c] = (live && kk < kb) ? Ab[(k + kb + r) + (k + kk) * n] : make_double2(0.0, 0.0);
+    emax = max(emax, max(dg::biased_exp(v[c].x), dg::biased_exp(v[c].y)));
+  }
+  emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+  emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+  if (live && kq == 0) rowexp[b * rest + r] = dg::scale_of(emax);
+  uint32_t pk[2][dg::kDigits][4];
+  dg::split8(v, emax, pk);
+  unsigned char* tiles = digA + ((b * nrt + r / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
+  const uint32_t off = tc::kmajor_offset((int)(r % kOzRows), 8 * kq, kOzK);
+#pragma unroll
+  for (int p = 0; p < kOzDigits; ++p) {
+    *reinterpret_cast<uint4*>(tiles + (2 * p) * kOzATile + off) = make_uint4(pk[0][p][0], pk[0][p][1], pk[0][p][2], pk[0][p][3]);
+    *reinterpret_cast<uint4*>(tiles + (2 * p + 1) * kOzATile + off) = make_uint4(pk[1][p][0], pk[1][p][1], pk[1][p][2], pk[1][p][3]);
   }
 }
 
-// U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1
-__global__ void ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k, int kb, int64_t rest,
-                                        int64_t nct, unsigned char* __restrict__ digB, int* __restrict__ colexp) {
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // padded column of the trailing block
+// U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1; four threads per
+// column, eight rows each
+__global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k,
+                                                               int kb, int64_t rest, int64_t nct,
+                                                               unsigned char* __restrict__ digB,
+                                                               int* __restrict__ colexp) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = t >> 2;  // padded column of the trailing block
+  const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (c >= nct * kOzCols) return;
   const int64_t n = d.n;
   const double2* Ab = A + b * d.stride;
   const bool live = c < rest;
-  double mx = 0.0;
-  if (live)
-    for (int kk = 0; kk < kb; ++kk) {
-      const double2 v = Ab[(k + kk) + (k + kb + c) * n];
-      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
-    }
-  const int e = scale_exponent(mx);
-  if (live) colexp[b * rest + c] = e;
-  unsigned char* tiles = digB + ((b * nct + c / kOzCols) * kOzDigits * 2) * (int64_t)kOzBTile;
-  const int cc = (int)(c % kOzCols);
-  for (int kk = 0; kk < kOzK; ++kk) {
-    double2 v = make_double2(0.0, 0.0);
-    if (live && kk < kb) v = Ab[(k + kk) + (k + kb + c) * n];
-    int dre[kOzDigits], dim[kOzDigits];
-    digits8(v.x, e, dre);
-    digits8(v.y, e, dim);
-    const uint32_t off = tc::kmajor_offset(cc, kk, kOzK);
+  double2 v[8];
+  int emax = 0;
 #pragma unroll
-    for (int p = 0; p < kOzDigits; ++p) {
-      *reinterpret_cast<__nv_bfloat16*>(tiles + p * kOzBTile + off) = __float2bfloat16_rn((float)dre[p]);
-      *reinterpret_cast<__nv_bfloat16*>(tiles + (kOzDigits + p) * kOzBTile + off) = __float2bfloat16_rn((float)dim[p]);
-    }
+  for (int q = 0; q < 8; ++q) {
+    const int kk = 8 * kq + q;
+    v[q] = (live && kk < kb) ? Ab[(k + kk) + (k + kb + c) * n] : make_double2(0.0, 0.0);
+    emax = max(emax, max(dg::biased_exp(v[q].x), dg::biased_exp(v[q].y)));
+  }
+  emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+  emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+  if (live && kq == 0) colexp[b * rest + c] = dg::scale_of(emax);
+  uint32_t pk[2][dg::kDigits][4];
+  dg::split8(v, emax, pk);
+  unsigned char* tiles = digB + ((b * nct + c / kOzCols) * kOzDigits * 2) * (int64_t)kOzBTile;
+  const uint32_t off = tc::kmajor_offset((int)(c % kOzCols), 8 * kq, kOzK);
+#pragma unroll
+  for (int p = 0; p < kOzDigits; ++p) {
+    *reinterpret_cast<uint4*>(tiles + p * kOzBTile + off) = make_uint4(pk[0][p][0], pk[0][p][1], pk[0][p][2], pk[0][p][3]);
+    *reinterpret_cast<uint4*>(tiles + (kOzDigits + p) * kOzBTile + off) = make_uint4(pk[1][p][0], pk[1][p][1], pk[1][p][2], pk[1][p][3]);
   }
 }
 
@@ -330,10 +315,10 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
   int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
   int* colexp = rowexp + d.batch * d.n;
-  dim3 gr((unsigned)((nrt * kOzRows + 127) / 128), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_rows_kernel<<<gr, 128, 0, st>>>(d, A, k, kb, rest, nrt, digA, rowexp));
-  dim3 gc((unsigned)((nct * kOzCols + 127) / 128), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 128, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
+  dim3 gr((unsigned)((nrt * kOzRows * 4 + 255) / 256), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_rows_kernel<<<gr, 256, 0, st>>>(d, A, k, kb, rest, nrt, digA, rowexp));
+  dim3 gc((unsigned)((nct * kOzCols * 4 + 255) / 256), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 256, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
   const size_t smem = kOzABytes + 2 * kOzBBytes;
   cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 gg((unsigned)nrt, (unsigned)((nct + kOzGroup - 1) / kOzGroup), (unsigned)d.batch);

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include "mh_digits.cuh"
 #include "mh_internal.cuh"
 #include "mh_tc.cuh"
 
@@ -47,62 +48,19 @@ constexpr uint32_t kZvWaitPolls = 1u << 26;
 constexpr size_t kZvSmem = (size_t)kZvA64 + kZvADig + 2 * kZvXTile;
 
 // BF16 bits of a small integer (|d| <= 64): through the FP32 magic number, exact
-__device__ __forceinline__ uint32_t bf16_of_small(int dg) {
-  const float f = __int_as_float(0x4B400000 + dg) - 12582912.0f;
+__device__ __forceinline__ uint32_t bf16_of_small(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
   return __float_as_uint(f) >> 16;
 }
 
-// round(v 2^(55 - E)) from the bit fields of v (|v| < 2^E, biased exponent of the row's
-// largest entry = E + 1022); zero and subnormal entries give 0
-__device__ __forceinline__ long long fixed55(double v, int emax_biased) {
-  const long long bits = __double_as_longlong(v);
-  const int ev = (int)((bits >> 52) & 0x7FF);
-  if (ev == 0) return 0;
-  const long long m = (bits & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
-  const int s = ev - emax_biased + 2;  // <= 2
-  long long X;
-  if (s >= 0) X = m << s;
-  else if (s > -63) X = (m + (1LL << (-s - 1))) >> (-s);
-  else X = 0;
-  return bits < 0 ? -X : X;
-}
-
-// the same digits with 32-bit arithmetic: X = hi 2^28 + lo, lo in [0, 2^28) gives digits 7..4
-// and a carry, hi (|hi| < 2^27) digits 3..0
-__device__ __forceinline__ void digits_of32(long long X, int (&dg)[kZvDigits]) {
-  int lo = (int)(X & 0xFFFFFFF);
-  int hi = (int)(X >> 28);
-#pragma unroll
-  for (int p = kZvDigits - 1; p >= 4; --p) {
-    const int c = lo + 64;
-    dg[p] = (c & 127) - 64;
-    lo = c >> 7;
-  }
-  hi += lo;
-#pragma unroll
-  for (int p = 3; p >= 1; --p) {
-    const int c = hi + 64;
-    dg[p] = (c & 127) - 64;
-    hi = c >> 7;
-  }
-  dg[0] = hi;
-}
-
-// two BF16 values (small integers) in one 32-bit word, the first in the low half
-__device__ __forceinline__ uint32_t bf16x2_of_small(int d0, int d1) {
-  const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
-  const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
-  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
-}
-
-__device__ __forceinline__ void digits_of(long long X, int (&dg)[kZvDigits]) {
+__device__ __forceinline__ void digits_of(long long X, int (&d8)[kZvDigits]) {
 #pragma unroll
   for (int p = kZvDigits - 1; p > 0; --p) {
     const long long t = ((X + 64) & 127) - 64;
-    dg[p] = (int)t;
+    d8[p] = (int)t;
     X = (X - t) >> 7;
   }
-  dg[0] = (int)X;
+  d8[0] = (int)X;
 }
 
 __device__ __forceinline__ int scale_exp(double maxabs) {
@@ -257,26 +215,12 @@ __global__ void __launch_bounds__(kZvThreads) zgemv_tc_kernel(BatchDesc d, const
         const int col = 8 * sq + c;
         vals[c] = (live && col < kbw) ? *reinterpret_cast<const double2*>(sA64 + col * (kZvRows * 16) + srow * 16)
                                       : make_double2(0.0, 0.0);
-        const int ex = (int)((__double_as_longlong(vals[c].x) >> 52) & 0x7FF);
-        const int ey = (int)((__double_as_longlong(vals[c].y) >> 52) & 0x7FF);
-        emax = max(emax, max(ex, ey));
+        emax = max(emax, max(dg::biased_exp(vals[c].x), dg::biased_exp(vals[c].y)));
       }
       emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
       emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
       uint32_t pk[2][kZvDigits][4];  // [part][digit][pairs of columns]
-#pragma unroll
-      for (int c = 0; c < 8; c += 2) {
-        int a0[kZvDigits], a1[kZvDigits], b0[kZvDigits], b1[kZvDigits];
-        digits_of32(fixed55(vals[c].x, emax), a0);
-        digits_of32(fixed55(vals[c + 1].x, emax), a1);
-        digits_of32(fixed55(vals[c].y, emax), b0);
-        digits_of32(fixed55(vals[c + 1].y, emax), b1);
-#pragma unroll
-        for (int p = 0; p < kZvDigits; ++p) {
-          pk[0][p][c >> 1] = bf16x2_of_small(a0[p], a1[p]);
-          pk[1][p][c >> 1] = bf16x2_of_small(b0[p], b1[p]);
-        }
-      }
+      dg::split8(vals, emax, pk);
       const uint32_t off = tc::kmajor_offset(srow, 8 * sq, kZvK);
 #pragma unroll
       for (int part = 0; part < 2; ++part)
@@ -285,7 +229,7 @@ __global__ void __launch_bounds__(kZvThreads) zgemv_tc_kernel(BatchDesc d, const
           *reinterpret_cast<uint4*>(sAd + (part * kZvDigits + p) * kZvPlane + off) =
               make_uint4(pk[part][p][0], pk[part][p][1], pk[part][p][2], pk[part][p][3]);
       // |v| < 2^E with E = emax - 1022 (the exponent scale of this row and block)
-      if (sq == 0) s_rowexp[kb & 1][srow] = emax > 0 ? emax - 1022 : 0;
+      if (sq == 0) s_rowexp[kb & 1][srow] = dg::scale_of(emax);
     }
     tc::fence_proxy_async_smem();
     __syncthreads();
