@@ -419,6 +419,20 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
                        "radiation, Rankine+image+GFWu direct; one CUDA graph over 4 streams",
            "units": units, "panel_pairs": pairs, "unit": UNIT}
     results = {}
+
+    def batch_shares(F):
+        # one more pass with per-launch events: uncaptured, serial on one stream
+        ctx.profile_reset()
+        ctx.profile(True)
+        mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO, g=G)
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        ctx._L.mh_batch_release(ctx.handle)
+        tot = sum(v[0] for v in prof.values())
+        sh = {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+        sh["serial_kernel_ms"] = round(tot, 1)
+        return sh
+
     for prec in ("fp64", "mixed", "fp64_tc"):
         F = mh.DirectBEM(precision=prec)
         # first call: graph capture + instantiation + one run (untimed warm-up, also the results)
@@ -428,6 +442,8 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
                                                                              g=G), steps, 0)
         out[prec] = {"value": units * steps / t, "ms_per_step": 1e3 * t / steps, "gpu_launches": launches}
         ctx._L.mh_batch_release(ctx.handle)
+        if prec != "fp64":
+            out[prec]["kernel_time_share"] = batch_shares(F)
     dev_max = 0.0
     for a, b in zip(results["mixed"], results["fp64"]):
         for key in ("added_mass", "radiation_damping"):
@@ -460,7 +476,9 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
     t, _, launches, _ = timed(lambda: mh.batch_hydrodynamic_coefficients(bodies, params, FS, ctx=ctx, rho=RHO, g=G),
                               1, 0)
     ctx._L.mh_batch_release(ctx.handle)
+    shares_s = batch_shares(FS)
     out["surrogate_mixed"] = {"value": units / t, "ms_per_step": 1e3 * t, "gpu_launches": launches,
+                              "kernel_time_share": shares_s,
                               "note": "Rankine + image + learned surrogate of the exact Delhommeau term (exact "
                                       "fallback queue per body), FP32 LU + FP64 refinement, one CUDA graph"}
     # accuracy against the exact Green function (FP64 oracle arithmetic) on the 4 smallest bodies

@@ -57,6 +57,7 @@ struct BatchCache {
   char* pinned = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t graph_kernels = 0;
+  std::vector<int64_t> order;  // bodies, longest first
   int device = 0;
   ~BatchCache() {
     cudaSetDevice(device);
@@ -1265,9 +1266,12 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
   BatchOpts o{gfs, direct ? 1 : 0, precision, 2, rho, g, n_dofs, n_rad, n_inf, n_beta, n_rad + n_beta};
 
   // cache key: everything the captured graph bakes in
+  // with profiling on, the schedule runs uncaptured on one stream so that every launch is
+  // timed by its own events (kernel shares of the batch); the graph is not built
+  const bool profiling = profiler_on(ctx->prof);
   std::vector<double> key = {(double)n_bodies, (double)gfs, (double)o.direct, (double)precision, (double)S, rho, g,
                              (double)n_dofs, (double)n_rad, (double)n_inf, (double)n_beta, ctx->quad_rtol,
-                             ctx->quad_atol};
+                             ctx->quad_atol, profiling ? 1.0 : 0.0};
   for (int64_t b = 0; b < n_bodies; ++b) {
     key.push_back((double)(uintptr_t)meshes[b]);
     key.push_back((double)n_omega[b]);
@@ -1333,36 +1337,41 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       MH_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
       ctx->side.push_back(st);
     }
-    // capture the schedule
-    cudaStream_t s0 = ctx->stream;
-    std::vector<cudaEvent_t> ev(S);
-    for (auto& e : ev) MH_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    LaunchCounter cap{&bc->graph_kernels, nullptr};
-    MH_CUDA(ctx, cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
-    cudaEventRecord(ev[0], s0);
-    for (int q = 1; q < S; ++q) cudaStreamWaitEvent(ctx->side[q - 1], ev[0], 0);
-    for (int64_t b : order) {
-      BodyPlan& p = bc->bodies[b];
-      enqueue_body(ctx, cap, p.stream == 0 ? s0 : ctx->side[p.stream - 1], p, o);
+    bc->order = order;
+    if (profiling) {
+      ctx->batch = bc;
+    } else {
+      // capture the schedule
+      cudaStream_t s0 = ctx->stream;
+      std::vector<cudaEvent_t> ev(S);
+      for (auto& e : ev) MH_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      LaunchCounter cap{&bc->graph_kernels, nullptr};
+      MH_CUDA(ctx, cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
+      cudaEventRecord(ev[0], s0);
+      for (int q = 1; q < S; ++q) cudaStreamWaitEvent(ctx->side[q - 1], ev[0], 0);
+      for (int64_t b : order) {
+        BodyPlan& p = bc->bodies[b];
+        enqueue_body(ctx, cap, p.stream == 0 ? s0 : ctx->side[p.stream - 1], p, o);
+      }
+      for (int q = 1; q < S; ++q) {
+        cudaEventRecord(ev[q], ctx->side[q - 1]);
+        cudaStreamWaitEvent(s0, ev[q], 0);
+      }
+      cudaGraph_t graph = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(s0, &graph);
+      for (auto& e : ev) cudaEventDestroy(e);
+      if (ce != cudaSuccess || !graph) {
+        delete bc;
+        return fail(ctx, MH_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+      }
+      ce = cudaGraphInstantiate(&bc->exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        delete bc;
+        return fail(ctx, MH_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce));
+      }
+      ctx->batch = bc;
     }
-    for (int q = 1; q < S; ++q) {
-      cudaEventRecord(ev[q], ctx->side[q - 1]);
-      cudaStreamWaitEvent(s0, ev[q], 0);
-    }
-    cudaGraph_t graph = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(s0, &graph);
-    for (auto& e : ev) cudaEventDestroy(e);
-    if (ce != cudaSuccess || !graph) {
-      delete bc;
-      return fail(ctx, MH_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
-    }
-    ce = cudaGraphInstantiate(&bc->exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) {
-      delete bc;
-      return fail(ctx, MH_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce));
-    }
-    ctx->batch = bc;
   }
   // per-call parameters -> the bodies' device buffers (outside the graph)
   for (int64_t b = 0; b < n_bodies; ++b) {
@@ -1385,8 +1394,12 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       }
     }
   }
-  MH_CUDA(ctx, cudaGraphLaunch(bc->exec, ctx->stream));
-  ctx->launches += bc->graph_kernels;
+  if (bc->exec) {
+    MH_CUDA(ctx, cudaGraphLaunch(bc->exec, ctx->stream));
+    ctx->launches += bc->graph_kernels;
+  } else {
+    for (int64_t b : bc->order) enqueue_body(ctx, ctx->lc(), ctx->stream, bc->bodies[b], o);
+  }
   MH_TRY(sync(ctx, "batch graph"));
   for (auto& p : bc->bodies) MH_TRY(finish_body(ctx, p, o));
   // pack per body (n_U = 1), bodies concatenated along the frequency axis

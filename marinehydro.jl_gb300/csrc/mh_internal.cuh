@@ -200,6 +200,7 @@ void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x);
 Profiler* profiler_create();
 void profiler_destroy(Profiler* p);
 void profiler_enable(Profiler* p, bool on);
+bool profiler_on(const Profiler* p);
 void profiler_reset(Profiler* p);
 int profiler_read(Profiler* p, int64_t capacity, char* names, double* total_ms, int64_t* launches, int64_t* n);
 int probe_fma_peaks(cudaStream_t st, double* fp64_tflops, double* fp32_tflops);

@@ -86,6 +86,7 @@ void LaunchCounter::post(cudaStream_t st, const char* group) const {
 Profiler* profiler_create() { return new Profiler(); }
 void profiler_destroy(Profiler* p) { delete p; }
 void profiler_enable(Profiler* p, bool on) { p->on = on; }
+bool profiler_on(const Profiler* p) { return p && p->on; }
 void profiler_reset(Profiler* p) { p->reset(); }
 int profiler_read(Profiler* p, int64_t capacity, char* names, double* total_ms, int64_t* launches, int64_t* n) {
   p->resolve();
