@@ -283,6 +283,11 @@ int mh_wu_wave_terms(mh_context* ctx, int64_t m, const double* hh, const double*
    tolerances (the reference's Integrals.jl call uses its defaults). */
 int mh_exact_wave_terms(mh_context* ctx, int64_t m, const double* r, const double* z, double rtol, double atol,
                         double* out, int mem);
+/* J0, J1, Y0, Y1 at m points x >= 0, as the Wu kernels evaluate them: out 4 doubles
+   per point (Y0, Y1 are NaN below x = 3, where the Wu term does not use them).  The
+   reference calls SpecialFunctions.jl besselj0/besselj1/bessely0/bessely1 at the same
+   argument (wu.jl:203, 335, 396, 431). */
+int mh_bessel01_points(mh_context* ctx, int64_t m, const double* x, double* out, int mem);
 /* Tolerances used by assembly with MH_GF_EXACT_DELHOMMEAU (default 1e-12, 1e-14). */
 int mh_set_quadrature_tolerance(mh_context* ctx, double rtol, double atol);
 

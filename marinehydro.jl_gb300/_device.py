@@ -123,6 +123,15 @@ def wu_wave_terms(ctx, hh, vv):
     return out
 
 
+def bessel01_points(ctx, x):
+    """J0, J1, Y0, Y1 as the Wu kernels evaluate them (m x 4; Y is NaN below x = 3)."""
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+    out = np.empty((x.size, 4), dtype=np.float64)
+    ctx.check(ctx._L.mh_bessel01_points(ctx.handle, x.size, x.ctypes.data, out.ctypes.data, MH_MEM_HOST),
+              "Bessel points")
+    return out
+
+
 def exact_wave_terms(ctx, r, z, rtol=1e-12, atol=1e-14):
     r = np.ascontiguousarray(np.asarray(r, dtype=np.float64).ravel())
     z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).ravel())

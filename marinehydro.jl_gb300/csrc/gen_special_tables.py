@@ -1,0 +1,212 @@
+"""Generate mh_special_tables.cuh: the polynomial tables of the joint J0, J1, Y0, Y1
+evaluators (mh_bessel01.cuh, FP64 and FP32) and the Chebyshev form of the Wu fits for the
+FP32 Wu term (mh_wu_f32.cuh).  Run once; the output is committed, mpmath is not needed to
+build.
+
+Bessel functions (all coefficients computed here from the functions' definitions with
+mpmath at 40 digits):
+
+* 0 <= x < 8: piecewise Chebyshev interpolation (Trefethen, Approximation Theory and
+  Approximation Practice, ch. 3-8) on the sixteen intervals [q/2, q/2 + 1/2) for J0 and J1,
+  and on [3, 8) for Y0 and Y1 (the Wu term needs Y only above x = 3), degree 11 at the
+  first-kind Chebyshev points, converted to monomials in t = x - (q/2 + 1/4), |t| <= 1/4.
+  Worst absolute error measured against mpmath: 6e-17.
+* x >= 8: Hankel's modulus-phase form (DLMF 10.17.3):
+      J_n(x) = sqrt(2/(pi x)) (P_n(x) cos w - Q_n(x) sin w),
+      Y_n(x) = sqrt(2/(pi x)) (P_n(x) sin w + Q_n(x) cos w),   w = x - n pi/2 - pi/4,
+  with P_n and Q_n / s (s = 8/x) interpolated as degree-12 polynomials of u = s^2 in [0, 1]
+  (Chebyshev points, monomials in u - 1/2), P_n and Q_n taken from mpmath's J_n, Y_n by
+  inverting the two relations.  Worst absolute error of P, Q/s: 3e-17.
+* FP32 tables: the same construction at degree 6 (half-unit intervals) and 6 (Hankel), for
+  errors below FP32 rounding.
+
+Wu fits: the polynomials A-D and dA-dC of Liang, Wu & Noblesse (wu.jl:131-197, 235-329) in
+rho in [0, 1] have monomial coefficients up to 2e5 of alternating sign, so evaluated in FP32
+their rounding is amplified ~1e5-fold.  The same polynomials written exactly in the
+Chebyshev basis of s = 2 rho - 1 have coefficients below 15, and Clenshaw's recurrence in
+FP32 keeps the error near FP32 rounding of the values.
+
+Usage: python gen_special_tables.py  (writes mh_special_tables.cuh beside this script)
+"""
+from __future__ import annotations
+
+import os
+
+import mpmath as mp
+
+mp.mp.dps = 40
+
+DEG_LOW = 11     # per half-unit interval below x = 8
+DEG_HANKEL = 12  # in u = (8/x)^2
+DEG_LOW_F = 6    # FP32 tables
+DEG_HANKEL_F = 6
+
+# monomial coefficients (degree 0 first) of the Wu fits, wu.jl:131-197 (dA-dC) and
+# 235-329 (A-D)
+WU_FITS = {
+    "A": [1.21, -13.328, 215.896, -1763.96, 8418.94, -24314.21, 42002.57, -41592.9, 21859.0, -4838.6],
+    "B": [0.938, 5.737, -67.92, 796.534, -4780.77, 17137.74, -36618.81, 44894.06, -29030.24, 7671.22],
+    "C": [1.268, -9.747, 209.653, -1397.89, 5155.67, -9844.35, 9136.4, -3272.62],
+    "D": [0.632, -40.97, 667.16, -6072.07, 31127.39, -96293.05, 181856.75, -205690.43, 128170.2, -33744.6],
+    "dA": [2.948, -24.53, 249.69, -754.85, -1187.71, 16370.75, -48811.41, 68220.87, -46688.0, 12622.25],
+    "dB": [1.11, 2.894, -76.765, 1565.35, -11336.19, 44270.15, -97014.11, 118879.26, -76209.82, 19923.28],
+    "dC": [14.19, -148.24, 847.8, -2318.58, 3168.35, -1590.27],
+}
+
+
+def cheb_monomials(f, a, b, n):
+    """Degree-n Chebyshev interpolant of f on [a, b] as monomial coefficients in t = x - (a+b)/2."""
+    mid, h = (a + b) / 2, (b - a) / 2
+    th = [mp.pi * (k + mp.mpf(1) / 2) / (n + 1) for k in range(n + 1)]
+    vals = [f(mid + h * mp.cos(t)) for t in th]
+    c = [2 * mp.fsum(vals[k] * mp.cos(j * th[k]) for k in range(n + 1)) / (n + 1) for j in range(n + 1)]
+    c[0] /= 2
+    T = [[mp.mpf(1)], [mp.mpf(0), mp.mpf(1)]]
+    for j in range(2, n + 1):
+        nxt = [mp.mpf(0)] * (j + 1)
+        for i, v in enumerate(T[j - 1]):
+            nxt[i + 1] += 2 * v
+        for i, v in enumerate(T[j - 2]):
+            nxt[i] -= v
+        T.append(nxt)
+    mono = [mp.mpf(0)] * (n + 1)
+    for j in range(n + 1):
+        for i, v in enumerate(T[j]):
+            mono[i] += c[j] * v
+    return [mono[i] / h ** i for i in range(n + 1)]
+
+
+def hankel_pq(nu, u):
+    """P_nu and Q_nu / s at u = (8/x)^2 (limits 1 and (4 nu^2 - 1)/64 at u = 0)."""
+    if u == 0:
+        return mp.mpf(1), mp.mpf(4 * nu * nu - 1) / 64
+    x = 8 / mp.sqrt(u)
+    w = x - nu * mp.pi / 2 - mp.pi / 4
+    J, Y = mp.besselj(nu, x), mp.bessely(nu, x)
+    f = mp.sqrt(mp.pi * x / 2)
+    return f * (J * mp.cos(w) + Y * mp.sin(w)), f * (Y * mp.cos(w) - J * mp.sin(w)) / (8 / x)
+
+
+def horner(co, t):
+    v = mp.mpf(0)
+    for c in reversed(co):
+        v = v * t + c
+    return v
+
+
+def fmt(vals, single=False):
+    f = (lambda v: f"{float(mp.mpf(v)):.9e}f") if single else (lambda v: f"{float(v):.17e}")
+    return ",\n    ".join(", ".join(f(v) for v in vals[i:i + 4]) for i in range(0, len(vals), 4))
+
+
+def bessel_tables(deg_low, deg_hankel, single):
+    """Coefficient rows of the low-region tables and the Hankel polynomials, rounded to the
+    target precision, and the worst absolute error of the rounded polynomials."""
+    rnd = (lambda c: float(__import__("numpy").float32(float(c)))) if single else float
+    J = [lambda x: mp.besselj(0, x), lambda x: mp.besselj(1, x)]
+    Y = [lambda x: mp.bessely(0, x), lambda x: mp.bessely(1, x)]
+    tabs, worst_low, worst_hk = {}, mp.mpf(0), mp.mpf(0)
+    for name, fs, q0 in (("J", J, 0), ("Y", Y, 6)):
+        for nu in (0, 1):
+            rows = []
+            for q in range(q0, 16):
+                a = mp.mpf(q) / 2
+                cf = [rnd(c) for c in cheb_monomials(fs[nu], a, a + mp.mpf(1) / 2, deg_low)]
+                for k in range(33):
+                    x = a + mp.mpf(k) / 64
+                    worst_low = max(worst_low, abs(horner(cf, float(x - a - mp.mpf(1) / 4)) - fs[nu](x)))
+                rows += cf
+            tabs[f"{name}{nu}"] = rows
+    for nu in (0, 1):
+        for part in (0, 1):
+            g = lambda u, nu=nu, part=part: hankel_pq(nu, u)[part]
+            cf = [rnd(c) for c in cheb_monomials(g, mp.mpf(0), mp.mpf(1), deg_hankel)]
+            for k in range(1, 65):
+                u = mp.mpf(k) / 64
+                worst_hk = max(worst_hk, abs(horner(cf, float(u - mp.mpf(1) / 2)) - g(u)))
+            tabs[f"{'PQ'[part]}{nu}"] = cf
+    return tabs, worst_low, worst_hk
+
+
+def wu_fit_chebyshev(mono):
+    """Exact Chebyshev coefficients (basis T_j(2 rho - 1)) of a monomial polynomial in rho."""
+    n = len(mono) - 1
+    # rho = (s + 1) / 2: expand in s, then monomials in s -> Chebyshev in s
+    from math import comb
+    sco = [mp.mpf(0)] * (n + 1)
+    for k, c in enumerate(mono):
+        for m in range(k + 1):
+            sco[m] += mp.mpf(c) * comb(k, m) / mp.mpf(2) ** k
+    # s^m = sum_j b_{m,j} T_j(s) (descending recursion on the Chebyshev series of s * T_j)
+    cheb = [mp.mpf(0)] * (n + 1)
+    for m, c in enumerate(sco):
+        t = [mp.mpf(0)] * (n + 1)
+        t[0] = mp.mpf(1)
+        for _ in range(m):  # multiply the series by s: s T_0 = T_1, s T_j = (T_{j+1} + T_{j-1}) / 2
+            u = [mp.mpf(0)] * (n + 1)
+            for j, v in enumerate(t):
+                if v == 0:
+                    continue
+                if j == 0:
+                    u[1] += v
+                else:
+                    u[j + 1] += v / 2
+                    u[j - 1] += v / 2
+            t = u
+        for j in range(n + 1):
+            cheb[j] += c * t[j]
+    return cheb
+
+
+def clenshaw(c, s):
+    b1 = b2 = mp.mpf(0)
+    for cj in reversed(c[1:]):
+        b1, b2 = 2 * s * b1 - b2 + cj, b1
+    return s * b1 - b2 + c[0]
+
+
+def main():
+    tabs, wl, wh = bessel_tables(DEG_LOW, DEG_HANKEL, False)
+    print("FP64 Bessel: worst abs error low region", mp.nstr(wl, 3), "Hankel P, Q/s", mp.nstr(wh, 3))
+    tabf, wlf, whf = bessel_tables(DEG_LOW_F, DEG_HANKEL_F, True)
+    print("FP32 Bessel: worst abs error low region", mp.nstr(wlf, 3), "Hankel P, Q/s", mp.nstr(whf, 3))
+    wu = {}
+    for key, mono in WU_FITS.items():
+        ch = wu_fit_chebyshev(mono)
+        worst = max(abs(clenshaw(ch, 2 * mp.mpf(k) / 200 - 1) - horner([mp.mpf(c) for c in mono], mp.mpf(k) / 200))
+                    for k in range(201))
+        assert worst < 1e-25, (key, worst)
+        wu[key] = ch
+        print(f"Wu fit {key}: Chebyshev coefficients up to {float(max(abs(c) for c in ch)):.3g}")
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mh_special_tables.cuh")
+    with open(out, "w") as fh:
+        fh.write("// mh_special_tables.cuh -- generated by gen_special_tables.py (mpmath, 40 digits); do not\n")
+        fh.write("// edit.  Polynomial coefficients, lowest degree first, of the J0, J1, Y0, Y1 evaluators\n")
+        fh.write("// (mh_bessel01.cuh) and the Chebyshev form of the Wu fits (mh_wu_f32.cuh).\n")
+        fh.write("#pragma once\n\nnamespace mh {\n")
+        for ns, tb, dl, dh, single in (("bes", tabs, DEG_LOW, DEG_HANKEL, False),
+                                       ("besf", tabf, DEG_LOW_F, DEG_HANKEL_F, True)):
+            ty = "float" if single else "double"
+            fh.write(f"namespace {ns} {{\n\n")
+            fh.write(f"constexpr int kLowTerms = {dl + 1};     // per half-unit interval, in t = x - (q/2 + 1/4)\n")
+            fh.write(f"constexpr int kHankelTerms = {dh + 1};  // in u - 1/2, u = (8/x)^2\n\n")
+            for key in ("J0", "J1"):
+                fh.write(f"// {key} on [q/2, q/2 + 1/2), q = 0..15\n")
+                fh.write(f"__device__ const {ty} k{key}[16 * kLowTerms] = {{\n    {fmt(tb[key], single)}}};\n\n")
+            for key in ("Y0", "Y1"):
+                fh.write(f"// {key} on [q/2, q/2 + 1/2), q = 6..15 (row q - 6)\n")
+                fh.write(f"__device__ const {ty} k{key}[10 * kLowTerms] = {{\n    {fmt(tb[key], single)}}};\n\n")
+            for key, what in (("P0", "P0"), ("Q0", "Q0 / s"), ("P1", "P1"), ("Q1", "Q1 / s")):
+                fh.write(f"// {what} for x >= 8\n")
+                fh.write(f"__constant__ {ty} k{key}[kHankelTerms] = {{\n    {fmt(tb[key], single)}}};\n\n")
+            fh.write(f"}}  // namespace {ns}\n\n")
+        fh.write("namespace wuf {\n\n")
+        fh.write("// Wu fits (wu.jl:131-197, 235-329) as sum_j c_j T_j(2 rho - 1), FP32\n")
+        for key in WU_FITS:
+            fh.write(f"__constant__ float kCheb{key}[{len(wu[key])}] = {{\n    {fmt(wu[key], True)}}};\n")
+        fh.write("\n}  // namespace wuf\n}  // namespace mh\n")
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    main()

@@ -92,7 +92,8 @@ __device__ void wu_terms_t(R hh, R vv, CR<R>& GF, CR<R>& Gh, CR<R>& Gv) {
   R omr = 1.0 - rho;
   R omr3 = omr * omr * omr;
   R ev = exp(vv);
-  R J0 = j0(hh), J1 = j1(hh), H0, H1;
+  R J0, J1, Y0, Y1, H0, H1;
+  bessel01_t(hh, J0, J1, Y0, Y1);
   if (val(hh) <= 3.0) {
     R yy = (hh / 3.0) * (hh / 3.0);
     R h0 = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
@@ -102,10 +103,10 @@ __device__ void wu_terms_t(R hh, R vv, CR<R>& GF, CR<R>& Gh, CR<R>& Gv) {
     R yy = (3.0 / hh) * (3.0 / hh);
     R c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
     R c2 = kPi * hh * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
-    H0 = c1 / c2 + y0(hh);
+    H0 = c1 / c2 + Y0;
     R d1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
     R d2 = kPi * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
-    H1 = d1 / d2 + y1(hh);
+    H1 = d1 / d2 + Y1;
   }
   R RR = (1.0 - beta) * pA(rho);
   RR -= beta * pB(rho);

@@ -21,6 +21,7 @@
 #include "mh_internal.cuh"
 #include "mh_mlp.cuh"
 #include "mh_tc.cuh"
+#include "mh_wu_f32.cuh"
 
 namespace mh {
 
@@ -213,37 +214,21 @@ struct WaveTerms {
   double2 gz;      // vertical gradient component, without area
 };
 
-// dynamic shared memory of the surrogate mode: the packed MLP parameters
-extern __shared__ float4 mh_wave_dyn_smem[];
-
-// WMODE bits: 1 = Wu, 2 = exact Delhommeau, 4 = learned surrogate (Wu + MLP correction).
-// Returns true when the pair lies outside the surrogate's training box (the terms
-// then hold the plain Wu values and the caller queues the pair for the exact kernel).
+// WMODE bits: 1 = Wu, 2 = exact Delhommeau (the learned surrogate has its own kernel,
+// wave_kernel_tc).
 template <bool DIRECT, int WMODE>
-__device__ __forceinline__ bool wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
+__device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
                                            WaveTerms& w) {
   w.I = make_double2(0.0, 0.0);
   w.gh[0] = w.gh[1] = w.gz = w.I;
   // (i, j) orientation: gradient w.r.t. the source (direct) or the field point (indirect)
   const double dx1 = DIRECT ? cj[0] - ci[0] : ci[0] - cj[0];
   const double dx2 = DIRECT ? cj[1] - ci[1] : ci[1] - cj[1];
-  bool fallback = false;
-  if (WMODE & 5) {  // _wu_sd (wu.jl:112-127); the surrogate adds its learned correction
+  if (WMODE & 1) {  // _wu_sd (wu.jl:112-127)
     double hh, vv;
     reduced_coords(ci, cj, k, hh, vv);
     double2 GF, Gh, Gv;
     wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
-    if (WMODE & 4) {
-      if (surrogate_in_box(hh, vv)) {
-        double2 dG, dGr, dGz;
-        surrogate_correction(reinterpret_cast<const float*>(mh_wave_dyn_smem), hh, vv, dG, dGr, dGz);
-        GF = zadd(GF, dG);
-        Gh = zadd(Gh, dGr);
-        Gv = zadd(Gv, dGz);
-      } else {
-        fallback = true;
-      }
-    }
     double dr1 = 0.0, dr2 = 0.0;
     if (fabs(hh) > 1e-6) {
       dr1 = k * k / hh * dx1;
@@ -270,7 +255,6 @@ __device__ __forceinline__ bool wave_terms(const AssemblyParams& p, const double
     w.gh[1] = zadd(w.gh[1], make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y)));
     w.gz = zadd(w.gz, make_double2(k * (k * dGdz.x), k * (k * dGdz.y)));
   }
-  return fallback;
 }
 
 // S and D entries (before adding the static part) from the wave terms; `sgn` = -1
@@ -323,7 +307,7 @@ __device__ __forceinline__ void store_pair(const AssemblyParams& p, const WaveTe
   Db[mdx] = dm;
 }
 
-template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both, 4 = surrogate
+template <bool DIRECT, int WMODE>  // WMODE 1 = Wu only, 2 = exact Delhommeau, 3 = both
 __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, const double* __restrict__ SR,
                                                            const double* __restrict__ DR,
                                                            const double* __restrict__ ks, double2* __restrict__ S,
@@ -339,10 +323,6 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
   double2* Sb = S + blockIdx.z * sstride;
   double2* Db = D + blockIdx.z * sstride;
   stage_panels(sp, p.P, j0, n);
-  if (WMODE & 4) {
-    const float4* src = reinterpret_cast<const float4*>(p.mlp);
-    for (int q = threadIdx.x; q < kMlpParamsPadded / 4; q += blockDim.x) mh_wave_dyn_smem[q] = __ldg(src + q);
-  }
   __syncthreads();
   if (i >= n) return;
   double ci[3], ni[3];
@@ -354,13 +334,7 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
     if (i > j) continue;
     const PanelRec& Pj = sp[jj];
     WaveTerms w;
-    const bool fb = wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
-    if ((WMODE & 4) && (fb || i == j)) {
-      // outside the training box, and the self pairs: queued for the exact kernel (the
-      // entries written here are replaced)
-      const unsigned long long slot = atomicAdd(p.fb_state, 1ull);
-      if ((int64_t)slot < p.fb_cap) p.fb_list[slot] = make_int4((int)i, (int)j, (int)blockIdx.z, 0);
-    }
+    wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
     store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
   }
 }
@@ -369,8 +343,9 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
 // Surrogate wave assembly with the network's two 64 x 64 layers on the tensor cores.
 //
 // The CTA's 128 threads own 128 rows i; for each of its kColsPerCta columns j the 128 pairs
-// (i, j) form one M = 128 batch: every thread evaluates its pair's Wu terms (FP64) and the
-// first layer (2 -> 64, CUDA cores) into row i of a BF16 activation tile in shared memory,
+// (i, j) form one M = 128 batch: every thread evaluates its pair's Wu terms (FP32,
+// mh_wu_f32.cuh: the network's own error is ~1e-3, so the base it corrects needs no FP64)
+// and the first layer (2 -> 64, CUDA cores) into row i of a BF16 activation tile in shared memory,
 // thread 0 issues tcgen05.mma (M = 128, N = 64, K = 64 in four K = 16 steps) against the
 // BF16 weight tile, the FP32 result lands in tensor memory, and each thread reads its row
 // back (tcgen05.ld), applies bias and tanh, and writes the next layer's activations; the
@@ -384,18 +359,69 @@ constexpr int kTcSmemW2 = 0, kTcSmemW3 = 8192, kTcSmemA = 16384, kTcSmemF = 3276
 constexpr int kTcSmemFloats = 128 + 64 + 64 + 64 + 128 + 2;  // W1, b1, b2, b3, W4 rows 0 and 2, b4[0], b4[2]
 constexpr int kTcSmemBytes = kTcSmemF + 4 * kTcSmemFloats;
 
-template <bool DIRECT>
-__device__ __forceinline__ void wu_to_wave_terms(double hh, double k, double dx1, double dx2, double2 GF, double2 Gh,
-                                                 double2 Gv, WaveTerms& w) {
-  double dr1 = 0.0, dr2 = 0.0;
-  if (fabs(hh) > 1e-6) {
-    dr1 = k * k / hh * dx1;
-    dr2 = k * k / hh * dx2;
+// FP32 wave terms of the surrogate path (as WaveTerms) and their S/D entries; the static
+// Rankine part they are added to stays FP64
+struct WaveTermsF {
+  float2 I, gh[2], gz;
+};
+
+__device__ __forceinline__ void wu_to_wave_terms_f(float hh, float k, float dx1, float dx2, float2 GF, float2 Gh,
+                                                   float2 Gv, WaveTermsF& w) {
+  float dr1 = 0.0f, dr2 = 0.0f;
+  if (fabsf(hh) > 1e-6f) {
+    const float kk_hh = k * k / hh;
+    dr1 = kk_hh * dx1;
+    dr2 = kk_hh * dx2;
   }
-  w.I = make_double2(k * GF.x, k * GF.y);
-  w.gh[0] = make_double2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
-  w.gh[1] = make_double2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));
-  w.gz = make_double2(k * (k * Gv.x), k * (k * Gv.y));
+  w.I = make_float2(k * GF.x, k * GF.y);
+  w.gh[0] = make_float2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
+  w.gh[1] = make_float2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));
+  w.gz = make_float2(k * (k * Gv.x), k * (k * Gv.y));
+}
+
+__device__ __forceinline__ void wave_entry_f(const WaveTermsF& w, float sgn, float area, const double nd[3],
+                                             double2& sv, double2& dv) {
+  const float nv[3] = {(float)nd[0], (float)nd[1], (float)nd[2]};
+  const float c = (float)kMinusInv4Pi * area;
+  const float g0x = sgn * w.gh[0].x, g0y = sgn * w.gh[0].y, g1x = sgn * w.gh[1].x, g1y = sgn * w.gh[1].y;
+  sv = make_double2(c * w.I.x, c * w.I.y);
+  dv = make_double2(c * fmaf(nv[0], g0x, fmaf(nv[1], g1x, nv[2] * w.gz.x)),
+                    c * fmaf(nv[0], g0y, fmaf(nv[1], g1y, nv[2] * w.gz.y)));
+}
+
+// store_pair for FP32 wave terms
+template <bool DIRECT>
+__device__ __forceinline__ void store_pair_f(const AssemblyParams& p, const WaveTermsF& w, int64_t i, int64_t j,
+                                             const double ni[3], double ai, const PanelRec& Pj,
+                                             const double* __restrict__ SR, const double* __restrict__ DR,
+                                             double2* __restrict__ Sb, double2* __restrict__ Db, int wave_identity) {
+  const int64_t n = p.n;
+  double nv[3];
+  pick_normal<DIRECT>(p, Pj, ni, nv);
+  double2 sv, dv;
+  wave_entry_f(w, 1.0f, (float)Pj.area, nv, sv, dv);
+  if (wave_identity && i == j) dv.x += identity_jump(p, ni);
+  const int64_t idx = i + j * n;
+  if (SR) {
+    sv.x = SR[idx] + sv.x;
+    dv.x = DR[idx] + dv.x;
+  }
+  Sb[idx] = sv;
+  Db[idx] = dv;
+  if (i == j) return;
+  double nm[3];
+  if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
+  else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
+  else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
+  double2 sm, dm;
+  wave_entry_f(w, -1.0f, (float)ai, nm, sm, dm);
+  const int64_t mdx = j + i * n;
+  if (SR) {
+    sm.x = SR[mdx] + sm.x;
+    dm.x = DR[mdx] + dm.x;
+  }
+  Sb[mdx] = sm;
+  Db[mdx] = dm;
 }
 
 template <bool DIRECT>
@@ -466,19 +492,23 @@ __global__ void __launch_bounds__(kTcRows) wave_kernel_tc(AssemblyParams p, cons
   uint32_t phase = 0;
   bool timed_out = false;
   const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  const float kf = (float)k;
   for (int jj = 0; jj < jmax && !timed_out; ++jj) {
     const int64_t j = j0 + jj;
     const bool active = row_ok && i <= j;
     const PanelRec& Pj = sp[jj];
-    double hh = 1.0, vv = -1.0;
-    double2 GF = make_double2(0, 0), Gh = GF, Gv = GF;
+    float hh = 1.0f, vv = -1.0f;
+    float2 GF = make_float2(0.0f, 0.0f), Gh = GF, Gv = GF;
     if (active) {
-      reduced_coords(ci, Pj.c, k, hh, vv);
-      wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
+      // reduced coordinates (wu.jl:7-18): the differences of the FP64 centres, then FP32
+      const float ex = (float)(ci[0] - Pj.c[0]), ey = (float)(ci[1] - Pj.c[1]);
+      hh = kf * sqrtf(fmaf(ex, ex, ey * ey));
+      vv = kf * (float)(ci[2] + Pj.c[2]);
+      wu_wave_term_and_derivs_f32(hh, vv, GF, Gh, Gv);
     }
     // first layer (CUDA cores) -> BF16 activation row `tid`
     float u, v;
-    mlp_inputs(fmax(hh, kSurrRMin), fmax(vv, kSurrZMin), u, v);
+    mlp_inputs_f(fmaxf(hh, (float)kSurrRMin), fmaxf(vv, (float)kSurrZMin), u, v);
 #pragma unroll 8
     for (int q = 0; q < kMlpH; ++q) {
       const float h = tanh_fast(fmaf(W1f[2 * q], u, fmaf(W1f[2 * q + 1], v, b1f[q])));
@@ -533,21 +563,21 @@ __global__ void __launch_bounds__(kTcRows) wave_kernel_tc(AssemblyParams p, cons
     if (!active) continue;
     const bool in_box = surrogate_in_box(hh, vv) && i != j;
     if (in_box) {
-      double2 dG, dGr, dGz;
+      float2 dG, dGr, dGz;
       surrogate_apply(y0, y2, hh, vv, dG, dGr, dGz);
-      GF = zadd(GF, dG);
-      Gh = zadd(Gh, dGr);
-      Gv = zadd(Gv, dGz);
+      GF = make_float2(GF.x + dG.x, GF.y + dG.y);
+      Gh = make_float2(Gh.x + dGr.x, Gh.y + dGr.y);
+      Gv = make_float2(Gv.x + dGz.x, Gv.y + dGz.y);
     } else {
       // outside the training box, and the self pairs: queued for the exact kernel
       const unsigned long long slot = atomicAdd(p.fb_state, 1ull);
       if ((int64_t)slot < p.fb_cap) p.fb_list[slot] = make_int4((int)i, (int)j, (int)blockIdx.z, 0);
     }
-    const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
-    const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
-    WaveTerms w;
-    wu_to_wave_terms<DIRECT>(hh, k, dx1, dx2, GF, Gh, Gv, w);
-    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
+    const float dx1 = (float)(DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0]);
+    const float dx2 = (float)(DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1]);
+    WaveTermsF w;
+    wu_to_wave_terms_f(hh, kf, dx1, dx2, GF, Gh, Gv, w);
+    store_pair_f<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
   }
   if (timed_out) {
     // reported by the host as a timeout; let the MMAs in flight finish (bounded) before the
@@ -659,6 +689,18 @@ __global__ void wu_points_kernel(int64_t m, const double* __restrict__ hh, const
   out[3 * q + 2] = c;
 }
 
+__global__ void bessel01_points_kernel(int64_t m, const double* __restrict__ x, double* __restrict__ out) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  double J0, J1, Y0, Y1;
+  bessel01(x[q], J0, J1, Y0, Y1);
+  const bool y_defined = x[q] >= 3.0;
+  out[4 * q] = J0;
+  out[4 * q + 1] = J1;
+  out[4 * q + 2] = y_defined ? Y0 : __longlong_as_double(0x7FF8000000000000LL);
+  out[4 * q + 3] = y_defined ? Y1 : __longlong_as_double(0x7FF8000000000000LL);
+}
+
 // one warp per point
 __global__ void __launch_bounds__(32 * kExactWarps) exact_points_kernel(int64_t m, const double* __restrict__ r,
                                                                          const double* __restrict__ z, double rtol,
@@ -753,6 +795,10 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
   }
 #undef MH_WAVE
   lc.post(st, mode == 1 ? "assemble_wave_wu" : "assemble_wave_exact");
+}
+
+void launch_bessel01_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out) {
+  MH_LAUNCH(lc, st, "bessel_points", bessel01_points_kernel<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(m, x, out));
 }
 
 void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out) {

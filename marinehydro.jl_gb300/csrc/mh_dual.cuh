@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include "mh_bessel01.cuh"
+
 namespace mh {
 
 template <int M>
@@ -42,10 +44,6 @@ __device__ __forceinline__ double log(double x) { return ::log(x); }
 __device__ __forceinline__ double exp(double x) { return ::exp(x); }
 __device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
 __device__ __forceinline__ double hypot(double x, double y) { return ::hypot(x, y); }
-__device__ __forceinline__ double j0(double x) { return ::j0(x); }
-__device__ __forceinline__ double j1(double x) { return ::j1(x); }
-__device__ __forceinline__ double y0(double x) { return ::y0(x); }
-__device__ __forceinline__ double y1(double x) { return ::y1(x); }
 
 // chain: r = f(a) with f'(a) = s
 template <int M> __device__ __forceinline__ Dn<M> chain1(const Dn<M>& a, double fv, double s) {
@@ -121,15 +119,21 @@ template <int M> __device__ __forceinline__ Dn<M> hypot(const Dn<M>& x, const Dn
   }
   return r;
 }
-template <int M> __device__ __forceinline__ Dn<M> j0(const Dn<M>& a) { return chain1(a, ::j0(a.v), -::j1(a.v)); }
-template <int M> __device__ __forceinline__ Dn<M> j1(const Dn<M>& a) {
-  const double x = a.v, J1 = ::j1(x);
-  return chain1(a, J1, x != 0.0 ? ::j0(x) - J1 / x : 0.5);
+// J0, J1 (and Y0, Y1 for x >= 3) from one joint evaluation (mh_bessel01.cuh), with
+// J0' = -J1, J1' = J0 - J1/x (1/2 at 0), Y0' = -Y1, Y1' = Y0 - Y1/x
+__device__ __forceinline__ void bessel01_t(double x, double& J0, double& J1, double& Y0, double& Y1) {
+  bessel01(x, J0, J1, Y0, Y1);
 }
-template <int M> __device__ __forceinline__ Dn<M> y0(const Dn<M>& a) { return chain1(a, ::y0(a.v), -::y1(a.v)); }
-template <int M> __device__ __forceinline__ Dn<M> y1(const Dn<M>& a) {
-  const double x = a.v, Y1 = ::y1(x);
-  return chain1(a, Y1, ::y0(x) - Y1 / x);
+template <int M>
+__device__ __forceinline__ void bessel01_t(const Dn<M>& a, Dn<M>& J0, Dn<M>& J1, Dn<M>& Y0, Dn<M>& Y1) {
+  const double x = a.v;
+  double j0v, j1v, y0v, y1v;
+  bessel01(x, j0v, j1v, y0v, y1v);
+  const double inv_x = x != 0.0 ? 1.0 / x : 0.0;
+  J0 = chain1(a, j0v, -j1v);
+  J1 = chain1(a, j1v, x != 0.0 ? j0v - j1v * inv_x : 0.5);
+  Y0 = chain1(a, y0v, -y1v);
+  Y1 = chain1(a, y1v, y0v - y1v * inv_x);
 }
 
 }  // namespace mh

@@ -1,14 +1,15 @@
 // mh_greens.cuh -- device Green-function kernels of the MarineHydro.jl hot path (FP64).
 //
 // Each function restates the reference function cited beside it (paths within the
-// MarineHydro.jl tree).  Special functions are CUDA's (j0, j1, y0, y1, exp, log,
-// atan2, sqrt, hypot, sincos); the complex exponential integral and the
-// Gauss-Kronrod rule are written from their published definitions (DLMF 6.6.2 /
-// 6.9.1; Kronrod's 15-point nodes, QUADPACK qk15).
+// MarineHydro.jl tree).  Elementary functions are CUDA's (exp, log, atan2, sqrt, hypot,
+// sincos); the Bessel functions J0, J1, Y0, Y1 (mh_bessel01.cuh, Chebyshev and Hankel
+// forms), the complex exponential integral and the Gauss-Kronrod rule are written from
+// published methods (DLMF 10.17.3, 6.6.2, 6.9.1; Kronrod's 15-point nodes, QUADPACK qk15).
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include "mh_bessel01.cuh"
 #include "mh_internal.cuh"
 
 namespace mh {
@@ -213,11 +214,11 @@ __device__ __forceinline__ double wu_A(double t) {
   return 1.21 + v;
 }
 
-// StruveH0 and StruveH1 fits (wu.jl:368-435); also returns J0/J1 so that the
-// Bessel calls are issued together.
+// StruveH0 and StruveH1 fits (wu.jl:368-435); also returns J0/J1.  The four Bessel
+// functions of the argument come from one joint evaluation (mh_bessel01.cuh).
 __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& J0, double& J1) {
-  J0 = j0(xx);
-  J1 = j1(xx);
+  double Y0, Y1;
+  bessel01(xx, J0, J1, Y0, Y1);
   if (xx <= 3.0) {
     double yy = (xx / 3.0) * (xx / 3.0);
     double h0 = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
@@ -227,10 +228,10 @@ __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& 
     double yy = (3.0 / xx) * (3.0 / xx);
     double c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
     double c2 = kPi * xx * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
-    H0 = c1 / c2 + y0(xx);
+    H0 = c1 / c2 + Y0;
     double d1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
     double d2 = kPi * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
-    H1 = d1 / d2 + y1(xx);
+    H1 = d1 / d2 + Y1;
   }
 }
 

@@ -114,6 +114,8 @@ void launch_mlp_loss_grad(cudaStream_t st, LaunchCounter lc, const float* qparam
 void launch_round_bf16(cudaStream_t st, LaunchCounter lc, const float* in, float* out);
 // point evaluators
 void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out);
+// J0, J1, Y0, Y1 (NaN for Y below x = 3) at m points: out 4 doubles per point
+void launch_bessel01_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out);
 void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* r, const double* z, double rtol,
                          double atol, double2* out);
 

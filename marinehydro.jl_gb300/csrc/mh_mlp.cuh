@@ -106,33 +106,41 @@ __device__ __forceinline__ void mlp_forward(const float* __restrict__ P, float u
   }
 }
 
+// At inference the surrogate runs in FP32 throughout: its inputs, the Wu base it corrects
+// (mh_wu_f32.cuh) and the correction.  The network's own error (~1e-3 of the coefficients
+// against the exact term) is far above FP32 rounding.
+__device__ __forceinline__ void mlp_inputs_f(float r, float z, float& u, float& v) {
+  u = log10f(r) * (1.0f / 3.0f);
+  v = fmaf(z, 1.0f / 25.0f, 1.0f);
+}
+
 // the correction from the network outputs y0 (Re dG) and y2 (Re dGr) at (r, z)
-__device__ __forceinline__ void surrogate_apply(float y0, float y2, double r, double z, double2& dG, double2& dGr,
-                                                double2& dGz) {
-  const double d = sqrt(r * r + z * z);
-  const double inv = 1.0 / ((1.0 + d) * (1.0 + d));
-  dG = make_double2(y0 * inv, 0.0);
-  dGr = make_double2(y2 * inv * (r / (1.0 + r)), 0.0);
+__device__ __forceinline__ void surrogate_apply(float y0, float y2, float r, float z, float2& dG, float2& dGr,
+                                                float2& dGz) {
+  const float d = sqrtf(fmaf(r, r, z * z));
+  const float inv = 1.0f / ((1.0f + d) * (1.0f + d));
+  dG = make_float2(y0 * inv, 0.0f);
+  dGr = make_float2(y2 * inv * (r / (1.0f + r)), 0.0f);
   dGz = dG;
 }
 
 // the surrogate's correction to the Wu terms at (r, z): dGF, dGh, dGv (complex) to add
-// to wu_wave_term_and_derivs' GF, Gh, Gv.  Below r = 1e-3 the network is read at
+// to wu_wave_term_and_derivs_f32's GF, Gh, Gv.  Below r = 1e-3 the network is read at
 // r = 1e-3: the remainder is even in r (its r-derivative vanishes like r), so its
 // value there differs from the r -> 0 limit by O(1e-6) of its size, and the dG/dr
 // correction keeps its factor r.
-__device__ __forceinline__ void surrogate_correction(const float* __restrict__ P, double r, double z, double2& dG,
-                                                     double2& dGr, double2& dGz) {
+__device__ __forceinline__ void surrogate_correction(const float* __restrict__ P, float r, float z, float2& dG,
+                                                     float2& dGr, float2& dGz) {
   float u, v, y[kMlpOut];
-  mlp_inputs(fmax(r, kSurrRMin), z, u, v);
+  mlp_inputs_f(fmaxf(r, (float)kSurrRMin), z, u, v);
   mlp_forward(P, u, v, y);
   surrogate_apply(y[0], y[2], r, z, dG, dGr, dGz);
 }
 
 // where the surrogate is used: r up to the top of the training box (below it, see
 // surrogate_correction) and z within it; elsewhere the exact kernel
-__device__ __forceinline__ bool surrogate_in_box(double r, double z) {
-  return r <= kSurrRMax && z >= kSurrZMin && z <= 0.0;
+__device__ __forceinline__ bool surrogate_in_box(float r, float z) {
+  return r <= (float)kSurrRMax && z >= (float)kSurrZMin && z <= 0.0f;
 }
 
 }  // namespace mh

@@ -23,6 +23,7 @@
 #include "mh_greens.cuh"
 #include "mh_internal.cuh"
 #include "mh_mlp.cuh"
+#include "mh_wu_f32.cuh"
 
 namespace mh {
 
@@ -302,14 +303,16 @@ __global__ void __launch_bounds__(32 * kSampleWarps) surrogate_points_kernel(con
   if (q >= m) return;  // warp-uniform
   const double rq = r[q], zq = z[q];
   double2 GF, Gh, Gv;
-  if (surrogate_in_box(rq, zq)) {
+  if (surrogate_in_box((float)rq, (float)zq)) {
+    // FP32 throughout, as the tensor-core assembly (wave_kernel_tc)
     if (lane != 0) return;
-    wu_wave_term_and_derivs(rq, zq, GF, Gh, Gv);
-    double2 dG, dGr, dGz;
-    surrogate_correction(reinterpret_cast<const float*>(spp4), rq, zq, dG, dGr, dGz);
-    GF = zadd(GF, dG);
-    Gh = zadd(Gh, dGr);
-    Gv = zadd(Gv, dGz);
+    const float rf = (float)rq, zf = (float)zq;
+    float2 g, gh, gv, dG, dGr, dGz;
+    wu_wave_term_and_derivs_f32(rf, zf, g, gh, gv);
+    surrogate_correction(reinterpret_cast<const float*>(spp4), rf, zf, dG, dGr, dGz);
+    GF = make_double2(g.x + dG.x, g.y + dG.y);
+    Gh = make_double2(gh.x + dGr.x, gh.y + dGr.y);
+    Gv = make_double2(gv.x + dGz.x, gv.y + dGz.y);
   } else {
     egd_warp(rq, zq, rtol, atol, sw[warp], GF, Gh);
     if (lane != 0) return;

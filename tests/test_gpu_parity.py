@@ -39,6 +39,23 @@ def gf_tuple(mh, names):
     return tuple(m[n]() for n in names)
 
 
+def test_bessel01_points(mh, ctx):
+    # the joint J0/J1/Y0/Y1 evaluator of the Wu kernels against scipy's (Cephes) Bessel
+    # functions: absolute error, dense over the polynomial intervals and the Hankel region
+    special = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(3)
+    x = np.concatenate([[0.0, 1e-12, 2.9999999, 3.0, 7.9999999999, 8.0, 8.0000000001, 1e3, 3.3e4],
+                        np.linspace(0, 8, 1601), rng.uniform(0, 40, 2000), 10 ** rng.uniform(1, 3, 500)])
+    got = mh._device.bessel01_points(ctx, x)
+    ref = np.stack([special.j0(x), special.j1(x), special.y0(x), special.y1(x)], axis=1)
+    for c in range(2):
+        assert np.abs(got[:, c] - ref[:, c]).max() < 4e-15, (c, np.abs(got[:, c] - ref[:, c]).max())
+    ok = x >= 3.0
+    assert np.isnan(got[~ok, 2:]).all()
+    for c in (2, 3):
+        assert np.abs(got[ok, c] - ref[ok, c]).max() < 4e-15, (c, np.abs(got[ok, c] - ref[ok, c]).max())
+
+
 def test_wu_wave_terms(mh, oracle, ctx):
     rng = np.random.default_rng(0)
     hh = np.concatenate([[0.0, 1e-7, 2.999, 3.0, 3.001], rng.uniform(0, 20, 300), 10 ** rng.uniform(-3, 2, 200)])

@@ -103,9 +103,30 @@ def test_points_fallback_and_correction(mh, ctx, trained):
     e_s = np.abs(sur[:k, 0] - ex[:k, 0]) / np.abs(ex[:k, 0])
     e_w = np.abs(wu[:k, 0] - ex[:k, 0]) / np.abs(ex[:k, 0])
     assert np.sqrt(np.mean(e_s ** 2)) < np.sqrt(np.mean(e_w ** 2))
-    # imaginary parts are the exact J0 / J1 terms in both kernels; the surrogate keeps Wu's
-    assert np.array_equal(sur[:k, 0].imag, wu[:k, 0].imag)
-    assert np.abs(sur[:k, 0].imag - ex[:k, 0].imag).max() < 1e-9
+    # imaginary parts are the exact J0 / J1 terms in both kernels; the surrogate keeps Wu's,
+    # evaluated in FP32 (the phase k r in FP32 costs ~6e-8 r of it)
+    assert np.abs(sur[:k, 0].imag - wu[:k, 0].imag).max() < 1e-5
+    assert np.abs(sur[:k, 0].imag - ex[:k, 0].imag).max() < 1e-5
+
+
+def test_fp32_wu_base(mh, ctx):
+    """With every network parameter zero the surrogate adds nothing, so its point values are
+    the FP32 Wu term it corrects: within FP32 rounding of the FP64 term (the phase k r in FP32
+    bounds it at large r) over the training box."""
+    rng = np.random.default_rng(11)
+    r = np.concatenate([10 ** rng.uniform(-3, 3, 3000), rng.uniform(0, 20, 2000)])
+    z = -np.concatenate([10 ** rng.uniform(-3, np.log10(50), 3000), rng.uniform(1e-3, 30, 2000)])
+    ctx.surrogate_set(np.zeros(N_PARAMS, dtype=np.float32))
+    try:
+        got = mh.surrogate_wave_terms(r, z, ctx=ctx)
+    finally:
+        mh.load_surrogate(ctx=ctx)
+    ref = _wu(mh, ctx, r, z)
+    for c in range(3):
+        err = np.abs(got[:, c] - ref[:, c]) / np.maximum(np.abs(ref[:, c]), 1.0)
+        small = r < 100
+        assert err[small].max() < 4e-6, (c, err[small].max())
+        assert err.max() < 2e-5, (c, err.max())
 
 
 def _exact(mh, ctx, r, z):
