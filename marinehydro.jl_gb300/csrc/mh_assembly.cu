@@ -602,8 +602,18 @@ __device__ __forceinline__ void exact_pair_warp(const AssemblyParams& p, int64_t
   double r, z;
   reduced_coords(ci, Pj.c, k, r, z);
   double2 GF, dGdr;
-  egd_warp(r, z, p.quad_rtol, p.quad_atol, sw, GF, dGdr);
-  if ((threadIdx.x & 31) != 0) return;
+  if (r == 0.0) {
+    // self pairs and vertically stacked centres: at r = 0 the integrand does not depend on
+    // theta (zeta = z), so 4 times its integral over [0, pi/2] is 2 pi times its value; the
+    // r-derivative is not needed (the horizontal gradient vanishes for r <= 1e-6)
+    if ((threadIdx.x & 31) != 0) return;
+    const double2 f = egd_integrand<false>(0.0, 0.0, z);
+    GF = make_double2(2.0 * kPi * f.x, 2.0 * kPi * f.y);
+    dGdr = make_double2(0.0, 0.0);
+  } else {
+    egd_warp(r, z, p.quad_rtol, p.quad_atol, sw, GF, dGdr);
+    if ((threadIdx.x & 31) != 0) return;
+  }
   // both_greens_and_gradient_greens + with_reduced_coordinates_derivative, as wave_terms<., 2>
   const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
   const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
