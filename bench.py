@@ -187,6 +187,11 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3] not in ("", "[N/A]"))}
 
 
+# DRAM bytes per launch of the FP64 trailing update on this workload, from one ncu capture of
+# the full sweep (dram__bytes_read.sum + dram__bytes_write.sum, 124 launches: 153.3 GB)
+GEMM_F64_TRAFFIC_PER_LAUNCH = 1.236e9
+
+
 def lu_gemm_flops(n, nb=32):
     """Algorithmic real flops of the trailing updates of one n x n complex LU (8 per complex MAC)."""
     f = 0
@@ -355,7 +360,11 @@ def run_gpu(args):
         flops_per_launch = lu_gemm_flops(n) * N_OMEGA / (top_launches / args.steps)
         achieved = flops_per_launch / (top_ms / top_launches * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": top_name, "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                "frac": achieved / peak64, "traffic": None,
+                "frac": achieved / peak64, "traffic": GEMM_F64_TRAFFIC_PER_LAUNCH,
+                "traffic_unit": "bytes per launch (DRAM read + write)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every gemm_kernel<double> "
+                                  "launch of the same 30-frequency sweep (profiles/lu_gemm_f64_cylinder2000.md); "
+                                  "algorithmic: 32 B per trailing-block entry, 1.26e9 B per launch",
                 "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks (MEASURED_PEAKS.json "
                                "has no FP64 figure)",
                 "work": "8 real flops per complex multiply-add of the trailing update, summed over panel steps"}

@@ -199,23 +199,27 @@ __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float
     const int64_t cbase = (ct0 + t) * kBxTile + half * 64;
     const uint32_t t_re = tmem + lane_off + (uint32_t)(t & 1) * 256u + (uint32_t)(half * 64), t_im = t_re + 128u;
 #pragma unroll 1
-    for (int c0 = 0; c0 < 64; c0 += 16) {
-      // all 16 loads of A22 first (loads and stores through one pointer would otherwise be
-      // issued one after another), then the accumulators, then the stores
-      float2 cv[16];
+    for (int c0 = 0; c0 < 64; c0 += 32) {
+      // all 32 loads of A22 first (loads and stores through one pointer would otherwise be
+      // issued one after another; 32 in flight per thread keep HBM busier than 16), then the
+      // accumulators, then the stores
+      float2 cv[32];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
+      for (int q = 0; q < 32; ++q) {
         const int64_t c = cbase + c0 + q;
         cv[q] = (row_live && c < rest) ? crow[c * n] : make_float2(0.f, 0.f);
       }
-      float re[16], im[16];
-      tc::tmem_ld16(t_re + (uint32_t)c0, re);
-      tc::tmem_ld16(t_im + (uint32_t)c0, im);
-      if (row_live) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int64_t c = cbase + c0 + q;
-          if (c < rest) crow[c * n] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+      for (int h = 0; h < 32; h += 16) {
+        float re[16], im[16];
+        tc::tmem_ld16(t_re + (uint32_t)(c0 + h), re);
+        tc::tmem_ld16(t_im + (uint32_t)(c0 + h), im);
+        if (row_live) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int64_t c = cbase + c0 + h + q;
+            if (c < rest) crow[c * n] = make_float2(cv[h + q].x - re[q], cv[h + q].y - im[q]);
+          }
         }
       }
     }

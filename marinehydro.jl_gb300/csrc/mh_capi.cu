@@ -107,7 +107,7 @@ namespace {
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
   kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
-  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotCount
+  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotAnorm, kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...) {
@@ -316,17 +316,21 @@ int ensure_static_cache(mh_context* ctx, mh_mesh* m, uint32_t gfs, int direct, i
 }
 
 // --- dense solve core on device arrays ------------------------------------------
-// FP32 copy of the batch `Adev` (left intact for the FP64 residuals), factored in place.
-int factor_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, float2** LU32_out) {
+// FP32 copy of the batch `Adev` (left intact for the FP64 residuals), factored in place;
+// the matrices' |.|_inf norms (for the refinement's stopping test) come from the same pass.
+int factor_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, float2** LU32_out, double** anrm_out) {
   const int64_t n = d.n, nn = n * n;
   int32_t *ipiv, *info;
   float2* LU32;
   MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * d.batch), &ipiv));
   MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)d.batch, &info));
   MH_TRY(ws_get_t(ctx, kSlotLU32, (size_t)(nn * d.batch), &LU32));
+  double* anrm;
+  MH_TRY(ws_get_t(ctx, kSlotAnorm, (size_t)d.batch, &anrm));
   BatchDesc d32 = d;
   d32.stride = nn;
-  for (int64_t b = 0; b < d.batch; ++b) convert_z_to_c(ctx->stream, ctx->lc(), Adev + b * d.stride, LU32 + b * nn, nn);
+  convert_with_norms(ctx->stream, ctx->lc(), d, Adev, LU32, nn, anrm);
+  *anrm_out = anrm;
   // the trailing updates on the BF16 tensor cores (three-way split, FP32 accuracy)
   unsigned char* ws;
   const size_t wsb = bx3_workspace_bytes(n, d.batch);
@@ -348,8 +352,8 @@ int factor_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, float
 // |b - A x|_inf <= sqrt(n) eps |A|_inf |x|_inf for every column, at most 30 sweeps.
 // X holds b on entry and x on exit; *converged reports whether every column met the test
 // (when it did not, X holds the last iterate and the caller falls back to FP64).
-int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const float2* LU32, double2* X,
-                 int64_t nrhs, int64_t xstride, bool adjoint, bool* converged, double2** B0_out) {
+int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const float2* LU32, const double* anrm,
+                 double2* X, int64_t nrhs, int64_t xstride, bool adjoint, bool* converged, double2** B0_out) {
   const int64_t n = d.n, nn = n * n;
   int32_t* ipiv;
   float2* X32;
@@ -371,7 +375,7 @@ int refine_mixed(mh_context* ctx, const BatchDesc& d, const double2* Adev, const
   double* norms;
   MH_TRY(ws_get_t(ctx, kSlotNorm, (size_t)(2 * ncols + d.batch), &norms));
   double* anrm_d = norms + 2 * ncols;
-  matrix_inf_norms(ctx->stream, ctx->lc(), d, Adev, anrm_d);
+  MH_CUDA(ctx, cudaMemcpyAsync(anrm_d, anrm, sizeof(double) * d.batch, cudaMemcpyDeviceToDevice, ctx->stream));
   double* hn;
   MH_TRY(pinned_get(ctx, sizeof(double) * (2 * ncols + d.batch) + 64, &hn));
   int* tcflag;  // the FP64-accurate residuals run on the tensor cores (forward solves)
@@ -454,10 +458,11 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
     if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
   } else {
     float2* LU32;
-    MH_TRY(factor_mixed(ctx, d, Adev, &LU32));
+    double* anrm;
+    MH_TRY(factor_mixed(ctx, d, Adev, &LU32, &anrm));
     bool converged = false;
     double2* B0 = nullptr;
-    MH_TRY(refine_mixed(ctx, d, Adev, LU32, X, nrhs, xstride, adjoint, &converged, &B0));
+    MH_TRY(refine_mixed(ctx, d, Adev, LU32, anrm, X, nrhs, xstride, adjoint, &converged, &B0));
     if (!converged) {
       // fall back to the FP64 factorization
       MH_CUDA(ctx, cudaMemcpyAsync(X, B0, sizeof(double2) * xstride * d.batch, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -584,14 +589,13 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
     lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
   } else {
     BatchDesc d32{n, nw, nn};
+    const int64_t ncols = o.nrhs * nw;
     cudaMemcpyAsync(b.B0, b.X, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
-    convert_z_to_c(st, lc, b.D, b.LU32, nn * nw);
+    convert_with_norms(st, lc, d, b.D, b.LU32, nn, b.norms + 2 * ncols);
     lu_factor_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.info, b.oz, b.ozflag);
     convert_z_to_c(st, lc, b.B0, b.X32, bstride * nw);
     lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
     widen_c_to_z(st, lc, b.X32, b.X, bstride * nw);
-    const int64_t ncols = o.nrhs * nw;
-    matrix_inf_norms(st, lc, d, b.D, b.norms + 2 * ncols);
     for (int it = 0; it < o.ir_sweeps; ++it) {
       residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
       convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
@@ -1576,13 +1580,14 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
       // FP32 factors, both solves refined to FP64 backward error; any column that does not
       // converge sends the whole chunk to the FP64 factorization below (D is left intact)
       float2* LU32;
-      MH_TRY(factor_mixed(ctx, d, D, &LU32));
+      double* anrm;
+      MH_TRY(factor_mixed(ctx, d, D, &LU32, &anrm));
       zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
       bool ok_fwd = false, ok_adj = false;
-      MH_TRY(refine_mixed(ctx, d, D, LU32, X, nh, bstride, false, &ok_fwd, nullptr));
+      MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, nh, bstride, false, &ok_fwd, nullptr));
       if (ok_fwd) {
         forces_and_weights();
-        MH_TRY(refine_mixed(ctx, d, D, LU32, lam, nh, bstride, true, &ok_adj, nullptr));
+        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, nh, bstride, true, &ok_adj, nullptr));
       }
       done = ok_fwd && ok_adj;
     }

@@ -165,7 +165,9 @@ void residual_tc_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, 
                          int* timeout_flag);
 void ir_update(cudaStream_t st, LaunchCounter lc, int64_t count, double2* X, const float2* C);
 void widen_c_to_z(cudaStream_t st, LaunchCounter lc, const float2* src, double2* dst, int64_t count);
-void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out);
+// FP32 copy of each matrix (matrix stride stride32) and its |.|_inf norm into out[b], one pass over A
+void convert_with_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, float2* A32,
+                        int64_t stride32, double* out);
 void inf_norms_batched(cudaStream_t st, LaunchCounter lc, int64_t n, int64_t ncols, const double2* X,
                        double* out);
 

@@ -927,22 +927,28 @@ __global__ void col_inf_norm_kernel(int64_t n, const double2* __restrict__ X, do
 }
 
 
-// out[b] = max_i sum_j |re|+|im| of matrix b (|.|_inf, order independent via atomicMax on the bits
-// of a non-negative double); out must be zeroed first
-// 128 rows x 8 column slices per CTA (more loads in flight than one thread per row); the
-// slices' partial row sums are added in a fixed order
-__global__ void __launch_bounds__(1024) mat_inf_norm_kernel(BatchDesc d, const double2* __restrict__ A,
+// the FP32 copy of matrix b (column stride n, matrix stride stride32) and, in the same pass
+// over A, out[b] = max_i sum_j |re|+|im| (|.|_inf, order independent via atomicMax on the bits
+// of a non-negative double; out zeroed first).  128 rows x 8 column slices per CTA, the
+// slices' partial row sums added in a fixed order.
+__global__ void __launch_bounds__(1024) convert_norm_kernel(BatchDesc d, const double2* __restrict__ A,
+                                                            float2* __restrict__ A32, int64_t stride32,
                                                             unsigned long long* __restrict__ out) {
   __shared__ double part[8][128];
   const int64_t i = blockIdx.x * (int64_t)128 + threadIdx.x;
   const int64_t b = blockIdx.y;
   const int64_t n = d.n;
   const double2* Ab = A + b * d.stride;
+  float2* Cb = A32 + b * stride32;
   const int64_t j0 = (n * threadIdx.y) / 8, j1 = (n * (threadIdx.y + 1)) / 8;
   double s = 0.0;
   if (i < n) {
 #pragma unroll 4
-    for (int64_t j = j0; j < j1; ++j) { const double2 v = Ab[i + j * n]; s += fabs(v.x) + fabs(v.y); }
+    for (int64_t j = j0; j < j1; ++j) {
+      const double2 v = Ab[i + j * n];
+      Cb[i + j * n] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+      s += fabs(v.x) + fabs(v.y);
+    }
   }
   part[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
@@ -955,11 +961,14 @@ __global__ void __launch_bounds__(1024) mat_inf_norm_kernel(BatchDesc d, const d
 
 }  // namespace
 
-void matrix_inf_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, double* out) {
+void convert_with_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, float2* A32,
+                        int64_t stride32, double* out) {
   cudaMemsetAsync(out, 0, sizeof(double) * d.batch, st);
   dim3 grid((unsigned)((d.n + 127) / 128), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "ir_norms", mat_inf_norm_kernel<<<grid, dim3(128, 8), 0, st>>>(d, A, (unsigned long long*)out));
+  MH_LAUNCH(lc, st, "convert", convert_norm_kernel<<<grid, dim3(128, 8), 0, st>>>(d, A, A32, stride32,
+                                                                                (unsigned long long*)out));
 }
+
 
 // CTAs per cluster for a panel of m rows in a batch of `batch` matrices: enough to hold
 // the panel in shared memory, and more (up to 8) while all `batch` clusters still fit on
