@@ -111,6 +111,16 @@ int mh_mesh_create(mh_context* ctx, int64_t n_panels, const double* vertices, co
                    const double* normals, const double* areas, const double* radii, int mem, mh_mesh** out);
 int mh_mesh_destroy(mh_mesh* mesh);
 int64_t mh_mesh_panels(const mh_mesh* mesh);
+/* Replaces the hull + lid mesh of irregular-frequency removal (solve.jl:20-28,
+   `_mesh_including_lid`; bodies.jl:9-23 `lid_mesh`): the mesh holds the hull's
+   n_hull panels first and the lid's panels after them (`fb.mesh + fb.lid_mesh`).
+   Assembly covers all panels; in mh_hydrodynamic_coefficients and the batch the
+   boundary conditions are zero on the lid (`_pad_hull_bc`, solve.jl:2-10) and
+   only hull pressures enter the forces (`pressure[hull_mask]`, solve.jl:47-55).
+   Every lid panel centre must lie below z = -1e-8 (at the free surface the wave
+   terms are singular at the self pairs); n_hull = n_panels removes the lid.
+   mh_hydro_gradient rejects meshes with a lid (MH_ERR_UNSUPPORTED). */
+int mh_mesh_set_lid(mh_mesh* mesh, int64_t n_hull);
 
 /* ---- assembly ----------------------------------------------------------- */
 /* Replaces assemble_matrices(green_functions, mesh::StaticArraysMesh, k;

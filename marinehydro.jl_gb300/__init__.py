@@ -18,7 +18,7 @@ from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineR
                            RankineReflectedNegative, SurrogateDelhommeau, bem_formulation, default_greens_functions, gf_flags, is_direct,
                            partition_greens_functions)
 from .meshes import (Mesh, StaticArraysMesh, barge_mesh, combine_meshes, config1_hemisphere,  # noqa: F401
-                     config2_cylinder, face_fields, face_fields_jacobian, hemisphere_mesh, random_body, smesh, tiny_static_mesh, vertical_cylinder_mesh)
+                     config2_cylinder, disc_lid_mesh, face_fields, face_fields_jacobian, hemisphere_mesh, random_body, smesh, tiny_static_mesh, vertical_cylinder_mesh)
 from .problems import (SETTINGS, DiffractionProblem, DiffractionResult, RadiationProblem,  # noqa: F401
                        RadiationResult, added_mass, compute_encountered_values, compute_wavenumber,
                        diffraction_force, make_result, radiation_coefficients, radiation_damping, remake, set_g,

@@ -12,7 +12,7 @@ from ._lib import MH_MEM_DEVICE, MH_MEM_HOST, ptr_and_mem
 class DeviceMesh:
     """An mh_mesh: one body's panels resident on the device of `ctx`."""
 
-    def __init__(self, ctx: _lib.Context, mesh):
+    def __init__(self, ctx: _lib.Context, mesh, n_hull=None):
         self.ctx = ctx
         self.n = mesh.nfaces
         V = np.ascontiguousarray(mesh.panel_vertices, dtype=np.float64)
@@ -25,6 +25,10 @@ class DeviceMesh:
                                         A.ctypes.data, R.ctypes.data, MH_MEM_HOST, ctypes.byref(h)),
                   "mh_mesh_create")
         self._h = h
+        self.n_hull = self.n
+        if n_hull is not None and n_hull != self.n:
+            ctx.check(ctx._L.mh_mesh_set_lid(self._h, int(n_hull)), "mh_mesh_set_lid")
+            self.n_hull = int(n_hull)
 
     @classmethod
     def from_device_arrays(cls, ctx, n, V, C, N, A, R):

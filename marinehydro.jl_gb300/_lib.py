@@ -34,7 +34,7 @@ GF_SURROGATE = 128
 EXPORTS = (
     "mh_abi_version", "mh_create", "mh_destroy", "mh_last_error", "mh_get_stream", "mh_set_stream",
     "mh_synchronize", "mh_launch_count", "mh_workspace_bytes", "mh_mesh_create", "mh_mesh_destroy",
-    "mh_mesh_panels", "mh_assemble_matrices", "mh_linsolve", "mh_solve", "mh_linsolve_adjoint",
+    "mh_mesh_panels", "mh_mesh_set_lid", "mh_assemble_matrices", "mh_linsolve", "mh_solve", "mh_linsolve_adjoint",
     "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_bessel01_points", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
@@ -84,6 +84,7 @@ def load(path: str | None = None):
         L.mh_mesh_destroy.argtypes = [vp]
         L.mh_mesh_panels.argtypes = [vp]
         L.mh_mesh_panels.restype = i64
+        L.mh_mesh_set_lid.argtypes = [vp, i64]
         L.mh_assemble_matrices.argtypes = [vp, vp, D, u32, I, I, vp, vp, vp, I]
         L.mh_linsolve.argtypes = [vp, i64, i64, vp, vp, vp, I, I]
         L.mh_linsolve_adjoint.argtypes = [vp, i64, i64, vp, vp, vp, I, I]

@@ -23,7 +23,7 @@ from .bodies import FloatingBody, evaluate_gradient_of_motion
 from .formulations import BEMFormulation, DirectBEM, bem_formulation, gf_flags, is_direct
 from .meshes import StaticArraysMesh, face_fields, face_fields_jacobian
 from .problems import (DiffractionProblem, DiffractionResult, RadiationProblem, RadiationResult, SETTINGS,
-                       compute_wavenumber, make_result)
+                       added_mass, compute_wavenumber, make_result, radiation_damping)
 
 
 def _ctx(ctx=None):
@@ -152,29 +152,48 @@ def excitation_force(res: DiffractionResult) -> dict:
 # problem level
 # ---------------------------------------------------------------------------
 def solve(problem, formulation: BEMFormulation | None = None, ctx=None):
-    """solve(problem, formulation) (solve.jl:195-201) or, for arrays, solve(D, S, bc; direct)."""
+    """solve(problem, formulation) (solve.jl:59-65) or, for arrays, solve(D, S, bc; direct)."""
     if isinstance(problem, (list, tuple)):
         return [solve(p, formulation, ctx=ctx) for p in problem]
     if isinstance(problem, np.ndarray):
         raise TypeError("use solve_linear(D, S, bc, direct=...) for the matrix-level solve")
-    f = formulation or DirectBEM()
-    c = _ctx(ctx)
+    return _solve_group([problem], formulation or DirectBEM(), _ctx(ctx))[0]
+
+
+def _solve_group(problems, f: BEMFormulation, c):
+    """solve(problem, f) for problems of one body that share the encountered frequency,
+    wavenumber and forward speed: one assembly and one factorization for all of their
+    right-hand sides, the rest as the reference's per-problem path (solve.jl:20-65):
+    hull + lid mesh with the hull conditions padded by zeros, pressure i rho omega phi on
+    the hull, plus rho U (K sigma) with K assembled for the normal [1, 0, 0] when U != 0."""
+    p0 = problems[0]
+    body = p0.floatingbody
     direct = is_direct(f)
-    omega = problem.omega if problem.forward_speed == 0 else problem.encountered_omega
-    k = problem.wavenumber if problem.forward_speed == 0 else problem.encountered_wavenumber
-    mesh = problem.floatingbody.mesh
-    bc = compute_bc(problem)
+    U = p0.forward_speed
+    omega = p0.omega if U == 0 else p0.encountered_omega
+    k = p0.wavenumber if U == 0 else p0.encountered_wavenumber
+    for p in problems[1:]:
+        if (p.floatingbody is not body or p.forward_speed != U or p.rho != p0.rho
+                or (p.omega if U == 0 else p.encountered_omega) != omega
+                or (p.wavenumber if U == 0 else p.encountered_wavenumber) != k):
+            raise ValueError("problems solved together must share body, frequency, wavenumber and forward speed")
+    if U != 0 and direct:
+        raise ValueError("nonzero forward speed is not supported with the direct method; use IndirectBEM "
+                         "(direct = false)")
+    mesh, n_hull = body.mesh_including_lid()
+    bc = np.zeros((mesh.nfaces, len(problems)), dtype=np.complex128)
+    for q, p in enumerate(problems):
+        bc[:n_hull, q] = compute_bc(p)
     S, D = assemble_matrices(f.greens, mesh, k, direct=direct, ctx=c)
     potential, sources = _device.solve_linear(c, D, S, bc, direct, f.precision_code)
-    pressure = 1j * problem.rho * omega * potential
-    if problem.forward_speed != 0:
-        # _maybe_forward_speed_pressure (solve.jl:171-181)
-        if direct:
-            raise ValueError("nonzero forward speed is not supported with the direct method; use IndirectBEM "
-                             "(direct = false)")
+    pressure = 1j * p0.rho * omega * potential
+    if U != 0:
+        # _maybe_forward_speed_pressure (solve.jl:35-45)
         _, K = assemble_matrices(f.greens, mesh, k, direct=False, all_normals=[1.0, 0.0, 0.0], ctx=c)
-        pressure = pressure + problem.rho * problem.forward_speed * (K @ sources)
-    return make_result(problem, integrate_pressure(problem.floatingbody, problem.influenced_dofs, pressure))
+        pressure = pressure + p0.rho * U * (K @ sources)
+    pressure = pressure[:n_hull]
+    return [make_result(p, integrate_pressure(body, p.influenced_dofs, pressure[:, q]))
+            for q, p in enumerate(problems)]
 
 
 def solve_problem(problem, formulation=None, direct=True, gf="Wu", greens_functions=None, ctx=None):
@@ -207,38 +226,85 @@ def problems_from_data(parameters: dict, body: FloatingBody) -> dict:
 
 def hydrodynamic_coefficients(body: FloatingBody, parameters: dict, formulation: BEMFormulation | None = None,
                               ctx=None, rho=None, g=None) -> dict:
-    """hydrodynamic_coefficients (problems_and_results.jl:464-495) for zero forward speed.
+    """hydrodynamic_coefficients (problems_and_results.jl:464-495).
 
-    Returns numpy arrays with the reference's shapes (n_U = 1):
+    Returns numpy arrays with the reference's shapes.  Without a `forward_speeds` key:
       added_mass, radiation_damping: (n_inf, n_rad, n_omega, 1)
       diffraction_force, Froude_Krylov_force, excitation_force: (n_inf, n_omega, n_beta, 1)
-    One assembly of S and D and one factorization per frequency serve every
-    radiation and diffraction right-hand side.
+    With `forward_speeds` (problems_and_results.jl:262-270, 346-363) the radiation arrays
+    gain the heading axis, (n_inf, n_rad, n_omega, n_U, n_beta), and the diffraction arrays
+    are (n_inf, n_omega, n_beta, n_U).
+    Zero speed runs the device sweep (mh_hydrodynamic_coefficients): one assembly of S and
+    D and one factorization per frequency serve every radiation and diffraction
+    right-hand side.  A nonzero speed needs IndirectBEM (solve.jl:35-45); its problems are
+    solved per (omega, beta) -- they share the encountered wavenumber -- with one
+    assembly, one K matrix and one factorization for every dof and the diffraction.
     """
     f = formulation or DirectBEM()
-    if any(u != 0 for u in parameters.get("forward_speeds", [0.0])):
-        raise ValueError("hydrodynamic_coefficients on the GPU sweep supports forward_speeds = [0] only; "
-                         "use solve(RadiationProblem(..., forward_speed=U), IndirectBEM())")
     c = _ctx(ctx)
     oms = np.atleast_1d(np.asarray(parameters["wave_frequencies"], dtype=float))
     names = list(body.dofs)
     inf = list(parameters.get("influenced_dofs", names))
     rad = list(parameters.get("radiating_dofs", []))
     betas = list(parameters.get("wave_directions", []))
-    idx = {n: i for i, n in enumerate(names)}
-    dofs = body.dof_array(names)
     rho = parameters.get("rho", SETTINGS["rho"]) if rho is None else rho
     g = parameters.get("g", SETTINGS["g"]) if g is None else g
-    A, B, Fd, Fk, Fe = _device.hydro_sweep(c, body.mesh.device_mesh(c), oms, rho, g, gf_flags(f.greens),
-                                           is_direct(f), dofs, [idx[d] for d in rad], [idx[d] for d in inf], betas,
-                                           f.precision_code)
+    if "forward_speeds" not in parameters:
+        A, B, Fd, Fk, Fe = _zero_speed_sweep(c, body, f, oms, rho, g, names, rad, inf, betas)
+        return {
+            "added_mass": A[..., None] if rad else np.zeros(0),
+            "radiation_damping": B[..., None] if rad else np.zeros(0),
+            "diffraction_force": Fd[..., None] if betas else np.zeros(0),
+            "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
+            "excitation_force": Fe[..., None] if betas else np.zeros(0),
+        }
+    Us = [float(u) for u in parameters["forward_speeds"]]
+    if rad and "wave_directions" not in parameters:
+        raise ValueError("radiation problems with forward_speeds need wave_directions "
+                         "(problems_and_results.jl:268-270)")
+    n_inf, n_rad, n_w, n_U, n_b = len(inf), len(rad), len(oms), len(Us), len(betas)
+    A = np.zeros((n_inf, n_rad, n_w, n_U, n_b))
+    B = np.zeros_like(A)
+    Fd = np.zeros((n_inf, n_w, n_b, n_U), dtype=np.complex128)
+    Fk = np.zeros_like(Fd)
+    for iU, U in enumerate(Us):
+        if U == 0:
+            a, b, fd, fk, _ = _zero_speed_sweep(c, body, f, oms, rho, g, names, rad, inf, betas)
+            if rad:
+                A[:, :, :, iU, :] = a[..., None]
+                B[:, :, :, iU, :] = b[..., None]
+            if betas:
+                Fd[..., iU] = fd
+                Fk[..., iU] = fk
+            continue
+        for iw, om in enumerate(oms):
+            for ib, beta in enumerate(betas):
+                probs = [RadiationProblem(body, om, d, inf, beta=beta, forward_speed=U, rho=rho, g=g) for d in rad]
+                probs.append(DiffractionProblem(body, om, beta, inf, forward_speed=U, rho=rho, g=g))
+                res = _solve_group(probs, f, c)
+                for ir in range(n_rad):
+                    am, bd = added_mass(res[ir]), radiation_damping(res[ir])
+                    A[:, ir, iw, iU, ib] = [am[d] for d in inf]
+                    B[:, ir, iw, iU, ib] = [bd[d] for d in inf]
+                fk = froude_krylov_force(res[-1])
+                Fd[:, iw, ib, iU] = [res[-1].forces[d] for d in inf]
+                Fk[:, iw, ib, iU] = [fk[d] for d in inf]
     return {
-        "added_mass": A[..., None] if rad else np.zeros(0),
-        "radiation_damping": B[..., None] if rad else np.zeros(0),
-        "diffraction_force": Fd[..., None] if betas else np.zeros(0),
-        "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
-        "excitation_force": Fe[..., None] if betas else np.zeros(0),
+        "added_mass": A if rad else np.zeros(0),
+        "radiation_damping": B if rad else np.zeros(0),
+        "diffraction_force": Fd if betas else np.zeros(0),
+        "Froude_Krylov_force": Fk if betas else np.zeros(0),
+        "excitation_force": Fd + Fk if betas else np.zeros(0),
     }
+
+
+def _zero_speed_sweep(c, body, f, oms, rho, g, names, rad, inf, betas):
+    """The zero-speed frequency sweep on the device (mh_hydrodynamic_coefficients)."""
+    idx = {n: i for i, n in enumerate(names)}
+    mesh, _ = body.mesh_including_lid()
+    return _device.hydro_sweep(c, mesh.device_mesh(c), oms, rho, g, gf_flags(f.greens), is_direct(f),
+                               body.padded_dof_array(names), [idx[d] for d in rad], [idx[d] for d in inf], betas,
+                               f.precision_code)
 
 
 def batch_hydrodynamic_coefficients(bodies, parameters_per_body, formulation: BEMFormulation | None = None,
@@ -262,10 +328,10 @@ def batch_hydrodynamic_coefficients(bodies, parameters_per_body, formulation: BE
     idx = {n: i for i, n in enumerate(names)}
     rho = p0.get("rho", SETTINGS["rho"]) if rho is None else rho
     g = p0.get("g", SETTINGS["g"]) if g is None else g
-    res = _device.batch_hydro(c, [b.mesh.device_mesh(c) for b in bodies],
+    res = _device.batch_hydro(c, [b.mesh_including_lid()[0].device_mesh(c) for b in bodies],
                               [np.atleast_1d(np.asarray(p["wave_frequencies"], dtype=float)) for p in
                                parameters_per_body], rho, g, gf_flags(f.greens), is_direct(f),
-                              [b.dof_array(names) for b in bodies], [idx[d] for d in rad], [idx[d] for d in inf],
+                              [b.padded_dof_array(names) for b in bodies], [idx[d] for d in rad], [idx[d] for d in inf],
                               betas, f.precision_code, n_streams)
     out = []
     for A, B, Fd, Fk, Fe in res:
@@ -301,6 +367,8 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     f = formulation or DirectBEM()
     if not is_direct(f):
         raise ValueError("hydro_gradient differentiates the direct formulation")
+    if body.lid_mesh is not None:
+        raise ValueError("hydro_gradient does not cover bodies with a lid")
     mesh = body.mesh
     c, nrm, a, _ = face_fields(mesh.vertices, mesh.faces - 1)
     if not (np.allclose(c, mesh.centers, rtol=0, atol=1e-12) and np.allclose(nrm, mesh.normals, rtol=0, atol=1e-12)

@@ -38,14 +38,21 @@ def evaluate_gradient_of_motion(mesh: StaticArraysMesh, name: str) -> np.ndarray
 
 
 class FloatingBody:
-    """FloatingBody (bodies.jl:9-51): mesh, optional lid, named dof fields (n x 3)."""
+    """FloatingBody (bodies.jl:9-51): mesh, optional lid, named dof fields (n x 3).
+
+    The dof fields live on the hull panels.  A lid (irregular-frequency removal) is a
+    mesh of panels inside the body's waterplane, below the free surface; the solve
+    runs on hull + lid with zero boundary conditions on the lid (solve.jl:2-28).
+    """
 
     def __init__(self, mesh: StaticArraysMesh, dofs=None, rotation_center=None, body_name: str = "body",
                  lid_mesh=None):
-        if lid_mesh is not None:
-            raise ValueError("lid meshes (irregular-frequency removal) are not supported by the GPU path")
+        if lid_mesh is not None and not np.all(np.asarray(lid_mesh.centers)[:, 2] < -1e-8):
+            raise ValueError("a lid must lie below the free surface (every lid panel centre at z < -1e-8); "
+                             "at z = 0 the wave Green functions are singular at the lid's self pairs")
         self.mesh = mesh
-        self.lid_mesh = None
+        self.lid_mesh = lid_mesh
+        self._with_lid = None
         self.body_name = body_name
         # rigid rotation dofs: name -> (axis index, rotation centre, first panel, end panel); their
         # fields follow the panel centres, which the gradient chain needs
@@ -69,6 +76,28 @@ class FloatingBody:
 
     def __add__(self, other):
         return combine_floatingbodies([self, other])
+
+    def mesh_including_lid(self):
+        """_mesh_including_lid (solve.jl:22-28): (hull + lid mesh, number of hull panels).
+
+        The hull panels come first, so the hull mask is `index < n_hull`; the combined
+        mesh carries `n_hull` to its device copy (mh_mesh_set_lid)."""
+        if self.lid_mesh is None:
+            return self.mesh, self.mesh.nfaces
+        if self._with_lid is None:
+            m = combine_meshes([self.mesh, self.lid_mesh])
+            m.n_hull = self.mesh.nfaces
+            self._with_lid = m
+        return self._with_lid, self.mesh.nfaces
+
+    def padded_dof_array(self, names=None) -> np.ndarray:
+        """dof_array on hull + lid panels: zeros on the lid."""
+        d = self.dof_array(names)
+        if self.lid_mesh is None or d.size == 0:
+            return d
+        out = np.zeros((d.shape[0], self.mesh.nfaces + self.lid_mesh.nfaces, 3))
+        out[:, :self.mesh.nfaces] = d
+        return out
 
     def dof_array(self, names=None) -> np.ndarray:
         names = list(self.dofs) if names is None else list(names)
@@ -109,6 +138,8 @@ def combine_floatingbodies(bodies, new_body_name: str | None = None) -> Floating
         for k, (ax, rc, p0, p1) in getattr(b, "rotations", {}).items():
             rotations[f"{nm}__{k}"] = (ax, rc, off + p0, off + p1)
         off += b.mesh.nfaces
-    out = FloatingBody(mesh, dofs, body_name=new_body_name or "+".join(names))
+    lids = [b.lid_mesh for b in bodies if b.lid_mesh is not None]  # bodies.jl:205-209
+    out = FloatingBody(mesh, dofs, body_name=new_body_name or "+".join(names),
+                       lid_mesh=combine_meshes(lids) if lids else None)
     out.rotations = rotations
     return out

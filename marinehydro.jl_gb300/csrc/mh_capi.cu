@@ -87,6 +87,7 @@ struct mh_context {
 struct mh_mesh {
   mh_context* ctx = nullptr;
   int64_t n = 0;
+  int64_t n_hull = 0;   // panels n_hull..n-1 are an irregular-frequency lid (mh_mesh_set_lid)
   double* V = nullptr;  // n x 12
   double* C = nullptr;  // n x 3
   double* N = nullptr;  // n x 3
@@ -573,7 +574,7 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   }
   launch_assemble_wave(st, lc, p, st_kinds ? b.SR : nullptr, st_kinds ? b.DR : nullptr, (int)nw, ks_d, b.S, b.D,
                        nn, st_kinds ? 0 : 1);
-  EpilogueGeom eg{n, b.m->C, b.m->N, b.m->A, b.dofs};
+  EpilogueGeom eg{n, b.m->n_hull, b.m->C, b.m->N, b.m->A, b.dofs};
   launch_build_rhs(st, lc, eg, (int)nw, om_d, o.g, (int)o.n_rad, rad_d, (int)o.n_beta, beta_d, b.B, bstride);
   BatchDesc d{n, nw, nn};
   if (b.ozflag) cudaMemsetAsync(b.ozflag, 0, sizeof(int), st);
@@ -684,7 +685,7 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
   const double* om_d = b.params;
   const double* beta_d = b.params + 2 * nw;
   const int32_t* inf_d = (const int32_t*)(b.params + 2 * nw + o.n_beta) + o.n_rad;
-  EpilogueGeom eg{n, b.m->C, b.m->N, b.m->A, b.dofs};
+  EpilogueGeom eg{n, b.m->n_hull, b.m->C, b.m->N, b.m->A, b.dofs};
   double2* phi = b.X;
   if (!o.direct) {
     zgemm_nn_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work);
@@ -825,6 +826,7 @@ int mh_mesh_create(mh_context* ctx, int64_t n, const double* vertices, const dou
   mh_mesh* m = new mh_mesh();
   m->ctx = ctx;
   m->n = n;
+  m->n_hull = n;
   const size_t nb = (size_t)n * sizeof(double);
   // one allocation: V | C | N | A | R | P
   char* base = nullptr;
@@ -871,6 +873,29 @@ int mh_mesh_destroy(mh_mesh* m) {
 }
 
 int64_t mh_mesh_panels(const mh_mesh* m) { return m ? m->n : -1; }
+
+int mh_mesh_set_lid(mh_mesh* m, int64_t n_hull) {
+  if (!m) return MH_ERR_ARG;
+  mh_context* ctx = m->ctx;
+  if (n_hull < 1 || n_hull > m->n)
+    return fail(ctx, MH_ERR_ARG, "n_hull must be in 1..%lld (got %lld)", (long long)m->n, (long long)n_hull);
+  if (n_hull < m->n) {
+    // Lid panels at the free surface meet the vv = 0 singularity of the wave terms at their
+    // self pairs (wu.jl:21-24: dd = 0; the exact term's E1(0)); the reference's lids sit below it.
+    MH_TRY(set_device(ctx));
+    const int64_t nl = m->n - n_hull;
+    std::vector<double> c((size_t)(3 * nl));
+    MH_CUDA(ctx, cudaMemcpyAsync(c.data(), m->C + 3 * n_hull, sizeof(double) * 3 * nl, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    MH_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < nl; ++i)
+      if (!(c[3 * i + 2] < -1e-8))
+        return fail(ctx, MH_ERR_ARG, "lid panel %lld has centre z = %g; a lid must lie below the free surface",
+                    (long long)(n_hull + i), c[3 * i + 2]);
+  }
+  m->n_hull = n_hull;
+  return MH_OK;
+}
 
 int mh_assemble_matrices(mh_context* ctx, mh_mesh* m, double k, uint32_t gfs, int direct, int include_identity,
                          const double* fixed_normal, double* S, double* D, int mem) {
@@ -1081,7 +1106,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
   MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(n_omega * std::max<int64_t>(n_inf, 1) * nrhs), &F));
   MH_TRY(ws_get_t(ctx, kSlotFK, (size_t)(n_omega * std::max<int64_t>(n_inf, 1) * std::max<int64_t>(n_beta, 1)), &FK));
 
-  EpilogueGeom eg{n, m->C, m->N, m->A, dofs_d};
+  EpilogueGeom eg{n, m->n_hull, m->C, m->N, m->A, dofs_d};
   AssemblyParams p = make_params(ctx, m, gfs, direct, 1, nullptr);
   MH_TRY(prepare_surrogate(ctx, p, chunk));
 
@@ -1469,6 +1494,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
   if (n_obj <= 0 || n_obj > 4 || !obj_idx) return fail(ctx, MH_ERR_ARG, "objective needs 1..4 dofs");
+  if (m->n_hull != m->n) return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint does not cover meshes with a lid");
   if (!dofs || n_dofs <= 0) return fail(ctx, MH_ERR_ARG, "dof fields required");
   const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU;
   if (gfs == 0 || (gfs & ~allowed))
@@ -1561,7 +1587,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   const double* om_d = small;
   const double* ks_d = small + n_omega;
   const int32_t* obj_d = (const int32_t*)(small + 2 * n_omega);
-  EpilogueGeom eg{n, m->C, m->N, m->A, dofs_d};
+  EpilogueGeom eg{n, m->n_hull, m->C, m->N, m->A, dofs_d};
   for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
     const int64_t nw = std::min<int64_t>(chunk, n_omega - w0);
     BatchDesc d{n, nw, (int64_t)nn};

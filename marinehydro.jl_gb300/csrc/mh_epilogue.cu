@@ -6,6 +6,9 @@
 // Forces: F = sum_i p_i * -(dof_i . n_i) * a_i with p = i rho omega phi
 //   (solve.jl:183-191, waves.jl:154-178); Froude-Krylov with the Airy pressure
 //   (waves.jl:259-264, 294-303).
+// Lid panels (index >= n_hull, irregular-frequency removal): the hull boundary
+//   conditions are padded with zeros there and only hull pressures enter the
+//   forces (solve.jl:2-10 _pad_hull_bc, :47-55 pressure[hull_mask]).
 #include <cuda_runtime.h>
 
 #include "mh_internal.cuh"
@@ -22,6 +25,10 @@ __global__ void build_rhs_kernel(EpilogueGeom g, const double* __restrict__ omeg
   const int col = blockIdx.y;
   const int w = blockIdx.z;
   if (i >= n) return;
+  if (i >= g.n_hull) {
+    B[w * bstride + col * n + i] = make_double2(0.0, 0.0);
+    return;
+  }
   const double omega = omegas[w];
   const double nx = g.N[3 * i], ny = g.N[3 * i + 1], nz = g.N[3 * i + 2];
   double2 v;
@@ -57,6 +64,7 @@ __global__ void __launch_bounds__(256) force_kernel(EpilogueGeom g, const double
                                                     int n_beta, const double* __restrict__ betas,
                                                     double2* __restrict__ F, double2* __restrict__ FK) {
   const int64_t n = g.n;
+  const int64_t nh = g.n_hull;
   const int d = blockIdx.x;
   const int col = blockIdx.y;  // 0..nrhs-1 pressure columns, then n_beta Froude-Krylov columns
   const int w = blockIdx.z;
@@ -67,7 +75,7 @@ __global__ void __launch_bounds__(256) force_kernel(EpilogueGeom g, const double
   if (col < nrhs) {
     const double2* phi = Phi + w * pstride + (int64_t)col * n;
     const double s = rho * omega;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = threadIdx.x; i < nh; i += blockDim.x) {
       double disp = g.N[3 * i] * dof[3 * i] + g.N[3 * i + 1] * dof[3 * i + 1] + g.N[3 * i + 2] * dof[3 * i + 2];
       double2 p = make_double2(-s * phi[i].y, s * phi[i].x);
       double f = -disp * g.A[i];
@@ -78,7 +86,7 @@ __global__ void __launch_bounds__(256) force_kernel(EpilogueGeom g, const double
     const double beta = betas[col - nrhs];
     double sb, cb;
     sincos(beta, &sb, &cb);
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = threadIdx.x; i < nh; i += blockDim.x) {
       double disp = g.N[3 * i] * dof[3 * i] + g.N[3 * i + 1] * dof[3 * i + 1] + g.N[3 * i + 2] * dof[3 * i + 2];
       const double cx = g.C[3 * i], cy = g.C[3 * i + 1], cz = g.C[3 * i + 2];
       const double wbar = cx * cb + cy * sb;

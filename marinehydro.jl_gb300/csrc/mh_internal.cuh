@@ -174,6 +174,7 @@ void inf_norms_batched(cudaStream_t st, LaunchCounter lc, int64_t n, int64_t nco
 // epilogue (mh_epilogue.cu)
 struct EpilogueGeom {
   int64_t n;
+  int64_t n_hull;    // panels n_hull..n-1 form a lid: zero boundary condition, no pressure in the forces
   const double* C;   // centers n x 3
   const double* N;   // normals n x 3
   const double* A;   // areas

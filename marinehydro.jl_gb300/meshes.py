@@ -65,7 +65,7 @@ class StaticArraysMesh:
 
         h = self._handles.get(id(ctx))
         if h is None:
-            h = DeviceMesh(ctx, self)
+            h = DeviceMesh(ctx, self, getattr(self, "n_hull", None))
             self._handles[id(ctx)] = h
         return h
 
@@ -227,6 +227,29 @@ def vertical_cylinder_mesh(radius=5.0, draft=10.0, n_theta=40, n_z=40, n_r=10, c
     brows.append([len(verts)])
     verts.append((cx, cy, -draft))
     quads += _ring_strip(brows)
+    return _assemble(verts, quads)
+
+
+def disc_lid_mesh(radius=5.0, z=-0.5, n_theta=40, n_r=10, center=(0.0, 0.0), normal_up=True) -> StaticArraysMesh:
+    """Horizontal disc at height z (below the free surface) for the lid of a vertical
+    cylinder's irregular-frequency removal: an n_r-ring polar grid with an n_theta-triangle
+    centre fan, normals +z (normal_up) or -z."""
+    cx, cy = center
+    verts = []
+    rows = []
+    for m in range(n_r):
+        rr = radius * (n_r - m) / n_r
+        row = []
+        for q in range(n_theta):
+            th = q * 2 * np.pi / n_theta
+            row.append(len(verts))
+            verts.append((cx + rr * np.cos(th), cy + rr * np.sin(th), z))
+        rows.append(row)
+    rows.append([len(verts)])
+    verts.append((cx, cy, z))
+    quads = _ring_strip(rows)  # rim inwards, counter-clockwise from above: normals -z
+    if normal_up:
+        quads = [(a, c, b, b) if c == d else (a, d, c, b) for a, b, c, d in quads]
     return _assemble(verts, quads)
 
 

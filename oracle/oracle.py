@@ -307,26 +307,39 @@ def integrate_dof_pressure(normals, areas, dof_field, pressure):
     return np.sum(np.asarray(pressure) * -disp * np.asarray(areas))
 
 
+def pad_hull_bc(bc_on_hull, n_total):
+    """_pad_hull_bc (solve.jl:2-10): hull values first, zeros on the lid panels after them."""
+    v = np.asarray(bc_on_hull, dtype=np.complex128)
+    out = np.zeros((n_total,) + v.shape[1:], dtype=np.complex128)
+    out[:v.shape[0]] = v
+    return out
+
+
 def hydro_one_frequency(mesh, dofs, omega, rho=1000.0, g=9.81, gfs=DEFAULT_WU, direct=True,
-                        radiating=None, influenced=None, betas=(), lapack=False, nthreads=0):
+                        radiating=None, influenced=None, betas=(), lapack=False, nthreads=0, lid_mesh=None):
     """_hydro_one_frequency (problems_and_results.jl:472-478) for one omega.
 
-    ``dofs`` maps dof name -> (n, 3) field.  Returns (A [n_inf, n_rad], B, Fd [n_inf, n_beta],
-    Fk, Fe) with the reference's per-problem arithmetic; S and D are assembled once (the
-    reference re-assembles them for each problem: identical matrices).
+    ``dofs`` maps dof name -> (n, 3) field on the hull.  Returns (A [n_inf, n_rad], B,
+    Fd [n_inf, n_beta], Fk, Fe) with the reference's per-problem arithmetic; S and D are
+    assembled once (the reference re-assembles them for each problem: identical matrices).
+    With ``lid_mesh`` the matrices cover hull + lid (``_mesh_including_lid``, solve.jl:22-28),
+    the boundary conditions are padded with zeros on the lid (solve.jl:2-10) and only the
+    hull pressures are integrated (solve.jl:47-55).
     """
     names = list(dofs.keys())
     radiating = names if radiating is None else list(radiating)
     influenced = names if influenced is None else list(influenced)
     k = omega * omega / g
-    S, D = assemble_matrices(mesh, k, gfs=gfs, direct=direct, nthreads=nthreads)
+    nh = mesh.nfaces
+    full = mesh if lid_mesh is None else _combine(mesh, lid_mesh)
+    S, D = assemble_matrices(full, k, gfs=gfs, direct=direct, nthreads=nthreads)
     rhs = [radiation_bc(mesh.normals, dofs[d], omega) for d in radiating]
     rhs += [airy_bc(mesh.centers, mesh.normals, omega, k, b, g) for b in betas]
     if not rhs:
         return (np.zeros((len(influenced), 0)),) * 2 + (np.zeros((len(influenced), 0), complex),) * 3
-    B = np.stack(rhs, axis=1)
+    B = pad_hull_bc(np.stack(rhs, axis=1), full.nfaces)
     phi, _ = solve(D, S, B, direct=direct, lapack=lapack)
-    p = 1j * rho * omega * phi
+    p = (1j * rho * omega * phi)[:nh]
     F = np.array([[integrate_dof_pressure(mesh.normals, mesh.areas, dofs[d], p[:, c]) for c in range(B.shape[1])]
                   for d in influenced])
     nr = len(radiating)
@@ -338,6 +351,83 @@ def hydro_one_frequency(mesh, dofs, omega, rho=1000.0, g=9.81, gfs=DEFAULT_WU, d
                                            airy_pressure(mesh.centers, omega, k, b, rho, g)) for b in betas]
                    for d in influenced]).reshape(len(influenced), len(betas))
     return A, Bd, Fd, Fk, Fd + Fk
+
+
+def encountered_values(omega, beta, forward_speed, g=9.81):
+    """compute_encountered_values (waves.jl:136-151) -> (omega_e, k_e, beta_e)."""
+    k = omega * omega / g
+    if forward_speed == 0:
+        return omega, k, beta
+    doppler = omega - k * forward_speed * np.cos(beta)
+    oe = abs(doppler)
+    return oe, oe * oe / g, (beta if doppler >= 0 else beta + np.pi)
+
+
+def gradient_of_motion(n, dof_name):
+    """evaluate_gradient_of_motion (bodies.jl:363-374): d(dof)/dx for rigid dofs."""
+    d = np.zeros((n, 3))
+    if dof_name == "Pitch":
+        d[:, 2] = 1.0
+    elif dof_name == "Yaw":
+        d[:, 1] = -1.0
+    return d
+
+
+def forward_speed_group(mesh, dofs, omega, beta, forward_speed, radiating=(), diffraction=True, influenced=None,
+                        rho=1000.0, g=9.81, gfs=DEFAULT_WU, lid_mesh=None, lapack=True):
+    """solve(problem, IndirectBEM()) (solve.jl:35-65) for the radiation problems of
+    ``radiating`` and (optionally) the diffraction problem at one (omega, beta, U):
+    encountered frequency and wavenumber (waves.jl:136-151), radiation condition with the
+    U * n . d(dof)/dx term (waves.jl:183-199), Airy condition with the encountered heading
+    (waves.jl:243-282), indirect solve, pressure i rho omega_e phi + rho U (K sigma)
+    with K assembled for the fixed normal [1, 0, 0] (solve.jl:35-45).  Returns
+    (omega_e, [force dict per problem]) in the order radiating..., diffraction."""
+    names = list(dofs.keys())
+    influenced = names if influenced is None else list(influenced)
+    oe, ke, be = encountered_values(omega, beta, forward_speed, g)
+    k = omega * omega / g
+    n = mesh.nfaces
+    rhs = []
+    for d in radiating:
+        bc = -1j * oe * np.einsum("ij,ij->i", mesh.normals, dofs[d])
+        if forward_speed != 0:
+            bc = bc + forward_speed * np.einsum("ij,ij->i", mesh.normals, gradient_of_motion(n, d))
+        rhs.append(bc)
+    if diffraction:
+        c = np.asarray(mesh.centers)
+        wbar = c[:, 0] * np.cos(be) + c[:, 1] * np.sin(be)
+        cih = np.exp(k * c[:, 2])
+        amp = g * k / omega * np.exp(1j * k * wbar)
+        v = np.stack([amp * np.cos(beta) * cih, amp * np.sin(beta) * cih, -1j * amp * cih], axis=1)
+        rhs.append(-np.einsum("ij,ij->i", v, mesh.normals))
+    full = mesh if lid_mesh is None else _combine(mesh, lid_mesh)
+    S, D = assemble_matrices(full, ke, gfs=gfs, direct=False)
+    B = pad_hull_bc(np.stack(rhs, axis=1), full.nfaces)
+    phi, src = solve(D, S, B, direct=False, lapack=lapack)
+    p = 1j * rho * oe * phi
+    if forward_speed != 0:
+        _, K = assemble_matrices(full, ke, gfs=gfs, direct=False, fixed_normal=[1.0, 0.0, 0.0])
+        p = p + rho * forward_speed * (K @ src)
+    p = p[:n]
+    out = [{d: integrate_dof_pressure(mesh.normals, mesh.areas, dofs[d], p[:, q]) for d in influenced}
+           for q in range(B.shape[1])]
+    return oe, out
+
+
+class _Panels:
+    """Concatenated panel arrays of hull + lid (combine_meshes, meshes.jl:56-92)."""
+
+    def __init__(self, meshes):
+        self.panel_vertices = np.concatenate([np.asarray(m.panel_vertices) for m in meshes])
+        self.centers = np.concatenate([np.asarray(m.centers) for m in meshes])
+        self.normals = np.concatenate([np.asarray(m.normals) for m in meshes])
+        self.areas = np.concatenate([np.asarray(m.areas) for m in meshes])
+        self.radii = np.concatenate([np.asarray(m.radii) for m in meshes])
+        self.nfaces = len(self.areas)
+
+
+def _combine(hull, lid):
+    return _Panels([hull, lid])
 
 
 def num_threads():

@@ -73,6 +73,7 @@ def test_null_and_bad_arguments_are_rejected_without_a_gpu(libpath, mh):
     assert L.mh_assemble_matrices(None, None, ctypes.c_double(1.0), 35, 1, 1, None, None, None, 0) == 1
     assert L.mh_linsolve(None, 3, 1, None, None, None, 0, 0) == 1
     assert L.mh_mesh_panels(None) == -1
+    assert L.mh_mesh_set_lid(None, 1) == 1
 
 
 def test_kernel_sources_target_sm103a():
