@@ -442,6 +442,8 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
         sh["serial_kernel_ms"] = round(tot, 1)
         return sh
 
+    # launch shapes: the defaults first, then the autotuned table shipped for GB300
+    ctx.set_tile_table([])
     for prec in ("fp64", "mixed", "fp64_tc"):
         F = mh.DirectBEM(precision=prec)
         # first call: graph capture + instantiation + one run (untimed warm-up, also the results)
@@ -465,6 +467,19 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
     out["fp64_tc"]["max_rel_dev_vs_fp64"] = dev_tc
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["fp64_tc_over_fp64"] = out["fp64_tc"]["value"] / out["fp64"]["value"]
+    mh.load_tile_table(ctx=ctx)
+    out["tile_table"] = {"source": "marinehydro.jl_gb300/data/tile_table_gb300.json (mh_autotune on a GB300)",
+                         "entries": [list(e) for e in ctx.tile_table()]}
+    for prec in ("mixed", "fp64_tc"):
+        F = mh.DirectBEM(precision=prec)
+        res_t = mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO, g=G)
+        t, _, launches, _ = timed(lambda: mh.batch_hydrodynamic_coefficients(bodies, params, F, ctx=ctx, rho=RHO,
+                                                                             g=G), 1, 0)
+        ctx._L.mh_batch_release(ctx.handle)
+        dev_t = max(float(np.abs(a[key] - b[key]).max() / np.abs(b[key]).max())
+                    for a, b in zip(res_t, results[prec]) for key in ("added_mass", "radiation_damping"))
+        out[prec]["autotuned_table"] = {"value": units / t, "ms_per_step": 1e3 * t, "gpu_launches": launches,
+                                        "max_rel_dev_vs_default_table": dev_t}
 
     # the plain FP64 GPU path: one hydrodynamic_coefficients call per body, no graph
     F64 = mh.DirectBEM(precision="fp64")
@@ -489,7 +504,8 @@ def run_batch_variant(mh, ctx, stream, dev, torch, timed):
     out["surrogate_mixed"] = {"value": units / t, "ms_per_step": 1e3 * t, "gpu_launches": launches,
                               "kernel_time_share": shares_s,
                               "note": "Rankine + image + learned surrogate of the exact Delhommeau term (exact "
-                                      "fallback queue per body), FP32 LU + FP64 refinement, one CUDA graph"}
+                                      "fallback queue per body), FP32 LU + FP64 refinement, one CUDA graph, "
+                                      "autotuned launch-shape table"}
     # accuracy against the exact Green function (FP64 oracle arithmetic) on the 4 smallest bodies
     small = sorted(range(len(bodies)), key=lambda q: bodies[q].mesh.nfaces)[:4]
     FE = mh.DirectBEM("ExactGuevelDelhommeau", precision="fp64")

@@ -7,7 +7,7 @@ name is not a Python identifier; load it with ``load_package()`` below or
 ``importlib`` under the name ``marinehydro_gb300``.
 """
 from ._lib import (Context, MarineHydroError, default_context, load as load_library)  # noqa: F401
-from .api import (airy_bc, airy_pressure, assemble_matrices, assemble_matrix_wu, batch_hydrodynamic_coefficients,  # noqa
+from .api import (airy_bc, airy_pressure, assemble_matrices, autotune, load_tile_table, assemble_matrix_wu, batch_hydrodynamic_coefficients,  # noqa
                   calculate_radiation_forces,
                   compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
                   gpu_linsolve, hydro_gradient, hydrodynamic_coefficients, load_surrogate, set_surrogate, surrogate_wave_terms, train_surrogate, integrate_pressure, linsolve, linsolve_adjoint,

@@ -39,7 +39,7 @@ EXPORTS = (
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
-    "mh_surrogate_wave_terms", "mh_surrogate_loss_grad",
+    "mh_surrogate_wave_terms", "mh_surrogate_loss_grad", "mh_tile_table_set", "mh_tile_table_get", "mh_autotune",
 )
 
 
@@ -102,6 +102,9 @@ def load(path: str | None = None):
         L.mh_batch_hydrodynamic_coefficients.argtypes = [vp, i64, vp, vp, vp, D, D, u32, I, i64, vp, i64, vp, i64,
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
+        L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]
+        L.mh_tile_table_get.argtypes = [vp, i64, vp, vp, vp]
+        L.mh_autotune.argtypes = [vp, I, i64, vp, i64, I, vp, vp]
         L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, I, vp, vp, vp, vp, vp, vp, I]
         L.mh_surrogate_param_count.restype = I
         L.mh_surrogate_train.argtypes = [vp, i64, ctypes.c_uint64, I, I, D, vp, vp]
@@ -212,6 +215,32 @@ class Context:
         self.check(self._L.mh_surrogate_loss_grad(self._h, p.ctypes.data, x.shape[0], x.ctypes.data, y.ctypes.data,
                                                   g.ctypes.data, ctypes.byref(loss)), "mh_surrogate_loss_grad")
         return loss.value, g
+
+    def tile_table(self):
+        """The launch-shape table: list of (n_max, oz_group, bx_group, cluster_f64, cluster_f32)."""
+        n_max = np.zeros(16, dtype=np.int64)
+        ch = np.zeros((16, 4), dtype=np.int32)
+        cnt = ctypes.c_int64()
+        self.check(self._L.mh_tile_table_get(self._h, 16, n_max.ctypes.data, ch.ctypes.data, ctypes.byref(cnt)),
+                   "mh_tile_table_get")
+        return [(int(n_max[q]),) + tuple(int(x) for x in ch[q]) for q in range(cnt.value)]
+
+    def set_tile_table(self, entries):
+        """Install a launch-shape table (entries as returned by tile_table(); [] = defaults)."""
+        n_max = np.ascontiguousarray([e[0] for e in entries], dtype=np.int64)
+        ch = np.ascontiguousarray([e[1:5] for e in entries], dtype=np.int32).reshape(-1, 4)
+        self.check(self._L.mh_tile_table_set(self._h, len(entries), n_max.ctypes.data if len(entries) else None,
+                                             ch.ctypes.data if len(entries) else None), "mh_tile_table_set")
+
+    def autotune(self, precision, sizes, batch=16, reps=3):
+        """mh_autotune: time the candidate launch shapes of the batched LU for `precision`
+        at each order in `sizes` and install the fastest; returns (best ms, default ms)."""
+        sz = np.ascontiguousarray(sizes, dtype=np.int64)
+        best = np.zeros(sz.size)
+        dflt = np.zeros(sz.size)
+        self.check(self._L.mh_autotune(self._h, int(precision), sz.size, sz.ctypes.data, int(batch), int(reps),
+                                       best.ctypes.data, dflt.ctypes.data), "mh_autotune")
+        return best, dflt
 
     def probe_fma_peaks(self):
         """(fp64, fp32) FMA throughput in TFLOP/s measured on this device."""

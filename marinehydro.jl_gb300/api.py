@@ -415,6 +415,49 @@ def set_surrogate(params, ctx=None):
     _ctx(ctx).surrogate_set(params)
 
 
+TILE_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "tile_table_gb300.json")
+_TILE_FIELDS = ("n_max", "ozaki_column_tiles", "bf16x3_column_tiles", "panel_cluster_fp64", "panel_cluster_fp32")
+
+
+def autotune(sizes=(384, 768, 1536, 3072), batch=16, precisions=("fp64", "mixed", "fp64_tc"), reps=3, path=None,
+             ctx=None) -> dict:
+    """Pick the batched LU's launch shapes per matrix-order bucket by timing them on the
+    device (mh_autotune) and install them on the context.  The table is keyed by order
+    bucket (bounds at the geometric means of neighbouring `sizes`); `batch` is the number of
+    matrices factored together (the frequencies of one body).  With `path` the table is
+    written there as JSON (load it again with load_tile_table).  Returns the table and the
+    tuned and default factorization times per precision and size."""
+    c = _ctx(ctx)
+    report = {"sizes": [int(n) for n in sizes], "batch": int(batch), "ms": {}}
+    for p in precisions:
+        best, dflt = c.autotune(_prec(p), sizes, batch, reps)
+        report["ms"][p] = {"tuned": best.tolist(), "default": dflt.tolist()}
+    table = [dict(zip(_TILE_FIELDS, e)) for e in c.tile_table()]
+    for e in table:
+        if e["n_max"] >= 2 ** 62:
+            e["n_max"] = None  # the last bucket covers every larger order
+    report["table"] = table
+    if path is not None:
+        import json
+
+        with open(path, "w") as f:
+            json.dump(report, f, indent=1)
+    return report
+
+
+def load_tile_table(path=None, ctx=None) -> list:
+    """Install a tile table written by autotune (default: the shipped GB300 table,
+    data/tile_table_gb300.json); returns its entries."""
+    import json
+
+    with open(path or TILE_TABLE) as f:
+        table = json.load(f)["table"]
+    entries = [((e["n_max"] if e["n_max"] is not None else 2 ** 63 - 1),) + tuple(int(e[k]) for k in _TILE_FIELDS[1:])
+               for e in table]
+    _ctx(ctx).set_tile_table(entries)
+    return entries
+
+
 SURROGATE_PARAMS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_delhommeau.npy")
 
 

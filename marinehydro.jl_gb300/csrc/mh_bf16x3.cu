@@ -36,7 +36,8 @@ constexpr int kBxK = 32;                                 // panel width (the LU'
 constexpr int kBxTile = 128;                             // rows of an A tile = columns of a B tile
 constexpr int kBxPlane = kBxTile * kBxK * 2;             // bytes of one 128 x 32 BF16 plane
 constexpr int kBxTileBytes = 2 * kBxTerms * kBxPlane;    // 48 KB: re/im x 3 terms
-constexpr int kBxGroup = 4;                              // column tiles per CTA
+constexpr int kBxGroupMax = 8;                           // column tiles per CTA: 1..8 from the
+                                                         // launch-shape table (default 4)
 constexpr int kBxThreads = 256;                          // two threads per output row
 constexpr uint32_t kBxTmemCols = 512;                    // 2 buffers x (Re 128 + Im 128)
 constexpr uint32_t kBxWaitPolls = 1u << 26;
@@ -120,15 +121,15 @@ __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float
                                                             int64_t rest, int64_t ntile,
                                                             const unsigned char* __restrict__ tA,
                                                             const unsigned char* __restrict__ tB,
-                                                            int* __restrict__ timeout_flag) {
+                                                            int* __restrict__ timeout_flag, int group) {
   extern __shared__ __align__(1024) unsigned char bsm[];
   __shared__ __align__(8) uint64_t mbar_load[2];
   __shared__ __align__(8) uint64_t mbar_mma[2];
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
-  const int64_t ct0 = blockIdx.y * (int64_t)kBxGroup;
-  const int ntiles = (int)((ntile - ct0) < kBxGroup ? (ntile - ct0) : kBxGroup);
+  const int64_t ct0 = blockIdx.y * (int64_t)group;
+  const int ntiles = (int)((ntile - ct0) < group ? (ntile - ct0) : group);
   const int64_t n = d.n;
   unsigned char* As = bsm;
   unsigned char* Bs[2] = {bsm + kBxTileBytes, bsm + 2 * kBxTileBytes};
@@ -297,9 +298,11 @@ void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, 
   MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_cols_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, tB));
   const size_t smem = 3 * (size_t)kBxTileBytes;
   cudaFuncSetAttribute(bx3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 gg((unsigned)nt, (unsigned)((nt + kBxGroup - 1) / kBxGroup), (unsigned)d.batch);
+  int group = lc.tile(d.n).bx_group;
+  group = group < 1 ? 1 : (group > kBxGroupMax ? kBxGroupMax : group);
+  dim3 gg((unsigned)nt, (unsigned)((nt + group - 1) / group), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_bx3",
-            bx3_gemm_kernel<<<gg, kBxThreads, smem, st>>>(d, A, k, kb, rest, nt, tA, tB, timeout_flag));
+            bx3_gemm_kernel<<<gg, kBxThreads, smem, st>>>(d, A, k, kb, rest, nt, tA, tB, timeout_flag, group));
 }
 
 }  // namespace mh

@@ -47,11 +47,35 @@ __host__ __device__ inline float2 cmk(float r, float i) { return make_float2(r, 
 // Counts kernel launches and, when profiling is on, brackets each launch with a
 // pair of CUDA events attributed to a named kernel group (see mh_profile_*).
 struct Profiler;
+
+// Launch shapes of the batched LU that depend on the matrix order, chosen per order
+// bucket by mh_autotune (or set with mh_tile_table_set).  The defaults are the
+// hand-picked shapes the table starts from.
+struct TileChoice {
+  int oz_group = 4;     // 32-column tiles per CTA of the Ozaki (FP64 tensor-core) update, 1..8
+  int bx_group = 4;     // 128-column tiles per CTA of the BF16x3 (FP32) update, 1..8
+  int cluster_f64 = 8;  // largest thread-block cluster of the FP64 LU panel, 1..8
+  int cluster_f32 = 8;  // largest thread-block cluster of the FP32 LU panel, 1..8
+};
+constexpr int kMaxTileEntries = 16;
+struct TileTable {
+  int n_entries = 0;                  // 0: defaults for every order
+  int64_t n_max[kMaxTileEntries];     // ascending bucket bounds (inclusive); the last covers the rest
+  TileChoice c[kMaxTileEntries];
+  TileChoice lookup(int64_t n) const {
+    for (int q = 0; q < n_entries; ++q)
+      if (n <= n_max[q] || q == n_entries - 1) return c[q];
+    return TileChoice{};
+  }
+};
+
 struct LaunchCounter {
   int64_t* count;
   Profiler* prof;
+  const TileTable* tiles = nullptr;
   void pre(cudaStream_t st) const;
   void post(cudaStream_t st, const char* group) const;
+  TileChoice tile(int64_t n) const { return tiles ? tiles->lookup(n) : TileChoice{}; }
 };
 
 #define MH_LAUNCH(lc, st, group, ...) \
@@ -128,6 +152,10 @@ struct BatchDesc {
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
                       int32_t* ipiv, int32_t* info, void* emu_ws = nullptr, int* emu_flag = nullptr);
+// d.batch random complex matrices for timing factorizations (mh_autotune)
+template <typename T>
+void fill_random_matrices(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
+                          uint64_t seed);
 // FP64 trailing update A22 -= L21 U12 of panel step k on the BF16 tensor cores (mh_ozaki.cu);
 // emu_ws: ozaki_workspace_bytes(n, batch) bytes; *timeout_flag set if a completion wait gave up
 size_t ozaki_workspace_bytes(int64_t n, int64_t batch);

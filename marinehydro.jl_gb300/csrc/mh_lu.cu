@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "mh_internal.cuh"
@@ -973,10 +974,11 @@ void convert_with_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, c
 // CTAs per cluster for a panel of m rows in a batch of `batch` matrices: enough to hold
 // the panel in shared memory, and more (up to 8) while all `batch` clusters still fit on
 // the GPU at once (clusters are placed within one GPC, so this is taken from the
-// occupancy query, not from the SM count); 0 when the panel does not fit the largest
-// cluster the GPU can schedule (panel_kernel then runs).
+// occupancy query, not from the SM count), at most `cap` beyond the minimum (the
+// launch-shape table's cluster bound); 0 when the panel does not fit the largest cluster
+// the GPU can schedule (panel_kernel then runs).
 template <typename T>
-int panel_cluster_size(int64_t m, int64_t batch) {
+int panel_cluster_size(int64_t m, int64_t batch, int cap_ctas) {
   using C = typename cplx_t<T>::type;
   constexpr int cap = PanelRows<T>::value;
   struct Table { int resident[17]; };
@@ -1011,7 +1013,7 @@ int panel_cluster_size(int64_t m, int64_t batch) {
   if (need > 16 || tab.resident[need] <= 0) return 0;
   const int64_t lim = m / kNB > 1 ? m / kNB : 1;  // keeps every chunk >= 32 rows (CTA 0 holds the diagonal block)
   int64_t p = need;
-  for (int64_t q = need + 1; q <= 8 && q <= lim; ++q)
+  for (int64_t q = need + 1; q <= 8 && q <= lim && q <= cap_ctas; ++q)
     if (tab.resident[q] >= batch) p = q;
   return (int)p;
 }
@@ -1029,7 +1031,8 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
   }
   for (int64_t k = 0; k < n; k += kNB) {
     const int64_t kb = (k + kNB < n) ? kNB : n - k;
-    const int P = panel_cluster_size<T>(n - k, d.batch);
+    const int P = panel_cluster_size<T>(n - k, d.batch, sizeof(T) == 8 ? lc.tile(n).cluster_f64
+                                                                       : lc.tile(n).cluster_f32);
     if (P > 0) {
       const int chunk = (int)((n - k + P - 1) / P);
       cudaLaunchConfig_t cfg = {};
@@ -1170,6 +1173,34 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   }
   lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
 }
+
+// Random complex matrices (entries uniform in [-1, 1] x [-1, 1] from a counter-based hash)
+// on which the autotuner times factorizations; every column needs partial pivoting.
+template <typename T>
+__global__ void fill_random_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ A, uint64_t seed) {
+  const int64_t count = d.n * d.n;
+  const int64_t b = blockIdx.y;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(b * count + q + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const T re = (T)((double)(z >> 40) * (2.0 / 16777216.0) - 1.0);
+    const T im = (T)((double)(z & 0xFFFFFFull) * (2.0 / 16777216.0) - 1.0);
+    A[b * d.stride + q] = cmk(re, im);
+  }
+}
+
+template <typename T>
+void fill_random_matrices(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,
+                          uint64_t seed) {
+  if (d.n <= 0 || d.batch <= 0) return;
+  const int64_t blocks = std::min<int64_t>((d.n * d.n + 255) / 256, 1216);
+  MH_LAUNCH(lc, st, "fill_random",
+            fill_random_kernel<T><<<dim3((unsigned)blocks, (unsigned)d.batch), 256, 0, st>>>(d, A, seed));
+}
+template void fill_random_matrices<double>(cudaStream_t, LaunchCounter, const BatchDesc&, double2*, uint64_t);
+template void fill_random_matrices<float>(cudaStream_t, LaunchCounter, const BatchDesc&, float2*, uint64_t);
 
 template int lu_factor_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, double2*, int32_t*, int32_t*,
                                        void*, int*);

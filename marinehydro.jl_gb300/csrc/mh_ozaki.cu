@@ -131,11 +131,12 @@ __global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, cons
 // 2^s as a double, s in the normal range
 __device__ __forceinline__ double pow2(int s) { return __longlong_as_double((long long)(s + 1023) << 52); }
 
-constexpr int kOzGroup = 4;    // column tiles per CTA (the A tiles are loaded once for all of them)
+constexpr int kOzGroupMax = 8; // column tiles per CTA (the A tiles are loaded once for all of them):
+                               // 1..8, from the launch-shape table (default 4)
 constexpr int kOzThreads = 256; // two threads per output row: warps w and w + 4 share TMEM lanes
                                 // 32 (w % 4) .. and take one half of the 32 columns each
 
-// One CTA per (row tile, group of kOzGroup column tiles, matrix).  The A digit tiles and the
+// One CTA per (row tile, group of `group` column tiles, matrix).  The A digit tiles and the
 // first B tile arrive by TMA bulk copies on one mbarrier; the B tiles are double-buffered,
 // the next one prefetched while the current tile's products and epilogue run.
 __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
@@ -144,15 +145,15 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
                                                               const unsigned char* __restrict__ digB,
                                                               const int* __restrict__ rowexp,
                                                               const int* __restrict__ colexp,
-                                                              int* __restrict__ timeout_flag) {
+                                                              int* __restrict__ timeout_flag, int group) {
   extern __shared__ __align__(1024) unsigned char osm[];
   __shared__ __align__(8) uint64_t mbar_load[2];
   __shared__ __align__(8) uint64_t mbar_mma;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
-  const int64_t ct0 = blockIdx.y * (int64_t)kOzGroup;
-  const int ntile = (int)((nct - ct0) < kOzGroup ? (nct - ct0) : kOzGroup);
+  const int64_t ct0 = blockIdx.y * (int64_t)group;
+  const int ntile = (int)((nct - ct0) < group ? (nct - ct0) : group);
   const int64_t n = d.n;
   unsigned char* As = osm;
   unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
@@ -321,10 +322,12 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 256, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
   const size_t smem = kOzABytes + 2 * kOzBBytes;
   cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 gg((unsigned)nrt, (unsigned)((nct + kOzGroup - 1) / kOzGroup), (unsigned)d.batch);
+  int group = lc.tile(d.n).oz_group;
+  group = group < 1 ? 1 : (group > kOzGroupMax ? kOzGroupMax : group);
+  dim3 gg((unsigned)nrt, (unsigned)((nct + group - 1) / group), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_ozaki",
             ozaki_gemm_kernel<<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp,
-                                                          timeout_flag));
+                                                          timeout_flag, group));
 }
 
 }  // namespace mh
