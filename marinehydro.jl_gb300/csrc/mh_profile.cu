@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "mh_internal.cuh"
+#include "mh_tc.cuh"
 
 namespace mh {
 
@@ -154,7 +155,39 @@ double run_probe(cudaStream_t st, int iters, T* scratch) {
   return best;
 }
 
+// The recovery path of every bounded completion wait in the tensor-core kernels, run
+// on purpose: the CTA (one warp) holds tensor memory, waits on an mbarrier that nothing
+// arrives at for `polls` polls, records the timeout, frees the tensor memory and returns.
+__global__ void __launch_bounds__(32) wait_timeout_probe_kernel(uint32_t polls, int* __restrict__ flag) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  tc::tmem_alloc(&tmem_base, 32);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const bool ok = tc::mbar_wait(&bar, 0, polls);
+  if (!ok && threadIdx.x == 0) atomicExch(flag, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::tmem_dealloc(tmem_base, 32);
+}
+
 }  // namespace
+
+int probe_wait_timeout(cudaStream_t st, uint32_t polls, int* timed_out) {
+  int* flag = nullptr;
+  if (cudaMallocAsync((void**)&flag, sizeof(int), st) != cudaSuccess) return MH_ERR_NOMEM;
+  cudaMemsetAsync(flag, 0, sizeof(int), st);
+  wait_timeout_probe_kernel<<<1, 32, 0, st>>>(polls, flag);
+  cudaError_t e = cudaGetLastError();
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(flag, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  *timed_out = h;
+  return e == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
 
 int probe_fma_peaks(cudaStream_t st, double* fp64_tflops, double* fp32_tflops) {
   double* scratch = nullptr;
