@@ -106,7 +106,8 @@ int64_t mh_workspace_bytes(const mh_context* ctx);
 /* ---- mesh --------------------------------------------------------------- */
 /* Replaces StaticArraysMesh(...) + element(mesh, j) (meshes.jl:42-51, 255-277):
    uploads one body's panels and precomputes the per-panel Birk frame
-   (birk_panel_geometry, rankine_vectorized.jl:129-137). */
+   (birk_panel_geometry, rankine_vectorized.jl:129-137).  Host arrays holding a NaN or
+   an infinity are rejected with MH_ERR_ARG. */
 int mh_mesh_create(mh_context* ctx, int64_t n_panels, const double* vertices, const double* centers,
                    const double* normals, const double* areas, const double* radii, int mem, mh_mesh** out);
 int mh_mesh_destroy(mh_mesh* mesh);
@@ -193,6 +194,24 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* mesh, int64_t n_omega
                                  const int32_t* inf_idx, int64_t n_beta, const double* betas, int precision,
                                  double* added_mass, double* radiation_damping, double* diffraction_force,
                                  double* froude_krylov_force, double* excitation_force, int mem);
+
+/* Replaces ForwardDiff.derivative(ω -> hydrodynamic_coefficients(body, (wave_frequencies = ω, …)), ω)
+   (test/outputs_differentiation.jl:39-150, solve_problem_differentiation.jl:89-110,
+   diffraction_differentiation.jl:63-78): the coefficients of mh_hydrodynamic_coefficients
+   (same arguments and layouts, FP64) and their derivatives with respect to ω, k = ω²/g
+   included.  Forward mode on the device: dS/dk, dD/dk of the Wu term from one dual
+   direction through the same fits, the boundary conditions' ω-derivatives, and
+   dφ = D⁻¹(dS b + S db − dD φ) (direct; indirect: dσ = D⁻¹(db − dD σ), dφ = dS σ + S dσ)
+   with the LU factors of D reused.  Green functions: the Rankine kinds and MH_GF_WU
+   (others: MH_ERR_UNSUPPORTED).  Derivative outputs may be NULL. */
+int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas,
+                                  double rho, double g, uint32_t gfs, int direct, int64_t n_dofs,
+                                  const double* dofs, int64_t n_rad, const int32_t* rad_idx, int64_t n_inf,
+                                  const int32_t* inf_idx, int64_t n_beta, const double* betas,
+                                  double* added_mass, double* radiation_damping, double* diffraction_force,
+                                  double* froude_krylov_force, double* excitation_force, double* d_added_mass,
+                                  double* d_radiation_damping, double* d_diffraction_force,
+                                  double* d_froude_krylov_force, double* d_excitation_force, int mem);
 
 /* Replaces a loop of hydrodynamic_coefficients over many bodies
    (problems_and_results.jl:464-495): body b is meshes[b] with n_omega[b]
@@ -340,6 +359,11 @@ int mh_profile_read(mh_context* ctx, int64_t capacity, char* names, double* tota
 /* Measured FP64 / FP32 fused-multiply-add throughput of the device (TFLOP/s),
    the denominators of the FP64-bound kernels' roofline. */
 int mh_probe_fma_peaks(mh_context* ctx, double* fp64_tflops, double* fp32_tflops);
+/* No counterpart in the reference: runs the recovery path of the bounded completion
+   waits of the tensor-core kernels on purpose.  One warp holds tensor memory, waits on
+   an mbarrier that nothing arrives at for `polls` (1..2^20) polls, frees the tensor
+   memory and returns; the call reports MH_ERR_TIMEOUT and the context stays usable. */
+int mh_probe_wait_timeout(mh_context* ctx, uint32_t polls);
 
 #ifdef __cplusplus
 }

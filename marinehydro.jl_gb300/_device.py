@@ -169,6 +169,27 @@ def hydro_sweep(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, direct, dofs, rad_i
     return A, B, Fd, Fk, Fe
 
 
+def hydro_frequency_derivative(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, direct, dofs, rad_idx, inf_idx, betas):
+    """mh_hydro_frequency_derivative with host buffers; returns the five arrays and their
+    omega-derivatives (ten arrays, layouts of hydro_sweep)."""
+    om = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
+    be = np.ascontiguousarray(np.asarray(betas, dtype=np.float64).ravel())
+    dofs = np.ascontiguousarray(np.asarray(dofs, dtype=np.float64))
+    ri = np.ascontiguousarray(np.asarray(rad_idx, dtype=np.int32).ravel())
+    ii = np.ascontiguousarray(np.asarray(inf_idx, dtype=np.int32).ravel())
+    nw, nb, nr, ni = om.size, be.size, ri.size, ii.size
+    nd = dofs.shape[0] if dofs.size else 0
+    out = []
+    for _ in range(2):
+        A = np.empty((ni, nr, nw), dtype=np.float64, order="F")
+        out += [A, np.empty_like(A)] + [np.empty((ni, nw, nb), dtype=np.complex128, order="F") for _ in range(3)]
+    p = lambda a: a.ctypes.data if a.size else None
+    ctx.check(ctx._L.mh_hydro_frequency_derivative(
+        ctx.handle, dmesh.handle, nw, om.ctypes.data, float(rho), float(g), int(gfs), int(bool(direct)), nd,
+        p(dofs), nr, p(ri), ni, p(ii), nb, p(be), *[p(a) for a in out], MH_MEM_HOST), "hydro_frequency_derivative")
+    return out
+
+
 def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_body, rad_idx, inf_idx, betas,
                 precision=_lib.MH_PREC_FP64, n_streams=0):
     """mh_batch_hydrodynamic_coefficients with host buffers; returns per-body lists of the five arrays."""

@@ -40,6 +40,7 @@ EXPORTS = (
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
     "mh_surrogate_wave_terms", "mh_surrogate_loss_grad", "mh_tile_table_set", "mh_tile_table_get", "mh_autotune",
+    "mh_probe_wait_timeout", "mh_hydro_frequency_derivative",
 )
 
 
@@ -102,6 +103,9 @@ def load(path: str | None = None):
         L.mh_batch_hydrodynamic_coefficients.argtypes = [vp, i64, vp, vp, vp, D, D, u32, I, i64, vp, i64, vp, i64,
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
+        L.mh_probe_wait_timeout.argtypes = [vp, ctypes.c_uint32]
+        L.mh_hydro_frequency_derivative.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64,
+                                                    vp] + [vp] * 10 + [I]
         L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]
         L.mh_tile_table_get.argtypes = [vp, i64, vp, vp, vp]
         L.mh_autotune.argtypes = [vp, I, i64, vp, i64, I, vp, vp]

@@ -298,6 +298,42 @@ def hydrodynamic_coefficients(body: FloatingBody, parameters: dict, formulation:
     }
 
 
+def hydrodynamic_coefficients_derivative(body: FloatingBody, parameters: dict,
+                                         formulation: BEMFormulation | None = None, ctx=None, rho=None,
+                                         g=None) -> dict:
+    """hydrodynamic_coefficients and its derivative with respect to the wave frequency,
+    what the reference obtains with ForwardDiff.derivative over wave_frequencies
+    (test/outputs_differentiation.jl:39-150, diffraction_differentiation.jl:63-78).
+
+    Returns the keys of hydrodynamic_coefficients (zero forward speed, shapes with n_U = 1)
+    plus "d_added_mass", "d_radiation_damping", "d_diffraction_force",
+    "d_Froude_Krylov_force", "d_excitation_force" (d/d omega, same shapes).  FP64, the
+    Rankine kinds with GFWu, direct or indirect, lids included (mh_hydro_frequency_derivative).
+    """
+    f = formulation or DirectBEM()
+    if any(u != 0 for u in parameters.get("forward_speeds", [0.0])):
+        raise ValueError("the frequency derivative covers zero forward speed")
+    c = _ctx(ctx)
+    oms = np.atleast_1d(np.asarray(parameters["wave_frequencies"], dtype=float))
+    names = list(body.dofs)
+    inf = list(parameters.get("influenced_dofs", names))
+    rad = list(parameters.get("radiating_dofs", []))
+    betas = list(parameters.get("wave_directions", []))
+    rho = parameters.get("rho", SETTINGS["rho"]) if rho is None else rho
+    g = parameters.get("g", SETTINGS["g"]) if g is None else g
+    idx = {n: i for i, n in enumerate(names)}
+    mesh, _ = body.mesh_including_lid()
+    arrs = _device.hydro_frequency_derivative(c, mesh.device_mesh(c), oms, rho, g, gf_flags(f.greens), is_direct(f),
+                                              body.padded_dof_array(names), [idx[d] for d in rad],
+                                              [idx[d] for d in inf], betas)
+    keys = ("added_mass", "radiation_damping", "diffraction_force", "Froude_Krylov_force", "excitation_force")
+    out = {}
+    for q, key in enumerate(keys + tuple("d_" + k for k in keys)):
+        radiation = key.endswith(("added_mass", "radiation_damping"))
+        out[key] = arrs[q][..., None] if (rad if radiation else betas) else np.zeros(0)
+    return out
+
+
 def _zero_speed_sweep(c, body, f, oms, rho, g, names, rad, inf, betas):
     """The zero-speed frequency sweep on the device (mh_hydrodynamic_coefficients)."""
     idx = {n: i for i, n in enumerate(names)}

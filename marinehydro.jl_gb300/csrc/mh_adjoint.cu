@@ -547,6 +547,68 @@ __global__ void __launch_bounds__(kRows) wave_adjoint_kernel(AssemblyParams p, d
   }
 }
 
+// dS_W/dk and dD_W/dk of the Wu term (the S, D entries of _assemble_wu_centers_loop,
+// matrix_assembly.jl:343-369, differentiated in the wavenumber): hh = k dis and
+// vv = k (z_i + z_j) carry their k-derivatives dis and z_i + z_j as one dual direction
+// through the same fits, and k itself is the seeded variable of the prefactors.  One
+// thread per ordered pair; the Rankine part does not depend on k.
+template <bool DIRECT>
+__global__ void __launch_bounds__(kRows) wave_dk_kernel(AssemblyParams p, const double* __restrict__ ks,
+                                                        double2* __restrict__ dS, double2* __restrict__ dD) {
+  __shared__ PanelRec sp[kCols];
+  const int64_t n = p.n;
+  const int64_t i0 = blockIdx.x * (int64_t)kRows;
+  const int64_t j0 = blockIdx.y * (int64_t)kCols;
+  const int64_t i = i0 + threadIdx.x;
+  const int ncol = (int)((n - j0) < kCols ? (n - j0) : kCols);
+  {
+    const double2* src = reinterpret_cast<const double2*>(p.P + j0);
+    double2* dst = reinterpret_cast<double2*>(sp);
+    for (int q = threadIdx.x; q < ncol * 16; q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  if (i >= n) return;
+  const double k = ks[0];
+  double ci[3], ni[3];
+  for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
+  for (int jj = 0; jj < ncol; ++jj) {
+    const int64_t j = j0 + jj;
+    const PanelRec& Pj = sp[jj];
+    // _wu_reduced_hh_vv (wu.jl:7-18)
+    const double d2 = (ci[0] - Pj.c[0]) * (ci[0] - Pj.c[0]) + (ci[1] - Pj.c[1]) * (ci[1] - Pj.c[1]);
+    const double purt = 1e-18;
+    const double dis = (d2 == 0) ? sqrt(d2 + purt * purt) - purt : sqrt(d2);
+    const double zz = ci[2] + Pj.c[2];
+    Dn<1> H(k * dis), V(k * zz), K = Dn<1>::var(k, 0);
+    H.d[0] = dis;
+    V.d[0] = zz;
+    CR<Dn<1>> GF, Gh, Gv;
+    wu_terms_t(H, V, GF, Gh, Gv);
+    const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+    const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+    // _wu_sd (wu.jl:112-127) on duals: s = k GF a, g = k (k^2/hh dx Gh, k^2/hh dy Gh, k Gv)
+    Dn<1> dr1(0.0), dr2(0.0);
+    if (fabs(H.v) > 1e-6) {
+      const Dn<1> f = K * K / H;
+      dr1 = f * dx1;
+      dr2 = f * dx2;
+    }
+    const Dn<1> sr = K * GF.x, si = K * GF.y;
+    const Dn<1> g0r = K * (dr1 * Gh.x), g0i = K * (dr1 * Gh.y);
+    const Dn<1> g1r = K * (dr2 * Gh.x), g1i = K * (dr2 * Gh.y);
+    const Dn<1> g2r = K * (K * Gv.x), g2i = K * (K * Gv.y);
+    double nv[3];
+    if (p.has_fixed) { nv[0] = p.fixed[0]; nv[1] = p.fixed[1]; nv[2] = p.fixed[2]; }
+    else if (DIRECT) { nv[0] = Pj.n[0]; nv[1] = Pj.n[1]; nv[2] = Pj.n[2]; }
+    else { nv[0] = ni[0]; nv[1] = ni[1]; nv[2] = ni[2]; }
+    const double a = kMinusInv4Pi * Pj.area;
+    const int64_t idx = i + j * n;
+    dS[idx] = make_double2(a * sr.d[0], a * si.d[0]);
+    dD[idx] = make_double2(a * (nv[0] * g0r.d[0] + nv[1] * g1r.d[0] + nv[2] * g2r.d[0]),
+                           a * (nv[0] * g0i.d[0] + nv[1] * g1i.d[0] + nv[2] * g2i.d[0]));
+  }
+}
+
 // RS += Re(c sum_h lam_h b_h^T), RD += Re(-c sum_h lam_h phi_h^T)
 __global__ void weights_accumulate_kernel(int64_t n, WaveWeights w, double* __restrict__ RS, double* __restrict__ RD) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -654,6 +716,15 @@ void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const do
   dim3 grid((unsigned)((n + 127) / 128), (unsigned)nh);
   MH_LAUNCH(lc, st, "adjoint_force_weights",
             force_weights_kernel<<<grid, 128, 0, st>>>(n, N, A, dofs, obj, nh, omega, rho, wconj));
+}
+
+void launch_wave_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* k_dev, double2* dS,
+                    double2* dD) {
+  dim3 grid((unsigned)((p.n + kRows - 1) / kRows), (unsigned)((p.n + kCols - 1) / kCols));
+  if (p.direct)
+    MH_LAUNCH(lc, st, "wave_dk", wave_dk_kernel<true><<<grid, kRows, 0, st>>>(p, k_dev, dS, dD));
+  else
+    MH_LAUNCH(lc, st, "wave_dk", wave_dk_kernel<false><<<grid, kRows, 0, st>>>(p, k_dev, dS, dD));
 }
 
 void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x) {

@@ -855,6 +855,15 @@ int mh_mesh_create(mh_context* ctx, int64_t n, const double* vertices, const dou
   if (!vertices || !centers || !normals || !areas || !radii)
     return fail(ctx, MH_ERR_ARG, "mesh arrays must not be NULL");
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (mem == MH_MEM_HOST) {
+    const double* arrs[5] = {vertices, centers, normals, areas, radii};
+    const int64_t lens[5] = {12 * n, 3 * n, 3 * n, n, n};
+    const char* names[5] = {"vertices", "centers", "normals", "areas", "radii"};
+    for (int a = 0; a < 5; ++a)
+      for (int64_t q = 0; q < lens[a]; ++q)
+        if (!std::isfinite(arrs[a][q]))
+          return fail(ctx, MH_ERR_ARG, "mesh %s[%lld] is not finite", names[a], (long long)q);
+  }
   MH_TRY(set_device(ctx));
   mh_mesh* m = new mh_mesh();
   m->ctx = ctx;
@@ -1228,6 +1237,217 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
   return sync(ctx, "sweep outputs");
 }
 
+int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho,
+                                  double g, uint32_t gfs, int direct, int64_t n_dofs, const double* dofs,
+                                  int64_t n_rad, const int32_t* rad_idx, int64_t n_inf, const int32_t* inf_idx,
+                                  int64_t n_beta, const double* betas, double* added_mass, double* radiation_damping,
+                                  double* diffraction_force, double* froude_krylov_force, double* excitation_force,
+                                  double* d_added_mass, double* d_radiation_damping, double* d_diffraction_force,
+                                  double* d_froude_krylov_force, double* d_excitation_force, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
+  if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
+  if (n_rad < 0 || n_inf < 0 || n_beta < 0 || n_dofs < 0) return fail(ctx, MH_ERR_ARG, "negative counts");
+  if (n_rad + n_beta == 0) return fail(ctx, MH_ERR_ARG, "nothing to solve: no radiating dof and no wave direction");
+  if ((n_rad > 0 || n_inf > 0) && (!dofs || n_dofs <= 0)) return fail(ctx, MH_ERR_ARG, "dof fields required");
+  MH_TRY(check_gfs(ctx, gfs));
+  if (gfs & (MH_GF_EXACT_DELHOMMEAU | MH_GF_SURROGATE))
+    return fail(ctx, MH_ERR_UNSUPPORTED, "the frequency derivative covers the Rankine kinds and GFWu (got 0x%x)", gfs);
+  if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
+  for (int64_t w = 0; w < n_omega; ++w)
+    if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive (omega[%lld]=%g)", (long long)w, omegas[w]);
+  for (int64_t q = 0; q < n_rad; ++q)
+    if (rad_idx[q] < 0 || rad_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "radiating dof index out of range");
+  for (int64_t q = 0; q < n_inf; ++q)
+    if (inf_idx[q] < 0 || inf_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "influenced dof index out of range");
+  if (m->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "mesh of %lld panels exceeds the supported %lld", (long long)m->n, (long long)kMaxOrder);
+  MH_TRY(set_device(ctx));
+  const int64_t n = m->n, nh = m->n_hull;
+  const size_t nn = (size_t)n * (size_t)n;
+  const int64_t nrhs = n_rad + n_beta, bstride = n * nrhs;
+  const uint32_t st = gfs & kStaticKinds;
+  cudaStream_t s0 = ctx->stream;
+
+  // [omegas | betas | wavenumbers | rad_idx, inf_idx]
+  const size_t n_int_d = (size_t)((n_rad + n_inf + 1) / 2) + 1;
+  const size_t nsmall = (size_t)n_omega * 2 + (size_t)n_beta + n_int_d + 8;
+  double* hs;
+  MH_TRY(pinned_get(ctx, nsmall * sizeof(double), &hs));
+  double* small_d;
+  MH_TRY(ws_get_t(ctx, kSlotIdx, nsmall, &small_d));
+  std::memcpy(hs, omegas, sizeof(double) * n_omega);
+  if (n_beta) std::memcpy(hs + n_omega, betas, sizeof(double) * n_beta);
+  for (int64_t w = 0; w < n_omega; ++w) hs[n_omega + n_beta + w] = omegas[w] * omegas[w] / g;
+  int32_t* hidx = (int32_t*)(hs + 2 * n_omega + n_beta);
+  for (int64_t q = 0; q < n_rad; ++q) hidx[q] = rad_idx[q];
+  for (int64_t q = 0; q < n_inf; ++q) hidx[n_rad + q] = inf_idx[q];
+  MH_CUDA(ctx, cudaMemcpyAsync(small_d, hs, nsmall * sizeof(double), cudaMemcpyHostToDevice, s0));
+  const double* om_d = small_d;
+  const double* beta_d = small_d + n_omega;
+  const double* ks_all = small_d + n_omega + n_beta;
+  const int32_t* rad_d = (const int32_t*)(small_d + 2 * n_omega + n_beta);
+  const int32_t* inf_d = rad_d + n_rad;
+
+  // dof fields on the device and, for the Froude-Krylov derivative, on the host
+  std::vector<double> hdofs((size_t)(n_dofs * n * 3)), hC((size_t)(3 * n)), hN((size_t)(3 * n)), hAr((size_t)n);
+  const double* dofs_d = nullptr;
+  if (n_dofs > 0) {
+    double* dd;
+    MH_TRY(ws_get_t(ctx, kSlotDofs, (size_t)(n_dofs * n * 3), &dd));
+    MH_TRY(copy_in(ctx, dd, dofs, sizeof(double) * n_dofs * n * 3, mem));
+    dofs_d = dd;
+    MH_CUDA(ctx, cudaMemcpyAsync(hdofs.data(), dd, sizeof(double) * hdofs.size(), cudaMemcpyDeviceToHost, s0));
+  }
+  MH_CUDA(ctx, cudaMemcpyAsync(hC.data(), m->C, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s0));
+  MH_CUDA(ctx, cudaMemcpyAsync(hN.data(), m->N, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s0));
+  MH_CUDA(ctx, cudaMemcpyAsync(hAr.data(), m->A, sizeof(double) * n, cudaMemcpyDeviceToHost, s0));
+
+  double *SR = nullptr, *DR = nullptr;
+  if (st) {
+    MH_TRY(ws_get_t(ctx, kSlotSR, nn, &SR));
+    MH_TRY(ws_get_t(ctx, kSlotDR, nn, &DR));
+    MH_TRY(compute_static(ctx, m, gfs, direct, 1, nullptr, SR, DR));
+  }
+  double2 *S, *D, *dS, *dD, *B, *X, *dB, *R, *T, *P2, *F, *FK, *dF, *work;
+  int32_t* ipiv;
+  MH_TRY(ws_get_t(ctx, kSlotS, nn, &S));
+  MH_TRY(ws_get_t(ctx, kSlotD, nn, &D));
+  MH_TRY(ws_get_t(ctx, kSlotA64, nn, &dS));
+  MH_TRY(ws_get_t(ctx, kSlotLU32, nn, &dD));
+  MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)bstride, &B));
+  MH_TRY(ws_get_t(ctx, kSlotX, (size_t)bstride, &X));
+  MH_TRY(ws_get_t(ctx, kSlotB, (size_t)bstride, &dB));
+  MH_TRY(ws_get_t(ctx, kSlotR, (size_t)bstride, &R));
+  MH_TRY(ws_get_t(ctx, kSlotT, (size_t)bstride, &T));
+  MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)bstride, &P2));
+  const int64_t ninf1 = std::max<int64_t>(n_inf, 1), nb1 = std::max<int64_t>(n_beta, 1);
+  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(n_omega * ninf1 * nrhs), &F));
+  MH_TRY(ws_get_t(ctx, kSlotFK, (size_t)(n_omega * ninf1 * nb1), &FK));
+  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)(n_omega * ninf1 * nrhs), &dF));
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, 1), &work));
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
+
+  EpilogueGeom eg{n, nh, m->C, m->N, m->A, dofs_d};
+  AssemblyParams p = make_params(ctx, m, gfs, direct, 1, nullptr);
+  const BatchDesc d{n, 1, (int64_t)nn};
+  LaunchCounter lc = ctx->lc();
+  auto times = [&](const double2* A, const double2* in, double2* out) {
+    zgemm_nn_batched(s0, lc, d, A, in, nrhs, bstride, out, work);
+  };
+  for (int64_t w = 0; w < n_omega; ++w) {
+    const double om = omegas[w];
+    launch_assemble_wave(s0, lc, p, SR, DR, 1, ks_all + w, S, D, (int64_t)nn, st ? 0 : 1);
+    launch_wave_dk(s0, lc, p, ks_all + w, dS, dD);
+    launch_build_rhs(s0, lc, eg, 1, om_d + w, g, (int)n_rad, rad_d, (int)n_beta, beta_d, B, bstride);
+    launch_build_drhs(s0, lc, eg, 1, om_d + w, g, (int)n_rad, rad_d, (int)n_beta, beta_d, dB, bstride);
+    MH_TRY(check_launch(ctx, "frequency-derivative assembly"));
+    // dS/domega = dS/dk dk/domega, likewise D: scale the products by dk/domega = 2 omega / g
+    const double dk = 2.0 * om / g;
+    if (direct) {
+      // phi = D^-1 S b;  dphi = D^-1 (dS b + S db - dD phi)
+      times(S, B, X);
+      MH_TRY(solve_core(ctx, d, D, X, nrhs, bstride, MH_PREC_FP64, false));
+      MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
+      times(dS, B, R);
+      MH_CUDA(ctx, cudaMemsetAsync(P2, 0, sizeof(double2) * bstride, s0));
+      launch_zaxpy(s0, lc, bstride, dk, R, P2);
+      times(S, dB, T);
+      launch_zaxpy(s0, lc, bstride, 1.0, T, P2);
+      times(dD, X, T);
+      launch_zaxpy(s0, lc, bstride, -dk, T, P2);
+      lu_solve_batched<double>(s0, lc, d, D, ipiv, P2, nrhs, bstride, false);
+      MH_TRY(check_launch(ctx, "frequency-derivative solve"));
+    } else {
+      // sigma = D^-1 b, phi = S sigma;  dsigma = D^-1 (db - dD sigma), dphi = dS sigma + S dsigma
+      MH_CUDA(ctx, cudaMemcpyAsync(X, B, sizeof(double2) * bstride, cudaMemcpyDeviceToDevice, s0));
+      MH_TRY(solve_core(ctx, d, D, X, nrhs, bstride, MH_PREC_FP64, false));
+      MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
+      MH_CUDA(ctx, cudaMemcpyAsync(R, dB, sizeof(double2) * bstride, cudaMemcpyDeviceToDevice, s0));
+      times(dD, X, T);
+      launch_zaxpy(s0, lc, bstride, -dk, T, R);
+      lu_solve_batched<double>(s0, lc, d, D, ipiv, R, nrhs, bstride, false);  // dsigma
+      times(dS, X, T);
+      MH_CUDA(ctx, cudaMemsetAsync(P2, 0, sizeof(double2) * bstride, s0));
+      launch_zaxpy(s0, lc, bstride, dk, T, P2);
+      times(S, R, T);
+      launch_zaxpy(s0, lc, bstride, 1.0, T, P2);                               // dphi
+      times(S, X, T);
+      MH_CUDA(ctx, cudaMemcpyAsync(X, T, sizeof(double2) * bstride, cudaMemcpyDeviceToDevice, s0));  // phi
+      MH_TRY(check_launch(ctx, "frequency-derivative solve"));
+    }
+    // p = i rho omega phi;  dp = i rho omega (phi / omega + dphi): forces of phi and of phi / omega + dphi
+    launch_zaxpy(s0, lc, bstride, 1.0 / om, X, P2);
+    if (n_inf > 0) {
+      launch_forces(s0, lc, eg, 1, om_d + w, rho, g, (int)nrhs, X, bstride, (int)n_inf, inf_d, (int)n_beta, beta_d,
+                    F + w * n_inf * nrhs, FK + w * n_inf * nb1);
+      launch_forces(s0, lc, eg, 1, om_d + w, rho, g, (int)nrhs, P2, bstride, (int)n_inf, inf_d, 0, nullptr,
+                    dF + w * n_inf * nrhs, nullptr);
+      MH_TRY(check_launch(ctx, "forces"));
+    }
+  }
+  std::vector<double2> hF((size_t)(n_omega * ninf1 * nrhs)), hdF(hF.size()), hFK((size_t)(n_omega * ninf1 * nb1));
+  if (n_inf > 0) {
+    MH_CUDA(ctx, cudaMemcpyAsync(hF.data(), F, sizeof(double2) * hF.size(), cudaMemcpyDeviceToHost, s0));
+    MH_CUDA(ctx, cudaMemcpyAsync(hdF.data(), dF, sizeof(double2) * hdF.size(), cudaMemcpyDeviceToHost, s0));
+    if (n_beta > 0) MH_CUDA(ctx, cudaMemcpyAsync(hFK.data(), FK, sizeof(double2) * hFK.size(), cudaMemcpyDeviceToHost, s0));
+  }
+  MH_TRY(sync(ctx, "frequency derivative"));
+  // pack; A = Re F / w^2, B = Im F / w (problems_and_results.jl:207-208) and their omega-derivatives;
+  // Froude-Krylov: p = rho g e^{kz} e^{i k wbar}, dp/domega = p (z + i wbar) 2 omega / g (waves.jl:259-264)
+  std::vector<double> hA((size_t)(n_inf * n_rad * n_omega)), hB(hA.size()), hdA(hA.size()), hdB(hA.size());
+  std::vector<double2> hd((size_t)(n_inf * n_omega * n_beta)), hk(hd.size()), he(hd.size()), hdd(hd.size()),
+      hdk(hd.size()), hde(hd.size());
+  for (int64_t w = 0; w < n_omega; ++w) {
+    const double om = omegas[w], k = om * om / g, dk = 2.0 * om / g;
+    for (int64_t i = 0; i < n_inf; ++i) {
+      for (int64_t r = 0; r < n_rad; ++r) {
+        const double2 f = hF[(w * n_inf + i) * nrhs + r], df = hdF[(w * n_inf + i) * nrhs + r];
+        const size_t o = (size_t)(i + n_inf * (r + n_rad * w));
+        hA[o] = f.x / (om * om);
+        hB[o] = f.y / om;
+        hdA[o] = df.x / (om * om) - 2.0 * f.x / (om * om * om);
+        hdB[o] = df.y / om - f.y / (om * om);
+      }
+      const double* dof = hdofs.data() + (size_t)inf_idx[i] * n * 3;
+      for (int64_t b = 0; b < n_beta; ++b) {
+        const double2 fd = hF[(w * n_inf + i) * nrhs + n_rad + b], dfd = hdF[(w * n_inf + i) * nrhs + n_rad + b];
+        const double2 fk = hFK[(w * n_inf + i) * n_beta + b];
+        const double cb = std::cos(betas[b]), sb = std::sin(betas[b]);
+        double dkr = 0.0, dki = 0.0;
+        for (int64_t j = 0; j < nh; ++j) {
+          const double wbar = hC[3 * j] * cb + hC[3 * j + 1] * sb, z = hC[3 * j + 2];
+          const double a = rho * g * std::exp(k * z);
+          const double pr = a * std::cos(k * wbar), pi = a * std::sin(k * wbar);
+          const double disp = hN[3 * j] * dof[3 * j] + hN[3 * j + 1] * dof[3 * j + 1] + hN[3 * j + 2] * dof[3 * j + 2];
+          const double f = -disp * hAr[j];
+          // (pr + i pi) (z + i wbar) dk
+          dkr += (pr * z - pi * wbar) * dk * f;
+          dki += (pr * wbar + pi * z) * dk * f;
+        }
+        const size_t o = (size_t)(i + n_inf * (w + n_omega * b));
+        hd[o] = fd;
+        hk[o] = fk;
+        he[o] = make_double2(fd.x + fk.x, fd.y + fk.y);
+        hdd[o] = dfd;
+        hdk[o] = make_double2(dkr, dki);
+        hde[o] = make_double2(dfd.x + dkr, dfd.y + dki);
+      }
+    }
+  }
+  MH_TRY(put_out(ctx, added_mass, hA.data(), hA.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, radiation_damping, hB.data(), hB.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, diffraction_force, hd.data(), hd.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, froude_krylov_force, hk.data(), hk.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, excitation_force, he.data(), he.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, d_added_mass, hdA.data(), hdA.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, d_radiation_damping, hdB.data(), hdB.size() * sizeof(double), mem));
+  MH_TRY(put_out(ctx, d_diffraction_force, hdd.data(), hdd.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, d_froude_krylov_force, hdk.data(), hdk.size() * sizeof(double2), mem));
+  MH_TRY(put_out(ctx, d_excitation_force, hde.data(), hde.size() * sizeof(double2), mem));
+  return sync(ctx, "frequency-derivative outputs");
+}
+
 int mh_wu_wave_terms(mh_context* ctx, int64_t m, const double* hh, const double* vv, double* out, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (m <= 0 || !hh || !vv || !out) return fail(ctx, MH_ERR_ARG, "bad wave-term arguments");
@@ -1306,6 +1526,17 @@ int mh_probe_fma_peaks(mh_context* ctx, double* fp64_tflops, double* fp32_tflops
   MH_TRY(set_device(ctx));
   int rc = probe_fma_peaks(ctx->stream, fp64_tflops, fp32_tflops);
   if (rc) return fail(ctx, rc, "FMA probe failed");
+  return MH_OK;
+}
+
+int mh_probe_wait_timeout(mh_context* ctx, uint32_t polls) {
+  if (!ctx) return MH_ERR_ARG;
+  if (polls < 1 || polls > (1u << 20)) return fail(ctx, MH_ERR_ARG, "polls must be 1..2^20 (got %u)", polls);
+  MH_TRY(set_device(ctx));
+  int timed_out = 0;
+  int rc = probe_wait_timeout(ctx->stream, polls, &timed_out);
+  if (rc) return fail(ctx, rc, "wait-timeout probe: %s", cudaGetErrorString(cudaGetLastError()));
+  if (timed_out) return fail(ctx, MH_ERR_TIMEOUT, "a bounded completion wait gave up after %u polls", polls);
   return MH_OK;
 }
 

@@ -57,6 +57,60 @@ __global__ void build_rhs_kernel(EpilogueGeom g, const double* __restrict__ omeg
   B[w * bstride + col * n + i] = v;
 }
 
+// d/d omega of build_rhs_kernel's columns, with k = omega^2 / g (compute_wavenumber):
+//   radiation   d bc / d omega = -i (n . dof)
+//   diffraction the Airy amplitude g k / omega = omega, so
+//               d bc / d omega = bc (1 / omega + (z + i wbar) 2 omega / g)
+__global__ void build_drhs_kernel(EpilogueGeom g, const double* __restrict__ omegas, double gacc, int n_rad,
+                                  const int32_t* __restrict__ rad_idx, int n_beta, const double* __restrict__ betas,
+                                  double2* __restrict__ dB, int64_t bstride) {
+  const int64_t n = g.n;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int col = blockIdx.y;
+  const int w = blockIdx.z;
+  if (i >= n) return;
+  if (i >= g.n_hull) {
+    dB[w * bstride + col * n + i] = make_double2(0.0, 0.0);
+    return;
+  }
+  const double omega = omegas[w];
+  const double nx = g.N[3 * i], ny = g.N[3 * i + 1], nz = g.N[3 * i + 2];
+  double2 v;
+  if (col < n_rad) {
+    const double* dof = g.dofs + (int64_t)rad_idx[col] * n * 3 + 3 * i;
+    double disp = nx * dof[0] + ny * dof[1] + nz * dof[2];
+    v = make_double2(0.0 * disp, -disp);
+  } else {
+    const double beta = betas[col - n_rad];
+    const double k = omega * omega / gacc;
+    const double cx = g.C[3 * i], cy = g.C[3 * i + 1], cz = g.C[3 * i + 2];
+    double sb, cb;
+    sincos(beta, &sb, &cb);
+    const double wbar = cx * cb + cy * sb;
+    const double cih = exp(k * cz);
+    double sw, cw;
+    sincos(k * wbar, &sw, &cw);
+    const double s = gacc * k / omega;
+    const double ar = s * cw, ai = s * sw;
+    const double v1r = ar * cb * cih, v1i = ai * cb * cih;
+    const double v2r = ar * sb * cih, v2i = ai * sb * cih;
+    const double v3r = ai * cih, v3i = -ar * cih;
+    const double br = -(v1r * nx + v2r * ny + v3r * nz), bi = -(v1i * nx + v2i * ny + v3i * nz);
+    const double dk = 2.0 * omega / gacc;
+    const double fr = 1.0 / omega + cz * dk, fi = wbar * dk;
+    v = make_double2(br * fr - bi * fi, br * fi + bi * fr);
+  }
+  dB[w * bstride + col * n + i] = v;
+}
+
+__global__ void zaxpy_kernel(int64_t count, double alpha, const double2* __restrict__ x, double2* __restrict__ y) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < count) {
+    const double2 a = x[q], b = y[q];
+    y[q] = make_double2(fma(alpha, a.x, b.x), fma(alpha, a.y, b.y));
+  }
+}
+
 // One CTA per (influenced dof, rhs column, omega): deterministic tree reduction.
 __global__ void __launch_bounds__(256) force_kernel(EpilogueGeom g, const double* __restrict__ omegas, double rho,
                                                     double gacc, int nrhs, const double2* __restrict__ Phi,
@@ -130,6 +184,22 @@ void launch_build_rhs(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, 
   MH_LAUNCH(lc, st, "build_rhs",
             build_rhs_kernel<<<grid, 128, 0, st>>>(g, omegas_dev, gacc, n_rad, rad_idx_dev, n_beta, betas_dev, Bmat,
                                                    bstride));
+}
+
+void launch_build_drhs(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int nw, const double* omegas_dev,
+                       double gacc, int n_rad, const int32_t* rad_idx_dev, int n_beta, const double* betas_dev,
+                       double2* dB, int64_t bstride) {
+  const int ncol = n_rad + n_beta;
+  if (g.n <= 0 || ncol <= 0 || nw <= 0) return;
+  dim3 grid((unsigned)((g.n + 127) / 128), (unsigned)ncol, (unsigned)nw);
+  MH_LAUNCH(lc, st, "build_drhs",
+            build_drhs_kernel<<<grid, 128, 0, st>>>(g, omegas_dev, gacc, n_rad, rad_idx_dev, n_beta, betas_dev, dB,
+                                                    bstride));
+}
+
+void launch_zaxpy(cudaStream_t st, LaunchCounter lc, int64_t count, double alpha, const double2* x, double2* y) {
+  if (count <= 0) return;
+  MH_LAUNCH(lc, st, "zaxpy", zaxpy_kernel<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(count, alpha, x, y));
 }
 
 void launch_forces(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int nw, const double* omegas_dev,

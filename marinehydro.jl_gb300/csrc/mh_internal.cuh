@@ -228,6 +228,15 @@ void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const doub
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
                           const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2* wconj);
 void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x);
+// dS/dk, dD/dk of the Wu wave part at the wavenumber *k_dev (n x n complex, no static part)
+void launch_wave_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* k_dev, double2* dS,
+                    double2* dD);
+// d(boundary conditions)/d omega of launch_build_rhs, same layout
+void launch_build_drhs(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int nw, const double* omegas_dev,
+                       double gacc, int n_rad, const int32_t* rad_idx_dev, int n_beta, const double* betas_dev,
+                       double2* dB, int64_t bstride);
+// y += alpha x (complex vectors of `count` entries, real alpha)
+void launch_zaxpy(cudaStream_t st, LaunchCounter lc, int64_t count, double alpha, const double2* x, double2* y);
 
 // profiling (mh_profile.cu)
 Profiler* profiler_create();
@@ -237,6 +246,8 @@ bool profiler_on(const Profiler* p);
 void profiler_reset(Profiler* p);
 int profiler_read(Profiler* p, int64_t capacity, char* names, double* total_ms, int64_t* launches, int64_t* n);
 int probe_fma_peaks(cudaStream_t st, double* fp64_tflops, double* fp32_tflops);
+// one bounded mbarrier wait that nothing satisfies (the timeout path of the tensor-core kernels)
+int probe_wait_timeout(cudaStream_t st, uint32_t polls, int* timed_out);
 
 // misc
 void launch_combine_real_to_complex(cudaStream_t st, LaunchCounter lc, int64_t count, const double* re,
