@@ -120,7 +120,7 @@ int64_t mh_mesh_panels(const mh_mesh* mesh);
    only hull pressures enter the forces (`pressure[hull_mask]`, solve.jl:47-55).
    Every lid panel centre must lie below z = -1e-8 (at the free surface the wave
    terms are singular at the self pairs); n_hull = n_panels removes the lid.
-   mh_hydro_gradient rejects meshes with a lid (MH_ERR_UNSUPPORTED). */
+   mh_hydro_gradient and mh_hydro_vjp reject meshes with a lid (MH_ERR_UNSUPPORTED). */
 int mh_mesh_set_lid(mh_mesh* mesh, int64_t n_hull);
 
 /* ---- assembly ----------------------------------------------------------- */
@@ -297,6 +297,20 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const dou
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem);
+/* The general pullback of the same sweep, what Zygote / Enzyme reverse mode returns for
+   arbitrary cotangents of hydrodynamic_coefficients' radiation arrays:
+       J = sum over omega, influenced q, radiating r of
+           added_mass_bar[q, r, w] A[q, r, w] + radiation_damping_bar[q, r, w] B[q, r, w]
+   (cotangents n_inf x n_rad x n_omega, column-major, the layout of the outputs of
+   mh_hydrodynamic_coefficients; 1..64 dofs each).  Same method, Green functions and
+   precisions as mh_hydro_gradient (which is this call with identity cotangents on the
+   objective dofs); per frequency one adjoint solve per radiating dof.  grad_dofs is
+   n_dofs x n x 3 (every dof field, zero for dofs outside rad_idx / inf_idx). */
+int mh_hydro_vjp(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
+                 uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                 int64_t n_inf, const int32_t* inf_idx, const double* added_mass_bar,
+                 const double* radiation_damping_bar, int precision, double* J, double* grad_centers,
+                 double* grad_normals, double* grad_areas, double* grad_vertices, double* grad_dofs, int mem);
 
 /* ---- learned wave-term surrogate (no counterpart in the reference) --------- */
 /* A 2 -> 64 -> 64 -> 64 -> 6 tanh network with BF16 weights and FP32 arithmetic that

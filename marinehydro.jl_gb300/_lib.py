@@ -40,7 +40,7 @@ EXPORTS = (
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
     "mh_surrogate_wave_terms", "mh_surrogate_loss_grad", "mh_tile_table_set", "mh_tile_table_get", "mh_autotune",
-    "mh_probe_wait_timeout", "mh_hydro_frequency_derivative",
+    "mh_probe_wait_timeout", "mh_hydro_frequency_derivative", "mh_hydro_vjp",
 )
 
 
@@ -104,6 +104,8 @@ def load(path: str | None = None):
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
         L.mh_probe_wait_timeout.argtypes = [vp, ctypes.c_uint32]
+        L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, i64, vp, vp, vp, I, vp, vp, vp, vp,
+                                   vp, vp, I]
         L.mh_hydro_frequency_derivative.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64,
                                                     vp] + [vp] * 10 + [I]
         L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]

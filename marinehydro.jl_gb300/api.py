@@ -406,10 +406,7 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     if body.lid_mesh is not None:
         raise ValueError("hydro_gradient does not cover bodies with a lid")
     mesh = body.mesh
-    c, nrm, a, _ = face_fields(mesh.vertices, mesh.faces - 1)
-    if not (np.allclose(c, mesh.centers, rtol=0, atol=1e-12) and np.allclose(nrm, mesh.normals, rtol=0, atol=1e-12)
-            and np.allclose(a, mesh.areas, rtol=1e-12, atol=0)):
-        raise ValueError("the vertex gradient needs panel fields derived from the vertices (meshes.face_fields)")
+    _check_derived_fields(mesh)
     ctx_ = _ctx(ctx)
     names = list(body.dofs)
     idx = {n: i for i, n in enumerate(names)}
@@ -419,15 +416,66 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
     J, gc, gn, ga, gv, gd = _device.hydro_gradient(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
                                                     body.dof_array(names), [idx[d] for d in obj], f.precision_code)
+    grad = _vertex_gradient(body, gc, gn, ga, gv, {name: gd[h] for h, name in enumerate(obj)})
+    if return_panel_terms:
+        return J, grad, {"centers": gc, "normals": gn, "areas": ga, "corners": gv, "dofs": gd}
+    return J, grad
+
+
+def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_dofs, added_mass_bar,
+              radiation_damping_bar, formulation: BEMFormulation | None = None, ctx=None, rho=None, g=None):
+    """Pullback of the radiation arrays of hydrodynamic_coefficients with respect to the mesh
+    vertices: for cotangents Abar, Bbar of shape (n_inf, n_rad, n_omega) (or with the
+    reference's trailing n_U = 1 axis) returns (J, dJ/dvertices) with
+    J = sum Abar * added_mass + Bbar * radiation_damping -- what Zygote / Enzyme reverse mode
+    gives for the reference (ad_rules.jl:79-414).  Hand-written on the device
+    (mh_hydro_vjp): one adjoint solve per radiating dof and frequency with the LU factors
+    reused, pair derivatives recomputed.  Same scope as hydro_gradient (DirectBEM, Birk
+    Rankine family with GFWu, zero forward speed, no lid)."""
+    f = formulation or DirectBEM()
+    if not is_direct(f):
+        raise ValueError("hydro_vjp differentiates the direct formulation")
+    if body.lid_mesh is not None:
+        raise ValueError("hydro_vjp does not cover bodies with a lid")
+    mesh = body.mesh
+    _check_derived_fields(mesh)
+    ctx_ = _ctx(ctx)
+    names = list(body.dofs)
+    idx = {n: i for i, n in enumerate(names)}
+    rad, inf = list(radiating_dofs), list(influenced_dofs)
+    oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
+    shape = (len(inf), len(rad), oms.size)
+    ab = np.asarray(added_mass_bar, dtype=float).reshape(shape)
+    bb = np.asarray(radiation_damping_bar, dtype=float).reshape(shape)
+    rho = SETTINGS["rho"] if rho is None else rho
+    g = SETTINGS["g"] if g is None else g
+    J, gc, gn, ga, gv, gd = _device.hydro_vjp(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
+                                              body.dof_array(names), [idx[d] for d in rad], [idx[d] for d in inf],
+                                              ab, bb, f.precision_code)
+    return J, _vertex_gradient(body, gc, gn, ga, gv, {name: gd[idx[name]] for name in set(rad) | set(inf)})
+
+
+def _check_derived_fields(mesh):
+    c, nrm, a, _ = face_fields(mesh.vertices, mesh.faces - 1)
+    if not (np.allclose(c, mesh.centers, rtol=0, atol=1e-12) and np.allclose(nrm, mesh.normals, rtol=0, atol=1e-12)
+            and np.allclose(a, mesh.areas, rtol=1e-12, atol=0)):
+        raise ValueError("the vertex gradient needs panel fields derived from the vertices (meshes.face_fields)")
+
+
+def _vertex_gradient(body, gc, gn, ga, gv, gd_by_name):
+    """Chain the per-panel gradient terms to the mesh vertices: rigid rotation dof fields
+    follow the panel centres, and centres, normals, areas and Birk corners are functions
+    of each panel's corners (meshes.face_fields)."""
+    mesh = body.mesh
     gc = gc.copy()
     # rotation dof field axis x (c - rc) on its panels: d/dc of gd . (axis x c) = gd x axis
     rot = getattr(body, "rotations", {})
-    for h, name in enumerate(obj):
+    for name, gdn in gd_by_name.items():
         if name in rot:
             ax, _, p0, p1 = rot[name]
             e = np.zeros(3)
             e[ax] = 1.0
-            gc[p0:p1] += np.cross(gd[h, p0:p1], e)
+            gc[p0:p1] += np.cross(gdn[p0:p1], e)
     dC, dN, dA = face_fields_jacobian(mesh.panel_vertices)
     corner = (np.einsum("ik,ikq->iq", gc, dC) + np.einsum("ik,ikq->iq", gn, dN) + ga[:, None] * dA
               + gv.reshape(-1, 12))
@@ -435,9 +483,7 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     faces0 = mesh.faces - 1
     for q in range(4):
         np.add.at(grad, faces0[:, q], corner[:, 3 * q:3 * q + 3])
-    if return_panel_terms:
-        return J, grad, {"centers": gc, "normals": gn, "areas": ga, "corners": gv, "dofs": gd}
-    return J, grad
+    return grad
 
 
 def train_surrogate(n_samples=10_000_000, seed=2026, epochs=8, batch=8192, lr=3e-3, ctx=None):

@@ -628,37 +628,49 @@ __global__ void weights_accumulate_kernel(int64_t n, WaveWeights w, double* __re
 // O(N) terms of one frequency (direct): force weights w_h = i rho omega (-n . dof_h) a and
 // boundary conditions b_h = -i omega (n . dof_h) depend on n and a.
 //   Re(c phi_h[i] dw_h[i]) + Re(c t_h[i] db_h[i]),  t_h = S^T lam_h
+// O(N) terms of one frequency (direct) for cotangents c[q, r] (influenced q, radiating r;
+// c = Abar / omega^2 - i Bbar / omega, J = sum Re(c F)):
+//   force weights  f_q = i rho omega (-n . dof_q) a, paired with psi_q = sum_r c[q, r] phi_r;
+//   conditions     b_r = -i omega (n . dof_r), paired with t_r = S^T lam_r (lam_r = D^-T w_r).
+// Both depend on the panel normal, the area and the dof fields; each thread owns one panel.
 __global__ void rhs_adjoint_kernel(int64_t n, const double* __restrict__ N, const double* __restrict__ A,
-                                   const double* __restrict__ dofs, const int32_t* __restrict__ obj, int nh,
-                                   double omega, double rho, double2 c, const double2* __restrict__ phi,
+                                   const double* __restrict__ dofs, const int32_t* __restrict__ rad, int n_rad,
+                                   const int32_t* __restrict__ inf, int n_inf, double omega, double rho,
+                                   const double2* __restrict__ cw, const double2* __restrict__ phi,
                                    const double2* __restrict__ t, double* __restrict__ gn, double* __restrict__ ga,
                                    double* __restrict__ gd) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double n0 = N[3 * i], n1 = N[3 * i + 1], n2 = N[3 * i + 2], a = A[i];
   double g0 = 0, g1 = 0, g2 = 0, gav = 0;
-  for (int h = 0; h < nh; ++h) {
-    const double* dof = dofs + (int64_t)obj[h] * n * 3 + 3 * i;
-    const double disp = N[3 * i] * dof[0] + N[3 * i + 1] * dof[1] + N[3 * i + 2] * dof[2];
-    // w = i rho omega (-disp) a :  dw/dn = i rho omega (-dof) a ; dw/da = i rho omega (-disp)
-    const double2 cphi = cmulz(c, phi[i + h * n]);
-    // Re(cphi * i s) = -s Im(cphi)
-    const double s_n = -rho * omega * A[i];
-    g0 += -cphi.y * (s_n * dof[0]);
-    g1 += -cphi.y * (s_n * dof[1]);
-    g2 += -cphi.y * (s_n * dof[2]);
-    gav += -cphi.y * (rho * omega * -disp);
-    // b = -i omega disp : db/dn = -i omega dof ;  Re(ct * (-i omega)) = omega Im(ct)
-    const double2 ct = cmulz(c, t[i + h * n]);
-    g0 += omega * ct.y * dof[0];
-    g1 += omega * ct.y * dof[1];
-    g2 += omega * ct.y * dof[2];
-    // the same two terms differentiated w.r.t. the dof field: dw/d dof = i rho omega (-n) a,
-    // db/d dof = -i omega n
-    const double sd = cphi.y * rho * omega * A[i] + omega * ct.y;
-    double* gdi = gd + ((int64_t)h * n + i) * 3;
-    gdi[0] += sd * N[3 * i];
-    gdi[1] += sd * N[3 * i + 1];
-    gdi[2] += sd * N[3 * i + 2];
+  for (int q = 0; q < n_inf; ++q) {
+    const double* dof = dofs + (int64_t)inf[q] * n * 3 + 3 * i;
+    const double disp = n0 * dof[0] + n1 * dof[1] + n2 * dof[2];
+    double2 psi = make_double2(0.0, 0.0);
+    for (int r = 0; r < n_rad; ++r) psi = zadd(psi, cmulz(cw[q + (int64_t)r * n_inf], phi[i + (int64_t)r * n]));
+    // Re(psi * i s) = -s Im(psi):  d/dn with s = rho omega (-dof) a, d/da with s = rho omega (-disp)
+    const double s_n = -rho * omega * a;
+    g0 += -psi.y * (s_n * dof[0]);
+    g1 += -psi.y * (s_n * dof[1]);
+    g2 += -psi.y * (s_n * dof[2]);
+    gav += -psi.y * (rho * omega * -disp);
+    const double sd = psi.y * rho * omega * a;  // d/d dof_q: s = rho omega (-n) a
+    double* gdi = gd + ((int64_t)inf[q] * n + i) * 3;
+    gdi[0] += sd * n0;
+    gdi[1] += sd * n1;
+    gdi[2] += sd * n2;
+  }
+  for (int r = 0; r < n_rad; ++r) {
+    const double* dof = dofs + (int64_t)rad[r] * n * 3 + 3 * i;
+    // b = -i omega disp:  Re(t (-i omega) x) = omega Im(t) x for x = dof (d/dn) and x = n (d/d dof)
+    const double ty = t[i + (int64_t)r * n].y;
+    g0 += omega * ty * dof[0];
+    g1 += omega * ty * dof[1];
+    g2 += omega * ty * dof[2];
+    double* gdi = gd + ((int64_t)rad[r] * n + i) * 3;
+    gdi[0] += omega * ty * n0;
+    gdi[1] += omega * ty * n1;
+    gdi[2] += omega * ty * n2;
   }
   gn[3 * i] += g0;
   gn[3 * i + 1] += g1;
@@ -666,16 +678,23 @@ __global__ void rhs_adjoint_kernel(int64_t n, const double* __restrict__ N, cons
   ga[i] += gav;
 }
 
-// w_h[i] = conj(i rho omega (-n . dof_h) a)   (conjugated for the A^H solve)
+// w_r[i] = conj(sum_q c[q, r] i rho omega (-n . dof_q) a)   (conjugated for the A^H solve)
 __global__ void force_weights_kernel(int64_t n, const double* __restrict__ N, const double* __restrict__ A,
-                                     const double* __restrict__ dofs, const int32_t* __restrict__ obj, int nh,
-                                     double omega, double rho, double2* __restrict__ wconj) {
+                                     const double* __restrict__ dofs, const int32_t* __restrict__ inf, int n_inf,
+                                     int n_rad, const double2* __restrict__ cw, double omega, double rho,
+                                     double2* __restrict__ wconj) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int h = blockIdx.y;
-  if (i >= n || h >= nh) return;
-  const double* dof = dofs + (int64_t)obj[h] * n * 3 + 3 * i;
-  const double disp = N[3 * i] * dof[0] + N[3 * i + 1] * dof[1] + N[3 * i + 2] * dof[2];
-  wconj[i + h * n] = make_double2(0.0, -(rho * omega * -disp * A[i]));
+  const int r = blockIdx.y;
+  if (i >= n || r >= n_rad) return;
+  double2 w = make_double2(0.0, 0.0);
+  for (int q = 0; q < n_inf; ++q) {
+    const double* dof = dofs + (int64_t)inf[q] * n * 3 + 3 * i;
+    const double disp = N[3 * i] * dof[0] + N[3 * i + 1] * dof[1] + N[3 * i + 2] * dof[2];
+    const double s = rho * omega * -disp * A[i];  // the force weight is i s
+    const double2 c = cw[q + (int64_t)r * n_inf];
+    w = zadd(w, make_double2(-c.y * s, c.x * s));
+  }
+  wconj[i + (int64_t)r * n] = make_double2(w.x, -w.y);
 }
 
 __global__ void conj_kernel(int64_t count, double2* __restrict__ x) {
@@ -704,18 +723,20 @@ void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams
 }
 
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                        const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2 c,
-                        const double2* phi, const double2* t, double* gn, double* ga, double* gd) {
+                        const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf, int n_inf,
+                        double omega, double rho, const double2* cw, const double2* phi, const double2* t, double* gn,
+                        double* ga, double* gd) {
   MH_LAUNCH(lc, st, "adjoint_rhs",
-            rhs_adjoint_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, N, A, dofs, obj, nh, omega, rho, c,
-                                                                             phi, t, gn, ga, gd));
+            rhs_adjoint_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, N, A, dofs, rad, n_rad, inf, n_inf,
+                                                                             omega, rho, cw, phi, t, gn, ga, gd));
 }
 
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                          const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2* wconj) {
-  dim3 grid((unsigned)((n + 127) / 128), (unsigned)nh);
+                          const double* dofs, const int32_t* inf, int n_inf, int n_rad, const double2* cw,
+                          double omega, double rho, double2* wconj) {
+  dim3 grid((unsigned)((n + 127) / 128), (unsigned)n_rad);
   MH_LAUNCH(lc, st, "adjoint_force_weights",
-            force_weights_kernel<<<grid, 128, 0, st>>>(n, N, A, dofs, obj, nh, omega, rho, wconj));
+            force_weights_kernel<<<grid, 128, 0, st>>>(n, N, A, dofs, inf, n_inf, n_rad, cw, omega, rho, wconj));
 }
 
 void launch_wave_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* k_dev, double2* dS,

@@ -110,7 +110,8 @@ namespace {
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
   kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
-  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotAnorm, kSlotCount
+  kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotAnorm, kSlotCw,
+  kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...) {
@@ -1913,14 +1914,25 @@ int mh_batch_release(mh_context* ctx) {
   return MH_OK;
 }
 
-int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
-                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
-                      int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
-                      double* grad_vertices, double* grad_dofs, int mem) {
+}  // extern "C"
+
+namespace {
+
+// Reverse-mode product of the zero-speed radiation sweep: J = sum over omega, influenced q
+// and radiating r of abar[q, r, w] A[q, r, w] + bbar[q, r, w] B[q, r, w] (host cotangents,
+// n_inf x n_rad x n_omega, column-major) and its gradient with respect to every panel's
+// centre, normal, area, Birk corners and the dof fields.  The gradient of the dof fields
+// stays on the device (n_dofs x n x 3, *gd_out, workspace memory).
+int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
+                   uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                   int64_t n_inf, const int32_t* inf_idx, const double* abar, const double* bbar, int precision,
+                   double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                   double* grad_vertices, const double** gd_out, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
-  if (n_obj <= 0 || n_obj > 4 || !obj_idx) return fail(ctx, MH_ERR_ARG, "objective needs 1..4 dofs");
+  if (n_rad <= 0 || n_inf <= 0 || !rad_idx || !inf_idx) return fail(ctx, MH_ERR_ARG, "need radiating and influenced dofs");
+  if (n_rad > 64 || n_inf > 64) return fail(ctx, MH_ERR_ARG, "at most 64 radiating and 64 influenced dofs");
   if (m->n_hull != m->n) return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint does not cover meshes with a lid");
   if (!dofs || n_dofs <= 0) return fail(ctx, MH_ERR_ARG, "dof fields required");
   const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU;
@@ -1929,13 +1941,15 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
-  for (int64_t q = 0; q < n_obj; ++q)
-    if (obj_idx[q] < 0 || obj_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "objective dof index out of range");
+  for (int64_t q = 0; q < n_rad; ++q)
+    if (rad_idx[q] < 0 || rad_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "radiating dof index out of range");
+  for (int64_t q = 0; q < n_inf; ++q)
+    if (inf_idx[q] < 0 || inf_idx[q] >= n_dofs) return fail(ctx, MH_ERR_ARG, "influenced dof index out of range");
   for (int64_t w = 0; w < n_omega; ++w)
     if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive");
   if (m->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "mesh exceeds %lld panels", (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
-  const int64_t n = m->n, nh = n_obj;
+  const int64_t n = m->n, nr = n_rad, ni = n_inf;
   const size_t nn = (size_t)n * n;
   cudaStream_t st = ctx->stream;
   const LaunchCounter lc = ctx->lc();
@@ -1943,13 +1957,13 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   // factorization and both solves run batched over a chunk, the adjoint kernels per frequency
   size_t free_b = 0, total_b = 0;
   MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nh * sizeof(double2) * 6;
-  if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * nh * sizeof(double2) * 3;
+  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nr * sizeof(double2) * 6;
+  if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * nr * sizeof(double2) * 3;
   const size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
   const int64_t chunk = std::min<int64_t>(n_omega, (int64_t)std::max<size_t>(1, budget / per_w));
-  const int64_t bstride = n * nh;
+  const int64_t bstride = n * nr;
   double *SR, *DR, *RS, *RD, *grad, *small, *dofs_d;
-  double2 *S, *D, *B, *X, *lam, *t, *work, *F, *FK;
+  double2 *S, *D, *B, *X, *lam, *t, *work, *F, *FK, *cw;
   int32_t *ipiv, *info;
   MH_TRY(ws_get_t(ctx, kSlotSR, nn, &SR));
   MH_TRY(ws_get_t(ctx, kSlotDR, nn, &DR));
@@ -1961,12 +1975,13 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(bstride * chunk), &X));
   MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(bstride * chunk), &lam));
   MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(bstride * chunk), &t));
-  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nh, chunk), &work));
-  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(nh * nh * n_omega), &F));
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nr, chunk), &work));
+  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(ni * nr * n_omega), &F));
   MH_TRY(ws_get_t(ctx, kSlotFK, 4, &FK));
+  MH_TRY(ws_get_t(ctx, kSlotCw, (size_t)(ni * nr * n_omega), &cw));  // not kSlotNorm: the refinement owns it
   MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * chunk), &ipiv));
   MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)chunk, &info));
-  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)((19 + 3 * nh) * n), &grad));
+  MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)((19 + 3 * n_dofs) * n), &grad));
   void* oz_ws = nullptr;  // FP64 LU update on the tensor cores (MH_PREC_FP64_TC)
   int* oz_flag = nullptr;
   if (precision == MH_PREC_FP64_TC) {
@@ -1977,8 +1992,8 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     oz_flag = reinterpret_cast<int*>(w + wsb);
     MH_CUDA(ctx, cudaMemsetAsync(oz_flag, 0, sizeof(int), st));
   }
-  // small device block: [omegas | wavenumbers | objective dof indices (int32)]
-  const size_t nsmall = (size_t)(2 * n_omega) + 4;
+  // small device block: [omegas | wavenumbers | radiating, influenced dof indices (int32)]
+  const size_t nsmall = (size_t)(2 * n_omega) + (size_t)(nr + ni + 1) / 2 + 2;
   MH_TRY(ws_get_t(ctx, kSlotIdx, nsmall, &small));
   if (mem == MH_MEM_DEVICE) {
     dofs_d = (double*)dofs;
@@ -1991,7 +2006,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   double* ga = grad + 6 * n;
   double* gv = grad + 7 * n;
   double* gd = grad + 19 * n;
-  MH_CUDA(ctx, cudaMemsetAsync(grad, 0, sizeof(double) * (19 + 3 * nh) * n, st));
+  MH_CUDA(ctx, cudaMemsetAsync(grad, 0, sizeof(double) * (19 + 3 * n_dofs) * n, st));
   MH_CUDA(ctx, cudaMemsetAsync(RS, 0, sizeof(double) * nn, st));
   MH_CUDA(ctx, cudaMemsetAsync(RD, 0, sizeof(double) * nn, st));
   const uint32_t stk = gfs & kStaticKinds;
@@ -2007,26 +2022,37 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     hsmall[w] = omegas[w];
     hsmall[n_omega + w] = omegas[w] * omegas[w] / g;
   }
-  int32_t* hobj = (int32_t*)(hsmall.data() + 2 * n_omega);
-  for (int64_t q = 0; q < nh; ++q) hobj[q] = obj_idx[q];
+  int32_t* hidx = (int32_t*)(hsmall.data() + 2 * n_omega);
+  for (int64_t q = 0; q < nr; ++q) hidx[q] = rad_idx[q];
+  for (int64_t q = 0; q < ni; ++q) hidx[nr + q] = inf_idx[q];
   MH_CUDA(ctx, cudaMemcpyAsync(small, hsmall.data(), sizeof(double) * nsmall, cudaMemcpyHostToDevice, st));
-  std::vector<double2> hF((size_t)(nh * nh * n_omega));
+  // cotangent factors c[q, r, w] = abar / w^2 - i bbar / w  (A = Re F / w^2, B = Im F / w)
+  std::vector<double2> hcw((size_t)(ni * nr * n_omega));
+  for (int64_t w = 0; w < n_omega; ++w)
+    for (int64_t q = 0; q < ni * nr; ++q) {
+      const size_t o = (size_t)(w * ni * nr + q);
+      hcw[o] = make_double2(abar[o] / (omegas[w] * omegas[w]), -bbar[o] / omegas[w]);
+    }
+  MH_CUDA(ctx, cudaMemcpyAsync(cw, hcw.data(), sizeof(double2) * hcw.size(), cudaMemcpyHostToDevice, st));
+  std::vector<double2> hF((size_t)(ni * nr * n_omega));
   const double* om_d = small;
   const double* ks_d = small + n_omega;
-  const int32_t* obj_d = (const int32_t*)(small + 2 * n_omega);
+  const int32_t* rad_d = (const int32_t*)(small + 2 * n_omega);
+  const int32_t* inf_d = rad_d + nr;
   EpilogueGeom eg{n, m->n_hull, m->C, m->N, m->A, dofs_d};
   for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
     const int64_t nw = std::min<int64_t>(chunk, n_omega - w0);
     BatchDesc d{n, nw, (int64_t)nn};
     launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, (int)nw, ks_d + w0, S, D, (int64_t)nn,
                          stk ? 0 : 1);
-    launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nh, obj_d, 0, nullptr, B, bstride);
+    launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nr, rad_d, 0, nullptr, B, bstride);
     // phi = D^-1 S b, forces, and mu = D^-H conj(w) for the force weights w
     auto forces_and_weights = [&]() {
-      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nh, X, bstride, (int)nh, obj_d, 0, nullptr,
-                    F + w0 * nh * nh, FK);
+      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nr, X, bstride, (int)ni, inf_d, 0, nullptr,
+                    F + w0 * ni * nr, FK);
       for (int64_t w = 0; w < nw; ++w)
-        launch_force_weights(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, omegas[w0 + w], rho, lam + w * bstride);
+        launch_force_weights(st, lc, n, m->N, m->A, dofs_d, inf_d, (int)ni, (int)nr, cw + (w0 + w) * ni * nr,
+                             omegas[w0 + w], rho, lam + w * bstride);
     };
     bool done = false;
     if (precision == MH_PREC_MIXED) {
@@ -2035,39 +2061,42 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
       float2* LU32;
       double* anrm;
       MH_TRY(factor_mixed(ctx, d, D, &LU32, &anrm));
-      zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
+      zgemm_nn_batched(st, lc, d, S, B, nr, bstride, X, work);
       bool ok_fwd = false, ok_adj = false;
-      MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, nh, bstride, false, &ok_fwd, nullptr));
+      MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, nr, bstride, false, &ok_fwd, nullptr));
       if (ok_fwd) {
         forces_and_weights();
-        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, nh, bstride, true, &ok_adj, nullptr));
+        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, nr, bstride, true, &ok_adj, nullptr));
       }
       done = ok_fwd && ok_adj;
     }
     if (!done) {
-      zgemm_nn_batched(st, lc, d, S, B, nh, bstride, X, work);
+      zgemm_nn_batched(st, lc, d, S, B, nr, bstride, X, work);
       lu_factor_batched<double>(st, lc, d, D, ipiv, info, oz_ws, oz_flag);
-      lu_solve_batched<double>(st, lc, d, D, ipiv, X, nh, bstride, false);     // X = phi
+      lu_solve_batched<double>(st, lc, d, D, ipiv, X, nr, bstride, false);     // X = phi
       forces_and_weights();
-      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nh, bstride, true);    // mu = D^-H conj(w)
+      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nr, bstride, true);    // mu = D^-H conj(w)
     }
     MH_TRY(check_launch(ctx, "gradient solves"));
     MH_TRY(check_pivots(ctx, d, w0));
-    zgemm_adj_batched(st, lc, d, S, lam, nh, bstride, t, work);                // S^H mu
+    zgemm_adj_batched(st, lc, d, S, lam, nr, bstride, t, work);                // S^H mu
     launch_conj(st, lc, nw * bstride, t);                                      // t = S^T lam
     launch_conj(st, lc, nw * bstride, lam);                                    // lam = D^-T w
     for (int64_t w = 0; w < nw; ++w) {
       const double om = omegas[w0 + w], k = om * om / g;
-      const double2 c = make_double2(1.0 / (om * om), -1.0 / om);
-      // wave-term gradient (GFWu only) and the frequency-summed Rankine weights
-      launch_wave_adjoint(st, lc, p, k, lam + w * bstride, B + w * bstride, X + w * bstride, (int)nh, c, gc, gn, ga,
-                          RS, RD);
-      launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, obj_d, (int)nh, om, rho, c, X + w * bstride,
-                         t + w * bstride, gn, ga, gd);
+      // wave-term gradient (GFWu only) and the frequency-summed Rankine weights, the
+      // cotangent factors already in lam; the wave kernel takes up to four columns at a time
+      for (int64_t c0 = 0; c0 < nr; c0 += 4) {
+        const int64_t off = w * bstride + c0 * n;
+        launch_wave_adjoint(st, lc, p, k, lam + off, B + off, X + off, (int)std::min<int64_t>(4, nr - c0),
+                            make_double2(1.0, 0.0), gc, gn, ga, RS, RD);
+      }
+      launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, rad_d, (int)nr, inf_d, (int)ni, om, rho,
+                         cw + (w0 + w) * ni * nr, X + w * bstride, t + w * bstride, gn, ga, gd);
     }
     MH_TRY(check_launch(ctx, "gradient frequencies"));
   }
-  MH_CUDA(ctx, cudaMemcpyAsync(hF.data(), F, sizeof(double2) * nh * nh * n_omega, cudaMemcpyDeviceToHost, st));
+  MH_CUDA(ctx, cudaMemcpyAsync(hF.data(), F, sizeof(double2) * hF.size(), cudaMemcpyDeviceToHost, st));
   if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
   MH_TRY(check_launch(ctx, "static adjoint"));
   MH_TRY(sync(ctx, "forces"));
@@ -2079,18 +2108,73 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   double Jsum = 0.0;
   for (int64_t w = 0; w < n_omega; ++w) {
     const double om = omegas[w];
-    for (int64_t h = 0; h < nh; ++h) {
-      const double2 f = hF[(w * nh + h) * nh + h];  // influenced dof h, right-hand side h
-      Jsum += f.x / (om * om) + f.y / om;
-    }
+    for (int64_t q = 0; q < ni; ++q)
+      for (int64_t r = 0; r < nr; ++r) {
+        const double2 f = hF[(w * ni + q) * nr + r];  // influenced q, right-hand side r
+        const size_t o = (size_t)(q + ni * (r + nr * w));
+        Jsum += abar[o] * f.x / (om * om) + bbar[o] * f.y / om;
+      }
   }
   if (J) *J = Jsum;
   MH_TRY(copy_out(ctx, grad_centers, gc, sizeof(double) * 3 * n, mem));
   MH_TRY(copy_out(ctx, grad_normals, gn, sizeof(double) * 3 * n, mem));
   MH_TRY(copy_out(ctx, grad_areas, ga, sizeof(double) * n, mem));
   MH_TRY(copy_out(ctx, grad_vertices, gv, sizeof(double) * 12 * n, mem));
-  MH_TRY(copy_out(ctx, grad_dofs, gd, sizeof(double) * 3 * nh * n, mem));
+  *gd_out = gd;
+  return MH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
+                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
+                      int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                      double* grad_vertices, double* grad_dofs, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (n_obj <= 0 || n_obj > 4 || !obj_idx) return fail(ctx, MH_ERR_ARG, "objective needs 1..4 dofs");
+  if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
+  // J = sum_w sum_h A_hh + B_hh: identity cotangents on the diagonal
+  std::vector<double> bar((size_t)(n_obj * n_obj * n_omega), 0.0);
+  for (int64_t w = 0; w < n_omega; ++w)
+    for (int64_t h = 0; h < n_obj; ++h) bar[(size_t)(h + n_obj * (h + n_obj * w))] = 1.0;
+  const double* gd = nullptr;
+  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_obj, obj_idx, n_obj, obj_idx,
+                        bar.data(), bar.data(), precision, J, grad_centers, grad_normals, grad_areas, grad_vertices,
+                        &gd, mem));
+  for (int64_t h = 0; h < n_obj; ++h)
+    MH_TRY(copy_out(ctx, grad_dofs ? grad_dofs + 3 * m->n * h : nullptr, gd + (size_t)obj_idx[h] * m->n * 3,
+                    sizeof(double) * 3 * m->n, mem));
   return sync(ctx, "gradient");
+}
+
+int mh_hydro_vjp(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
+                 uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                 int64_t n_inf, const int32_t* inf_idx, const double* added_mass_bar,
+                 const double* radiation_damping_bar, int precision, double* J, double* grad_centers,
+                 double* grad_normals, double* grad_areas, double* grad_vertices, double* grad_dofs, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (!added_mass_bar || !radiation_damping_bar) return fail(ctx, MH_ERR_ARG, "cotangents must not be NULL");
+  if (n_omega <= 0 || !omegas || n_rad <= 0 || n_inf <= 0 || n_rad > 64 || n_inf > 64)
+    return fail(ctx, MH_ERR_ARG, "need 1..64 radiating and influenced dofs and at least one frequency");
+  if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
+  const size_t nb = (size_t)(n_inf * n_rad * n_omega);
+  std::vector<double> ab(nb), bb(nb);
+  if (mem == MH_MEM_DEVICE) {
+    MH_TRY(set_device(ctx));
+    MH_CUDA(ctx, cudaMemcpy(ab.data(), added_mass_bar, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+    MH_CUDA(ctx, cudaMemcpy(bb.data(), radiation_damping_bar, sizeof(double) * nb, cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(ab.data(), added_mass_bar, sizeof(double) * nb);
+    std::memcpy(bb.data(), radiation_damping_bar, sizeof(double) * nb);
+  }
+  const double* gd = nullptr;
+  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_rad, rad_idx, n_inf, inf_idx,
+                        ab.data(), bb.data(), precision, J, grad_centers, grad_normals, grad_areas, grad_vertices,
+                        &gd, mem));
+  MH_TRY(copy_out(ctx, grad_dofs, gd, sizeof(double) * 3 * m->n * n_dofs, mem));
+  return sync(ctx, "vector-Jacobian product");
 }
 
 int mh_surrogate_param_count(void) { return kMlpParams; }

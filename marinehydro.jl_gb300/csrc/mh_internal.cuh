@@ -222,11 +222,15 @@ void launch_static_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyPara
 void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lam,
                          const double2* b, const double2* phi, int nh, double2 c, double* gc, double* gn, double* ga,
                          double* RS, double* RD);
+// cw: n_inf x n_rad complex cotangent factors c[q, r] of one frequency (device);
+// gd: n_dofs x n x 3, indexed by the dof indices in rad / inf
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                        const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2 c,
-                        const double2* phi, const double2* t, double* gn, double* ga, double* gd);
+                        const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf, int n_inf,
+                        double omega, double rho, const double2* cw, const double2* phi, const double2* t, double* gn,
+                        double* ga, double* gd);
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                          const double* dofs, const int32_t* obj, int nh, double omega, double rho, double2* wconj);
+                          const double* dofs, const int32_t* inf, int n_inf, int n_rad, const double2* cw,
+                          double omega, double rho, double2* wconj);
 void launch_conj(cudaStream_t st, LaunchCounter lc, int64_t count, double2* x);
 // dS/dk, dD/dk of the Wu wave part at the wavenumber *k_dev (n x n complex, no static part)
 void launch_wave_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* k_dev, double2* dS,

@@ -158,3 +158,46 @@ def test_other_precisions_match_fp64(mh, ctx, precision):
     J32, g32 = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(precision=precision), ctx=ctx, rho=1025.0)
     assert abs(J32 - J64) <= 1e-12 * abs(J64)
     assert np.abs(g32 - g64).max() <= 1e-10 * np.abs(g64).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_vjp_with_full_cotangents_matches_finite_differences(mh, ctx, precision):
+    """mh_hydro_vjp with dense random cotangents on every (influenced, radiating, omega)
+    entry of A and B, off-diagonal couplings and rotation dofs included."""
+    F = mh.DirectBEM(precision=precision)
+    m1, m2 = _geometry(mh)
+    dofs = ["Surge", "Heave", "Pitch"]
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
+    rad = ["c1__Heave", "c2__Pitch", "c1__Surge", "c2__Heave", "c1__Pitch"]  # five columns: two kernel groups
+    inf = ["c2__Heave", "c1__Pitch", "c1__Heave"]
+    rng = np.random.default_rng(5)
+    ab = rng.standard_normal((3, 5, len(OMEGAS)))
+    bb = rng.standard_normal((3, 5, len(OMEGAS)))
+
+    def objective(b):
+        r = mh.hydrodynamic_coefficients(b, {"wave_frequencies": OMEGAS, "radiating_dofs": rad,
+                                             "influenced_dofs": inf}, mh.DirectBEM(), ctx=ctx, rho=1025.0, g=9.81)
+        return float(np.sum(ab * r["added_mass"][..., 0]) + np.sum(bb * r["radiation_damping"][..., 0]))
+
+    J, grad = mh.hydro_vjp(body, OMEGAS, rad, inf, ab, bb, F, ctx=ctx, rho=1025.0, g=9.81)
+    J0 = objective(body)
+    assert abs(J - J0) <= 1e-11 * np.abs(ab).sum() * 1e3 + 1e-12 * abs(J0)
+    n1 = m1.nvertices
+    for d1, d2 in _affine_moves(m1.vertices, m2.vertices, np.random.default_rng(17)):
+        jp = objective(_body(mh, m1.vertices + H * d1, m2.vertices + H * d2, m1, m2, dofs))
+        jm = objective(_body(mh, m1.vertices - H * d1, m2.vertices - H * d2, m1, m2, dofs))
+        fd = (jp - jm) / (2 * H)
+        ad = float(np.sum(grad[:n1] * d1) + np.sum(grad[n1:] * d2))
+        scale = np.abs(grad).sum() * max(np.abs(d1).max(), np.abs(d2).max())
+        assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
+
+
+def test_vjp_with_identity_cotangents_equals_gradient(mh, ctx):
+    m1, m2 = _geometry(mh)
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave", "Pitch"])
+    obj = ["c1__Pitch", "c2__Heave"]
+    J1, g1 = mh.hydro_gradient(body, OMEGAS, obj, ctx=ctx, rho=1025.0, g=9.81)
+    eye = np.repeat(np.eye(2)[:, :, None], len(OMEGAS), axis=2)
+    J2, g2 = mh.hydro_vjp(body, OMEGAS, obj, obj, eye, eye, ctx=ctx, rho=1025.0, g=9.81)
+    assert J1 == pytest.approx(J2, rel=1e-14)
+    assert np.abs(g1 - g2).max() <= 1e-13 * np.abs(g1).max()
