@@ -298,19 +298,25 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const dou
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem);
 /* The general pullback of the same sweep, what Zygote / Enzyme reverse mode returns for
-   arbitrary cotangents of hydrodynamic_coefficients' radiation arrays:
+   arbitrary cotangents of hydrodynamic_coefficients' arrays:
        J = sum over omega, influenced q, radiating r of
-           added_mass_bar[q, r, w] A[q, r, w] + radiation_damping_bar[q, r, w] B[q, r, w]
-   (cotangents n_inf x n_rad x n_omega, column-major, the layout of the outputs of
-   mh_hydrodynamic_coefficients; 1..64 dofs each).  Same method, Green functions and
-   precisions as mh_hydro_gradient (which is this call with identity cotangents on the
-   objective dofs); per frequency one adjoint solve per radiating dof.  grad_dofs is
-   n_dofs x n x 3 (every dof field, zero for dofs outside rad_idx / inf_idx). */
+             added_mass_bar[q, r, w] A[q, r, w] + radiation_damping_bar[q, r, w] B[q, r, w]
+         + sum over omega, influenced q, heading b of
+             Re(excitation_force_bar[q, w, b]) Re Fe[q, w, b] + Im(…) Im Fe[q, w, b]
+   (A, B cotangents n_inf x n_rad x n_omega doubles; excitation cotangents n_inf x n_omega x
+   n_beta complex; column-major, the output layouts of mh_hydrodynamic_coefficients;
+   1..64 dofs and headings each, n_rad or n_beta may be 0).  Fe = diffraction +
+   Froude-Krylov, both differentiated (the Airy condition and pressure depend on the panel
+   centres).  Same method, Green functions and precisions as mh_hydro_gradient, which is
+   this call with identity cotangents on the objective dofs; per frequency one adjoint
+   solve per radiating dof and heading.  grad_dofs is n_dofs x n x 3 (every dof field,
+   zero for dofs outside rad_idx / inf_idx). */
 int mh_hydro_vjp(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
                  uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
-                 int64_t n_inf, const int32_t* inf_idx, const double* added_mass_bar,
-                 const double* radiation_damping_bar, int precision, double* J, double* grad_centers,
-                 double* grad_normals, double* grad_areas, double* grad_vertices, double* grad_dofs, int mem);
+                 int64_t n_inf, const int32_t* inf_idx, int64_t n_beta, const double* betas,
+                 const double* added_mass_bar, const double* radiation_damping_bar, const double* excitation_force_bar,
+                 int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                 double* grad_vertices, double* grad_dofs, int mem);
 
 /* ---- learned wave-term surrogate (no counterpart in the reference) --------- */
 /* A 2 -> 64 -> 64 -> 64 -> 6 tanh network with BF16 weights and FP32 arithmetic that

@@ -227,18 +227,22 @@ def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_bod
     return out
 
 
-def hydro_vjp(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, rad_idx, inf_idx, abar, bbar,
+def hydro_vjp(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, rad_idx, inf_idx, abar, bbar, betas=(), fbar=None,
               precision=_lib.MH_PREC_FP64):
-    """mh_hydro_vjp with host buffers: cotangents abar, bbar of shape (n_inf, n_rad, n_omega).
+    """mh_hydro_vjp with host buffers: cotangents abar, bbar of shape (n_inf, n_rad, n_omega),
+    fbar complex (n_inf, n_omega, n_beta).
 
     Returns (J, gc (n,3), gn (n,3), ga (n,), gv (n,4,3), gd (n_dofs,n,3))."""
     om = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
+    be = np.ascontiguousarray(np.asarray(betas, dtype=np.float64).ravel())
     dofs = np.ascontiguousarray(np.asarray(dofs, dtype=np.float64))
     ri = np.ascontiguousarray(np.asarray(rad_idx, dtype=np.int32).ravel())
     ii = np.ascontiguousarray(np.asarray(inf_idx, dtype=np.int32).ravel())
     shape = (ii.size, ri.size, om.size)
     ab = np.asfortranarray(np.asarray(abar, dtype=np.float64).reshape(shape))
     bb = np.asfortranarray(np.asarray(bbar, dtype=np.float64).reshape(shape))
+    fb = np.asfortranarray(np.zeros((ii.size, om.size, be.size), dtype=np.complex128) if fbar is None else
+                           np.asarray(fbar, dtype=np.complex128).reshape((ii.size, om.size, be.size)))
     n = dmesh.n
     J = ctypes.c_double()
     gc = np.empty((n, 3))
@@ -246,9 +250,10 @@ def hydro_vjp(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, rad_idx, inf_id
     ga = np.empty(n)
     gv = np.empty((n, 4, 3))
     gd = np.empty((dofs.shape[0], n, 3))
+    p = lambda a: a.ctypes.data if a.size else None
     ctx.check(ctx._L.mh_hydro_vjp(
         ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), dofs.shape[0],
-        dofs.ctypes.data, ri.size, ri.ctypes.data, ii.size, ii.ctypes.data, ab.ctypes.data, bb.ctypes.data,
+        dofs.ctypes.data, ri.size, p(ri), ii.size, ii.ctypes.data, be.size, p(be), p(ab), p(bb), p(fb),
         int(precision), ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data, gv.ctypes.data,
         gd.ctypes.data, MH_MEM_HOST), "hydro_vjp")
     return J.value, gc, gn, ga, gv, gd

@@ -104,8 +104,8 @@ def load(path: str | None = None):
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
         L.mh_probe_wait_timeout.argtypes = [vp, ctypes.c_uint32]
-        L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, i64, vp, vp, vp, I, vp, vp, vp, vp,
-                                   vp, vp, I]
+        L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, I,
+                                   vp, vp, vp, vp, vp, vp, I]
         L.mh_hydro_frequency_derivative.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64,
                                                     vp] + [vp] * 10 + [I]
         L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]

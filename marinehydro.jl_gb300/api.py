@@ -422,16 +422,18 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     return J, grad
 
 
-def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_dofs, added_mass_bar,
-              radiation_damping_bar, formulation: BEMFormulation | None = None, ctx=None, rho=None, g=None):
-    """Pullback of the radiation arrays of hydrodynamic_coefficients with respect to the mesh
-    vertices: for cotangents Abar, Bbar of shape (n_inf, n_rad, n_omega) (or with the
-    reference's trailing n_U = 1 axis) returns (J, dJ/dvertices) with
-    J = sum Abar * added_mass + Bbar * radiation_damping -- what Zygote / Enzyme reverse mode
-    gives for the reference (ad_rules.jl:79-414).  Hand-written on the device
-    (mh_hydro_vjp): one adjoint solve per radiating dof and frequency with the LU factors
-    reused, pair derivatives recomputed.  Same scope as hydro_gradient (DirectBEM, Birk
-    Rankine family with GFWu, zero forward speed, no lid)."""
+def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_dofs, added_mass_bar=None,
+              radiation_damping_bar=None, formulation: BEMFormulation | None = None, ctx=None, rho=None, g=None,
+              wave_directions=(), excitation_force_bar=None):
+    """Pullback of hydrodynamic_coefficients with respect to the mesh vertices: for
+    cotangents Abar, Bbar of shape (n_inf, n_rad, n_omega) and, with wave_directions, a
+    complex Fbar of shape (n_inf, n_omega, n_beta) (the reference's trailing n_U = 1 axis
+    may be present) returns (J, dJ/dvertices) with
+    J = sum Abar * added_mass + Bbar * radiation_damping + Re Fbar * Re Fe + Im Fbar * Im Fe
+    -- what Zygote / Enzyme reverse mode gives for the reference (ad_rules.jl:79-414).
+    Hand-written on the device (mh_hydro_vjp): one adjoint solve per radiating dof, heading
+    and frequency with the LU factors reused, pair derivatives recomputed.  Same scope as
+    hydro_gradient (DirectBEM, Birk Rankine family with GFWu, zero forward speed, no lid)."""
     f = formulation or DirectBEM()
     if not is_direct(f):
         raise ValueError("hydro_vjp differentiates the direct formulation")
@@ -442,16 +444,20 @@ def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_d
     ctx_ = _ctx(ctx)
     names = list(body.dofs)
     idx = {n: i for i, n in enumerate(names)}
-    rad, inf = list(radiating_dofs), list(influenced_dofs)
+    rad, inf, betas = list(radiating_dofs), list(influenced_dofs), list(wave_directions)
     oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
     shape = (len(inf), len(rad), oms.size)
-    ab = np.asarray(added_mass_bar, dtype=float).reshape(shape)
-    bb = np.asarray(radiation_damping_bar, dtype=float).reshape(shape)
+    ab = np.zeros(shape) if added_mass_bar is None else np.asarray(added_mass_bar, dtype=float).reshape(shape)
+    bb = np.zeros(shape) if radiation_damping_bar is None else np.asarray(radiation_damping_bar,
+                                                                          dtype=float).reshape(shape)
+    fshape = (len(inf), oms.size, len(betas))
+    fb = (np.zeros(fshape, complex) if excitation_force_bar is None
+          else np.asarray(excitation_force_bar, dtype=complex).reshape(fshape))
     rho = SETTINGS["rho"] if rho is None else rho
     g = SETTINGS["g"] if g is None else g
     J, gc, gn, ga, gv, gd = _device.hydro_vjp(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
                                               body.dof_array(names), [idx[d] for d in rad], [idx[d] for d in inf],
-                                              ab, bb, f.precision_code)
+                                              ab, bb, betas, fb, f.precision_code)
     return J, _vertex_gradient(body, gc, gn, ga, gv, {name: gd[idx[name]] for name in set(rad) | set(inf)})
 
 

@@ -628,37 +628,59 @@ __global__ void weights_accumulate_kernel(int64_t n, WaveWeights w, double* __re
 // O(N) terms of one frequency (direct): force weights w_h = i rho omega (-n . dof_h) a and
 // boundary conditions b_h = -i omega (n . dof_h) depend on n and a.
 //   Re(c phi_h[i] dw_h[i]) + Re(c t_h[i] db_h[i]),  t_h = S^T lam_h
-// O(N) terms of one frequency (direct) for cotangents c[q, r] (influenced q, radiating r;
-// c = Abar / omega^2 - i Bbar / omega, J = sum Re(c F)):
-//   force weights  f_q = i rho omega (-n . dof_q) a, paired with psi_q = sum_r c[q, r] phi_r;
-//   conditions     b_r = -i omega (n . dof_r), paired with t_r = S^T lam_r (lam_r = D^-T w_r).
-// Both depend on the panel normal, the area and the dof fields; each thread owns one panel.
+// O(N) terms of one frequency (direct) for cotangents c[q, col] (influenced q; columns: the
+// n_rad radiating dofs, then the n_beta headings; J = sum Re(c F), F the forces of the
+// columns plus, for the headings, the Froude-Krylov forces):
+//   force weights  f_q = i rho omega (-n . dof_q) a, paired with psi_q = sum_col c[q, col] phi_col;
+//   radiation      b_r = -i omega (n . dof_r), paired with t_r = S^T lam_r (lam = D^-T w);
+//   diffraction    b_beta = -(v . n), v = omega e^{k z} e^{i k wbar} (cos b, sin b, -i), also
+//                  paired with t_beta, depends on the centre through e^{kz + ikwbar};
+//   Froude-Krylov  sum p_beta (-n . dof_q) a, p_beta = rho g e^{k z} e^{i k wbar}.
+// Each thread owns one panel.
 __global__ void rhs_adjoint_kernel(int64_t n, const double* __restrict__ N, const double* __restrict__ A,
-                                   const double* __restrict__ dofs, const int32_t* __restrict__ rad, int n_rad,
-                                   const int32_t* __restrict__ inf, int n_inf, double omega, double rho,
-                                   const double2* __restrict__ cw, const double2* __restrict__ phi,
-                                   const double2* __restrict__ t, double* __restrict__ gn, double* __restrict__ ga,
-                                   double* __restrict__ gd) {
+                                   const double* __restrict__ C, const double* __restrict__ dofs,
+                                   const int32_t* __restrict__ rad, int n_rad, const int32_t* __restrict__ inf,
+                                   int n_inf, int n_beta, const double* __restrict__ betas, double omega, double rho,
+                                   double gacc, const double2* __restrict__ cw, const double2* __restrict__ phi,
+                                   const double2* __restrict__ t, double* __restrict__ gc, double* __restrict__ gn,
+                                   double* __restrict__ ga, double* __restrict__ gd) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int ncol = n_rad + n_beta;
   const double n0 = N[3 * i], n1 = N[3 * i + 1], n2 = N[3 * i + 2], a = A[i];
-  double g0 = 0, g1 = 0, g2 = 0, gav = 0;
+  const double k = omega * omega / gacc;
+  double g0 = 0, g1 = 0, g2 = 0, gav = 0, c0 = 0, c1 = 0, c2 = 0;
   for (int q = 0; q < n_inf; ++q) {
     const double* dof = dofs + (int64_t)inf[q] * n * 3 + 3 * i;
     const double disp = n0 * dof[0] + n1 * dof[1] + n2 * dof[2];
     double2 psi = make_double2(0.0, 0.0);
-    for (int r = 0; r < n_rad; ++r) psi = zadd(psi, cmulz(cw[q + (int64_t)r * n_inf], phi[i + (int64_t)r * n]));
+    for (int r = 0; r < ncol; ++r) psi = zadd(psi, cmulz(cw[q + (int64_t)r * n_inf], phi[i + (int64_t)r * n]));
     // Re(psi * i s) = -s Im(psi):  d/dn with s = rho omega (-dof) a, d/da with s = rho omega (-disp)
-    const double s_n = -rho * omega * a;
-    g0 += -psi.y * (s_n * dof[0]);
-    g1 += -psi.y * (s_n * dof[1]);
-    g2 += -psi.y * (s_n * dof[2]);
-    gav += -psi.y * (rho * omega * -disp);
-    const double sd = psi.y * rho * omega * a;  // d/d dof_q: s = rho omega (-n) a
+    double re = -psi.y * rho * omega;  // coefficient of the real factor (-disp a) below
+    // Froude-Krylov of every heading: Re(c p) times the same real factor, and its centre terms
+    for (int b = 0; b < n_beta; ++b) {
+      double sb, cb;
+      sincos(betas[b], &sb, &cb);
+      const double wbar = C[3 * i] * cb + C[3 * i + 1] * sb;
+      double sw, cw_;
+      sincos(k * wbar, &sw, &cw_);
+      const double pa = rho * gacc * exp(k * C[3 * i + 2]);
+      const double2 cp = cmulz(cw[q + (int64_t)(n_rad + b) * n_inf], make_double2(pa * cw_, pa * sw));
+      re += cp.x;
+      // d p / d centre = p (i k cos b, i k sin b, k):  Re(cp (i k cos b)) = -k cos b Im(cp)
+      const double f = -disp * a;
+      c0 += -k * cb * cp.y * f;
+      c1 += -k * sb * cp.y * f;
+      c2 += k * cp.x * f;
+    }
+    g0 += re * (-dof[0] * a);
+    g1 += re * (-dof[1] * a);
+    g2 += re * (-dof[2] * a);
+    gav += re * (-disp);
     double* gdi = gd + ((int64_t)inf[q] * n + i) * 3;
-    gdi[0] += sd * n0;
-    gdi[1] += sd * n1;
-    gdi[2] += sd * n2;
+    gdi[0] += re * (-n0 * a);
+    gdi[1] += re * (-n1 * a);
+    gdi[2] += re * (-n2 * a);
   }
   for (int r = 0; r < n_rad; ++r) {
     const double* dof = dofs + (int64_t)rad[r] * n * 3 + 3 * i;
@@ -672,10 +694,34 @@ __global__ void rhs_adjoint_kernel(int64_t n, const double* __restrict__ N, cons
     gdi[1] += omega * ty * n1;
     gdi[2] += omega * ty * n2;
   }
+  for (int b = 0; b < n_beta; ++b) {
+    double sb, cb;
+    sincos(betas[b], &sb, &cb);
+    const double wbar = C[3 * i] * cb + C[3 * i + 1] * sb;
+    double sw, cw_;
+    sincos(k * wbar, &sw, &cw_);
+    const double e = omega * exp(k * C[3 * i + 2]);
+    const double2 amp = make_double2(e * cw_, e * sw);  // v = amp (cos b, sin b, -i)
+    const double2 v0 = make_double2(amp.x * cb, amp.y * cb), v1 = make_double2(amp.x * sb, amp.y * sb);
+    const double2 v2 = make_double2(amp.y, -amp.x);
+    const double2 tb = t[i + (int64_t)(n_rad + b) * n];
+    // b = -(v . n):  d/dn = -v;  d/dc = b (i k cos b, i k sin b, k)
+    g0 += -cmulz(tb, v0).x;
+    g1 += -cmulz(tb, v1).x;
+    g2 += -cmulz(tb, v2).x;
+    const double2 bv = make_double2(-(v0.x * n0 + v1.x * n1 + v2.x * n2), -(v0.y * n0 + v1.y * n1 + v2.y * n2));
+    const double2 tbv = cmulz(tb, bv);
+    c0 += -k * cb * tbv.y;
+    c1 += -k * sb * tbv.y;
+    c2 += k * tbv.x;
+  }
   gn[3 * i] += g0;
   gn[3 * i + 1] += g1;
   gn[3 * i + 2] += g2;
   ga[i] += gav;
+  gc[3 * i] += c0;
+  gc[3 * i + 1] += c1;
+  gc[3 * i + 2] += c2;
 }
 
 // w_r[i] = conj(sum_q c[q, r] i rho omega (-n . dof_q) a)   (conjugated for the A^H solve)
@@ -723,12 +769,14 @@ void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams
 }
 
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                        const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf, int n_inf,
-                        double omega, double rho, const double2* cw, const double2* phi, const double2* t, double* gn,
-                        double* ga, double* gd) {
+                        const double* C, const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf,
+                        int n_inf, int n_beta, const double* betas, double omega, double rho, double gacc,
+                        const double2* cw, const double2* phi, const double2* t, double* gc, double* gn, double* ga,
+                        double* gd) {
   MH_LAUNCH(lc, st, "adjoint_rhs",
-            rhs_adjoint_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, N, A, dofs, rad, n_rad, inf, n_inf,
-                                                                             omega, rho, cw, phi, t, gn, ga, gd));
+            rhs_adjoint_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, N, A, C, dofs, rad, n_rad, inf, n_inf,
+                                                                             n_beta, betas, omega, rho, gacc, cw, phi,
+                                                                             t, gc, gn, ga, gd));
 }
 
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,

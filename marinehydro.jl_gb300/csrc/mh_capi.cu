@@ -1925,14 +1925,16 @@ namespace {
 // stays on the device (n_dofs x n x 3, *gd_out, workspace memory).
 int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
                    uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
-                   int64_t n_inf, const int32_t* inf_idx, const double* abar, const double* bbar, int precision,
-                   double* J, double* grad_centers, double* grad_normals, double* grad_areas,
-                   double* grad_vertices, const double** gd_out, int mem) {
+                   int64_t n_inf, const int32_t* inf_idx, const double* abar, const double* bbar, int64_t n_beta,
+                   const double* betas, const double* fbar, int precision, double* J, double* grad_centers,
+                   double* grad_normals, double* grad_areas, double* grad_vertices, const double** gd_out, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
-  if (n_rad <= 0 || n_inf <= 0 || !rad_idx || !inf_idx) return fail(ctx, MH_ERR_ARG, "need radiating and influenced dofs");
-  if (n_rad > 64 || n_inf > 64) return fail(ctx, MH_ERR_ARG, "at most 64 radiating and 64 influenced dofs");
+  if (n_rad < 0 || n_beta < 0 || n_rad + n_beta <= 0 || n_inf <= 0 || (n_rad && !rad_idx) || !inf_idx ||
+      (n_beta && (!betas || !fbar)))
+    return fail(ctx, MH_ERR_ARG, "need influenced dofs and radiating dofs or headings");
+  if (n_rad > 64 || n_inf > 64 || n_beta > 64) return fail(ctx, MH_ERR_ARG, "at most 64 dofs and 64 headings each");
   if (m->n_hull != m->n) return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint does not cover meshes with a lid");
   if (!dofs || n_dofs <= 0) return fail(ctx, MH_ERR_ARG, "dof fields required");
   const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU;
@@ -1949,7 +1951,7 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
     if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive");
   if (m->n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "mesh exceeds %lld panels", (long long)kMaxOrder);
   MH_TRY(set_device(ctx));
-  const int64_t n = m->n, nr = n_rad, ni = n_inf;
+  const int64_t n = m->n, nr = n_rad, ni = n_inf, nb = n_beta, ncol = n_rad + n_beta;
   const size_t nn = (size_t)n * n;
   cudaStream_t st = ctx->stream;
   const LaunchCounter lc = ctx->lc();
@@ -1957,11 +1959,11 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   // factorization and both solves run batched over a chunk, the adjoint kernels per frequency
   size_t free_b = 0, total_b = 0;
   MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nr * sizeof(double2) * 6;
-  if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * nr * sizeof(double2) * 3;
+  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * ncol * sizeof(double2) * 6;
+  if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * ncol * sizeof(double2) * 3;
   const size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
   const int64_t chunk = std::min<int64_t>(n_omega, (int64_t)std::max<size_t>(1, budget / per_w));
-  const int64_t bstride = n * nr;
+  const int64_t bstride = n * ncol;
   double *SR, *DR, *RS, *RD, *grad, *small, *dofs_d;
   double2 *S, *D, *B, *X, *lam, *t, *work, *F, *FK, *cw;
   int32_t *ipiv, *info;
@@ -1975,10 +1977,10 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(bstride * chunk), &X));
   MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(bstride * chunk), &lam));
   MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(bstride * chunk), &t));
-  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nr, chunk), &work));
-  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(ni * nr * n_omega), &F));
-  MH_TRY(ws_get_t(ctx, kSlotFK, 4, &FK));
-  MH_TRY(ws_get_t(ctx, kSlotCw, (size_t)(ni * nr * n_omega), &cw));  // not kSlotNorm: the refinement owns it
+  MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, ncol, chunk), &work));
+  MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(ni * ncol * n_omega), &F));
+  MH_TRY(ws_get_t(ctx, kSlotFK, (size_t)(ni * std::max<int64_t>(nb, 1) * n_omega), &FK));
+  MH_TRY(ws_get_t(ctx, kSlotCw, (size_t)(ni * ncol * n_omega), &cw));  // not kSlotNorm: the refinement owns it
   MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * chunk), &ipiv));
   MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)chunk, &info));
   MH_TRY(ws_get_t(ctx, kSlotGrad, (size_t)((19 + 3 * n_dofs) * n), &grad));
@@ -1992,8 +1994,8 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
     oz_flag = reinterpret_cast<int*>(w + wsb);
     MH_CUDA(ctx, cudaMemsetAsync(oz_flag, 0, sizeof(int), st));
   }
-  // small device block: [omegas | wavenumbers | radiating, influenced dof indices (int32)]
-  const size_t nsmall = (size_t)(2 * n_omega) + (size_t)(nr + ni + 1) / 2 + 2;
+  // small device block: [omegas | wavenumbers | headings | radiating, influenced dof indices (int32)]
+  const size_t nsmall = (size_t)(2 * n_omega + nb) + (size_t)(nr + ni + 1) / 2 + 2;
   MH_TRY(ws_get_t(ctx, kSlotIdx, nsmall, &small));
   if (mem == MH_MEM_DEVICE) {
     dofs_d = (double*)dofs;
@@ -2022,22 +2024,34 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
     hsmall[w] = omegas[w];
     hsmall[n_omega + w] = omegas[w] * omegas[w] / g;
   }
-  int32_t* hidx = (int32_t*)(hsmall.data() + 2 * n_omega);
+  for (int64_t b = 0; b < nb; ++b) hsmall[2 * n_omega + b] = betas[b];
+  int32_t* hidx = (int32_t*)(hsmall.data() + 2 * n_omega + nb);
   for (int64_t q = 0; q < nr; ++q) hidx[q] = rad_idx[q];
   for (int64_t q = 0; q < ni; ++q) hidx[nr + q] = inf_idx[q];
   MH_CUDA(ctx, cudaMemcpyAsync(small, hsmall.data(), sizeof(double) * nsmall, cudaMemcpyHostToDevice, st));
-  // cotangent factors c[q, r, w] = abar / w^2 - i bbar / w  (A = Re F / w^2, B = Im F / w)
-  std::vector<double2> hcw((size_t)(ni * nr * n_omega));
-  for (int64_t w = 0; w < n_omega; ++w)
-    for (int64_t q = 0; q < ni * nr; ++q) {
-      const size_t o = (size_t)(w * ni * nr + q);
-      hcw[o] = make_double2(abar[o] / (omegas[w] * omegas[w]), -bbar[o] / omegas[w]);
-    }
+  // cotangent factors per frequency, n_inf x (n_rad + n_beta): c = abar / w^2 - i bbar / w for the
+  // radiating columns (A = Re F / w^2, B = Im F / w), c = conj(fbar) for the headings
+  // (J = Re fbar Re Fe + Im fbar Im Fe = Re(conj(fbar) Fe))
+  std::vector<double2> hcw((size_t)(ni * ncol * n_omega));
+  for (int64_t w = 0; w < n_omega; ++w) {
+    for (int64_t r = 0; r < nr; ++r)
+      for (int64_t q = 0; q < ni; ++q) {
+        const size_t o = (size_t)(q + ni * (r + nr * w));
+        hcw[(size_t)(w * ni * ncol + r * ni + q)] = make_double2(abar[o] / (omegas[w] * omegas[w]), -bbar[o] / omegas[w]);
+      }
+    for (int64_t b = 0; b < nb; ++b)
+      for (int64_t q = 0; q < ni; ++q) {
+        const size_t o = (size_t)(q + ni * (w + n_omega * b));
+        hcw[(size_t)(w * ni * ncol + (nr + b) * ni + q)] = make_double2(fbar[2 * o], -fbar[2 * o + 1]);
+      }
+  }
   MH_CUDA(ctx, cudaMemcpyAsync(cw, hcw.data(), sizeof(double2) * hcw.size(), cudaMemcpyHostToDevice, st));
-  std::vector<double2> hF((size_t)(ni * nr * n_omega));
+  const int64_t nb1 = std::max<int64_t>(nb, 1);
+  std::vector<double2> hF((size_t)(ni * ncol * n_omega)), hFK((size_t)(ni * nb1 * n_omega));
   const double* om_d = small;
   const double* ks_d = small + n_omega;
-  const int32_t* rad_d = (const int32_t*)(small + 2 * n_omega);
+  const double* beta_d = small + 2 * n_omega;
+  const int32_t* rad_d = (const int32_t*)(small + 2 * n_omega + nb);
   const int32_t* inf_d = rad_d + nr;
   EpilogueGeom eg{n, m->n_hull, m->C, m->N, m->A, dofs_d};
   for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
@@ -2045,13 +2059,13 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
     BatchDesc d{n, nw, (int64_t)nn};
     launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, (int)nw, ks_d + w0, S, D, (int64_t)nn,
                          stk ? 0 : 1);
-    launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nr, rad_d, 0, nullptr, B, bstride);
+    launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nr, rad_d, (int)nb, beta_d, B, bstride);
     // phi = D^-1 S b, forces, and mu = D^-H conj(w) for the force weights w
     auto forces_and_weights = [&]() {
-      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)nr, X, bstride, (int)ni, inf_d, 0, nullptr,
-                    F + w0 * ni * nr, FK);
+      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)ncol, X, bstride, (int)ni, inf_d, (int)nb, beta_d,
+                    F + w0 * ni * ncol, FK + w0 * ni * nb1);
       for (int64_t w = 0; w < nw; ++w)
-        launch_force_weights(st, lc, n, m->N, m->A, dofs_d, inf_d, (int)ni, (int)nr, cw + (w0 + w) * ni * nr,
+        launch_force_weights(st, lc, n, m->N, m->A, dofs_d, inf_d, (int)ni, (int)ncol, cw + (w0 + w) * ni * ncol,
                              omegas[w0 + w], rho, lam + w * bstride);
     };
     bool done = false;
@@ -2061,42 +2075,43 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
       float2* LU32;
       double* anrm;
       MH_TRY(factor_mixed(ctx, d, D, &LU32, &anrm));
-      zgemm_nn_batched(st, lc, d, S, B, nr, bstride, X, work);
+      zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
       bool ok_fwd = false, ok_adj = false;
-      MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, nr, bstride, false, &ok_fwd, nullptr));
+      MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, ncol, bstride, false, &ok_fwd, nullptr));
       if (ok_fwd) {
         forces_and_weights();
-        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, nr, bstride, true, &ok_adj, nullptr));
+        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, ncol, bstride, true, &ok_adj, nullptr));
       }
       done = ok_fwd && ok_adj;
     }
     if (!done) {
-      zgemm_nn_batched(st, lc, d, S, B, nr, bstride, X, work);
+      zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
       lu_factor_batched<double>(st, lc, d, D, ipiv, info, oz_ws, oz_flag);
-      lu_solve_batched<double>(st, lc, d, D, ipiv, X, nr, bstride, false);     // X = phi
+      lu_solve_batched<double>(st, lc, d, D, ipiv, X, ncol, bstride, false);   // X = phi
       forces_and_weights();
-      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, nr, bstride, true);    // mu = D^-H conj(w)
+      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, ncol, bstride, true);  // mu = D^-H conj(w)
     }
     MH_TRY(check_launch(ctx, "gradient solves"));
     MH_TRY(check_pivots(ctx, d, w0));
-    zgemm_adj_batched(st, lc, d, S, lam, nr, bstride, t, work);                // S^H mu
+    zgemm_adj_batched(st, lc, d, S, lam, ncol, bstride, t, work);              // S^H mu
     launch_conj(st, lc, nw * bstride, t);                                      // t = S^T lam
     launch_conj(st, lc, nw * bstride, lam);                                    // lam = D^-T w
     for (int64_t w = 0; w < nw; ++w) {
       const double om = omegas[w0 + w], k = om * om / g;
       // wave-term gradient (GFWu only) and the frequency-summed Rankine weights, the
       // cotangent factors already in lam; the wave kernel takes up to four columns at a time
-      for (int64_t c0 = 0; c0 < nr; c0 += 4) {
+      for (int64_t c0 = 0; c0 < ncol; c0 += 4) {
         const int64_t off = w * bstride + c0 * n;
-        launch_wave_adjoint(st, lc, p, k, lam + off, B + off, X + off, (int)std::min<int64_t>(4, nr - c0),
+        launch_wave_adjoint(st, lc, p, k, lam + off, B + off, X + off, (int)std::min<int64_t>(4, ncol - c0),
                             make_double2(1.0, 0.0), gc, gn, ga, RS, RD);
       }
-      launch_rhs_adjoint(st, lc, n, m->N, m->A, dofs_d, rad_d, (int)nr, inf_d, (int)ni, om, rho,
-                         cw + (w0 + w) * ni * nr, X + w * bstride, t + w * bstride, gn, ga, gd);
+      launch_rhs_adjoint(st, lc, n, m->N, m->A, m->C, dofs_d, rad_d, (int)nr, inf_d, (int)ni, (int)nb, beta_d, om,
+                         rho, g, cw + (w0 + w) * ni * ncol, X + w * bstride, t + w * bstride, gc, gn, ga, gd);
     }
     MH_TRY(check_launch(ctx, "gradient frequencies"));
   }
   MH_CUDA(ctx, cudaMemcpyAsync(hF.data(), F, sizeof(double2) * hF.size(), cudaMemcpyDeviceToHost, st));
+  if (nb) MH_CUDA(ctx, cudaMemcpyAsync(hFK.data(), FK, sizeof(double2) * hFK.size(), cudaMemcpyDeviceToHost, st));
   if (stk) launch_static_adjoint(st, lc, pst, RS, RD, gc, gn, ga, gv);
   MH_TRY(check_launch(ctx, "static adjoint"));
   MH_TRY(sync(ctx, "forces"));
@@ -2108,12 +2123,18 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   double Jsum = 0.0;
   for (int64_t w = 0; w < n_omega; ++w) {
     const double om = omegas[w];
-    for (int64_t q = 0; q < ni; ++q)
+    for (int64_t q = 0; q < ni; ++q) {
       for (int64_t r = 0; r < nr; ++r) {
-        const double2 f = hF[(w * ni + q) * nr + r];  // influenced q, right-hand side r
+        const double2 f = hF[(w * ni + q) * ncol + r];  // influenced q, right-hand side r
         const size_t o = (size_t)(q + ni * (r + nr * w));
         Jsum += abar[o] * f.x / (om * om) + bbar[o] * f.y / om;
       }
+      for (int64_t b = 0; b < nb; ++b) {  // excitation = diffraction + Froude-Krylov
+        const double2 fd = hF[(w * ni + q) * ncol + nr + b], fk = hFK[(w * ni + q) * nb1 + b];
+        const size_t o = (size_t)(q + ni * (w + n_omega * b));
+        Jsum += fbar[2 * o] * (fd.x + fk.x) + fbar[2 * o + 1] * (fd.y + fk.y);
+      }
+    }
   }
   if (J) *J = Jsum;
   MH_TRY(copy_out(ctx, grad_centers, gc, sizeof(double) * 3 * n, mem));
@@ -2141,8 +2162,8 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
     for (int64_t h = 0; h < n_obj; ++h) bar[(size_t)(h + n_obj * (h + n_obj * w))] = 1.0;
   const double* gd = nullptr;
   MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_obj, obj_idx, n_obj, obj_idx,
-                        bar.data(), bar.data(), precision, J, grad_centers, grad_normals, grad_areas, grad_vertices,
-                        &gd, mem));
+                        bar.data(), bar.data(), 0, nullptr, nullptr, precision, J, grad_centers, grad_normals,
+                        grad_areas, grad_vertices, &gd, mem));
   for (int64_t h = 0; h < n_obj; ++h)
     MH_TRY(copy_out(ctx, grad_dofs ? grad_dofs + 3 * m->n * h : nullptr, gd + (size_t)obj_idx[h] * m->n * 3,
                     sizeof(double) * 3 * m->n, mem));
@@ -2151,28 +2172,38 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
 
 int mh_hydro_vjp(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
                  uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
-                 int64_t n_inf, const int32_t* inf_idx, const double* added_mass_bar,
-                 const double* radiation_damping_bar, int precision, double* J, double* grad_centers,
-                 double* grad_normals, double* grad_areas, double* grad_vertices, double* grad_dofs, int mem) {
+                 int64_t n_inf, const int32_t* inf_idx, int64_t n_beta, const double* betas,
+                 const double* added_mass_bar, const double* radiation_damping_bar, const double* excitation_force_bar,
+                 int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
+                 double* grad_vertices, double* grad_dofs, int mem) {
   if (!ctx) return MH_ERR_ARG;
-  if (!added_mass_bar || !radiation_damping_bar) return fail(ctx, MH_ERR_ARG, "cotangents must not be NULL");
-  if (n_omega <= 0 || !omegas || n_rad <= 0 || n_inf <= 0 || n_rad > 64 || n_inf > 64)
-    return fail(ctx, MH_ERR_ARG, "need 1..64 radiating and influenced dofs and at least one frequency");
+  if (n_omega <= 0 || !omegas || n_rad < 0 || n_beta < 0 || n_rad + n_beta <= 0 || n_inf <= 0 || n_rad > 64 ||
+      n_inf > 64 || n_beta > 64)
+    return fail(ctx, MH_ERR_ARG, "need a frequency, 1..64 influenced dofs and 1..64 radiating dofs or headings");
+  if ((n_rad && (!added_mass_bar || !radiation_damping_bar)) || (n_beta && (!excitation_force_bar || !betas)))
+    return fail(ctx, MH_ERR_ARG, "cotangents must not be NULL");
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
-  const size_t nb = (size_t)(n_inf * n_rad * n_omega);
-  std::vector<double> ab(nb), bb(nb);
-  if (mem == MH_MEM_DEVICE) {
-    MH_TRY(set_device(ctx));
-    MH_CUDA(ctx, cudaMemcpy(ab.data(), added_mass_bar, sizeof(double) * nb, cudaMemcpyDeviceToHost));
-    MH_CUDA(ctx, cudaMemcpy(bb.data(), radiation_damping_bar, sizeof(double) * nb, cudaMemcpyDeviceToHost));
-  } else {
-    std::memcpy(ab.data(), added_mass_bar, sizeof(double) * nb);
-    std::memcpy(bb.data(), radiation_damping_bar, sizeof(double) * nb);
-  }
+  const size_t nrb = (size_t)(n_inf * n_rad * n_omega), nfb = (size_t)(2 * n_inf * n_omega * n_beta);
+  std::vector<double> ab(nrb), bb(nrb), fb(nfb);
+  auto get = [&](double* dst, const double* src, size_t count) -> int {
+    if (!count) return MH_OK;
+    if (mem == MH_MEM_DEVICE) {
+      MH_TRY(set_device(ctx));
+      MH_CUDA(ctx, cudaMemcpy(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost));
+    } else {
+      std::memcpy(dst, src, sizeof(double) * count);
+    }
+    return MH_OK;
+  };
+  MH_TRY(get(ab.data(), added_mass_bar, nrb));
+  MH_TRY(get(bb.data(), radiation_damping_bar, nrb));
+  MH_TRY(get(fb.data(), excitation_force_bar, nfb));
+  std::vector<double> hb((size_t)std::max<int64_t>(n_beta, 1));
+  MH_TRY(get(hb.data(), betas, (size_t)n_beta));
   const double* gd = nullptr;
   MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_rad, rad_idx, n_inf, inf_idx,
-                        ab.data(), bb.data(), precision, J, grad_centers, grad_normals, grad_areas, grad_vertices,
-                        &gd, mem));
+                        ab.data(), bb.data(), n_beta, hb.data(), fb.data(), precision, J, grad_centers, grad_normals,
+                        grad_areas, grad_vertices, &gd, mem));
   MH_TRY(copy_out(ctx, grad_dofs, gd, sizeof(double) * 3 * m->n * n_dofs, mem));
   return sync(ctx, "vector-Jacobian product");
 }

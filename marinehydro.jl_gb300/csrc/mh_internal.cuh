@@ -224,10 +224,12 @@ void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams
                          double* RS, double* RD);
 // cw: n_inf x n_rad complex cotangent factors c[q, r] of one frequency (device);
 // gd: n_dofs x n x 3, indexed by the dof indices in rad / inf
+// (cw: n_inf x (n_rad + n_beta); the heading columns follow the radiating ones)
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
-                        const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf, int n_inf,
-                        double omega, double rho, const double2* cw, const double2* phi, const double2* t, double* gn,
-                        double* ga, double* gd);
+                        const double* C, const double* dofs, const int32_t* rad, int n_rad, const int32_t* inf,
+                        int n_inf, int n_beta, const double* betas, double omega, double rho, double gacc,
+                        const double2* cw, const double2* phi, const double2* t, double* gc, double* gn, double* ga,
+                        double* gd);
 void launch_force_weights(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,
                           const double* dofs, const int32_t* inf, int n_inf, int n_rad, const double2* cw,
                           double omega, double rho, double2* wconj);

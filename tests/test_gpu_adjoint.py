@@ -170,16 +170,23 @@ def test_vjp_with_full_cotangents_matches_finite_differences(mh, ctx, precision)
     body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
     rad = ["c1__Heave", "c2__Pitch", "c1__Surge", "c2__Heave", "c1__Pitch"]  # five columns: two kernel groups
     inf = ["c2__Heave", "c1__Pitch", "c1__Heave"]
+    betas = [0.0, 1.1]
     rng = np.random.default_rng(5)
     ab = rng.standard_normal((3, 5, len(OMEGAS)))
     bb = rng.standard_normal((3, 5, len(OMEGAS)))
+    # excitation forces are ~1e4 times larger than A, B here: scale their cotangents alike
+    fb = 1e-4 * (rng.standard_normal((3, len(OMEGAS), 2)) + 1j * rng.standard_normal((3, len(OMEGAS), 2)))
 
     def objective(b):
         r = mh.hydrodynamic_coefficients(b, {"wave_frequencies": OMEGAS, "radiating_dofs": rad,
-                                             "influenced_dofs": inf}, mh.DirectBEM(), ctx=ctx, rho=1025.0, g=9.81)
-        return float(np.sum(ab * r["added_mass"][..., 0]) + np.sum(bb * r["radiation_damping"][..., 0]))
+                                             "influenced_dofs": inf, "wave_directions": betas}, mh.DirectBEM(),
+                                         ctx=ctx, rho=1025.0, g=9.81)
+        fe = r["excitation_force"][..., 0]
+        return float(np.sum(ab * r["added_mass"][..., 0]) + np.sum(bb * r["radiation_damping"][..., 0])
+                     + np.sum(fb.real * fe.real) + np.sum(fb.imag * fe.imag))
 
-    J, grad = mh.hydro_vjp(body, OMEGAS, rad, inf, ab, bb, F, ctx=ctx, rho=1025.0, g=9.81)
+    J, grad = mh.hydro_vjp(body, OMEGAS, rad, inf, ab, bb, F, ctx=ctx, rho=1025.0, g=9.81, wave_directions=betas,
+                           excitation_force_bar=fb)
     J0 = objective(body)
     assert abs(J - J0) <= 1e-11 * np.abs(ab).sum() * 1e3 + 1e-12 * abs(J0)
     n1 = m1.nvertices
@@ -201,3 +208,33 @@ def test_vjp_with_identity_cotangents_equals_gradient(mh, ctx):
     J2, g2 = mh.hydro_vjp(body, OMEGAS, obj, obj, eye, eye, ctx=ctx, rho=1025.0, g=9.81)
     assert J1 == pytest.approx(J2, rel=1e-14)
     assert np.abs(g1 - g2).max() <= 1e-13 * np.abs(g1).max()
+
+
+def test_vjp_of_excitation_forces_alone(mh, ctx):
+    """Only excitation cotangents (no radiating dofs): the diffraction solve, the Airy
+    condition's and the Froude-Krylov pressure's dependence on the panel centres."""
+    m1, m2 = _geometry(mh)
+    dofs = ["Surge", "Heave", "Pitch"]
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
+    inf = ["c1__Surge", "c2__Heave", "c1__Pitch"]
+    betas = [0.3, 2.0]
+    rng = np.random.default_rng(23)
+    fb = rng.standard_normal((3, len(OMEGAS), 2)) + 1j * rng.standard_normal((3, len(OMEGAS), 2))
+
+    def objective(b):
+        r = mh.hydrodynamic_coefficients(b, {"wave_frequencies": OMEGAS, "influenced_dofs": inf,
+                                             "wave_directions": betas}, ctx=ctx, rho=1025.0, g=9.81)
+        fe = r["excitation_force"][..., 0]
+        return float(np.sum(fb.real * fe.real) + np.sum(fb.imag * fe.imag))
+
+    J, grad = mh.hydro_vjp(body, OMEGAS, [], inf, ctx=ctx, rho=1025.0, g=9.81, wave_directions=betas,
+                           excitation_force_bar=fb)
+    assert abs(J - objective(body)) <= 1e-11 * abs(J)
+    n1 = m1.nvertices
+    for d1, d2 in _affine_moves(m1.vertices, m2.vertices, np.random.default_rng(29)):
+        jp = objective(_body(mh, m1.vertices + H * d1, m2.vertices + H * d2, m1, m2, dofs))
+        jm = objective(_body(mh, m1.vertices - H * d1, m2.vertices - H * d2, m1, m2, dofs))
+        fd = (jp - jm) / (2 * H)
+        ad = float(np.sum(grad[:n1] * d1) + np.sum(grad[n1:] * d2))
+        scale = np.abs(grad).sum() * max(np.abs(d1).max(), np.abs(d2).max())
+        assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
