@@ -256,7 +256,7 @@ int mh_batch_release(mh_context* ctx);
 int mh_tile_table_set(mh_context* ctx, int64_t n_entries, const int64_t* n_max, const int32_t* choices);
 /* Copies the context's table out (*n_entries = its length; n_max, choices need capacity). */
 int mh_tile_table_get(mh_context* ctx, int64_t capacity, int64_t* n_max, int32_t* choices, int64_t* n_entries);
-/* The project's autotuner: for each order sizes[q] (ascending, 32..kMaxOrder) times the
+/* The project's autotuner: for each order sizes[q] (ascending, 32..12000) times the
    batched factorization of `batch` random complex matrices in `precision` with every
    candidate launch shape -- panel cluster bound 8, 4, 2 and, for the tensor-core updates,
    1, 2, 4 or 8 column tiles per CTA -- (smallest of `reps` timed runs after a warm-up,
