@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "mh_internal.cuh"
 #include "mh_mlp.cuh"
 
@@ -106,6 +108,15 @@ struct mh_mesh {
 };
 
 namespace {
+
+// One NVTX range per C-ABI call, so that timeline tools and ncu's --nvtx filters see the
+// library's phases (assembly, solves, sweeps) by name.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
@@ -850,6 +861,7 @@ int mh_set_quadrature_tolerance(mh_context* ctx, double rtol, double atol) {
 
 int mh_mesh_create(mh_context* ctx, int64_t n, const double* vertices, const double* centers, const double* normals,
                    const double* areas, const double* radii, int mem, mh_mesh** out) {
+  NvtxRange nvtx_range("mh_mesh_create");
   if (!ctx || !out) return MH_ERR_ARG;
   *out = nullptr;
   if (n <= 0) return fail(ctx, MH_ERR_ARG, "mesh needs at least one panel (got %lld)", (long long)n);
@@ -942,6 +954,7 @@ int mh_mesh_set_lid(mh_mesh* m, int64_t n_hull) {
 
 int mh_assemble_matrices(mh_context* ctx, mh_mesh* m, double k, uint32_t gfs, int direct, int include_identity,
                          const double* fixed_normal, double* S, double* D, int mem) {
+  NvtxRange nvtx_range("mh_assemble_matrices");
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (!S || !D) return fail(ctx, MH_ERR_ARG, "S and D must not be NULL");
@@ -983,6 +996,7 @@ int mh_assemble_matrices(mh_context* ctx, mh_mesh* m, double k, uint32_t gfs, in
 
 int mh_linsolve(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const double* B, double* X, int precision,
                 int mem) {
+  NvtxRange nvtx_range("mh_linsolve");
   if (!ctx) return MH_ERR_ARG;
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!A || !B || !X) return fail(ctx, MH_ERR_ARG, "A, B and X must not be NULL");
@@ -1004,6 +1018,7 @@ int mh_linsolve(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const
 
 int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* A, const double* Ybar,
                         double* Lambda, int precision, int mem) {
+  NvtxRange nvtx_range("mh_linsolve_adjoint");
   if (!ctx) return MH_ERR_ARG;
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!A || !Ybar || !Lambda) return fail(ctx, MH_ERR_ARG, "A, Ybar and Lambda must not be NULL");
@@ -1025,6 +1040,7 @@ int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* 
 
 int mh_solve(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const double* S, const double* bc, int direct,
              double* phi, double* sources, int precision, int mem) {
+  NvtxRange nvtx_range("mh_solve");
   if (!ctx) return MH_ERR_ARG;
   if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
   if (!D || !S || !bc || !phi) return fail(ctx, MH_ERR_ARG, "D, S, bc and phi must not be NULL");
@@ -1067,6 +1083,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
                                  int64_t n_beta, const double* betas, int precision, double* added_mass,
                                  double* radiation_damping, double* diffraction_force, double* froude_krylov_force,
                                  double* excitation_force, int mem) {
+  NvtxRange nvtx_range("mh_hydrodynamic_coefficients");
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
@@ -1245,6 +1262,7 @@ int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* m, int64_t n_omega, 
                                   double* diffraction_force, double* froude_krylov_force, double* excitation_force,
                                   double* d_added_mass, double* d_radiation_damping, double* d_diffraction_force,
                                   double* d_froude_krylov_force, double* d_excitation_force, int mem) {
+  NvtxRange nvtx_range("mh_hydro_frequency_derivative");
   if (!ctx) return MH_ERR_ARG;
   if (!m || m->ctx != ctx) return fail(ctx, MH_ERR_ARG, "mesh does not belong to this context");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
@@ -1585,6 +1603,7 @@ int mh_tile_table_get(mh_context* ctx, int64_t capacity, int64_t* n_max, int32_t
 
 int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* sizes, int64_t batch, int reps,
                 double* ms_best, double* ms_default) {
+  NvtxRange nvtx_range("mh_autotune");
   if (!ctx) return MH_ERR_ARG;
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC)
     return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
@@ -1706,6 +1725,7 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
                                        int64_t n_beta, const double* betas, int precision, int n_streams,
                                        double* added_mass, double* radiation_damping, double* diffraction_force,
                                        double* froude_krylov_force, double* excitation_force, int mem) {
+  NvtxRange nvtx_range("mh_batch_hydrodynamic_coefficients");
   if (!ctx) return MH_ERR_ARG;
   if (n_bodies <= 0 || !meshes || !n_omega || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one body");
   if (n_rad < 0 || n_inf < 0 || n_beta < 0 || n_dofs < 0) return fail(ctx, MH_ERR_ARG, "negative counts");
@@ -2153,6 +2173,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
                       uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem) {
+  NvtxRange nvtx_range("mh_hydro_gradient");
   if (!ctx) return MH_ERR_ARG;
   if (n_obj <= 0 || n_obj > 4 || !obj_idx) return fail(ctx, MH_ERR_ARG, "objective needs 1..4 dofs");
   if (n_omega <= 0 || !omegas) return fail(ctx, MH_ERR_ARG, "need at least one wave frequency");
@@ -2176,6 +2197,7 @@ int mh_hydro_vjp(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* ome
                  const double* added_mass_bar, const double* radiation_damping_bar, const double* excitation_force_bar,
                  int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                  double* grad_vertices, double* grad_dofs, int mem) {
+  NvtxRange nvtx_range("mh_hydro_vjp");
   if (!ctx) return MH_ERR_ARG;
   if (n_omega <= 0 || !omegas || n_rad < 0 || n_beta < 0 || n_rad + n_beta <= 0 || n_inf <= 0 || n_rad > 64 ||
       n_inf > 64 || n_beta > 64)
@@ -2287,6 +2309,7 @@ int mh_surrogate_loss_grad(mh_context* ctx, const float* params, int64_t m, cons
 
 int mh_surrogate_train(mh_context* ctx, int64_t n_samples, uint64_t seed, int epochs, int batch, double lr,
                        float* params_out, double* report) {
+  NvtxRange nvtx_range("mh_surrogate_train");
   if (!ctx) return MH_ERR_ARG;
   if (n_samples < 1024 || n_samples > ((int64_t)1 << 27)) return fail(ctx, MH_ERR_ARG, "n_samples must be in [1024, 2^27]");
   if (epochs <= 0 || batch <= 0 || batch > (1 << 16) || !(lr > 0)) return fail(ctx, MH_ERR_ARG, "bad training settings");
