@@ -192,13 +192,14 @@ class ClockSampler:
 GEMM_F64_TRAFFIC_PER_LAUNCH = 1.236e9
 
 
-def lu_gemm_flops(n, nb=32):
-    """Algorithmic real flops of the trailing updates of one n x n complex LU (8 per complex MAC)."""
+def lu_gemm_flops(n, nb=32, per_mac=8):
+    """Real flops of the trailing updates of one n x n complex LU: per_mac per complex
+    multiply-add (8 with the four-multiplication product, 6 with the 3M product)."""
     f = 0
     for k in range(0, n, nb):
         kb = min(nb, n - k)
         rest = n - k - kb
-        f += 8 * rest * rest * kb
+        f += per_mac * rest * rest * kb
     return f
 
 
@@ -357,17 +358,18 @@ def run_gpu(args):
     asm_ms = sum(v[0] for k, v in prof.items() if k.startswith("assemble"))
     roof = None
     if top_name == "lu_gemm_f64":
-        flops_per_launch = lu_gemm_flops(n) * N_OMEGA / (top_launches / args.steps)
+        flops_per_launch = lu_gemm_flops(n, per_mac=6) * N_OMEGA / (top_launches / args.steps)
         achieved = flops_per_launch / (top_ms / top_launches * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": top_name, "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                 "frac": achieved / peak64, "traffic": GEMM_F64_TRAFFIC_PER_LAUNCH,
                 "traffic_unit": "bytes per launch (DRAM read + write)",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every gemm_kernel<double> "
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every FP64 trailing-update "
                                   "launch of the same 30-frequency sweep (profiles/lu_gemm_f64_cylinder2000.md); "
                                   "algorithmic: 32 B per trailing-block entry, 1.26e9 B per launch",
                 "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks (MEASURED_PEAKS.json "
                                "has no FP64 figure)",
-                "work": "8 real flops per complex multiply-add of the trailing update, summed over panel steps"}
+                "work": "6 real flops (three FP64 FMAs, the 3M complex product) per complex multiply-add of the "
+                        "trailing update, summed over panel steps; the four-multiplication count would be 4/3 of it"}
     else:
         roof = {"bound": "fp64", "kernel": top_name, "achieved": None, "peak": peak64, "unit": "TFLOP/s",
                 "frac": None, "traffic": None}

@@ -465,6 +465,96 @@ __global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<
   }
 }
 
+// A22 -= L21 U12 in FP64 with Gauss's three-multiplication complex product (the ZGEMM3M
+// scheme): per complex multiply-add P1 += ar br, P2 += ai bi, P3 += (ar + ai)(br + bi), and
+// at the end Re = P1 - P2, Im = P3 - P1 - P2 -- three FP64 FMAs instead of four.  The sums
+// ar + ai, br + bi are formed once per element when the tiles are staged in shared memory
+// (three planes: Re, Im, Re + Im).  The product is normwise stable (its error is bounded by
+// a small multiple of the unit roundoff times |L21| |U12|), which is the property the LU's
+// backward stability rests on; componentwise the imaginary parts can differ from the
+// four-multiplication product in the last digits.
+constexpr int kG3TM = 64, kG3RM = 4, kG3KC = 16;
+constexpr size_t kG3Smem = 6 * sizeof(double) * kG3KC * (kG3TM + 1);
+
+__global__ void __launch_bounds__(256) gemm3m_kernel(BatchDesc d, double2* __restrict__ Aall, int64_t k) {
+  extern __shared__ unsigned char gemm_smem[];
+  double (*sAr)[kG3TM + 1] = reinterpret_cast<double (*)[kG3TM + 1]>(gemm_smem);
+  double (*sAi)[kG3TM + 1] = sAr + kG3KC;
+  double (*sAs)[kG3TM + 1] = sAi + kG3KC;
+  double (*sBr)[kG3TM + 1] = sAs + kG3KC;
+  double (*sBi)[kG3TM + 1] = sBr + kG3KC;
+  double (*sBs)[kG3TM + 1] = sBi + kG3KC;
+  const int64_t n = d.n;
+  double2* A = Aall + blockIdx.z * d.stride;
+  const int kb = (int)((k + kNB < n) ? kNB : n - k);
+  const int64_t base = k + kb;
+  const int64_t row0 = base + blockIdx.x * (int64_t)kG3TM;
+  const int64_t col0 = base + blockIdx.y * (int64_t)kG3TM;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double p1[kG3RM][kG3RM], p2[kG3RM][kG3RM], p3[kG3RM][kG3RM];
+#pragma unroll
+  for (int r = 0; r < kG3RM; ++r)
+#pragma unroll
+    for (int c = 0; c < kG3RM; ++c) p1[r][c] = p2[r][c] = p3[r][c] = 0.0;
+  for (int k0 = 0; k0 < kb; k0 += kG3KC) {
+    for (int idx = threadIdx.x; idx < kG3KC * kG3TM; idx += 256) {
+      const int r = idx % kG3TM, q = idx / kG3TM;
+      const int64_t gi = row0 + r;
+      const int kk = k0 + q;
+      const double2 v = (gi < n && kk < kb) ? A[gi + (k + kk) * n] : make_double2(0.0, 0.0);
+      sAr[q][r] = v.x;
+      sAi[q][r] = v.y;
+      sAs[q][r] = v.x + v.y;
+    }
+    for (int idx = threadIdx.x; idx < kG3KC * kG3TM; idx += 256) {
+      const int q = idx % kG3KC, c = idx / kG3KC;
+      const int64_t gc = col0 + c;
+      const int kk = k0 + q;
+      const double2 v = (gc < n && kk < kb) ? A[(k + kk) + gc * n] : make_double2(0.0, 0.0);
+      sBr[q][c] = v.x;
+      sBi[q][c] = v.y;
+      sBs[q][c] = v.x + v.y;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int q = 0; q < kG3KC; ++q) {
+      double ar[kG3RM], ai[kG3RM], as[kG3RM];
+#pragma unroll
+      for (int r = 0; r < kG3RM; ++r) {
+        ar[r] = sAr[q][tx + 16 * r];
+        ai[r] = sAi[q][tx + 16 * r];
+        as[r] = sAs[q][tx + 16 * r];
+      }
+#pragma unroll
+      for (int c = 0; c < kG3RM; ++c) {
+        const double br = sBr[q][ty + 16 * c], bi = sBi[q][ty + 16 * c], bs = sBs[q][ty + 16 * c];
+#pragma unroll
+        for (int r = 0; r < kG3RM; ++r) {
+          p1[r][c] = fma(ar[r], br, p1[r][c]);
+          p2[r][c] = fma(ai[r], bi, p2[r][c]);
+          p3[r][c] = fma(as[r], bs, p3[r][c]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int c = 0; c < kG3RM; ++c) {
+    const int64_t gc = col0 + ty + 16 * c;
+    if (gc >= n) continue;
+#pragma unroll
+    for (int r = 0; r < kG3RM; ++r) {
+      const int64_t gi = row0 + tx + 16 * r;
+      if (gi < n) {
+        double2 v = A[gi + gc * n];
+        v.x -= p1[r][c] - p2[r][c];
+        v.y -= p3[r][c] - p1[r][c] - p2[r][c];
+        A[gi + gc * n] = v;
+      }
+    }
+  }
+}
+
 // ------------------------------ substitution ---------------------------------
 // x_r[i] -= sum_{j in [jb, je)} M[i, j] x_r[j] for the g right-hand sides of the
 // group (M = the stored factor, or its conjugate transpose when CT); every matrix
@@ -1028,6 +1118,8 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     constexpr int TM = GemmTile<T>::TM;
     constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
     cudaFuncSetAttribute(gemm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
+    if (sizeof(T) == 8)
+      cudaFuncSetAttribute(gemm3m_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG3Smem);
   }
   for (int64_t k = 0; k < n; k += kNB) {
     const int64_t kb = (k + kNB < n) ? kNB : n - k;
@@ -1070,11 +1162,15 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
       }
       continue;
     }
-    constexpr int TM = GemmTile<T>::TM;
-    dim3 gg((unsigned)((rest + TM - 1) / TM), (unsigned)((rest + TM - 1) / TM), (unsigned)d.batch);
-    constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
-    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_gemm_f64" : "lu_gemm_f32",
-              gemm_kernel<T><<<gg, 256, gsmem, st>>>(d, A, k));
+    if constexpr (sizeof(T) == 8) {  // FP64: three real products per complex multiply-add
+      dim3 gg((unsigned)((rest + kG3TM - 1) / kG3TM), (unsigned)((rest + kG3TM - 1) / kG3TM), (unsigned)d.batch);
+      MH_LAUNCH(lc, st, "lu_gemm_f64", gemm3m_kernel<<<gg, 256, kG3Smem, st>>>(d, A, k));
+    } else {
+      constexpr int TM = GemmTile<T>::TM;
+      dim3 gg((unsigned)((rest + TM - 1) / TM), (unsigned)((rest + TM - 1) / TM), (unsigned)d.batch);
+      constexpr size_t gsmem = 2 * sizeof(typename cplx_t<T>::type) * GemmTile<T>::KC * (TM + 1);
+      MH_LAUNCH(lc, st, "lu_gemm_f32", gemm_kernel<T><<<gg, 256, gsmem, st>>>(d, A, k));
+    }
   }
   return 0;
 }
