@@ -1762,6 +1762,7 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
   for (int64_t b = 0; b < n_bodies; ++b) {
     key.push_back((double)(uintptr_t)meshes[b]);
     key.push_back((double)n_omega[b]);
+    key.push_back((double)meshes[b]->n_hull);  // the lid split is baked into the epilogue launches
   }
   for (int64_t q = 0; q < n_rad; ++q) key.push_back(rad_idx[q]);
   for (int64_t q = 0; q < n_inf; ++q) key.push_back(inf_idx[q]);
