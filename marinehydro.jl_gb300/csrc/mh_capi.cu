@@ -919,6 +919,17 @@ int mh_mesh_destroy(mh_mesh* m) {
   if (!m) return MH_OK;
   mh_context* ctx = m->ctx;
   cudaSetDevice(ctx->device);
+  // a cached batch graph that reads this mesh's buffers goes with it (the cache is keyed by
+  // mesh address, which a later mesh may reuse)
+  if (ctx->batch) {
+    bool uses = false;
+    for (const BodyPlan& b : ctx->batch->bodies) uses = uses || b.m == m;
+    if (uses) {
+      cudaStreamSynchronize(ctx->stream);
+      delete ctx->batch;
+      ctx->batch = nullptr;
+    }
+  }
   if (m->SR) cudaFreeAsync(m->SR, ctx->stream);
   if (m->DR) cudaFreeAsync(m->DR, ctx->stream);
   if (m->V) cudaFreeAsync(m->V, ctx->stream);

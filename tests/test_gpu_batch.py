@@ -48,3 +48,17 @@ def test_batch_rejects_mixed_dof_names(mh, ctx):
     with pytest.raises(ValueError):
         mh.batch_hydrodynamic_coefficients(b, [{"wave_frequencies": [1.0], "radiating_dofs": ["Heave"]}] * 3,
                                            ctx=ctx)
+
+
+def test_batch_after_a_mesh_is_destroyed(mh, ctx):
+    """The cached batch graph is keyed by mesh addresses; destroying a mesh drops the graph,
+    so a new mesh (possibly at the same address) is never served the old one's buffers."""
+    p = {"wave_frequencies": [0.8, 1.5], "radiating_dofs": ["Heave"]}
+    for q in range(4):
+        body = mh.FloatingBody(mh.hemisphere_mesh(1.0 + 0.3 * q, 5, 10), ["Heave"])
+        out = mh.batch_hydrodynamic_coefficients([body], [p], ctx=ctx, rho=1025.0)
+        ref = mh.hydrodynamic_coefficients(body, p, ctx=ctx, rho=1025.0)
+        assert np.abs(out[0]["added_mass"] - ref["added_mass"]).max() <= 1e-12 * np.abs(ref["added_mass"]).max()
+        for h in list(body.mesh._handles.values()):
+            h.close()
+        body.mesh._handles.clear()

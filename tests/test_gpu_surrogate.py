@@ -37,7 +37,7 @@ def _torch_loss_grad(params, x, y):
     out = h @ W4.T + b4
     loss = ((out - Y) ** 2).mean()
     loss.backward()
-    return float(loss), p.grad.numpy().astype(np.float64)
+    return float(loss.detach()), p.grad.numpy().astype(np.float64)
 
 
 def _bf16(a):
