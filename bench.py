@@ -61,6 +61,18 @@ def dist_info():
     return ws, rank, local
 
 
+def max_over_ranks(x, device=None):
+    """The largest value of x over the ranks of the process group (x itself on one rank):
+    every rank times its own replica, the job's time is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def batch_workload(mh, seed=2026, n_bodies=64, n_omega=16):
     """64 seeded bodies (spheres r in [0.5,5] m, vertical cylinders, barges L/B in [2,6]), panel counts
     log-uniform in [300, 4000], 16 frequencies log-uniform in [0.3, 2.5] rad/s each, heave + pitch."""
@@ -296,9 +308,7 @@ def run_gpu(args):
             ctx.profile(False)
         torch.cuda.synchronize(dev)
         if ws > 1:
-            t = torch.tensor([tot], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
+            tot = max_over_ranks(tot, dev)
             dist.barrier()
         return tot, wall, launches, prof
 
