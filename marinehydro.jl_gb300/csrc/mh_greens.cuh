@@ -311,44 +311,67 @@ __device__ inline void wu_sd(const double x[3], const double xi[3], const double
 }
 
 // ------------------------- exact Guevel-Delhommeau --------------------------
+// 1/n for the power series of E1 (every entry the correctly rounded quotient, as 1.0 / n)
+struct InvN {
+  double v[400];
+};
+__constant__ static const InvN kInvN = [] {
+  InvN t{};
+  for (int n = 1; n < 400; ++n) t.v[n] = 1.0 / (double)n;
+  return t;
+}();
+
+// a / b for a real numerator: a conj(b) / |b|^2, one division (|b| stays far inside the
+// FP64 range in the continued fraction below: its terms are b_i = z + 2i + 1 and their
+// quotients)
+__device__ __forceinline__ double2 rdivz(double a, double2 b) {
+  const double s = a / (b.x * b.x + b.y * b.y);
+  return make_double2(b.x * s, -b.y * s);
+}
+
 // e^z E1(z): power series of E1 (DLMF 6.6.2) where its cancellation loss
 // exp(|z| + Re z) is below e^4, else the even continued fraction of DLMF 6.9.1
-// by the modified Lentz method.  Iteration counts are bounded.
-__device__ inline double2 exp_e1(double2 z) {
-  double az = hypot(z.x, z.y);
+// by the modified Lentz method.  Iteration counts are bounded.  `ez` = e^z (the
+// integrands have it already).  Convergence and underflow tests compare squared
+// magnitudes (no hypot in the loops); 1/n comes from a table.
+__device__ inline double2 exp_e1(double2 z, double2 ez) {
+  const double az = hypot(z.x, z.y);
   if (az + z.x < 4.0) {
     double2 term = make_double2(1.0, 0.0), sum = make_double2(0.0, 0.0);
-    double2 mz = make_double2(-z.x, -z.y);
+    const double2 mz = make_double2(-z.x, -z.y);
     for (int n = 1; n < 400; ++n) {
-      term = zscale(1.0 / (double)n, zmul(term, mz));
-      double2 add = zscale(1.0 / (double)n, term);
+      const double inv = kInvN.v[n];
+      term = zscale(inv, zmul(term, mz));
+      const double2 add = zscale(inv, term);
       sum = zadd(sum, add);
-      if (hypot(add.x, add.y) <= 1e-17 * hypot(sum.x, sum.y)) break;
+      if (add.x * add.x + add.y * add.y <= 1e-34 * (sum.x * sum.x + sum.y * sum.y)) break;
     }
     const double euler_gamma = 0.57721566490153286061;
-    double2 lz = zlog(z);
-    double2 e1 = make_double2(-euler_gamma - lz.x - sum.x, -lz.y - sum.y);
-    return zmul(zexp(z), e1);
+    const double2 lz = make_double2(log(az), atan2(z.y, z.x));
+    const double2 e1 = make_double2(-euler_gamma - lz.x - sum.x, -lz.y - sum.y);
+    return zmul(ez, e1);
   }
   const double tiny = 1e-300;
   double2 b = make_double2(z.x + 1.0, z.y);
   double2 f = b;
   double2 C = f, D = make_double2(0.0, 0.0);
   for (int i = 1; i < 400; ++i) {
-    double a = -(double)i * (double)i;
+    const double a = -(double)i * (double)i;
     b.x += 2.0;
     D = make_double2(b.x + a * D.x, b.y + a * D.y);
-    if (hypot(D.x, D.y) < tiny) D = make_double2(tiny, 0.0);
-    double2 q = zdiv(make_double2(a, 0.0), C);
+    if (fabs(D.x) + fabs(D.y) < tiny) D = make_double2(tiny, 0.0);
+    const double2 q = rdivz(a, C);
     C = make_double2(b.x + q.x, b.y + q.y);
-    if (hypot(C.x, C.y) < tiny) C = make_double2(tiny, 0.0);
-    D = zdiv(make_double2(1.0, 0.0), D);
-    double2 delta = zmul(C, D);
+    if (fabs(C.x) + fabs(C.y) < tiny) C = make_double2(tiny, 0.0);
+    D = rdivz(1.0, D);
+    const double2 delta = zmul(C, D);
     f = zmul(f, delta);
-    if (hypot(delta.x - 1.0, delta.y) < 1e-16) break;
+    const double dx = delta.x - 1.0;
+    if (dx * dx + delta.y * delta.y < 1e-32) break;
   }
   return zdiv(make_double2(1.0, 0.0), f);
 }
+__device__ inline double2 exp_e1(double2 z) { return exp_e1(z, zexp(z)); }
 
 // integrands of _dimless_wave_term / _d_dimless_wave_term_dr
 // (exact_Guevel_Delhommeau.jl:16-23, 36-43)
@@ -357,7 +380,7 @@ __device__ __forceinline__ double2 egd_integrand(double theta, double r, double 
   double ct = cos(theta);
   double2 zeta = make_double2(z, r * ct);
   double2 ez = zexp(zeta);
-  double2 g = exp_e1(zeta);
+  double2 g = exp_e1(zeta, ez);
   // j = e^zeta (E1(zeta)/pi + i) = g/pi + i e^zeta
   double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
   if (!DR) return make_double2(j.x, ez.x);
@@ -475,7 +498,7 @@ __device__ __forceinline__ void egd_integrands(double theta, double r, double z,
   const double ct = cos(theta);
   const double2 zeta = make_double2(z, r * ct);
   const double2 ez = zexp(zeta);
-  const double2 g = exp_e1(zeta);
+  const double2 g = exp_e1(zeta, ez);
   const double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
   f[0] = j.x;
   f[1] = ez.x;
