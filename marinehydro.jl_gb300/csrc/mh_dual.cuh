@@ -72,9 +72,12 @@ template <int M> __device__ __forceinline__ Dn<M> operator*(const Dn<M>& a, cons
   for (int q = 0; q < M; ++q) r.d[q] = a.d[q] * b.v + a.v * b.d[q];
   return r;
 }
+// Divisions take one FP64 reciprocal (a multi-instruction sequence on the FP64 pipe) and
+// multiply by it; the value is then within an ulp of the correctly rounded quotient, which
+// is immaterial for the derivatives these kernels produce.
 template <int M> __device__ __forceinline__ Dn<M> operator/(const Dn<M>& a, const Dn<M>& b) {
   const double inv = 1.0 / b.v, rv = a.v * inv;
-  Dn<M> r(a.v / b.v);
+  Dn<M> r(rv);
 #pragma unroll
   for (int q = 0; q < M; ++q) r.d[q] = (a.d[q] - rv * b.d[q]) * inv;
   return r;
@@ -85,9 +88,13 @@ template <int M> __device__ __forceinline__ Dn<M> operator-(const Dn<M>& a, doub
 template <int M> __device__ __forceinline__ Dn<M> operator-(double b, const Dn<M>& a) { return chain1(a, b - a.v, -1.0); }
 template <int M> __device__ __forceinline__ Dn<M> operator*(const Dn<M>& a, double b) { return chain1(a, a.v * b, b); }
 template <int M> __device__ __forceinline__ Dn<M> operator*(double b, const Dn<M>& a) { return chain1(a, b * a.v, b); }
-template <int M> __device__ __forceinline__ Dn<M> operator/(const Dn<M>& a, double b) { return chain1(a, a.v / b, 1.0 / b); }
+template <int M> __device__ __forceinline__ Dn<M> operator/(const Dn<M>& a, double b) {
+  const double inv = 1.0 / b;
+  return chain1(a, a.v * inv, inv);
+}
 template <int M> __device__ __forceinline__ Dn<M> operator/(double b, const Dn<M>& a) {
-  return chain1(a, b / a.v, -b / (a.v * a.v));
+  const double inv = 1.0 / a.v, rv = b * inv;
+  return chain1(a, rv, -rv * inv);
 }
 template <int M> __device__ __forceinline__ Dn<M>& operator+=(Dn<M>& a, const Dn<M>& b) { a = a + b; return a; }
 template <int M> __device__ __forceinline__ Dn<M>& operator-=(Dn<M>& a, const Dn<M>& b) { a = a - b; return a; }
