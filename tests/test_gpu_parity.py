@@ -1,6 +1,6 @@
 """CUDA path vs the CPU oracle, through the C-ABI (libmarinehydro_cuda.so).
 
-Tolerances (the spec parity bar): S, D relative error <= 1e-10 (Frobenius
+Tolerances (the parity bar of the plain FP64 path): S, D relative error <= 1e-10 (Frobenius
 norm over the matrix); added mass, damping and excitation force <= 1e-8.
 """
 import numpy as np
