@@ -219,19 +219,25 @@ __device__ __forceinline__ double wu_A(double t) {
 __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& J0, double& J1) {
   double Y0, Y1;
   bessel01(xx, J0, J1, Y0, Y1);
+  // FP64 division is a multi-instruction sequence on the FP64 pipe: x / 3 is taken as
+  // x * (1/3) and the two rational fits share one reciprocal (changes of an ulp, far below
+  // the fits' own 1e-9 accuracy)
   if (xx <= 3.0) {
-    double yy = (xx / 3.0) * (xx / 3.0);
+    const double x3 = xx * (1.0 / 3.0);
+    double yy = x3 * x3;
     double h0 = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
-    H0 = h0 * (xx / 3.0);
+    H0 = h0 * x3;
     H1 = (1.909859286 + (-1.145914713 + (0.294656958 + (-0.042070508 + (0.003785727 + -0.000207183 * yy) * yy) * yy) * yy) * yy) * yy;
   } else {
-    double yy = (3.0 / xx) * (3.0 / xx);
+    const double t = 3.0 / xx;
+    double yy = t * t;
     double c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
     double c2 = kPi * xx * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
-    H0 = c1 / c2 + Y0;
     double d1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
     double d2 = kPi * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
-    H1 = d1 / d2 + Y1;
+    const double inv = 1.0 / (c2 * d2);
+    H0 = c1 * d2 * inv + Y0;
+    H1 = d1 * c2 * inv + Y1;
   }
 }
 
