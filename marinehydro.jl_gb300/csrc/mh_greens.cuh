@@ -243,15 +243,22 @@ __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& 
 
 // _wu_wave_term_and_derivs (wu.jl:28-37) with GF_Func_L0/Lp/W/Ls/Lsp/Wh (wu.jl:201-366)
 // FP64 division is a multi-instruction sequence on GB300's FP64 pipe, which bounds this
-// kernel; 1/dd and 1/(1 + dd^3) are formed once and multiplied (rho stays a true division:
-// it feeds the fits A-D, whose alternating coefficients up to 2e5 amplify its last bit).
+// kernel; 1/dd, 1/(dd - vv) and 1/(1 + dd^3) come from one division and are multiplied
+// (rho stays a true division: it feeds the fits A-D, whose alternating coefficients up to
+// 2e5 amplify its last bit).
 __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv) {
   double dd = sqrt(hh * hh + vv * vv);
-  const double inv_dd = 1.0 / dd;
+  double dd2 = dd * dd, dd3 = dd * dd * dd;
+  // 1/dd, 1/(dd - vv) and 1/(1 + dd^3) from one division of their product (all three
+  // factors are positive, dd - vv >= dd >= 0 with vv <= 0, and moderate)
+  const double dmv = dd - vv, opd3 = 1.0 + dd3;
+  const double inv_all = 1.0 / (dd * dmv * opd3);
+  const double inv_dd = dmv * opd3 * inv_all;
+  const double inv_dmv = dd * opd3 * inv_all;
+  const double inv_1dd3 = dd * dmv * inv_all;
   double alpha = -vv * inv_dd;
   double beta = hh * inv_dd;
   double rho = dd / (1 + dd);
-  double dd2 = dd * dd, dd3 = dd * dd * dd;
   double omr = 1.0 - rho;
   double omr3 = omr * omr * omr;
   double ev = exp(vv);
@@ -268,7 +275,6 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   double PP = log(0.5 * (dd - vv)) + gama - 2.0 * dd2;
   PP = ev * PP;
   PP = PP + dd2 - vv;
-  const double inv_1dd3 = 1.0 / (1.0 + dd3);
   double L0 = 2.0 * PP * inv_1dd3 + 2.0 * Lp;
   const double twopi = 2 * kPi;
   GF = make_double2(-L0 - (twopi * H0) * ev, -((twopi * -J0) * ev));
@@ -278,7 +284,7 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   RS += beta * (1.0 - beta) * rho * (1.0 - 2.0 * rho) * wu_dC(rho);
   double Lsp = rho * omr3 * RS;
   // GF_Func_Ls
-  double PS = (beta + hh) / (dd - vv);
+  double PS = (beta + hh) * inv_dmv;
   PS = PS - 2.0 * beta + 2.0 * ev * dd - hh;
   double QS = exp(-dd) * (1.0 - beta);
   QS = QS * (1.0 + dd * inv_1dd3);
