@@ -381,7 +381,7 @@ __device__ inline double2 exp_e1(double2 z, double2 ez) {
     const double dx = delta.x - 1.0;
     if (dx * dx + delta.y * delta.y < 1e-32) break;
   }
-  return zdiv(make_double2(1.0, 0.0), f);
+  return rdivz(1.0, f);
 }
 __device__ inline double2 exp_e1(double2 z) { return exp_e1(z, zexp(z)); }
 
@@ -394,9 +394,10 @@ __device__ __forceinline__ double2 egd_integrand(double theta, double r, double 
   double2 ez = zexp(zeta);
   double2 g = exp_e1(zeta, ez);
   // j = e^zeta (E1(zeta)/pi + i) = g/pi + i e^zeta
-  double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
+  const double inv_pi = 1.0 / kPi;
+  double2 j = make_double2(g.x * inv_pi - ez.y, g.y * inv_pi + ez.x);
   if (!DR) return make_double2(j.x, ez.x);
-  double2 inv = zdiv(make_double2(1.0, 0.0), make_double2(kPi * zeta.x, kPi * zeta.y));
+  double2 inv = rdivz(inv_pi, zeta);  // 1 / (pi zeta); |zeta| >= -z > 0 below the free surface
   double2 w = make_double2(j.x - inv.x, j.y - inv.y);
   // Re(i ct w) = -ct Im(w); Re(i ct e^zeta) = -ct Im(e^zeta)
   return make_double2(-ct * w.y, -ct * ez.y);
@@ -511,10 +512,11 @@ __device__ __forceinline__ void egd_integrands(double theta, double r, double z,
   const double2 zeta = make_double2(z, r * ct);
   const double2 ez = zexp(zeta);
   const double2 g = exp_e1(zeta, ez);
-  const double2 j = make_double2(g.x / kPi - ez.y, g.y / kPi + ez.x);
+  const double inv_pi = 1.0 / kPi;
+  const double2 j = make_double2(g.x * inv_pi - ez.y, g.y * inv_pi + ez.x);
   f[0] = j.x;
   f[1] = ez.x;
-  const double2 inv = zdiv(make_double2(1.0, 0.0), make_double2(kPi * zeta.x, kPi * zeta.y));
+  const double2 inv = rdivz(inv_pi, zeta);  // 1 / (pi zeta); |zeta| >= -z > 0 below the free surface
   const double2 w = make_double2(j.x - inv.x, j.y - inv.y);
   f[2] = -ct * w.y;
   f[3] = -ct * ez.y;
