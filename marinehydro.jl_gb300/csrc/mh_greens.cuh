@@ -97,11 +97,13 @@ __device__ inline void vrankine_from_geom(const double pt[3], const PanelRec& P,
   double rb0 = pt[0] - P.c[0], rb1 = pt[1] - P.c[1], rb2 = pt[2] - P.c[2];
   double r = sqrt(rb0 * rb0 + rb1 * rb1 + rb2 * rb2);
   if (r > 7 * P.radius) {
-    double r3 = r * r * r;
-    phi = P.area / r;
-    g[0] = (rb0 / r3) * P.area;
-    g[1] = (rb1 / r3) * P.area;
-    g[2] = (rb2 / r3) * P.area;
+    // a/r and a r_vec/r^3 from one FP64 division (within an ulp or two of the quotients)
+    const double inv_r = 1.0 / r;
+    const double s = P.area * inv_r * inv_r * inv_r;
+    phi = P.area * inv_r;
+    g[0] = rb0 * s;
+    g[1] = rb1 * s;
+    g[2] = rb2 * s;
     return;
   }
   double d0 = pt[0] - P.qgc[0], d1 = pt[1] - P.qgc[1], d2 = pt[2] - P.qgc[2];
