@@ -93,7 +93,10 @@ __global__ void panel_geometry_kernel(int64_t n, const double* __restrict__ V, c
   }
   P.area = A[j];
   P.radius = R[j];
-  P.pad[0] = P.pad[1] = P.pad[2] = P.pad[3] = 0.0;
+  for (int k = 0; k < 4; ++k) {  // the same expression the Birk integral evaluated per pair
+    const int kn = (k + 1) & 3;
+    P.edge[k] = hypot(P.lc[2 * kn] - P.lc[2 * k], P.lc[2 * kn + 1] - P.lc[2 * k + 1]);
+  }
   out[j] = P;
 }
 

@@ -52,9 +52,10 @@ __device__ __forceinline__ double atan_ratio(double num, double den) {
   return atan2(flipped, abs_ad(den));
 }
 
-// birk_phi_and_velocity (rankine_vectorized.jl:241-267); lc = 4 local corners (x, y)
-__device__ inline void birk_phi_and_velocity(double x, double y, double z, const double* lc, double& phi,
-                                             double v[3]) {
+// birk_phi_and_velocity (rankine_vectorized.jl:241-267); lc = 4 local corners (x, y),
+// edge = their 4 edge lengths (per panel, precomputed; the same hypot of the corner offsets)
+__device__ inline void birk_phi_and_velocity(double x, double y, double z, const double* lc, const double* edge,
+                                             double& phi, double v[3]) {
   double sx[4], sy[4], r[4], e[4], h[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -71,7 +72,7 @@ __device__ inline void birk_phi_and_velocity(double x, double y, double z, const
     const int kn = (k + 1) & 3;
     double dx = lc[2 * kn] - lc[2 * k];
     double dy = lc[2 * kn + 1] - lc[2 * k + 1];
-    double dk = hypot(dx, dy);
+    const double dk = edge[k];
     if (!(dk <= kBirkDkTol)) {
       double rsum = r[k] + r[kn];
       double log_term = log((rsum - dk) / (rsum + dk));
@@ -111,7 +112,7 @@ __device__ inline void vrankine_from_geom(const double pt[3], const PanelRec& P,
   double fy = P.T[3] * d0 + P.T[4] * d1 + P.T[5] * d2;
   double fz = P.T[6] * d0 + P.T[7] * d1 + P.T[8] * d2;
   double phb, vl[3];
-  birk_phi_and_velocity(fx, fy, fz, P.lc, phb, vl);
+  birk_phi_and_velocity(fx, fy, fz, P.lc, P.edge, phb, vl);
 #pragma unroll
   for (int i = 0; i < 3; ++i) g[i] = kFourPi * (P.T[i] * vl[0] + P.T[3 + i] * vl[1] + P.T[6 + i] * vl[2]);
   phi = -kFourPi * phb;

@@ -27,7 +27,7 @@ struct __align__(16) PanelRec {
   double n[3];      // mesh normal
   double area;      // mesh area
   double radius;    // mesh radius
-  double pad[4];
+  double edge[4];   // lengths of the local edges, corner k to corner k+1 (Birk integral)
 };
 static_assert(sizeof(PanelRec) == 256, "PanelRec layout");
 
