@@ -4,7 +4,7 @@ Mirrors (names, argument meaning, errors):
   assemble_matrices(gfs, mesh, k; direct, include_identity, all_normals)   matrix_assembly.jl:164-222
   linsolve(A, b) / gpu_linsolve                                            matrix_assembly.jl:396-434
   solve(D, S, bc; direct) -> (phi, sources)                                matrix_assembly.jl:436-449
-  solve(problem, formulation)                                              solve.jl:183-214
+  solve(problem, formulation)                                              solve.jl:47-65
   radiation_bc / airy_bc / integrate_pressure / froude_krylov_force       waves.jl:154-303
   problems_from_data / hydrodynamic_coefficients                          problems_and_results.jl:242-495
 Assembly and dense solves always run on the GPU; there is no CPU fallback.  The

@@ -10,14 +10,14 @@ ROTATIONS = ("Roll", "Pitch", "Yaw")
 
 
 def translational_dofs(mesh: StaticArraysMesh, name: str) -> np.ndarray:
-    """translational_dofs (bodies.jl:382-394): a unit vector on every panel."""
+    """translational_dofs (bodies.jl:74-86): a unit vector on every panel."""
     dof = np.zeros((mesh.nfaces, 3))
     dof[:, TRANSLATIONS.index(name)] = 1.0
     return dof
 
 
 def rotational_dofs(mesh: StaticArraysMesh, name: str, rotation_center=(0.0, 0.0, 0.0)) -> np.ndarray:
-    """rotational_dofs (bodies.jl:411-426): axis x (center_i - rotation_center)."""
+    """rotational_dofs (bodies.jl:103-118): axis x (center_i - rotation_center)."""
     if name not in ROTATIONS:
         raise ValueError(f"unknown rotational dof {name}")
     axis = np.zeros(3)
@@ -26,7 +26,7 @@ def rotational_dofs(mesh: StaticArraysMesh, name: str, rotation_center=(0.0, 0.0
 
 
 def evaluate_gradient_of_motion(mesh: StaticArraysMesh, name: str) -> np.ndarray:
-    """evaluate_gradient_of_motion (bodies.jl:363-374), forward-speed problems only."""
+    """evaluate_gradient_of_motion (bodies.jl:54-66), forward-speed problems only."""
     if name not in TRANSLATIONS + ROTATIONS:
         raise ValueError("forward speed problems are only developed for rigid body dofs")
     d = np.zeros((mesh.nfaces, 3))
@@ -105,7 +105,7 @@ class FloatingBody:
 
 
 def _unique_names(names):
-    """make_body_name_list_unique (bodies.jl:446-469)."""
+    """make_body_name_list_unique (bodies.jl:138-163)."""
     seen, out = {}, []
     for s in names:
         if s not in seen:
@@ -124,7 +124,7 @@ def _unique_names(names):
 
 
 def combine_floatingbodies(bodies, new_body_name: str | None = None) -> FloatingBody:
-    """combine_floatingbodies (bodies.jl:473-525): one mesh, dofs named body__dof, zero on other bodies."""
+    """combine_floatingbodies (bodies.jl:165-225): one mesh, dofs named body__dof, zero on other bodies."""
     names = _unique_names([b.body_name.replace(" ", "_") for b in bodies])
     mesh = combine_meshes([b.mesh for b in bodies])
     total = mesh.nfaces

@@ -4,7 +4,7 @@
 //   radiation  bc_i = -i omega (n_i . dof_i)                 waves.jl:183-199, 203-211
 //   diffraction bc_i = -(v_airy(c_i) . n_i)                   waves.jl:266-282
 // Forces: F = sum_i p_i * -(dof_i . n_i) * a_i with p = i rho omega phi
-//   (solve.jl:183-191, waves.jl:154-178); Froude-Krylov with the Airy pressure
+//   (solve.jl:47-55, waves.jl:154-178); Froude-Krylov with the Airy pressure
 //   (waves.jl:259-264, 294-303).
 // Lid panels (index >= n_hull, irregular-frequency removal): the hull boundary
 //   conditions are padded with zeros there and only hull pressures enter the

@@ -296,7 +296,7 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   dGv = make_double2(GF.x + 2 * inv_dd, GF.y);
 }
 
-// _wu_reduced_hh_vv (wu.jl:7-18) == with_reduced_coordinates (abstract_greens_function.jl:192-213)
+// _wu_reduced_hh_vv (wu.jl:7-18) == with_reduced_coordinates (abstract_greens_function.jl:117-138)
 __device__ __forceinline__ void reduced_coords(const double x[3], const double xi[3], double k, double& hh,
                                                double& vv) {
   double d2 = (x[0] - xi[0]) * (x[0] - xi[0]) + (x[1] - xi[1]) * (x[1] - xi[1]);
@@ -659,7 +659,7 @@ __device__ inline void egd_warp(double r, double z, double rtol, double atol, do
 
 // both_greens_and_gradient_greens(::ExactGuevelDelhommeau) with
 // with_reduced_coordinates_derivative (exact_Guevel_Delhommeau.jl:52-59;
-// abstract_greens_function.jl:215-260); outputs already multiplied by the area
+// abstract_greens_function.jl:140-185); outputs already multiplied by the area
 // (integral / integral_gradient, exact_Guevel_Delhommeau.jl:61-69).
 __device__ inline void egd_integrals(const double x[3], const double xi[3], double k, double area, int wrt_first,
                                      double rtol, double atol, double2& I, double2 g[3]) {

@@ -95,7 +95,7 @@ def gf_flags(gfs) -> int:
 
 
 def default_greens_functions(gf: str = "Wu"):
-    """default_greens_functions (formulations.jl:241-250)."""
+    """default_greens_functions (formulations.jl:22-30)."""
     if gf == "Wu":
         wave = GFWu()
     elif gf == "ExactGuevelDelhommeau":
@@ -130,12 +130,12 @@ class BEMFormulation:
 
 
 class DirectBEM(BEMFormulation):
-    """DirectBEM{G} (formulations.jl:226-230)."""
+    """DirectBEM{G} (formulations.jl:7-11)."""
     direct = True
 
 
 class IndirectBEM(BEMFormulation):
-    """IndirectBEM{G} (formulations.jl:232-236)."""
+    """IndirectBEM{G} (formulations.jl:13-17)."""
     direct = False
 
 
@@ -144,7 +144,7 @@ def is_direct(f: BEMFormulation) -> bool:
 
 
 def bem_formulation(formulation=None, direct=True, gf="Wu", greens_functions=None):
-    """bem_formulation (formulations.jl:252-256)."""
+    """bem_formulation (formulations.jl:33-37)."""
     if formulation is not None:
         return formulation
     gfs = default_greens_functions(gf) if greens_functions is None else greens_functions

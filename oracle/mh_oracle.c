@@ -518,7 +518,7 @@ void or_wu_wave_term_and_derivs(double hh, double vv, double* GF, double* dGF_dh
 }
 
 /* _wu_reduced_hh_vv (wu.jl:7-18); the same reduction as with_reduced_coordinates
-   (abstract_greens_function.jl:192-213) */
+   (abstract_greens_function.jl:117-138) */
 static inline void reduced_coords(const double* x, const double* xi, double k, double* hh, double* vv) {
     double d2 = (x[0] - xi[0]) * (x[0] - xi[0]) + (x[1] - xi[1]) * (x[1] - xi[1]);
     const double purt = 1e-18;
@@ -713,7 +713,7 @@ void or_egd_dimless_dr(double r, double z, double rtol, double atol, double* dG)
     dG[0] = creal(v); dG[1] = cimag(v);
 }
 
-/* with_reduced_coordinates(_derivative) (abstract_greens_function.jl:192-260) with
+/* with_reduced_coordinates(_derivative) (abstract_greens_function.jl:117-185) with
    both_greens_and_gradient_greens(::ExactGuevelDelhommeau) (exact_Guevel_Delhommeau.jl:52-59) */
 static void egd_greens_and_gradient(const double* x, const double* xi, double k, int wrt_first, int want_grad,
                                     cplx* G, cplx* grad) {

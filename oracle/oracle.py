@@ -364,7 +364,7 @@ def encountered_values(omega, beta, forward_speed, g=9.81):
 
 
 def gradient_of_motion(n, dof_name):
-    """evaluate_gradient_of_motion (bodies.jl:363-374): d(dof)/dx for rigid dofs."""
+    """evaluate_gradient_of_motion (bodies.jl:54-66): d(dof)/dx for rigid dofs."""
     d = np.zeros((n, 3))
     if dof_name == "Pitch":
         d[:, 2] = 1.0

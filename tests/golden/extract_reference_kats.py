@@ -9,9 +9,15 @@ their hard-coded expected values are transcribed mechanically:
                                   element pair, Wu-vs-Delhommeau tolerance
   test/consistency_with_analytical_solutions.jl
                                   Hulme (1982) heaving-hemisphere added mass / damping
+  src/green_functions/wu.jl       every numeric constant of the Liang-Wu-Noblesse fits
+                                  GF_FuncA-D, GF_dFuncA-C, the Struve fits StruveH0/H1
+                                  and Euler's constant of GF_Func_L0, as written there
+  every .jl / .toml / .ipynb file the line count (so that file:line citations in this
+                                  repository can be checked without the reference tree)
 
-Usage:  python tests/golden/extract_reference_kats.py [REFERENCE_ROOT]
-(default REFERENCE_ROOT = /root/reference).  Writes tests/golden/reference_kats.json.
+Usage:  python tests/golden/extract_reference_kats.py REFERENCE_ROOT
+where REFERENCE_ROOT is the root of a MarineHydro.jl checkout.  Writes
+tests/golden/reference_kats.json.
 """
 from __future__ import annotations
 
@@ -140,14 +146,66 @@ def extract(root: str) -> dict:
         "A": _eval(re.search(r"A_heave = (\[[^\]]*\])", blk).group(1)),
         "B": _eval(re.search(r"B_heave = (\[[^\]]*\])", blk).group(1)),
         "g_for_omega": 9.8, "rho": 1025.0, "radius": 1.0, "rtol": 0.1,
-        "citation": "Hulme 1982, J. Fluid Mech. 121:443-463 (test/consistency_with_analytical_solutions.jl:355-379)",
+        "citation": "Hulme 1982, J. Fluid Mech. 121:443-463 (test/consistency_with_analytical_solutions.jl:52-76)",
     }
     return out
 
 
+WU_FUNCTIONS = ("GF_dFuncC", "GF_dFuncB", "GF_dFuncA", "GF_FuncD", "GF_FuncC", "GF_FuncB", "GF_FuncA",
+                "StruveH0", "StruveH1", "GF_Func_L0")
+
+
+def _julia_function(src: str, name: str) -> str:
+    """Body of `@inline function name(...)` up to its matching `end` (keywords counted per line)."""
+    m = re.search(r"^[ \t]*(?:@inline[ \t]+)?function[ \t]+" + re.escape(name) + r"\(", src, re.M)
+    if not m:
+        raise ValueError(f"function {name} not found")
+    lines = src[m.start():].split("\n")
+    depth, out = 0, []
+    for line in lines:
+        code = re.sub(r"#.*", "", line)
+        depth += len(re.findall(r"\b(?:function|if|for|while|begin|let)\b", code))
+        depth -= len(re.findall(r"\bend\b", code))
+        out.append(line)
+        if depth <= 0:
+            return "\n".join(out)
+    raise ValueError(f"unterminated function {name}")
+
+
+def extract_wu_constants(root: str) -> dict:
+    """Every `NAME = literal` assignment of the fit functions of wu.jl, in source order,
+    with the literal kept as written (the tests parse it to the same double)."""
+    src = open(os.path.join(root, "src", "green_functions", "wu.jl")).read()
+    lit = re.compile(r"^\s*([A-Za-z]\w*)\s*=\s*([-+]?\d+\.\d*(?:[eE][-+]?\d+)?)\s*$")
+    out = {}
+    for name in WU_FUNCTIONS:
+        body = _julia_function(src, name)
+        out[name] = [[m.group(1), m.group(2)] for m in map(lit.match, body.split("\n")) if m]
+        if not out[name]:
+            raise ValueError(f"no constants found in {name}")
+    return out
+
+
+def reference_line_counts(root: str) -> dict:
+    counts = {}
+    for d, _, files in os.walk(root):
+        if os.path.basename(d).startswith("."):
+            continue
+        for f in files:
+            if f.endswith((".jl", ".toml", ".ipynb")):
+                p = os.path.join(d, f)
+                with open(p, errors="replace") as fh:
+                    counts[os.path.relpath(p, root)] = sum(1 for _ in fh)
+    return dict(sorted(counts.items()))
+
+
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_reference_kats.py REFERENCE_ROOT")
+    root = sys.argv[1]
     data = extract(root)
+    data["wu_constants"] = extract_wu_constants(root)
+    data["reference_files"] = reference_line_counts(root)
     path = os.path.join(HERE, "reference_kats.json")
     with open(path, "w") as f:
         json.dump(data, f, indent=1)

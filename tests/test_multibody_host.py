@@ -1,4 +1,4 @@
-"""combine_floatingbodies / `+` (bodies.jl:165-225, 446-469): host logic, CPU only."""
+"""combine_floatingbodies / `+` (bodies.jl:138-225): host logic, CPU only."""
 import numpy as np
 
 

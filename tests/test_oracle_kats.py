@@ -86,7 +86,7 @@ def test_delhommeau_green_function_pair(oracle, kats):
 
 
 def test_wu_matches_delhommeau(oracle, kats):
-    """greens_function.jl:101-104: Wu approximates the exact term within 2e-2."""
+    """greens_function.jl:96-99: Wu approximates the exact term within 2e-2."""
     cp = kats["canonical_pair"]
     for k in cp["wu_vs_delhommeau_k"]:
         for wrt in (False,):
