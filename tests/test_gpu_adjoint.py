@@ -75,6 +75,37 @@ def test_gradient_matches_finite_differences(mh, ctx, gf, obj):
         assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
 
 
+def _oracle_objective(oracle, body, obj):
+    J = 0.0
+    for om in OMEGAS:
+        A, B, _, _, _ = oracle.hydro_one_frequency(body.mesh, body.dofs, om, rho=1025.0, g=9.81, radiating=obj,
+                                                   influenced=obj)
+        J += float(np.trace(A) + np.trace(B))
+    return J
+
+
+@pytest.mark.parametrize("obj", [["c1__Heave", "c2__Heave"], ["c1__Pitch", "c2__Heave"]])
+def test_gradient_matches_oracle_finite_differences(mh, oracle, ctx, obj):
+    """The device adjoint against central differences of the CPU oracle (not of the device sweep):
+    the two-cylinder mesh of 120 panels, the same affine moves, h = 1e-6."""
+    m1, m2 = _geometry(mh)
+    dofs = ["Heave", "Pitch"]
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
+    assert body.mesh.nfaces <= 150
+    J, grad = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(), ctx=ctx, rho=1025.0, g=9.81)
+    J_oracle = _oracle_objective(oracle, body, obj)
+    assert abs(J - J_oracle) <= 1e-8 * abs(J_oracle)
+    n1 = m1.nvertices
+    rng = np.random.default_rng(23)
+    for d1, d2 in _affine_moves(m1.vertices, m2.vertices, rng):
+        jp = _oracle_objective(oracle, _body(mh, m1.vertices + H * d1, m2.vertices + H * d2, m1, m2, dofs), obj)
+        jm = _oracle_objective(oracle, _body(mh, m1.vertices - H * d1, m2.vertices - H * d2, m1, m2, dofs), obj)
+        fd = (jp - jm) / (2 * H)
+        ad = float(np.sum(grad[:n1] * d1) + np.sum(grad[n1:] * d2))
+        scale = np.abs(grad).sum() * max(np.abs(d1).max(), np.abs(d2).max())
+        assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
+
+
 def test_gradient_rejects_unsupported(mh, ctx):
     m1, m2 = _geometry(mh)
     body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave"])

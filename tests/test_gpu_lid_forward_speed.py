@@ -26,14 +26,15 @@ def _cylinder_with_lid(mh):
     return hull, lid
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
 @pytest.mark.parametrize("direct", [True, False])
-def test_sweep_with_lid_matches_oracle(mh, oracle, ctx, direct):
+def test_sweep_with_lid_matches_oracle(mh, oracle, ctx, direct, precision):
     hull, lid = _cylinder_with_lid(mh)
     dofs = ["Surge", "Heave", "Pitch"]
     body = mh.FloatingBody(hull, dofs, rotation_center=(0.0, 0.0, -0.5), lid_mesh=lid)
     oms = [1.5, 4.9]
     betas = [0.0, np.pi / 4]
-    F = mh.DirectBEM() if direct else mh.IndirectBEM()
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)(precision=precision)
     res = mh.hydrodynamic_coefficients(body, {"wave_frequencies": oms, "radiating_dofs": dofs,
                                               "wave_directions": betas}, F, ctx=ctx, rho=1025.0)
     for w, om in enumerate(oms):
@@ -90,7 +91,8 @@ def test_device_rejects_lid_at_free_surface(mh, ctx):
     assert ctx._L.mh_mesh_set_lid(dm.handle, both.nfaces) == 0  # no lid
 
 
-def test_forward_speed_coefficients_match_oracle(mh, oracle, ctx):
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
+def test_forward_speed_coefficients_match_oracle(mh, oracle, ctx, precision):
     """forward_speeds = [0, 0.8] m/s, two headings, IndirectBEM, hemisphere with 3 dofs."""
     mesh = mh.hemisphere_mesh(1.0, 6, 12)
     dofs = ["Surge", "Heave", "Pitch"]
@@ -99,7 +101,7 @@ def test_forward_speed_coefficients_match_oracle(mh, oracle, ctx):
     betas = [0.0, 2.0]
     Us = [0.0, 0.8]
     params = {"wave_frequencies": oms, "radiating_dofs": dofs, "wave_directions": betas, "forward_speeds": Us}
-    res = mh.hydrodynamic_coefficients(body, params, mh.IndirectBEM(), ctx=ctx, rho=1025.0)
+    res = mh.hydrodynamic_coefficients(body, params, mh.IndirectBEM(precision=precision), ctx=ctx, rho=1025.0)
     assert res["added_mass"].shape == (3, 3, 2, 2, 2)
     assert res["excitation_force"].shape == (3, 2, 2, 2)
     for iU, U in enumerate(Us):
@@ -114,7 +116,8 @@ def test_forward_speed_coefficients_match_oracle(mh, oracle, ctx):
                 assert close(res["diffraction_force"][:, iw, ib, iU], F[3])
     # zero speed equals the plain sweep, for every heading
     plain = mh.hydrodynamic_coefficients(body, {"wave_frequencies": oms, "radiating_dofs": dofs,
-                                                "wave_directions": betas}, mh.IndirectBEM(), ctx=ctx, rho=1025.0)
+                                                "wave_directions": betas}, mh.IndirectBEM(precision=precision),
+                                         ctx=ctx, rho=1025.0)
     for ib in range(2):
         assert close(res["added_mass"][:, :, :, 0, ib], plain["added_mass"][..., 0], 1e-12)
     assert close(res["excitation_force"][..., 0], plain["excitation_force"][..., 0], 1e-12)

@@ -187,7 +187,7 @@ def test_solve_matrix_level(mh, oracle, ctx, direct):
 
 
 @pytest.mark.parametrize("direct", [True, False])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
 def test_hydro_config1(mh, oracle, ctx, direct, precision):
     """200-panel hemisphere, omega = 1.03, rho = 1025, Heave radiation + beta = 0 diffraction."""
     mesh = mh.config1_hemisphere()
@@ -204,20 +204,26 @@ def test_hydro_config1(mh, oracle, ctx, direct, precision):
     assert abs(res["excitation_force"].ravel()[0] - Fe[0, 0]) <= REL_COEF * abs(Fe[0, 0])
 
 
-def test_hydro_sweep_six_dofs(mh, oracle, ctx):
-    """Several frequencies, 6 rigid dofs radiating + 2 headings, against the oracle per frequency."""
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_tc"])
+@pytest.mark.parametrize("direct", [True, False])
+def test_hydro_sweep_six_dofs(mh, oracle, ctx, precision, direct):
+    """Several frequencies, 6 rigid dofs radiating + 2 headings, against the oracle per frequency,
+    for each precision of the LU (FP64 CUDA-core update, FP32 factors refined in FP64, FP64 with
+    the tensor-core update)."""
     mesh = mh.vertical_cylinder_mesh(2.0, 3.0, 16, 6, 4)
     dofs = ["Surge", "Sway", "Heave", "Roll", "Pitch", "Yaw"]
     body = mh.FloatingBody(mesh, dofs, rotation_center=(0.0, 0.0, -1.0), body_name="cyl")
     oms = [0.4, 1.1, 2.3]
     betas = [0.0, np.pi / 3]
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)(precision=precision)
     res = mh.hydrodynamic_coefficients(body, {"wave_frequencies": oms, "radiating_dofs": dofs,
                                               "influenced_dofs": dofs, "wave_directions": betas},
-                                       ctx=ctx, rho=1025.0)
+                                       F, ctx=ctx, rho=1025.0)
     assert res["added_mass"].shape == (6, 6, 3, 1)
     assert res["excitation_force"].shape == (6, 3, 2, 1)
     for w, om in enumerate(oms):
-        A, B, Fd, Fk, Fe = oracle.hydro_one_frequency(mesh, body.dofs, om, rho=1025.0, betas=betas)
+        A, B, Fd, Fk, Fe = oracle.hydro_one_frequency(mesh, body.dofs, om, rho=1025.0, betas=betas,
+                                                      direct=direct)
         scale_a = np.abs(A).max()
         scale_b = np.abs(B).max()
         assert np.abs(res["added_mass"][:, :, w, 0] - A).max() <= REL_COEF * scale_a
@@ -241,7 +247,7 @@ def test_problem_level_solve_matches_sweep(mh, ctx):
 
 
 def test_hulme_heaving_hemisphere(mh, kats, ctx):
-    """Hulme (1982) table, rtol 0.1 (consistency_with_analytical_solutions.jl:355-379)."""
+    """Hulme (1982) table, rtol 0.1 (consistency_with_analytical_solutions.jl:52-76)."""
     h = kats["hulme_heave"]
     mesh = mh.hemisphere_mesh(1.0, 10, 20)
     body = mh.FloatingBody(mesh, ["Heave"], body_name="hemisphere")
