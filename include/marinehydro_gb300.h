@@ -7,8 +7,7 @@
  * mass, radiation damping and excitation forces.
  *
  * Every entry point names the reference (MarineHydro.jl) interface it replaces,
- * as file:line in the MarineHydro.jl tree.  The reference-side ccall bindings are
- * listed in INTEGRATION.md.
+ * as file:line in the MarineHydro.jl tree.
  *
  * Conventions
  *   - All arithmetic on the plain path is FP64.
@@ -163,8 +162,14 @@ int mh_linsolve_adjoint(mh_context* ctx, int64_t n, int64_t nrhs, const double* 
        n_panels > 8192 is rejected with MH_ERR_ARG.  Calls share the array and it
        keeps the last call's contents (each call rewrites its own panels first);
        calls whose work overlaps on the GPU (other streams or host threads) race.
-     - The first call on a device looks up the array's device address (setup);
-       make that first call before any stream capture.
+     - The first call in a CUDA context (per device, and again once the context
+       has been replaced, e.g. after cudaDeviceReset) is the set-up: it looks up
+       the array's device address and loads the module of every kernel this entry
+       point launches.  Loading a module can allocate, so make that first call
+       before any stream capture; under a pool that leaves no device memory free
+       it can fail with MH_ERR_CUDA.
+     - A CUDA error that earlier work left pending on the calling thread is
+       returned as MH_ERR_CUDA before anything is launched, and left pending.
      - Stream-ordered: kernels are queued on `stream` (a cudaStream_t, NULL = the
        default stream) and the call returns without synchronizing; S and D are
        complete when the stream reaches that point.  No cudaMalloc, cudaFree or
@@ -179,7 +184,7 @@ int mh_assemble_matrices_noalloc(void* stream, int64_t n_panels, const double* v
    (problems_and_results.jl:464-495) with _hydro_one_frequency (:472-478) for a
    zero-forward-speed body: for every omega, S and D are assembled once and all
    radiation and diffraction right-hand sides are solved together.
-     dofs:      n_dofs x n x 3 dof fields (bodies.jl:382-426), [d][i][xyz]
+     dofs:      n_dofs x n x 3 dof fields (bodies.jl:74-118), [d][i][xyz]
      rad_idx:   n_rad indices into dofs (radiating_dofs)
      inf_idx:   n_inf indices into dofs (influenced_dofs)
      betas:     n_beta wave directions (wave_directions)

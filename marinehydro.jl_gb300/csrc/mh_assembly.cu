@@ -739,6 +739,11 @@ void launch_panel_geometry(cudaStream_t st, LaunchCounter lc, int64_t n, const d
             panel_geometry_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, V, C, N, A, R, out));
 }
 
+cudaError_t load_panel_geometry_kernel() {
+  cudaFuncAttributes attr;
+  return cudaFuncGetAttributes(&attr, panel_geometry_kernel);
+}
+
 void launch_assemble_static(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double* SR, double* DR) {
   if (p.n <= 0) return;
   dim3 grid((unsigned)((p.n + kRowsPerCta - 1) / kRowsPerCta), (unsigned)((p.n + kColsPerCta - 1) / kColsPerCta));

@@ -88,6 +88,9 @@ struct LaunchCounter {
 // assembly (mh_assembly.cu)
 void launch_panel_geometry(cudaStream_t st, LaunchCounter lc, int64_t n, const double* V, const double* C,
                            const double* N, const double* A, const double* R, PanelRec* out);
+// loads panel_geometry_kernel's module on the current device now (lazy loading would do it
+// at the first launch)
+cudaError_t load_panel_geometry_kernel();
 
 struct AssemblyParams {
   int64_t n;

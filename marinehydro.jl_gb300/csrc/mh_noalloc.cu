@@ -15,6 +15,13 @@
 // own panels before reading them, so nothing needs clearing, but two calls whose
 // work overlaps on the GPU (different streams, or different host threads) race
 // on it.
+//
+// Set-up: the first call in a CUDA context (per device, and again after the
+// context is replaced, e.g. by cudaDeviceReset) looks up the array's device
+// address with cudaGetSymbolAddress and loads the module of every kernel the
+// entry point launches.  Loading a module can allocate (the 2 MiB array comes
+// into being then), so that first call belongs before any stream capture and may
+// fail with MH_ERR_CUDA when the pool leaves no room for the module.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,29 +42,82 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) PanelRec g_noalloc_panels[kNoAllocMaxPanels];
 
-// Host-side: the device address of g_noalloc_panels, looked up once per device.
-// (In host code the symbol name is only a host-side stand-in for the array.)
-std::mutex g_setup_mutex;
-PanelRec* g_panels_addr[kMaxDevices] = {};
+template <bool DIRECT>
+__global__ void __launch_bounds__(128) noalloc_assembly_kernel(int64_t n, const PanelRec* __restrict__ P,
+                                                               uint32_t gfs, int include_identity, int has_fixed,
+                                                               double fx, double fy, double fz, double k,
+                                                               double2* __restrict__ S, double2* __restrict__ D);
 
+// Host-side: the device address of g_noalloc_panels per device, valid for the CUDA
+// context it was looked up in.  (In host code the symbol name is only a host-side
+// stand-in for the array, not a device address.)  The context is identified by the
+// driver's context id, reached through the runtime's driver entry-point query so the
+// library needs no link against libcuda; without it the address is looked up on
+// every call.
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+
+struct NoAllocSetup {
+  unsigned long long ctx_id = 0;  // 0: not set up
+  PanelRec* panels = nullptr;
+};
+
+std::mutex g_setup_mutex;
+NoAllocSetup g_setup[kMaxDevices];
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_ctx_fns_resolved = false;
+
+unsigned long long current_context_id() {
+  if (!g_ctx_fns_resolved) {
+    g_ctx_fns_resolved = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != 0 || !ctx || g_ctx_get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Once per device and context, with that device current: the array's address, and every
+// kernel of the entry point loaded now rather than lazily at a later (possibly captured)
+// launch.
 int panels_address(int device, PanelRec** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_panels_addr[device]) {
+  NoAllocSetup& su = g_setup[device];
+  const unsigned long long id = current_context_id();
+  if (id == 0 || su.ctx_id != id) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_panels) != cudaSuccess) return MH_ERR_CUDA;
-    g_panels_addr[device] = static_cast<PanelRec*>(p);
+    cudaFuncAttributes attr;
+    if (cudaFuncGetAttributes(&attr, noalloc_assembly_kernel<true>) != cudaSuccess ||
+        cudaFuncGetAttributes(&attr, noalloc_assembly_kernel<false>) != cudaSuccess ||
+        load_panel_geometry_kernel() != cudaSuccess)
+      return MH_ERR_CUDA;
+    su.panels = static_cast<PanelRec*>(p);
+    su.ctx_id = id;
   }
-  *out = g_panels_addr[device];
+  *out = su.panels;
   return MH_OK;
 }
 
 // Static (Birk Rankine + image) and Wu parts of one pair, summed in the same
 // order as the cached-static path: S = scale*s_static + scale*s_wave.
 template <bool DIRECT>
-__global__ void __launch_bounds__(kRows) noalloc_assembly_kernel(int64_t n, const PanelRec* __restrict__ P,
-                                                                 uint32_t gfs, int include_identity, int has_fixed,
-                                                                 double fx, double fy, double fz, double k,
-                                                                 double2* __restrict__ S, double2* __restrict__ D) {
+__global__ void __launch_bounds__(128) noalloc_assembly_kernel(int64_t n, const PanelRec* __restrict__ P,
+                                                               uint32_t gfs, int include_identity, int has_fixed,
+                                                               double fx, double fy, double fz, double k,
+                                                               double2* __restrict__ S, double2* __restrict__ D) {
   __shared__ PanelRec sp[kCols];
   const int64_t i = blockIdx.x * (int64_t)kRows + threadIdx.x;
   const int64_t j0 = blockIdx.y * (int64_t)kCols;
@@ -138,6 +198,9 @@ extern "C" int mh_assemble_matrices_noalloc(void* stream, int64_t n_panels, cons
   if (!vertices || !centers || !normals || !areas || !radii || !S || !D) return MH_ERR_ARG;
   if (gfs == 0 || (gfs & ~kNoAllocKinds)) return MH_ERR_UNSUPPORTED;
   if ((gfs & MH_GF_WU) && !(wavenumber > 0)) return MH_ERR_ARG;
+  // an error that earlier work left pending on this thread is reported, and left pending,
+  // before anything is launched, so that it is not taken for this call's own failure
+  if (cudaPeekAtLastError() != cudaSuccess) return MH_ERR_CUDA;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return MH_ERR_CUDA;
   PanelRec* panels = nullptr;

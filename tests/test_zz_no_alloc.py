@@ -5,9 +5,13 @@ that already owns the GPU (a Julia CUDA.jl session, a framework's caching
 allocator) or code that must not allocate after start-up.  For them
 mh_assemble_matrices_noalloc keeps its per-panel scratch in a fixed device array
 (8192 panels) instead of allocating a workspace.  This checks it, called through
-the C-ABI, against the allocating mh_assemble_matrices on two calls in a row
-with different meshes and wavenumbers, so the second call also shows that the
-shared array's previous contents do not leak into the next result.
+the C-ABI, against the allocating mh_assemble_matrices on calls in a row that
+share that array: each case's mesh has fewer panels than the one before, so
+records of the previous mesh lie right past the current mesh's records, and a
+call that read past its own panels, or skipped rewriting them, would give S and
+D that differ from the allocating path's.  The cases cover the direct and
+indirect forms, with and without a fixed normal and the identity jump, and the
+static-only, wave-only and mixed Green-function sets.
 
 Kept in a file of its own that pytest collects last.
 """
@@ -49,15 +53,24 @@ def rel(a, b):
 
 def test_noalloc_matches_allocating_entry_point_twice(mh, ctx):
     torch = pytest.importorskip("torch")
-    gfs = mh.default_greens_functions("Wu")
-    flags = mh.gf_flags(gfs)
-    cases = [(mh.config1_hemisphere(), 1.03 ** 2 / 9.81, True, None),
-             (mh.vertical_cylinder_mesh(2.0, 3.0, 12, 5, 3), 0.8, False, [1.0, 0.0, 0.0])]
-    for mesh, k, direct, fixed in cases:  # two calls in a row on the shared array
-        S, D = _noalloc(mh, torch, mesh, k, flags, direct, True, fixed)
-        S0, D0 = mh.assemble_matrices(gfs, mesh, k, direct=direct, all_normals=fixed, ctx=ctx)
-        assert rel(S, S0) < REL_SD
-        assert rel(D, D0) < REL_SD
+    wu = mh.default_greens_functions("Wu")
+    rankine_neg = (mh.Rankine(), mh.RankineReflectedNegative())
+    wave_only = (mh.GFWu(),)
+    # (mesh, k, gfs, direct, include_identity, fixed normal); panel counts decrease
+    cases = [(mh.config1_hemisphere(), 1.03 ** 2 / 9.81, wu, True, True, None),                       # 200
+             (mh.vertical_cylinder_mesh(2.0, 3.0, 12, 5, 3), 0.8, wu, False, True, [1.0, 0.0, 0.0]),  # 96
+             (mh.hemisphere_mesh(1.5, 5, 16), 0.5, wu, False, True, None),                             # 80
+             (mh.vertical_cylinder_mesh(1.0, 2.0, 10, 4, 2), 1.7, rankine_neg, True, False, None),    # 60
+             (mh.hemisphere_mesh(0.8, 3, 12), 2.2, wave_only, False, True, None),                      # 36
+             (mh.hemisphere_mesh(0.8, 2, 10), 0.9, wave_only, True, False, [0.0, 0.0, 1.0])]          # 20
+    sizes = [c[0].nfaces for c in cases]
+    assert sizes == sorted(sizes, reverse=True) and len(set(sizes)) == len(sizes), sizes
+    for mesh, k, gfs, direct, ident, fixed in cases:
+        S, D = _noalloc(mh, torch, mesh, k, mh.gf_flags(gfs), direct, ident, fixed)
+        S0, D0 = mh.assemble_matrices(gfs, mesh, k, direct=direct, include_identity=ident, all_normals=fixed,
+                                      ctx=ctx)
+        assert rel(S, S0) < REL_SD, (mesh.nfaces, direct)
+        assert rel(D, D0) < REL_SD, (mesh.nfaces, direct)
 
 
 def test_noalloc_rejects_oversize_and_unsupported(mh):
