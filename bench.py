@@ -9,7 +9,10 @@ direct BEM, infinite depth, rho = 1025, g = 9.81.  One frequency-solve = one
 (body, omega): assemble S and D, factorize, solve all 7 right-hand sides,
 integrate forces.  Synthetic mesh (no dataset).
 
-  value  -- inputs resident in HBM (mesh handle, dof fields, device outputs)
+  value  -- inputs resident in HBM (mesh handle, dof fields, device outputs); FP64 LU
+            whose trailing update runs on the tensor cores by exact digit products
+            (MH_PREC_FP64_TC), panel, pivoting, triangular solves and refinement-free
+            substitution in FP64 -- results equal the FP64 CUDA-core path to rounding
   e2e    -- the public C-ABI call with host buffers: mesh upload, dof upload,
             sweep, coefficient read-back, all inside the timed region
   --impl reference -- the CPU oracle (C restatement of the reference) on the
@@ -199,11 +202,6 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3] not in ("", "[N/A]"))}
 
 
-# DRAM bytes per launch of the FP64 trailing update on this workload, from one ncu capture of
-# the full sweep (dram__bytes_read.sum + dram__bytes_write.sum, 124 launches: 153.3 GB)
-GEMM_F64_TRAFFIC_PER_LAUNCH = 1.236e9
-
-
 def lu_gemm_flops(n, nb=32, per_mac=8):
     """Real flops of the trailing updates of one n x n complex LU: per_mac per complex
     multiply-add (8 with the four-multiplication product, 6 with the 3M product)."""
@@ -213,6 +211,83 @@ def lu_gemm_flops(n, nb=32, per_mac=8):
         rest = n - k - kb
         f += per_mac * rest * rest * kb
     return f
+
+
+# Tensor work of the exact-digit (Ozaki) update per complex multiply-add: 36 digit pairs
+# (p + q <= 7 of eight digits each) x 4 real products x 2 flops
+OZAKI_TENSOR_FLOPS_PER_MAC = 36 * 4 * 2
+# FP64 instructions of the Wu pair evaluation (ncu instruction mix of wave_kernel<1,1>:
+# 241 DFMA + 88 DMUL + 45 DADD per unordered pair, a DFMA counted as 2 flops)
+WU_FLOPS_PER_UNORDERED_PAIR = 615
+# ncu figures of the dominant kernels (small cases of the same kernels; the capture command
+# of each is kept with its summary under profiles/)
+NCU = {
+    "lu_gemm_ozaki": {"tensor_pipe_active": 0.197, "fp64_pipe_active": 0.515,
+                      "dram_bytes_per_trailing_entry": None},
+    "assemble_wave_wu": {"fp64_pipe_active": 0.871, "dram_bytes_per_unordered_pair": 358e6 / 4.0e6},
+    "lu_gemm_f64": {"fp64_pipe_active": 0.977, "dram_bytes_per_launch": 1.236e9},
+}
+
+
+def measured_peaks():
+    """HBM and BF16 tensor peaks measured on this GPU model (MEASURED_PEAKS.json), else the
+    fallback figures of an earlier GB300 measurement."""
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"bf16_tflops": float(d["bf16_tflops"]), "hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"bf16_tflops": 1900.0, "hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def roofline(prof, steps, n, n_omega, peak64, peaks):
+    """Roofline of the kernel group with the largest device time in `prof` ({group: (ms, launches)})."""
+    top_name, (top_ms, top_launches) = max(prof.items(), key=lambda kv: kv[1][0])
+    per_launch_s = top_ms / top_launches * 1e-3
+    launches_per_step = top_launches / steps
+    out = {"kernel": top_name, "share": top_ms / sum(v[0] for v in prof.values())}
+    if top_name == "lu_gemm_ozaki":
+        macs = lu_gemm_flops(n, per_mac=1) * n_omega / launches_per_step  # complex multiply-adds per launch
+        achieved = macs * OZAKI_TENSOR_FLOPS_PER_MAC / per_launch_s / 1e12
+        out.update({"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": achieved / peaks["bf16_tflops"],
+                    "peak_source": f"dense BF16 burst ({peaks['source']}, MEASURED_PEAKS.json)",
+                    "work": "BF16 tensor flops of the exact-digit update: 36 digit pairs x 4 real products x 2 "
+                            "flops per complex multiply-add, summed over the panel steps",
+                    "fp64_equivalent_tflops": macs * 8 / per_launch_s / 1e12,
+                    "fp64_equivalent_frac_of_fp64_peak": macs * 8 / per_launch_s / 1e12 / peak64,
+                    "ncu": NCU["lu_gemm_ozaki"],
+                    "traffic": None})
+        bpe = NCU["lu_gemm_ozaki"]["dram_bytes_per_trailing_entry"]
+        if bpe:
+            out["traffic"] = bpe * macs / 32
+            out["traffic_unit"] = "bytes per launch (DRAM read + write), scaled from a smaller capture per entry"
+    elif top_name == "assemble_wave_wu":
+        pairs = n * (n + 1) / 2 * n_omega / launches_per_step  # unordered pairs per launch
+        achieved = pairs * WU_FLOPS_PER_UNORDERED_PAIR / per_launch_s / 1e12
+        out.update({"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                    "frac": achieved / peak64,
+                    "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks "
+                                   "(MEASURED_PEAKS.json has no FP64 figure)",
+                    "work": f"{WU_FLOPS_PER_UNORDERED_PAIR} FP64 flops per unordered pair (both entries written)",
+                    "ncu": NCU["assemble_wave_wu"],
+                    "traffic": NCU["assemble_wave_wu"]["dram_bytes_per_unordered_pair"] * pairs,
+                    "traffic_unit": "bytes per launch (DRAM read + write), scaled per pair from a 2-frequency "
+                                    "capture"})
+    elif top_name == "lu_gemm_f64":
+        flops = lu_gemm_flops(n, per_mac=6) * n_omega / launches_per_step
+        achieved = flops / per_launch_s / 1e12
+        out.update({"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                    "frac": achieved / peak64, "ncu": NCU["lu_gemm_f64"],
+                    "traffic": NCU["lu_gemm_f64"]["dram_bytes_per_launch"],
+                    "traffic_unit": "bytes per launch (DRAM read + write)",
+                    "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks",
+                    "work": "6 real flops (three FP64 FMAs, the 3M complex product) per complex multiply-add"})
+    else:
+        out.update({"bound": "fp64", "achieved": None, "peak": peak64, "unit": "TFLOP/s", "frac": None,
+                    "traffic": None})
+    return out
 
 
 def run_gpu(args):
@@ -326,21 +401,22 @@ def run_gpu(args):
                           "launches": ctx.launch_count()}))
         return 0
     peak64, peak32 = ctx.probe_fma_peaks()
+    peaks = measured_peaks()
+    HEAD = _lib.MH_PREC_FP64_TC
     with ClockSampler(local) as clk:
-        t_dev, wall_dev, launches, prof = timed(lambda: step_device(_lib.MH_PREC_FP64), args.steps, args.warmup,
-                                                profile=True)
+        t_dev, wall_dev, launches, prof = timed(lambda: step_device(HEAD), args.steps, args.warmup, profile=True)
     clocks = clk.summary()
-    res64 = [o.cpu().numpy().copy() for o in outs_d]
-    t_e2e, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_FP64), max(2, args.steps // 2), 1)
+    res_head = [o.cpu().numpy().copy() for o in outs_d]
     e2e_steps = max(2, args.steps // 2)
+    t_e2e, _, _, _ = timed(lambda: step_e2e(HEAD), e2e_steps, 1)
+    t_64, _, launches_64, prof_64 = timed(lambda: step_device(_lib.MH_PREC_FP64), args.steps, 1, profile=True)
+    res64 = [o.cpu().numpy().copy() for o in outs_d]
+    dev_head = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(res_head, res64))
+    t_e2e_64, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_FP64), e2e_steps, 1)
     t_mix, _, _, prof_mix = timed(lambda: step_device(_lib.MH_PREC_MIXED), args.steps, 1, profile=True)
     resmx = [o.cpu().numpy() for o in outs_d]
     dev_mix = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(resmx, res64))
     t_e2e_mix, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_MIXED), e2e_steps, 1)
-    t_tc, _, launches_tc, prof_tc = timed(lambda: step_device(_lib.MH_PREC_FP64_TC), args.steps, 1, profile=True)
-    restc = [o.cpu().numpy() for o in outs_d]
-    dev_tc = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) for a, b in zip(restc, res64))
-    t_e2e_tc, _, _, _ = timed(lambda: step_e2e(_lib.MH_PREC_FP64_TC), e2e_steps, 1)
 
     batch = None
     if not args.no_batch:
@@ -359,61 +435,49 @@ def run_gpu(args):
     value = units / t_dev
     ms_step = 1e3 * t_dev / args.steps
 
-    # roofline of the dominant kernel group (FP64 FMA bound)
-    total_ms = sum(v[0] for v in prof.values())
-    top = max(prof.items(), key=lambda kv: kv[1][0])
-    top_name, (top_ms, top_launches) = top
-    share = {k: round(v[0] / total_ms, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    def shares(p):
+        tot = sum(v[0] for v in p.values())
+        return {k: round(v[0] / tot, 4) for k, v in sorted(p.items(), key=lambda kv: -kv[1][0])}
+
     pairs_per_step = N_OMEGA * n * n
     asm_ms = sum(v[0] for k, v in prof.items() if k.startswith("assemble"))
-    roof = None
-    if top_name == "lu_gemm_f64":
-        flops_per_launch = lu_gemm_flops(n, per_mac=6) * N_OMEGA / (top_launches / args.steps)
-        achieved = flops_per_launch / (top_ms / top_launches * 1e-3) / 1e12
-        roof = {"bound": "fp64", "kernel": top_name, "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                "frac": achieved / peak64, "traffic": GEMM_F64_TRAFFIC_PER_LAUNCH,
-                "traffic_unit": "bytes per launch (DRAM read + write)",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every FP64 trailing-update "
-                                  "launch of the same 30-frequency sweep (profiles/lu_gemm_f64_cylinder2000.md); "
-                                  "algorithmic: 32 B per trailing-block entry, 1.26e9 B per launch",
-                "peak_source": "FP64 FMA throughput measured in this run by mh_probe_fma_peaks (MEASURED_PEAKS.json "
-                               "has no FP64 figure)",
-                "work": "6 real flops (three FP64 FMAs, the 3M complex product) per complex multiply-add of the "
-                        "trailing update, summed over panel steps; the four-multiplication count would be 4/3 of it"}
-    else:
-        roof = {"bound": "fp64", "kernel": top_name, "achieved": None, "peak": peak64, "unit": "TFLOP/s",
-                "frac": None, "traffic": None}
+    roof = roofline(prof, args.steps, n, N_OMEGA, peak64, peaks)
+    # the other large kernel group of the headline sweep, with its own roofline
+    rest = {k: v for k, v in prof.items() if k != roof["kernel"]}
+    roof_next = roofline(rest, args.steps, n, N_OMEGA, peak64, peaks) if rest else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "panels": n, "omegas": N_OMEGA, "rhs_per_omega": len(DOFS) + len(BETAS),
-                   "precision": "fp64 (LU, pivoting and substitution in FP64)",
+                   "precision": "fp64: LU panel, pivoting, triangular solves and substitution in FP64; trailing "
+                                "update as exact BF16 digit products on the tensor cores, recombined in integers "
+                                "and FP64 (FP64 results to rounding)",
                    "l2": "flushed before every timed step (256 MiB write); per-step working set 3.8 GB > L2"},
         "panel_pairs_per_sec": pairs_per_step * args.steps * ws / (asm_ms * 1e-3) if asm_ms > 0 else None,
         "gpu_launches": launches,
         "e2e": {"value": N_OMEGA * e2e_steps * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": roof,
-        "kernel_time_share": share,
+        "roofline_next_kernel": roof_next,
+        "kernel_time_share": shares(prof),
+        "max_rel_dev_vs_fp64_cuda_core_update": dev_head,
         "clocks": clocks,
-        "variants": {"mixed_precision_ir": {
-            "value": N_OMEGA * args.steps * ws / t_mix, "unit": UNIT,
-            "e2e": N_OMEGA * e2e_steps * ws / t_e2e_mix,
-            "max_rel_dev_vs_fp64": dev_mix,
-            "note": "FP32 LU factors + FP64 iterative refinement to FP64 accuracy; same assembly",
-            "kernel_time_share": {k: round(v[0] / sum(x[0] for x in prof_mix.values()), 4)
-                                  for k, v in sorted(prof_mix.items(), key=lambda kv: -kv[1][0])}},
-            "fp64_tensor_core_update": {
-            "value": N_OMEGA * args.steps * ws / t_tc, "unit": UNIT,
-            "e2e": N_OMEGA * e2e_steps * ws / t_e2e_tc,
-            "max_rel_dev_vs_fp64": dev_tc, "gpu_launches": launches_tc,
-            "note": "FP64 LU whose trailing update runs on the BF16 tensor cores by Ozaki splitting (8 x 7-bit "
-                    "digits, exact FP32 digit products, exact integer recombination); panel, pivoting and "
-                    "substitution in FP64; same assembly",
-            "kernel_time_share": {k: round(v[0] / sum(x[0] for x in prof_tc.values()), 4)
-                                  for k, v in sorted(prof_tc.items(), key=lambda kv: -kv[1][0])}}},
-        "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32},
+        "variants": {
+            "fp64_cuda_core_update": {
+                "value": N_OMEGA * args.steps * ws / t_64, "unit": UNIT,
+                "e2e": N_OMEGA * e2e_steps * ws / t_e2e_64, "gpu_launches": launches_64,
+                "note": "the same FP64 LU with its trailing update on the FP64 CUDA cores (3M complex product)",
+                "roofline": roofline(prof_64, args.steps, n, N_OMEGA, peak64, peaks),
+                "kernel_time_share": shares(prof_64)},
+            "mixed_precision_ir": {
+                "value": N_OMEGA * args.steps * ws / t_mix, "unit": UNIT,
+                "e2e": N_OMEGA * e2e_steps * ws / t_e2e_mix,
+                "max_rel_dev_vs_fp64": dev_mix,
+                "note": "FP32 LU factors + FP64 iterative refinement to FP64 accuracy; same assembly",
+                "kernel_time_share": shares(prof_mix)}},
+        "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32, "bf16_tflops": peaks["bf16_tflops"],
+                           "hbm_gbs": peaks["hbm_gbs"], "source": peaks["source"]},
     }
     if batch is not None:
         line["variants"]["batched_64_bodies"] = batch
@@ -705,7 +769,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+1 device sweeps and exit (the command profiled with ncu)")
     ap.add_argument("--omegas", type=int, default=30, help="number of the 30 frequencies per step")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp64_tc"], help="for --profile-only")
+    ap.add_argument("--precision", default="fp64_tc", choices=["fp64", "mixed", "fp64_tc"], help="for --profile-only")
     ap.add_argument("--case", default="cylinder", choices=["cylinder", "surrogate", "adjoint", "exact"],
                     help="for --profile-only: the headline sweep, or a small surrogate / adjoint / exact-kernel case")
     args = ap.parse_args()

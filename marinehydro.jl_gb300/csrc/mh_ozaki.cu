@@ -31,8 +31,9 @@
 //     fit TMEM twice so that the products overlap the epilogue, measured 12 % slower: they
 //     read every A tile twice as often.)  The epilogue converts the exact integers
 //     with magic-number additions (no integer-to-FP64 conversion instructions), combines
-//     them in 32/64-bit integers and applies C -= 2^s (hi + lo 2^-28) with one FP64 add and
-//     two FMAs per real entry; C is prefetched into registers while the MMAs run.
+//     them in 32/64-bit integers, rounds hi + lo 2^-28 to one 53-bit integer, builds its
+//     scaled double with integer operations and applies it with one FP64 subtraction per real
+//     entry; C is prefetched into registers while the MMAs run.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -128,8 +129,18 @@ __global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, cons
   }
 }
 
-// 2^s as a double, s in the normal range
-__device__ __forceinline__ double pow2(int s) { return __longlong_as_double((long long)(s + 1023) << 52); }
+// v 2^s as a double, exactly, for |v| < 2^53, built from the integer's bits (leading-zero
+// count, shift, exponent field) without the FP64 pipe.  Results below the normal range are
+// flushed to zero (they lie below 2^-1022).
+__device__ __forceinline__ double scaled_i64(long long v, int s) {
+  const unsigned long long sign = (unsigned long long)v & 0x8000000000000000ULL;
+  unsigned long long m = (unsigned long long)(v < 0 ? -v : v);
+  const int msb = 63 - __clzll(m);  // <= 52
+  m <<= (52 - msb);
+  const long long e = (long long)msb + s + 1023;
+  const unsigned long long bits = sign | ((unsigned long long)e << 52) | (m & 0x000FFFFFFFFFFFFFULL);
+  return (v == 0 || e <= 0) ? 0.0 : __longlong_as_double((long long)bits);
+}
 
 constexpr int kOzGroupMax = 8; // column tiles per CTA (the A tiles are loaded once for all of them):
                                // 1..8, from the launch-shape table (default 4)
@@ -260,18 +271,18 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int qq = 8 * h8 + q;
-        // hi = T0..T3 and lo = T4..T7 in base 2^7 (|.| < 2^43); 1.5 2^52 + x as a double is exact
-        const long long kMagic = 0x4338000000000000LL;
+        // hi = T0..T3 and lo = T4..T7 in base 2^7 (|hi|, |lo| <= 2^21 (2^21 + 2^14 + 2^7 + 1)
+        // < 1.008 2^42).  L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28); v = hi 2^10 + lo 2^-18,
+        // rounded to an integer (|v| < 2^53, error <= 2^-11 in units of hi: FP64 rounding of the
+        // largest possible sum), is scaled into a double by integer operations, so the FP64 pipe
+        // does one subtraction per real entry
         const long long hr = (long long)pr[0][q] * 16384 + pr[1][q], lr = (long long)pr[2][q] * 16384 + pr[3][q];
         const long long hi = (long long)pi[0][q] * 16384 + pi[1][q], li = (long long)pi[2][q] * 16384 + pi[3][q];
-        // (1.5 2^52 + lo) 2^-28 + (hi - 1.5 2^24) = hi + lo 2^-28, rounded once
-        constexpr double kBias = 6755399441055744.0 + 25165824.0;  // 1.5 2^52 + 1.5 2^24
-        const double xr = fma(__longlong_as_double(lr + kMagic), 0x1p-28, __longlong_as_double(hr + kMagic) - kBias);
-        const double xi = fma(__longlong_as_double(li + kMagic), 0x1p-28, __longlong_as_double(hi + kMagic) - kBias);
-        // L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28)
-        const double sc = pow2(er + ce[qq] - 33);
-        cv[qq].x = fma(-xr, sc, cv[qq].x);
-        cv[qq].y = fma(-xi, sc, cv[qq].y);
+        const long long vr = hr * 1024 + ((lr + (1LL << 17)) >> 18);
+        const long long vi = hi * 1024 + ((li + (1LL << 17)) >> 18);
+        const int sc = er + ce[qq] - 43;
+        cv[qq].x -= scaled_i64(vr, sc);
+        cv[qq].y -= scaled_i64(vi, sc);
       }
     }
     if (row_live) {
