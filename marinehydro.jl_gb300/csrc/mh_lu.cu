@@ -158,6 +158,19 @@ template <typename T> struct PanelRows;
 template <> struct PanelRows<double> { static constexpr int value = 432; };
 template <> struct PanelRows<float> { static constexpr int value = 864; };
 
+// Pivot candidates compare |re| + |im| through the bit pattern of the (non-negative) value as
+// a signed integer, which orders like the value: FP64 comparisons run on GB300's narrow FP64
+// pipe, integer ones do not.  -1 stands below every candidate.
+template <typename T> struct PivotKey;
+template <> struct PivotKey<double> {
+  using type = long long;
+  __device__ static __forceinline__ long long of(double v) { return __double_as_longlong(v); }
+};
+template <> struct PivotKey<float> {
+  using type = int;
+  __device__ static __forceinline__ int of(float v) { return __float_as_int(v); }
+};
+
 // (value, row) of the larger |re| + |im|; ties go to the smaller row (izamax's first maximum)
 template <typename T> __device__ __forceinline__ void argmax_merge(T& v, int& i, T ov, int oi) {
   if (ov > v || (ov == v && oi < i)) { v = ov; i = oi; }
@@ -196,16 +209,17 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
                                                                      int32_t* __restrict__ info_all, int64_t k,
                                                                      int chunk) {
   using C = typename cplx_t<T>::type;
+  using K = typename PivotKey<T>::type;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char panel_smem[];
   C* sp = reinterpret_cast<C*>(panel_smem);  // chunk x kb, column-major (leading dimension chunk)
   __shared__ C pub_row[2][kNB];               // this CTA's candidate row, by column parity
   __shared__ C pub_j[2][kNB];                 // CTA 0: row j
-  __shared__ T cand_v[2];
+  __shared__ K cand_v[2];
   __shared__ int cand_i[2];
   __shared__ C urow[kNB], jrow[kNB];
-  __shared__ T red_v[kPanelThreads / 32];
+  __shared__ K red_v[kPanelThreads / 32];
   __shared__ int red_i[kPanelThreads / 32];
   __shared__ int s_piv;
   __shared__ C s_inv;
@@ -221,11 +235,11 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
   for (int c = 0; c < kb; ++c)
     for (int i = tid; i < rows; i += kPanelThreads) sp[c * chunk + i] = A[(k + r0 + i) + (k + c) * n];
   // candidate for column 0 (each thread reads only its own rows)
-  T best = -1;
+  K best = -1;
   int bi = INT_MAX;
   for (int i = tid; i < rows; i += kPanelThreads) {
     const C a = sp[i];
-    argmax_merge(best, bi, fabs(a.x) + fabs(a.y), r0 + i);
+    argmax_merge(best, bi, PivotKey<T>::of(fabs(a.x) + fabs(a.y)), r0 + i);
   }
   for (int j = 0; j < kb; ++j) {
     const int par = j & 1;
@@ -234,7 +248,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
     if (lane == 0) { red_v[warp] = best; red_i[warp] = bi; }
     __syncthreads();
     if (warp == 0) {
-      best = lane < kPanelThreads / 32 ? red_v[lane] : (T)-1;
+      best = lane < kPanelThreads / 32 ? red_v[lane] : (K)-1;
       bi = lane < kPanelThreads / 32 ? red_i[lane] : INT_MAX;
       warp_argmax(best, bi);
       if (lane == 0) { cand_v[par] = best; cand_i[par] = bi; }
@@ -243,7 +257,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
     }
     cl.sync();  // candidates and rows posted
     if (warp == 0) {
-      T v = -1;
+      K v = -1;
       int vi = INT_MAX;
       if (lane < P) {
         v = *cl.map_shared_rank(&cand_v[par], (unsigned)lane);
@@ -289,7 +303,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
       for (int c = j + 1; c < kb; ++c) {
         const C v = cfms(sp[c * chunk + i], l, urow[c]);
         sp[c * chunk + i] = v;
-        if (c == j + 1) argmax_merge(best, bi, fabs(v.x) + fabs(v.y), pr);
+        if (c == j + 1) argmax_merge(best, bi, PivotKey<T>::of(fabs(v.x) + fabs(v.y)), pr);
       }
     }
   }
