@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define MH_ABI_VERSION 1
+#define MH_ABI_VERSION 2
 
 typedef enum {
     MH_OK = 0,
@@ -280,12 +280,19 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
    dA = -lambda y^H) and the Birk kernel rules (ad_rules.jl:79-294), applied
    to the objective
        J = sum_omega sum_h ( A_hh(omega) + B_hh(omega) ),  h over obj_idx
-   (added mass plus radiation damping of the objective dofs, the direct
-   formulation, zero forward speed).  Each frequency reuses its LU factors for
-   one adjoint solve; no N^2 cotangent is stored: the pair derivatives are
-   recomputed tile by tile and contracted with rank-n_obj weights, the
-   frequency-independent Rankine part once with frequency-summed weights.
-     gfs:       Birk Rankine kinds (MH_GF_RANKINE*) and/or MH_GF_WU
+   (added mass plus radiation damping of the objective dofs, zero forward
+   speed).  Each frequency reuses its LU factors for one adjoint solve; no N^2
+   cotangent is stored: the pair derivatives are recomputed tile by tile and
+   contracted with rank-n_obj weights, the frequency-independent Rankine part
+   once with frequency-summed weights.
+     gfs:       Birk Rankine kinds (MH_GF_RANKINE*) with MH_GF_WU or
+                MH_GF_EXACT_DELHOMMEAU (not both).  The exact term's second
+                derivatives come from its value and r-derivative at each pair
+                (dG/dz = G + 2/d, exact_Guevel_Delhommeau.jl:52-59, and Laplace's
+                equation in (r, z)); its quadrature runs once per pair and frequency
+                at the context's tolerance, as in the primal
+     direct:    1 DirectBEM (phi = D^-1 S bc), 0 IndirectBEM (sigma = K^-1 bc,
+                phi = S sigma): solve(D, S, bc; direct), matrix_assembly.jl:436-449
      dofs:      n_dofs x n x 3 dof fields, held fixed
      obj_idx:   1..4 indices into dofs
      precision: MH_PREC_FP64, or MH_PREC_MIXED: FP32 factors with both the forward and
@@ -299,7 +306,7 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
      grad_dofs[n_obj][n][3]: dJ w.r.t. the objective dof fields
    The caller chains these through its mesh and dof construction. */
 int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
-                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
+                      uint32_t gfs, int direct, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem);
 /* The general pullback of the same sweep, what Zygote / Enzyme reverse mode returns for
@@ -317,11 +324,29 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const dou
    solve per radiating dof and heading.  grad_dofs is n_dofs x n x 3 (every dof field,
    zero for dofs outside rad_idx / inf_idx). */
 int mh_hydro_vjp(mh_context* ctx, mh_mesh* mesh, int64_t n_omega, const double* omegas, double rho, double g,
-                 uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                 uint32_t gfs, int direct, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
                  int64_t n_inf, const int32_t* inf_idx, int64_t n_beta, const double* betas,
                  const double* added_mass_bar, const double* radiation_damping_bar, const double* excitation_force_bar,
                  int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                  double* grad_vertices, double* grad_dofs, int mem);
+
+/* The pullback of solve(D, S, bc; direct) (matrix_assembly.jl:436-449) through the
+   _mulvec and _linearsolve rules (ad_rules.jl:300-414): given the cotangent phi_bar of
+   the potential (and, indirect, sources_bar of the sources, may be NULL), returns the
+   primal outputs and the cotangents of D, S and bc (complex, Julia's conventions:
+   dS = ybar bc^H, lambda = A^-H ybar, dA = -lambda y^H, dbc = lambda):
+     direct:   phi = D^-1 (S bc); lambda = D^-H phi_bar;
+               D_bar = -lambda phi^H, S_bar = lambda bc^H, bc_bar = S^H lambda
+     indirect: sources = K^-1 bc, phi = S sources (K = D);
+               lambda = K^-H (S^H phi_bar + sources_bar);
+               S_bar = phi_bar sources^H, D_bar = -lambda sources^H, bc_bar = lambda
+   D, S, D_bar, S_bar: n x n complex column-major; bc, phi_bar, sources_bar, phi,
+   sources, bc_bar: n x nrhs complex.  D_bar, S_bar, bc_bar may be NULL; `sources` is
+   required for the indirect method.  FP64 precisions factor once and reuse the factors
+   for the adjoint solve; MH_PREC_MIXED refines both solves to FP64 backward error. */
+int mh_solve_pullback(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const double* S, const double* bc,
+                      int direct, const double* phi_bar, const double* sources_bar, int precision, double* phi,
+                      double* sources, double* D_bar, double* S_bar, double* bc_bar, int mem);
 
 /* ---- learned wave-term surrogate (no counterpart in the reference) --------- */
 /* A 2 -> 64 -> 64 -> 64 -> 6 tanh network with BF16 weights and FP32 arithmetic that

@@ -11,7 +11,7 @@ from .api import (airy_bc, airy_pressure, assemble_matrices, autotune, load_tile
                   calculate_radiation_forces,
                   compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
                   gpu_linsolve, hydro_gradient, hydro_vjp, hydrodynamic_coefficients, hydrodynamic_coefficients_derivative, load_surrogate, set_surrogate, surrogate_wave_terms, train_surrogate, integrate_pressure, linsolve, linsolve_adjoint,
-                  problems_from_data, radiation_bc, solve, solve_linear, solve_problem)
+                  problems_from_data, radiation_bc, solve, solve_linear, solve_problem, solve_pullback)
 from .bodies import FloatingBody, combine_floatingbodies, rotational_dofs, translational_dofs  # noqa: F401
 from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineReflected, DirectBEM,  # noqa: F401
                            ExactGuevelDelhommeau, GFWu, GreensFunction, IndirectBEM, Rankine, RankineReflected,
@@ -19,6 +19,7 @@ from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineR
                            partition_greens_functions)
 from .meshes import (Mesh, StaticArraysMesh, barge_mesh, combine_meshes, config1_hemisphere,  # noqa: F401
                      config2_cylinder, disc_lid_mesh, face_fields, face_fields_jacobian, hemisphere_mesh, random_body, smesh, tiny_static_mesh, vertical_cylinder_mesh)
+from .mesh_io import mesh_from_arrays, mesh_from_capytaine, read_gdf, write_gdf  # noqa: F401
 from .problems import (SETTINGS, DiffractionProblem, DiffractionResult, RadiationProblem,  # noqa: F401
                        RadiationResult, added_mass, compute_encountered_values, compute_wavenumber,
                        diffraction_force, make_result, radiation_coefficients, radiation_damping, remake, set_g,

@@ -117,6 +117,34 @@ def solve_linear(ctx, D, S, bc, direct=True, precision=_lib.MH_PREC_FP64):
     return phi, src
 
 
+def solve_pullback(ctx, D, S, bc, phi_bar, direct=True, sources_bar=None, precision=_lib.MH_PREC_FP64):
+    """mh_solve_pullback with host buffers: (phi, sources, D_bar, S_bar, bc_bar)."""
+    D = _c128(D)
+    S = _c128(S)
+    n = D.shape[0]
+    b = np.asarray(bc, dtype=np.complex128)
+    vec = b.ndim == 1
+    if b.shape[0] != n or S.shape != (n, n) or D.shape != (n, n):
+        raise ValueError("dimension mismatch between D, S and bc")
+    B = np.asfortranarray(b.reshape(n, -1, order="F"))
+    Pb = np.asfortranarray(np.asarray(phi_bar, dtype=np.complex128).reshape(B.shape, order="F"))
+    Sb = None if sources_bar is None else np.asfortranarray(
+        np.asarray(sources_bar, dtype=np.complex128).reshape(B.shape, order="F"))
+    phi = np.empty_like(B, order="F")
+    src = None if direct else np.empty_like(B, order="F")
+    Dbar = np.empty((n, n), dtype=np.complex128, order="F")
+    Sbar = np.empty((n, n), dtype=np.complex128, order="F")
+    bcbar = np.empty_like(B, order="F")
+    ctx.check(ctx._L.mh_solve_pullback(ctx.handle, n, B.shape[1], D.ctypes.data, S.ctypes.data, B.ctypes.data,
+                                       int(bool(direct)), Pb.ctypes.data, None if Sb is None else Sb.ctypes.data,
+                                       int(precision), phi.ctypes.data, None if direct else src.ctypes.data,
+                                       Dbar.ctypes.data, Sbar.ctypes.data, bcbar.ctypes.data, MH_MEM_HOST),
+              "solve pullback")
+    if vec:
+        return phi[:, 0].copy(), (None if direct else src[:, 0].copy()), Dbar, Sbar, bcbar[:, 0].copy()
+    return phi, src, Dbar, Sbar, bcbar
+
+
 def wu_wave_terms(ctx, hh, vv):
     hh = np.ascontiguousarray(np.asarray(hh, dtype=np.float64).ravel())
     vv = np.ascontiguousarray(np.asarray(vv, dtype=np.float64).ravel())
@@ -228,7 +256,7 @@ def batch_hydro(ctx, dmeshes, omegas_per_body, rho, g, gfs, direct, dofs_per_bod
 
 
 def hydro_vjp(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, rad_idx, inf_idx, abar, bbar, betas=(), fbar=None,
-              precision=_lib.MH_PREC_FP64):
+              precision=_lib.MH_PREC_FP64, direct=True):
     """mh_hydro_vjp with host buffers: cotangents abar, bbar of shape (n_inf, n_rad, n_omega),
     fbar complex (n_inf, n_omega, n_beta).
 
@@ -252,14 +280,15 @@ def hydro_vjp(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, rad_idx, inf_id
     gd = np.empty((dofs.shape[0], n, 3))
     p = lambda a: a.ctypes.data if a.size else None
     ctx.check(ctx._L.mh_hydro_vjp(
-        ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), dofs.shape[0],
-        dofs.ctypes.data, ri.size, p(ri), ii.size, ii.ctypes.data, be.size, p(be), p(ab), p(bb), p(fb),
+        ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), int(bool(direct)),
+        dofs.shape[0], dofs.ctypes.data, ri.size, p(ri), ii.size, ii.ctypes.data, be.size, p(be), p(ab), p(bb), p(fb),
         int(precision), ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data, gv.ctypes.data,
         gd.ctypes.data, MH_MEM_HOST), "hydro_vjp")
     return J.value, gc, gn, ga, gv, gd
 
 
-def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx, precision=_lib.MH_PREC_FP64):
+def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx, precision=_lib.MH_PREC_FP64,
+                   direct=True):
     """mh_hydro_gradient with host buffers.
 
     Returns (J, gc (n,3), gn (n,3), ga (n,), gv (n,4,3), gd (n_obj,n,3)): the objective
@@ -276,7 +305,7 @@ def hydro_gradient(ctx, dmesh: DeviceMesh, omegas, rho, g, gfs, dofs, obj_idx, p
     gv = np.empty((n, 4, 3))
     gd = np.empty((oi.size, n, 3))
     ctx.check(ctx._L.mh_hydro_gradient(
-        ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), dofs.shape[0],
-        dofs.ctypes.data, oi.size, oi.ctypes.data, int(precision), ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data,
+        ctx.handle, dmesh.handle, om.size, om.ctypes.data, float(rho), float(g), int(gfs), int(bool(direct)),
+        dofs.shape[0], dofs.ctypes.data, oi.size, oi.ctypes.data, int(precision), ctypes.byref(J), gc.ctypes.data, gn.ctypes.data, ga.ctypes.data,
         gv.ctypes.data, gd.ctypes.data, MH_MEM_HOST), "hydro_gradient")
     return J.value, gc, gn, ga, gv, gd

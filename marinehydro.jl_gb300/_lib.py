@@ -30,6 +30,9 @@ GF_WU = 32
 GF_EXACT_DELHOMMEAU = 64
 GF_SURROGATE = 128
 
+# MH_ABI_VERSION of include/marinehydro_gb300.h that these bindings follow
+ABI_VERSION = 2
+
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = (
     "mh_abi_version", "mh_create", "mh_destroy", "mh_last_error", "mh_get_stream", "mh_set_stream",
@@ -40,7 +43,7 @@ EXPORTS = (
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
     "mh_surrogate_wave_terms", "mh_surrogate_loss_grad", "mh_tile_table_set", "mh_tile_table_get", "mh_autotune",
-    "mh_probe_wait_timeout", "mh_hydro_frequency_derivative", "mh_hydro_vjp",
+    "mh_probe_wait_timeout", "mh_hydro_frequency_derivative", "mh_hydro_vjp", "mh_solve_pullback",
 )
 
 
@@ -104,14 +107,15 @@ def load(path: str | None = None):
                                                          vp, i64, vp, I, I, vp, vp, vp, vp, vp, I]
         L.mh_batch_release.argtypes = [vp]
         L.mh_probe_wait_timeout.argtypes = [vp, ctypes.c_uint32]
-        L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, I,
+        L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, I,
                                    vp, vp, vp, vp, vp, vp, I]
+        L.mh_solve_pullback.argtypes = [vp, i64, i64, vp, vp, vp, I, vp, vp, I, vp, vp, vp, vp, vp, I]
         L.mh_hydro_frequency_derivative.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64,
                                                     vp] + [vp] * 10 + [I]
         L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]
         L.mh_tile_table_get.argtypes = [vp, i64, vp, vp, vp]
         L.mh_autotune.argtypes = [vp, I, i64, vp, i64, I, vp, vp]
-        L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, i64, vp, i64, vp, I, vp, vp, vp, vp, vp, vp, I]
+        L.mh_hydro_gradient.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, I, vp, vp, vp, vp, vp, vp, I]
         L.mh_surrogate_param_count.restype = I
         L.mh_surrogate_train.argtypes = [vp, i64, ctypes.c_uint64, I, I, D, vp, vp]
         L.mh_surrogate_set.argtypes = [vp, vp]
@@ -120,6 +124,9 @@ def load(path: str | None = None):
         L.mh_assemble_matrices_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, D, u32, I, I, vp, vp, vp]
         for name in EXPORTS:
             getattr(L, name)  # AttributeError if the build lacks a declared entry point
+        if L.mh_abi_version() != ABI_VERSION:
+            raise MarineHydroError(f"{p} reports ABI version {L.mh_abi_version()}, these bindings need "
+                                   f"{ABI_VERSION}: rebuild the library")
         _lib = L
         return _lib
 

@@ -72,6 +72,17 @@ def linsolve_adjoint(A, ybar, precision="fp64", ctx=None):
     return _device.linsolve(_ctx(ctx), A, ybar, _prec(precision), adjoint=True)
 
 
+def solve_pullback(D, S, bc, phi_bar, direct=True, sources_bar=None, precision="fp64", ctx=None):
+    """The reverse-mode pullback of solve(D, S, bc; direct) (matrix_assembly.jl:436-449) through
+    the _mulvec and _linearsolve rules (ad_rules.jl:300-414), on the device
+    (mh_solve_pullback).  Given the cotangent phi_bar of the potential (and, indirect,
+    sources_bar of the sources) returns (phi, sources, D_bar, S_bar, bc_bar) with Julia's
+    complex conventions: direct lambda = D^-H phi_bar, D_bar = -lambda phi^H,
+    S_bar = lambda bc^H, bc_bar = S^H lambda; indirect lambda = K^-H (S^H phi_bar +
+    sources_bar), S_bar = phi_bar sources^H, D_bar = -lambda sources^H, bc_bar = lambda."""
+    return _device.solve_pullback(_ctx(ctx), D, S, bc, phi_bar, direct, sources_bar, _prec(precision))
+
+
 def solve_linear(D, S, bc, direct=True, precision="fp64", ctx=None):
     """solve(D, S, bc; direct) -> (phi, sources) (matrix_assembly.jl:436-449)."""
     return _device.solve_linear(_ctx(ctx), D, S, bc, direct, _prec(precision))
@@ -308,7 +319,8 @@ def hydrodynamic_coefficients_derivative(body: FloatingBody, parameters: dict,
     Returns the keys of hydrodynamic_coefficients (zero forward speed, shapes with n_U = 1)
     plus "d_added_mass", "d_radiation_damping", "d_diffraction_force",
     "d_Froude_Krylov_force", "d_excitation_force" (d/d omega, same shapes).  FP64, the
-    Rankine kinds with GFWu, direct or indirect, lids included (mh_hydro_frequency_derivative).
+    Rankine kinds with GFWu or ExactGuevelDelhommeau, direct or indirect, lids included
+    (mh_hydro_frequency_derivative).
     """
     f = formulation or DirectBEM()
     if any(u != 0 for u in parameters.get("forward_speeds", [0.0])):
@@ -393,16 +405,15 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     The panel centres, normals and areas must be those meshes.face_fields derives from
     the vertices (they are differentiated through it); rigid rotation dofs follow the
     panel centres and are chained through them, other dof fields are held fixed.
-    DirectBEM with the Birk Rankine family and GFWu, zero forward speed, FP64
-    arithmetic; formulation precision "mixed" factors in FP32 and refines both the
-    forward and the adjoint solve to the FP64 backward-error test.
+    DirectBEM or IndirectBEM with the Birk Rankine family and GFWu or
+    ExactGuevelDelhommeau, zero forward speed, FP64 arithmetic; formulation precision
+    "mixed" factors in FP32 and refines both the forward and the adjoint solve to the
+    FP64 backward-error test.
 
     Returns (J, dJ/dvertices as an (nvertices, 3) array); with return_panel_terms the
     raw per-panel terms of the C-ABI come back as a third item (a dict).
     """
     f = formulation or DirectBEM()
-    if not is_direct(f):
-        raise ValueError("hydro_gradient differentiates the direct formulation")
     if body.lid_mesh is not None:
         raise ValueError("hydro_gradient does not cover bodies with a lid")
     mesh = body.mesh
@@ -415,7 +426,8 @@ def hydro_gradient(body: FloatingBody, wave_frequencies, objective_dofs, formula
     g = SETTINGS["g"] if g is None else g
     oms = np.atleast_1d(np.asarray(wave_frequencies, dtype=float))
     J, gc, gn, ga, gv, gd = _device.hydro_gradient(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
-                                                    body.dof_array(names), [idx[d] for d in obj], f.precision_code)
+                                                    body.dof_array(names), [idx[d] for d in obj], f.precision_code,
+                                                    is_direct(f))
     grad = _vertex_gradient(body, gc, gn, ga, gv, {name: gd[h] for h, name in enumerate(obj)})
     if return_panel_terms:
         return J, grad, {"centers": gc, "normals": gn, "areas": ga, "corners": gv, "dofs": gd}
@@ -433,10 +445,9 @@ def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_d
     -- what Zygote / Enzyme reverse mode gives for the reference (ad_rules.jl:79-414).
     Hand-written on the device (mh_hydro_vjp): one adjoint solve per radiating dof, heading
     and frequency with the LU factors reused, pair derivatives recomputed.  Same scope as
-    hydro_gradient (DirectBEM, Birk Rankine family with GFWu, zero forward speed, no lid)."""
+    hydro_gradient (DirectBEM or IndirectBEM, Birk Rankine family with GFWu or
+    ExactGuevelDelhommeau, zero forward speed, no lid)."""
     f = formulation or DirectBEM()
-    if not is_direct(f):
-        raise ValueError("hydro_vjp differentiates the direct formulation")
     if body.lid_mesh is not None:
         raise ValueError("hydro_vjp does not cover bodies with a lid")
     mesh = body.mesh
@@ -457,7 +468,7 @@ def hydro_vjp(body: FloatingBody, wave_frequencies, radiating_dofs, influenced_d
     g = SETTINGS["g"] if g is None else g
     J, gc, gn, ga, gv, gd = _device.hydro_vjp(ctx_, mesh.device_mesh(ctx_), oms, rho, g, gf_flags(f.greens),
                                               body.dof_array(names), [idx[d] for d in rad], [idx[d] for d in inf],
-                                              ab, bb, betas, fb, f.precision_code)
+                                              ab, bb, betas, fb, f.precision_code, is_direct(f))
     return J, _vertex_gradient(body, gc, gn, ga, gv, {name: gd[idx[name]] for name in set(rad) | set(inf)})
 
 

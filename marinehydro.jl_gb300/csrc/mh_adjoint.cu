@@ -7,9 +7,15 @@
 //
 // Objective weights.  With J = sum Re(W^S_ij dS_ij + W^D_ij dD_ij) over pairs,
 // the caller supplies, per wavenumber, the weight factors as vectors
-//   W^S_ij = c sum_h lam_h[i] b_h[j],   W^D_ij = -c sum_h lam_h[i] phi_h[j]
+//   W^S_ij = c sum_h lS_h[i] rS_h[j],   W^D_ij = -c sum_h lD_h[i] rD_h[j]
 // (rank-nh outer products, never formed), and for the wavenumber-independent
 // Rankine part the real, frequency-summed matrices RS = Re sum W^S, RD = Re sum W^D.
+// Direct BEM (phi = D^-1 S b, lam = D^-T w for the force weights w): lS = lD = lam,
+// rS = b, rD = phi.  Indirect BEM (sigma = K^-1 b, phi = S sigma, lam = K^-T S^T w):
+// lS = w, rS = rD = sigma, lD = lam -- the _mulvec and _linearsolve rules
+// (ad_rules.jl:300-414) applied to the two formulations of solve (matrix_assembly.jl:436-449).
+// The pair kernels are templated on the formulation: the indirect D differentiates the
+// field point and carries the field panel's normal.
 //
 // Per-panel gradient accumulators (device, FP64, atomically summed):
 //   gc[n][3] centre, gn[n][3] normal, ga[n] area, gv[n][12] Birk corner vertices.
@@ -291,8 +297,12 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* red /*NV * 4*
 }
 
 // ---------------------------------------------------------------------------
-// static (Rankine + image, Birk) adjoint, direct formulation, real weights
+// static (Rankine + image, Birk) adjoint, real weights.  Direct: D = a (n_j . g) with g the
+// source gradient of the panel integral at the field point (or its image).  Indirect: the
+// field-point gradient of the same integral, -M g (M = diag(1, 1, -1) for the image point),
+// with the field panel's normal: D = a (nv . g), nv = -M n_i.
 // ---------------------------------------------------------------------------
+template <bool DIRECT>
 __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p, const double* __restrict__ RS,
                                                                const double* __restrict__ RD, GradPtrs gp) {
   __shared__ PanelRec sp[kCols];
@@ -309,14 +319,14 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
   }
   __syncthreads();
   const bool active = i < n;
-  double ci[3] = {0, 0, 0};
+  double ci[3] = {0, 0, 0}, ni[3] = {0, 0, 0};
   if (active)
-    for (int c = 0; c < 3; ++c) ci[c] = p.P[i].c[c];
+    for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
   const bool need_R = (p.gfs & MH_GF_RANKINE) != 0;
   const bool need_I = (p.gfs & (MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE)) != 0;
   const double image_sign = ((p.gfs & MH_GF_RANKINE_REFLECTED) ? 1.0 : 0.0) -
                             ((p.gfs & MH_GF_RANKINE_REFLECTED_NEGATIVE) ? 1.0 : 0.0);
-  double gci[3] = {0, 0, 0};
+  double gci[3] = {0, 0, 0}, gni[3] = {0, 0, 0};
   for (int jj = 0; jj < ncol; ++jj) {
     const int64_t j = j0 + jj;
     const PanelRec& Pj = sp[jj];
@@ -326,7 +336,6 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
     for (int q = 0; q < 19; ++q) col[q] = 0.0;
     if (active) {
       const double ws = RS[i + j * n], wd = RD[i + j * n];
-      const double* nv = Pj.n;  // direct: source normal
       for (int img = 0; img < 2; ++img) {
         if (img == 0 && !need_R) continue;
         if (img == 1 && !need_I) continue;
@@ -334,10 +343,14 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
         const double pt[3] = {ci[0], ci[1], img ? -ci[2] : ci[2]};
         const double zf = img ? -1.0 : 1.0;  // d pt / d ci_z
         const double a = kMinusInv4Pi * sgn;
+        double nv[3];
+        if (DIRECT) { nv[0] = Pj.n[0]; nv[1] = Pj.n[1]; nv[2] = Pj.n[2]; }
+        else { nv[0] = -ni[0]; nv[1] = -ni[1]; nv[2] = -zf * ni[2]; }
         double rb[3] = {pt[0] - Pj.c[0], pt[1] - Pj.c[1], pt[2] - Pj.c[2]};
         double r = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+        double g[3];  // source gradient of the integral (far field: A rb / r^3)
         if (r > 7 * Pj.radius) {
-          // S = a A/r ; D = a A (n . rb)/r^3
+          // S = a A/r ; D = a A (nv . rb)/r^3
           const double r3 = r * r * r, r5 = r3 * r * r, A = Pj.area;
           const double nr = nv[0] * rb[0] + nv[1] * rb[1] + nv[2] * rb[2];
           for (int c = 0; c < 3; ++c) {
@@ -346,11 +359,11 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
             const double gtot = ws * dS + wd * dD;  // d/d pt_c
             gci[c] += (c == 2 ? zf : 1.0) * gtot;
             col[c] -= gtot;  // d/d c_j = - d/d pt
-            col[3 + c] += wd * a * A * rb[c] / r3;  // d/d n_j
+            g[c] = A * rb[c] / r3;
           }
           col[6] += ws * a / r + wd * a * nr / r3;  // d/d A_j
         } else {
-          double dphi[15], dg[3][15], phi, g[3];
+          double dphi[15], dg[3][15], phi;
           birk_near_jacobian(pt, p.V + 12 * j, dphi, dg, phi, g);
           for (int q = 0; q < 15; ++q) {
             const double dS = a * dphi[q];
@@ -359,7 +372,11 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
             if (q < 3) gci[q] += (q == 2 ? zf : 1.0) * gtot;
             else col[7 + (q - 3)] += gtot;
           }
-          for (int c = 0; c < 3; ++c) col[3 + c] += wd * a * g[c];
+        }
+        // d/d normal: the source's (direct) or the field panel's through nv = -M n_i (indirect)
+        for (int c = 0; c < 3; ++c) {
+          if (DIRECT) col[3 + c] += wd * a * g[c];
+          else gni[c] -= wd * a * (c == 2 ? zf : 1.0) * g[c];
         }
       }
     }
@@ -374,22 +391,53 @@ __global__ void __launch_bounds__(kRows) static_adjoint_kernel(AssemblyParams p,
     }
   }
   if (active)
-    for (int c = 0; c < 3; ++c) atomicAdd(gp.gc + 3 * i + c, gci[c]);
+    for (int c = 0; c < 3; ++c) {
+      atomicAdd(gp.gc + 3 * i + c, gci[c]);
+      if (!DIRECT) atomicAdd(gp.gn + 3 * i + c, gni[c]);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Wu wave adjoint, direct formulation, one wavenumber, complex rank-nh weights
+// wave adjoint (Wu or exact Delhommeau), one wavenumber, complex rank-nh weights
 // ---------------------------------------------------------------------------
 struct WaveWeights {
-  const double2* lam;  // n x nh
-  const double2* b;    // n x nh
-  const double2* phi;  // n x nh
+  const double2* lS;  // n x nh:  W^S_ij = c sum_h lS_h[i] rS_h[j]
+  const double2* rS;
+  const double2* lD;  //          W^D_ij = -c sum_h lD_h[i] rD_h[j]
+  const double2* rD;
   int nh;
-  double2 c;           // objective factor of this frequency
+  double2 c;          // objective factor of this frequency
 };
 
 __device__ __forceinline__ double2 cmulz(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+constexpr int kWaveWu = 1, kWaveExact = 2;
+
+// index of the unordered pair i <= j in the packed upper triangle
+__device__ __forceinline__ int64_t packed_pair(int64_t i, int64_t j) { return j * (j + 1) / 2 + i; }
+
+// The exact term and its first and second derivatives in (r, z) = (hh, vv) as duals, from
+// G and dG/dr at the pair: dG/dz = G + 2/d (d = |(r, z)|, the relation the primal uses,
+// exact_Guevel_Delhommeau.jl:52-59), so G_zz = G_z - 2 z/d^3 and G_rz = G_r - 2 r/d^3; the
+// wave term is harmonic below the free surface, so G_rr = -G_r/r - G_zz.  For r <= 1e-6
+// (where the primal zeroes every horizontal term) G_rr only ever meets zero weights and is
+// set to 0.
+__device__ void egd_terms_from_values(double2 G, double2 Gr, double r, double z, CR<Dn<2>>& GF, CR<Dn<2>>& Gh,
+                                      CR<Dn<2>>& Gv) {
+  const double d = hypot(r, z);
+  const double id3 = 1.0 / (d * d * d);
+  const double2 Gz = make_double2(G.x + 2 / d, G.y);
+  const double2 Gzz = make_double2(Gz.x - 2.0 * z * id3, Gz.y);
+  const double2 Grz = make_double2(Gr.x - 2.0 * r * id3, Gr.y);
+  const double2 Grr = fabs(r) > 1e-6 ? make_double2(-Gr.x / r - Gzz.x, -Gr.y / r - Gzz.y) : make_double2(0.0, 0.0);
+  GF.x.v = G.x;   GF.x.d[0] = Gr.x;  GF.x.d[1] = Gz.x;
+  GF.y.v = G.y;   GF.y.d[0] = Gr.y;  GF.y.d[1] = Gz.y;
+  Gh.x.v = Gr.x;  Gh.x.d[0] = Grr.x; Gh.x.d[1] = Grz.x;
+  Gh.y.v = Gr.y;  Gh.y.d[0] = Grr.y; Gh.y.d[1] = Grz.y;
+  Gv.x.v = Gz.x;  Gv.x.d[0] = Grz.x; Gv.x.d[1] = Gzz.x;
+  Gv.y.v = Gz.y;  Gv.y.d[0] = Grz.y; Gv.y.d[1] = Gzz.y;
 }
 
 // contribution of one oriented pair (field f, source s) to the gradient:
@@ -455,10 +503,15 @@ __device__ void wave_pair_grad(double k, double dx, double dy, double dis, doubl
   o.gas = re(WS, dS_da) + re(WD, dD_da);
 }
 
+// One thread per unordered pair (i <= j), both orientations.  DIRECT: the pair (field f,
+// source s) enters D through the source normal and the offset s - f; indirect: through the
+// field normal and the offset f - s.  WAVE: the Wu fits on duals, or the exact term from the
+// packed values gv[2q] = G, gv[2q + 1] = dG/dr of pair q.
+template <bool DIRECT, int WAVE>
 __global__ void __launch_bounds__(kRows) wave_adjoint_kernel(AssemblyParams p, double k, WaveWeights w,
-                                                             GradPtrs gp) {
+                                                             const double2* __restrict__ gv, GradPtrs gp) {
   __shared__ PanelRec sp[kCols];
-  __shared__ double2 sl[kCols][kMaxH], sb[kCols][kMaxH], sphi[kCols][kMaxH];
+  __shared__ double2 slS[kCols][kMaxH], srS[kCols][kMaxH], slD[kCols][kMaxH], srD[kCols][kMaxH];
   __shared__ double red[7 * 4];
   const int64_t n = p.n;
   const int64_t i0 = blockIdx.x * (int64_t)kRows;
@@ -472,20 +525,25 @@ __global__ void __launch_bounds__(kRows) wave_adjoint_kernel(AssemblyParams p, d
     for (int q = threadIdx.x; q < ncol * 16; q += blockDim.x) dst[q] = src[q];
     for (int q = threadIdx.x; q < ncol * w.nh; q += blockDim.x) {
       int jj = q % ncol, h = q / ncol;
-      sl[jj][h] = w.lam[(j0 + jj) + h * n];
-      sb[jj][h] = w.b[(j0 + jj) + h * n];
-      sphi[jj][h] = w.phi[(j0 + jj) + h * n];
+      slS[jj][h] = w.lS[(j0 + jj) + h * n];
+      srS[jj][h] = w.rS[(j0 + jj) + h * n];
+      slD[jj][h] = w.lD[(j0 + jj) + h * n];
+      srD[jj][h] = w.rD[(j0 + jj) + h * n];
     }
   }
   __syncthreads();
   const bool active = i < n;
   double ci[3] = {0, 0, 0}, ni[3] = {0, 0, 0}, ai = 0.0;
-  double2 li[kMaxH], bi[kMaxH], pi_[kMaxH];
+  double2 lSi[kMaxH], rSi[kMaxH], lDi[kMaxH], rDi[kMaxH];
   if (active) {
     for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
     ai = p.P[i].area;
-    for (int h = 0; h < w.nh; ++h) { li[h] = w.lam[i + h * n]; bi[h] = w.b[i + h * n]; pi_[h] = w.phi[i + h * n]; }
+    for (int h = 0; h < w.nh; ++h) {
+      lSi[h] = w.lS[i + h * n]; rSi[h] = w.rS[i + h * n];
+      lDi[h] = w.lD[i + h * n]; rDi[h] = w.rD[i + h * n];
+    }
   }
+  const double2 cS = w.c, cD = make_double2(-w.c.x, -w.c.y);
   double gci[3] = {0, 0, 0}, gni[3] = {0, 0, 0}, gai = 0.0;
   for (int jj = 0; jj < ncol; ++jj) {
     const int64_t j = j0 + jj;
@@ -495,36 +553,43 @@ __global__ void __launch_bounds__(kRows) wave_adjoint_kernel(AssemblyParams p, d
       double hh, vv;
       reduced_coords(ci, Pj.c, k, hh, vv);
       CR<Dn<2>> GF, Gh, Gv;
-      wu_terms_t(Dn<2>::var(hh, 0), Dn<2>::var(vv, 1), GF, Gh, Gv);
+      if (WAVE == kWaveWu) {
+        wu_terms_t(Dn<2>::var(hh, 0), Dn<2>::var(vv, 1), GF, Gh, Gv);
+      } else {
+        const int64_t q = packed_pair(i, j);
+        egd_terms_from_values(gv[2 * q], gv[2 * q + 1], hh, vv, GF, Gh, Gv);
+      }
       const double dx = Pj.c[0] - ci[0], dy = Pj.c[1] - ci[1];
       const double dis = sqrt(dx * dx + dy * dy);
       // weights of (i, j) and (j, i)
       double2 WSij = make_double2(0, 0), WDij = WSij, WSji = WSij, WDji = WSij;
       for (int h = 0; h < w.nh; ++h) {
-        WSij = zadd(WSij, cmulz(li[h], sb[jj][h]));
-        WDij = zadd(WDij, cmulz(li[h], sphi[jj][h]));
-        WSji = zadd(WSji, cmulz(sl[jj][h], bi[h]));
-        WDji = zadd(WDji, cmulz(sl[jj][h], pi_[h]));
+        WSij = zadd(WSij, cmulz(lSi[h], srS[jj][h]));
+        WDij = zadd(WDij, cmulz(lDi[h], srD[jj][h]));
+        WSji = zadd(WSji, cmulz(slS[jj][h], rSi[h]));
+        WDji = zadd(WDji, cmulz(slD[jj][h], rDi[h]));
       }
-      WSij = cmulz(w.c, WSij);
-      WSji = cmulz(w.c, WSji);
-      WDij = cmulz(make_double2(-w.c.x, -w.c.y), WDij);
-      WDji = cmulz(make_double2(-w.c.x, -w.c.y), WDji);
-      PairGrad g1;
-      wave_pair_grad(k, dx, dy, dis, Pj.area, Pj.n, GF, Gh, Gv, WSij, WDij, g1);
-      for (int c = 0; c < 3; ++c) {
-        gci[c] += g1.gcf[c];
-        col[c] += g1.gcs[c];
-        col[3 + c] += g1.gns[c];
+      WSij = cmulz(cS, WSij);
+      WSji = cmulz(cS, WSji);
+      WDij = cmulz(cD, WDij);
+      WDji = cmulz(cD, WDji);
+      PairGrad g1;  // field i, source j
+      if (DIRECT) {
+        wave_pair_grad(k, dx, dy, dis, Pj.area, Pj.n, GF, Gh, Gv, WSij, WDij, g1);
+        for (int c = 0; c < 3; ++c) { gci[c] += g1.gcf[c]; col[c] += g1.gcs[c]; col[3 + c] += g1.gns[c]; }
+      } else {
+        wave_pair_grad(k, -dx, -dy, dis, Pj.area, ni, GF, Gh, Gv, WSij, WDij, g1);
+        for (int c = 0; c < 3; ++c) { gci[c] += g1.gcs[c]; col[c] += g1.gcf[c]; gni[c] += g1.gns[c]; }
       }
       col[6] += g1.gas;
       if (i != j) {
         PairGrad g2;  // field j, source i
-        wave_pair_grad(k, -dx, -dy, dis, ai, ni, GF, Gh, Gv, WSji, WDji, g2);
-        for (int c = 0; c < 3; ++c) {
-          col[c] += g2.gcf[c];
-          gci[c] += g2.gcs[c];
-          gni[c] += g2.gns[c];
+        if (DIRECT) {
+          wave_pair_grad(k, -dx, -dy, dis, ai, ni, GF, Gh, Gv, WSji, WDji, g2);
+          for (int c = 0; c < 3; ++c) { col[c] += g2.gcf[c]; gci[c] += g2.gcs[c]; gni[c] += g2.gns[c]; }
+        } else {
+          wave_pair_grad(k, dx, dy, dis, ai, Pj.n, GF, Gh, Gv, WSji, WDji, g2);
+          for (int c = 0; c < 3; ++c) { col[c] += g2.gcs[c]; gci[c] += g2.gcf[c]; col[3 + c] += g2.gns[c]; }
         }
         gai += g2.gas;
       }
@@ -545,6 +610,101 @@ __global__ void __launch_bounds__(kRows) wave_adjoint_kernel(AssemblyParams p, d
     }
     atomicAdd(gp.ga + i, gai);
   }
+}
+
+// G and dG/dr of the exact term for every unordered pair (i <= j) at wavenumber k, packed
+// (pair q = j (j + 1)/2 + i at out[2q], out[2q + 1]), one warp per pair, with the primal's
+// rules: the adaptive quadrature at the assembly's tolerance, the closed form at r = 0.
+constexpr int kEgdWarps = 4;
+__global__ void __launch_bounds__(32 * kEgdWarps) egd_pair_values_kernel(AssemblyParams p, double k, int64_t npairs,
+                                                                         double2* __restrict__ out) {
+  __shared__ double sw[kEgdWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5;
+  const int64_t q = blockIdx.x * (int64_t)kEgdWarps + warp;
+  if (q >= npairs) return;  // warp-uniform
+  int64_t j = (int64_t)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+  while (j * (j + 1) / 2 > q) --j;
+  while ((j + 1) * (j + 2) / 2 <= q) ++j;
+  const int64_t i = q - j * (j + 1) / 2;
+  double r, z;
+  reduced_coords(p.P[i].c, p.P[j].c, k, r, z);
+  double2 G, Gr;
+  if (r == 0.0) {
+    if ((threadIdx.x & 31) != 0) return;
+    const double2 f = egd_integrand<false>(0.0, 0.0, z);
+    G = make_double2(2.0 * kPi * f.x, 2.0 * kPi * f.y);
+    Gr = make_double2(0.0, 0.0);
+  } else {
+    egd_warp(r, z, p.quad_rtol, p.quad_atol, sw[warp], G, Gr);
+    if ((threadIdx.x & 31) != 0) return;
+  }
+  out[2 * q] = G;
+  out[2 * q + 1] = Gr;
+}
+
+// dS/dk and dD/dk of the exact term from the packed values: S = sc a k G(k dis, k Z) and
+// D = sc a k^2 (u G_r + n_3 G_z) (u = n . offset / dis, zero for r <= 1e-6), so with
+// (r, z) = k (dis, Z):  dS/dk = sc a (G + r G_r + z G_z),
+// dD/dk = sc a k (2 (u G_r + n_3 G_z) + u (r G_rr + z G_rz) + n_3 (r G_rz + z G_zz)).
+template <bool DIRECT>
+__global__ void __launch_bounds__(kRows) egd_dk_kernel(AssemblyParams p, double k, const double2* __restrict__ gv,
+                                                       double2* __restrict__ dS, double2* __restrict__ dD) {
+  __shared__ PanelRec sp[kCols];
+  const int64_t n = p.n;
+  const int64_t i0 = blockIdx.x * (int64_t)kRows;
+  const int64_t j0 = blockIdx.y * (int64_t)kCols;
+  const int64_t i = i0 + threadIdx.x;
+  const int ncol = (int)((n - j0) < kCols ? (n - j0) : kCols);
+  {
+    const double2* src = reinterpret_cast<const double2*>(p.P + j0);
+    double2* dst = reinterpret_cast<double2*>(sp);
+    for (int q = threadIdx.x; q < ncol * 16; q += blockDim.x) dst[q] = src[q];
+  }
+  __syncthreads();
+  if (i >= n) return;
+  double ci[3], ni[3];
+  for (int c = 0; c < 3; ++c) { ci[c] = p.P[i].c[c]; ni[c] = p.P[i].n[c]; }
+  for (int jj = 0; jj < ncol; ++jj) {
+    const int64_t j = j0 + jj;
+    const PanelRec& Pj = sp[jj];
+    double r, z;
+    reduced_coords(ci, Pj.c, k, r, z);
+    const int64_t q = i <= j ? packed_pair(i, j) : packed_pair(j, i);
+    CR<Dn<2>> GF, Gh, Gv;
+    egd_terms_from_values(gv[2 * q], gv[2 * q + 1], r, z, GF, Gh, Gv);
+    const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+    const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+    double nv[3];
+    if (p.has_fixed) { nv[0] = p.fixed[0]; nv[1] = p.fixed[1]; nv[2] = p.fixed[2]; }
+    else if (DIRECT) { nv[0] = Pj.n[0]; nv[1] = Pj.n[1]; nv[2] = Pj.n[2]; }
+    else { nv[0] = ni[0]; nv[1] = ni[1]; nv[2] = ni[2]; }
+    const double u = fabs(r) > 1e-6 ? k / r * (nv[0] * dx1 + nv[1] * dx2) : 0.0;
+    const double a = kMinusInv4Pi * Pj.area;
+    const double n3 = nv[2];
+    dS[i + j * n] = make_double2(a * (GF.x.v + r * GF.x.d[0] + z * GF.x.d[1]),
+                                 a * (GF.y.v + r * GF.y.d[0] + z * GF.y.d[1]));
+    const double ux = fabs(r) > 1e-6 ? 1.0 : 0.0;  // the horizontal term is absent for r <= 1e-6
+    dD[i + j * n] = make_double2(
+        a * k * (2.0 * (u * Gh.x.v + n3 * Gv.x.v) + ux * u * (r * Gh.x.d[0] + z * Gh.x.d[1]) +
+                 n3 * (r * Gv.x.d[0] + z * Gv.x.d[1])),
+        a * k * (2.0 * (u * Gh.y.v + n3 * Gv.y.v) + ux * u * (r * Gh.y.d[0] + z * Gh.y.d[1]) +
+                 n3 * (r * Gv.y.d[0] + z * Gv.y.d[1])));
+  }
+}
+
+// out[i + j n] = alpha sum_h U[i + h n] conj(V[j + h n])  (a rank-nh outer product, N x N)
+__global__ void outer_adj_kernel(int64_t n, int nh, const double2* __restrict__ U, const double2* __restrict__ V,
+                                 double alpha, double2* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j = blockIdx.y;
+  if (i >= n) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int h = 0; h < nh; ++h) {
+    const double2 u = U[i + h * n], v = V[j + h * n];
+    s.x += u.x * v.x + u.y * v.y;
+    s.y += u.y * v.x - u.x * v.y;
+  }
+  out[i + j * n] = make_double2(alpha * s.x, alpha * s.y);
 }
 
 // dS_W/dk and dD_W/dk of the Wu term (the S, D entries of _assemble_wu_centers_loop,
@@ -609,15 +769,15 @@ __global__ void __launch_bounds__(kRows) wave_dk_kernel(AssemblyParams p, const 
   }
 }
 
-// RS += Re(c sum_h lam_h b_h^T), RD += Re(-c sum_h lam_h phi_h^T)
+// RS += Re(c sum_h lS_h rS_h^T), RD += Re(-c sum_h lD_h rD_h^T)
 __global__ void weights_accumulate_kernel(int64_t n, WaveWeights w, double* __restrict__ RS, double* __restrict__ RD) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t j = blockIdx.y;
   if (i >= n) return;
   double2 s = make_double2(0, 0), d = s;
   for (int h = 0; h < w.nh; ++h) {
-    s = zadd(s, cmulz(w.lam[i + h * n], w.b[j + h * n]));
-    d = zadd(d, cmulz(w.lam[i + h * n], w.phi[j + h * n]));
+    s = zadd(s, cmulz(w.lS[i + h * n], w.rS[j + h * n]));
+    d = zadd(d, cmulz(w.lD[i + h * n], w.rD[j + h * n]));
   }
   s = cmulz(w.c, s);
   d = cmulz(w.c, d);
@@ -753,19 +913,59 @@ __global__ void conj_kernel(int64_t count, double2* __restrict__ x) {
 void launch_static_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* RS,
                            const double* RD, double* gc, double* gn, double* ga, double* gv) {
   dim3 grid((unsigned)((p.n + kRows - 1) / kRows), (unsigned)((p.n + kCols - 1) / kCols));
-  MH_LAUNCH(lc, st, "adjoint_static", static_adjoint_kernel<<<grid, kRows, 0, st>>>(p, RS, RD, GradPtrs{gc, gn, ga, gv}));
+  if (p.direct)
+    MH_LAUNCH(lc, st, "adjoint_static",
+              static_adjoint_kernel<true><<<grid, kRows, 0, st>>>(p, RS, RD, GradPtrs{gc, gn, ga, gv}));
+  else
+    MH_LAUNCH(lc, st, "adjoint_static",
+              static_adjoint_kernel<false><<<grid, kRows, 0, st>>>(p, RS, RD, GradPtrs{gc, gn, ga, gv}));
 }
 
-void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lam,
-                         const double2* b, const double2* phi, int nh, double2 c, double* gc, double* gn, double* ga,
-                         double* RS, double* RD) {
-  WaveWeights w{lam, b, phi, nh, c};
+void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lS,
+                         const double2* rS, const double2* lD, const double2* rD, int nh, double2 c,
+                         const double2* egd_values, double* gc, double* gn, double* ga, double* RS, double* RD) {
+  WaveWeights w{lS, rS, lD, rD, nh, c};
   dim3 grid((unsigned)((p.n + kRows - 1) / kRows), (unsigned)((p.n + kCols - 1) / kCols));
-  if (p.gfs & MH_GF_WU)
-    MH_LAUNCH(lc, st, "adjoint_wave",
-              wave_adjoint_kernel<<<grid, kRows, 0, st>>>(p, k, w, GradPtrs{gc, gn, ga, nullptr}));
+  const GradPtrs gp{gc, gn, ga, nullptr};
+  if (p.gfs & MH_GF_WU) {
+    if (p.direct)
+      MH_LAUNCH(lc, st, "adjoint_wave", (wave_adjoint_kernel<true, kWaveWu><<<grid, kRows, 0, st>>>(p, k, w, nullptr, gp)));
+    else
+      MH_LAUNCH(lc, st, "adjoint_wave", (wave_adjoint_kernel<false, kWaveWu><<<grid, kRows, 0, st>>>(p, k, w, nullptr, gp)));
+  } else if (p.gfs & MH_GF_EXACT_DELHOMMEAU) {
+    if (p.direct)
+      MH_LAUNCH(lc, st, "adjoint_wave",
+                (wave_adjoint_kernel<true, kWaveExact><<<grid, kRows, 0, st>>>(p, k, w, egd_values, gp)));
+    else
+      MH_LAUNCH(lc, st, "adjoint_wave",
+                (wave_adjoint_kernel<false, kWaveExact><<<grid, kRows, 0, st>>>(p, k, w, egd_values, gp)));
+  }
   dim3 g2((unsigned)((p.n + 255) / 256), (unsigned)p.n);
   MH_LAUNCH(lc, st, "adjoint_weights", weights_accumulate_kernel<<<g2, 256, 0, st>>>(p.n, w, RS, RD));
+}
+
+int64_t egd_packed_pairs(int64_t n) { return n * (n + 1) / 2; }
+
+void launch_egd_pair_values(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, double2* out) {
+  const int64_t m = egd_packed_pairs(p.n);
+  if (m <= 0) return;
+  MH_LAUNCH(lc, st, "egd_pair_values",
+            egd_pair_values_kernel<<<(unsigned)((m + kEgdWarps - 1) / kEgdWarps), 32 * kEgdWarps, 0, st>>>(p, k, m, out));
+}
+
+void launch_egd_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* values,
+                   double2* dS, double2* dD) {
+  dim3 grid((unsigned)((p.n + kRows - 1) / kRows), (unsigned)((p.n + kCols - 1) / kCols));
+  if (p.direct)
+    MH_LAUNCH(lc, st, "wave_dk", egd_dk_kernel<true><<<grid, kRows, 0, st>>>(p, k, values, dS, dD));
+  else
+    MH_LAUNCH(lc, st, "wave_dk", egd_dk_kernel<false><<<grid, kRows, 0, st>>>(p, k, values, dS, dD));
+}
+
+void launch_outer_adj(cudaStream_t st, LaunchCounter lc, int64_t n, int nh, const double2* U, const double2* V,
+                      double alpha, double2* out) {
+  dim3 grid((unsigned)((n + 255) / 256), (unsigned)n);
+  MH_LAUNCH(lc, st, "outer", outer_adj_kernel<<<grid, 256, 0, st>>>(n, nh, U, V, alpha, out));
 }
 
 void launch_rhs_adjoint(cudaStream_t st, LaunchCounter lc, int64_t n, const double* N, const double* A,

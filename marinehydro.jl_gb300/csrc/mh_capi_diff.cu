@@ -9,8 +9,10 @@ namespace {
 // n_inf x n_rad x n_omega, column-major) and its gradient with respect to every panel's
 // centre, normal, area, Birk corners and the dof fields.  The gradient of the dof fields
 // stays on the device (n_dofs x n x 3, *gd_out, workspace memory).
+// Direct: phi = D^-1 S b, lam = D^-T w.  Indirect: sigma = K^-1 b, phi = S sigma,
+// lam = K^-T S^T w, and the boundary conditions pair with lam instead of S^T lam.
 int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
-                   uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                   uint32_t gfs, int direct, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
                    int64_t n_inf, const int32_t* inf_idx, const double* abar, const double* bbar, int64_t n_beta,
                    const double* betas, const double* fbar, int precision, double* J, double* grad_centers,
                    double* grad_normals, double* grad_areas, double* grad_vertices, const double** gd_out, int mem) {
@@ -23,9 +25,11 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   if (n_rad > 64 || n_inf > 64 || n_beta > 64) return fail(ctx, MH_ERR_ARG, "at most 64 dofs and 64 headings each");
   if (m->n_hull != m->n) return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint does not cover meshes with a lid");
   if (!dofs || n_dofs <= 0) return fail(ctx, MH_ERR_ARG, "dof fields required");
-  const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU;
-  if (gfs == 0 || (gfs & ~allowed))
-    return fail(ctx, MH_ERR_UNSUPPORTED, "the adjoint covers the Birk Rankine family and GFWu (got 0x%x)", gfs);
+  const uint32_t allowed = MH_GF_RANKINE | MH_GF_RANKINE_REFLECTED | MH_GF_RANKINE_REFLECTED_NEGATIVE | MH_GF_WU |
+                           MH_GF_EXACT_DELHOMMEAU;
+  if (gfs == 0 || (gfs & ~allowed) || ((gfs & MH_GF_WU) && (gfs & MH_GF_EXACT_DELHOMMEAU)))
+    return fail(ctx, MH_ERR_UNSUPPORTED,
+                "the adjoint covers the Birk Rankine family with GFWu or ExactGuevelDelhommeau (got 0x%x)", gfs);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC) return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
@@ -45,7 +49,7 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   // factorization and both solves run batched over a chunk, the adjoint kernels per frequency
   size_t free_b = 0, total_b = 0;
   MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * ncol * sizeof(double2) * 6;
+  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * ncol * sizeof(double2) * 7;
   if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2) + (size_t)n * ncol * sizeof(double2) * 3;
   const size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
   const int64_t chunk = std::min<int64_t>(n_omega, (int64_t)std::max<size_t>(1, budget / per_w));
@@ -63,6 +67,11 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(bstride * chunk), &X));
   MH_TRY(ws_get_t(ctx, kSlotLam, (size_t)(bstride * chunk), &lam));
   MH_TRY(ws_get_t(ctx, kSlotT, (size_t)(bstride * chunk), &t));
+  double2* Y = nullptr;  // indirect: phi = S sigma (X holds sigma)
+  if (!direct) MH_TRY(ws_get_t(ctx, kSlotY, (size_t)(bstride * chunk), &Y));
+  const bool exact = (gfs & MH_GF_EXACT_DELHOMMEAU) != 0;
+  double2* gvals = nullptr;  // exact term: G, dG/dr of every unordered pair at one wavenumber
+  if (exact) MH_TRY(ws_get_t(ctx, kSlotEgd, (size_t)(2 * egd_packed_pairs(n)), &gvals));
   MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, ncol, chunk), &work));
   MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(ni * ncol * n_omega), &F));
   MH_TRY(ws_get_t(ctx, kSlotFK, (size_t)(ni * std::max<int64_t>(nb, 1) * n_omega), &FK));
@@ -98,12 +107,12 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
   MH_CUDA(ctx, cudaMemsetAsync(RS, 0, sizeof(double) * nn, st));
   MH_CUDA(ctx, cudaMemsetAsync(RD, 0, sizeof(double) * nn, st));
   const uint32_t stk = gfs & kStaticKinds;
-  AssemblyParams pst = make_params(ctx, m, stk, 1, 1, nullptr);
+  AssemblyParams pst = make_params(ctx, m, stk, direct, 1, nullptr);
   if (stk) {
     launch_assemble_static(st, lc, pst, SR, DR);
     MH_TRY(check_launch(ctx, "static assembly"));
   }
-  AssemblyParams p = make_params(ctx, m, gfs, 1, 1, nullptr);
+  AssemblyParams p = make_params(ctx, m, gfs, direct, 1, nullptr);
   // host staging in pageable memory (the mixed solver owns the pinned block)
   std::vector<double> hsmall(nsmall, 0.0);
   for (int64_t w = 0; w < n_omega; ++w) {
@@ -146,14 +155,20 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
     launch_assemble_wave(st, lc, p, stk ? SR : nullptr, stk ? DR : nullptr, (int)nw, ks_d + w0, S, D, (int64_t)nn,
                          stk ? 0 : 1);
     launch_build_rhs(st, lc, eg, (int)nw, om_d + w0, g, (int)nr, rad_d, (int)nb, beta_d, B, bstride);
-    // phi = D^-1 S b, forces, and mu = D^-H conj(w) for the force weights w
+    // phi = D^-1 S b (direct) or phi = S K^-1 b (indirect), the forces, and the force weights
+    // conj(w) (into lam, for the A^H solves)
+    double2* Phi = direct ? X : Y;
     auto forces_and_weights = [&]() {
-      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)ncol, X, bstride, (int)ni, inf_d, (int)nb, beta_d,
+      if (!direct) zgemm_nn_batched(st, lc, d, S, X, ncol, bstride, Y, work);  // phi = S sigma
+      launch_forces(st, lc, eg, (int)nw, om_d + w0, rho, g, (int)ncol, Phi, bstride, (int)ni, inf_d, (int)nb, beta_d,
                     F + w0 * ni * ncol, FK + w0 * ni * nb1);
       for (int64_t w = 0; w < nw; ++w)
         launch_force_weights(st, lc, n, m->N, m->A, dofs_d, inf_d, (int)ni, (int)ncol, cw + (w0 + w) * ni * ncol,
                              omegas[w0 + w], rho, lam + w * bstride);
+      // indirect: the adjoint solve's right-hand side is conj(S^T w) = S^H conj(w), into t
+      if (!direct) zgemm_adj_batched(st, lc, d, S, lam, ncol, bstride, t, work);
     };
+    double2* adj = direct ? lam : t;  // the right-hand sides of the A^H solve
     bool done = false;
     if (precision == MH_PREC_MIXED) {
       // FP32 factors, both solves refined to FP64 backward error; any column that does not
@@ -161,38 +176,51 @@ int hydro_vjp_core(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* o
       float2* LU32;
       double* anrm;
       MH_TRY(factor_mixed(ctx, d, D, &LU32, &anrm));
-      zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
+      if (direct) zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
+      else MH_CUDA(ctx, cudaMemcpyAsync(X, B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st));
       bool ok_fwd = false, ok_adj = false;
       MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, X, ncol, bstride, false, &ok_fwd, nullptr));
       if (ok_fwd) {
         forces_and_weights();
-        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, lam, ncol, bstride, true, &ok_adj, nullptr));
+        MH_TRY(refine_mixed(ctx, d, D, LU32, anrm, adj, ncol, bstride, true, &ok_adj, nullptr));
       }
       done = ok_fwd && ok_adj;
     }
     if (!done) {
-      zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
+      if (direct) zgemm_nn_batched(st, lc, d, S, B, ncol, bstride, X, work);
+      else MH_CUDA(ctx, cudaMemcpyAsync(X, B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st));
       lu_factor_batched<double>(st, lc, d, D, ipiv, info, oz_ws, oz_flag);
-      lu_solve_batched<double>(st, lc, d, D, ipiv, X, ncol, bstride, false);   // X = phi
+      lu_solve_batched<double>(st, lc, d, D, ipiv, X, ncol, bstride, false);    // phi (direct) / sigma
       forces_and_weights();
-      lu_solve_batched<double>(st, lc, d, D, ipiv, lam, ncol, bstride, true);  // mu = D^-H conj(w)
+      lu_solve_batched<double>(st, lc, d, D, ipiv, adj, ncol, bstride, true);   // conj(lam)
     }
     MH_TRY(check_launch(ctx, "gradient solves"));
     MH_TRY(check_pivots(ctx, d, w0));
-    zgemm_adj_batched(st, lc, d, S, lam, ncol, bstride, t, work);              // S^H mu
-    launch_conj(st, lc, nw * bstride, t);                                      // t = S^T lam
-    launch_conj(st, lc, nw * bstride, lam);                                    // lam = D^-T w
+    if (direct) {
+      zgemm_adj_batched(st, lc, d, S, lam, ncol, bstride, t, work);  // S^H conj(lam)
+      launch_conj(st, lc, nw * bstride, t);                          // t = S^T lam
+      launch_conj(st, lc, nw * bstride, lam);                        // lam = D^-T w
+    } else {
+      launch_conj(st, lc, nw * bstride, t);                          // t = lam = K^-T S^T w
+      launch_conj(st, lc, nw * bstride, lam);                        // lam buffer = w
+    }
     for (int64_t w = 0; w < nw; ++w) {
       const double om = omegas[w0 + w], k = om * om / g;
-      // wave-term gradient (GFWu only) and the frequency-summed Rankine weights, the
-      // cotangent factors already in lam; the wave kernel takes up to four columns at a time
+      if (exact) launch_egd_pair_values(st, lc, p, k, gvals);
+      // wave-term gradient and the frequency-summed Rankine weights, the cotangent factors
+      // already in the vectors; the wave kernel takes up to four columns at a time
       for (int64_t c0 = 0; c0 < ncol; c0 += 4) {
         const int64_t off = w * bstride + c0 * n;
-        launch_wave_adjoint(st, lc, p, k, lam + off, B + off, X + off, (int)std::min<int64_t>(4, ncol - c0),
-                            make_double2(1.0, 0.0), gc, gn, ga, RS, RD);
+        const int nh = (int)std::min<int64_t>(4, ncol - c0);
+        if (direct)
+          launch_wave_adjoint(st, lc, p, k, lam + off, B + off, lam + off, X + off, nh, make_double2(1.0, 0.0), gvals,
+                              gc, gn, ga, RS, RD);
+        else
+          launch_wave_adjoint(st, lc, p, k, lam + off, X + off, t + off, X + off, nh, make_double2(1.0, 0.0), gvals,
+                              gc, gn, ga, RS, RD);
       }
       launch_rhs_adjoint(st, lc, n, m->N, m->A, m->C, dofs_d, rad_d, (int)nr, inf_d, (int)ni, (int)nb, beta_d, om,
-                         rho, g, cw + (w0 + w) * ni * ncol, X + w * bstride, t + w * bstride, gc, gn, ga, gd);
+                         rho, g, cw + (w0 + w) * ni * ncol, Phi + w * bstride, t + w * bstride, gc, gn, ga, gd);
     }
     MH_TRY(check_launch(ctx, "gradient frequencies"));
   }
@@ -249,9 +277,10 @@ int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* m, int64_t n_omega, 
   if (n_rad < 0 || n_inf < 0 || n_beta < 0 || n_dofs < 0) return fail(ctx, MH_ERR_ARG, "negative counts");
   if (n_rad + n_beta == 0) return fail(ctx, MH_ERR_ARG, "nothing to solve: no radiating dof and no wave direction");
   if ((n_rad > 0 || n_inf > 0) && (!dofs || n_dofs <= 0)) return fail(ctx, MH_ERR_ARG, "dof fields required");
+  if ((gfs & MH_GF_SURROGATE) || ((gfs & MH_GF_WU) && (gfs & MH_GF_EXACT_DELHOMMEAU)))
+    return fail(ctx, MH_ERR_UNSUPPORTED,
+                "the frequency derivative covers the Rankine kinds with GFWu or ExactGuevelDelhommeau (got 0x%x)", gfs);
   MH_TRY(check_gfs(ctx, gfs));
-  if (gfs & (MH_GF_EXACT_DELHOMMEAU | MH_GF_SURROGATE))
-    return fail(ctx, MH_ERR_UNSUPPORTED, "the frequency derivative covers the Rankine kinds and GFWu (got 0x%x)", gfs);
   if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
   if (!(rho > 0) || !(g > 0)) return fail(ctx, MH_ERR_ARG, "rho and g must be positive");
   for (int64_t w = 0; w < n_omega; ++w)
@@ -331,13 +360,25 @@ int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* m, int64_t n_omega, 
   AssemblyParams p = make_params(ctx, m, gfs, direct, 1, nullptr);
   const BatchDesc d{n, 1, (int64_t)nn};
   LaunchCounter lc = ctx->lc();
+  const bool exact = (gfs & MH_GF_EXACT_DELHOMMEAU) != 0;
+  double2* gvals = nullptr;  // exact term: G, dG/dr of every unordered pair at one wavenumber
+  if (exact) MH_TRY(ws_get_t(ctx, kSlotEgd, (size_t)(2 * egd_packed_pairs(n)), &gvals));
   auto times = [&](const double2* A, const double2* in, double2* out) {
     zgemm_nn_batched(s0, lc, d, A, in, nrhs, bstride, out, work);
   };
   for (int64_t w = 0; w < n_omega; ++w) {
     const double om = omegas[w];
     launch_assemble_wave(s0, lc, p, SR, DR, 1, ks_all + w, S, D, (int64_t)nn, st ? 0 : 1);
-    launch_wave_dk(s0, lc, p, ks_all + w, dS, dD);
+    if (exact) {
+      const double kw = om * om / g;
+      launch_egd_pair_values(s0, lc, p, kw, gvals);
+      launch_egd_dk(s0, lc, p, kw, gvals, dS, dD);
+    } else if (gfs & MH_GF_WU) {
+      launch_wave_dk(s0, lc, p, ks_all + w, dS, dD);
+    } else {
+      MH_CUDA(ctx, cudaMemsetAsync(dS, 0, sizeof(double2) * nn, s0));
+      MH_CUDA(ctx, cudaMemsetAsync(dD, 0, sizeof(double2) * nn, s0));
+    }
     launch_build_rhs(s0, lc, eg, 1, om_d + w, g, (int)n_rad, rad_d, (int)n_beta, beta_d, B, bstride);
     launch_build_drhs(s0, lc, eg, 1, om_d + w, g, (int)n_rad, rad_d, (int)n_beta, beta_d, dB, bstride);
     MH_TRY(check_launch(ctx, "frequency-derivative assembly"));
@@ -448,7 +489,7 @@ int mh_hydro_frequency_derivative(mh_context* ctx, mh_mesh* m, int64_t n_omega, 
 }
 
 int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
-                      uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
+                      uint32_t gfs, int direct, int64_t n_dofs, const double* dofs, int64_t n_obj, const int32_t* obj_idx,
                       int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
                       double* grad_vertices, double* grad_dofs, int mem) {
   NvtxRange nvtx_range("mh_hydro_gradient");
@@ -460,7 +501,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
   for (int64_t w = 0; w < n_omega; ++w)
     for (int64_t h = 0; h < n_obj; ++h) bar[(size_t)(h + n_obj * (h + n_obj * w))] = 1.0;
   const double* gd = nullptr;
-  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_obj, obj_idx, n_obj, obj_idx,
+  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, direct, n_dofs, dofs, n_obj, obj_idx, n_obj, obj_idx,
                         bar.data(), bar.data(), 0, nullptr, nullptr, precision, J, grad_centers, grad_normals,
                         grad_areas, grad_vertices, &gd, mem));
   for (int64_t h = 0; h < n_obj; ++h)
@@ -470,7 +511,7 @@ int mh_hydro_gradient(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double
 }
 
 int mh_hydro_vjp(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* omegas, double rho, double g,
-                 uint32_t gfs, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
+                 uint32_t gfs, int direct, int64_t n_dofs, const double* dofs, int64_t n_rad, const int32_t* rad_idx,
                  int64_t n_inf, const int32_t* inf_idx, int64_t n_beta, const double* betas,
                  const double* added_mass_bar, const double* radiation_damping_bar, const double* excitation_force_bar,
                  int precision, double* J, double* grad_centers, double* grad_normals, double* grad_areas,
@@ -501,11 +542,95 @@ int mh_hydro_vjp(mh_context* ctx, mh_mesh* m, int64_t n_omega, const double* ome
   std::vector<double> hb((size_t)std::max<int64_t>(n_beta, 1));
   MH_TRY(get(hb.data(), betas, (size_t)n_beta));
   const double* gd = nullptr;
-  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, n_dofs, dofs, n_rad, rad_idx, n_inf, inf_idx,
+  MH_TRY(hydro_vjp_core(ctx, m, n_omega, omegas, rho, g, gfs, direct, n_dofs, dofs, n_rad, rad_idx, n_inf, inf_idx,
                         ab.data(), bb.data(), n_beta, hb.data(), fb.data(), precision, J, grad_centers, grad_normals,
                         grad_areas, grad_vertices, &gd, mem));
   MH_TRY(copy_out(ctx, grad_dofs, gd, sizeof(double) * 3 * m->n * n_dofs, mem));
   return sync(ctx, "vector-Jacobian product");
+}
+
+int mh_solve_pullback(mh_context* ctx, int64_t n, int64_t nrhs, const double* D, const double* S, const double* bc,
+                      int direct, const double* phi_bar, const double* sources_bar, int precision, double* phi,
+                      double* sources, double* D_bar, double* S_bar, double* bc_bar, int mem) {
+  NvtxRange nvtx_range("mh_solve_pullback");
+  if (!ctx) return MH_ERR_ARG;
+  if (n <= 0 || nrhs <= 0) return fail(ctx, MH_ERR_ARG, "bad sizes n=%lld nrhs=%lld", (long long)n, (long long)nrhs);
+  if (!D || !S || !bc || !phi_bar || !phi) return fail(ctx, MH_ERR_ARG, "D, S, bc, phi_bar and phi must not be NULL");
+  if (!direct && !sources) return fail(ctx, MH_ERR_ARG, "the indirect method needs a `sources` buffer");
+  if (direct && sources_bar) return fail(ctx, MH_ERR_ARG, "the direct method has no sources to take a cotangent of");
+  if (precision != MH_PREC_FP64 && precision != MH_PREC_MIXED && precision != MH_PREC_FP64_TC)
+    return fail(ctx, MH_ERR_ARG, "bad precision %d", precision);
+  if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  if (n > kMaxOrder) return fail(ctx, MH_ERR_UNSUPPORTED, "order %lld exceeds the supported %lld", (long long)n, (long long)kMaxOrder);
+  MH_TRY(set_device(ctx));
+  const size_t nn = (size_t)n * (size_t)n, nx = (size_t)n * (size_t)nrhs;
+  cudaStream_t st = ctx->stream;
+  const LaunchCounter lc = ctx->lc();
+  double2 *Ad, *Sd, *Bd, *Pb, *X, *T, *Y, *work;
+  MH_TRY(ws_get_t(ctx, kSlotA64, nn, &Ad));
+  MH_TRY(ws_get_t(ctx, kSlotS, nn, &Sd));
+  MH_TRY(ws_get_t(ctx, kSlotIn, nx, &Bd));
+  MH_TRY(ws_get_t(ctx, kSlotLam, nx, &Pb));
+  MH_TRY(ws_get_t(ctx, kSlotT, nx, &T));
+  MH_TRY(ws_get_t(ctx, kSlotY, nx, &Y));
+  MH_TRY(copy_in(ctx, Ad, D, nn * sizeof(double2), mem));
+  MH_TRY(copy_in(ctx, Sd, S, nn * sizeof(double2), mem));
+  MH_TRY(copy_in(ctx, Bd, bc, nx * sizeof(double2), mem));
+  MH_TRY(copy_in(ctx, Pb, phi_bar, nx * sizeof(double2), mem));
+  const BatchDesc d{n, 1, (int64_t)nn};
+  // the adjoint solve A^H x = rhs with the factors of the forward solve (FP64 modes), or a
+  // fresh mixed-precision solve of the caller's matrix
+  auto adjoint_solve = [&](double2* rhs) -> int {
+    if (precision == MH_PREC_MIXED) {
+      MH_TRY(copy_in(ctx, Ad, D, nn * sizeof(double2), mem));
+      return solve_core(ctx, d, Ad, rhs, nrhs, (int64_t)nx, precision, true);
+    }
+    int32_t* ipiv;
+    MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)n, &ipiv));
+    lu_solve_batched<double>(st, lc, d, Ad, ipiv, rhs, nrhs, (int64_t)nx, true);
+    return check_launch(ctx, "adjoint solve");
+  };
+  MH_TRY(ws_get_t(ctx, kSlotX, nx, &X));
+  if (direct) {
+    // phi = D^-1 (S bc);  lam = D^-H phi_bar;  D_bar = -lam phi^H, S_bar = lam bc^H, bc_bar = S^H lam
+    MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, 1), &work));
+    zgemm_nn_batched(st, lc, d, Sd, Bd, nrhs, (int64_t)nx, X, work);
+    MH_TRY(check_launch(ctx, "S*bc"));
+    MH_TRY(solve_core(ctx, d, Ad, X, nrhs, (int64_t)nx, precision, false));
+    MH_CUDA(ctx, cudaMemcpyAsync(T, Pb, nx * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    MH_TRY(adjoint_solve(T));
+    MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, 1), &work));
+    zgemm_adj_batched(st, lc, d, Sd, T, nrhs, (int64_t)nx, Y, work);  // bc_bar
+    launch_outer_adj(st, lc, n, (int)nrhs, T, Bd, 1.0, Sd);            // S_bar (S no longer needed)
+    launch_outer_adj(st, lc, n, (int)nrhs, T, X, -1.0, Ad);            // D_bar
+    MH_TRY(check_launch(ctx, "pullback"));
+    MH_TRY(copy_out(ctx, phi, X, nx * sizeof(double2), mem));
+  } else {
+    // sigma = K^-1 bc, phi = S sigma;  lam = K^-H (S^H phi_bar + sources_bar);
+    // S_bar = phi_bar sigma^H, K_bar = -lam sigma^H, bc_bar = lam
+    MH_CUDA(ctx, cudaMemcpyAsync(X, Bd, nx * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    MH_TRY(solve_core(ctx, d, Ad, X, nrhs, (int64_t)nx, precision, false));
+    MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, 1), &work));
+    zgemm_nn_batched(st, lc, d, Sd, X, nrhs, (int64_t)nx, Y, work);    // phi
+    zgemm_adj_batched(st, lc, d, Sd, Pb, nrhs, (int64_t)nx, T, work);  // S^H phi_bar
+    if (sources_bar) {
+      double2* sb;
+      MH_TRY(ws_get_t(ctx, kSlotR, nx, &sb));
+      MH_TRY(copy_in(ctx, sb, sources_bar, nx * sizeof(double2), mem));
+      launch_zaxpy(st, lc, (int64_t)nx, 1.0, sb, T);
+    }
+    MH_TRY(check_launch(ctx, "S products"));
+    MH_TRY(adjoint_solve(T));                                          // lam
+    launch_outer_adj(st, lc, n, (int)nrhs, Pb, X, 1.0, Sd);            // S_bar
+    launch_outer_adj(st, lc, n, (int)nrhs, T, X, -1.0, Ad);            // K_bar
+    MH_TRY(check_launch(ctx, "pullback"));
+    MH_TRY(copy_out(ctx, phi, Y, nx * sizeof(double2), mem));
+    MH_TRY(copy_out(ctx, sources, X, nx * sizeof(double2), mem));
+  }
+  if (D_bar) MH_TRY(copy_out(ctx, D_bar, Ad, nn * sizeof(double2), mem));
+  if (S_bar) MH_TRY(copy_out(ctx, S_bar, Sd, nn * sizeof(double2), mem));
+  if (bc_bar) MH_TRY(copy_out(ctx, bc_bar, direct ? Y : T, nx * sizeof(double2), mem));
+  return sync(ctx, "solve pullback");
 }
 
 }  // extern "C"

@@ -222,9 +222,21 @@ void launch_forces(cudaStream_t st, LaunchCounter lc, const EpilogueGeom& g, int
 // adjoint (mh_adjoint.cu)
 void launch_static_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* RS,
                            const double* RD, double* gc, double* gn, double* ga, double* gv);
-void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lam,
-                         const double2* b, const double2* phi, int nh, double2 c, double* gc, double* gn, double* ga,
-                         double* RS, double* RD);
+// weights W^S = c lS rS^T, W^D = -c lD rD^T (n x nh each); egd_values: the packed exact
+// values of launch_egd_pair_values at k when p.gfs holds MH_GF_EXACT_DELHOMMEAU
+void launch_wave_adjoint(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* lS,
+                         const double2* rS, const double2* lD, const double2* rD, int nh, double2 c,
+                         const double2* egd_values, double* gc, double* gn, double* ga, double* RS, double* RD);
+// G and dG/dr of the exact term for the egd_packed_pairs(n) unordered pairs at wavenumber k
+// (2 complex values per pair, pair (i <= j) at index j (j + 1)/2 + i)
+int64_t egd_packed_pairs(int64_t n);
+void launch_egd_pair_values(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, double2* out);
+// dS/dk, dD/dk of the exact wave part from those values (n x n complex, no static part)
+void launch_egd_dk(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, double k, const double2* values,
+                   double2* dS, double2* dD);
+// out = alpha U V^H for n x nh complex U, V (an n x n complex matrix)
+void launch_outer_adj(cudaStream_t st, LaunchCounter lc, int64_t n, int nh, const double2* U, const double2* V,
+                      double alpha, double2* out);
 // cw: n_inf x n_rad complex cotangent factors c[q, r] of one frequency (device);
 // gd: n_dofs x n x 3, indexed by the dof indices in rad / inf
 // (cw: n_inf x (n_rad + n_beta); the heading columns follow the radiating ones)

@@ -271,6 +271,36 @@ def solve(D, S, bc, direct=True, lapack=False):
     return S @ src, src
 
 
+def solve_pullback(D, S, bc, phi_bar, direct=True, sources_bar=None, lapack=False):
+    """Reverse-mode pullback of solve(D, S, bc; direct) (matrix_assembly.jl:436-449) by the
+    reference's rules: _mulvec y = S bc -> S_bar = ybar bc', bc_bar = S' ybar
+    (ad_rules.jl:300-312) and _linearsolve y = A \\ b -> lambda = A' \\ ybar,
+    A_bar = -lambda y', b_bar = lambda (ad_rules.jl:360-371); ' is the adjoint.
+    Returns (phi, sources, D_bar, S_bar, bc_bar)."""
+    D = np.asarray(D, dtype=np.complex128)
+    S = np.asarray(S, dtype=np.complex128)
+    b = np.asarray(bc, dtype=np.complex128)
+    pb = np.asarray(phi_bar, dtype=np.complex128)
+    outer = lambda u, v: (u.reshape(len(u), -1) @ v.reshape(len(v), -1).conj().T)
+    if direct:
+        y = S @ b
+        phi = linsolve(D, y, lapack)
+        lam = linsolve(D.conj().T, pb, lapack)    # _linearsolve pullback
+        D_bar = -outer(lam, phi)
+        S_bar = outer(lam, b)                      # _mulvec pullback with ybar = lam
+        bc_bar = S.conj().T @ lam
+        return phi, None, D_bar, S_bar, bc_bar
+    src = linsolve(D, b, lapack)
+    phi = S @ src
+    S_bar = outer(pb, src)                         # _mulvec pullback
+    src_bar = S.conj().T @ pb
+    if sources_bar is not None:
+        src_bar = src_bar + np.asarray(sources_bar, dtype=np.complex128)
+    lam = linsolve(D.conj().T, src_bar, lapack)   # _linearsolve pullback
+    D_bar = -outer(lam, src)
+    return phi, src, D_bar, S_bar, lam
+
+
 # --------------------------------------------------------------------------
 # O(N) physics around the solve (numpy)
 # --------------------------------------------------------------------------

@@ -52,7 +52,9 @@ def test_library_exports_every_declared_symbol(libpath):
 
 def test_library_loads_and_reports_version(libpath, mh):
     L = mh.load_library()
-    assert L.mh_abi_version() == 1
+    with open(os.path.join(REPO, "include", "marinehydro_gb300.h")) as f:
+        declared = int(re.search(r"#define MH_ABI_VERSION (\d+)", f.read()).group(1))
+    assert L.mh_abi_version() == declared
     for n in declared_functions():
         assert hasattr(L, n)
 

@@ -75,44 +75,93 @@ def test_gradient_matches_finite_differences(mh, ctx, gf, obj):
         assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
 
 
-def _oracle_objective(oracle, body, obj):
+def _oracle_objective(oracle, body, obj, gfs, direct):
     J = 0.0
     for om in OMEGAS:
         A, B, _, _, _ = oracle.hydro_one_frequency(body.mesh, body.dofs, om, rho=1025.0, g=9.81, radiating=obj,
-                                                   influenced=obj)
+                                                   influenced=obj, gfs=gfs, direct=direct)
         J += float(np.trace(A) + np.trace(B))
     return J
 
 
+@pytest.mark.parametrize("gf", ["Wu", "ExactGuevelDelhommeau"])
+@pytest.mark.parametrize("direct", [True, False])
 @pytest.mark.parametrize("obj", [["c1__Heave", "c2__Heave"], ["c1__Pitch", "c2__Heave"]])
-def test_gradient_matches_oracle_finite_differences(mh, oracle, ctx, obj):
+def test_gradient_matches_oracle_finite_differences(mh, oracle, ctx, obj, direct, gf):
     """The device adjoint against central differences of the CPU oracle (not of the device sweep):
-    the two-cylinder mesh of 120 panels, the same affine moves, h = 1e-6."""
+    the two-cylinder mesh of 120 panels, the same affine moves; DirectBEM and IndirectBEM, the Wu
+    and the exact Guevel-Delhommeau wave terms.  h = 1e-6: the moves are large affine maps, whose
+    h^2 truncation already reaches 2e-5 at h = 1e-5; the oracle's quadrature noise (1e-13 of J)
+    over h stays near 1e-7."""
     m1, m2 = _geometry(mh)
     dofs = ["Heave", "Pitch"]
     body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
     assert body.mesh.nfaces <= 150
-    J, grad = mh.hydro_gradient(body, OMEGAS, obj, mh.DirectBEM(), ctx=ctx, rho=1025.0, g=9.81)
-    J_oracle = _oracle_objective(oracle, body, obj)
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)(gf)
+    gfs = oracle.DEFAULT_WU if gf == "Wu" else oracle.DEFAULT_EGD
+    h = H
+    J, grad = mh.hydro_gradient(body, OMEGAS, obj, F, ctx=ctx, rho=1025.0, g=9.81)
+    J_oracle = _oracle_objective(oracle, body, obj, gfs, direct)
     assert abs(J - J_oracle) <= 1e-8 * abs(J_oracle)
     n1 = m1.nvertices
     rng = np.random.default_rng(23)
     for d1, d2 in _affine_moves(m1.vertices, m2.vertices, rng):
-        jp = _oracle_objective(oracle, _body(mh, m1.vertices + H * d1, m2.vertices + H * d2, m1, m2, dofs), obj)
-        jm = _oracle_objective(oracle, _body(mh, m1.vertices - H * d1, m2.vertices - H * d2, m1, m2, dofs), obj)
-        fd = (jp - jm) / (2 * H)
+        jp = _oracle_objective(oracle, _body(mh, m1.vertices + h * d1, m2.vertices + h * d2, m1, m2, dofs), obj,
+                               gfs, direct)
+        jm = _oracle_objective(oracle, _body(mh, m1.vertices - h * d1, m2.vertices - h * d2, m1, m2, dofs), obj,
+                               gfs, direct)
+        fd = (jp - jm) / (2 * h)
         ad = float(np.sum(grad[:n1] * d1) + np.sum(grad[n1:] * d2))
         scale = np.abs(grad).sum() * max(np.abs(d1).max(), np.abs(d2).max())
         assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * scale), (ad, fd)
 
 
+@pytest.mark.parametrize("direct", [True, False])
+def test_vjp_with_full_cotangents_matches_oracle(mh, oracle, ctx, direct):
+    """General cotangents of A, B and the excitation forces, IndirectBEM and DirectBEM, against
+    central differences of the oracle's sweep along one affine move."""
+    m1, m2 = _geometry(mh)
+    dofs = ["Heave", "Pitch"]
+    body = _body(mh, m1.vertices, m2.vertices, m1, m2, dofs)
+    names = list(body.dofs)
+    rng = np.random.default_rng(31)
+    betas = [0.0, 1.1]
+    ab = rng.standard_normal((4, 4, len(OMEGAS)))
+    bb = rng.standard_normal((4, 4, len(OMEGAS)))
+    fb = rng.standard_normal((4, len(OMEGAS), 2)) + 1j * rng.standard_normal((4, len(OMEGAS), 2))
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)()
+    J, grad = mh.hydro_vjp(body, OMEGAS, names, names, ab, bb, F, ctx=ctx, rho=1025.0, g=9.81,
+                           wave_directions=betas, excitation_force_bar=fb)
+
+    def objective(b):
+        tot = 0.0
+        for w, om in enumerate(OMEGAS):
+            A, B, _, _, Fe = oracle.hydro_one_frequency(b.mesh, b.dofs, om, rho=1025.0, g=9.81, betas=betas,
+                                                        direct=direct)
+            tot += np.sum(ab[:, :, w] * A) + np.sum(bb[:, :, w] * B)
+            tot += np.sum(fb[:, w, :].real * Fe.real + fb[:, w, :].imag * Fe.imag)
+        return float(tot)
+
+    assert abs(J - objective(body)) <= 1e-8 * abs(J)
+    M = rng.standard_normal((3, 3))
+    M[2, :2] = 0.0
+    d1 = m1.vertices @ M.T
+    d2 = np.zeros_like(m2.vertices)
+    jp = objective(_body(mh, m1.vertices + H * d1, m2.vertices, m1, m2, dofs))
+    jm = objective(_body(mh, m1.vertices - H * d1, m2.vertices, m1, m2, dofs))
+    fd = (jp - jm) / (2 * H)
+    ad = float(np.sum(grad[:m1.nvertices] * d1))
+    assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-3 * np.abs(grad).sum() * np.abs(d1).max()), (ad, fd)
+
+
 def test_gradient_rejects_unsupported(mh, ctx):
     m1, m2 = _geometry(mh)
     body = _body(mh, m1.vertices, m2.vertices, m1, m2, ["Heave"])
+    both = (mh.Rankine(), mh.RankineReflected(), mh.GFWu(), mh.ExactGuevelDelhommeau())
     with pytest.raises(ValueError):
-        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.IndirectBEM(), ctx=ctx)
+        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.DirectBEM(both), ctx=ctx)
     with pytest.raises(ValueError):
-        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.DirectBEM("ExactGuevelDelhommeau"), ctx=ctx)
+        mh.hydro_gradient(body, OMEGAS, ["c1__Heave"], mh.DirectBEM("Surrogate"), ctx=ctx)
 
 
 def _soup(mh, V4, C, N, A, R):

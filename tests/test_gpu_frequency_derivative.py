@@ -5,7 +5,8 @@ checks it against central finite differences (test/outputs_differentiation.jl:39
 solve_problem_differentiation.jl:89-110, diffraction_differentiation.jl:63-78).  Here the
 forward-mode device derivative is checked against central differences of the GPU sweep
 and of the CPU oracle (h = 1e-5 omega: truncation ~h^2, rounding ~1e-11), bar 1e-6 of the
-largest entry of each array; the coefficients themselves equal the plain sweep's.
+largest entry of each array, for the Wu and the exact Guevel-Delhommeau wave terms; the
+coefficients themselves equal the plain sweep's.
 """
 import numpy as np
 import pytest
@@ -60,14 +61,23 @@ def test_derivative_with_lid_and_several_frequencies(mh, ctx):
         assert close(res["d_excitation_force"][:, w], fd["excitation_force"][:, 0], 1e-6)
 
 
-def test_derivative_matches_oracle_differences(mh, oracle, ctx):
+@pytest.mark.parametrize("gf,direct", [("Wu", True), ("ExactGuevelDelhommeau", True),
+                                       ("ExactGuevelDelhommeau", False)])
+def test_derivative_matches_oracle_differences(mh, oracle, ctx, gf, direct):
+    """The device derivative against central differences of the CPU oracle, with the Wu term and
+    with the exact Guevel-Delhommeau term (the latter as ForwardDiff over omega with
+    ExactGuevelDelhommeau in test/outputs_differentiation.jl:70-84); h = 1e-5 omega."""
     mesh = mh.hemisphere_mesh(1.0, 6, 12)
     body = mh.FloatingBody(mesh, ["Heave", "Surge"])
     om, h = 1.4, 1.4e-5
+    F = (mh.DirectBEM if direct else mh.IndirectBEM)(gf)
+    gfs = oracle.DEFAULT_WU if gf == "Wu" else oracle.DEFAULT_EGD
     res = mh.hydrodynamic_coefficients_derivative(body, {"wave_frequencies": [om], "radiating_dofs": ["Heave", "Surge"],
-                                                         "wave_directions": [0.0]}, ctx=ctx, rho=1025.0)
-    hi = oracle.hydro_one_frequency(mesh, body.dofs, om + h, rho=1025.0, betas=[0.0], lapack=True)
-    lo = oracle.hydro_one_frequency(mesh, body.dofs, om - h, rho=1025.0, betas=[0.0], lapack=True)
+                                                         "wave_directions": [0.0]}, F, ctx=ctx, rho=1025.0)
+    hi = oracle.hydro_one_frequency(mesh, body.dofs, om + h, rho=1025.0, betas=[0.0], lapack=True, gfs=gfs,
+                                    direct=direct)
+    lo = oracle.hydro_one_frequency(mesh, body.dofs, om - h, rho=1025.0, betas=[0.0], lapack=True, gfs=gfs,
+                                    direct=direct)
     dA, dB, dFd, dFk, dFe = [(a - b) / (2 * h) for a, b in zip(hi, lo)]
     assert close(res["d_added_mass"][:, :, 0, 0], dA, 1e-6)
     assert close(res["d_radiation_damping"][:, :, 0, 0], dB, 1e-6)
@@ -80,4 +90,4 @@ def test_derivative_rejects_other_green_functions(mh, ctx):
     body = mh.FloatingBody(mh.hemisphere_mesh(1.0, 4, 8), ["Heave"])
     with pytest.raises(ValueError, match="frequency derivative covers"):
         mh.hydrodynamic_coefficients_derivative(body, {"wave_frequencies": [1.0], "radiating_dofs": ["Heave"]},
-                                                mh.DirectBEM("ExactGuevelDelhommeau"), ctx=ctx)
+                                                mh.DirectBEM("Surrogate"), ctx=ctx)
