@@ -381,6 +381,23 @@ int mh_surrogate_wave_terms(mh_context* ctx, int64_t m, const double* r, const d
 int mh_surrogate_loss_grad(mh_context* ctx, const float* params, int64_t m, const float* inputs, const float* targets,
                            float* grad, double* loss);
 
+/* The exact path's check of surrogate results (no counterpart in the reference; the
+   surrogate approximates exact_Guevel_Delhommeau.jl:15-46).  With n_samples > 0, every
+   sweep (mh_hydrodynamic_coefficients) and batch that assembles with MH_GF_SURROGATE has
+   each frequency's S and D checked against the exact term on n_samples ordered panel
+   pairs drawn from `seed` (the adaptive quadrature at the context's tolerance): the
+   estimate is the relative error sqrt(sum |S - S_exact|^2 + |D - D_exact|^2) /
+   sqrt(sum |S|^2 + |D|^2) over the sampled entries.  A frequency whose estimate exceeds
+   `tolerance` is solved with the exact term instead (the sweep assembles that matrix
+   again before its factorization; the batch re-runs those frequency-solves after its
+   graph).  n_samples = 0 turns the check off (the default). */
+int mh_surrogate_set_judge(mh_context* ctx, int64_t n_samples, uint64_t seed, double tolerance);
+/* The estimates (count doubles) and re-run flags (count int32, 1 = solved with the exact
+   term) of the last judged sweep or batch, one per frequency-solve in output order (a
+   batch: bodies in input order); count must equal that call's number of frequency-solves.
+   Either output may be NULL. */
+int mh_surrogate_judge_read(mh_context* ctx, int64_t count, double* estimates, int32_t* rerun);
+
 /* ---- wave-term evaluators (kernel-level parity entry points) ------------- */
 /* _wu_wave_term_and_derivs(hh, vv) (wu.jl:28-37) for m points: out 3 complex
    per point (GF, dGF/dhh, dGF/dvv), i.e. 6 doubles. */

@@ -10,7 +10,7 @@ from ._lib import (Context, MarineHydroError, default_context, load as load_libr
 from .api import (airy_bc, airy_pressure, assemble_matrices, autotune, load_tile_table, assemble_matrix_wu, batch_hydrodynamic_coefficients,  # noqa
                   calculate_radiation_forces,
                   compute_bc, compute_hydrodynamic_coefficients, excitation_force, froude_krylov_force,
-                  gpu_linsolve, hydro_gradient, hydro_vjp, hydrodynamic_coefficients, hydrodynamic_coefficients_derivative, load_surrogate, set_surrogate, surrogate_wave_terms, train_surrogate, integrate_pressure, linsolve, linsolve_adjoint,
+                  gpu_linsolve, hydro_gradient, hydro_vjp, hydrodynamic_coefficients, hydrodynamic_coefficients_derivative, load_surrogate, set_surrogate, set_surrogate_judge, surrogate_judge_report, surrogate_wave_terms, train_surrogate, integrate_pressure, linsolve, linsolve_adjoint,
                   problems_from_data, radiation_bc, solve, solve_linear, solve_problem, solve_pullback)
 from .bodies import FloatingBody, combine_floatingbodies, rotational_dofs, translational_dofs  # noqa: F401
 from .formulations import (BEMFormulation, DelhommeauRankine, DelhommeauRankineReflected, DirectBEM,  # noqa: F401

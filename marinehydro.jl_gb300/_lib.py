@@ -44,6 +44,7 @@ EXPORTS = (
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
     "mh_surrogate_wave_terms", "mh_surrogate_loss_grad", "mh_tile_table_set", "mh_tile_table_get", "mh_autotune",
     "mh_probe_wait_timeout", "mh_hydro_frequency_derivative", "mh_hydro_vjp", "mh_solve_pullback",
+    "mh_surrogate_set_judge", "mh_surrogate_judge_read",
 )
 
 
@@ -110,6 +111,8 @@ def load(path: str | None = None):
         L.mh_hydro_vjp.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64, vp, vp, vp, vp, I,
                                    vp, vp, vp, vp, vp, vp, I]
         L.mh_solve_pullback.argtypes = [vp, i64, i64, vp, vp, vp, I, vp, vp, I, vp, vp, vp, vp, vp, I]
+        L.mh_surrogate_set_judge.argtypes = [vp, i64, ctypes.c_uint64, D]
+        L.mh_surrogate_judge_read.argtypes = [vp, i64, vp, vp]
         L.mh_hydro_frequency_derivative.argtypes = [vp, vp, i64, vp, D, D, u32, I, i64, vp, i64, vp, i64, vp, i64,
                                                     vp] + [vp] * 10 + [I]
         L.mh_tile_table_set.argtypes = [vp, i64, vp, vp]

@@ -20,7 +20,7 @@ import numpy as np
 
 from . import _device, _lib
 from .bodies import FloatingBody, evaluate_gradient_of_motion
-from .formulations import BEMFormulation, DirectBEM, bem_formulation, gf_flags, is_direct
+from .formulations import BEMFormulation, DirectBEM, SurrogateDelhommeau, bem_formulation, gf_flags, is_direct
 from .meshes import StaticArraysMesh, face_fields, face_fields_jacobian
 from .problems import (DiffractionProblem, DiffractionResult, RadiationProblem, RadiationResult, SETTINGS,
                        added_mass, compute_wavenumber, make_result, radiation_damping)
@@ -262,13 +262,17 @@ def hydrodynamic_coefficients(body: FloatingBody, parameters: dict, formulation:
     g = parameters.get("g", SETTINGS["g"]) if g is None else g
     if "forward_speeds" not in parameters:
         A, B, Fd, Fk, Fe = _zero_speed_sweep(c, body, f, oms, rho, g, names, rad, inf, betas)
-        return {
+        out = {
             "added_mass": A[..., None] if rad else np.zeros(0),
             "radiation_damping": B[..., None] if rad else np.zeros(0),
             "diffraction_force": Fd[..., None] if betas else np.zeros(0),
             "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
             "excitation_force": Fe[..., None] if betas else np.zeros(0),
         }
+        if _judged(c, f):
+            est, rerun = surrogate_judge_report(oms.size, c)
+            out["surrogate_judge"] = {"estimate": est, "rerun": rerun}
+        return out
     Us = [float(u) for u in parameters["forward_speeds"]]
     if rad and "wave_directions" not in parameters:
         raise ValueError("radiation problems with forward_speeds need wave_directions "
@@ -388,6 +392,13 @@ def batch_hydrodynamic_coefficients(bodies, parameters_per_body, formulation: BE
                     "diffraction_force": Fd[..., None] if betas else np.zeros(0),
                     "Froude_Krylov_force": Fk[..., None] if betas else np.zeros(0),
                     "excitation_force": Fe[..., None] if betas else np.zeros(0)})
+    if _judged(c, f):
+        counts = [len(np.atleast_1d(p["wave_frequencies"])) for p in parameters_per_body]
+        est, rerun = surrogate_judge_report(sum(counts), c)
+        off = 0
+        for o, m in zip(out, counts):
+            o["surrogate_judge"] = {"estimate": est[off:off + m], "rerun": rerun[off:off + m]}
+            off += m
     return out
 
 
@@ -558,6 +569,33 @@ def load_tile_table(path=None, ctx=None) -> list:
 
 
 SURROGATE_PARAMS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_delhommeau.npy")
+
+
+def set_surrogate_judge(n_samples=2048, tolerance=1e-3, seed=0x5EED, ctx=None):
+    """Have the exact Guevel-Delhommeau term judge every surrogate result (mh_surrogate_set_judge):
+    each frequency's surrogate-assembled S and D are checked on `n_samples` sampled panel pairs
+    against the exact term, and a frequency whose sampled relative error exceeds `tolerance`
+    is solved with the exact term instead.  n_samples = 0 turns the check off.  The
+    per-frequency estimates and re-run flags come back with the results under
+    "surrogate_judge"."""
+    c = _ctx(ctx)
+    c.check(c._L.mh_surrogate_set_judge(c.handle, int(n_samples), int(seed) & (2 ** 64 - 1), float(tolerance)),
+            "surrogate judge")
+    c._judge_on = n_samples > 0
+
+
+def surrogate_judge_report(count, ctx=None):
+    """(estimates, rerun flags) of the last judged surrogate sweep or batch (count frequency-solves)."""
+    c = _ctx(ctx)
+    est = np.empty(int(count))
+    rerun = np.empty(int(count), dtype=np.int32)
+    c.check(c._L.mh_surrogate_judge_read(c.handle, int(count), est.ctypes.data, rerun.ctypes.data),
+            "surrogate judge report")
+    return est, rerun.astype(bool)
+
+
+def _judged(c, f):
+    return getattr(c, "_judge_on", False) and any(isinstance(gf, SurrogateDelhommeau) for gf in f.greens)
 
 
 def load_surrogate(path=None, ctx=None):

@@ -730,6 +730,83 @@ __global__ void __launch_bounds__(32 * kExactWarps) exact_points_kernel(int64_t 
   }
 }
 
+// The exact path's check of a surrogate-assembled matrix (the learned term approximates
+// exact_Guevel_Delhommeau.jl:15-46): one warp per sampled ordered pair (i, j), drawn from a
+// counter-based SplitMix64 stream of (seed, matrix, sample), recomputes the pair's S and D
+// entries with the exact term (the adaptive quadrature at the assembly's tolerance; the
+// closed form at r = 0), adds the static part as the assembly does, and accumulates the
+// squared differences to the assembled entries and the squared assembled entries per matrix:
+// acc[2 b] += |dS|^2 + |dD|^2, acc[2 b + 1] += |S|^2 + |D|^2.
+__device__ __forceinline__ uint64_t judge_mix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+
+template <bool DIRECT>
+__global__ void __launch_bounds__(32 * kExactWarps) surrogate_judge_kernel(
+    AssemblyParams p, const double* __restrict__ SR, const double* __restrict__ DR, const double* __restrict__ ks,
+    const double2* __restrict__ S, const double2* __restrict__ D, int64_t sstride, int64_t n_samples, uint64_t seed,
+    int64_t first_matrix, int wave_identity, double* __restrict__ acc) {
+  __shared__ double sw[kExactWarps][8 * kGKWarpStack];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t q = blockIdx.x * (int64_t)kExactWarps + warp;
+  const int b = blockIdx.y;
+  if (q >= n_samples) return;  // warp-uniform
+  const int64_t n = p.n;
+  const uint64_t h = judge_mix(seed ^ judge_mix(((uint64_t)(first_matrix + b) << 32) ^ (uint64_t)q));
+  const int64_t i = (int64_t)((h & 0xFFFFFFFFULL) % (uint64_t)n);
+  const int64_t j = (int64_t)((h >> 32) % (uint64_t)n);
+  const double k = ks[b];
+  const PanelRec& Pi = p.P[i];
+  const PanelRec& Pj = p.P[j];
+  const double ci[3] = {Pi.c[0], Pi.c[1], Pi.c[2]};
+  double r, z;
+  reduced_coords(ci, Pj.c, k, r, z);
+  double2 GF, dGdr;
+  if (r == 0.0) {
+    if (lane != 0) return;
+    const double2 f = egd_integrand<false>(0.0, 0.0, z);
+    GF = make_double2(2.0 * kPi * f.x, 2.0 * kPi * f.y);
+    dGdr = make_double2(0.0, 0.0);
+  } else {
+    egd_warp(r, z, p.quad_rtol, p.quad_atol, sw[warp], GF, dGdr);
+    if (lane != 0) return;
+  }
+  // the (i, j) entries as exact_pair_warp and store_pair form them
+  const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+  const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+  const double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
+  double d1 = 0.0, d2 = 0.0;
+  if (fabs(r) > 1e-6) {
+    d1 = k * k / r * dx1;
+    d2 = k * k / r * dx2;
+  }
+  WaveTerms w;
+  w.I = make_double2(k * GF.x, k * GF.y);
+  w.gh[0] = make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y));
+  w.gh[1] = make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y));
+  w.gz = make_double2(k * (k * dGdz.x), k * (k * dGdz.y));
+  const double ni[3] = {Pi.n[0], Pi.n[1], Pi.n[2]};
+  double nv[3];
+  pick_normal<DIRECT>(p, Pj, ni, nv);
+  double2 sv, dv;
+  wave_entry(w, 1.0, Pj.area, nv, sv, dv);
+  if (wave_identity && i == j) dv.x += identity_jump(p, ni);
+  const int64_t idx = i + j * n;
+  if (SR) {
+    sv.x = SR[idx] + sv.x;
+    dv.x = DR[idx] + dv.x;
+  }
+  const double2 sa = S[b * sstride + idx], da = D[b * sstride + idx];
+  const double e2 = (sa.x - sv.x) * (sa.x - sv.x) + (sa.y - sv.y) * (sa.y - sv.y) + (da.x - dv.x) * (da.x - dv.x) +
+                    (da.y - dv.y) * (da.y - dv.y);
+  const double t2 = sa.x * sa.x + sa.y * sa.y + da.x * da.x + da.y * da.y;
+  atomicAdd(acc + 2 * b, e2);
+  atomicAdd(acc + 2 * b + 1, t2);
+}
+
 }  // namespace
 
 void launch_panel_geometry(cudaStream_t st, LaunchCounter lc, int64_t n, const double* V, const double* C,
@@ -813,6 +890,22 @@ void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParam
   }
 #undef MH_WAVE
   lc.post(st, mode == 1 ? "assemble_wave_wu" : "assemble_wave_exact");
+}
+
+void launch_surrogate_judge(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
+                            const double* DR, int nk, const double* ks_dev, const double2* S, const double2* D,
+                            int64_t sstride, int64_t n_samples, uint64_t seed, int64_t first_matrix,
+                            int wave_identity, double* acc) {
+  if (p.n <= 0 || nk <= 0 || n_samples <= 0) return;
+  dim3 g((unsigned)((n_samples + kExactWarps - 1) / kExactWarps), (unsigned)nk);
+  if (p.direct)
+    MH_LAUNCH(lc, st, "surrogate_judge",
+              surrogate_judge_kernel<true><<<g, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, n_samples,
+                                                                         seed, first_matrix, wave_identity, acc));
+  else
+    MH_LAUNCH(lc, st, "surrogate_judge",
+              surrogate_judge_kernel<false><<<g, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, n_samples,
+                                                                          seed, first_matrix, wave_identity, acc));
 }
 
 void launch_bessel01_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out) {

@@ -748,12 +748,44 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
   EpilogueGeom eg{n, m->n_hull, m->C, m->N, m->A, dofs_d};
   AssemblyParams p = make_params(ctx, m, gfs, direct, 1, nullptr);
   MH_TRY(prepare_surrogate(ctx, p, chunk));
+  const bool judging = (gfs & MH_GF_SURROGATE) && ctx->judge_samples > 0;
+  double* judge_acc = nullptr;
+  if (judging) {
+    MH_TRY(ws_get_t(ctx, kSlotJudge, (size_t)(2 * chunk), &judge_acc));
+    ctx->judge_err.assign((size_t)n_omega, 0.0);
+    ctx->judge_rerun.assign((size_t)n_omega, 0);
+  }
 
   for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
     const int64_t nw = std::min<int64_t>(chunk, n_omega - w0);
     launch_assemble_wave(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)nn,
                          st ? 0 : 1);
     MH_TRY(check_launch(ctx, "wave assembly"));
+    if (judging) {
+      // the exact term judges each surrogate matrix on sampled pairs; a matrix whose sampled
+      // relative error exceeds the tolerance is assembled again with the exact term
+      MH_TRY(check_surrogate(ctx, p));
+      MH_CUDA(ctx, cudaMemsetAsync(judge_acc, 0, sizeof(double) * 2 * nw, ctx->stream));
+      launch_surrogate_judge(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)nn,
+                             ctx->judge_samples, ctx->judge_seed, w0, st ? 0 : 1, judge_acc);
+      MH_TRY(check_launch(ctx, "surrogate judge"));
+      std::vector<double> hacc((size_t)(2 * nw));
+      MH_CUDA(ctx, cudaMemcpyAsync(hacc.data(), judge_acc, sizeof(double) * 2 * nw, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+      MH_TRY(sync(ctx, "surrogate judge"));
+      const AssemblyParams pe = make_params(ctx, m, (gfs & ~MH_GF_SURROGATE) | MH_GF_EXACT_DELHOMMEAU, direct, 1,
+                                            nullptr);
+      for (int64_t b = 0; b < nw; ++b) {
+        const double err = hacc[2 * b + 1] > 0 ? std::sqrt(hacc[2 * b] / hacc[2 * b + 1]) : 0.0;
+        ctx->judge_err[(size_t)(w0 + b)] = err;
+        if (!(err <= ctx->judge_tol)) {
+          ctx->judge_rerun[(size_t)(w0 + b)] = 1;
+          launch_assemble_wave(ctx->stream, ctx->lc(), pe, SR, DR, 1, ks_all + w0 + b, S + b * nn, D + b * nn,
+                               (int64_t)nn, st ? 0 : 1);
+        }
+      }
+      MH_TRY(check_launch(ctx, "exact re-assembly"));
+    }
     const int64_t bstride = n * nrhs;
     launch_build_rhs(ctx->stream, ctx->lc(), eg, (int)nw, om_d + w0, g, (int)n_rad, rad_d, (int)n_beta, beta_d, B,
                      bstride);

@@ -15,6 +15,8 @@ struct BatchOpts {
   int direct, precision, ir_sweeps;
   double rho, g;
   int64_t n_dofs, n_rad, n_inf, n_beta, nrhs;
+  int64_t judge_samples;  // surrogate batches: pairs the exact term checks per matrix (0: none)
+  uint64_t judge_seed;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -54,6 +56,7 @@ size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
     b.fb_cap = b.n * (b.nw + 64) + 4096;
     b.fb_list = (int4*)take((size_t)b.fb_cap * sizeof(int4));
     b.fb_state = (unsigned long long*)take(4 * sizeof(unsigned long long));
+    if (o.judge_samples > 0) b.judge = (double*)take(2 * nw * sizeof(double));
   }
   b.F = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
   b.FK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
@@ -77,6 +80,7 @@ size_t pinned_body(BodyPlan& b, const BatchOpts& o, char* base) {
   b.hnorms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
   b.hparams = (double*)take(b.nparams * 8);
   b.hdofs = (double*)take((size_t)o.n_dofs * (size_t)b.n * 3 * 8);
+  if ((o.gfs & MH_GF_SURROGATE) && o.judge_samples > 0) b.hjudge = (double*)take(2 * nw * sizeof(double));
   return off;
 }
 
@@ -103,6 +107,14 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   }
   launch_assemble_wave(st, lc, p, st_kinds ? b.SR : nullptr, st_kinds ? b.DR : nullptr, (int)nw, ks_d, b.S, b.D,
                        nn, st_kinds ? 0 : 1);
+  if (b.judge) {
+    // the exact term judges every surrogate matrix on sampled pairs; the host re-runs the
+    // frequency-solves whose estimate exceeds the tolerance after the graph
+    cudaMemsetAsync(b.judge, 0, sizeof(double) * 2 * nw, st);
+    launch_surrogate_judge(st, lc, p, st_kinds ? b.SR : nullptr, st_kinds ? b.DR : nullptr, (int)nw, ks_d, b.S, b.D,
+                           nn, o.judge_samples, o.judge_seed, b.w_off, st_kinds ? 0 : 1, b.judge);
+    cudaMemcpyAsync(b.hjudge, b.judge, sizeof(double) * 2 * nw, cudaMemcpyDeviceToHost, st);
+  }
   EpilogueGeom eg{n, b.m->n_hull, b.m->C, b.m->N, b.m->A, b.dofs};
   launch_build_rhs(st, lc, eg, (int)nw, om_d, o.g, (int)o.n_rad, rad_d, (int)o.n_beta, beta_d, b.B, bstride);
   BatchDesc d{n, nw, nn};
@@ -271,7 +283,9 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
     if (!(omegas[w] > 0)) return fail(ctx, MH_ERR_ARG, "wave frequencies must be positive");
   MH_TRY(set_device(ctx));
   const int S = n_streams > 0 ? (int)std::min(n_streams, 16) : 4;
-  BatchOpts o{gfs, direct ? 1 : 0, precision, 2, rho, g, n_dofs, n_rad, n_inf, n_beta, n_rad + n_beta};
+  const bool judging = (gfs & MH_GF_SURROGATE) && ctx->judge_samples > 0;
+  BatchOpts o{gfs, direct ? 1 : 0, precision, 2, rho, g, n_dofs, n_rad, n_inf, n_beta, n_rad + n_beta,
+              judging ? ctx->judge_samples : 0, judging ? ctx->judge_seed : 0};
 
   // cache key: everything the captured graph bakes in
   // with profiling on, the schedule runs uncaptured on one stream so that every launch is
@@ -279,7 +293,8 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
   const bool profiling = profiler_on(ctx->prof);
   std::vector<double> key = {(double)n_bodies, (double)gfs, (double)o.direct, (double)precision, (double)S, rho, g,
                              (double)n_dofs, (double)n_rad, (double)n_inf, (double)n_beta, ctx->quad_rtol,
-                             ctx->quad_atol, profiling ? 1.0 : 0.0};
+                             ctx->quad_atol, profiling ? 1.0 : 0.0, (double)o.judge_samples,
+                             (double)(o.judge_seed >> 32), (double)(o.judge_seed & 0xFFFFFFFFULL)};
   for (int64_t b = 0; b < n_bodies; ++b) {
     key.push_back((double)(uintptr_t)meshes[b]);
     key.push_back((double)n_omega[b]);
@@ -439,12 +454,87 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       }
     }
   }
+  if (judging) {
+    // per frequency-solve estimate; the ones above the tolerance go through the exact term
+    ctx->judge_err.assign((size_t)total_w, 0.0);
+    ctx->judge_rerun.assign((size_t)total_w, 0);
+    const uint32_t exact_gfs = (gfs & ~MH_GF_SURROGATE) | MH_GF_EXACT_DELHOMMEAU;
+    for (int64_t b = 0; b < n_bodies; ++b) {
+      BodyPlan& p = bc->bodies[b];
+      std::vector<double> redo;
+      std::vector<int64_t> redo_w;
+      for (int64_t w = 0; w < p.nw; ++w) {
+        const double e2 = p.hjudge[2 * w], t2 = p.hjudge[2 * w + 1];
+        const double err = t2 > 0 ? std::sqrt(e2 / t2) : 0.0;
+        ctx->judge_err[(size_t)(p.w_off + w)] = err;
+        if (!(err <= ctx->judge_tol)) {
+          ctx->judge_rerun[(size_t)(p.w_off + w)] = 1;
+          redo.push_back(omegas[p.w_off + w]);
+          redo_w.push_back(w);
+        }
+      }
+      if (redo.empty()) continue;
+      const double* dofs_h = nullptr;
+      if (n_dofs > 0) {
+        if (mem == MH_MEM_DEVICE)
+          MH_CUDA(ctx, cudaMemcpy(p.hdofs, dofs[b], sizeof(double) * n_dofs * p.n * 3, cudaMemcpyDeviceToHost));
+        dofs_h = mem == MH_MEM_DEVICE ? p.hdofs : dofs[b];
+      }
+      const int64_t nr = (int64_t)redo.size();
+      std::vector<double> rA((size_t)(n_inf * n_rad * nr)), rB(rA.size());
+      std::vector<double2> rd((size_t)(n_inf * nr * n_beta)), rk(rd.size()), re(rd.size());
+      // the exact re-run has no surrogate, so it leaves the judge's record of this call alone
+      MH_TRY(mh_hydrodynamic_coefficients(ctx, p.m, nr, redo.data(), rho, g, exact_gfs, direct, n_dofs, dofs_h,
+                                          n_rad, rad_idx, n_inf, inf_idx, n_beta, betas, precision,
+                                          n_rad ? (double*)rA.data() : nullptr, n_rad ? (double*)rB.data() : nullptr,
+                                          n_beta ? (double*)rd.data() : nullptr, n_beta ? (double*)rk.data() : nullptr,
+                                          n_beta ? (double*)re.data() : nullptr, MH_MEM_HOST));
+      for (int64_t q = 0; q < nr; ++q) {
+        const int64_t w = redo_w[(size_t)q];
+        for (int64_t i = 0; i < n_inf; ++i) {
+          for (int64_t r = 0; r < n_rad; ++r) {
+            const size_t dst = (size_t)(n_inf * n_rad * p.w_off) + (size_t)(i + n_inf * (r + n_rad * w));
+            const size_t src = (size_t)(i + n_inf * (r + n_rad * q));
+            hA[dst] = rA[src];
+            hB[dst] = rB[src];
+          }
+          for (int64_t bb = 0; bb < n_beta; ++bb) {
+            const size_t dst = (size_t)(n_inf * n_beta * p.w_off) + (size_t)(i + n_inf * (w + p.nw * bb));
+            const size_t src = (size_t)(i + n_inf * (q + nr * bb));
+            hd[dst] = rd[src];
+            hk[dst] = rk[src];
+            he[dst] = re[src];
+          }
+        }
+      }
+    }
+  }
   MH_TRY(put_out(ctx, added_mass, hA.data(), hA.size() * sizeof(double), mem));
   MH_TRY(put_out(ctx, radiation_damping, hB.data(), hB.size() * sizeof(double), mem));
   MH_TRY(put_out(ctx, diffraction_force, hd.data(), hd.size() * sizeof(double2), mem));
   MH_TRY(put_out(ctx, froude_krylov_force, hk.data(), hk.size() * sizeof(double2), mem));
   MH_TRY(put_out(ctx, excitation_force, he.data(), he.size() * sizeof(double2), mem));
   return sync(ctx, "batch outputs");
+}
+
+int mh_surrogate_set_judge(mh_context* ctx, int64_t n_samples, uint64_t seed, double tolerance) {
+  if (!ctx) return MH_ERR_ARG;
+  if (n_samples < 0 || n_samples > (int64_t)1 << 24) return fail(ctx, MH_ERR_ARG, "n_samples must be in [0, 2^24]");
+  if (!(tolerance >= 0)) return fail(ctx, MH_ERR_ARG, "the tolerance must be >= 0");
+  ctx->judge_samples = n_samples;
+  ctx->judge_seed = seed;
+  ctx->judge_tol = tolerance;
+  return MH_OK;
+}
+
+int mh_surrogate_judge_read(mh_context* ctx, int64_t count, double* estimates, int32_t* rerun) {
+  if (!ctx) return MH_ERR_ARG;
+  if (count != (int64_t)ctx->judge_err.size())
+    return fail(ctx, MH_ERR_ARG, "the last judged call had %lld frequency-solves, not %lld",
+                (long long)ctx->judge_err.size(), (long long)count);
+  if (estimates) std::memcpy(estimates, ctx->judge_err.data(), sizeof(double) * ctx->judge_err.size());
+  if (rerun) std::memcpy(rerun, ctx->judge_rerun.data(), sizeof(int32_t) * ctx->judge_rerun.size());
+  return MH_OK;
 }
 
 int mh_batch_release(mh_context* ctx) {

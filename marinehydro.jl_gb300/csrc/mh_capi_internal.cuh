@@ -44,6 +44,8 @@ struct BodyPlan {
   int4* fb_list = nullptr;  // learned surrogate: pairs queued for the exact kernel
   unsigned long long* fb_state = nullptr;  // queue count, overflow and timeout flags
   int64_t fb_cap = 0;
+  double* judge = nullptr;   // surrogate judge sums, 2 per frequency (device)
+  double* hjudge = nullptr;  // and their pinned copy
   double2 *hF = nullptr, *hFK = nullptr;
   int32_t* hinfo = nullptr;
   double *hnorms = nullptr, *hparams = nullptr, *hdofs = nullptr;
@@ -81,6 +83,14 @@ struct mh_context {
   std::vector<cudaStream_t> side;  // extra streams of the many-body batch schedule
   BatchCache* batch = nullptr;
   float* mlp = nullptr;  // learned surrogate parameters (BF16-rounded), device
+  // the exact term's check of surrogate results (mh_surrogate_set_judge): pairs sampled per
+  // matrix (0: off), stream seed, tolerance on the sampled relative error; the estimates and
+  // re-run flags of the last surrogate sweep or batch, one per frequency-solve
+  int64_t judge_samples = 0;
+  uint64_t judge_seed = 0;
+  double judge_tol = 0.0;
+  std::vector<double> judge_err;
+  std::vector<int32_t> judge_rerun;
   TileTable tiles;       // launch shapes of the batched LU per matrix-order bucket (mh_autotune)
   LaunchCounter lc() { return LaunchCounter{&launches, prof, &tiles}; }
 };
@@ -120,7 +130,7 @@ enum Slot {
   kSlotS = 0, kSlotD, kSlotSR, kSlotDR, kSlotB, kSlotX, kSlotWork, kSlotIpiv, kSlotInfo, kSlotLU32, kSlotX32,
   kSlotR, kSlotSmall, kSlotF, kSlotFK, kSlotDofs, kSlotIdx, kSlotNorm, kSlotA64, kSlotIn, kSlotRS, kSlotRD,
   kSlotGrad, kSlotLam, kSlotT, kSlotFb, kSlotFbState, kSlotOzaki, kSlotBx3, kSlotTcFlag, kSlotAnorm, kSlotCw,
-  kSlotY, kSlotEgd, kSlotCount
+  kSlotY, kSlotEgd, kSlotJudge, kSlotCount
 };
 
 int fail(mh_context* ctx, int code, const char* fmt, ...);

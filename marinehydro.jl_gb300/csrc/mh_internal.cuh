@@ -119,6 +119,13 @@ void launch_assemble_static(cudaStream_t st, LaunchCounter lc, const AssemblyPar
 void launch_assemble_wave(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
                           const double* DR, int nk, const double* ks_dev, double2* S, double2* D, int64_t sstride,
                           int wave_identity);
+// The exact term's check of surrogate-assembled matrices: n_samples pairs per matrix drawn from
+// (seed, first_matrix + b, sample); acc[2 b] += sum |assembled - exact|^2 over S and D entries,
+// acc[2 b + 1] += sum |assembled|^2 (acc zeroed by the caller)
+void launch_surrogate_judge(cudaStream_t st, LaunchCounter lc, const AssemblyParams& p, const double* SR,
+                            const double* DR, int nk, const double* ks_dev, const double2* S, const double2* D,
+                            int64_t sstride, int64_t n_samples, uint64_t seed, int64_t first_matrix,
+                            int wave_identity, double* acc);
 // learned surrogate (mh_surrogate.cu)
 void launch_surrogate_points(cudaStream_t st, LaunchCounter lc, const float* mlp, int64_t m, const double* r,
                              const double* z, double rtol, double atol, double2* out);
