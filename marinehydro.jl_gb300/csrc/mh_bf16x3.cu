@@ -33,6 +33,7 @@ namespace {
 
 constexpr int kBxTerms = 3;
 constexpr int kBxK = 32;                                 // panel width (the LU's kNB)
+constexpr int kBxNB = kBxK;
 constexpr int kBxTile = 128;                             // rows of an A tile = columns of a B tile
 constexpr int kBxPlane = kBxTile * kBxK * 2;             // bytes of one 128 x 32 BF16 plane
 constexpr int kBxTileBytes = 2 * kBxTerms * kBxPlane;    // 48 KB: re/im x 3 terms
@@ -84,9 +85,13 @@ __global__ void bx3_split_rows_kernel(BatchDesc d, const float2* __restrict__ A,
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (r >= ntile * kBxTile) return;
-  const int64_t n = d.n;
-  const float2* Ab = A + b * d.stride;
-  const bool live = r < rest;
+  // a grouped batch: this matrix's order, panel width and trailing size (the launch's tile
+  // count stays the stride of the term tiles)
+  const int64_t n = d.order(b);
+  if (k + kBxNB >= n) return;
+  kb = (int)((k + kBxNB < n) ? kBxNB : n - k);
+  const float2* Ab = A + d.offset(b);
+  const bool live = r < n - k - kb;
   float2 v[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
@@ -105,9 +110,11 @@ __global__ void bx3_split_cols_kernel(BatchDesc d, const float2* __restrict__ A,
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (c >= ntile * kBxTile) return;
-  const int64_t n = d.n;
-  const float2* Ab = A + b * d.stride;
-  const bool live = c < rest;
+  const int64_t n = d.order(b);
+  if (k + kBxNB >= n) return;
+  kb = (int)((k + kBxNB < n) ? kBxNB : n - k);
+  const float2* Ab = A + d.offset(b);
+  const bool live = c < n - k - kb;
   float2 v[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
@@ -129,8 +136,15 @@ __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float
   const int tid = threadIdx.x, warp = tid >> 5;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
   const int64_t ct0 = blockIdx.y * (int64_t)group;
-  const int ntiles = (int)((ntile - ct0) < group ? (ntile - ct0) : group);
-  const int64_t n = d.n;
+  // a grouped batch: CTAs past this matrix's trailing block leave before any barrier or
+  // tensor-memory allocation
+  const int64_t n = d.order(b);
+  if (k + kBxNB >= n) return;
+  kb = (int)((k + kBxNB < n) ? kBxNB : n - k);
+  rest = n - k - kb;
+  if (rt * kBxTile >= rest || ct0 * kBxTile >= rest) return;
+  const int64_t ntile_b = (rest + kBxTile - 1) / kBxTile;
+  const int ntiles = (int)((ntile_b - ct0) < group ? (ntile_b - ct0) : group);
   unsigned char* As = bsm;
   unsigned char* Bs[2] = {bsm + kBxTileBytes, bsm + 2 * kBxTileBytes};
   const unsigned char* srcA = tA + (b * ntile + rt) * (int64_t)kBxTileBytes;
@@ -165,7 +179,7 @@ __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float
   const int64_t r = rt * kBxTile + lrow;
   const bool row_live = r < rest;
   const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
-  float2* crow = A + b * d.stride + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
+  float2* crow = A + d.offset(b) + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
   bool failed = false;
   int loads_pending = ntiles > 1 ? 2 : 1, mma_pending = 0;
 

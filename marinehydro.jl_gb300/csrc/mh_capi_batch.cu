@@ -5,10 +5,12 @@
 namespace {
 
 // ---------------------------------------------------------------------------
-// Many-body batch: every body's sweep is enqueued without host synchronisation on
-// one of several streams (longest-processing-time order), the whole schedule is
-// captured into one CUDA graph, and the instantiated graph is cached for repeated
-// calls with the same bodies and options.
+// Many-body batch: the bodies are grouped into size classes (orders within a factor of
+// two); per class, on one of several streams, the bodies' assembly and right-hand sides,
+// then one grouped factorization and solve of every matrix of the class (one launch per
+// kernel and panel step for all of them), then the bodies' forces.  The whole schedule is
+// captured into one CUDA graph, and the instantiated graph is cached for repeated calls
+// with the same bodies and options.
 // ---------------------------------------------------------------------------
 struct BatchOpts {
   uint32_t gfs;
@@ -21,7 +23,8 @@ struct BatchOpts {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Lay out (or size, when base == nullptr) the device buffers of one body.
+// Lay out (or size, when base == nullptr) the device buffers of one body.  The matrices D,
+// their FP32 copies, the solutions and pivots live in the grouped arrays of the cache.
 size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
   const size_t n = (size_t)b.n, nw = (size_t)b.nw, nn = n * n, nx = n * (size_t)o.nrhs;
   const bool mixed = o.precision == MH_PREC_MIXED;
@@ -34,24 +37,12 @@ size_t layout_body(BodyPlan& b, const BatchOpts& o, char* base) {
   b.SR = (double*)take(nn * 8);
   b.DR = (double*)take(nn * 8);
   b.S = (double2*)take(nw * nn * 16);
-  b.D = (double2*)take(nw * nn * 16);
   b.B = (double2*)take(nw * nx * 16);
-  b.X = (double2*)take(nw * nx * 16);
   b.B0 = mixed ? (double2*)take(nw * nx * 16) : nullptr;
   b.R = mixed ? (double2*)take(nw * nx * 16) : nullptr;
   b.work = (double2*)take(zgemm_work_elems(b.n, o.nrhs, b.nw) * 16);
-  b.LU32 = mixed ? (float2*)take(nw * nn * 8) : nullptr;
-  b.X32 = mixed ? (float2*)take(nw * nx * 8) : nullptr;
-  b.ipiv = (int32_t*)take(nw * n * 4);
-  b.info = (int32_t*)take(nw * 4);
   b.norms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
-  if (o.precision == MH_PREC_FP64_TC) {
-    b.oz = take(ozaki_workspace_bytes(b.n, b.nw));
-    b.ozflag = (int*)take(64);
-  } else if (mixed) {
-    b.oz = take(bx3_workspace_bytes(b.n, b.nw));
-    b.ozflag = (int*)take(64);
-  }
+  if (o.precision != MH_PREC_FP64) b.ozflag = (int*)take(64);  // the tensor-core products' timeout flag
   if (o.gfs & MH_GF_SURROGATE) {  // every self pair plus room for pairs outside the training box
     b.fb_cap = b.n * (b.nw + 64) + 4096;
     b.fb_list = (int4*)take((size_t)b.fb_cap * sizeof(int4));
@@ -76,7 +67,6 @@ size_t pinned_body(BodyPlan& b, const BatchOpts& o, char* base) {
   };
   b.hF = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * o.nrhs * 16);
   b.hFK = (double2*)take(nw * (size_t)std::max<int64_t>(o.n_inf, 1) * std::max<int64_t>(o.n_beta, 1) * 16);
-  b.hinfo = (int32_t*)take(nw * 4);
   b.hnorms = (double*)take((2 * (size_t)o.nrhs * nw + nw) * 8);
   b.hparams = (double*)take(b.nparams * 8);
   b.hdofs = (double*)take((size_t)o.n_dofs * (size_t)b.n * 3 * 8);
@@ -84,14 +74,74 @@ size_t pinned_body(BodyPlan& b, const BatchOpts& o, char* base) {
   return off;
 }
 
-// One body's whole sweep, enqueued on `st` with no host synchronisation.
-void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& b, const BatchOpts& o) {
+// The grouped arrays (device, then pinned): sizes and, with a base, the pointers.
+size_t layout_grouped(BatchCache& c, const BatchOpts& o, char* base) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += align256(std::max<size_t>(bytes, 8));
+    return p;
+  };
+  size_t dn = 0, xn = 0;
+  for (auto& b : c.bodies) {
+    dn += (size_t)(b.nw * b.n * b.n);
+    xn += (size_t)(b.nw * b.n * o.nrhs);
+  }
+  const size_t M = (size_t)c.M;
+  c.D_all = (double2*)take(dn * 16);
+  c.X_all = (double2*)take(xn * 16);
+  if (o.precision == MH_PREC_MIXED) {
+    c.LU32_all = (float2*)take(dn * 8);
+    c.X32_all = (float2*)take(xn * 8);
+    c.anorm_all = (double*)take(M * 8);
+  }
+  c.ipiv_all = (int32_t*)take(M * (size_t)c.n_max * 4);
+  c.info_all = (int32_t*)take(M * 4);
+  c.orders = (int64_t*)take(M * 8);
+  c.offsets = (int64_t*)take(M * 8);
+  c.xoffsets = (int64_t*)take(M * 8);
+  for (auto& k : c.classes) {
+    if (o.precision == MH_PREC_FP64_TC) k.oz = take(ozaki_workspace_bytes(k.n_max, k.count));
+    else if (o.precision == MH_PREC_MIXED) k.oz = take(bx3_workspace_bytes(k.n_max, k.count));
+    k.ozflag = (int*)take(64);
+  }
+  return off;
+}
+
+size_t pinned_grouped(BatchCache& c, const BatchOpts& o, char* base) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += align256(std::max<size_t>(bytes, 8));
+    return p;
+  };
+  c.hinfo_all = (int32_t*)take((size_t)c.M * 4);
+  if (o.precision == MH_PREC_MIXED) c.hanorm_all = (double*)take((size_t)c.M * 8);
+  return off;
+}
+
+// `count` matrices from global index m0 of class k in the grouped layout: orders, offsets and
+// solution offsets from the global arrays, pivots at the class's stride (its largest order).
+BatchDesc grouped_desc(const BatchCache& c, const BatchCache::SizeClass& k, int64_t m0, int64_t count) {
+  BatchDesc d{k.n_max, count, 0};
+  d.orders = c.orders + m0;
+  d.offsets = c.offsets + m0;
+  d.xoffsets = c.xoffsets + m0;
+  return d;
+}
+int32_t* grouped_ipiv(const BatchCache& c, const BatchCache::SizeClass& k, int64_t m0) {
+  return c.ipiv_all + k.m_start * c.n_max + (m0 - k.m_start) * k.n_max;
+}
+
+// The body's work before the factorization, enqueued on `st` with no host synchronisation:
+// static and wave assembly (and the surrogate judge), boundary conditions, the right-hand
+// sides of the factored system.
+void enqueue_front(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& b, const BatchOpts& o) {
   const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs;
   const double* om_d = b.params;
   const double* ks_d = b.params + nw;
   const double* beta_d = b.params + 2 * nw;
   const int32_t* rad_d = (const int32_t*)(b.params + 2 * nw + o.n_beta);
-  const int32_t* inf_d = rad_d + o.n_rad;
   const uint32_t st_kinds = o.gfs & kStaticKinds;
   AssemblyParams p = make_params(ctx, b.m, o.gfs, o.direct, 1, nullptr);
   if (b.fb_state) {
@@ -119,48 +169,81 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
   launch_build_rhs(st, lc, eg, (int)nw, om_d, o.g, (int)o.n_rad, rad_d, (int)o.n_beta, beta_d, b.B, bstride);
   BatchDesc d{n, nw, nn};
   if (b.ozflag) cudaMemsetAsync(b.ozflag, 0, sizeof(int), st);
-  // S products on the tensor cores (FP64-accurate) outside the plain FP64 path
-  auto s_times = [&](const double2* in, double2* out) {
-    if (o.precision == MH_PREC_FP64) zgemm_nn_batched(st, lc, d, b.S, in, o.nrhs, bstride, out, b.work);
-    else zgemm_nn_tc_batched(st, lc, d, b.S, in, o.nrhs, bstride, out, b.work, b.ozflag);
-  };
-  if (o.direct) s_times(b.B, b.X);
-  else cudaMemcpyAsync(b.X, b.B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
-  if (o.precision == MH_PREC_FP64 || o.precision == MH_PREC_FP64_TC) {
-    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info, b.oz, b.ozflag);
-    lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
+  // direct: X = S B (on the tensor cores, FP64-accurate, outside the plain FP64 path);
+  // indirect: X = B
+  if (o.direct) {
+    if (o.precision == MH_PREC_FP64) zgemm_nn_batched(st, lc, d, b.S, b.B, o.nrhs, bstride, b.X, b.work);
+    else zgemm_nn_tc_batched(st, lc, d, b.S, b.B, o.nrhs, bstride, b.X, b.work, b.ozflag);
   } else {
-    BatchDesc d32{n, nw, nn};
-    const int64_t ncols = o.nrhs * nw;
-    cudaMemcpyAsync(b.B0, b.X, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
-    convert_with_norms(st, lc, d, b.D, b.LU32, nn, b.norms + 2 * ncols);
-    lu_factor_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.info, b.oz, b.ozflag);
-    convert_z_to_c(st, lc, b.B0, b.X32, bstride * nw);
-    lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
-    widen_c_to_z(st, lc, b.X32, b.X, bstride * nw);
-    for (int it = 0; it < o.ir_sweeps; ++it) {
-      residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
-      convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
-      lu_solve_batched<float>(st, lc, d32, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
-      ir_update(st, lc, bstride * nw, b.X, b.X32);
-    }
-    // the residual of the returned x, judged on the host after the graph
-    residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
-    for (int64_t w = 0; w < nw; ++w) {
-      inf_norms_batched(st, lc, n, o.nrhs, b.R + w * bstride, b.norms + w * o.nrhs);
-      inf_norms_batched(st, lc, n, o.nrhs, b.X + w * bstride, b.norms + ncols + w * o.nrhs);
-    }
-    cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * (2 * ncols + nw), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(b.X, b.B, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
   }
+  if (o.precision == MH_PREC_MIXED)
+    cudaMemcpyAsync(b.B0, b.X, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st);
+}
+
+// Every matrix of size class k factored and solved together: one launch per kernel and
+// panel step for the class (matrices already factored leave at once), on `st`.
+void enqueue_grouped(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BatchCache& c, BatchCache::SizeClass& k,
+                     const BatchOpts& o) {
+  const BatchDesc g = grouped_desc(c, k, k.m_start, k.count);
+  int32_t* ipiv = grouped_ipiv(c, k, k.m_start);
+  int32_t* info = c.info_all + k.m_start;
+  cudaMemsetAsync(k.ozflag, 0, sizeof(int), st);
+  if (o.precision == MH_PREC_FP64 || o.precision == MH_PREC_FP64_TC) {
+    lu_factor_batched<double>(st, lc, g, c.D_all, ipiv, info, k.oz, k.oz ? k.ozflag : nullptr);
+    lu_solve_batched<double>(st, lc, g, c.D_all, ipiv, c.X_all, o.nrhs, 0, false);
+  } else {
+    // the class's solutions are contiguous: elementwise passes cover them in one launch
+    const int64_t x0 = c.h_xoffsets[(size_t)k.m_start];
+    const BodyPlan& last = c.bodies[(size_t)k.bodies.back()];
+    const int64_t xn = c.h_xoffsets[(size_t)(last.m0 + last.nw - 1)] + last.n * o.nrhs - x0;
+    convert_with_norms(st, lc, g, c.D_all, c.LU32_all, 0, c.anorm_all + k.m_start);
+    lu_factor_batched<float>(st, lc, g, c.LU32_all, ipiv, info, k.oz, k.ozflag);
+    convert_z_to_c(st, lc, c.X_all + x0, c.X32_all + x0, xn);
+    lu_solve_batched<float>(st, lc, g, c.LU32_all, ipiv, c.X32_all, o.nrhs, 0, false);
+    widen_c_to_z(st, lc, c.X32_all + x0, c.X_all + x0, xn);
+    for (int it = 0; it < o.ir_sweeps; ++it) {
+      for (int64_t bi : k.bodies) {
+        BodyPlan& b = c.bodies[(size_t)bi];
+        BatchDesc d{b.n, b.nw, b.n * b.n};
+        residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, b.n * o.nrhs, b.R, b.work, b.ozflag);
+        convert_z_to_c(st, lc, b.R, b.X32, b.n * o.nrhs * b.nw);
+      }
+      lu_solve_batched<float>(st, lc, g, c.LU32_all, ipiv, c.X32_all, o.nrhs, 0, false);
+      ir_update(st, lc, xn, c.X_all + x0, c.X32_all + x0);
+    }
+    cudaMemcpyAsync(c.hanorm_all + k.m_start, c.anorm_all + k.m_start, sizeof(double) * k.count,
+                    cudaMemcpyDeviceToHost, st);
+  }
+  cudaMemcpyAsync(c.hinfo_all + k.m_start, info, sizeof(int32_t) * k.count, cudaMemcpyDeviceToHost, st);
+}
+
+// The body's work after the solves: the refinement's residual (mixed), phi (indirect: S x),
+// forces and the copies to the host.
+void enqueue_back(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& b, const BatchOpts& o) {
+  const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs;
+  const double* om_d = b.params;
+  const double* beta_d = b.params + 2 * nw;
+  const int32_t* inf_d = (const int32_t*)(b.params + 2 * nw + o.n_beta) + o.n_rad;
+  BatchDesc d{n, nw, nn};
+  if (o.precision == MH_PREC_MIXED) {
+    // the residual of the returned x, judged on the host after the graph
+    const int64_t ncols = o.nrhs * nw;
+    residual_tc_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, b.ozflag);
+    inf_norms_batched(st, lc, n, ncols, b.R, b.norms);
+    inf_norms_batched(st, lc, n, ncols, b.X, b.norms + ncols);
+    cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, st);
+  }
+  EpilogueGeom eg{n, b.m->n_hull, b.m->C, b.m->N, b.m->A, b.dofs};
   double2* phi = b.X;
   if (!o.direct) {
-    s_times(b.X, b.B);
+    if (o.precision == MH_PREC_FP64) zgemm_nn_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work);
+    else zgemm_nn_tc_batched(st, lc, d, b.S, b.X, o.nrhs, bstride, b.B, b.work, b.ozflag);
     phi = b.B;
   }
   if (o.n_inf > 0)
     launch_forces(st, lc, eg, (int)nw, om_d, o.rho, o.g, (int)o.nrhs, phi, bstride, (int)o.n_inf, inf_d,
                   (int)o.n_beta, beta_d, b.F, b.FK);
-  cudaMemcpyAsync(b.hinfo, b.info, sizeof(int32_t) * nw, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(b.hF, b.F, sizeof(double2) * nw * std::max<int64_t>(o.n_inf, 1) * o.nrhs,
                   cudaMemcpyDeviceToHost, st);
   if (o.n_beta > 0)
@@ -170,7 +253,7 @@ void enqueue_body(mh_context* ctx, LaunchCounter lc, cudaStream_t st, BodyPlan& 
 
 // Host-side completion of one body after the graph: singular check, refinement
 // convergence (extra sweeps or the FP64 fallback on the context stream).
-int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
+int finish_body(mh_context* ctx, BatchCache& c, BodyPlan& b, const BatchOpts& o) {
   for (int64_t w = 0; w < b.nw; ++w)
     if (b.hinfo[w] != 0)
       return fail(ctx, MH_ERR_SINGULAR, "body with %lld panels, frequency %lld: zero pivot in column %d",
@@ -178,7 +261,7 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
   if (b.ozflag) {
     int flag = 0;
     MH_CUDA(ctx, cudaMemcpy(&flag, b.ozflag, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+    if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of a batch product gave up");
   }
   if (b.fb_state) {
     unsigned long long fs[3] = {0, 0, 0};
@@ -193,9 +276,9 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
   const int64_t n = b.n, nw = b.nw, nn = n * n, bstride = n * o.nrhs, ncols = o.nrhs * nw;
   const double cte = std::sqrt((double)n) * 2.220446049250313e-16;
   auto converged = [&]() {
-    for (int64_t c = 0; c < ncols; ++c) {
-      const double anrm = b.hnorms[2 * ncols + c / o.nrhs];
-      if (!(b.hnorms[c] <= cte * anrm * b.hnorms[ncols + c])) return false;
+    for (int64_t col = 0; col < ncols; ++col) {
+      const double anrm = c.hanorm_all[b.m0 + col / o.nrhs];
+      if (!(b.hnorms[col] <= cte * anrm * b.hnorms[ncols + col])) return false;
     }
     return true;
   };
@@ -203,24 +286,27 @@ int finish_body(mh_context* ctx, BodyPlan& b, const BatchOpts& o) {
   cudaStream_t st = ctx->stream;
   const LaunchCounter lc = ctx->lc();
   BatchDesc d{n, nw, nn};
+  const BatchCache::SizeClass& cls = c.classes[(size_t)b.cls];
+  const BatchDesc gb = grouped_desc(c, cls, b.m0, nw);  // this body's matrices in the grouped layout
+  int32_t* ipiv_b = grouped_ipiv(c, cls, b.m0);
   bool ok = false;
   for (int it = 0; it < 30 && !ok; ++it) {
     convert_z_to_c(st, lc, b.R, b.X32, bstride * nw);
-    lu_solve_batched<float>(st, lc, d, b.LU32, b.ipiv, b.X32, o.nrhs, bstride, false);
+    lu_solve_batched<float>(st, lc, gb, c.LU32_all, ipiv_b, c.X32_all, o.nrhs, 0, false);
     ir_update(st, lc, bstride * nw, b.X, b.X32);
     residual_batched(st, lc, d, b.D, b.X, b.B0, o.nrhs, bstride, b.R, b.work, false);
-    for (int64_t w = 0; w < nw; ++w) {
-      inf_norms_batched(st, lc, n, o.nrhs, b.R + w * bstride, b.norms + w * o.nrhs);
-      inf_norms_batched(st, lc, n, o.nrhs, b.X + w * bstride, b.norms + ncols + w * o.nrhs);
-    }
-    MH_CUDA(ctx, cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * (2 * ncols + nw), cudaMemcpyDeviceToHost, st));
+    inf_norms_batched(st, lc, n, ncols, b.R, b.norms);
+    inf_norms_batched(st, lc, n, ncols, b.X, b.norms + ncols);
+    MH_CUDA(ctx, cudaMemcpyAsync(b.hnorms, b.norms, sizeof(double) * 2 * ncols, cudaMemcpyDeviceToHost, st));
     MH_TRY(sync(ctx, "batch refinement"));
     ok = converged();
   }
   if (!ok) {
+    // FP64 factors of this body's matrices (a uniform batch of its own, pivots at stride n
+    // inside its slice of the grouped pivot array)
     MH_CUDA(ctx, cudaMemcpyAsync(b.X, b.B0, sizeof(double2) * bstride * nw, cudaMemcpyDeviceToDevice, st));
-    lu_factor_batched<double>(st, lc, d, b.D, b.ipiv, b.info);
-    lu_solve_batched<double>(st, lc, d, b.D, b.ipiv, b.X, o.nrhs, bstride, false);
+    lu_factor_batched<double>(st, lc, d, b.D, ipiv_b, b.info);
+    lu_solve_batched<double>(st, lc, d, b.D, ipiv_b, b.X, o.nrhs, bstride, false);
   }
   // forces of the corrected solution
   const double* om_d = b.params;
@@ -326,16 +412,63 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       const double n = (double)p.n;
       p.cost = (double)p.nw * (precision == MH_PREC_FP64 ? n * n * n : n * n * n / 20.0 + 60.0 * n * n);
     }
-    // longest processing time first onto the least-loaded stream
+    // size classes: bodies by decreasing order, a new class whenever the order falls below
+    // half the class's largest; matrices numbered class by class, body by body
     std::vector<int64_t> order(n_bodies);
     for (int64_t b = 0; b < n_bodies; ++b) order[b] = b;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return bc->bodies[a].cost > bc->bodies[c].cost; });
-    std::vector<double> load(S, 0.0);
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t c) {
+      return bc->bodies[a].n != bc->bodies[c].n ? bc->bodies[a].n > bc->bodies[c].n : a < c;
+    });
+    int64_t m = 0;
     for (int64_t b : order) {
-      int best = 0;
-      for (int q = 1; q < S; ++q) if (load[q] < load[best]) best = q;
-      bc->bodies[b].stream = best;
-      load[best] += bc->bodies[b].cost;
+      BodyPlan& p = bc->bodies[b];
+      if (bc->classes.empty() || 2 * p.n < bc->classes.back().n_max) {
+        BatchCache::SizeClass k;
+        k.m_start = m;
+        k.n_max = p.n;
+        bc->classes.push_back(k);
+      }
+      BatchCache::SizeClass& k = bc->classes.back();
+      k.bodies.push_back(b);
+      k.count += p.nw;
+      p.cls = (int)bc->classes.size() - 1;
+      p.m0 = m;
+      m += p.nw;
+    }
+    bc->M = m;
+    bc->n_max = bc->classes.front().n_max;
+    // classes onto streams, the costliest first onto the least-loaded stream
+    {
+      std::vector<double> load(S, 0.0);
+      std::vector<double> cost(bc->classes.size(), 0.0);
+      for (auto& p : bc->bodies) cost[(size_t)p.cls] += p.cost;
+      std::vector<size_t> co(bc->classes.size());
+      for (size_t q = 0; q < co.size(); ++q) co[q] = q;
+      std::sort(co.begin(), co.end(), [&](size_t a, size_t c) { return cost[a] > cost[c]; });
+      for (size_t q : co) {
+        int best = 0;
+        for (int t = 1; t < S; ++t) if (load[t] < load[best]) best = t;
+        bc->classes[q].stream = best;
+        load[best] += cost[q];
+      }
+      for (auto& p : bc->bodies) p.stream = bc->classes[(size_t)p.cls].stream;
+    }
+    bc->h_orders.resize((size_t)bc->M);
+    bc->h_offsets.resize((size_t)bc->M);
+    bc->h_xoffsets.resize((size_t)bc->M);
+    {
+      int64_t doffs = 0, xoffs = 0;
+      for (auto& k : bc->classes)
+        for (int64_t b : k.bodies) {
+          BodyPlan& p = bc->bodies[b];
+          for (int64_t w = 0; w < p.nw; ++w) {
+            bc->h_orders[(size_t)(p.m0 + w)] = p.n;
+            bc->h_offsets[(size_t)(p.m0 + w)] = doffs;
+            bc->h_xoffsets[(size_t)(p.m0 + w)] = xoffs;
+            doffs += p.n * p.n;
+            xoffs += p.n * o.nrhs;
+          }
+        }
     }
     size_t dev_bytes = 0, host_bytes = 0;
     std::vector<size_t> doff(n_bodies), hoff(n_bodies);
@@ -345,6 +478,10 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       hoff[b] = host_bytes;
       host_bytes += pinned_body(bc->bodies[b], o, nullptr);
     }
+    const size_t gdev = dev_bytes;
+    dev_bytes += layout_grouped(*bc, o, nullptr);
+    const size_t ghost = host_bytes;
+    host_bytes += pinned_grouped(*bc, o, nullptr);
     size_t free_b = 0, total_b = 0;
     MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
     if (dev_bytes > (size_t)(0.8 * (double)free_b)) {
@@ -361,6 +498,23 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       layout_body(bc->bodies[b], o, (char*)bc->arena + doff[b]);
       pinned_body(bc->bodies[b], o, bc->pinned + hoff[b]);
     }
+    layout_grouped(*bc, o, (char*)bc->arena + gdev);
+    pinned_grouped(*bc, o, bc->pinned + ghost);
+    for (auto& p : bc->bodies) {
+      const BatchCache::SizeClass& k = bc->classes[(size_t)p.cls];
+      p.D = bc->D_all + bc->h_offsets[(size_t)p.m0];
+      p.X = bc->X_all + bc->h_xoffsets[(size_t)p.m0];
+      if (bc->LU32_all) {
+        p.LU32 = bc->LU32_all + bc->h_offsets[(size_t)p.m0];
+        p.X32 = bc->X32_all + bc->h_xoffsets[(size_t)p.m0];
+      }
+      p.ipiv = grouped_ipiv(*bc, k, p.m0);
+      p.info = bc->info_all + p.m0;
+      p.hinfo = bc->hinfo_all + p.m0;
+    }
+    MH_CUDA(ctx, cudaMemcpy(bc->orders, bc->h_orders.data(), sizeof(int64_t) * bc->M, cudaMemcpyHostToDevice));
+    MH_CUDA(ctx, cudaMemcpy(bc->offsets, bc->h_offsets.data(), sizeof(int64_t) * bc->M, cudaMemcpyHostToDevice));
+    MH_CUDA(ctx, cudaMemcpy(bc->xoffsets, bc->h_xoffsets.data(), sizeof(int64_t) * bc->M, cudaMemcpyHostToDevice));
     while ((int)ctx->side.size() < S - 1) {
       cudaStream_t st;
       MH_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -370,7 +524,8 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
     if (profiling) {
       ctx->batch = bc;
     } else {
-      // capture the schedule
+      // capture the schedule: per size class on its stream, the bodies' assembly, the class's
+      // grouped factorization and solves, the bodies' forces
       cudaStream_t s0 = ctx->stream;
       std::vector<cudaEvent_t> ev(S);
       for (auto& e : ev) MH_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -378,9 +533,11 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
       MH_CUDA(ctx, cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
       cudaEventRecord(ev[0], s0);
       for (int q = 1; q < S; ++q) cudaStreamWaitEvent(ctx->side[q - 1], ev[0], 0);
-      for (int64_t b : order) {
-        BodyPlan& p = bc->bodies[b];
-        enqueue_body(ctx, cap, p.stream == 0 ? s0 : ctx->side[p.stream - 1], p, o);
+      for (auto& k : bc->classes) {
+        cudaStream_t st = k.stream == 0 ? s0 : ctx->side[k.stream - 1];
+        for (int64_t b : k.bodies) enqueue_front(ctx, cap, st, bc->bodies[b], o);
+        enqueue_grouped(ctx, cap, st, *bc, k, o);
+        for (int64_t b : k.bodies) enqueue_back(ctx, cap, st, bc->bodies[b], o);
       }
       for (int q = 1; q < S; ++q) {
         cudaEventRecord(ev[q], ctx->side[q - 1]);
@@ -427,10 +584,19 @@ int mh_batch_hydrodynamic_coefficients(mh_context* ctx, int64_t n_bodies, mh_mes
     MH_CUDA(ctx, cudaGraphLaunch(bc->exec, ctx->stream));
     ctx->launches += bc->graph_kernels;
   } else {
-    for (int64_t b : bc->order) enqueue_body(ctx, ctx->lc(), ctx->stream, bc->bodies[b], o);
+    for (auto& k : bc->classes) {
+      for (int64_t b : k.bodies) enqueue_front(ctx, ctx->lc(), ctx->stream, bc->bodies[b], o);
+      enqueue_grouped(ctx, ctx->lc(), ctx->stream, *bc, k, o);
+      for (int64_t b : k.bodies) enqueue_back(ctx, ctx->lc(), ctx->stream, bc->bodies[b], o);
+    }
   }
   MH_TRY(sync(ctx, "batch graph"));
-  for (auto& p : bc->bodies) MH_TRY(finish_body(ctx, p, o));
+  for (auto& k : bc->classes) {
+    int flag = 0;
+    MH_CUDA(ctx, cudaMemcpy(&flag, k.ozflag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+  }
+  for (auto& p : bc->bodies) MH_TRY(finish_body(ctx, *bc, p, o));
   // pack per body (n_U = 1), bodies concatenated along the frequency axis
   std::vector<double> hA((size_t)(n_inf * n_rad * total_w)), hB(hA.size());
   std::vector<double2> hd((size_t)(n_inf * total_w * n_beta)), hk(hd.size()), he(hd.size());

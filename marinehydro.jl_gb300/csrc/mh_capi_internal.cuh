@@ -32,6 +32,8 @@ struct DevBuf {
 struct BodyPlan {
   mh_mesh* m = nullptr;
   int64_t n = 0, nw = 0, w_off = 0, out_off = 0;
+  int64_t m0 = 0;                 // index of the body's first matrix in the grouped factorization
+  int cls = 0;                    // its size class
   int stream = 0;
   double cost = 0.0;
   double *SR = nullptr, *DR = nullptr, *params = nullptr, *dofs = nullptr, *norms = nullptr;
@@ -57,6 +59,25 @@ struct BatchCache {
   std::vector<BodyPlan> bodies;
   void* arena = nullptr;
   char* pinned = nullptr;
+  // The grouped factorization: every body's matrices (M in all, stored body after body; the
+  // bodies' D, X, LU32, X32 point into these arrays) factored and solved together per size
+  // class (bodies whose orders lie within a factor of two), one launch per kernel and panel
+  // step for the whole class.
+  struct SizeClass {
+    int64_t m_start = 0, count = 0, n_max = 0;
+    int stream = 0;
+    std::vector<int64_t> bodies;
+    void* oz = nullptr;      // tensor-core update workspace of the class
+    int* ozflag = nullptr;
+  };
+  std::vector<SizeClass> classes;
+  int64_t M = 0, n_max = 0;
+  double2 *D_all = nullptr, *X_all = nullptr;
+  float2 *LU32_all = nullptr, *X32_all = nullptr;
+  int32_t *ipiv_all = nullptr, *info_all = nullptr, *hinfo_all = nullptr;
+  int64_t *orders = nullptr, *offsets = nullptr, *xoffsets = nullptr;  // device
+  std::vector<int64_t> h_orders, h_offsets, h_xoffsets;
+  double *anorm_all = nullptr, *hanorm_all = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t graph_kernels = 0;
   std::vector<int64_t> order;  // bodies, longest first

@@ -155,9 +155,21 @@ void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const dou
 
 // dense linear algebra (mh_lu.cu)
 struct BatchDesc {
-  int64_t n;        // order
+  int64_t n;        // order (a grouped batch: the largest order)
   int64_t batch;    // number of matrices
-  int64_t stride;   // complex elements between matrices
+  int64_t stride;   // complex elements between matrices (uniform batches)
+  // A grouped batch holds matrices of different orders (the many-body batch factors every
+  // body's matrices in one launch per panel step): device arrays of each matrix's order,
+  // the element offset of the matrix and of its block of right-hand sides.  Null for a
+  // uniform batch.  Pivot indices keep the stride n per matrix either way.
+  const int64_t* orders = nullptr;
+  const int64_t* offsets = nullptr;
+  const int64_t* xoffsets = nullptr;
+  __device__ __forceinline__ int64_t order(int64_t b) const { return orders ? orders[b] : n; }
+  __device__ __forceinline__ int64_t offset(int64_t b) const { return offsets ? offsets[b] : b * stride; }
+  __device__ __forceinline__ int64_t xoffset(int64_t b, int64_t xstride) const {
+    return xoffsets ? xoffsets[b] : b * xstride;
+  }
 };
 template <typename T>
 int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typename cplx_t<T>::type* A,

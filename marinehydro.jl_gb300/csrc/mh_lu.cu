@@ -86,9 +86,10 @@ __global__ void __launch_bounds__(512) panel_kernel(BatchDesc d, typename cplx_t
   __shared__ int wi[16];
   __shared__ int s_piv;
   __shared__ T s_best;
-  const int64_t n = d.n;
-  C* A = Aall + blockIdx.x * d.stride;
-  int32_t* ipiv = ipiv_all + blockIdx.x * n;
+  const int64_t n = d.order(blockIdx.x);
+  if (k >= n) return;  // a grouped batch: this matrix is factored
+  C* A = Aall + d.offset(blockIdx.x);
+  int32_t* ipiv = ipiv_all + blockIdx.x * d.n;
   const int64_t kend = (k + kNB < n) ? k + kNB : n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   for (int64_t j = k; j < kend; ++j) {
@@ -207,7 +208,7 @@ template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
                                                                      int32_t* __restrict__ ipiv_all,
                                                                      int32_t* __restrict__ info_all, int64_t k,
-                                                                     int chunk) {
+                                                                     int chunk_cap) {
   using C = typename cplx_t<T>::type;
   using K = typename PivotKey<T>::type;
   namespace cg = cooperative_groups;
@@ -225,10 +226,13 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
   __shared__ C s_inv;
   const int P = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t n = d.n, bmat = blockIdx.y;
-  C* A = Aall + bmat * d.stride;
+  const int64_t bmat = blockIdx.y, n = d.order(bmat);
+  if (k >= n) return;  // a grouped batch: this matrix is factored (the whole cluster leaves)
+  C* A = Aall + d.offset(bmat);
   const int64_t m = n - k;
   const int kb = (int)(m < kNB ? m : kNB);
+  // rows per CTA for this matrix: at most the launch's capacity, at least the diagonal block
+  const int chunk = (int)max((int64_t)kb, min((int64_t)chunk_cap, (m + P - 1) / P));
   const int r0 = rank * chunk;  // first panel row of this CTA
   const int rows = (int)((m - r0) < chunk ? ((m - r0) > 0 ? (m - r0) : 0) : chunk);
 
@@ -278,7 +282,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
       if (lane == 0) {
         s_piv = p;
         if (rank == 0) {
-          ipiv_all[bmat * n + k + j] = (int32_t)(k + p);
+          ipiv_all[bmat * d.n + k + j] = (int32_t)(k + p);
           if (zero && info_all[bmat] == 0) info_all[bmat] = (int32_t)(k + j + 1);
         }
       }
@@ -357,12 +361,14 @@ __global__ void __launch_bounds__(256) laswp_kernel(BatchDesc d, typename cplx_t
                                                    const int32_t* __restrict__ ipiv_all, int64_t k, int kb) {
   using C = typename cplx_t<T>::type;
   __shared__ int s_slot[32], s_content[64], s_dst[64], s_src[64];
-  const int64_t n = d.n, bmat = blockIdx.y;
-  if (threadIdx.x < 32) panel_permutation(ipiv_all + bmat * n, k, kb, s_slot, s_content, s_dst, s_src);
+  const int64_t bmat = blockIdx.y, n = d.order(bmat);
+  if (k >= n) return;  // a grouped batch: this matrix is factored
+  kb = (int)((k + kNB < n) ? kNB : n - k);
+  if (threadIdx.x < 32) panel_permutation(ipiv_all + bmat * d.n, k, kb, s_slot, s_content, s_dst, s_src);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int d0 = s_dst[lane], s0 = s_src[lane], d1 = s_dst[lane + 32], s1 = s_src[lane + 32];
-  C* A = Aall + bmat * d.stride;
+  C* A = Aall + d.offset(bmat);
   const int64_t nout = n - kb;
   const int64_t q0 = blockIdx.x * (int64_t)kSwpCols;
   const int64_t q1 = (q0 + kSwpCols < nout) ? q0 + kSwpCols : nout;
@@ -383,8 +389,9 @@ __global__ void __launch_bounds__(128) trsm_kernel(BatchDesc d, typename cplx_t<
                                                    int64_t k) {
   using C = typename cplx_t<T>::type;
   __shared__ C sL[kNB][kNB + 1];
-  const int64_t n = d.n;
-  C* A = Aall + blockIdx.y * d.stride;
+  const int64_t n = d.order(blockIdx.y);
+  if (k + kNB >= n) return;  // nothing right of this matrix's panel (grouped batches)
+  C* A = Aall + d.offset(blockIdx.y);
   const int kb = (int)((k + kNB < n) ? kNB : n - k);
   for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
     int r = idx % kb, q = idx / kb;
@@ -422,12 +429,14 @@ __global__ void __launch_bounds__(256) gemm_kernel(BatchDesc d, typename cplx_t<
   extern __shared__ unsigned char gemm_smem[];
   C (*sA)[TM + 1] = reinterpret_cast<C (*)[TM + 1]>(gemm_smem);
   C (*sB)[TM + 1] = reinterpret_cast<C (*)[TM + 1]>(gemm_smem + sizeof(C) * KC * (TM + 1));
-  const int64_t n = d.n;
-  C* A = Aall + blockIdx.z * d.stride;
+  const int64_t n = d.order(blockIdx.z);
+  if (k + kNB >= n) return;  // no trailing block for this matrix (grouped batches)
+  C* A = Aall + d.offset(blockIdx.z);
   const int kb = (int)((k + kNB < n) ? kNB : n - k);
   const int64_t base = k + kb;
   const int64_t row0 = base + blockIdx.x * (int64_t)TM;
   const int64_t col0 = base + blockIdx.y * (int64_t)TM;
+  if (row0 >= n || col0 >= n) return;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   C acc[RM][RM];
 #pragma unroll
@@ -498,12 +507,14 @@ __global__ void __launch_bounds__(256) gemm3m_kernel(BatchDesc d, double2* __res
   double (*sBr)[kG3TM + 1] = sAs + kG3KC;
   double (*sBi)[kG3TM + 1] = sBr + kG3KC;
   double (*sBs)[kG3TM + 1] = sBi + kG3KC;
-  const int64_t n = d.n;
-  double2* A = Aall + blockIdx.z * d.stride;
+  const int64_t n = d.order(blockIdx.z);
+  if (k + kNB >= n) return;  // no trailing block for this matrix (grouped batches)
+  double2* A = Aall + d.offset(blockIdx.z);
   const int kb = (int)((k + kNB < n) ? kNB : n - k);
   const int64_t base = k + kb;
   const int64_t row0 = base + blockIdx.x * (int64_t)kG3TM;
   const int64_t col0 = base + blockIdx.y * (int64_t)kG3TM;
+  if (row0 >= n || col0 >= n) return;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   double p1[kG3RM][kG3RM], p2[kG3RM][kG3RM], p3[kG3RM][kG3RM];
 #pragma unroll
@@ -659,10 +670,10 @@ __global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename 
   extern __shared__ unsigned char smem_raw[];
   C* blk = reinterpret_cast<C*>(smem_raw);
   C* xs = blk + 32 * 33;
-  const int64_t n = d.n;
-  const C* LU = LUall + blockIdx.y * d.stride;
-  const int32_t* ipiv = ipiv_all + blockIdx.y * n;
-  C* X = Xall + blockIdx.y * xstride;
+  const int64_t n = d.order(blockIdx.y);
+  const C* LU = LUall + d.offset(blockIdx.y);
+  const int32_t* ipiv = ipiv_all + blockIdx.y * d.n;
+  C* X = Xall + d.xoffset(blockIdx.y, xstride);
   const int64_t r0 = blockIdx.x * (int64_t)group;
   const int g = (int)((r0 + group <= nrhs) ? group : nrhs - r0);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -867,11 +878,11 @@ __global__ void __launch_bounds__(512) solve_cluster_kernel(BatchDesc d, const t
   __shared__ C pub[2][32 * kSG];
   __shared__ C xb[2][kXbStride * kSG];
   const int P = (int)cl.num_blocks(), rank = (int)cl.block_rank();
-  const int64_t n = d.n;
+  const int64_t n = d.order(blockIdx.z);
   const int nblk = (int)((n + 31) / 32);
-  const C* LU = LUall + blockIdx.z * d.stride;
-  const int32_t* ipiv = ipiv_all + blockIdx.z * n;
-  C* X = Xall + blockIdx.z * xstride;
+  const C* LU = LUall + d.offset(blockIdx.z);
+  const int32_t* ipiv = ipiv_all + blockIdx.z * d.n;
+  C* X = Xall + d.xoffset(blockIdx.z, xstride);
   const int64_t r0 = blockIdx.y * (int64_t)group;
   const int g = (int)((r0 + group <= nrhs) ? group : nrhs - r0);
   const int tid = threadIdx.x;
@@ -1032,7 +1043,8 @@ __global__ void col_inf_norm_kernel(int64_t n, const double2* __restrict__ X, do
 }
 
 
-// the FP32 copy of matrix b (column stride n, matrix stride stride32) and, in the same pass
+// the FP32 copy of matrix b (column stride n, matrix stride stride32; a grouped batch: at the
+// matrix's own element offset) and, in the same pass
 // over A, out[b] = max_i sum_j |re|+|im| (|.|_inf, order independent via atomicMax on the bits
 // of a non-negative double; out zeroed first).  128 rows x 8 column slices per CTA, the
 // slices' partial row sums added in a fixed order.
@@ -1042,9 +1054,10 @@ __global__ void __launch_bounds__(1024) convert_norm_kernel(BatchDesc d, const d
   __shared__ double part[8][128];
   const int64_t i = blockIdx.x * (int64_t)128 + threadIdx.x;
   const int64_t b = blockIdx.y;
-  const int64_t n = d.n;
-  const double2* Ab = A + b * d.stride;
-  float2* Cb = A32 + b * stride32;
+  // a grouped batch: the FP32 copies sit at the same element offsets as the matrices
+  const int64_t n = d.order(b);
+  const double2* Ab = A + d.offset(b);
+  float2* Cb = A32 + (d.offsets ? d.offsets[b] : b * stride32);
   const int64_t j0 = (n * threadIdx.y) / 8, j1 = (n * (threadIdx.y + 1)) / 8;
   double s = 0.0;
   if (i < n) {

@@ -46,6 +46,7 @@ namespace mh {
 namespace {
 
 constexpr int kOzDigits = 8;
+constexpr int kNB_oz = 32;          // the LU's panel width
 constexpr int kOzK = 32;            // panel width (the LU's kNB)
 constexpr int kOzRows = 128;        // output rows per CTA (MMA M)
 constexpr int kOzCols = 32;         // output columns per CTA (MMA N)
@@ -68,9 +69,14 @@ __global__ void __launch_bounds__(256) ozaki_split_rows_kernel(BatchDesc d, cons
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (r >= nrt * kOzRows) return;  // whole groups of four leave together
-  const int64_t n = d.n;
-  const double2* Ab = A + b * d.stride;
-  const bool live = r < rest;
+  // a grouped batch: this matrix's order, panel width and trailing size (the launch's `rest`
+  // stays the stride of the exponent arrays)
+  const int64_t n = d.order(b);
+  if (k + kNB_oz >= n) return;
+  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
+  const int64_t rest_b = n - k - kb;
+  const double2* Ab = A + d.offset(b);
+  const bool live = r < rest_b;
   double2 v[8];
   int emax = 0;
 #pragma unroll
@@ -104,9 +110,12 @@ __global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, cons
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
   if (c >= nct * kOzCols) return;
-  const int64_t n = d.n;
-  const double2* Ab = A + b * d.stride;
-  const bool live = c < rest;
+  const int64_t n = d.order(b);
+  if (k + kNB_oz >= n) return;
+  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
+  const int64_t rest_b = n - k - kb;
+  const double2* Ab = A + d.offset(b);
+  const bool live = c < rest_b;
   double2 v[8];
   int emax = 0;
 #pragma unroll
@@ -164,8 +173,15 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const int tid = threadIdx.x, warp = tid >> 5;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
   const int64_t ct0 = blockIdx.y * (int64_t)group;
-  const int ntile = (int)((nct - ct0) < group ? (nct - ct0) : group);
-  const int64_t n = d.n;
+  // a grouped batch: this matrix's panel width and trailing size; CTAs past its trailing
+  // block leave before any barrier or tensor-memory allocation
+  const int64_t n = d.order(b);
+  if (k + kNB_oz >= n) return;
+  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
+  const int64_t rest_b = n - k - kb;
+  if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_b) return;
+  const int64_t nct_b = (rest_b + kOzCols - 1) / kOzCols;
+  const int ntile = (int)((nct_b - ct0) < group ? (nct_b - ct0) : group);
   unsigned char* As = osm;
   unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
   const unsigned char* srcA = digA + (b * nrt + rt) * (int64_t)kOzABytes;
@@ -192,10 +208,10 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
   const int lrow = tid & (kOzRows - 1), half = tid >> 7;  // TMEM lane (output row) and column half
   const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
-  const bool row_live = r < rest;
+  const bool row_live = r < rest_b;
   const int er = row_live ? rowexp[b * rest + r] : 0;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  double2* Ab = A + b * d.stride;
+  double2* Ab = A + d.offset(b);
   double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
   bool failed = false;
   int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
@@ -236,7 +252,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
     for (int q = 0; q < kOzCols / 2; ++q) {
       const int64_t c = cbase + q;
-      const bool live = row_live && c < rest;
+      const bool live = row_live && c < rest_b;
       cv[q] = live ? crow[c * n] : make_double2(0.0, 0.0);
       ce[q] = live ? colexp[b * rest + c] : 0;
     }
@@ -288,7 +304,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
     if (row_live) {
 #pragma unroll
       for (int q = 0; q < kOzCols / 2; ++q)
-        if (cbase + q < rest) crow[(cbase + q) * n] = cv[q];
+        if (cbase + q < rest_b) crow[(cbase + q) * n] = cv[q];
     }
     // every TMEM read of this tile is done before the next tile's products overwrite it
     tc::fence_before_sync();
