@@ -78,9 +78,9 @@ __device__ __forceinline__ void store_terms8(unsigned char* tile, int r, int k8,
 
 // L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32); four
 // threads per row, eight columns each
-__global__ void bx3_split_rows_kernel(BatchDesc d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
+__device__ __forceinline__ void bx3_split_rows(int64_t bx, const BatchDesc& d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
                                       int64_t ntile, unsigned char* __restrict__ tiles) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = bx * (int64_t)blockDim.x + threadIdx.x;
   const int64_t r = t >> 2;  // padded row of the trailing block
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
@@ -103,9 +103,9 @@ __global__ void bx3_split_rows_kernel(BatchDesc d, const float2* __restrict__ A,
 
 // U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1; four threads per
 // column, eight rows each
-__global__ void bx3_split_cols_kernel(BatchDesc d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
+__device__ __forceinline__ void bx3_split_cols(int64_t bx, const BatchDesc& d, const float2* __restrict__ A, int64_t k, int kb, int64_t rest,
                                       int64_t ntile, unsigned char* __restrict__ tiles) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = bx * (int64_t)blockDim.x + threadIdx.x;
   const int64_t c = t >> 2;  // padded column of the trailing block
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
@@ -122,6 +122,14 @@ __global__ void bx3_split_cols_kernel(BatchDesc d, const float2* __restrict__ A,
     v[q] = (live && kk < kb) ? Ab[(k + kk) + (k + kb + c) * n] : make_float2(0.f, 0.f);
   }
   store_terms8(tiles + (b * ntile + c / kBxTile) * (int64_t)kBxTileBytes, (int)(c % kBxTile), 8 * kq, v);
+}
+
+// Both splits of a panel step in one launch: CTAs [0, half) cut L21, the rest U12.
+__global__ void __launch_bounds__(256) bx3_split_kernel(BatchDesc d, const float2* __restrict__ A, int64_t k, int kb,
+                                                        int64_t rest, int64_t ntile, int64_t half,
+                                                        unsigned char* __restrict__ tA, unsigned char* __restrict__ tB) {
+  if ((int64_t)blockIdx.x < half) bx3_split_rows(blockIdx.x, d, A, k, kb, rest, ntile, tA);
+  else bx3_split_cols(blockIdx.x - half, d, A, k, kb, rest, ntile, tB);
 }
 
 __global__ void __launch_bounds__(kBxThreads) bx3_gemm_kernel(BatchDesc d, float2* __restrict__ A, int64_t k, int kb,
@@ -307,9 +315,8 @@ void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, 
   const int64_t nt = (rest + kBxTile - 1) / kBxTile, nt_max = (d.n + kBxTile - 1) / kBxTile;
   unsigned char* tA = static_cast<unsigned char*>(ws);
   unsigned char* tB = tA + d.batch * nt_max * (int64_t)kBxTileBytes;
-  dim3 gs((unsigned)(nt * 2), (unsigned)d.batch);  // 4 threads per row / column, 256 per CTA
-  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_rows_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, tA));
-  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_cols_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, tB));
+  dim3 gs((unsigned)(nt * 4), (unsigned)d.batch);  // 4 threads per row / column, 256 per CTA; rows then columns
+  MH_LAUNCH(lc, st, "lu_bx3_split", bx3_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nt, nt * 2, tA, tB));
   const size_t smem = 3 * (size_t)kBxTileBytes;
   cudaFuncSetAttribute(bx3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int group = lc.tile(d.n).bx_group;

@@ -17,9 +17,9 @@
 // of the FP64 update.
 //
 // Kernels per panel step (all batched over the matrices of the sweep):
-//   ozaki_split_rows: L21 -> digit tiles A[row tile][digit][re/im] (128 x 32 BF16 each, in the
+//   ozaki_split (one launch, both halves) -- rows: L21 -> digit tiles A[row tile][digit][re/im] (128 x 32 BF16 each, in the
 //     canonical no-swizzle K-major layout) and the row exponents;
-//   ozaki_split_cols: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
+//                    columns: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
 //     column exponents; the eight digit tiles of one part are consecutive, so digits
 //     q .. 7 form one (32 (8 - q)) x 32 operand;
 //   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 16 A digit
@@ -60,11 +60,11 @@ constexpr uint32_t kOzWaitPolls = 1u << 26;
 // L21 of matrix b at panel step k: rows k+kb .. n-1, columns k .. k+kb-1 (kb <= 32).  Four
 // threads per row, eight columns each: the row's largest exponent by shuffles, then its
 // digits with integer arithmetic (mh_digits.cuh), one 16-byte store per digit plane.
-__global__ void __launch_bounds__(256) ozaki_split_rows_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k,
+__device__ __forceinline__ void ozaki_split_rows(int64_t bx, const BatchDesc& d, const double2* __restrict__ A, int64_t k,
                                                                int kb, int64_t rest, int64_t nrt,
                                                                unsigned char* __restrict__ digA,
                                                                int* __restrict__ rowexp) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = bx * (int64_t)blockDim.x + threadIdx.x;
   const int64_t r = t >> 2;  // padded row of the trailing block
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
@@ -101,11 +101,11 @@ __global__ void __launch_bounds__(256) ozaki_split_rows_kernel(BatchDesc d, cons
 
 // U12 of matrix b at panel step k: rows k .. k+kb-1, columns k+kb .. n-1; four threads per
 // column, eight rows each
-__global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k,
+__device__ __forceinline__ void ozaki_split_cols(int64_t bx, const BatchDesc& d, const double2* __restrict__ A, int64_t k,
                                                                int kb, int64_t rest, int64_t nct,
                                                                unsigned char* __restrict__ digB,
                                                                int* __restrict__ colexp) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t t = bx * (int64_t)blockDim.x + threadIdx.x;
   const int64_t c = t >> 2;  // padded column of the trailing block
   const int kq = (int)(t & 3);
   const int64_t b = blockIdx.y;
@@ -136,6 +136,16 @@ __global__ void __launch_bounds__(256) ozaki_split_cols_kernel(BatchDesc d, cons
     *reinterpret_cast<uint4*>(tiles + p * kOzBTile + off) = make_uint4(pk[0][p][0], pk[0][p][1], pk[0][p][2], pk[0][p][3]);
     *reinterpret_cast<uint4*>(tiles + (kOzDigits + p) * kOzBTile + off) = make_uint4(pk[1][p][0], pk[1][p][1], pk[1][p][2], pk[1][p][3]);
   }
+}
+
+// Both splits of a panel step in one launch: CTAs [0, row_ctas) cut L21, the rest U12.
+__global__ void __launch_bounds__(256) ozaki_split_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k, int kb,
+                                                          int64_t rest, int64_t nrt, int64_t nct, int64_t row_ctas,
+                                                          unsigned char* __restrict__ digA,
+                                                          unsigned char* __restrict__ digB, int* __restrict__ rowexp,
+                                                          int* __restrict__ colexp) {
+  if ((int64_t)blockIdx.x < row_ctas) ozaki_split_rows(blockIdx.x, d, A, k, kb, rest, nrt, digA, rowexp);
+  else ozaki_split_cols(blockIdx.x - row_ctas, d, A, k, kb, rest, nct, digB, colexp);
 }
 
 // v 2^s as a double, exactly, for |v| < 2^53, built from the integer's bits (leading-zero
@@ -343,10 +353,10 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
   int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
   int* colexp = rowexp + d.batch * d.n;
-  dim3 gr((unsigned)((nrt * kOzRows * 4 + 255) / 256), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_rows_kernel<<<gr, 256, 0, st>>>(d, A, k, kb, rest, nrt, digA, rowexp));
-  dim3 gc((unsigned)((nct * kOzCols * 4 + 255) / 256), (unsigned)d.batch);
-  MH_LAUNCH(lc, st, "lu_ozaki_split", ozaki_split_cols_kernel<<<gc, 256, 0, st>>>(d, A, k, kb, rest, nct, digB, colexp));
+  const int64_t row_ctas = (nrt * kOzRows * 4 + 255) / 256, col_ctas = (nct * kOzCols * 4 + 255) / 256;
+  dim3 gs((unsigned)(row_ctas + col_ctas), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_ozaki_split",
+            ozaki_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nrt, nct, row_ctas, digA, digB, rowexp, colexp));
   const size_t smem = kOzABytes + 2 * kOzBBytes;
   cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int group = lc.tile(d.n).oz_group;
