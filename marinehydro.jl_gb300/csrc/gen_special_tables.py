@@ -19,6 +19,13 @@ mpmath at 40 digits):
   inverting the two relations.  Worst absolute error of P, Q/s: 3e-17.
 * FP32 tables: the same construction at degree 6 (half-unit intervals) and 6 (Hankel), for
   errors below FP32 rounding.
+* Fixed-point tables (namespace besq) of the same FP64 polynomials for the integer-pipe
+  evaluator (mh_fixpoint.cuh): 64-bit integers c 2^61 (|values| < 4).  Below x = 8 the
+  variable is z = 2 t in [-1/2, 1/2) (coefficient i divided by 2^i), above it z = (u - 1/2) / 2
+  in [-1/4, 1/4] (coefficient i times 2^i), so that z 2^64 is a 64-bit integer and one
+  Horner step is v <- c + floor(v z) (a signed 64 x 64 -> high 64 multiply).  The coefficients
+  are rounded from the 40-digit values; the integer evaluation, emulated here bit for bit,
+  is checked against mpmath below.
 
 Wu fits: the polynomials A-D and dA-dC of Liang, Wu & Noblesse (wu.jl:131-197, 235-329) in
 rho in [0, 1] have monomial coefficients up to 2e5 of alternating sign, so evaluated in FP32
@@ -94,6 +101,76 @@ def horner(co, t):
     return v
 
 
+QF = 61  # fraction bits of the fixed-point Bessel coefficients and values
+
+
+def q_int(x, frac=QF):
+    return int(mp.nint(mp.mpf(x) * mp.mpf(2) ** frac))
+
+
+def fx_horner(cq, z):
+    """v <- c + floor(v z / 2^64) from the highest degree down (the device's Horner step)."""
+    v = cq[-1]
+    for c in reversed(cq[:-1]):
+        v = c + ((v * z) >> 64)
+    return v
+
+
+def fx_low(rows, x):
+    """The device's fixed-point evaluation below x = 8 for a double x: X = floor(x 2^60),
+    interval q = X >> 59, z = (X - q 2^59 - 2^58) 2^5."""
+    X = int(mp.floor(mp.mpf(x) * 2 ** 60))
+    q = min(X >> 59, 15)
+    z = (X - (q << 59) - (1 << 58)) << 5
+    return rows, q, z
+
+
+def fx_bessel_tables(tabs_exact):
+    """Fixed-point rows: below 8 (variable 2 t) coefficient i / 2^i, above 8 (variable
+    (u - 1/2) / 2) coefficient i * 2^i; all as integers c 2^61."""
+    out = {}
+    for key in ("J0", "J1", "Y0", "Y1"):
+        rows = tabs_exact[key]
+        n = len(rows) // (DEG_LOW + 1)
+        out[key] = [q_int(rows[r * (DEG_LOW + 1) + i] / mp.mpf(2) ** i) for r in range(n) for i in range(DEG_LOW + 1)]
+    for key in ("P0", "Q0", "P1", "Q1"):
+        out[key] = [q_int(c * mp.mpf(2) ** i) for i, c in enumerate(tabs_exact[key])]
+    for key, vals in out.items():
+        assert max(abs(v) for v in vals) < 2 ** 62, key
+    return out
+
+
+def fx_bessel_errors(fq):
+    """Worst absolute error of the integer evaluation (emulated bit for bit) against mpmath."""
+    J = {"J0": lambda x: mp.besselj(0, x), "J1": lambda x: mp.besselj(1, x),
+         "Y0": lambda x: mp.bessely(0, x), "Y1": lambda x: mp.bessely(1, x)}
+    worst_low = mp.mpf(0)
+    for key, f in J.items():
+        q0 = 6 if key[0] == "Y" else 0
+        for k in range(q0 * 32, 8 * 64):
+            x = float(mp.mpf(k) / 64 + mp.mpf(1) / 193)
+            X = int(mp.floor(mp.mpf(x) * 2 ** 60))
+            q = min(X >> 59, 15)
+            z = (X - (q << 59) - (1 << 58)) << 5
+            assert -2 ** 63 <= z < 2 ** 63
+            row = fq[key][(q - q0) * (DEG_LOW + 1):(q - q0 + 1) * (DEG_LOW + 1)]
+            worst_low = max(worst_low, abs(mp.mpf(fx_horner(row, z)) / 2 ** QF - f(x)))
+    worst_hk = mp.mpf(0)
+    for nu in (0, 1):
+        for part in (0, 1):
+            key = f"{'PQ'[part]}{nu}"
+            for k in range(0, 65):
+                u = mp.mpf(k) / 64
+                w = float(u) - 0.5
+                z = int(mp.floor(mp.mpf(w) * 2 ** 63)) if w >= 0 else -int(mp.floor(-mp.mpf(w) * 2 ** 63))
+                worst_hk = max(worst_hk, abs(mp.mpf(fx_horner(fq[key], z)) / 2 ** QF - hankel_pq(nu, mp.mpf(w) + mp.mpf(1) / 2)[part]))
+    return worst_low, worst_hk
+
+
+def fmt_int(vals):
+    return ",\n    ".join(", ".join(f"{v}LL" for v in vals[i:i + 3]) for i in range(0, len(vals), 3))
+
+
 def fmt(vals, single=False):
     f = (lambda v: f"{float(mp.mpf(v)):.9e}f") if single else (lambda v: f"{float(v):.17e}")
     return ",\n    ".join(", ".join(f(v) for v in vals[i:i + 4]) for i in range(0, len(vals), 4))
@@ -105,27 +182,32 @@ def bessel_tables(deg_low, deg_hankel, single):
     rnd = (lambda c: float(__import__("numpy").float32(float(c)))) if single else float
     J = [lambda x: mp.besselj(0, x), lambda x: mp.besselj(1, x)]
     Y = [lambda x: mp.bessely(0, x), lambda x: mp.bessely(1, x)]
-    tabs, worst_low, worst_hk = {}, mp.mpf(0), mp.mpf(0)
+    tabs, exact, worst_low, worst_hk = {}, {}, mp.mpf(0), mp.mpf(0)
     for name, fs, q0 in (("J", J, 0), ("Y", Y, 6)):
         for nu in (0, 1):
-            rows = []
+            rows, rows_x = [], []
             for q in range(q0, 16):
                 a = mp.mpf(q) / 2
-                cf = [rnd(c) for c in cheb_monomials(fs[nu], a, a + mp.mpf(1) / 2, deg_low)]
+                cx = cheb_monomials(fs[nu], a, a + mp.mpf(1) / 2, deg_low)
+                cf = [rnd(c) for c in cx]
                 for k in range(33):
                     x = a + mp.mpf(k) / 64
                     worst_low = max(worst_low, abs(horner(cf, float(x - a - mp.mpf(1) / 4)) - fs[nu](x)))
                 rows += cf
+                rows_x += cx
             tabs[f"{name}{nu}"] = rows
+            exact[f"{name}{nu}"] = rows_x
     for nu in (0, 1):
         for part in (0, 1):
             g = lambda u, nu=nu, part=part: hankel_pq(nu, u)[part]
-            cf = [rnd(c) for c in cheb_monomials(g, mp.mpf(0), mp.mpf(1), deg_hankel)]
+            cx = cheb_monomials(g, mp.mpf(0), mp.mpf(1), deg_hankel)
+            cf = [rnd(c) for c in cx]
             for k in range(1, 65):
                 u = mp.mpf(k) / 64
                 worst_hk = max(worst_hk, abs(horner(cf, float(u - mp.mpf(1) / 2)) - g(u)))
             tabs[f"{'PQ'[part]}{nu}"] = cf
-    return tabs, worst_low, worst_hk
+            exact[f"{'PQ'[part]}{nu}"] = cx
+    return tabs, exact, worst_low, worst_hk
 
 
 def wu_fit_chebyshev(mono):
@@ -166,9 +248,13 @@ def clenshaw(c, s):
 
 
 def main():
-    tabs, wl, wh = bessel_tables(DEG_LOW, DEG_HANKEL, False)
+    tabs, tabx, wl, wh = bessel_tables(DEG_LOW, DEG_HANKEL, False)
     print("FP64 Bessel: worst abs error low region", mp.nstr(wl, 3), "Hankel P, Q/s", mp.nstr(wh, 3))
-    tabf, wlf, whf = bessel_tables(DEG_LOW_F, DEG_HANKEL_F, True)
+    tabq = fx_bessel_tables(tabx)
+    wlq, whq = fx_bessel_errors(tabq)
+    print("fixed-point Bessel: worst abs error low region", mp.nstr(wlq, 3), "Hankel P, Q/s", mp.nstr(whq, 3))
+    assert wlq < 1e-16 and whq < 1e-16
+    tabf, _, wlf, whf = bessel_tables(DEG_LOW_F, DEG_HANKEL_F, True)
     print("FP32 Bessel: worst abs error low region", mp.nstr(wlf, 3), "Hankel P, Q/s", mp.nstr(whf, 3))
     wu = {}
     for key, mono in WU_FITS.items():
@@ -182,7 +268,8 @@ def main():
     with open(out, "w") as fh:
         fh.write("// mh_special_tables.cuh -- generated by gen_special_tables.py (mpmath, 40 digits); do not\n")
         fh.write("// edit.  Polynomial coefficients, lowest degree first, of the J0, J1, Y0, Y1 evaluators\n")
-        fh.write("// (mh_bessel01.cuh) and the Chebyshev form of the Wu fits (mh_wu_f32.cuh).\n")
+        fh.write("// (mh_bessel01.cuh; FP64, fixed-point and FP32) and the Chebyshev form of the Wu fits\n")
+        fh.write("// (mh_wu_f32.cuh).\n")
         fh.write("#pragma once\n\nnamespace mh {\n")
         for ns, tb, dl, dh, single in (("bes", tabs, DEG_LOW, DEG_HANKEL, False),
                                        ("besf", tabf, DEG_LOW_F, DEG_HANKEL_F, True)):
@@ -200,6 +287,18 @@ def main():
                 fh.write(f"// {what} for x >= 8\n")
                 fh.write(f"__constant__ {ty} k{key}[kHankelTerms] = {{\n    {fmt(tb[key], single)}}};\n\n")
             fh.write(f"}}  // namespace {ns}\n\n")
+        fh.write("namespace besq {\n\n")
+        fh.write(f"constexpr int kFrac = {QF};  // coefficients and values are integers v 2^-kFrac\n\n")
+        for key in ("J0", "J1"):
+            fh.write(f"// {key} on [q/2, q/2 + 1/2), q = 0..15, in z = 2 (x - q/2 - 1/4)\n")
+            fh.write(f"__device__ const long long k{key}[16 * bes::kLowTerms] = {{\n    {fmt_int(tabq[key])}}};\n\n")
+        for key in ("Y0", "Y1"):
+            fh.write(f"// {key} on [q/2, q/2 + 1/2), q = 6..15 (row q - 6), in z = 2 (x - q/2 - 1/4)\n")
+            fh.write(f"__device__ const long long k{key}[10 * bes::kLowTerms] = {{\n    {fmt_int(tabq[key])}}};\n\n")
+        for key, what in (("P0", "P0"), ("Q0", "Q0 / s"), ("P1", "P1"), ("Q1", "Q1 / s")):
+            fh.write(f"// {what} for x >= 8, in z = (u - 1/2) / 2\n")
+            fh.write(f"__constant__ long long k{key}[bes::kHankelTerms] = {{\n    {fmt_int(tabq[key])}}};\n\n")
+        fh.write("}  // namespace besq\n\n")
         fh.write("namespace wuf {\n\n")
         fh.write("// Wu fits (wu.jl:131-197, 235-329) as sum_j c_j T_j(2 rho - 1), FP32\n")
         for key in WU_FITS:

@@ -231,12 +231,10 @@ __device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double
     double hh, vv;
     reduced_coords(ci, cj, k, hh, vv);
     double2 GF, Gh, Gv;
-    wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv);
-    double dr1 = 0.0, dr2 = 0.0;
-    if (fabs(hh) > 1e-6) {
-      dr1 = k * k / hh * dx1;
-      dr2 = k * k / hh * dx2;
-    }
+    double inv_hh;  // 1/hh, or 0 where the horizontal gradient is zeroed (hh <= 1e-6)
+    wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv, &inv_hh);
+    const double kk_hh = k * k * inv_hh;
+    const double dr1 = kk_hh * dx1, dr2 = kk_hh * dx2;
     w.I = make_double2(k * GF.x, k * GF.y);
     w.gh[0] = make_double2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
     w.gh[1] = make_double2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));

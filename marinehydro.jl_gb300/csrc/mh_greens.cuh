@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "mh_bessel01.cuh"
+#include "mh_fixpoint.cuh"
 #include "mh_internal.cuh"
 
 namespace mh {
@@ -174,70 +175,85 @@ __device__ inline void delhommeau_rankine(const double pt[3], const PanelRec& P,
 }
 
 // ------------------------------------ Wu -----------------------------------
-// Polynomial fits A-D and dA-dC of Liang, Wu & Noblesse (wu.jl:131-197, 235-329).
-__device__ __forceinline__ double wu_dC(double t) {
-  double v = (3168.35 + -1590.27 * t) * t;
-  v = (-2318.58 + v) * t; v = (847.8 + v) * t; v = (-148.24 + v) * t;
-  return 14.19 + v;
-}
-__device__ __forceinline__ double wu_dB(double t) {
-  double v = (-76209.82 + 19923.28 * t) * t;
-  v = (118879.26 + v) * t; v = (-97014.11 + v) * t; v = (44270.15 + v) * t; v = (-11336.19 + v) * t;
-  v = (1565.35 + v) * t; v = (-76.765 + v) * t; v = (2.894 + v) * t;
-  return 1.11 + v;
-}
-__device__ __forceinline__ double wu_dA(double t) {
-  double v = (-46688.0 + 12622.25 * t) * t;
-  v = (68220.87 + v) * t; v = (-48811.41 + v) * t; v = (16370.75 + v) * t; v = (-1187.71 + v) * t;
-  v = (-754.85 + v) * t; v = (249.69 + v) * t; v = (-24.53 + v) * t;
-  return 2.948 + v;
-}
-__device__ __forceinline__ double wu_D(double t) {
-  double v = (128170.2 + -33744.6 * t) * t;
-  v = (-205690.43 + v) * t; v = (181856.75 + v) * t; v = (-96293.05 + v) * t; v = (31127.39 + v) * t;
-  v = (-6072.07 + v) * t; v = (667.16 + v) * t; v = (-40.97 + v) * t;
-  return 0.632 + v;
-}
-__device__ __forceinline__ double wu_C(double t) {
-  double v = (9136.4 + -3272.62 * t) * t;
-  v = (-9844.35 + v) * t; v = (5155.67 + v) * t; v = (-1397.89 + v) * t; v = (209.653 + v) * t;
-  v = (-9.747 + v) * t;
-  return 1.268 + v;
-}
-__device__ __forceinline__ double wu_B(double t) {
-  double v = (-29030.24 + 7671.22 * t) * t;
-  v = (44894.06 + v) * t; v = (-36618.81 + v) * t; v = (17137.74 + v) * t; v = (-4780.77 + v) * t;
-  v = (796.534 + v) * t; v = (-67.92 + v) * t; v = (5.737 + v) * t;
-  return 0.938 + v;
-}
-__device__ __forceinline__ double wu_A(double t) {
-  double v = (21859.0 + -4838.6 * t) * t;
-  v = (-41592.9 + v) * t; v = (42002.57 + v) * t; v = (-24314.21 + v) * t; v = (8418.94 + v) * t;
-  v = (-1763.96 + v) * t; v = (215.896 + v) * t; v = (-13.328 + v) * t;
-  return 1.21 + v;
+// Polynomial fits A-D and dA-dC of Liang, Wu & Noblesse (wu.jl:131-197, 235-329), lowest
+// degree first, all seven at one rho in [0, 1), in 64-bit fixed point on the integer pipe
+// (mh_fixpoint.cuh): coefficients and partial sums are integers v 2^-44 (the partial sums
+// stay below 2^18 on [0, 1)), so each Horner step truncates at 5.7e-14 absolute where FP64
+// rounds partial sums up to 2e5 at 2.9e-11 (worst error of a fit 4e-13 here, up to 3e-11 in
+// the reference's FP64 order); the coefficients are the FP64 values of the literals, as in
+// the reference, exactly.
+struct WuFits {
+  double A, B, C, D, dA, dB, dC;
+};
+
+__device__ __forceinline__ void wu_fits(double rho, WuFits& f) {
+  constexpr int F = 44;
+  constexpr long long kA[10] = {fx::q(1.21, F), fx::q(-13.328, F), fx::q(215.896, F), fx::q(-1763.96, F),
+                                fx::q(8418.94, F), fx::q(-24314.21, F), fx::q(42002.57, F), fx::q(-41592.9, F),
+                                fx::q(21859.0, F), fx::q(-4838.6, F)};
+  constexpr long long kB[10] = {fx::q(0.938, F), fx::q(5.737, F), fx::q(-67.92, F), fx::q(796.534, F),
+                                fx::q(-4780.77, F), fx::q(17137.74, F), fx::q(-36618.81, F), fx::q(44894.06, F),
+                                fx::q(-29030.24, F), fx::q(7671.22, F)};
+  constexpr long long kC[8] = {fx::q(1.268, F), fx::q(-9.747, F), fx::q(209.653, F), fx::q(-1397.89, F),
+                               fx::q(5155.67, F), fx::q(-9844.35, F), fx::q(9136.4, F), fx::q(-3272.62, F)};
+  constexpr long long kD[10] = {fx::q(0.632, F), fx::q(-40.97, F), fx::q(667.16, F), fx::q(-6072.07, F),
+                                fx::q(31127.39, F), fx::q(-96293.05, F), fx::q(181856.75, F), fx::q(-205690.43, F),
+                                fx::q(128170.2, F), fx::q(-33744.6, F)};
+  constexpr long long kdA[10] = {fx::q(2.948, F), fx::q(-24.53, F), fx::q(249.69, F), fx::q(-754.85, F),
+                                 fx::q(-1187.71, F), fx::q(16370.75, F), fx::q(-48811.41, F), fx::q(68220.87, F),
+                                 fx::q(-46688.0, F), fx::q(12622.25, F)};
+  constexpr long long kdB[10] = {fx::q(1.11, F), fx::q(2.894, F), fx::q(-76.765, F), fx::q(1565.35, F),
+                                 fx::q(-11336.19, F), fx::q(44270.15, F), fx::q(-97014.11, F), fx::q(118879.26, F),
+                                 fx::q(-76209.82, F), fx::q(19923.28, F)};
+  constexpr long long kdC[6] = {fx::q(14.19, F), fx::q(-148.24, F), fx::q(847.8, F), fx::q(-2318.58, F),
+                                fx::q(3168.35, F), fx::q(-1590.27, F)};
+  const unsigned long long t = fx::unit_q64(rho);
+  f.A = fx::to_double(fx::horner_u(kA, t), F);
+  f.B = fx::to_double(fx::horner_u(kB, t), F);
+  f.C = fx::to_double(fx::horner_u(kC, t), F);
+  f.D = fx::to_double(fx::horner_u(kD, t), F);
+  f.dA = fx::to_double(fx::horner_u(kdA, t), F);
+  f.dB = fx::to_double(fx::horner_u(kdB, t), F);
+  f.dC = fx::to_double(fx::horner_u(kdC, t), F);
 }
 
 // StruveH0 and StruveH1 fits (wu.jl:368-435); also returns J0/J1.  The four Bessel
-// functions of the argument come from one joint evaluation (mh_bessel01.cuh).
-__device__ inline void struve_bessel(double xx, double& H0, double& H1, double& J0, double& J1) {
+// functions of the argument come from one joint evaluation (mh_bessel01.cuh).  The
+// polynomials in yy in [0, 1] run in fixed point (v 2^-59 below 3, 2^-55 above, variable
+// yy / 2, so coefficient i carries 2^i); the rational fits' quotients stay FP64.
+// inv_xx = 1 / xx (used above 3).
+__device__ inline void struve_bessel(double xx, double inv_xx, double& H0, double& H1, double& J0, double& J1) {
   double Y0, Y1;
   bessel01(xx, J0, J1, Y0, Y1);
-  // FP64 division is a multi-instruction sequence on the FP64 pipe: x / 3 is taken as
-  // x * (1/3) and the two rational fits share one reciprocal (changes of an ulp, far below
-  // the fits' own 1e-9 accuracy)
+  constexpr int F = 59;
   if (xx <= 3.0) {
     const double x3 = xx * (1.0 / 3.0);
-    double yy = x3 * x3;
-    double h0 = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
-    H0 = h0 * x3;
-    H1 = (1.909859286 + (-1.145914713 + (0.294656958 + (-0.042070508 + (0.003785727 + -0.000207183 * yy) * yy) * yy) * yy) * yy) * yy;
+    const unsigned long long t = fx::unit_q63(x3 * x3);
+    constexpr long long kH0[6] = {fx::q(1.909859164, F), fx::q(-1.909855001, F + 1), fx::q(0.687514637, F + 2),
+                                  fx::q(-0.126164557, F + 3), fx::q(0.013828813, F + 4),
+                                  fx::q(-0.000876918, F + 5)};
+    // H1 = yy (1.909859286 + ...): the factor yy as one more Horner step with c = 0
+    constexpr long long kH1[7] = {0, fx::q(1.909859286, F + 1), fx::q(-1.145914713, F + 2),
+                                  fx::q(0.294656958, F + 3), fx::q(-0.042070508, F + 4),
+                                  fx::q(0.003785727, F + 5), fx::q(-0.000207183, F + 6)};
+    H0 = fx::to_double(fx::horner_u(kH0, t), F) * x3;
+    H1 = fx::to_double(fx::horner_u(kH1, t), F);
   } else {
-    const double t = 3.0 / xx;
-    double yy = t * t;
-    double c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
-    double c2 = kPi * xx * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
-    double d1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
-    double d2 = kPi * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
+    constexpr int G = 55;  // partial sums up to 2^7
+    const double t3 = 3.0 * inv_xx;
+    const unsigned long long t = fx::unit_q63(t3 * t3);
+    constexpr long long kC1[4] = {fx::q(0.99999906, G + 1), fx::q(4.77228920, G + 2), fx::q(3.85542044, G + 3),
+                                  fx::q(0.32303607, G + 4)};  // 2 (a0 + a1 yy + ...)
+    constexpr long long kC2[4] = {fx::q(1.0, G), fx::q(4.88331068, G + 1), fx::q(4.28957333, G + 2),
+                                  fx::q(0.52120508, G + 3)};
+    constexpr long long kD1[4] = {fx::q(1.00000004, G + 1), fx::q(3.92205313, G + 2), fx::q(2.64893033, G + 3),
+                                  fx::q(0.27450895, G + 4)};
+    constexpr long long kD2[4] = {fx::q(1.0, G), fx::q(3.81095112, G + 1), fx::q(2.26216956, G + 2),
+                                  fx::q(0.10885141, G + 3)};
+    const double c1 = fx::to_double(fx::horner_u(kC1, t), G);
+    const double c2 = kPi * xx * fx::to_double(fx::horner_u(kC2, t), G);
+    const double d1 = fx::to_double(fx::horner_u(kD1, t), G);
+    const double d2 = kPi * fx::to_double(fx::horner_u(kD2, t), G);
     const double inv = 1.0 / (c2 * d2);
     H0 = c1 * d2 * inv + Y0;
     H1 = d1 * c2 * inv + Y1;
@@ -246,19 +262,28 @@ __device__ inline void struve_bessel(double xx, double& H0, double& H1, double& 
 
 // _wu_wave_term_and_derivs (wu.jl:28-37) with GF_Func_L0/Lp/W/Ls/Lsp/Wh (wu.jl:201-366)
 // FP64 division is a multi-instruction sequence on GB300's FP64 pipe, which bounds this
-// kernel; 1/dd, 1/(dd - vv) and 1/(1 + dd^3) come from one division and are multiplied
-// (rho stays a true division: it feeds the fits A-D, whose alternating coefficients up to
-// 2e5 amplify its last bit).
-__device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv) {
+// kernel; 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh come from one division and are
+// multiplied (rho stays a true division: it feeds the fits A-D, whose alternating
+// coefficients up to 2e5 amplify its last bit).  inv_hh: 1/hh for hh > 1e-6 (the only pairs
+// whose horizontal gradient factor k^2/hh is used, wu.jl:118-121), else 0.
+__device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv,
+                                               double* inv_hh = nullptr) {
   double dd = sqrt(hh * hh + vv * vv);
   double dd2 = dd * dd, dd3 = dd * dd * dd;
-  // 1/dd, 1/(dd - vv) and 1/(1 + dd^3) from one division of their product (all three
-  // factors are positive, dd - vv >= dd >= 0 with vv <= 0, and moderate)
+  // 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh from one division of their product (all
+  // factors are positive, dd - vv >= dd >= hh with vv <= 0, and moderate: below 1e6 in the
+  // reduced coordinates, so the product stays far inside the FP64 range)
   const double dmv = dd - vv, opd3 = 1.0 + dd3;
-  const double inv_all = 1.0 / (dd * dmv * opd3);
-  const double inv_dd = dmv * opd3 * inv_all;
-  const double inv_dmv = dd * opd3 * inv_all;
-  const double inv_1dd3 = dd * dmv * inv_all;
+  const bool has_h = fabs(hh) > 1e-6;
+  const double hf = has_h ? hh : 1.0;
+  const double prod3 = dd * dmv * opd3;
+  const double inv_all = 1.0 / (prod3 * hf);
+  const double inv_all3 = inv_all * hf;  // 1 / (dd dmv opd3)
+  const double inv_dd = dmv * opd3 * inv_all3;
+  const double inv_dmv = dd * opd3 * inv_all3;
+  const double inv_1dd3 = dd * dmv * inv_all3;
+  const double inv_h = has_h ? prod3 * inv_all : 0.0;
+  if (inv_hh) *inv_hh = inv_h;
   double alpha = -vv * inv_dd;
   double beta = hh * inv_dd;
   double rho = dd / (1 + dd);
@@ -266,12 +291,14 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   double omr3 = omr * omr * omr;
   double ev = exp(vv);
   double H0, H1, J0, J1;
-  struve_bessel(hh, H0, H1, J0, J1);
+  struve_bessel(hh, inv_h, H0, H1, J0, J1);
   // GF_Func_Lp
-  double RR = (1.0 - beta) * wu_A(rho);
-  RR -= beta * wu_B(rho);
-  RR -= alpha * wu_C(rho) / (1.0 + 6.0 * alpha * rho * (1.0 - rho));
-  RR += beta * (1.0 - beta) * wu_D(rho);
+  WuFits fit;
+  wu_fits(rho, fit);
+  double RR = (1.0 - beta) * fit.A;
+  RR -= beta * fit.B;
+  RR -= alpha * fit.C / (1.0 + 6.0 * alpha * rho * (1.0 - rho));
+  RR += beta * (1.0 - beta) * fit.D;
   double Lp = rho * omr3 * RR;
   // GF_Func_L0
   const double gama = 0.5772156649;
@@ -282,9 +309,9 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   const double twopi = 2 * kPi;
   GF = make_double2(-L0 - (twopi * H0) * ev, -((twopi * -J0) * ev));
   // GF_Func_Lsp
-  double RS = beta * wu_dA(rho);
-  RS -= (1.0 - alpha) * wu_dB(rho);
-  RS += beta * (1.0 - beta) * rho * (1.0 - 2.0 * rho) * wu_dC(rho);
+  double RS = beta * fit.dA;
+  RS -= (1.0 - alpha) * fit.dB;
+  RS += beta * (1.0 - beta) * rho * (1.0 - 2.0 * rho) * fit.dC;
   double Lsp = rho * omr3 * RS;
   // GF_Func_Ls
   double PS = (beta + hh) * inv_dmv;

@@ -63,8 +63,9 @@ def test_wu_wave_terms(mh, oracle, ctx):
     got = mh._device.wu_wave_terms(ctx, hh, vv)
     ref = np.array([oracle.wu_wave_term_and_derivs(h, v) for h, v in zip(hh, vv)])
     # The polynomial fits A-D of wu.jl:131-329 have coefficients up to 2e5 with
-    # alternating signs evaluated at rho in (0, 1): a last-bit difference (the GPU
-    # fuses multiply-adds, the reference does not) is amplified to ~1e-11 absolute.
+    # alternating signs evaluated at rho in (0, 1): the reference's FP64 rounding of the
+    # partial sums (the oracle follows it) is amplified to ~3e-11 absolute, while the GPU
+    # evaluates them in 64-bit fixed point (error ~4e-13).
     for c in range(3):
         err = np.abs(got[:, c] - ref[:, c]) / np.maximum(np.abs(ref[:, c]), 1.0)
         assert err.max() < 1e-10, (c, err.max())

@@ -10,7 +10,8 @@
   fits (StruveH0/H1) and Euler's constant of GF_Func_L0, as extracted from wu.jl, appears
   bit for bit in the oracle, in the FP64 kernels (primal and dual-number adjoint), in the
   FP32 surrogate base and in the generator of the Chebyshev tables -- each polynomial as
-  one contiguous run of literals in the order its Horner form uses them.  A mistyped or
+  one contiguous run of literals in the order its Horner form uses them (the FP64 kernel's
+  fixed-point tables list them lowest degree first).  A mistyped or
   reordered coefficient in any copy fails here, below the 2e-2 level at which the
   reference's own tests compare Wu with the exact Green function.
 """
@@ -165,7 +166,8 @@ def test_wu_fit_constants_match_wu_jl(path):
     lits = _literals(os.path.join(REPO, path))
     for name in POLYS:
         coeffs = [v for _, v in wu[name]]
-        assert _contains_run(lits, _horner_run(coeffs)), (path, name)
+        # the reference's nested order, or lowest degree first (the fixed-point tables)
+        assert _contains_run(lits, _horner_run(coeffs)) or _contains_run(lits, coeffs), (path, name)
     for name in ("StruveH0", "StruveH1"):
         for run in _struve_runs(wu[name]):
             assert _contains_run(lits, run), (path, name, run)
