@@ -19,6 +19,9 @@ mpmath at 40 digits):
   inverting the two relations.  Worst absolute error of P, Q/s: 3e-17.
 * FP32 tables: the same construction at degree 6 (half-unit intervals) and 6 (Hankel), for
   errors below FP32 rounding.
+* exp and log on the integer pipe (namespace fxq): 2^(j/32) and the degree-7 series of
+  2^(g/32) for exp, degree-10 Chebyshev interpolants of log on the 32 intervals of [1, 2)
+  for log, all as integers c 2^62; the integer evaluation is emulated bit for bit below.
 * Fixed-point tables (namespace besq) of the same FP64 polynomials for the integer-pipe
   evaluator (mh_fixpoint.cuh): 64-bit integers c 2^61 (|values| < 4).  Below x = 8 the
   variable is z = 2 t in [-1/2, 1/2) (coefficient i divided by 2^i), above it z = (u - 1/2) / 2
@@ -167,6 +170,71 @@ def fx_bessel_errors(fq):
     return worst_low, worst_hk
 
 
+# ---- exp and log on the integer pipe (mh_fixpoint.cuh) ------------------------------------
+EXP_DEG = 7   # 2^(g/32), g in [0, 1)
+LOG_DEG = 10  # log(1 + j/32 + u/32), u in [0, 1), per interval j = 0..31
+
+
+def fx_exp_tables():
+    tab = [q_int(mp.mpf(2) ** (mp.mpf(j) / 32), 62) for j in range(32)]
+    c = mp.log(2) / 32
+    poly = [q_int(c ** k / mp.factorial(k), 62) for k in range(EXP_DEG + 1)]
+    log2e = int(mp.nint(mp.log(mp.e, 2) * mp.mpf(2) ** 63))
+    return tab, poly, log2e
+
+
+def fx_log_tables():
+    rows = []
+    for j in range(32):
+        a = 1 + mp.mpf(j) / 32
+        f = lambda u, a=a: mp.log(a + u / 32)
+        cx = cheb_monomials(f, mp.mpf(0), mp.mpf(1), LOG_DEG)  # monomials in t = u - 1/2
+        # re-expand in u: sum c_i (u - 1/2)^i
+        from math import comb
+        cu = [mp.mpf(0)] * (LOG_DEG + 1)
+        for i, ci in enumerate(cx):
+            for m in range(i + 1):
+                cu[m] += ci * comb(i, m) * (-mp.mpf(1) / 2) ** (i - m)
+        rows += [q_int(c, 62) for c in cu]
+    ln2 = int(mp.nint(mp.log(2) * mp.mpf(2) ** 64))
+    return rows, ln2
+
+
+def mulhi_su(v, t):
+    return (v * t) >> 64
+
+
+def emu_exp(x, tab, poly, log2e):
+    """Bit-for-bit model of fx::exp (x <= 0, x > -745): see mh_fixpoint.cuh."""
+    s = 60 if abs(x) < 8 else 53
+    X = int(mp.mpf(x) * 2 ** s)  # truncation toward zero, as to_q
+    prod = X * log2e             # exact 128-bit signed product
+    n = prod >> (64 + s - 1)
+    F = (prod >> (s - 1)) & ((1 << 64) - 1)
+    j = F >> 59
+    G = (F << 5) & ((1 << 64) - 1)
+    v = poly[-1]
+    for c in reversed(poly[:-1]):
+        v = c + mulhi_su(v, G)
+    R = (tab[j] * v) >> 64
+    return mp.mpf(R) * mp.mpf(2) ** (n - 60)
+
+
+def emu_log(w, rows, ln2):
+    """Bit-for-bit model of fx::log (w > 0 normal, before the final rounding)."""
+    m, e = mp.frexp(mp.mpf(w))   # w = m 2^e, m in [1/2, 1)
+    n = int(e) - 1
+    frac = int((m * 2 - 1) * 2 ** 52)
+    j = frac >> 47
+    U = (frac << 17) & ((1 << 64) - 1)
+    row = rows[j * (LOG_DEG + 1):(j + 1) * (LOG_DEG + 1)]
+    v = row[-1]
+    for c in reversed(row[:-1]):
+        v = c + mulhi_su(v, U)
+    total = n * ln2 + (v << 2)
+    return mp.mpf(total) / mp.mpf(2) ** 64
+
+
 def fmt_int(vals):
     return ",\n    ".join(", ".join(f"{v}LL" for v in vals[i:i + 3]) for i in range(0, len(vals), 3))
 
@@ -254,6 +322,18 @@ def main():
     wlq, whq = fx_bessel_errors(tabq)
     print("fixed-point Bessel: worst abs error low region", mp.nstr(wlq, 3), "Hankel P, Q/s", mp.nstr(whq, 3))
     assert wlq < 1e-16 and whq < 1e-16
+    etab, epoly, log2e = fx_exp_tables()
+    import random
+    rng = random.Random(7)
+    xs = [-rng.uniform(0, 1) for _ in range(400)] + [-10 ** rng.uniform(-12, 2.8) for _ in range(400)]
+    xs += [0.0, -1e-300, -7.999999999, -8.0, -744.0, -0.5, -2.0 ** -40]
+    worst_e = max(abs(emu_exp(x, etab, epoly, log2e) / mp.exp(x) - 1) for x in xs)
+    ltab, ln2 = fx_log_tables()
+    ws = [10 ** rng.uniform(-300, 300) for _ in range(300)] + [rng.uniform(0.5, 2) for _ in range(300)]
+    ws += [1.0, 1 + 2.0 ** -52, 2 - 2.0 ** -52, 0.5, 3.0]
+    worst_l = max(abs(emu_log(w, ltab, ln2) - mp.log(w)) for w in ws)
+    print("fixed-point exp: worst relative error", mp.nstr(worst_e, 3), "; log: worst absolute error", mp.nstr(worst_l, 3))
+    assert worst_e < 5e-17 and worst_l < 4e-17
     tabf, _, wlf, whf = bessel_tables(DEG_LOW_F, DEG_HANKEL_F, True)
     print("FP32 Bessel: worst abs error low region", mp.nstr(wlf, 3), "Hankel P, Q/s", mp.nstr(whf, 3))
     wu = {}
@@ -299,6 +379,19 @@ def main():
             fh.write(f"// {what} for x >= 8, in z = (u - 1/2) / 2\n")
             fh.write(f"__constant__ long long k{key}[bes::kHankelTerms] = {{\n    {fmt_int(tabq[key])}}};\n\n")
         fh.write("}  // namespace besq\n\n")
+        fh.write("namespace fxq {\n\n")
+        fh.write("// exp on the integer pipe: 2^(j/32) 2^62, j = 0..31; 2^(g/32) = sum_k c_k g^k, c_k 2^62,\n")
+        fh.write("// g in [0, 1); log2(e) 2^63\n")
+        fh.write(f"__device__ const long long kExp2Tab[32] = {{\n    {fmt_int(etab)}}};\n")
+        fh.write(f"constexpr int kExpDeg = {EXP_DEG};\n")
+        fh.write(f"__constant__ long long kExp2Poly[{EXP_DEG + 1}] = {{\n    {fmt_int(epoly)}}};\n")
+        fh.write(f"constexpr unsigned long long kLog2eQ63 = {log2e}ULL;\n\n")
+        fh.write("// log on the integer pipe: log(1 + j/32 + u/32) = sum_k c_k u^k on u in [0, 1), c_k 2^62,\n")
+        fh.write("// row j = 0..31; ln 2 2^64\n")
+        fh.write(f"constexpr int kLogTerms = {LOG_DEG + 1};\n")
+        fh.write(f"__device__ const long long kLogTab[32 * kLogTerms] = {{\n    {fmt_int(ltab)}}};\n")
+        fh.write(f"constexpr unsigned long long kLn2Q64 = {ln2}ULL;\n\n")
+        fh.write("}  // namespace fxq\n\n")
         fh.write("namespace wuf {\n\n")
         fh.write("// Wu fits (wu.jl:131-197, 235-329) as sum_j c_j T_j(2 rho - 1), FP32\n")
         for key in WU_FITS:

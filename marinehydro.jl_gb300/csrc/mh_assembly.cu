@@ -212,77 +212,86 @@ __global__ void __launch_bounds__(kRowsPerCta) static_kernel(AssemblyParams p, d
 // as evaluating every ordered pair.  CTAs whose tile lies strictly below the
 // diagonal exit at once; within a tile, a thread handles the pairs with i <= j.
 struct WaveTerms {
-  double2 I;       // integral before the -1/4pi scale, without the source area
-  double2 gh[2];   // horizontal gradient components for the (i, j) orientation, without area
-  double2 gz;      // vertical gradient component, without area
+  double2 I;    // -1/4pi times the integral, without the source area
+  double2 Gh;   // -1/4pi times the horizontal gradient factor: the gradient component c of the
+                // (i, j) orientation is Gh dx_c
+  double2 Gz;   // -1/4pi times the vertical gradient component
 };
 
+// the wave terms of one exact Delhommeau pair from its integrals G and dG/dr at (r, z)
+__device__ __forceinline__ WaveTerms egd_wave_terms(double r, double z, double k, double2 GF, double2 dGdr) {
+  const double kc1 = kMinusInv4Pi * k, kc2 = kc1 * k, kc3 = kc2 * k;
+  const double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
+  const double a = fabs(r) > 1e-6 ? kc3 / r : 0.0;
+  WaveTerms w;
+  w.I = make_double2(kc1 * GF.x, kc1 * GF.y);
+  w.Gh = make_double2(a * dGdr.x, a * dGdr.y);
+  w.Gz = make_double2(kc2 * dGdz.x, kc2 * dGdz.y);
+  return w;
+}
+
 // WMODE bits: 1 = Wu, 2 = exact Delhommeau (the learned surrogate has its own kernel,
-// wave_kernel_tc).
+// wave_kernel_tc).  kc[m] = -k^m / 4pi (m = 1, 2, 3), the pair-independent factors of the
+// terms: I = kc1 G, Gh dx_c = kc3 (1/hh) dx_c dG/dh, Gz = kc2 dG/dz (wu.jl:118-126).
 template <bool DIRECT, int WMODE>
 __device__ __forceinline__ void wave_terms(const AssemblyParams& p, const double ci[3], const double cj[3], double k,
-                                           WaveTerms& w) {
+                                           const double kc[4], WaveTerms& w) {
   w.I = make_double2(0.0, 0.0);
-  w.gh[0] = w.gh[1] = w.gz = w.I;
-  // (i, j) orientation: gradient w.r.t. the source (direct) or the field point (indirect)
-  const double dx1 = DIRECT ? cj[0] - ci[0] : ci[0] - cj[0];
-  const double dx2 = DIRECT ? cj[1] - ci[1] : ci[1] - cj[1];
+  w.Gh = w.Gz = w.I;
   if (WMODE & 1) {  // _wu_sd (wu.jl:112-127)
     double hh, vv;
     reduced_coords(ci, cj, k, hh, vv);
     double2 GF, Gh, Gv;
     double inv_hh;  // 1/hh, or 0 where the horizontal gradient is zeroed (hh <= 1e-6)
     wu_wave_term_and_derivs(hh, vv, GF, Gh, Gv, &inv_hh);
-    const double kk_hh = k * k * inv_hh;
-    const double dr1 = kk_hh * dx1, dr2 = kk_hh * dx2;
-    w.I = make_double2(k * GF.x, k * GF.y);
-    w.gh[0] = make_double2(k * (dr1 * Gh.x), k * (dr1 * Gh.y));
-    w.gh[1] = make_double2(k * (dr2 * Gh.x), k * (dr2 * Gh.y));
-    w.gz = make_double2(k * (k * Gv.x), k * (k * Gv.y));
+    const double a = kc[3] * inv_hh;
+    w.I = make_double2(kc[1] * GF.x, kc[1] * GF.y);
+    w.Gh = make_double2(a * Gh.x, a * Gh.y);
+    w.Gz = make_double2(kc[2] * Gv.x, kc[2] * Gv.y);
   }
   if (WMODE & 2) {  // both_greens_and_gradient_greens(::ExactGuevelDelhommeau)
     double r, z;
     reduced_coords(ci, cj, k, r, z);
-    double2 GF = egd_adaptive<false>(r, z, p.quad_rtol, p.quad_atol);
-    double2 dGdr = egd_adaptive<true>(r, z, p.quad_rtol, p.quad_atol);
-    double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
-    double d1 = 0.0, d2 = 0.0;
-    if (fabs(r) > 1e-6) {
-      d1 = k * k / r * dx1;
-      d2 = k * k / r * dx2;
-    }
-    w.I = zadd(w.I, make_double2(k * GF.x, k * GF.y));
-    w.gh[0] = zadd(w.gh[0], make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y)));
-    w.gh[1] = zadd(w.gh[1], make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y)));
-    w.gz = zadd(w.gz, make_double2(k * (k * dGdz.x), k * (k * dGdz.y)));
+    const WaveTerms e = egd_wave_terms(r, z, k, egd_adaptive<false>(r, z, p.quad_rtol, p.quad_atol),
+                                       egd_adaptive<true>(r, z, p.quad_rtol, p.quad_atol));
+    w.I = zadd(w.I, e.I);
+    w.Gh = zadd(w.Gh, e.Gh);
+    w.Gz = zadd(w.Gz, e.Gz);
   }
 }
 
-// S and D entries (before adding the static part) from the wave terms; `sgn` = -1
-// gives the mirrored (j, i) orientation, `area` and `nv` are that entry's.
-__device__ __forceinline__ void wave_entry(const WaveTerms& w, double sgn, double area, const double nv[3],
-                                           double2& sv, double2& dv) {
-  const double2 g0 = make_double2(sgn * w.gh[0].x, sgn * w.gh[0].y);
-  const double2 g1 = make_double2(sgn * w.gh[1].x, sgn * w.gh[1].y);
-  const double2 s = make_double2(w.I.x * area, w.I.y * area);
-  const double2 d = make_double2((nv[0] * g0.x + nv[1] * g1.x + nv[2] * w.gz.x) * area,
-                                 (nv[0] * g0.y + nv[1] * g1.y + nv[2] * w.gz.y) * area);
-  sv = make_double2(kMinusInv4Pi * s.x, kMinusInv4Pi * s.y);
-  dv = make_double2(kMinusInv4Pi * d.x, kMinusInv4Pi * d.y);
+// S and D entries (before adding the static part) from the wave terms: `sgn` = -1 gives the
+// mirrored (j, i) orientation, `area` is the entry's source area and `an` its normal times
+// that area.
+__device__ __forceinline__ void wave_entry(const WaveTerms& w, double dx1, double dx2, double sgn, double area,
+                                           const double an[3], double2& sv, double2& dv) {
+  const double proj = sgn * (an[0] * dx1 + an[1] * dx2);
+  sv = make_double2(w.I.x * area, w.I.y * area);
+  dv = make_double2(fma(proj, w.Gh.x, an[2] * w.Gz.x), fma(proj, w.Gh.y, an[2] * w.Gz.y));
 }
 
-// writes the (i, j) entry and, for i != j, the mirrored (j, i) entry of one unordered pair
+// writes the (i, j) entry and, for i != j, the mirrored (j, i) entry of one unordered pair;
+// ani, anj: area-weighted normals of panels i and j (used as the entries' normals in the
+// direct formulation with panel normals)
 template <bool DIRECT>
 __device__ __forceinline__ void store_pair(const AssemblyParams& p, const WaveTerms& w, int64_t i, int64_t j,
-                                           const double ni[3], double ai, const PanelRec& Pj,
+                                           const double ni[3], double ai, const double ani[3], const PanelRec& Pj,
+                                           const double anj[3], double dx1, double dx2,
                                            const double* __restrict__ SR, const double* __restrict__ DR,
                                            double2* __restrict__ Sb, double2* __restrict__ Db, int wave_identity) {
   const int64_t n = p.n;
+  const bool own = DIRECT && !p.has_fixed;  // entry normals are the source panels' own
   // (i, j): source j
-  double nv[3];
-  pick_normal<DIRECT>(p, Pj, ni, nv);
+  double an[3];
+  if (own) {
+    an[0] = anj[0]; an[1] = anj[1]; an[2] = anj[2];
+  } else {
+    double nv[3];
+    pick_normal<DIRECT>(p, Pj, ni, nv);
+    for (int c = 0; c < 3; ++c) an[c] = Pj.area * nv[c];
+  }
   double2 sv, dv;
-  wave_entry(w, 1.0, Pj.area, nv, sv, dv);
+  wave_entry(w, dx1, dx2, 1.0, Pj.area, an, sv, dv);
   if (wave_identity && i == j) dv.x += identity_jump(p, ni);
   const int64_t idx = i + j * n;
   if (SR) {
@@ -293,12 +302,17 @@ __device__ __forceinline__ void store_pair(const AssemblyParams& p, const WaveTe
   Db[idx] = dv;
   if (i == j) return;
   // (j, i): source i, field j -- normal of the source (direct) / field (indirect) swaps
-  double nm[3];
-  if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
-  else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
-  else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
+  if (own) {
+    an[0] = ani[0]; an[1] = ani[1]; an[2] = ani[2];
+  } else {
+    double nm[3];
+    if (p.has_fixed) { nm[0] = p.fixed[0]; nm[1] = p.fixed[1]; nm[2] = p.fixed[2]; }
+    else if (DIRECT) { nm[0] = ni[0]; nm[1] = ni[1]; nm[2] = ni[2]; }
+    else { nm[0] = Pj.n[0]; nm[1] = Pj.n[1]; nm[2] = Pj.n[2]; }
+    for (int c = 0; c < 3; ++c) an[c] = ai * nm[c];
+  }
   double2 sm, dm;
-  wave_entry(w, -1.0, ai, nm, sm, dm);
+  wave_entry(w, dx1, dx2, -1.0, ai, an, sm, dm);
   const int64_t mdx = j + i * n;
   if (SR) {
     sm.x = SR[mdx] + sm.x;
@@ -315,28 +329,36 @@ __global__ void __launch_bounds__(kRowsPerCta) wave_kernel(AssemblyParams p, con
                                                            double2* __restrict__ D, int64_t sstride,
                                                            int wave_identity) {
   __shared__ PanelRec sp[kColsPerCta];
+  __shared__ double san[kColsPerCta][3];  // area-weighted normals of the staged panels
   const int64_t n = p.n;
   const int64_t i0 = blockIdx.x * (int64_t)kRowsPerCta;
   const int64_t j0 = blockIdx.y * (int64_t)kColsPerCta;
   if (i0 > j0 + kColsPerCta - 1) return;  // tile strictly below the diagonal
   const int64_t i = i0 + threadIdx.x;
   const double k = ks[blockIdx.z];
+  const double kc[4] = {0.0, kMinusInv4Pi * k, kMinusInv4Pi * k * k, kMinusInv4Pi * k * k * k};
   double2* Sb = S + blockIdx.z * sstride;
   double2* Db = D + blockIdx.z * sstride;
   stage_panels(sp, p.P, j0, n);
   __syncthreads();
+  const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  for (int q = threadIdx.x; q < 3 * jmax; q += blockDim.x) san[q / 3][q % 3] = sp[q / 3].area * sp[q / 3].n[q % 3];
+  __syncthreads();
   if (i >= n) return;
-  double ci[3], ni[3];
+  double ci[3], ni[3], ani[3];
   for (int c = 0; c < 3; ++c) { ci[c] = __ldg(&p.P[i].c[c]); ni[c] = __ldg(&p.P[i].n[c]); }
   const double ai = __ldg(&p.P[i].area);
-  const int jmax = (int)((n - j0) < kColsPerCta ? (n - j0) : kColsPerCta);
+  for (int c = 0; c < 3; ++c) ani[c] = ai * ni[c];
   for (int jj = 0; jj < jmax; ++jj) {
     const int64_t j = j0 + jj;
     if (i > j) continue;
     const PanelRec& Pj = sp[jj];
     WaveTerms w;
-    wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, w);
-    store_pair<DIRECT>(p, w, i, j, ni, ai, Pj, SR, DR, Sb, Db, wave_identity);
+    wave_terms<DIRECT, WMODE>(p, ci, Pj.c, k, kc, w);
+    // (i, j) orientation: gradient w.r.t. the source (direct) or the field point (indirect)
+    const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
+    const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
+    store_pair<DIRECT>(p, w, i, j, ni, ai, ani, Pj, san[jj], dx1, dx2, SR, DR, Sb, Db, wave_identity);
   }
 }
 
@@ -618,19 +640,11 @@ __device__ __forceinline__ void exact_pair_warp(const AssemblyParams& p, int64_t
   // both_greens_and_gradient_greens + with_reduced_coordinates_derivative, as wave_terms<., 2>
   const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
   const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
-  const double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
-  double d1 = 0.0, d2 = 0.0;
-  if (fabs(r) > 1e-6) {
-    d1 = k * k / r * dx1;
-    d2 = k * k / r * dx2;
-  }
-  WaveTerms w;
-  w.I = make_double2(k * GF.x, k * GF.y);
-  w.gh[0] = make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y));
-  w.gh[1] = make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y));
-  w.gz = make_double2(k * (k * dGdz.x), k * (k * dGdz.y));
+  const WaveTerms w = egd_wave_terms(r, z, k, GF, dGdr);
   const double ni[3] = {Pi.n[0], Pi.n[1], Pi.n[2]};
-  store_pair<DIRECT>(p, w, i, j, ni, Pi.area, Pj, SR, DR, Sb, Db, wave_identity);
+  const double ani[3] = {Pi.area * ni[0], Pi.area * ni[1], Pi.area * ni[2]};
+  const double anj[3] = {Pj.area * Pj.n[0], Pj.area * Pj.n[1], Pj.area * Pj.n[2]};
+  store_pair<DIRECT>(p, w, i, j, ni, Pi.area, ani, Pj, anj, dx1, dx2, SR, DR, Sb, Db, wave_identity);
 }
 
 constexpr int kExactWarps = 4;  // warps per CTA of the warp-per-pair exact kernels
@@ -775,22 +789,13 @@ __global__ void __launch_bounds__(32 * kExactWarps) surrogate_judge_kernel(
   // the (i, j) entries as exact_pair_warp and store_pair form them
   const double dx1 = DIRECT ? Pj.c[0] - ci[0] : ci[0] - Pj.c[0];
   const double dx2 = DIRECT ? Pj.c[1] - ci[1] : ci[1] - Pj.c[1];
-  const double2 dGdz = make_double2(GF.x + 2 / hypot(r, z), GF.y);
-  double d1 = 0.0, d2 = 0.0;
-  if (fabs(r) > 1e-6) {
-    d1 = k * k / r * dx1;
-    d2 = k * k / r * dx2;
-  }
-  WaveTerms w;
-  w.I = make_double2(k * GF.x, k * GF.y);
-  w.gh[0] = make_double2(k * (d1 * dGdr.x), k * (d1 * dGdr.y));
-  w.gh[1] = make_double2(k * (d2 * dGdr.x), k * (d2 * dGdr.y));
-  w.gz = make_double2(k * (k * dGdz.x), k * (k * dGdz.y));
+  const WaveTerms w = egd_wave_terms(r, z, k, GF, dGdr);
   const double ni[3] = {Pi.n[0], Pi.n[1], Pi.n[2]};
   double nv[3];
   pick_normal<DIRECT>(p, Pj, ni, nv);
+  const double an[3] = {Pj.area * nv[0], Pj.area * nv[1], Pj.area * nv[2]};
   double2 sv, dv;
-  wave_entry(w, 1.0, Pj.area, nv, sv, dv);
+  wave_entry(w, dx1, dx2, 1.0, Pj.area, an, sv, dv);
   if (wave_identity && i == j) dv.x += identity_jump(p, ni);
   const int64_t idx = i + j * n;
   if (SR) {

@@ -10,11 +10,14 @@
 // |partial sums| < 2^18) or 59-61 (Struve, Bessel) that truncation is below the FP64
 // rounding of the same partial sums, so the results are at least as accurate as the FP64
 // evaluation they replace.  Conversions between double and fixed point are done on the
-// bits (exponent field, shifts, leading-zero count), also without the FP64 pipe.
+// bits (exponent field, shifts, leading-zero count), also without the FP64 pipe; so are the
+// reciprocal, exp and log below.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "mh_special_tables.cuh"
 
 namespace mh {
 namespace fx {
@@ -84,6 +87,91 @@ __device__ __forceinline__ double to_double(long long v, int frac) {
   }
   const unsigned long long bits = sign | ((unsigned long long)e << 52) | (m & 0x000FFFFFFFFFFFFFull);
   return (v == 0 || e <= 0) ? 0.0 : __longlong_as_double((long long)bits);
+}
+
+// 1/x for a normal x > 0, on the integer pipe: the FP32 reciprocal (one MUFU operation) of
+// the leading 24 mantissa bits as the seed, two Newton steps y <- y (2 - m y) in 64-bit fixed
+// point (mantissa m in [1, 2) as m 2^63, y in (1/2, 1) as y 2^64; the seed's 2^-22 error
+// squares to below the fixed point's 2^-62), rounded to 53 bits: within one ulp of the
+// correctly rounded quotient, without the FP64 pipe.  x = 0 gives +inf, as 1.0 / 0.0 does.
+__device__ __forceinline__ double recip(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long frac = b & 0x000FFFFFFFFFFFFFull;
+  if (e == 0) return __longlong_as_double(0x7FF0000000000000ll);
+  if (frac == 0) return __longlong_as_double((long long)((unsigned long long)(2046 - e) << 52));  // 2^(1023 - e)
+  const unsigned long long M = (frac | (1ull << 52)) << 11;
+  float yf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__int_as_float(0x3F800000 | (int)(frac >> 29))));
+  const unsigned int yb = __float_as_uint(yf);  // in [1/2 - 2^-24, 1]
+  unsigned long long Y = yb >= 0x3F800000u
+                             ? ~0ull
+                             : (unsigned long long)((yb & 0x7FFFFFu) | 0x800000u) << (40 + (int)(yb >> 23) - 126);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const unsigned long long E = 0ull - __umul64hi(M, Y);  // (2 - m y) 2^63
+    Y = __umul64hi(Y, E) << 1;                             // y (2 - m y) 2^64 <= 2^64 / m
+  }
+  const int p = 63 - __clzll(Y);  // 62 or 63
+  const int sh = p - 52;
+  unsigned long long mant = (Y >> sh) + ((Y >> (sh - 1)) & 1ull);
+  int ex = p + 1982 - e;  // 1/x = (Y 2^-64) 2^(1023 - e)
+  if (mant >> 53) { mant >>= 1; ++ex; }
+  if (ex <= 0) return 0.0;
+  return __longlong_as_double((long long)(((unsigned long long)ex << 52) | (mant & 0x000FFFFFFFFFFFFFull)));
+}
+
+// e^x for x <= 0 on the integer pipe (0 for x <= -745.25 and where the result is below the
+// normal range).  y = x log2(e) from a 128-bit product of x 2^s (s = 60 for |x| < 8, else
+// 53: exact) and log2(e) 2^63, so y's fraction f carries 64 bits; 2^f = 2^(j/32) 2^(g/32)
+// with j the top five bits of f, 2^(g/32) a degree-7 series and both factors as integers
+// c 2^62 (tables fxq); relative error below 3e-17 before the final rounding (emulated bit
+// for bit against mpmath by gen_special_tables.py).
+__device__ __forceinline__ double exp_nonpos(double x) {
+  const unsigned long long ax = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  if (ax >= 0x40874A0000000000ull) return 0.0;  // |x| >= 745.25
+  const int s = ax < 0x4020000000000000ull ? 60 : 53;  // |x| < 8
+  const long long X = to_q(x, s);
+  const long long hi = mulhi_su(X, fxq::kLog2eQ63);
+  const unsigned long long lo = (unsigned long long)X * fxq::kLog2eQ63;
+  const long long n = hi >> (s - 1);  // floor(y)
+  const unsigned long long F = ((unsigned long long)hi << (65 - s)) | (lo >> (s - 1));  // frac(y) 2^64
+  const int j = (int)(F >> 59);
+  const unsigned long long G = F << 5;
+  long long v = fxq::kExp2Poly[fxq::kExpDeg];
+#pragma unroll
+  for (int i = fxq::kExpDeg - 1; i >= 0; --i) v = fxq::kExp2Poly[i] + mulhi_su(v, G);
+  const long long R = (long long)__umul64hi((unsigned long long)__ldg(fxq::kExp2Tab + j), (unsigned long long)v);
+  return to_double(R, 60 - (int)n);  // R = 2^f 2^60
+}
+
+// log(w) for a normal w > 0 on the integer pipe (-inf for 0): w = m 2^n, m in [1, 2);
+// n ln 2 + log(m) with log(m) from a degree-10 interpolant on the 1/32-interval of m (table
+// fxq::kLogTab, c 2^62), summed as a 128-bit integer in units of 2^-64 and rounded to 2^-53:
+// absolute error below 8e-17, which is what the Wu term needs (log enters as
+// log(...) + gamma - 2 dd^2).
+__device__ __forceinline__ double log_pos(double w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return __longlong_as_double((long long)0xFFF0000000000000ull);
+  const unsigned long long frac = b & 0x000FFFFFFFFFFFFFull;
+  const long long* __restrict__ row = fxq::kLogTab + (int)(frac >> 47) * fxq::kLogTerms;
+  const unsigned long long U = frac << 17;
+  long long v = __ldg(row + fxq::kLogTerms - 1);
+#pragma unroll
+  for (int i = fxq::kLogTerms - 2; i >= 0; --i) v = __ldg(row + i) + mulhi_su(v, U);
+  // n ln2 2^64 + v 2^2 as a signed 128-bit (hi, lo), |total| < 2^74
+  const long long nn = e - 1023;
+  long long hi = mulhi_su(nn, fxq::kLn2Q64);
+  unsigned long long lo = (unsigned long long)nn * fxq::kLn2Q64;
+  const unsigned long long add = (unsigned long long)(v << 2);
+  const unsigned long long lo2 = lo + add;
+  hi += (v < 0 ? -1 : 0) + (lo2 < lo ? 1 : 0);
+  // round to 2^-53 and convert (|total 2^-11| < 2^63)
+  const unsigned long long lo3 = lo2 + 1024ull;
+  hi += lo3 < lo2 ? 1 : 0;
+  const long long q = (long long)(((unsigned long long)hi << 53) | (lo3 >> 11));
+  return to_double(q, 53);
 }
 
 // sum_i c[i] t^i for t in [0, 1) as unit_q64(t); coefficients and result v 2^-F

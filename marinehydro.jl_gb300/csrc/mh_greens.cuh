@@ -2,7 +2,8 @@
 //
 // Each function restates the reference function cited beside it (paths within the
 // MarineHydro.jl tree).  Elementary functions are CUDA's (exp, log, atan2, sqrt, hypot,
-// sincos); the Bessel functions J0, J1, Y0, Y1 (mh_bessel01.cuh, Chebyshev and Hankel
+// sincos), except in the Wu term, whose exp, log and reciprocals run on the integer pipe
+// (mh_fixpoint.cuh); the Bessel functions J0, J1, Y0, Y1 (mh_bessel01.cuh, Chebyshev and Hankel
 // forms), the complex exponential integral and the Gauss-Kronrod rule are written from
 // published methods (DLMF 10.17.3, 6.6.2, 6.9.1; Kronrod's 15-point nodes, QUADPACK qk15).
 #pragma once
@@ -254,7 +255,7 @@ __device__ inline void struve_bessel(double xx, double inv_xx, double& H0, doubl
     const double c2 = kPi * xx * fx::to_double(fx::horner_u(kC2, t), G);
     const double d1 = fx::to_double(fx::horner_u(kD1, t), G);
     const double d2 = kPi * fx::to_double(fx::horner_u(kD2, t), G);
-    const double inv = 1.0 / (c2 * d2);
+    const double inv = fx::recip(c2 * d2);
     H0 = c1 * d2 * inv + Y0;
     H1 = d1 * c2 * inv + Y1;
   }
@@ -262,9 +263,10 @@ __device__ inline void struve_bessel(double xx, double inv_xx, double& H0, doubl
 
 // _wu_wave_term_and_derivs (wu.jl:28-37) with GF_Func_L0/Lp/W/Ls/Lsp/Wh (wu.jl:201-366)
 // FP64 division is a multi-instruction sequence on GB300's FP64 pipe, which bounds this
-// kernel; 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh come from one division and are
-// multiplied (rho stays a true division: it feeds the fits A-D, whose alternating
-// coefficients up to 2e5 amplify its last bit).  inv_hh: 1/hh for hh > 1e-6 (the only pairs
+// kernel; 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh come from one reciprocal of their
+// product, taken on the integer pipe (fx::recip, within an ulp) like the other reciprocals
+// of the term, and are multiplied out (rho stays a correctly rounded FP64 division: an ulp
+// of rho moves the fits A-D by up to 1e-13).  inv_hh: 1/hh for hh > 1e-6 (the only pairs
 // whose horizontal gradient factor k^2/hh is used, wu.jl:118-121), else 0.
 __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv,
                                                double* inv_hh = nullptr) {
@@ -277,7 +279,7 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   const bool has_h = fabs(hh) > 1e-6;
   const double hf = has_h ? hh : 1.0;
   const double prod3 = dd * dmv * opd3;
-  const double inv_all = 1.0 / (prod3 * hf);
+  const double inv_all = fx::recip(prod3 * hf);
   const double inv_all3 = inv_all * hf;  // 1 / (dd dmv opd3)
   const double inv_dd = dmv * opd3 * inv_all3;
   const double inv_dmv = dd * opd3 * inv_all3;
@@ -289,7 +291,7 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   double rho = dd / (1 + dd);
   double omr = 1.0 - rho;
   double omr3 = omr * omr * omr;
-  double ev = exp(vv);
+  double ev = fx::exp_nonpos(vv);
   double H0, H1, J0, J1;
   struve_bessel(hh, inv_h, H0, H1, J0, J1);
   // GF_Func_Lp
@@ -297,12 +299,12 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   wu_fits(rho, fit);
   double RR = (1.0 - beta) * fit.A;
   RR -= beta * fit.B;
-  RR -= alpha * fit.C / (1.0 + 6.0 * alpha * rho * (1.0 - rho));
+  RR -= alpha * fit.C * fx::recip(1.0 + 6.0 * alpha * rho * (1.0 - rho));
   RR += beta * (1.0 - beta) * fit.D;
   double Lp = rho * omr3 * RR;
   // GF_Func_L0
   const double gama = 0.5772156649;
-  double PP = log(0.5 * (dd - vv)) + gama - 2.0 * dd2;
+  double PP = fx::log_pos(0.5 * (dd - vv)) + gama - 2.0 * dd2;
   PP = ev * PP;
   PP = PP + dd2 - vv;
   double L0 = 2.0 * PP * inv_1dd3 + 2.0 * Lp;
@@ -316,7 +318,7 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   // GF_Func_Ls
   double PS = (beta + hh) * inv_dmv;
   PS = PS - 2.0 * beta + 2.0 * ev * dd - hh;
-  double QS = exp(-dd) * (1.0 - beta);
+  double QS = fx::exp_nonpos(-dd) * (1.0 - beta);
   QS = QS * (1.0 + dd * inv_1dd3);
   double Ls = 2.0 * PS * inv_1dd3 - 4.0 * QS + 2.0 * Lsp;
   dGh = make_double2(-Ls - (twopi * (2 / kPi - H1)) * ev, -((twopi * J1) * ev));
