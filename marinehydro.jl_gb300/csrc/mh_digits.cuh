@@ -3,7 +3,8 @@
 //
 // A row (or column) of values with largest biased exponent emax (|v| < 2^E, E = emax - 1022)
 // is scaled to a 55-bit fixed point X = round(v 2^(55 - E)) and cut into eight balanced
-// base-128 digits d_0 .. d_7 in [-64, 64], X = sum_p d_p 128^(7 - p), each exact in BF16.
+// base-128 digits d_0 .. d_7 in [-64, 64], X = sum_p d_p 128^(7 - p) (the GEMV), or seven
+// balanced base-256 digits in [-128, 128] (the LU update); each digit is exact in BF16.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -76,6 +77,46 @@ __device__ __forceinline__ void split8(const double2 (&v)[8], int emax, uint32_t
     digits(fixed55(v[c + 1].y, emax), b1);
 #pragma unroll
     for (int p = 0; p < kDigits; ++p) {
+      pk[0][p][c >> 1] = bf16x2(a0[p], a1[p]);
+      pk[1][p][c >> 1] = bf16x2(b0[p], b1[p]);
+    }
+  }
+}
+
+// Seven balanced base-256 digits in [-128, 128] of the same X (|X| < 2^55), most significant
+// first: X = sum_p d_p 256^(6 - p).  X = hi 2^24 + lo, lo in [0, 2^24) gives digits 6..4 and
+// a carry, hi (|hi| < 2^31) digits 3..0.  Each is exact in BF16 (eight significant bits).
+constexpr int kDigits7 = 7;
+__device__ __forceinline__ void digits7(long long X, int (&d)[kDigits7]) {
+  int lo = (int)(X & 0xFFFFFF);
+  int hi = (int)(X >> 24);
+#pragma unroll
+  for (int p = kDigits7 - 1; p >= 4; --p) {
+    const int c = lo + 128;
+    d[p] = (c & 255) - 128;
+    lo = c >> 8;
+  }
+  hi += lo;
+#pragma unroll
+  for (int p = 3; p >= 1; --p) {
+    const int c = hi + 128;
+    d[p] = (c & 255) - 128;
+    hi = c >> 8;
+  }
+  d[0] = hi;
+}
+
+// split8 with seven base-256 digit planes
+__device__ __forceinline__ void split7(const double2 (&v)[8], int emax, uint32_t (&pk)[2][kDigits7][4]) {
+#pragma unroll
+  for (int c = 0; c < 8; c += 2) {
+    int a0[kDigits7], a1[kDigits7], b0[kDigits7], b1[kDigits7];
+    digits7(fixed55(v[c].x, emax), a0);
+    digits7(fixed55(v[c + 1].x, emax), a1);
+    digits7(fixed55(v[c].y, emax), b0);
+    digits7(fixed55(v[c + 1].y, emax), b1);
+#pragma unroll
+    for (int p = 0; p < kDigits7; ++p) {
       pk[0][p][c >> 1] = bf16x2(a0[p], a1[p]);
       pk[1][p][c >> 1] = bf16x2(b0[p], b1[p]);
     }

@@ -5,35 +5,36 @@
 // rate.  Each row i of L21 is scaled by 2^-e_i (e_i: the exponent of the row's largest
 // |re|, |im|) and each column j of U12 by 2^-f_j; a scaled value is rounded to a 55-bit
 // fixed-point integer (54 significant bits for the row's largest entry, more than FP64's 53)
-// and cut into eight balanced base-128 digits, each in [-64, 64] and exact in BF16:
-//     x = 2^e sum_p x_p 2^(-7 p - 6),   p = 0 (most significant) .. 7.
-// Then L21 U12 = 2^(e_i + f_j - 12) sum_d 2^(-7 d) T_d with T_d = sum_{p+q=d} X_p Y_q (complex),
-// and every T_d is an integer below 2^21 in magnitude, so the tensor cores accumulate it
-// exactly in FP32 (K = 32, at most 8 digit pairs and 2 real products per complex term).
-// Terms with p + q > 7 are dropped: they are below 2^-55 of the row/column scale product, the
-// size of FP64 rounding.  The T_d are combined exactly in 64-bit integers (d = 0..3 and
-// 4..7 separately, each below 2^43), converted once to FP64, scaled by the power of two and
-// subtracted from A22 -- a handful of FP64 operations per element instead of the 128 FMAs
-// of the FP64 update.
+// and cut into seven balanced base-256 digits, each in [-128, 128] and exact in BF16:
+//     x = 2^(e - 7) sum_p x_p 2^(-8 p),   p = 0 (most significant) .. 6.
+// Then L21 U12 = 2^(e_i + f_j - 14) sum_d 2^(-8 d) T_d with T_d = sum_{p+q=d} X_p Y_q (complex),
+// and every T_d is an integer of magnitude at most (d + 1) 2^20 < 2^23, so the tensor cores
+// accumulate it exactly in FP32 (K = 32, d + 1 <= 7 digit pairs, 2 real products per
+// complex term).  Terms with p + q > 6 are dropped: they are below 2^-55 of the row/column
+// scale product, the size of FP64 rounding.  The T_d are combined exactly in 64-bit integers
+// (d = 0..3 and 4..6 separately), rounded once to a 53-bit integer, scaled by the power of
+// two and subtracted from A22 -- one FP64 operation per real element instead of the 128 FMAs
+// of the FP64 update.  (Eight base-128 digits need 36 digit products for the same 55 bits;
+// seven base-256 digits need 28.)
 //
 // Kernels per panel step (all batched over the matrices of the sweep):
-//   ozaki_split (one launch, both halves) -- rows: L21 -> digit tiles A[row tile][digit][re/im] (128 x 32 BF16 each, in the
-//     canonical no-swizzle K-major layout) and the row exponents;
-//                    columns: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
-//     column exponents; the eight digit tiles of one part are consecutive, so digits
-//     q .. 7 form one (32 (8 - q)) x 32 operand;
-//   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 16 A digit
-//     tiles (128 KB) and double-buffered B tiles (2 x 32 KB) arrive in shared memory by TMA
-//     bulk copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (8 - p)
-//     multiplies X_p by the stacked Y_0 .. Y_{7-p} and accumulates X_p Y_q into the TMEM
-//     columns of T_{p+q} (Re: 32 d, Im: 256 + 32 d), so 64 MMAs (8 digits x 2 K-steps x 4
-//     real products) cover the 36 digit pairs.  (16-column tiles, whose two accumulator sets
+//   ozaki_split (one launch, both halves) -- rows: L21 -> digit tiles A[row tile][digit][re/im]
+//     (128 x 32 BF16 each, in the canonical no-swizzle K-major layout) and the row
+//     exponents; columns: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
+//     column exponents; the seven digit tiles of one part are consecutive, so digits
+//     q .. 6 form one (32 (7 - q)) x 32 operand;
+//   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 14 A digit
+//     tiles (112 KB) and double-buffered B tiles (2 x 28 KB) arrive in shared memory by TMA
+//     bulk copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (7 - p)
+//     multiplies X_p by the stacked Y_0 .. Y_{6-p} and accumulates X_p Y_q into the TMEM
+//     columns of T_{p+q} (Re: 32 d, Im: 224 + 32 d), so 56 MMAs (7 digits x 2 K-steps x 4
+//     real products) cover the 28 digit pairs.  (16-column tiles, whose two accumulator sets
 //     fit TMEM twice so that the products overlap the epilogue, measured 12 % slower: they
-//     read every A tile twice as often.)  The epilogue converts the exact integers
-//     with magic-number additions (no integer-to-FP64 conversion instructions), combines
-//     them in 32/64-bit integers, rounds hi + lo 2^-28 to one 53-bit integer, builds its
-//     scaled double with integer operations and applies it with one FP64 subtraction per real
-//     entry; C is prefetched into registers while the MMAs run.
+//     read every A tile twice as often.)  The epilogue converts the exact integers with
+//     magic-number additions (no integer-to-FP64 conversion instructions), combines them in
+//     32/64-bit integers, rounds hi + lo 2^-24 to one 53-bit integer, builds its scaled double
+//     with integer operations and applies it with one FP64 subtraction per real entry; C is
+//     prefetched into registers while the MMAs run.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -45,15 +46,15 @@ namespace mh {
 
 namespace {
 
-constexpr int kOzDigits = 8;
+constexpr int kOzDigits = 7;       // balanced base-256 digits (mh_digits.cuh, digits7)
 constexpr int kNB_oz = 32;          // the LU's panel width
 constexpr int kOzK = 32;            // panel width (the LU's kNB)
 constexpr int kOzRows = 128;        // output rows per CTA (MMA M)
 constexpr int kOzCols = 32;         // output columns per CTA (MMA N)
 constexpr int kOzATile = kOzRows * kOzK * 2;    // bytes of one A digit tile (128 x 32 BF16)
 constexpr int kOzBTile = kOzCols * kOzK * 2;    // bytes of one B digit tile (32 x 32 BF16)
-constexpr int kOzABytes = kOzDigits * 2 * kOzATile;   // 128 KB per row tile
-constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 32 KB per column tile
+constexpr int kOzABytes = kOzDigits * 2 * kOzATile;   // 112 KB per row tile
+constexpr int kOzBBytes = kOzDigits * 2 * kOzBTile;   // 28 KB per column tile
 constexpr uint32_t kOzTmemCols = 512;
 constexpr uint32_t kOzWaitPolls = 1u << 26;
 
@@ -88,8 +89,8 @@ __device__ __forceinline__ void ozaki_split_rows(int64_t bx, const BatchDesc& d,
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
   if (live && kq == 0) rowexp[b * rest + r] = dg::scale_of(emax);
-  uint32_t pk[2][dg::kDigits][4];
-  dg::split8(v, emax, pk);
+  uint32_t pk[2][dg::kDigits7][4];
+  dg::split7(v, emax, pk);
   unsigned char* tiles = digA + ((b * nrt + r / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
   const uint32_t off = tc::kmajor_offset((int)(r % kOzRows), 8 * kq, kOzK);
 #pragma unroll
@@ -127,8 +128,8 @@ __device__ __forceinline__ void ozaki_split_cols(int64_t bx, const BatchDesc& d,
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
   if (live && kq == 0) colexp[b * rest + c] = dg::scale_of(emax);
-  uint32_t pk[2][dg::kDigits][4];
-  dg::split8(v, emax, pk);
+  uint32_t pk[2][dg::kDigits7][4];
+  dg::split7(v, emax, pk);
   unsigned char* tiles = digB + ((b * nct + c / kOzCols) * kOzDigits * 2) * (int64_t)kOzBTile;
   const uint32_t off = tc::kmajor_offset((int)(c % kOzCols), 8 * kq, kOzK);
 #pragma unroll
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const uint32_t tmem = tmem_base;
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(&mbar_load[0], kOzABytes + kOzBBytes);
-    for (int q = 0; q < kOzABytes; q += 32768) tc::bulk_g2s(As + q, srcA + q, 32768, &mbar_load[0]);
+    for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, srcA + q, 16384, &mbar_load[0]);
     tc::bulk_g2s(Bs[0], srcB(ct0), kOzBBytes, &mbar_load[0]);
     if (ntile > 1) {
       tc::mbar_arrive_expect_tx(&mbar_load[1], kOzBBytes);
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
       const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
 #pragma unroll 1
       for (int p = 0; p < kOzDigits; ++p) {
-        const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{7-p} stacked along N
+        const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{6-p} stacked along N
         const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
         const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
         const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
@@ -278,7 +279,8 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
     for (int h8 = 0; h8 < 2; ++h8) {
       const int c0 = half * (kOzCols / 2) + 8 * h8;
-      // T_d as exact integers: (T0 2^7 + T1, T2 2^7 + T3, T4 2^7 + T5, T6 2^7 + T7), re and im
+      // T_d as exact integers, paired: (T0 2^8 + T1, T2 2^8 + T3, T4 2^8 + T5, T6), re and im.
+      // |T_d| <= (d + 1) 2^20 (d + 1 digit pairs, K = 32, two real products, |digit| <= 2^7)
       int pr[4][8], pi[4][8];
 #pragma unroll
       for (int dd = 0; dd < kOzDigits; ++dd) {
@@ -287,26 +289,36 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
         tc::tmem_ld8(trow + (uint32_t)(kOzDigits * kOzCols + dd * kOzCols + c0), vi);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          // |T| < 2^21: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
-          const int ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
-          const int ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
-          if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 128 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 128 + ii; }
+          int ir, ii;
+          if (dd <= 3) {
+            // |T| <= 2^22: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
+            ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
+            ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
+          } else {
+            // |T| < 2^23: 1.5 2^24 rounds T to an even integer 2 h exactly; the remainder
+            // T - 2 h in {-1, 0, 1} is exact too
+            const float yr = vr[q] + 25165824.0f, yi = vi[q] + 25165824.0f;
+            const float rr = vr[q] - (yr - 25165824.0f), ri = vi[q] - (yi - 25165824.0f);
+            ir = 2 * (__float_as_int(yr) - 0x4BC00000) + (__float_as_int(rr + 12582912.0f) - 0x4B400000);
+            ii = 2 * (__float_as_int(yi) - 0x4BC00000) + (__float_as_int(ri + 12582912.0f) - 0x4B400000);
+          }
+          if (dd == 6) { pr[3][q] = ir; pi[3][q] = ii; }
+          else if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 256 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 256 + ii; }
           else { pr[dd >> 1][q] = ir; pi[dd >> 1][q] = ii; }
         }
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int qq = 8 * h8 + q;
-        // hi = T0..T3 and lo = T4..T7 in base 2^7 (|hi|, |lo| <= 2^21 (2^21 + 2^14 + 2^7 + 1)
-        // < 1.008 2^42).  L21 U12 = 2^(e_i + f_j - 33) (hi + lo 2^-28); v = hi 2^10 + lo 2^-18,
-        // rounded to an integer (|v| < 2^53, error <= 2^-11 in units of hi: FP64 rounding of the
-        // largest possible sum), is scaled into a double by integer operations, so the FP64 pipe
-        // does one subtraction per real entry
-        const long long hr = (long long)pr[0][q] * 16384 + pr[1][q], lr = (long long)pr[2][q] * 16384 + pr[3][q];
-        const long long hi = (long long)pi[0][q] * 16384 + pi[1][q], li = (long long)pi[2][q] * 16384 + pi[3][q];
-        const long long vr = hr * 1024 + ((lr + (1LL << 17)) >> 18);
-        const long long vi = hi * 1024 + ((li + (1LL << 17)) >> 18);
-        const int sc = er + ce[qq] - 43;
+        // hi = T0 2^24 + T1 2^16 + T2 2^8 + T3 (< 2^44.01), lo = T4 2^16 + T5 2^8 + T6 (< 2^38.4);
+        // L21 U12 = 2^(e_i + f_j - 38) (hi + lo 2^-24); v = hi 2^8 + lo 2^-16, rounded to an
+        // integer (|v| < 2^52.1), is scaled into a double by integer operations, so the FP64
+        // pipe does one subtraction per real entry
+        const long long hr = (long long)pr[0][q] * 65536 + pr[1][q], lr = (long long)pr[2][q] * 256 + pr[3][q];
+        const long long hi = (long long)pi[0][q] * 65536 + pi[1][q], li = (long long)pi[2][q] * 256 + pi[3][q];
+        const long long vr = hr * 256 + ((lr + (1LL << 15)) >> 16);
+        const long long vi = hi * 256 + ((li + (1LL << 15)) >> 16);
+        const int sc = er + ce[qq] - 46;
         cv[qq].x -= scaled_i64(vr, sc);
         cv[qq].y -= scaled_i64(vi, sc);
       }
