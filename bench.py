@@ -235,12 +235,14 @@ def lu_gemm_flops(n, nb=32, per_mac=8):
     return f
 
 
-# Tensor work of the exact-digit (Ozaki) update per complex multiply-add: 36 digit pairs
-# (p + q <= 7 of eight digits each) x 4 real products x 2 flops
-OZAKI_TENSOR_FLOPS_PER_MAC = 36 * 4 * 2
-# FP64 instructions of the Wu pair evaluation (ncu instruction mix of wave_kernel<1,1>:
-# 241 DFMA + 88 DMUL + 45 DADD per unordered pair, a DFMA counted as 2 flops)
-WU_FLOPS_PER_UNORDERED_PAIR = 615
+# Tensor work of the exact-digit (Ozaki) update per complex multiply-add: 28 digit pairs
+# (p + q <= 6 of seven base-256 digits each) x 4 real products x 2 flops
+OZAKI_TENSOR_FLOPS_PER_MAC = 28 * 4 * 2
+# FP64 work of the Wu pair evaluation as the kernel executes it (ncu instruction mix of
+# wave_kernel<1,1>: 48 DFMA + 83 DMUL + 35 DADD per unordered pair, a DFMA counted as 2
+# flops); the fits, Struve and Bessel polynomials, exp, log and the reciprocals run on the
+# integer pipe and are not counted (the all-FP64 evaluation executed 615 flops per pair)
+WU_FLOPS_PER_UNORDERED_PAIR = 214
 # ncu figures of the dominant kernels (small cases of the same kernels; the capture command
 # of each is kept with its summary under profiles/)
 NCU = {
@@ -279,7 +281,7 @@ def roofline(prof, steps, n, n_omega, peak64, peaks, total_ms=None):
         out.update({"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                     "frac": achieved / peaks["bf16_tflops"],
                     "peak_source": f"dense BF16 burst ({peaks['source']}, MEASURED_PEAKS.json)",
-                    "work": "BF16 tensor flops of the exact-digit update: 36 digit pairs x 4 real products x 2 "
+                    "work": "BF16 tensor flops of the exact-digit update: 28 digit pairs x 4 real products x 2 "
                             "flops per complex multiply-add, summed over the panel steps",
                     "fp64_equivalent_tflops": macs * 8 / per_launch_s / 1e12,
                     "fp64_equivalent_frac_of_fp64_peak": macs * 8 / per_launch_s / 1e12 / peak64,

@@ -174,6 +174,40 @@ __device__ __forceinline__ double log_pos(double w) {
   return to_double(q, 53);
 }
 
+// sqrt(x) for x >= 0 on the integer pipe (0 for x below the normal range): x = m 2^(2h),
+// m in [1, 4); the FP32 reciprocal square root (one MUFU operation) of m's leading bits as
+// the seed, two Newton steps y <- y (3 - m y^2) / 2 in 64-bit fixed point (m 2^62, y 2^63),
+// then sqrt(m) = m y rounded to 53 bits: within one ulp of the correctly rounded root.
+__device__ __forceinline__ double sqrt_pos(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return 0.0;
+  const unsigned long long frac = b & 0x000FFFFFFFFFFFFFull;
+  const int odd = (e - 1023) & 1;  // the exponent made even: m = 1.f 2^odd
+  const unsigned long long M = ((frac | (1ull << 52)) << 9) << odd;  // m 2^61 (m < 4: < 2^63)
+  float yf;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__int_as_float(((127 + odd) << 23) | (int)(frac >> 29))));
+  const unsigned int yb = __float_as_uint(yf);  // in (1/2 - 2^-22, 1 + 2^-22)
+  unsigned long long Y = yb >= 0x3F800000u
+                             ? (1ull << 63)
+                             : (unsigned long long)((yb & 0x7FFFFFu) | 0x800000u) << (40 + (int)(yb >> 23) - 126 - 1);
+  const unsigned long long M62 = M << 1;  // m 2^62 (< 2^64)
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const unsigned long long Y2 = __umul64hi(Y, Y);        // y^2 2^62
+    const unsigned long long T = __umul64hi(M62, Y2);      // m y^2 2^60
+    const unsigned long long E = 3ull * (1ull << 60) - T;   // (3 - m y^2) 2^60
+    Y = __umul64hi(Y, E) << 3;                             // y (3 - m y^2) / 2  2^63
+  }
+  const unsigned long long S = __umul64hi(M62, Y);  // m y 2^61 = sqrt(m) 2^61, in [2^61, 2^62)
+  const int p = 63 - __clzll(S);
+  const int sh = p - 52;
+  unsigned long long mant = (S >> sh) + ((S >> (sh - 1)) & 1ull);
+  int ex = ((e - 1023 - odd) >> 1) + 1023 + (p - 61);
+  if (mant >> 53) { mant >>= 1; ++ex; }
+  return __longlong_as_double((long long)(((unsigned long long)ex << 52) | (mant & 0x000FFFFFFFFFFFFFull)));
+}
+
 // sum_i c[i] t^i for t in [0, 1) as unit_q64(t); coefficients and result v 2^-F
 template <int N>
 __device__ __forceinline__ long long horner_u(const long long (&c)[N], unsigned long long t) {

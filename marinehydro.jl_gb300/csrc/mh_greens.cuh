@@ -265,12 +265,12 @@ __device__ inline void struve_bessel(double xx, double inv_xx, double& H0, doubl
 // FP64 division is a multi-instruction sequence on GB300's FP64 pipe, which bounds this
 // kernel; 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh come from one reciprocal of their
 // product, taken on the integer pipe (fx::recip, within an ulp) like the other reciprocals
-// of the term, and are multiplied out (rho stays a correctly rounded FP64 division: an ulp
-// of rho moves the fits A-D by up to 1e-13).  inv_hh: 1/hh for hh > 1e-6 (the only pairs
+// and the square roots of the term, and are multiplied out (rho gets one residual
+// correction on top: an ulp of rho moves the fits A-D by up to 1e-13).  inv_hh: 1/hh for hh > 1e-6 (the only pairs
 // whose horizontal gradient factor k^2/hh is used, wu.jl:118-121), else 0.
 __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF, double2& dGh, double2& dGv,
                                                double* inv_hh = nullptr) {
-  double dd = sqrt(hh * hh + vv * vv);
+  double dd = fx::sqrt_pos(hh * hh + vv * vv);
   double dd2 = dd * dd, dd3 = dd * dd * dd;
   // 1/dd, 1/(dd - vv), 1/(1 + dd^3) and 1/hh from one division of their product (all
   // factors are positive, dd - vv >= dd >= hh with vv <= 0, and moderate: below 1e6 in the
@@ -288,7 +288,12 @@ __device__ inline void wu_wave_term_and_derivs(double hh, double vv, double2& GF
   if (inv_hh) *inv_hh = inv_h;
   double alpha = -vv * inv_dd;
   double beta = hh * inv_dd;
-  double rho = dd / (1 + dd);
+  // rho = dd / (1 + dd): the integer-pipe reciprocal and one residual correction, which
+  // leaves rho within a rounding of the correctly rounded quotient
+  const double opdd = 1 + dd;
+  const double r1 = fx::recip(opdd);
+  double rho = dd * r1;
+  rho = fma(fma(-rho, opdd, dd), r1, rho);
   double omr = 1.0 - rho;
   double omr3 = omr * omr * omr;
   double ev = fx::exp_nonpos(vv);
@@ -330,7 +335,7 @@ __device__ __forceinline__ void reduced_coords(const double x[3], const double x
                                                double& vv) {
   double d2 = (x[0] - xi[0]) * (x[0] - xi[0]) + (x[1] - xi[1]) * (x[1] - xi[1]);
   const double purt = 1e-18;
-  double dis = (d2 == 0) ? sqrt(d2 + purt * purt) - purt : sqrt(d2);
+  double dis = (d2 == 0) ? sqrt(d2 + purt * purt) - purt : fx::sqrt_pos(d2);
   hh = k * dis;
   vv = k * (x[2] + xi[2]);
 }
