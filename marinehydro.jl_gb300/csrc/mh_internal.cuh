@@ -188,6 +188,10 @@ void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, 
                          void* ws, int* timeout_flag);
 void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
                            void* ws, int* timeout_flag);
+// U12 = L11^-1 A12 of panel step k (a full 32-column panel) as an exact-digit product on the
+// tensor cores (mh_ozaki.cu); same workspace as the trailing update
+void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,
+                int* timeout_flag);
 template <typename T>
 void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
                       const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,

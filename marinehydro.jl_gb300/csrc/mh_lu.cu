@@ -1179,8 +1179,17 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     }
     const int64_t rest = n - k - kb;
     if (rest <= 0) continue;
-    dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
-    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
+    bool trsm_done = false;
+    if constexpr (sizeof(T) == 8) {  // FP64 with the tensor-core update: U12 on the tensor cores too
+      if (emu_ws && kb == kNB) {
+        ozaki_trsm(st, lc, d, A, k, emu_ws, emu_flag);
+        trsm_done = true;
+      }
+    }
+    if (!trsm_done) {
+      dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
+      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
+    }
     if (emu_ws) {
       if constexpr (sizeof(T) == 8) {  // FP64 update on the BF16 tensor cores (mh_ozaki.cu)
         ozaki_trailing_update(st, lc, d, A, k, (int)kb, emu_ws, emu_flag);

@@ -149,6 +149,105 @@ __global__ void __launch_bounds__(256) ozaki_split_kernel(BatchDesc d, const dou
   else ozaki_split_cols(blockIdx.x - row_ctas, d, A, k, kb, rest, nct, digB, colexp);
 }
 
+// ---- U12 = L11^-1 A12 on the tensor cores -------------------------------------------------
+// The triangular solve of a panel step is the product U12^T = A12^T (L11^-1)^T: rows = the
+// columns of A12 (the A operand, 128-row tiles, K = the panel's 32 rows), columns = the 32
+// rows of U12 (one B tile).  ozaki_trsm_prep_kernel: CTAs [0, row_ctas) cut the columns of
+// A12 into A digit tiles (their 32 entries are contiguous); the last CTA of each matrix
+// inverts the unit lower triangular L11 in FP64 (column-oriented forward substitution of
+// L X = I over all its threads) and cuts the columns of (L11^-1)^T into the B tile.
+// ozaki_gemm_kernel<true> then writes the products into U12.  The inverse of a unit lower
+// triangular matrix whose multipliers are bounded by partial pivoting is well conditioned
+// in practice; the error of U12 is of the order of the substitution's (Higham, Accuracy and
+// Stability of Numerical Algorithms, 2nd ed., sec. 14.2).
+__global__ void __launch_bounds__(256) ozaki_trsm_prep_kernel(BatchDesc d, const double2* __restrict__ A, int64_t k,
+                                                              int64_t rest, int64_t nrt, int64_t row_ctas,
+                                                              unsigned char* __restrict__ digA,
+                                                              unsigned char* __restrict__ digB, int* __restrict__ rowexp,
+                                                              int* __restrict__ colexp) {
+  const int64_t b = blockIdx.y;
+  const int64_t n = d.order(b);
+  if (k + kNB_oz >= n) return;  // no U12 for this matrix
+  const int kb = kNB_oz;
+  const int64_t rest_b = n - k - kb;
+  const double2* Ab = A + d.offset(b);
+  if ((int64_t)blockIdx.x < row_ctas) {
+    // column c of A12 (rows k .. k+31) as row c of the A operand; four threads per column
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t c = t >> 2;
+    const int kq = (int)(t & 3);
+    if (c >= nrt * kOzRows) return;  // whole groups of four leave together
+    const bool live = c < rest_b;
+    double2 v[8];
+    int emax = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = live ? Ab[(k + 8 * kq + q) + (k + kb + c) * n] : make_double2(0.0, 0.0);
+      emax = max(emax, max(dg::biased_exp(v[q].x), dg::biased_exp(v[q].y)));
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    if (live && kq == 0) rowexp[b * rest + c] = dg::scale_of(emax);
+    uint32_t pk[2][dg::kDigits7][4];
+    dg::split7(v, emax, pk);
+    unsigned char* tiles = digA + ((b * nrt + c / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
+    const uint32_t off = tc::kmajor_offset((int)(c % kOzRows), 8 * kq, kOzK);
+#pragma unroll
+    for (int p = 0; p < kOzDigits; ++p) {
+      *reinterpret_cast<uint4*>(tiles + (2 * p) * kOzATile + off) = make_uint4(pk[0][p][0], pk[0][p][1], pk[0][p][2], pk[0][p][3]);
+      *reinterpret_cast<uint4*>(tiles + (2 * p + 1) * kOzATile + off) = make_uint4(pk[1][p][0], pk[1][p][1], pk[1][p][2], pk[1][p][3]);
+    }
+    return;
+  }
+  // L11 and its inverse X in shared memory.  L X = I column-oriented (right-looking): once row
+  // r of X is final, rows s > r take -L[s][r] X[r][c] for c <= r -- (31 - r)(r + 1) entries per
+  // step spread over all threads (GB300's FP64 rate per SM sub-partition is a quarter of
+  // the SM's, so the work has to reach every warp scheduler)
+  __shared__ double2 sL[kNB_oz][kNB_oz + 1];
+  __shared__ double2 sX[kNB_oz][kNB_oz + 1];
+  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+    const int r = idx % kb, q = idx / kb;
+    sL[r][q] = Ab[(k + r) + (k + q) * n];
+    sX[r][q] = make_double2(r == q ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int r = 0; r < kb - 1; ++r) {
+    const int w = r + 1, ne = (kb - 1 - r) * w;
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+      const int srow = r + 1 + e / w, c = e % w;
+      const double2 l = sL[srow][r], x = sX[r][c];
+      double2 t = sX[srow][c];
+      t.x = fma(-l.x, x.x, fma(l.y, x.y, t.x));
+      t.y = fma(-l.x, x.y, fma(-l.y, x.x, t.y));
+      sX[srow][c] = t;
+    }
+    __syncthreads();
+  }
+  // B tile: column j of (L11^-1)^T is row j of X, K index q; four threads per column
+  if (threadIdx.x < 4 * kNB_oz) {
+    const int j = threadIdx.x >> 2, kq = threadIdx.x & 3;
+    double2 v[8];
+    int emax = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      v[q] = sX[j][8 * kq + q];
+      emax = max(emax, max(dg::biased_exp(v[q].x), dg::biased_exp(v[q].y)));
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    if (kq == 0) colexp[b * kNB_oz + j] = dg::scale_of(emax);  // 32 per matrix (rest may be smaller)
+    uint32_t pk[2][dg::kDigits7][4];
+    dg::split7(v, emax, pk);
+    unsigned char* tiles = digB + (b * kOzDigits * 2) * (int64_t)kOzBTile;  // one column tile per matrix
+    const uint32_t off = tc::kmajor_offset(j, 8 * kq, kOzK);
+#pragma unroll
+    for (int p = 0; p < kOzDigits; ++p) {
+      *reinterpret_cast<uint4*>(tiles + p * kOzBTile + off) = make_uint4(pk[0][p][0], pk[0][p][1], pk[0][p][2], pk[0][p][3]);
+      *reinterpret_cast<uint4*>(tiles + (kOzDigits + p) * kOzBTile + off) = make_uint4(pk[1][p][0], pk[1][p][1], pk[1][p][2], pk[1][p][3]);
+    }
+  }
+}
+
 // v 2^s as a double, exactly, for |v| < 2^53, built from the integer's bits (leading-zero
 // count, shift, exponent field) without the FP64 pipe.  Results below the normal range are
 // flushed to zero (they lie below 2^-1022).
@@ -170,6 +269,7 @@ constexpr int kOzThreads = 256; // two threads per output row: warps w and w + 4
 // One CTA per (row tile, group of `group` column tiles, matrix).  The A digit tiles and the
 // first B tile arrive by TMA bulk copies on one mbarrier; the B tiles are double-buffered,
 // the next one prefetched while the current tile's products and epilogue run.
+template <bool TRSM>
 __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
                                                               int64_t rest, int64_t nrt, int64_t nct,
                                                               const unsigned char* __restrict__ digA,
@@ -191,7 +291,8 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
   const int64_t rest_b = n - k - kb;
   if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_b) return;
-  const int64_t nct_b = (rest_b + kOzCols - 1) / kOzCols;
+  // TRSM: one 32-column tile, the rows of U12 (the output is U12 transposed)
+  const int64_t nct_b = TRSM ? 1 : (rest_b + kOzCols - 1) / kOzCols;
   const int ntile = (int)((nct_b - ct0) < group ? (nct_b - ct0) : group);
   unsigned char* As = osm;
   unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
@@ -224,6 +325,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   double2* Ab = A + d.offset(b);
   double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
+  double2* ucol = Ab + k + (k + kb + r) * n;         // TRSM: column k + kb + r of U12
   bool failed = false;
   int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
   for (int t = 0; t < ntile; ++t) {
@@ -263,9 +365,9 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
     for (int q = 0; q < kOzCols / 2; ++q) {
       const int64_t c = cbase + q;
-      const bool live = row_live && c < rest_b;
-      cv[q] = live ? crow[c * n] : make_double2(0.0, 0.0);
-      ce[q] = live ? colexp[b * rest + c] : 0;
+      const bool live = row_live && (TRSM ? c < kb : c < rest_b);
+      cv[q] = (live && !TRSM) ? crow[c * n] : make_double2(0.0, 0.0);
+      ce[q] = live ? colexp[TRSM ? b * kNB_oz + c : b * rest + c] : 0;  // TRSM: 32 per matrix
     }
     ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
     if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -319,14 +421,23 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
         const long long vr = hr * 256 + ((lr + (1LL << 15)) >> 16);
         const long long vi = hi * 256 + ((li + (1LL << 15)) >> 16);
         const int sc = er + ce[qq] - 46;
-        cv[qq].x -= scaled_i64(vr, sc);
-        cv[qq].y -= scaled_i64(vi, sc);
+        if (TRSM) {
+          cv[qq] = make_double2(scaled_i64(vr, sc), scaled_i64(vi, sc));
+        } else {
+          cv[qq].x -= scaled_i64(vr, sc);
+          cv[qq].y -= scaled_i64(vi, sc);
+        }
       }
     }
     if (row_live) {
 #pragma unroll
-      for (int q = 0; q < kOzCols / 2; ++q)
-        if (cbase + q < rest_b) crow[(cbase + q) * n] = cv[q];
+      for (int q = 0; q < kOzCols / 2; ++q) {
+        if (TRSM) {
+          if (cbase + q < kb) ucol[cbase + q] = cv[q];
+        } else {
+          if (cbase + q < rest_b) crow[(cbase + q) * n] = cv[q];
+        }
+      }
     }
     // every TMEM read of this tile is done before the next tile's products overwrite it
     tc::fence_before_sync();
@@ -370,13 +481,36 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   MH_LAUNCH(lc, st, "lu_ozaki_split",
             ozaki_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nrt, nct, row_ctas, digA, digB, rowexp, colexp));
   const size_t smem = kOzABytes + 2 * kOzBBytes;
-  cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int group = lc.tile(d.n).oz_group;
   group = group < 1 ? 1 : (group > kOzGroupMax ? kOzGroupMax : group);
   dim3 gg((unsigned)nrt, (unsigned)((nct + group - 1) / group), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_ozaki",
-            ozaki_gemm_kernel<<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp,
-                                                          timeout_flag, group));
+            ozaki_gemm_kernel<false><<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp,
+                                                                 colexp, timeout_flag, group));
+}
+
+void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,
+                int* timeout_flag) {
+  const int kb = kNB_oz;
+  const int64_t rest = d.n - k - kb;
+  if (rest <= 0) return;
+  const int64_t nrt = (rest + kOzRows - 1) / kOzRows, nct = 1;
+  const int64_t nrt_max = (d.n + kOzRows - 1) / kOzRows, nct_max = (d.n + kOzCols - 1) / kOzCols;
+  unsigned char* digA = static_cast<unsigned char*>(ws);
+  unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
+  int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
+  int* colexp = rowexp + d.batch * d.n;
+  const int64_t row_ctas = (nrt * kOzRows * 4 + 255) / 256;
+  dim3 gs((unsigned)(row_ctas + 1), (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_trsm_ozaki_prep",
+            ozaki_trsm_prep_kernel<<<gs, 256, 0, st>>>(d, A, k, rest, nrt, row_ctas, digA, digB, rowexp, colexp));
+  const size_t smem = kOzABytes + 2 * kOzBBytes;
+  cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 gg((unsigned)nrt, 1u, (unsigned)d.batch);
+  MH_LAUNCH(lc, st, "lu_trsm_ozaki",
+            ozaki_gemm_kernel<true><<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp,
+                                                                colexp, timeout_flag, 1));
 }
 
 }  // namespace mh
