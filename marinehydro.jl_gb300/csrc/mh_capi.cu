@@ -346,6 +346,32 @@ int solve_core(mh_context* ctx, const BatchDesc& d, double2* Adev, double2* X, i
   return check_pivots(ctx, d, 0);
 }
 
+// FP64 factorization with the tensor-core update of matrices that carry their right-hand
+// sides as d.extra appended columns: after the factorization those columns hold L^-1 P b, and
+// the upper triangular solve overwrites them with the solution.
+int solve_core_appended(mh_context* ctx, const BatchDesc& d, double2* Adev) {
+  const int64_t n = d.n;
+  int32_t *ipiv, *info;
+  MH_TRY(ws_get_t(ctx, kSlotIpiv, (size_t)(n * d.batch), &ipiv));
+  MH_TRY(ws_get_t(ctx, kSlotInfo, (size_t)d.batch, &info));
+  unsigned char* ws;
+  const size_t wsb = ozaki_workspace_bytes(n, d.batch, d.extra);
+  MH_TRY(ws_get_t(ctx, kSlotOzaki, wsb + 256, &ws));
+  int* flag = reinterpret_cast<int*>(ws + wsb);
+  MH_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+  if (lu_factor_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, info, ws, flag) != 0)
+    return fail(ctx, MH_ERR_UNSUPPORTED, "appended right-hand sides need the uniform tensor-core FP64 factorization");
+  MH_TRY(check_launch(ctx, "lu factor (tensor-core update, appended right-hand sides)"));
+  lu_solve_batched<double>(ctx->stream, ctx->lc(), d, Adev, ipiv, Adev + (size_t)n * (size_t)n, d.extra, d.stride,
+                           false, true);
+  MH_TRY(check_launch(ctx, "upper triangular solve"));
+  int hflag = 0;
+  MH_CUDA(ctx, cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MH_TRY(sync(ctx, "tensor-core update"));
+  if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the LU update gave up");
+  return check_pivots(ctx, d, 0);
+}
+
 }  // namespace capi
 }  // namespace mh
 
@@ -728,18 +754,23 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
     MH_TRY(compute_static(ctx, m, gfs, direct, 1, nullptr, SR, DR));
   }
 
+  // FP64 with the tensor-core update: the right-hand sides ride along as appended columns of
+  // D (and S keeps the same stride), so the factorization performs the forward substitution
+  const bool appended = precision == MH_PREC_FP64_TC;
+  const size_t mstride = nn + (appended ? (size_t)n * (size_t)nrhs : 0);
+
   // chunk the frequencies by memory
   size_t free_b = 0, total_b = 0;
   MH_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
-  size_t per_w = nn * sizeof(double2) * 2 + (size_t)n * nrhs * sizeof(double2) * 4;
+  size_t per_w = mstride * sizeof(double2) * 2 + (size_t)n * nrhs * sizeof(double2) * 4;
   if (precision == MH_PREC_MIXED) per_w += nn * sizeof(float2);
   size_t budget = std::min<size_t>(free_b / 2, (size_t)48 << 30);
   int64_t chunk = (int64_t)std::max<size_t>(1, budget / per_w);
   chunk = std::min<int64_t>(chunk, n_omega);
 
   double2 *S, *D, *B, *X, *work, *F, *FK;
-  MH_TRY(ws_get_t(ctx, kSlotS, nn * chunk, &S));
-  MH_TRY(ws_get_t(ctx, kSlotD, nn * chunk, &D));
+  MH_TRY(ws_get_t(ctx, kSlotS, mstride * chunk, &S));
+  MH_TRY(ws_get_t(ctx, kSlotD, mstride * chunk, &D));
   MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)(n * nrhs * chunk), &B));
   MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(n * nrhs * chunk), &X));
   MH_TRY(ws_get_t(ctx, kSlotF, (size_t)(n_omega * std::max<int64_t>(n_inf, 1) * nrhs), &F));
@@ -758,7 +789,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
 
   for (int64_t w0 = 0; w0 < n_omega; w0 += chunk) {
     const int64_t nw = std::min<int64_t>(chunk, n_omega - w0);
-    launch_assemble_wave(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)nn,
+    launch_assemble_wave(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)mstride,
                          st ? 0 : 1);
     MH_TRY(check_launch(ctx, "wave assembly"));
     if (judging) {
@@ -766,7 +797,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
       // relative error exceeds the tolerance is assembled again with the exact term
       MH_TRY(check_surrogate(ctx, p));
       MH_CUDA(ctx, cudaMemsetAsync(judge_acc, 0, sizeof(double) * 2 * nw, ctx->stream));
-      launch_surrogate_judge(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)nn,
+      launch_surrogate_judge(ctx->stream, ctx->lc(), p, SR, DR, (int)nw, ks_all + w0, S, D, (int64_t)mstride,
                              ctx->judge_samples, ctx->judge_seed, w0, st ? 0 : 1, judge_acc);
       MH_TRY(check_launch(ctx, "surrogate judge"));
       std::vector<double> hacc((size_t)(2 * nw));
@@ -780,8 +811,8 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
         ctx->judge_err[(size_t)(w0 + b)] = err;
         if (!(err <= ctx->judge_tol)) {
           ctx->judge_rerun[(size_t)(w0 + b)] = 1;
-          launch_assemble_wave(ctx->stream, ctx->lc(), pe, SR, DR, 1, ks_all + w0 + b, S + b * nn, D + b * nn,
-                               (int64_t)nn, st ? 0 : 1);
+          launch_assemble_wave(ctx->stream, ctx->lc(), pe, SR, DR, 1, ks_all + w0 + b, S + b * mstride,
+                               D + b * mstride, (int64_t)mstride, st ? 0 : 1);
         }
       }
       MH_TRY(check_launch(ctx, "exact re-assembly"));
@@ -790,7 +821,7 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
     launch_build_rhs(ctx->stream, ctx->lc(), eg, (int)nw, om_d + w0, g, (int)n_rad, rad_d, (int)n_beta, beta_d, B,
                      bstride);
     MH_TRY(check_launch(ctx, "boundary conditions"));
-    BatchDesc d{n, nw, (int64_t)nn};
+    BatchDesc d{n, nw, (int64_t)mstride};
     MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, nw), &work));
     // S times a block of vectors: FP64 FMAs in the plain path, the FP64-accurate tensor-core
     // product in the others
@@ -810,7 +841,27 @@ int mh_hydrodynamic_coefficients(mh_context* ctx, mh_mesh* m, int64_t n_omega, c
       if (hflag) return fail(ctx, MH_ERR_TIMEOUT, "a tensor-core completion wait of the S product gave up");
       return MH_OK;
     };
-    if (direct) {
+    if (appended) {
+      // right-hand sides (S b, or b for the sources) into the appended columns, factor, solve
+      // U x = y in place, and the solution back to X
+      const double2* rhs = B;
+      if (direct) {
+        MH_TRY(s_times(B, X));
+        rhs = X;
+      }
+      MH_CUDA(ctx, cudaMemcpy2DAsync(D + nn, mstride * sizeof(double2), rhs, bstride * sizeof(double2),
+                                     bstride * sizeof(double2), (size_t)nw, cudaMemcpyDeviceToDevice, ctx->stream));
+      BatchDesc da = d;
+      da.extra = nrhs;
+      MH_TRY(solve_core_appended(ctx, da, D));
+      MH_CUDA(ctx, cudaMemcpy2DAsync(X, bstride * sizeof(double2), D + nn, mstride * sizeof(double2),
+                                     bstride * sizeof(double2), (size_t)nw, cudaMemcpyDeviceToDevice, ctx->stream));
+      if (!direct) {
+        MH_TRY(ws_get_t(ctx, kSlotWork, zgemm_work_elems(n, nrhs, nw), &work));
+        MH_TRY(s_times(X, B));
+        std::swap(B, X);
+      }
+    } else if (direct) {
       MH_TRY(s_times(B, X));
       MH_TRY(solve_core(ctx, d, D, X, nrhs, bstride, precision, false));
     } else {

@@ -165,6 +165,13 @@ struct BatchDesc {
   const int64_t* orders = nullptr;
   const int64_t* offsets = nullptr;
   const int64_t* xoffsets = nullptr;
+  // Columns stored after each matrix's n columns (same leading dimension n) that the
+  // factorization carries along: right-hand sides appended to the matrix receive the row
+  // interchanges and the elimination, so that after lu_factor_batched they hold L^-1 P b and
+  // only the upper triangular solve remains.  Uniform batches with the tensor-core FP64
+  // update only (the trailing update is rectangular, n - k - kb rows by n + extra - k - kb
+  // columns); 0 otherwise.
+  int64_t extra = 0;
   __device__ __forceinline__ int64_t order(int64_t b) const { return orders ? orders[b] : n; }
   __device__ __forceinline__ int64_t offset(int64_t b) const { return offsets ? offsets[b] : b * stride; }
   __device__ __forceinline__ int64_t xoffset(int64_t b, int64_t xstride) const {
@@ -180,7 +187,7 @@ void fill_random_matrices(cudaStream_t st, LaunchCounter lc, const BatchDesc& d,
                           uint64_t seed);
 // FP64 trailing update A22 -= L21 U12 of panel step k on the BF16 tensor cores (mh_ozaki.cu);
 // emu_ws: ozaki_workspace_bytes(n, batch) bytes; *timeout_flag set if a completion wait gave up
-size_t ozaki_workspace_bytes(int64_t n, int64_t batch);
+size_t ozaki_workspace_bytes(int64_t n, int64_t batch, int64_t extra = 0);
 // FP32 trailing update of the mixed-precision factors on the BF16 tensor cores, three-way
 // split (mh_bf16x3.cu); ws: bx3_workspace_bytes(n, batch) bytes
 size_t bx3_workspace_bytes(int64_t n, int64_t batch);
@@ -192,10 +199,12 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
 // tensor cores (mh_ozaki.cu); same workspace as the trailing update
 void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,
                 int* timeout_flag);
+// upper_only: X already holds L^-1 P b (right-hand sides carried through the factorization,
+// BatchDesc::extra): only U x = y is solved, without the interchanges
 template <typename T>
 void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
                       const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,
-                      bool adjoint);
+                      bool adjoint, bool upper_only = false);
 // Y_b = A_b X_b (n x n times n x nrhs), batched, FP64; partial sums in `work`
 void zgemm_nn_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const double2* A, const double2* X,
                       int64_t nrhs, int64_t xstride, double2* Y, double2* work);

@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) laswp_kernel(BatchDesc d, typename cplx_t
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int d0 = s_dst[lane], s0 = s_src[lane], d1 = s_dst[lane + 32], s1 = s_src[lane + 32];
   C* A = Aall + d.offset(bmat);
-  const int64_t nout = n - kb;
+  const int64_t nout = n + d.extra - kb;  // columns outside the panel, appended right-hand sides included
   const int64_t q0 = blockIdx.x * (int64_t)kSwpCols;
   const int64_t q1 = (q0 + kSwpCols < nout) ? q0 + kSwpCols : nout;
   for (int64_t q = q0 + warp; q < q1; q += 8) {
@@ -389,17 +389,18 @@ __global__ void __launch_bounds__(128) trsm_kernel(BatchDesc d, typename cplx_t<
                                                    int64_t k) {
   using C = typename cplx_t<T>::type;
   __shared__ C sL[kNB][kNB + 1];
-  const int64_t n = d.order(blockIdx.y);
-  if (k + kNB >= n) return;  // nothing right of this matrix's panel (grouped batches)
+  const int64_t n = d.order(blockIdx.y), ncols = n + d.extra;
+  if (k >= n) return;  // this matrix is factored (grouped batches)
   C* A = Aall + d.offset(blockIdx.y);
   const int kb = (int)((k + kNB < n) ? kNB : n - k);
+  if (k + kb >= ncols) return;  // nothing right of the panel
   for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
     int r = idx % kb, q = idx / kb;
     sL[r][q] = A[(k + r) + (k + q) * n];
   }
   __syncthreads();
   const int64_t c = k + kb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= n) return;
+  if (c >= ncols) return;
   C x[kNB];
 #pragma unroll
   for (int r = 0; r < kNB; ++r) x[r] = (r < kb) ? A[(k + r) + c * n] : czero<C>();
@@ -665,7 +666,7 @@ template <typename T, bool ADJ>
 __global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
                                                     const int32_t* __restrict__ ipiv_all,
                                                     typename cplx_t<T>::type* __restrict__ Xall, int64_t nrhs,
-                                                    int64_t xstride, int group) {
+                                                    int64_t xstride, int group, int upper_only) {
   using C = typename cplx_t<T>::type;
   extern __shared__ unsigned char smem_raw[];
   C* blk = reinterpret_cast<C*>(smem_raw);
@@ -683,7 +684,7 @@ __global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename 
   }
   __syncthreads();
   if (!ADJ) {
-    if (tid < g) {  // apply the row interchanges in order (zgetrs / zlaswp)
+    if (tid < g && !upper_only) {  // apply the row interchanges in order (zgetrs / zlaswp)
       C* x = xs + tid * n;
       for (int64_t j = 0; j < n; ++j) {
         int64_t p = ipiv[j];
@@ -692,7 +693,7 @@ __global__ void __launch_bounds__(512) solve_kernel(BatchDesc d, const typename 
     }
     __syncthreads();
     // L y = b
-    for (int64_t jb = 0; jb < n; jb += 32) {
+    for (int64_t jb = 0; jb < (upper_only ? 0 : n); jb += 32) {
       const int64_t je = (jb + 32 < n) ? jb + 32 : n;
       load_diag_block(LU, n, jb, (int)(je - jb), blk);
       __syncthreads();
@@ -865,7 +866,7 @@ template <typename T, bool ADJ>
 __global__ void __launch_bounds__(512) solve_cluster_kernel(BatchDesc d, const typename cplx_t<T>::type* __restrict__ LUall,
                                                             const int32_t* __restrict__ ipiv_all,
                                                             typename cplx_t<T>::type* __restrict__ Xall, int64_t nrhs,
-                                                            int64_t xstride, int group, int ln) {
+                                                            int64_t xstride, int group, int ln, int upper_only) {
   using C = typename cplx_t<T>::type;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -886,10 +887,11 @@ __global__ void __launch_bounds__(512) solve_cluster_kernel(BatchDesc d, const t
   const int64_t r0 = blockIdx.y * (int64_t)group;
   const int g = (int)((r0 + group <= nrhs) ? group : nrhs - r0);
   const int tid = threadIdx.x;
-  // sigma: the row interchanges composed in order (x = b[sigma] applies them to b)
-  for (int64_t i = tid; i < n; i += blockDim.x) { sig[i] = (int)i; spv[i] = ipiv[i]; }
+  // sigma: the row interchanges composed in order (x = b[sigma] applies them to b); the
+  // identity when the right-hand sides went through the factorization (upper_only)
+  for (int64_t i = tid; i < n; i += blockDim.x) { sig[i] = (int)i; spv[i] = upper_only ? (int)i : ipiv[i]; }
   __syncthreads();
-  if (tid == 0)
+  if (tid == 0 && !upper_only)
     for (int64_t j = 0; j < n; ++j) {
       const int p = spv[j];
       if (p != j) { const int t = sig[j]; sig[j] = sig[p]; sig[p] = t; }
@@ -904,12 +906,13 @@ __global__ void __launch_bounds__(512) solve_cluster_kernel(BatchDesc d, const t
   }
   __syncthreads();
   const int nsteps = 2 * nblk;
+  const int s0 = upper_only ? nblk : 0;  // upper_only: the U steps alone
   int kind, bI;
-  solve_step<ADJ>(0, nblk, kind, bI);
-  if (bI % P == rank) cluster_solve_block<C, ADJ>(LU, n, kind, bI, P, g, ln, xl, blk, rd, pub[0]);
+  solve_step<ADJ>(s0, nblk, kind, bI);
+  if (bI % P == rank) cluster_solve_block<C, ADJ>(LU, n, kind, bI, P, g, ln, xl, blk, rd, pub[s0 & 1]);
   cluster_arrive();
   cluster_wait();
-  for (int s = 0; s < nsteps; ++s) {
+  for (int s = s0; s < nsteps; ++s) {
     solve_step<ADJ>(s, nblk, kind, bI);
     const int bw = (int)(((int64_t)bI * 32 + 32 < n) ? 32 : n - (int64_t)bI * 32);
     C* xs = xb[s & 1];
@@ -1140,6 +1143,8 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
                       int32_t* ipiv, int32_t* info, void* emu_ws, int* emu_flag) {
   const int64_t n = d.n;
   if (n <= 0 || d.batch <= 0) return 0;
+  // appended right-hand sides need the rectangular trailing update of the FP64 tensor-core path
+  if (d.extra > 0 && (sizeof(T) != 8 || !emu_ws || d.orders)) return -1;
   cudaMemsetAsync(info, 0, sizeof(int32_t) * d.batch, st);
   {
     constexpr int TM = GemmTile<T>::TM;
@@ -1172,13 +1177,14 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
       MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
                 panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
     }
-    if (n - kb > 0) {
-      dim3 sg((unsigned)((n - kb + kSwpCols - 1) / kSwpCols), (unsigned)d.batch);
+    if (n + d.extra - kb > 0) {
+      dim3 sg((unsigned)((n + d.extra - kb + kSwpCols - 1) / kSwpCols), (unsigned)d.batch);
       MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_laswp_f64" : "lu_laswp_f32",
                 laswp_kernel<T><<<sg, 256, 0, st>>>(d, A, ipiv, k, (int)kb));
     }
-    const int64_t rest = n - k - kb;
-    if (rest <= 0) continue;
+    const int64_t rest = n - k - kb;              // trailing rows
+    const int64_t rest_c = n + d.extra - k - kb;  // columns right of the panel
+    if (rest_c <= 0) continue;
     bool trsm_done = false;
     if constexpr (sizeof(T) == 8) {  // FP64 with the tensor-core update: U12 on the tensor cores too
       if (emu_ws && kb == kNB) {
@@ -1187,9 +1193,10 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
       }
     }
     if (!trsm_done) {
-      dim3 tg((unsigned)((rest + 127) / 128), (unsigned)d.batch);
+      dim3 tg((unsigned)((rest_c + 127) / 128), (unsigned)d.batch);
       MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_trsm_f64" : "lu_trsm_f32", trsm_kernel<T><<<tg, 128, 0, st>>>(d, A, k));
     }
+    if (rest <= 0) continue;
     if (emu_ws) {
       if constexpr (sizeof(T) == 8) {  // FP64 update on the BF16 tensor cores (mh_ozaki.cu)
         ozaki_trailing_update(st, lc, d, A, k, (int)kb, emu_ws, emu_flag);
@@ -1216,7 +1223,8 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
 // Returns false when even 8 CTAs cannot hold the vectors (the one-CTA kernel then runs).
 template <typename T>
 bool solve_on_cluster(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
-                      const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride, bool adjoint) {
+                      const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride, bool adjoint,
+                      bool upper_only) {
   using C = typename cplx_t<T>::type;
   const int64_t n = d.n;
   const int g = (int)(nrhs < kSG ? nrhs : kSG);
@@ -1265,8 +1273,8 @@ bool solve_on_cluster(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   cudaLaunchConfig_t cfg = make_cfg(P, attr);
   const int ln = (int)((nblk + P - 1) / P * 32);
   lc.pre(st);
-  if (adjoint) cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, true>, d, LU, ipiv, X, nrhs, xstride, g, ln);
-  else cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, false>, d, LU, ipiv, X, nrhs, xstride, g, ln);
+  if (adjoint) cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, true>, d, LU, ipiv, X, nrhs, xstride, g, ln, 0);
+  else cudaLaunchKernelEx(&cfg, solve_cluster_kernel<T, false>, d, LU, ipiv, X, nrhs, xstride, g, ln, (int)upper_only);
   lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
   return true;
 }
@@ -1274,11 +1282,12 @@ bool solve_on_cluster(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
 template <typename T>
 void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, const typename cplx_t<T>::type* LU,
                       const int32_t* ipiv, typename cplx_t<T>::type* X, int64_t nrhs, int64_t xstride,
-                      bool adjoint) {
+                      bool adjoint, bool upper_only) {
   using C = typename cplx_t<T>::type;
   const int64_t n = d.n;
   if (n <= 0 || nrhs <= 0 || d.batch <= 0) return;
-  if (solve_on_cluster<T>(st, lc, d, LU, ipiv, X, nrhs, xstride, adjoint)) return;
+  upper_only = upper_only && !adjoint;
+  if (solve_on_cluster<T>(st, lc, d, LU, ipiv, X, nrhs, xstride, adjoint, upper_only)) return;
   const size_t max_smem = 200 * 1024;
   const size_t blk_bytes = sizeof(C) * 32 * 33;
   int64_t group = (int64_t)((max_smem - blk_bytes) / (sizeof(C) * n));
@@ -1298,10 +1307,10 @@ void lu_solve_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, con
   lc.pre(st);
   if (adjoint) {
     cudaFuncSetAttribute(solve_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
-    solve_kernel<T, true><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+    solve_kernel<T, true><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group, 0);
   } else {
     cudaFuncSetAttribute(solve_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
-    solve_kernel<T, false><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group);
+    solve_kernel<T, false><<<grid, 512, smem, st>>>(d, LU, ipiv, X, nrhs, xstride, (int)group, (int)upper_only);
   }
   lc.post(st, sizeof(T) == 8 ? "lu_solve_f64" : "lu_solve_f32");
 }
@@ -1339,9 +1348,9 @@ template int lu_factor_batched<double>(cudaStream_t, LaunchCounter, const BatchD
 template int lu_factor_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, float2*, int32_t*, int32_t*,
                                       void*, int*);
 template void lu_solve_batched<double>(cudaStream_t, LaunchCounter, const BatchDesc&, const double2*,
-                                       const int32_t*, double2*, int64_t, int64_t, bool);
+                                       const int32_t*, double2*, int64_t, int64_t, bool, bool);
 template void lu_solve_batched<float>(cudaStream_t, LaunchCounter, const BatchDesc&, const float2*, const int32_t*,
-                                      float2*, int64_t, int64_t, bool);
+                                      float2*, int64_t, int64_t, bool, bool);
 
 size_t zgemm_work_elems(int64_t n, int64_t nrhs, int64_t batch) {
   const size_t fp64 = (size_t)gemm_split(n, batch) * (size_t)batch * (size_t)nrhs * (size_t)n;

@@ -114,7 +114,7 @@ __device__ __forceinline__ void ozaki_split_cols(int64_t bx, const BatchDesc& d,
   const int64_t n = d.order(b);
   if (k + kNB_oz >= n) return;
   kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
-  const int64_t rest_b = n - k - kb;
+  const int64_t rest_b = n + d.extra - k - kb;  // columns of U12 (appended right-hand sides included)
   const double2* Ab = A + d.offset(b);
   const bool live = c < rest_b;
   double2 v[8];
@@ -167,9 +167,10 @@ __global__ void __launch_bounds__(256) ozaki_trsm_prep_kernel(BatchDesc d, const
                                                               int* __restrict__ colexp) {
   const int64_t b = blockIdx.y;
   const int64_t n = d.order(b);
-  if (k + kNB_oz >= n) return;  // no U12 for this matrix
+  if (k + kNB_oz > n) return;  // no full panel at this step
   const int kb = kNB_oz;
-  const int64_t rest_b = n - k - kb;
+  const int64_t rest_b = n + d.extra - k - kb;  // columns of A12 (appended right-hand sides included)
+  if (rest_b <= 0) return;
   const double2* Ab = A + d.offset(b);
   if ((int64_t)blockIdx.x < row_ctas) {
     // column c of A12 (rows k .. k+31) as row c of the A operand; four threads per column
@@ -287,12 +288,15 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   // a grouped batch: this matrix's panel width and trailing size; CTAs past its trailing
   // block leave before any barrier or tensor-memory allocation
   const int64_t n = d.order(b);
-  if (k + kNB_oz >= n) return;
+  if (TRSM ? k + kNB_oz > n : k + kNB_oz >= n) return;
   kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
-  const int64_t rest_b = n - k - kb;
-  if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_b) return;
+  // output rows: trailing rows of A22, or (TRSM) the columns of A12; output columns: the
+  // columns of A22 right of the panel (appended right-hand sides included), or the 32 rows of U12
+  const int64_t rest_b = TRSM ? n + d.extra - k - kb : n - k - kb;
+  const int64_t rest_cb = TRSM ? kb : n + d.extra - k - kb;
+  if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_cb) return;
   // TRSM: one 32-column tile, the rows of U12 (the output is U12 transposed)
-  const int64_t nct_b = TRSM ? 1 : (rest_b + kOzCols - 1) / kOzCols;
+  const int64_t nct_b = TRSM ? 1 : (rest_cb + kOzCols - 1) / kOzCols;
   const int ntile = (int)((nct_b - ct0) < group ? (nct_b - ct0) : group);
   unsigned char* As = osm;
   unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
@@ -365,7 +369,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
     for (int q = 0; q < kOzCols / 2; ++q) {
       const int64_t c = cbase + q;
-      const bool live = row_live && (TRSM ? c < kb : c < rest_b);
+      const bool live = row_live && c < rest_cb;
       cv[q] = (live && !TRSM) ? crow[c * n] : make_double2(0.0, 0.0);
       ce[q] = live ? colexp[TRSM ? b * kNB_oz + c : b * rest + c] : 0;  // TRSM: 32 per matrix
     }
@@ -433,9 +437,9 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 #pragma unroll
       for (int q = 0; q < kOzCols / 2; ++q) {
         if (TRSM) {
-          if (cbase + q < kb) ucol[cbase + q] = cv[q];
+          if (cbase + q < rest_cb) ucol[cbase + q] = cv[q];
         } else {
-          if (cbase + q < rest_b) crow[(cbase + q) * n] = cv[q];
+          if (cbase + q < rest_cb) crow[(cbase + q) * n] = cv[q];
         }
       }
     }
@@ -461,21 +465,27 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 
 }  // namespace
 
-size_t ozaki_workspace_bytes(int64_t n, int64_t batch) {
-  const int64_t t = (n + kOzRows - 1) / kOzRows, c = (n + kOzCols - 1) / kOzCols;
-  return (size_t)batch * ((size_t)t * kOzABytes + (size_t)c * kOzBBytes + 2 * sizeof(int) * (size_t)n) + 1024;
+// workspace layout per batch: A digit tiles (row tiles of the widest operand), B digit tiles,
+// row and column exponents (stride n + extra per matrix)
+static int64_t oz_row_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzRows - 1) / kOzRows; }
+static int64_t oz_col_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzCols - 1) / kOzCols; }
+
+size_t ozaki_workspace_bytes(int64_t n, int64_t batch, int64_t extra) {
+  const int64_t w = n + extra;
+  const int64_t t = (w + kOzRows - 1) / kOzRows, c = (w + kOzCols - 1) / kOzCols;
+  return (size_t)batch * ((size_t)t * kOzABytes + (size_t)c * kOzBBytes + 2 * sizeof(int) * (size_t)w) + 1024;
 }
 
 void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
                            void* ws, int* timeout_flag) {
-  const int64_t rest = d.n - k - kb;
-  if (rest <= 0) return;
-  const int64_t nrt = (rest + kOzRows - 1) / kOzRows, nct = (rest + kOzCols - 1) / kOzCols;
-  const int64_t nrt_max = (d.n + kOzRows - 1) / kOzRows, nct_max = (d.n + kOzCols - 1) / kOzCols;
+  const int64_t rows = d.n - k - kb;           // trailing rows
+  const int64_t rest = d.n + d.extra - k - kb;  // trailing columns: the exponent arrays' stride
+  if (rows <= 0) return;
+  const int64_t nrt = (rows + kOzRows - 1) / kOzRows, nct = (rest + kOzCols - 1) / kOzCols;
   unsigned char* digA = static_cast<unsigned char*>(ws);
-  unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
-  int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
-  int* colexp = rowexp + d.batch * d.n;
+  unsigned char* digB = digA + d.batch * oz_row_tiles(d) * (int64_t)kOzABytes;
+  int* rowexp = reinterpret_cast<int*>(digB + d.batch * oz_col_tiles(d) * (int64_t)kOzBBytes);
+  int* colexp = rowexp + d.batch * (d.n + d.extra);
   const int64_t row_ctas = (nrt * kOzRows * 4 + 255) / 256, col_ctas = (nct * kOzCols * 4 + 255) / 256;
   dim3 gs((unsigned)(row_ctas + col_ctas), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_ozaki_split",
@@ -493,14 +503,13 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
 void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,
                 int* timeout_flag) {
   const int kb = kNB_oz;
-  const int64_t rest = d.n - k - kb;
+  const int64_t rest = d.n + d.extra - k - kb;  // columns of A12 (appended right-hand sides included)
   if (rest <= 0) return;
   const int64_t nrt = (rest + kOzRows - 1) / kOzRows, nct = 1;
-  const int64_t nrt_max = (d.n + kOzRows - 1) / kOzRows, nct_max = (d.n + kOzCols - 1) / kOzCols;
   unsigned char* digA = static_cast<unsigned char*>(ws);
-  unsigned char* digB = digA + d.batch * nrt_max * (int64_t)kOzABytes;
-  int* rowexp = reinterpret_cast<int*>(digB + d.batch * nct_max * (int64_t)kOzBBytes);
-  int* colexp = rowexp + d.batch * d.n;
+  unsigned char* digB = digA + d.batch * oz_row_tiles(d) * (int64_t)kOzABytes;
+  int* rowexp = reinterpret_cast<int*>(digB + d.batch * oz_col_tiles(d) * (int64_t)kOzBBytes);
+  int* colexp = rowexp + d.batch * (d.n + d.extra);
   const int64_t row_ctas = (nrt * kOzRows * 4 + 255) / 256;
   dim3 gs((unsigned)(row_ctas + 1), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_trsm_ozaki_prep",
