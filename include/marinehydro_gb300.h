@@ -416,6 +416,9 @@ int mh_bessel01_points(mh_context* ctx, int64_t m, const double* x, double* out,
 int mh_set_quadrature_tolerance(mh_context* ctx, double rtol, double atol);
 
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* exp(-|x|), log|x|, 1/|x| and sqrt|x| for each x as the Wu kernels evaluate them in 64-bit
+   fixed point on the integer pipe: m x 4 values, `out` row-major (4 per point). */
+int mh_fixpoint_points(mh_context* ctx, int64_t m, const double* x, double* out, int mem);
 /* Per-kernel-group device timing with CUDA events on the launching stream.
    mh_profile_read fills up to `capacity` groups: names (32 chars each, NUL
    padded), total milliseconds and launch counts; *n_groups = groups recorded. */

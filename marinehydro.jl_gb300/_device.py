@@ -155,6 +155,15 @@ def wu_wave_terms(ctx, hh, vv):
     return out
 
 
+def fixpoint_points(ctx, x):
+    """exp(-|x|), log|x|, 1/|x|, sqrt|x| as the Wu kernels evaluate them on the integer pipe (m x 4)."""
+    x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+    out = np.empty((x.size, 4), dtype=np.float64)
+    ctx.check(ctx._L.mh_fixpoint_points(ctx.handle, x.size, x.ctypes.data, out.ctypes.data, MH_MEM_HOST),
+              "fixed-point points")
+    return out
+
+
 def bessel01_points(ctx, x):
     """J0, J1, Y0, Y1 as the Wu kernels evaluate them (m x 4; Y is NaN below x = 3)."""
     x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())

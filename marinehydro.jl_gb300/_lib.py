@@ -38,7 +38,7 @@ EXPORTS = (
     "mh_abi_version", "mh_create", "mh_destroy", "mh_last_error", "mh_get_stream", "mh_set_stream",
     "mh_synchronize", "mh_launch_count", "mh_workspace_bytes", "mh_mesh_create", "mh_mesh_destroy",
     "mh_mesh_panels", "mh_mesh_set_lid", "mh_assemble_matrices", "mh_linsolve", "mh_solve", "mh_linsolve_adjoint",
-    "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_bessel01_points", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
+    "mh_hydrodynamic_coefficients", "mh_wu_wave_terms", "mh_bessel01_points", "mh_fixpoint_points", "mh_exact_wave_terms", "mh_set_quadrature_tolerance",
     "mh_profile_enable", "mh_profile_reset", "mh_profile_read", "mh_probe_fma_peaks",
     "mh_assemble_matrices_noalloc", "mh_batch_hydrodynamic_coefficients", "mh_batch_release",
     "mh_hydro_gradient", "mh_surrogate_param_count", "mh_surrogate_train", "mh_surrogate_set",
@@ -98,6 +98,7 @@ def load(path: str | None = None):
                                                    I, vp, vp, vp, vp, vp, I]
         L.mh_wu_wave_terms.argtypes = [vp, i64, vp, vp, vp, I]
         L.mh_bessel01_points.argtypes = [vp, i64, vp, vp, I]
+        L.mh_fixpoint_points.argtypes = [vp, i64, vp, vp, I]
         L.mh_exact_wave_terms.argtypes = [vp, i64, vp, vp, D, D, vp, I]
         L.mh_set_quadrature_tolerance.argtypes = [vp, D, D]
         L.mh_profile_enable.argtypes = [vp, I]

@@ -714,6 +714,16 @@ __global__ void wu_points_kernel(int64_t m, const double* __restrict__ hh, const
   out[3 * q + 2] = c;
 }
 
+__global__ void fixpoint_points_kernel(int64_t m, const double* __restrict__ x, double* __restrict__ out) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const double a = fabs(x[q]);
+  out[4 * q] = fx::exp_nonpos(-a);
+  out[4 * q + 1] = fx::log_pos(a);
+  out[4 * q + 2] = fx::recip(a);
+  out[4 * q + 3] = fx::sqrt_pos(a);
+}
+
 __global__ void bessel01_points_kernel(int64_t m, const double* __restrict__ x, double* __restrict__ out) {
   int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= m) return;
@@ -909,6 +919,10 @@ void launch_surrogate_judge(cudaStream_t st, LaunchCounter lc, const AssemblyPar
     MH_LAUNCH(lc, st, "surrogate_judge",
               surrogate_judge_kernel<false><<<g, 32 * kExactWarps, 0, st>>>(p, SR, DR, ks_dev, S, D, sstride, n_samples,
                                                                           seed, first_matrix, wave_identity, acc));
+}
+
+void launch_fixpoint_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out) {
+  MH_LAUNCH(lc, st, "fixpoint_points", fixpoint_points_kernel<<<(unsigned)((m + 127) / 128), 128, 0, st>>>(m, x, out));
 }
 
 void launch_bessel01_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out) {

@@ -933,6 +933,21 @@ int mh_wu_wave_terms(mh_context* ctx, int64_t m, const double* hh, const double*
   return sync(ctx, "wu wave terms");
 }
 
+int mh_fixpoint_points(mh_context* ctx, int64_t m, const double* x, double* out, int mem) {
+  if (!ctx) return MH_ERR_ARG;
+  if (m <= 0 || !x || !out) return fail(ctx, MH_ERR_ARG, "bad fixed-point arguments");
+  if (mem != MH_MEM_HOST && mem != MH_MEM_DEVICE) return fail(ctx, MH_ERR_ARG, "bad memory kind %d", mem);
+  MH_TRY(set_device(ctx));
+  double *in, *o;
+  MH_TRY(ws_get_t(ctx, kSlotIn, (size_t)m, &in));
+  MH_TRY(ws_get_t(ctx, kSlotX, (size_t)(4 * m), &o));
+  MH_TRY(copy_in(ctx, in, x, sizeof(double) * m, mem));
+  launch_fixpoint_points(ctx->stream, ctx->lc(), m, in, o);
+  MH_TRY(check_launch(ctx, "fixed-point points"));
+  MH_TRY(copy_out(ctx, out, o, sizeof(double) * 4 * m, mem));
+  return sync(ctx, "fixed-point points");
+}
+
 int mh_bessel01_points(mh_context* ctx, int64_t m, const double* x, double* out, int mem) {
   if (!ctx) return MH_ERR_ARG;
   if (m <= 0 || !x || !out) return fail(ctx, MH_ERR_ARG, "bad Bessel arguments");

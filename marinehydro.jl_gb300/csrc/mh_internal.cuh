@@ -150,6 +150,8 @@ void launch_round_bf16(cudaStream_t st, LaunchCounter lc, const float* in, float
 void launch_wu_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* hh, const double* vv, double2* out);
 // J0, J1, Y0, Y1 (NaN for Y below x = 3) at m points: out 4 doubles per point
 void launch_bessel01_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out);
+// exp(-|x|), log|x|, 1/|x|, sqrt|x| as the Wu term evaluates them on the integer pipe (mh_fixpoint.cuh)
+void launch_fixpoint_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* x, double* out);
 void launch_exact_points(cudaStream_t st, LaunchCounter lc, int64_t m, const double* r, const double* z, double rtol,
                          double atol, double2* out);
 

@@ -56,6 +56,29 @@ def test_bessel01_points(mh, ctx):
         assert np.abs(got[ok, c] - ref[ok, c]).max() < 4e-15, (c, np.abs(got[ok, c] - ref[ok, c]).max())
 
 
+def test_fixpoint_functions(mh, ctx):
+    # exp, log, reciprocal and square root of the Wu term, evaluated in 64-bit fixed point on
+    # the integer pipe, against numpy's FP64 functions: reciprocal and square root within an
+    # ulp of the correctly rounded result, exp and log within two ulps of numpy's (log: ulps
+    # of max(|log x|, 1/2), the absolute error the Wu term sees)
+    rng = np.random.default_rng(11)
+    x = np.concatenate([[1.0, 2.0, 0.5, 1 + 2.0 ** -52, 2 - 2.0 ** -52, 3.0, 7.999999999999, 8.0, 744.0, 1e-300,
+                         2.0 ** -40],
+                        rng.uniform(0, 2, 4000), 10 ** rng.uniform(-12, 2.85, 4000), 10 ** rng.uniform(-300, 300, 2000)])
+    got = mh._device.fixpoint_points(ctx, x)
+    ulp = lambda v: np.spacing(np.abs(v))
+    e = np.exp(-x)
+    ok = e > 2.3e-308  # below the normal range the integer path flushes to zero
+    assert np.all(np.abs(got[ok, 0] - e[ok]) <= 2.0 * ulp(e[ok])), np.max(np.abs(got[ok, 0] - e[ok]) / ulp(e[ok]))
+    assert np.all(np.abs(got[~ok, 0]) < 2.3e-308)
+    lg = np.log(x)
+    assert np.all(np.abs(got[:, 1] - lg) <= 2.0 * ulp(np.maximum(np.abs(lg), 0.5)))
+    r = 1.0 / x
+    assert np.all(np.abs(got[:, 2] - r) <= ulp(r))
+    q = np.sqrt(x)
+    assert np.all(np.abs(got[:, 3] - q) <= ulp(q))
+
+
 def test_wu_wave_terms(mh, oracle, ctx):
     rng = np.random.default_rng(0)
     hh = np.concatenate([[0.0, 1e-7, 2.999, 3.0, 3.001], rng.uniform(0, 20, 300), 10 ** rng.uniform(-3, 2, 200)])
