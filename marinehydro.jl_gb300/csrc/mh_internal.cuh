@@ -1,6 +1,8 @@
 // mh_internal.cuh -- shared declarations of libmarinehydro_cuda.so (not part of the C-ABI).
 #pragma once
 
+#include <cstdint>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -195,8 +197,10 @@ size_t ozaki_workspace_bytes(int64_t n, int64_t batch, int64_t extra = 0);
 size_t bx3_workspace_bytes(int64_t n, int64_t batch);
 void bx3_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, float2* A, int64_t k, int kb,
                          void* ws, int* timeout_flag);
+// kb: the panel's width (32; 16 for the update inside a two-level panel), cols: at most this
+// many columns right of the panel are updated
 void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
-                           void* ws, int* timeout_flag);
+                           void* ws, int* timeout_flag, int64_t cols = INT64_MAX);
 // U12 = L11^-1 A12 of panel step k (a full 32-column panel) as an exact-digit product on the
 // tensor cores (mh_ozaki.cu); same workspace as the trailing update
 void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,

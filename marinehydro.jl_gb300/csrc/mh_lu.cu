@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <climits>
 
+#include "mh_fixpoint.cuh"
 #include "mh_internal.cuh"
 
 namespace mh {
@@ -65,6 +66,19 @@ template <typename C> __device__ __forceinline__ C crecip(C a) {
     r.x = q / den; r.y = -1 / den;
   }
   return r;
+}
+// FP64: 1/a = conj(a) f / |a f|^2 with a scaled by a power of two f (so |a f| is near 1), the
+// reciprocal of the squared magnitude on the integer pipe (fx::recip): seven FP64 operations
+// instead of Smith's three divisions -- this is the pivot reciprocal on the panel's
+// per-column critical path, computed by one lane while the CTA waits.  Within a few ulps.
+template <> __device__ __forceinline__ double2 crecip<double2>(double2 a) {
+  const int ex = (int)((__double_as_longlong(a.x) >> 52) & 0x7FF);
+  const int ey = (int)((__double_as_longlong(a.y) >> 52) & 0x7FF);
+  const int e = ex > ey ? ex : ey;  // biased exponent of the larger part (a != 0)
+  const double f = __longlong_as_double((long long)(2046 - e) << 52);  // 2^(1023 - (e - 1023)), exact
+  const double sx = a.x * f, sy = a.y * f;
+  const double rf = fx::recip(fma(sx, sx, sy * sy)) * f;
+  return make_double2(sx * rf, -sy * rf);
 }
 template <typename C> __device__ __forceinline__ C cdiv(C a, C b) { return cmul(a, crecip(b)); }
 template <typename C> __device__ __forceinline__ C czero() { C r; r.x = 0; r.y = 0; return r; }
@@ -208,7 +222,7 @@ template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
                                                                      int32_t* __restrict__ ipiv_all,
                                                                      int32_t* __restrict__ info_all, int64_t k,
-                                                                     int chunk_cap) {
+                                                                     int chunk_cap, int width) {
   using C = typename cplx_t<T>::type;
   using K = typename PivotKey<T>::type;
   namespace cg = cooperative_groups;
@@ -230,7 +244,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_cluster_kernel(BatchDesc 
   if (k >= n) return;  // a grouped batch: this matrix is factored (the whole cluster leaves)
   C* A = Aall + d.offset(bmat);
   const int64_t m = n - k;
-  const int kb = (int)(m < kNB ? m : kNB);
+  const int kb = (int)(m < width ? m : width);  // panel width: 32, or 16 for a half of a two-level panel
   // rows per CTA for this matrix: at most the launch's capacity, at least the diagonal block
   const int chunk = (int)max((int64_t)kb, min((int64_t)chunk_cap, (m + P - 1) / P));
   const int r0 = rank * chunk;  // first panel row of this CTA
@@ -380,6 +394,66 @@ __global__ void __launch_bounds__(256) laswp_kernel(BatchDesc d, typename cplx_t
     __syncwarp();
     if (d0 >= 0) col[d0] = v0;
     if (d1 >= 0) col[d1] = v1;
+  }
+}
+
+// The interchanges of the kb panel rows at k applied to the columns [c0, c1) (the other half
+// of a two-level panel); one warp per column as in laswp_kernel.
+template <typename T>
+__global__ void __launch_bounds__(256) laswp_cols_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                        const int32_t* __restrict__ ipiv_all, int64_t k, int kb,
+                                                        int64_t c0, int64_t c1) {
+  using C = typename cplx_t<T>::type;
+  __shared__ int s_slot[32], s_content[64], s_dst[64], s_src[64];
+  const int64_t bmat = blockIdx.y, n = d.order(bmat);
+  if (k + kb > n) return;
+  if (threadIdx.x < 32) panel_permutation(ipiv_all + bmat * d.n, k, kb, s_slot, s_content, s_dst, s_src);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int d0 = s_dst[lane], s0 = s_src[lane], d1 = s_dst[lane + 32], s1 = s_src[lane + 32];
+  C* A = Aall + d.offset(bmat);
+  const int64_t q0 = c0 + blockIdx.x * (int64_t)kSwpCols;
+  const int64_t q1 = (q0 + kSwpCols < c1) ? q0 + kSwpCols : c1;
+  for (int64_t q = q0 + warp; q < q1; q += 8) {
+    C* col = A + q * n;
+    C v0 = czero<C>(), v1 = czero<C>();
+    if (d0 >= 0) v0 = col[s0];
+    if (d1 >= 0) v1 = col[s1];
+    __syncwarp();
+    if (d0 >= 0) col[d0] = v0;
+    if (d1 >= 0) col[d1] = v1;
+  }
+}
+
+// U12' = L11'^-1 A[k:k+16, k+16:k+32] of a two-level panel (L11' the unit lower 16 x 16 block of
+// the left half): the column-oriented forward substitution with the (15 - r) x 16 updates of
+// step r spread over the CTA's threads (GB300's FP64 work has to reach all four schedulers).
+template <typename T>
+__global__ void __launch_bounds__(256) trsm16_kernel(BatchDesc d, typename cplx_t<T>::type* __restrict__ Aall,
+                                                    int64_t k) {
+  using C = typename cplx_t<T>::type;
+  constexpr int H = kNB / 2;
+  __shared__ C sL[H][H + 1], sB[H][H + 1];
+  const int64_t n = d.order(blockIdx.x);
+  if (k + kNB > n) return;
+  C* A = Aall + d.offset(blockIdx.x);
+  for (int idx = threadIdx.x; idx < H * H; idx += blockDim.x) {
+    const int r = idx % H, q = idx / H;
+    sL[r][q] = A[(k + r) + (k + q) * n];
+    sB[r][q] = A[(k + r) + (k + H + q) * n];
+  }
+  __syncthreads();
+  for (int r = 0; r < H - 1; ++r) {
+    const int ne = (H - 1 - r) * H;
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+      const int srow = r + 1 + e / H, c = e % H;
+      sB[srow][c] = cfms(sB[srow][c], sL[srow][r], sB[r][c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < H * H; idx += blockDim.x) {
+    const int r = idx % H, q = idx / H;
+    A[(k + r) + (k + H + q) * n] = sB[r][q];
   }
 }
 
@@ -1098,15 +1172,19 @@ void convert_with_norms(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, c
 // launch-shape table's cluster bound); 0 when the panel does not fit the largest cluster
 // the GPU can schedule (panel_kernel then runs).
 template <typename T>
-int panel_cluster_size(int64_t m, int64_t batch, int cap_ctas) {
+int panel_cluster_size(int64_t m, int64_t batch, int cap_ctas, int width = kNB) {
   using C = typename cplx_t<T>::type;
   constexpr int cap = PanelRows<T>::value;
   struct Table { int resident[17]; };
-  static const Table tab = [] {
+  // clusters resident at once at the largest chunk: a full-width panel fills one SM's shared
+  // memory, a half-width one (two-level panels) half of it
+  auto make_table = [](int w) {
     Table t{};
-    const int smem = cap * kNB * (int)sizeof(C);
-    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // the attribute always allows the full-width panel; the query uses this width's size
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         cap * kNB * (int)sizeof(C));
     cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    const int smem = cap * w * (int)sizeof(C);
     for (int p = 1; p <= 16; ++p) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)p, 1, 1);
@@ -1127,15 +1205,62 @@ int panel_cluster_size(int64_t m, int64_t batch, int cap_ctas) {
       t.resident[p] = num;  // clusters of p CTAs resident at once, at the largest chunk
     }
     return t;
+  };
+  static const Table tab_full = make_table(kNB);
+  static const Table tab_half = make_table(kNB / 2);
+  static const int sms = [] {
+    int dev = 0, v = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v;
   }();
+  const Table& tab = width < kNB ? tab_half : tab_full;
   int64_t need = (m + cap - 1) / cap;
   if (need < 1) need = 1;
   if (need > 16 || tab.resident[need] <= 0) return 0;
   const int64_t lim = m / kNB > 1 ? m / kNB : 1;  // keeps every chunk >= 32 rows (CTA 0 holds the diagonal block)
   int64_t p = need;
+  // more CTAs per matrix while all clusters stay resident and every CTA keeps an SM of its own
+  // (the panel is FP64-bound per SM)
   for (int64_t q = need + 1; q <= 8 && q <= lim && q <= cap_ctas; ++q)
-    if (tab.resident[q] >= batch) p = q;
+    if (tab.resident[q] >= batch && q * batch <= sms) p = q;
   return (int)p;
+}
+
+// true when the full-width panel of m rows runs its clusters for all `batch` matrices at once
+// (its rows need at most as many CTAs per matrix as fit every cluster on the GPU); a panel that
+// does not fit runs in waves, and the FP64 tensor-core path factors it in two halves instead
+template <typename T>
+bool panel_fits_one_wave(int64_t m, int64_t batch) {
+  constexpr int cap = PanelRows<T>::value;
+  const int64_t need = (m + cap - 1) / cap;
+  static int resident[17] = {-1};
+  if (resident[0] < 0) {
+    using C = typename cplx_t<T>::type;
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap * kNB * (int)sizeof(C));
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int p = 1; p <= 16; ++p) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)p, 1, 1);
+      cfg.blockDim = dim3(kPanelThreads, 1, 1);
+      cfg.dynamicSmemBytes = (size_t)cap * kNB * sizeof(C);
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)p;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int num = 0;
+      if (cudaOccupancyMaxActiveClusters(&num, panel_cluster_kernel<T>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        num = 0;
+      }
+      resident[p] = num;
+    }
+    resident[0] = 0;
+  }
+  return need <= 16 && resident[need] >= batch;
 }
 
 template <typename T>
@@ -1153,29 +1278,56 @@ int lu_factor_batched(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, typ
     if (sizeof(T) == 8)
       cudaFuncSetAttribute(gemm3m_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG3Smem);
   }
+  const int cap_ctas = sizeof(T) == 8 ? lc.tile(n).cluster_f64 : lc.tile(n).cluster_f32;
+  // the panel at k0 of `width` columns on a cluster of P CTAs
+  auto cluster_panel = [&](int64_t k0, int width, int P) {
+    const int chunk = (int)((n - k0 + P - 1) / P);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)P, (unsigned)d.batch, 1);
+    cfg.blockDim = dim3(kPanelThreads, 1, 1);
+    cfg.dynamicSmemBytes = (size_t)chunk * width * sizeof(typename cplx_t<T>::type);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)P;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
+              cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, d, A, ipiv, info, k0, chunk, width));
+  };
   for (int64_t k = 0; k < n; k += kNB) {
     const int64_t kb = (k + kNB < n) ? kNB : n - k;
-    const int P = panel_cluster_size<T>(n - k, d.batch, sizeof(T) == 8 ? lc.tile(n).cluster_f64
-                                                                       : lc.tile(n).cluster_f32);
-    if (P > 0) {
-      const int chunk = (int)((n - k + P - 1) / P);
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((unsigned)P, (unsigned)d.batch, 1);
-      cfg.blockDim = dim3(kPanelThreads, 1, 1);
-      cfg.dynamicSmemBytes = (size_t)chunk * kNB * sizeof(typename cplx_t<T>::type);
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = (unsigned)P;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
-                cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, d, A, ipiv, info, k, chunk));
+    // Two-level panel (FP64 with the tensor-core update, tall panels): two 16-column halves
+    // on the CUDA cores, the left half's update of the right half (K = 16) on the tensor
+    // cores -- half the panel's FP64 work, and half its shared memory per row
+    int Pl = 0, P16 = 0;
+    if constexpr (sizeof(T) == 8) {
+      if (emu_ws && kb == kNB && !d.orders && !panel_fits_one_wave<T>(n - k, d.batch)) {
+        Pl = panel_cluster_size<T>(n - k, d.batch, cap_ctas, kNB / 2);
+        P16 = panel_cluster_size<T>(n - k - kNB / 2, d.batch, cap_ctas, kNB / 2);
+      }
+    }
+    if (Pl > 0 && P16 > 0) {
+      if constexpr (sizeof(T) == 8) {
+        const int H = kNB / 2;
+        cluster_panel(k, H, Pl);
+        dim3 sg(1u, (unsigned)d.batch);
+        MH_LAUNCH(lc, st, "lu_laswp_f64", laswp_cols_kernel<T><<<sg, 256, 0, st>>>(d, A, ipiv, k, H, k + H, k + kNB));
+        MH_LAUNCH(lc, st, "lu_trsm16_f64", trsm16_kernel<T><<<(unsigned)d.batch, 256, 0, st>>>(d, A, k));
+        ozaki_trailing_update(st, lc, d, A, k, H, emu_ws, emu_flag, H);
+        cluster_panel(k + H, H, P16);
+        MH_LAUNCH(lc, st, "lu_laswp_f64", laswp_cols_kernel<T><<<sg, 256, 0, st>>>(d, A, ipiv, k + H, H, k, k + H));
+      }
     } else {
-      MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
-                panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
+      const int P = panel_cluster_size<T>(n - k, d.batch, cap_ctas);
+      if (P > 0) {
+        cluster_panel(k, kNB, P);
+      } else {
+        MH_LAUNCH(lc, st, sizeof(T) == 8 ? "lu_panel_f64" : "lu_panel_f32",
+                  panel_kernel<T><<<(unsigned)d.batch, 512, 0, st>>>(d, A, ipiv, info, k));
+      }
     }
     if (n + d.extra - kb > 0) {
       dim3 sg((unsigned)((n + d.extra - kb + kSwpCols - 1) / kSwpCols), (unsigned)d.batch);

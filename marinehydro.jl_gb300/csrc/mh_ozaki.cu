@@ -38,6 +38,8 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "mh_digits.cuh"
 #include "mh_internal.cuh"
 #include "mh_tc.cuh"
@@ -71,10 +73,11 @@ __device__ __forceinline__ void ozaki_split_rows(int64_t bx, const BatchDesc& d,
   const int64_t b = blockIdx.y;
   if (r >= nrt * kOzRows) return;  // whole groups of four leave together
   // a grouped batch: this matrix's order, panel width and trailing size (the launch's `rest`
-  // stays the stride of the exponent arrays)
+  // stays the stride of the exponent arrays); kb: the launch's panel width (32, or 16 inside a
+  // two-level panel)
   const int64_t n = d.order(b);
-  if (k + kNB_oz >= n) return;
-  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
+  kb = (int)((k + kb < n) ? kb : n - k);
+  if (k + kb >= n) return;
   const int64_t rest_b = n - k - kb;
   const double2* Ab = A + d.offset(b);
   const bool live = r < rest_b;
@@ -88,7 +91,7 @@ __device__ __forceinline__ void ozaki_split_rows(int64_t bx, const BatchDesc& d,
   }
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-  if (live && kq == 0) rowexp[b * rest + r] = dg::scale_of(emax);
+  if (live && kq == 0) rowexp[b * (d.n + d.extra) + r] = dg::scale_of(emax);
   uint32_t pk[2][dg::kDigits7][4];
   dg::split7(v, emax, pk);
   unsigned char* tiles = digA + ((b * nrt + r / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
@@ -112,9 +115,11 @@ __device__ __forceinline__ void ozaki_split_cols(int64_t bx, const BatchDesc& d,
   const int64_t b = blockIdx.y;
   if (c >= nct * kOzCols) return;
   const int64_t n = d.order(b);
-  if (k + kNB_oz >= n) return;
-  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
-  const int64_t rest_b = n + d.extra - k - kb;  // columns of U12 (appended right-hand sides included)
+  kb = (int)((k + kb < n) ? kb : n - k);
+  if (k + kb >= n) return;
+  // columns of U12 (appended right-hand sides included), at most the launch's `rest` (which is
+  // the column limit of the update inside a two-level panel)
+  const int64_t rest_b = min(rest, n + d.extra - k - kb);
   const double2* Ab = A + d.offset(b);
   const bool live = c < rest_b;
   double2 v[8];
@@ -127,7 +132,7 @@ __device__ __forceinline__ void ozaki_split_cols(int64_t bx, const BatchDesc& d,
   }
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
   emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-  if (live && kq == 0) colexp[b * rest + c] = dg::scale_of(emax);
+  if (live && kq == 0) colexp[b * (d.n + d.extra) + c] = dg::scale_of(emax);
   uint32_t pk[2][dg::kDigits7][4];
   dg::split7(v, emax, pk);
   unsigned char* tiles = digB + ((b * nct + c / kOzCols) * kOzDigits * 2) * (int64_t)kOzBTile;
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(256) ozaki_trsm_prep_kernel(BatchDesc d, const
     }
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-    if (live && kq == 0) rowexp[b * rest + c] = dg::scale_of(emax);
+    if (live && kq == 0) rowexp[b * (d.n + d.extra) + c] = dg::scale_of(emax);
     uint32_t pk[2][dg::kDigits7][4];
     dg::split7(v, emax, pk);
     unsigned char* tiles = digA + ((b * nrt + c / kOzRows) * kOzDigits * 2) * (int64_t)kOzATile;
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(256) ozaki_trsm_prep_kernel(BatchDesc d, const
     }
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-    if (kq == 0) colexp[b * kNB_oz + j] = dg::scale_of(emax);  // 32 per matrix (rest may be smaller)
+    if (kq == 0) colexp[b * (d.n + d.extra) + j] = dg::scale_of(emax);
     uint32_t pk[2][dg::kDigits7][4];
     dg::split7(v, emax, pk);
     unsigned char* tiles = digB + (b * kOzDigits * 2) * (int64_t)kOzBTile;  // one column tile per matrix
@@ -288,12 +293,13 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   // a grouped batch: this matrix's panel width and trailing size; CTAs past its trailing
   // block leave before any barrier or tensor-memory allocation
   const int64_t n = d.order(b);
-  if (TRSM ? k + kNB_oz > n : k + kNB_oz >= n) return;
-  kb = (int)((k + kNB_oz < n) ? kNB_oz : n - k);
+  if (TRSM ? k + kNB_oz > n : k + kb >= n) return;
+  kb = (int)((k + kb < n) ? kb : n - k);  // the launch's panel width (32, or 16 inside a two-level panel)
   // output rows: trailing rows of A22, or (TRSM) the columns of A12; output columns: the
-  // columns of A22 right of the panel (appended right-hand sides included), or the 32 rows of U12
+  // columns of A22 right of the panel (appended right-hand sides included, at most the launch's
+  // `rest`), or the 32 rows of U12
   const int64_t rest_b = TRSM ? n + d.extra - k - kb : n - k - kb;
-  const int64_t rest_cb = TRSM ? kb : n + d.extra - k - kb;
+  const int64_t rest_cb = TRSM ? kb : min(rest, n + d.extra - k - kb);
   if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_cb) return;
   // TRSM: one 32-column tile, the rows of U12 (the output is U12 transposed)
   const int64_t nct_b = TRSM ? 1 : (rest_cb + kOzCols - 1) / kOzCols;
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const int lrow = tid & (kOzRows - 1), half = tid >> 7;  // TMEM lane (output row) and column half
   const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
   const bool row_live = r < rest_b;
-  const int er = row_live ? rowexp[b * rest + r] : 0;
+  const int er = row_live ? rowexp[b * (d.n + d.extra) + r] : 0;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   double2* Ab = A + d.offset(b);
   double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
@@ -348,8 +354,10 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
         const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
         const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
         const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
+        const int nks = (kb + 15) / 16;  // K = 16 steps with data (the digits beyond kb are zero)
 #pragma unroll
         for (int kk = 0; kk < kOzK / 16; ++kk) {
+          if (kk >= nks) break;
           const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
           const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
           const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
@@ -371,7 +379,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
       const int64_t c = cbase + q;
       const bool live = row_live && c < rest_cb;
       cv[q] = (live && !TRSM) ? crow[c * n] : make_double2(0.0, 0.0);
-      ce[q] = live ? colexp[TRSM ? b * kNB_oz + c : b * rest + c] : 0;  // TRSM: 32 per matrix
+      ce[q] = live ? colexp[b * (d.n + d.extra) + c] : 0;
     }
     ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
     if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -466,7 +474,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
 }  // namespace
 
 // workspace layout per batch: A digit tiles (row tiles of the widest operand), B digit tiles,
-// row and column exponents (stride n + extra per matrix)
+// row and column exponents (n + extra per matrix, indexed b (n + extra) + row or column)
 static int64_t oz_row_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzRows - 1) / kOzRows; }
 static int64_t oz_col_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzCols - 1) / kOzCols; }
 
@@ -477,9 +485,9 @@ size_t ozaki_workspace_bytes(int64_t n, int64_t batch, int64_t extra) {
 }
 
 void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, int kb,
-                           void* ws, int* timeout_flag) {
-  const int64_t rows = d.n - k - kb;           // trailing rows
-  const int64_t rest = d.n + d.extra - k - kb;  // trailing columns: the exponent arrays' stride
+                           void* ws, int* timeout_flag, int64_t cols) {
+  const int64_t rows = d.n - k - kb;                           // trailing rows
+  const int64_t rest = std::min(cols, d.n + d.extra - k - kb);  // trailing columns: the exponent arrays' stride
   if (rows <= 0) return;
   const int64_t nrt = (rows + kOzRows - 1) / kOzRows, nct = (rest + kOzCols - 1) / kOzCols;
   unsigned char* digA = static_cast<unsigned char*>(ws);
