@@ -23,18 +23,21 @@
 //     exponents; columns: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
 //     column exponents; the seven digit tiles of one part are consecutive, so digits
 //     q .. 6 form one (32 (7 - q)) x 32 operand;
-//   ozaki_gemm: one CTA per 128-row tile and group of four 32-column tiles: the 14 A digit
-//     tiles (112 KB) and double-buffered B tiles (2 x 28 KB) arrive in shared memory by TMA
-//     bulk copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (7 - p)
+//   ozaki_gemm: one CTA of 512 threads per 128-row tile and group of four 32-column tiles:
+//     the 14 A digit tiles (112 KB) and one B tile (28 KB) arrive in shared memory by TMA bulk
+//     copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (7 - p)
 //     multiplies X_p by the stacked Y_0 .. Y_{6-p} and accumulates X_p Y_q into the TMEM
 //     columns of T_{p+q} (Re: 32 d, Im: 224 + 32 d), so 56 MMAs (7 digits x 2 K-steps x 4
 //     real products) cover the 28 digit pairs.  (16-column tiles, whose two accumulator sets
-//     fit TMEM twice so that the products overlap the epilogue, measured 12 % slower: they
-//     read every A tile twice as often.)  The epilogue converts the exact integers with
-//     magic-number additions (no integer-to-FP64 conversion instructions), combines them in
-//     32/64-bit integers, rounds hi + lo 2^-24 to one 53-bit integer, builds its scaled double
-//     with integer operations and applies it with one FP64 subtraction per real entry; C is
-//     prefetched into registers while the MMAs run.
+//     fit TMEM twice, measured 12 % slower: they read every A tile twice as often.)  The
+//     epilogue converts the exact integers T0..T3 with magic-number additions (no
+//     integer-to-FP64 conversion instructions) and combines them in 32/64-bit integers, adds
+//     T4 + T5 2^-8 + T6 2^-16 formed in FP32, builds the scaled double of the 53-bit integer
+//     with integer operations and applies it with one FP64 subtraction per real entry.  The
+//     subtractions of one column tile run while the tensor cores compute the next one (the
+//     accumulators of a tile fill 448 of the 512 TMEM columns, so the TMEM reads of a tile
+//     come first); four warps per SM sub-partition keep its FP64 pipe busy, and each tile of
+//     A22 is prefetched into L2 one tile ahead.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -269,14 +272,112 @@ __device__ __forceinline__ double scaled_i64(long long v, int s) {
 
 constexpr int kOzGroupMax = 8; // column tiles per CTA (the A tiles are loaded once for all of them):
                                // 1..8, from the launch-shape table (default 4)
-constexpr int kOzThreads = 256; // two threads per output row: warps w and w + 4 share TMEM lanes
-                                // 32 (w % 4) .. and take one half of the 32 columns each
+constexpr int kOzThreads = 512; // four threads per output row: warps w, w + 4, w + 8, w + 12 share
+                                // the TMEM lanes 32 (w % 4) .. and take a quarter of the columns each
 
-// One CTA per (row tile, group of `group` column tiles, matrix).  The A digit tiles and the
-// first B tile arrive by TMA bulk copies on one mbarrier; the B tiles are double-buffered,
-// the next one prefetched while the current tile's products and epilogue run.
+// The eight MMAs of digit p of L21 for one column tile (one thread): X_p (A tiles at a0)
+// times the stacked Y_0 .. Y_{6-p} (B tiles at b0) into the TMEM columns of T_p .. T_6, Re and
+// Im; K = 16 steps past the panel width kb are skipped (their digits are zero)
+__device__ __forceinline__ void ozaki_issue_digit(uint32_t tmem, uint32_t a0, uint32_t b0, int p, int kb) {
+  constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
+  const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
+  const int nn = kOzCols * (kOzDigits - p);
+  const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
+  const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
+  const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
+  const int nks = (kb + 15) / 16;
+#pragma unroll
+  for (int kk = 0; kk < kOzK / 16; ++kk) {
+    if (kk >= nks) break;
+    const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
+    const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
+    const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
+    const uint64_t dbr = tc::smem_desc(bre + ko, 128, sbo), dbi = tc::smem_desc(bim + ko, 128, sbo);
+    tc::mma_bf16(t_re, dar, dbr, id, acc);      // Re T += Xre Yre
+    tc::mma_bf16(t_re, dai, dbi, id_neg, 1u);   // Re T -= Xim Yim
+    tc::mma_bf16(t_im, dar, dbi, id, acc);      // Im T += Xre Yim
+    tc::mma_bf16(t_im, dai, dbr, id, 1u);       // Im T += Xim Yre
+  }
+}
+
+constexpr int kOzSmem = kOzABytes + kOzBBytes;  // 140 KB: the A digit tiles and one B tile
+
+// x + 1.5 2^23 holds an integer-valued x with |x| <= 2^22 in its low mantissa bits exactly
+__device__ __forceinline__ int exact_int22(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+// the integer nearest x, |x| < 2^23: 1.5 2^24 rounds x to an even integer 2 h exactly, and the
+// remainder x - 2 h (exact, |.| <= 1) is rounded by 1.5 2^23
+__device__ __forceinline__ int rint23(float x) {
+  const float y = x + 25165824.0f;
+  const float rr = x - (y - 25165824.0f);
+  return 2 * (__float_as_int(y) - 0x4BC00000) + exact_int22(rr);
+}
+
+// The products of 8 columns of this thread's lane (TMEM columns c0 ..) as integers:
+// v = (T0 2^24 + T1 2^16 + T2 2^8 + T3) 2^8 + rint(T4 + T5 2^-8 + T6 2^-16).  T0..T3 (|T_d| <=
+// (d + 1) 2^20 <= 2^22) convert exactly and combine in 32/64-bit integers; the low sum is formed
+// in FP32 (two FMAs, rounding error below 0.26), so v is within 0.76 of the exact
+// sum_d T_d 2^(32 - 8 d) (|v| < 2^52.1).  Four TMEM waits per 8 columns.
+__device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long long* vr, long long* vi) {
+  constexpr uint32_t im = kOzDigits * kOzCols;  // the Im accumulators follow the Re ones
+  auto col = [&](int d, bool imag) { return trow + (imag ? im : 0u) + (uint32_t)(d * kOzCols + c0); };
+  int hr[8], hi[8], gr[8], gi[8];
+  float f[4][8];
+  {
+    const uint32_t a[4] = {col(0, false), col(0, true), col(1, false), col(1, true)};
+    tc::tmem_ld8x4(a, f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      hr[q] = exact_int22(f[0][q]) * 256 + exact_int22(f[2][q]);
+      hi[q] = exact_int22(f[1][q]) * 256 + exact_int22(f[3][q]);
+    }
+  }
+  {
+    const uint32_t a[4] = {col(2, false), col(2, true), col(3, false), col(3, true)};
+    tc::tmem_ld8x4(a, f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      gr[q] = exact_int22(f[0][q]) * 256 + exact_int22(f[2][q]);
+      gi[q] = exact_int22(f[1][q]) * 256 + exact_int22(f[3][q]);
+    }
+  }
+  float lr[8], li[8];
+  {
+    const uint32_t a[4] = {col(5, false), col(5, true), col(6, false), col(6, true)};
+    tc::tmem_ld8x4(a, f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      lr[q] = fmaf(f[2][q], 0.00390625f, f[0][q]);  // T5 + T6 2^-8
+      li[q] = fmaf(f[3][q], 0.00390625f, f[1][q]);
+    }
+  }
+  {
+    float g[2][8];
+    const uint32_t a[2] = {col(4, false), col(4, true)};
+    tc::tmem_ld8x2(a, g);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int lor = rint23(fmaf(lr[q], 0.00390625f, g[0][q]));  // T4 + (T5 + T6 2^-8) 2^-8
+      const int loi = rint23(fmaf(li[q], 0.00390625f, g[1][q]));
+      vr[q] = ((long long)hr[q] * 65536 + gr[q]) * 256 + lor;
+      vi[q] = ((long long)hi[q] * 65536 + gi[q]) * 256 + loi;
+    }
+  }
+}
+
+// One CTA of 512 threads per (row tile, group of `group` column tiles, matrix): four threads
+// per output row (warps w, w + 4, w + 8, w + 12 share the TMEM lanes 32 (w % 4) .. and take 8
+// of the 32 columns each), so that four warps per SM sub-partition keep its FP64 pipe busy.
+// Shared memory: the 14 A digit tiles (112 KB, loaded once) and one B tile (28 KB).  Per
+// column tile t:
+//   1. wait for tile t's products; thread 0 starts the bulk copy of tile t + 1's B tile;
+//   2. every thread reads its lane's accumulators for its 8 columns and forms the integers v;
+//   3. once every thread has read the TMEM, thread 0 prefetches tile t + 1's A22 entries into
+//      L2 and issues its 56 MMAs, while every thread subtracts tile t's products from its A22
+//      entries (doubles built from v by integer operations, one FP64 subtraction per real
+//      entry) and stores them: the FP64 work of one tile runs under the tensor work of the next.
+// TRSM: a single column tile whose products are assigned into U12.
 template <bool TRSM>
-__global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
+__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
                                                               int64_t rest, int64_t nrt, int64_t nct,
                                                               const unsigned char* __restrict__ digA,
                                                               const unsigned char* __restrict__ digB,
@@ -284,10 +385,10 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
                                                               const int* __restrict__ colexp,
                                                               int* __restrict__ timeout_flag, int group) {
   extern __shared__ __align__(1024) unsigned char osm[];
-  __shared__ __align__(8) uint64_t mbar_load[2];
-  __shared__ __align__(8) uint64_t mbar_mma;
+  __shared__ __align__(8) uint64_t mbar_a, mbar_b, mbar_mma;
   __shared__ uint32_t tmem_base;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  __shared__ int sce[kOzCols];  // column exponents of the current tile
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
   const int64_t ct0 = blockIdx.y * (int64_t)group;
   // a grouped batch: this matrix's panel width and trailing size; CTAs past its trailing
@@ -305,12 +406,12 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   const int64_t nct_b = TRSM ? 1 : (rest_cb + kOzCols - 1) / kOzCols;
   const int ntile = (int)((nct_b - ct0) < group ? (nct_b - ct0) : group);
   unsigned char* As = osm;
-  unsigned char* Bs[2] = {osm + kOzABytes, osm + kOzABytes + kOzBBytes};
+  unsigned char* Bs = osm + kOzABytes;
   const unsigned char* srcA = digA + (b * nrt + rt) * (int64_t)kOzABytes;
   auto srcB = [&](int64_t ct) { return digB + (b * nct + ct) * (int64_t)kOzBBytes; };
   if (tid == 0) {
-    tc::mbar_init(&mbar_load[0], 1);
-    tc::mbar_init(&mbar_load[1], 1);
+    tc::mbar_init(&mbar_a, 1);
+    tc::mbar_init(&mbar_b, 1);
     tc::mbar_init(&mbar_mma, 1);
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base, kOzTmemCols);
@@ -318,17 +419,7 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
-  if (tid == 0) {
-    tc::mbar_arrive_expect_tx(&mbar_load[0], kOzABytes + kOzBBytes);
-    for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, srcA + q, 16384, &mbar_load[0]);
-    tc::bulk_g2s(Bs[0], srcB(ct0), kOzBBytes, &mbar_load[0]);
-    if (ntile > 1) {
-      tc::mbar_arrive_expect_tx(&mbar_load[1], kOzBBytes);
-      tc::bulk_g2s(Bs[1], srcB(ct0 + 1), kOzBBytes, &mbar_load[1]);
-    }
-  }
-  constexpr uint32_t sbo = (kOzK / 8) * 128;  // 8-row core groups are K * 16 bytes apart
-  const int lrow = tid & (kOzRows - 1), half = tid >> 7;  // TMEM lane (output row) and column half
+  const int lrow = tid & (kOzRows - 1), quarter = tid >> 7;  // TMEM lane (output row) and column quarter
   const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
   const bool row_live = r < rest_b;
   const int er = row_live ? rowexp[b * (d.n + d.extra) + r] : 0;
@@ -336,135 +427,104 @@ __global__ void __launch_bounds__(kOzThreads) ozaki_gemm_kernel(BatchDesc d, dou
   double2* Ab = A + d.offset(b);
   double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
   double2* ucol = Ab + k + (k + kb + r) * n;         // TRSM: column k + kb + r of U12
+  const int nrow = (int)min((int64_t)kOzRows, rest_b - rt * kOzRows);  // live rows of the tile
+  const double2* ctile = Ab + (k + kb + rt * kOzRows) + (k + kb) * n;  // the row tile of A22
+  auto prefetch_c = [&](int64_t ct) {  // one thread: the tile's A22 columns into L2
+    const int nc = (int)min((int64_t)kOzCols, rest_cb - ct * kOzCols);
+    for (int c = 0; c < nc; ++c) tc::bulk_prefetch_l2(ctile + (ct * kOzCols + c) * n, (uint32_t)nrow * 16u);
+  };
+  // copies and products issued / waited for (identical in every thread; for the drain)
+  int a_iss = 0, b_iss = 0, m_iss = 0, a_wt = 0, b_wt = 0, m_wt = 0;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(&mbar_a, kOzABytes);
+    for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, srcA + q, 16384, &mbar_a);
+    tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
+    tc::bulk_g2s(Bs, srcB(ct0), kOzBBytes, &mbar_b);
+    if (!TRSM) prefetch_c(ct0);
+  }
+  a_iss = b_iss = 1;
   bool failed = false;
-  int outstanding_load = ntile > 1 ? 2 : 1;  // loads in flight (for the drain after a timeout)
-  for (int t = 0; t < ntile; ++t) {
-    const int buf = t & 1;
-    const int64_t ct = ct0 + t;
-    bool ok = tc::mbar_wait(&mbar_load[buf], (uint32_t)((t >> 1) & 1), kOzWaitPolls);
-    if (__syncthreads_or(!ok)) { failed = true; break; }
-    --outstanding_load;
-    if (tid == 0) {
-      tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs[buf]);
-      const uint32_t bre = b0, bim = b0 + (uint32_t)kOzDigits * kOzBTile;  // Y_0 of each part
+  {
+    bool ok = tc::mbar_wait(&mbar_a, 0u, kOzWaitPolls);
+    ok = ok && tc::mbar_wait(&mbar_b, 0u, kOzWaitPolls);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+    } else {
+      a_wt = b_wt = 1;
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
 #pragma unroll 1
-      for (int p = 0; p < kOzDigits; ++p) {
-        const int nn = kOzCols * (kOzDigits - p);  // Y_0 .. Y_{6-p} stacked along N
-        const uint32_t id = tc::idesc_bf16_f32(kOzRows, nn), id_neg = tc::idesc_bf16_f32_nega(kOzRows, nn);
-        const uint32_t t_re = tmem + (uint32_t)(kOzCols * p), t_im = t_re + (uint32_t)(kOzCols * kOzDigits);
-        const uint32_t ar = a0 + (uint32_t)(2 * p) * kOzATile, ai = ar + kOzATile;
-        const int nks = (kb + 15) / 16;  // K = 16 steps with data (the digits beyond kb are zero)
-#pragma unroll
-        for (int kk = 0; kk < kOzK / 16; ++kk) {
-          if (kk >= nks) break;
-          const uint32_t ko = (uint32_t)kk * 256;  // two K-adjacent core matrices per K = 16 step
-          const uint32_t acc = (p == 0 && kk == 0) ? 0u : 1u;
-          const uint64_t dar = tc::smem_desc(ar + ko, 128, sbo), dai = tc::smem_desc(ai + ko, 128, sbo);
-          const uint64_t dbr = tc::smem_desc(bre + ko, 128, sbo), dbi = tc::smem_desc(bim + ko, 128, sbo);
-          tc::mma_bf16(t_re, dar, dbr, id, acc);      // Re T += Xre Yre
-          tc::mma_bf16(t_re, dai, dbi, id_neg, 1u);   // Re T -= Xim Yim
-          tc::mma_bf16(t_im, dar, dbi, id, acc);      // Im T += Xre Yim
-          tc::mma_bf16(t_im, dai, dbr, id, 1u);       // Im T += Xim Yre
-        }
+        for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, kb);
+        tc::mma_commit(&mbar_mma);
       }
+      m_iss = 1;
+    }
+  }
+  for (int t = 0; t < ntile && !failed; ++t) {
+    const int64_t ct = ct0 + t;
+    const bool more = t + 1 < ntile;
+    bool ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+    ++m_wt;
+    tc::fence_after_sync();
+    // the B tile is free (tile t's products are done): bring in tile t + 1's
+    if (tid == 0 && more) {
+      tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
+      tc::bulk_g2s(Bs, srcB(ct + 1), kOzBBytes, &mbar_b);
+    }
+    if (more) ++b_iss;
+    if (warp == 1) {
+      const int64_t c = ct * kOzCols + lane;
+      sce[lane] = c < rest_cb ? colexp[b * (d.n + d.extra) + c] : 0;
+    }
+    long long vr[8], vi[8];
+    ozaki_levels_to_int(trow, quarter * 8, vr, vi);
+    bool okw = true;
+    if (more) okw = tc::mbar_wait(&mbar_b, (uint32_t)((t + 1) & 1), kOzWaitPolls);
+    // every TMEM read of this tile is done before thread 0 issues the next products
+    tc::fence_before_sync();
+    if (__syncthreads_or(!okw)) { failed = true; break; }
+    if (more) ++b_wt;
+    tc::fence_after_sync();
+    if (more && tid == 0) {
+      if (!TRSM) prefetch_c(ct + 1);
+      const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
+#pragma unroll 1
+      for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, kb);
       tc::mma_commit(&mbar_mma);
     }
-    // while the products run: this thread's 16 entries of A22 and their column exponents
-    double2 cv[kOzCols / 2];
-    int ce[kOzCols / 2];
-    const int64_t cbase = ct * kOzCols + half * (kOzCols / 2);
+    if (more) ++m_iss;
+    // v 2^(e_i + f_j - 46) as a double by integer operations, one FP64 subtraction per real entry
+    const int64_t cbase = ct * kOzCols + quarter * 8;
+    double2 cv[8];
 #pragma unroll
-    for (int q = 0; q < kOzCols / 2; ++q) {
+    for (int q = 0; q < 8; ++q) {
+      const bool live = row_live && cbase + q < rest_cb;
+      cv[q] = (live && !TRSM) ? crow[(cbase + q) * n] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
       const int64_t c = cbase + q;
       const bool live = row_live && c < rest_cb;
-      cv[q] = (live && !TRSM) ? crow[c * n] : make_double2(0.0, 0.0);
-      ce[q] = live ? colexp[b * (d.n + d.extra) + c] : 0;
-    }
-    ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
-    if (__syncthreads_or(!ok)) { failed = true; break; }
-    tc::fence_after_sync();
-    // this B buffer is free again: prefetch tile t + 2 into it
-    if (tid == 0 && t + 2 < ntile) {
-      tc::mbar_arrive_expect_tx(&mbar_load[buf], kOzBBytes);
-      tc::bulk_g2s(Bs[buf], srcB(ct + 2), kOzBBytes, &mbar_load[buf]);
-    }
-    if (t + 2 < ntile) ++outstanding_load;
-#pragma unroll
-    for (int h8 = 0; h8 < 2; ++h8) {
-      const int c0 = half * (kOzCols / 2) + 8 * h8;
-      // T_d as exact integers, paired: (T0 2^8 + T1, T2 2^8 + T3, T4 2^8 + T5, T6), re and im.
-      // |T_d| <= (d + 1) 2^20 (d + 1 digit pairs, K = 32, two real products, |digit| <= 2^7)
-      int pr[4][8], pi[4][8];
-#pragma unroll
-      for (int dd = 0; dd < kOzDigits; ++dd) {
-        float vr[8], vi[8];
-        tc::tmem_ld8(trow + (uint32_t)(dd * kOzCols + c0), vr);
-        tc::tmem_ld8(trow + (uint32_t)(kOzDigits * kOzCols + dd * kOzCols + c0), vi);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          int ir, ii;
-          if (dd <= 3) {
-            // |T| <= 2^22: adding 1.5 2^23 puts the integer in the low mantissa bits exactly
-            ir = __float_as_int(vr[q] + 12582912.0f) - 0x4B400000;
-            ii = __float_as_int(vi[q] + 12582912.0f) - 0x4B400000;
-          } else {
-            // |T| < 2^23: 1.5 2^24 rounds T to an even integer 2 h exactly; the remainder
-            // T - 2 h in {-1, 0, 1} is exact too
-            const float yr = vr[q] + 25165824.0f, yi = vi[q] + 25165824.0f;
-            const float rr = vr[q] - (yr - 25165824.0f), ri = vi[q] - (yi - 25165824.0f);
-            ir = 2 * (__float_as_int(yr) - 0x4BC00000) + (__float_as_int(rr + 12582912.0f) - 0x4B400000);
-            ii = 2 * (__float_as_int(yi) - 0x4BC00000) + (__float_as_int(ri + 12582912.0f) - 0x4B400000);
-          }
-          if (dd == 6) { pr[3][q] = ir; pi[3][q] = ii; }
-          else if (dd & 1) { pr[dd >> 1][q] = pr[dd >> 1][q] * 256 + ir; pi[dd >> 1][q] = pi[dd >> 1][q] * 256 + ii; }
-          else { pr[dd >> 1][q] = ir; pi[dd >> 1][q] = ii; }
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int qq = 8 * h8 + q;
-        // hi = T0 2^24 + T1 2^16 + T2 2^8 + T3 (< 2^44.01), lo = T4 2^16 + T5 2^8 + T6 (< 2^38.4);
-        // L21 U12 = 2^(e_i + f_j - 38) (hi + lo 2^-24); v = hi 2^8 + lo 2^-16, rounded to an
-        // integer (|v| < 2^52.1), is scaled into a double by integer operations, so the FP64
-        // pipe does one subtraction per real entry
-        const long long hr = (long long)pr[0][q] * 65536 + pr[1][q], lr = (long long)pr[2][q] * 256 + pr[3][q];
-        const long long hi = (long long)pi[0][q] * 65536 + pi[1][q], li = (long long)pi[2][q] * 256 + pi[3][q];
-        const long long vr = hr * 256 + ((lr + (1LL << 15)) >> 16);
-        const long long vi = hi * 256 + ((li + (1LL << 15)) >> 16);
-        const int sc = er + ce[qq] - 46;
-        if (TRSM) {
-          cv[qq] = make_double2(scaled_i64(vr, sc), scaled_i64(vi, sc));
-        } else {
-          cv[qq].x -= scaled_i64(vr, sc);
-          cv[qq].y -= scaled_i64(vi, sc);
-        }
+      const int sc = er + sce[quarter * 8 + q] - 46;
+      const double sr = scaled_i64(vr[q], sc), si = scaled_i64(vi[q], sc);
+      if (TRSM) {
+        if (live) ucol[c] = make_double2(sr, si);
+      } else {
+        cv[q].x -= sr;
+        cv[q].y -= si;
+        if (live) crow[c * n] = cv[q];
       }
     }
-    if (row_live) {
-#pragma unroll
-      for (int q = 0; q < kOzCols / 2; ++q) {
-        if (TRSM) {
-          if (cbase + q < rest_cb) ucol[cbase + q] = cv[q];
-        } else {
-          if (cbase + q < rest_cb) crow[(cbase + q) * n] = cv[q];
-        }
-      }
-    }
-    // every TMEM read of this tile is done before the next tile's products overwrite it
-    tc::fence_before_sync();
-    __syncthreads();
   }
   if (failed) {
     // reported by the host as a timeout; drain the products and copies in flight (bounded)
     // before the tensor memory and shared memory are released
     if (tid == 0) atomicExch(timeout_flag, 1);
-    tc::mbar_wait(&mbar_mma, 0, kOzWaitPolls);
-    tc::mbar_wait(&mbar_mma, 1, kOzWaitPolls);
-    if (outstanding_load > 0) {
-      tc::mbar_wait(&mbar_load[0], 0, kOzWaitPolls);
-      tc::mbar_wait(&mbar_load[1], 0, kOzWaitPolls);
-    }
+    if (m_wt < m_iss) tc::mbar_wait(&mbar_mma, (uint32_t)(m_wt & 1), kOzWaitPolls);
+    if (a_wt < a_iss) tc::mbar_wait(&mbar_a, 0u, kOzWaitPolls);
+    if (b_wt < b_iss) tc::mbar_wait(&mbar_b, (uint32_t)(b_wt & 1), kOzWaitPolls);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -498,7 +558,7 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   dim3 gs((unsigned)(row_ctas + col_ctas), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_ozaki_split",
             ozaki_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nrt, nct, row_ctas, digA, digB, rowexp, colexp));
-  const size_t smem = kOzABytes + 2 * kOzBBytes;
+  const size_t smem = kOzSmem;
   cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int group = lc.tile(d.n).oz_group;
   group = group < 1 ? 1 : (group > kOzGroupMax ? kOzGroupMax : group);
@@ -522,7 +582,7 @@ void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* 
   dim3 gs((unsigned)(row_ctas + 1), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_trsm_ozaki_prep",
             ozaki_trsm_prep_kernel<<<gs, 256, 0, st>>>(d, A, k, rest, nrt, row_ctas, digA, digB, rowexp, colexp));
-  const size_t smem = kOzABytes + 2 * kOzBBytes;
+  const size_t smem = kOzSmem;
   cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 gg((unsigned)nrt, 1u, (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_trsm_ozaki",

@@ -185,5 +185,58 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   for (int q = 0; q < 8; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+// four groups of 8 consecutive FP32 columns of this thread's lane (at taddr[0..3]) with a
+// single wait; the registers pass through the wait so that no use is scheduled before it
+__device__ __forceinline__ void tmem_ld8x4(const uint32_t (&taddr)[4], float (&v)[4][8]) {
+  uint32_t r[4][8];
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[g][0]), "=r"(r[g][1]), "=r"(r[g][2]), "=r"(r[g][3]), "=r"(r[g][4]), "=r"(r[g][5]),
+                   "=r"(r[g][6]), "=r"(r[g][7])
+                 : "r"(taddr[g])
+                 : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[0][4]), "+r"(r[0][5]),
+                 "+r"(r[0][6]), "+r"(r[0][7]), "+r"(r[1][0]), "+r"(r[1][1]), "+r"(r[1][2]), "+r"(r[1][3]),
+                 "+r"(r[1][4]), "+r"(r[1][5]), "+r"(r[1][6]), "+r"(r[1][7]), "+r"(r[2][0]), "+r"(r[2][1]),
+                 "+r"(r[2][2]), "+r"(r[2][3]), "+r"(r[2][4]), "+r"(r[2][5]), "+r"(r[2][6]), "+r"(r[2][7]),
+                 "+r"(r[3][0]), "+r"(r[3][1]), "+r"(r[3][2]), "+r"(r[3][3]), "+r"(r[3][4]), "+r"(r[3][5]),
+                 "+r"(r[3][6]), "+r"(r[3][7])
+               :
+               : "memory");
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[g][q] = __uint_as_float(r[g][q]);
+}
+
+// two groups of 8 columns with a single wait (as tmem_ld8x4)
+__device__ __forceinline__ void tmem_ld8x2(const uint32_t (&taddr)[2], float (&v)[2][8]) {
+  uint32_t r[2][8];
+#pragma unroll
+  for (int g = 0; g < 2; ++g)
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[g][0]), "=r"(r[g][1]), "=r"(r[g][2]), "=r"(r[g][3]), "=r"(r[g][4]), "=r"(r[g][5]),
+                   "=r"(r[g][6]), "=r"(r[g][7])
+                 : "r"(taddr[g])
+                 : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[0][4]), "+r"(r[0][5]),
+                 "+r"(r[0][6]), "+r"(r[0][7]), "+r"(r[1][0]), "+r"(r[1][1]), "+r"(r[1][2]), "+r"(r[1][3]),
+                 "+r"(r[1][4]), "+r"(r[1][5]), "+r"(r[1][6]), "+r"(r[1][7])
+               :
+               : "memory");
+#pragma unroll
+  for (int g = 0; g < 2; ++g)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[g][q] = __uint_as_float(r[g][q]);
+}
+
+// L2 prefetch of `bytes` (multiple of 16) of global memory at a 16-byte aligned address
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src_gmem, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
+}
+
 }  // namespace tc
 }  // namespace mh
