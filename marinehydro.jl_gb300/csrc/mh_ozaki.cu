@@ -372,9 +372,10 @@ __device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long 
 //   1. wait for tile t's products; thread 0 starts the bulk copy of tile t + 1's B tile;
 //   2. every thread reads its lane's accumulators for its 8 columns and forms the integers v;
 //   3. once every thread has read the TMEM, thread 0 prefetches tile t + 1's A22 entries into
-//      L2 and issues its 56 MMAs, while every thread subtracts tile t's products from its A22
-//      entries (doubles built from v by integer operations, one FP64 subtraction per real
-//      entry) and stores them: the FP64 work of one tile runs under the tensor work of the next.
+//      L2 and issues its 56 MMAs, while the other threads subtract tile t's products from
+//      their A22 entries (doubles built from v by integer operations, one FP64 subtraction per
+//      real entry) and store them; warps 4, 8 and 12 also take warp 0's entries (handed over
+//      in shared memory): the FP64 work of one tile runs under the tensor work of the next.
 // TRSM: a single column tile whose products are assigned into U12.
 template <bool TRSM>
 __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
@@ -388,6 +389,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
   __shared__ __align__(8) uint64_t mbar_a, mbar_b, mbar_mma;
   __shared__ uint32_t tmem_base;
   __shared__ int sce[kOzCols];  // column exponents of the current tile
+  __shared__ longlong2 shand[8 * 32];  // warp 0's integers, handed to warps 4, 8 and 12
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t rt = blockIdx.x, b = blockIdx.z;
   const int64_t ct0 = blockIdx.y * (int64_t)group;
@@ -480,6 +482,13 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     }
     long long vr[8], vi[8];
     ozaki_levels_to_int(trow, quarter * 8, vr, vi);
+    // while thread 0 issues the next products, warps 4, 8 and 12 (on warp 0's SM sub-partition)
+    // subtract warp 0's entries
+    const bool handoff = more && !TRSM;
+    if (handoff && warp == 0) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) shand[q * 32 + lane] = make_longlong2(vr[q], vi[q]);
+    }
     bool okw = true;
     if (more) okw = tc::mbar_wait(&mbar_b, (uint32_t)((t + 1) & 1), kOzWaitPolls);
     // every TMEM read of this tile is done before thread 0 issues the next products
@@ -496,25 +505,52 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     }
     if (more) ++m_iss;
     // v 2^(e_i + f_j - 46) as a double by integer operations, one FP64 subtraction per real entry
-    const int64_t cbase = ct * kOzCols + quarter * 8;
-    double2 cv[8];
+    if (!(handoff && warp == 0)) {
+      const int64_t cbase = ct * kOzCols + quarter * 8;
+      // warp 0's entries q0 .. q0 + nx - 1 (column quarter 0): three each for warps 4 and 8, two
+      // for warp 12
+      const bool recv = handoff && (warp & 3) == 0;
+      const int q0 = 3 * (quarter - 1), nx = recv ? min(3, 8 - q0) : 0;
+      double2 cv[8], xv[3];
+      long long xr[3], xi[3];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const bool live = row_live && cbase + q < rest_cb;
-      cv[q] = (live && !TRSM) ? crow[(cbase + q) * n] : make_double2(0.0, 0.0);
-    }
+      for (int q = 0; q < 8; ++q) {
+        const bool live = row_live && cbase + q < rest_cb;
+        cv[q] = (live && !TRSM) ? crow[(cbase + q) * n] : make_double2(0.0, 0.0);
+      }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int64_t c = cbase + q;
-      const bool live = row_live && c < rest_cb;
-      const int sc = er + sce[quarter * 8 + q] - 46;
-      const double sr = scaled_i64(vr[q], sc), si = scaled_i64(vi[q], sc);
-      if (TRSM) {
-        if (live) ucol[c] = make_double2(sr, si);
-      } else {
-        cv[q].x -= sr;
-        cv[q].y -= si;
-        if (live) crow[c * n] = cv[q];
+      for (int j = 0; j < 3; ++j) {
+        if (j < nx) {
+          const int64_t c = ct * kOzCols + q0 + j;
+          xv[j] = (row_live && c < rest_cb) ? crow[c * n] : make_double2(0.0, 0.0);
+          const longlong2 w = shand[(q0 + j) * 32 + lane];
+          xr[j] = w.x;
+          xi[j] = w.y;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int64_t c = cbase + q;
+        const bool live = row_live && c < rest_cb;
+        const int sc = er + sce[quarter * 8 + q] - 46;
+        const double sr = scaled_i64(vr[q], sc), si = scaled_i64(vi[q], sc);
+        if (TRSM) {
+          if (live) ucol[c] = make_double2(sr, si);
+        } else {
+          cv[q].x -= sr;
+          cv[q].y -= si;
+          if (live) crow[c * n] = cv[q];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (j < nx) {
+          const int64_t c = ct * kOzCols + q0 + j;
+          const int sc = er + sce[q0 + j] - 46;
+          xv[j].x -= scaled_i64(xr[j], sc);
+          xv[j].y -= scaled_i64(xi[j], sc);
+          if (row_live && c < rest_cb) crow[c * n] = xv[j];
+        }
       }
     }
   }
