@@ -94,7 +94,9 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
   // candidates: the cluster bound of the panel and, for the tensor-core updates, the
   // column tiles per CTA; the first candidate is the default shape
   std::vector<TileChoice> cands;
-  const int caps[3] = {8, 4, 2}, groups[4] = {4, 1, 2, 8};
+  const int caps[3] = {8, 4, 2};
+  const int groups_tc[4] = {8, 4, 2, 1}, groups_bx[4] = {4, 1, 2, 8};  // the defaults first
+  const int* groups = precision == MH_PREC_FP64_TC ? groups_tc : groups_bx;
   for (int cap : caps) {
     if (precision == MH_PREC_FP64) {
       TileChoice c;
@@ -102,7 +104,8 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
       cands.push_back(c);
       continue;
     }
-    for (int gr : groups) {
+    for (int gi = 0; gi < 4; ++gi) {
+      const int gr = groups[gi];
       TileChoice c;
       if (precision == MH_PREC_MIXED) {
         c.bx_group = gr;

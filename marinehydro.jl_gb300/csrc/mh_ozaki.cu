@@ -596,8 +596,17 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
             ozaki_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nrt, nct, row_ctas, digA, digB, rowexp, colexp));
   const size_t smem = kOzSmem;
   cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // column tiles per CTA: the launch-shape table's value as the upper bound, halved while the
+  // grid would fill fewer than two waves of CTAs (one CTA per SM)
+  static const int sms = [] {
+    int dev = 0, v = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v;
+  }();
   int group = lc.tile(d.n).oz_group;
   group = group < 1 ? 1 : (group > kOzGroupMax ? kOzGroupMax : group);
+  while (group > 1 && nrt * ((nct + group - 1) / group) * d.batch < 2 * (int64_t)sms) group /= 2;
   dim3 gg((unsigned)nrt, (unsigned)((nct + group - 1) / group), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_ozaki",
             ozaki_gemm_kernel<false><<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp,
