@@ -23,8 +23,9 @@
 //     exponents; columns: U12 -> digit tiles B[col tile][re/im][digit] (32 x 32 BF16) and the
 //     column exponents; the seven digit tiles of one part are consecutive, so digits
 //     q .. 6 form one (32 (7 - q)) x 32 operand;
-//   ozaki_gemm: one CTA of 512 threads per 128-row tile and group of four 32-column tiles:
-//     the 14 A digit tiles (112 KB) and one B tile (28 KB) arrive in shared memory by TMA bulk
+//   ozaki_gemm: a persistent kernel, one CTA of 512 threads per SM walking a slice of the
+//     128 x 32 output tiles: the 14 A digit tiles of the current row tile (112 KB) and one B
+//     tile (28 KB) arrive in shared memory by TMA bulk
 //     copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (7 - p)
 //     multiplies X_p by the stacked Y_0 .. Y_{6-p} and accumulates X_p Y_q into the TMEM
 //     columns of T_{p+q} (Re: 32 d, Im: 224 + 32 d), so 56 MMAs (7 digits x 2 K-steps x 4
@@ -270,8 +271,6 @@ __device__ __forceinline__ double scaled_i64(long long v, int s) {
   return (v == 0 || e <= 0) ? 0.0 : __longlong_as_double((long long)bits);
 }
 
-constexpr int kOzGroupMax = 8; // column tiles per CTA (the A tiles are loaded once for all of them):
-                               // 1..8, from the launch-shape table (default 4)
 constexpr int kOzThreads = 512; // four threads per output row: warps w, w + 4, w + 8, w + 12 share
                                 // the TMEM lanes 32 (w % 4) .. and take a quarter of the columns each
 
@@ -364,53 +363,86 @@ __device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long 
   }
 }
 
-// One CTA of 512 threads per (row tile, group of `group` column tiles, matrix): four threads
-// per output row (warps w, w + 4, w + 8, w + 12 share the TMEM lanes 32 (w % 4) .. and take 8
-// of the 32 columns each), so that four warps per SM sub-partition keep its FP64 pipe busy.
-// Shared memory: the 14 A digit tiles (112 KB, loaded once) and one B tile (28 KB).  Per
-// column tile t:
-//   1. wait for tile t's products; thread 0 starts the bulk copy of tile t + 1's B tile;
+// A persistent kernel: one CTA of 512 threads per SM walks a contiguous slice of the launch's
+// tiles (matrix, 128-row tile, 32-column tile; column tiles innermost).  Four threads per
+// output row (warps w, w + 4, w + 8, w + 12 share the TMEM lanes 32 (w % 4) .. and take 8 of
+// the 32 columns each), so that four warps per SM sub-partition keep its FP64 pipe busy.
+// Shared memory: the 14 A digit tiles of the current row tile (112 KB) and one B tile
+// (28 KB).  Per tile t, with t' the CTA's next tile:
+//   1. wait for tile t's products; thread 0 starts the bulk copies of t''s B tile and, when
+//      t' starts another row tile, of its A tiles (both buffers are free once t's MMAs are
+//      done);
 //   2. every thread reads its lane's accumulators for its 8 columns and forms the integers v;
-//   3. once every thread has read the TMEM, thread 0 prefetches tile t + 1's A22 entries into
-//      L2 and issues its 56 MMAs, while the other threads subtract tile t's products from
-//      their A22 entries (doubles built from v by integer operations, one FP64 subtraction per
-//      real entry) and store them; warps 4, 8 and 12 also take warp 0's entries (handed over
-//      in shared memory): the FP64 work of one tile runs under the tensor work of the next.
-// TRSM: a single column tile whose products are assigned into U12.
+//   3. once every thread has read the TMEM (and t''s tiles have arrived), thread 0 prefetches
+//      t''s A22 entries into L2 and issues its 56 MMAs, while the other threads subtract t's
+//      products from their A22 entries (doubles built from v by integer operations, one FP64
+//      subtraction per real entry) and store them; warps 4, 8 and 12 also take warp 0's
+//      entries (handed over in shared memory).  The FP64 work of one tile runs under the
+//      tensor work of the next, and a new row tile's A digits load under the epilogue.
+// TRSM: the tiles are (matrix, 128-row tile) with one column tile, whose products are
+// assigned into U12.
 template <bool TRSM>
-__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb,
+__global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, double2* __restrict__ A, int64_t k, int kb0,
                                                               int64_t rest, int64_t nrt, int64_t nct,
                                                               const unsigned char* __restrict__ digA,
                                                               const unsigned char* __restrict__ digB,
                                                               const int* __restrict__ rowexp,
                                                               const int* __restrict__ colexp,
-                                                              int* __restrict__ timeout_flag, int group) {
+                                                              int* __restrict__ timeout_flag) {
   extern __shared__ __align__(1024) unsigned char osm[];
   __shared__ __align__(8) uint64_t mbar_a, mbar_b, mbar_mma;
   __shared__ uint32_t tmem_base;
   __shared__ int sce[kOzCols];  // column exponents of the current tile
   __shared__ longlong2 shand[8 * 32];  // warp 0's integers, handed to warps 4, 8 and 12
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t rt = blockIdx.x, b = blockIdx.z;
-  const int64_t ct0 = blockIdx.y * (int64_t)group;
-  // a grouped batch: this matrix's panel width and trailing size; CTAs past its trailing
-  // block leave before any barrier or tensor-memory allocation
-  const int64_t n = d.order(b);
-  if (TRSM ? k + kNB_oz > n : k + kb >= n) return;
-  kb = (int)((k + kb < n) ? kb : n - k);  // the launch's panel width (32, or 16 inside a two-level panel)
-  // output rows: trailing rows of A22, or (TRSM) the columns of A12; output columns: the
-  // columns of A22 right of the panel (appended right-hand sides included, at most the launch's
-  // `rest`), or the 32 rows of U12
-  const int64_t rest_b = TRSM ? n + d.extra - k - kb : n - k - kb;
-  const int64_t rest_cb = TRSM ? kb : min(rest, n + d.extra - k - kb);
-  if (rt * kOzRows >= rest_b || ct0 * kOzCols >= rest_cb) return;
-  // TRSM: one 32-column tile, the rows of U12 (the output is U12 transposed)
-  const int64_t nct_b = TRSM ? 1 : (rest_cb + kOzCols - 1) / kOzCols;
-  const int ntile = (int)((nct_b - ct0) < group ? (nct_b - ct0) : group);
+  const int64_t ntiles = d.batch * nrt * nct;
+  const int64_t g0 = blockIdx.x * ntiles / gridDim.x, g1 = (blockIdx.x + 1) * ntiles / gridDim.x;
+  // tile g: matrix b, row tile rt, column tile ct, and its geometry (a grouped batch: the
+  // matrix's own order, panel width and trailing sizes; tiles past them are skipped)
+  struct Tile {  // (32-bit fields: matrix orders and tile counts stay far below 2^31)
+    int b, rt, ct, n, rest_b, rest_cb, kb;
+  };
+  // the geometry of tile (T.b, T.rt, T.ct); false for a tile past its matrix's trailing block
+  auto fill = [&](Tile& T) -> bool {
+    const int64_t nb = d.order(T.b);
+    T.n = (int)nb;
+    if (TRSM ? k + kNB_oz > nb : k + kb0 >= nb) return false;
+    T.kb = (int)((k + kb0 < nb) ? kb0 : nb - k);  // 32, or 16 inside a two-level panel
+    // output rows: trailing rows of A22, or (TRSM) the columns of A12; output columns: the
+    // columns of A22 right of the panel (appended right-hand sides included, at most the
+    // launch's `rest`), or the 32 rows of U12
+    T.rest_b = (int)(TRSM ? nb + d.extra - k - T.kb : nb - k - T.kb);
+    T.rest_cb = (int)(TRSM ? T.kb : min(rest, nb + d.extra - k - T.kb));
+    return T.rt * kOzRows < T.rest_b && T.ct * kOzCols < T.rest_cb;
+  };
+  // the first live tile at or after tile g (whose indices T holds) in the slice; the indices
+  // advance by counting (no divisions)
+  auto next_live = [&](int64_t g, Tile& T) {
+    while (g < g1 && !fill(T)) {
+      ++g;
+      if (++T.ct == (int)nct) {
+        T.ct = 0;
+        if (++T.rt == (int)nrt) { T.rt = 0; ++T.b; }
+      }
+    }
+    return g;
+  };
+  auto advance = [&](Tile& T) {
+    if (++T.ct == (int)nct) {
+      T.ct = 0;
+      if (++T.rt == (int)nrt) { T.rt = 0; ++T.b; }
+    }
+  };
+  Tile cur;
+  cur.ct = (int)(g0 % nct);
+  cur.rt = (int)((g0 / nct) % nrt);
+  cur.b = (int)(g0 / (nct * nrt));
+  int64_t g = next_live(g0, cur);
+  if (g >= g1) return;  // nothing here: leave before any barrier or tensor-memory allocation
   unsigned char* As = osm;
   unsigned char* Bs = osm + kOzABytes;
-  const unsigned char* srcA = digA + (b * nrt + rt) * (int64_t)kOzABytes;
-  auto srcB = [&](int64_t ct) { return digB + (b * nct + ct) * (int64_t)kOzBBytes; };
+  auto srcA = [&](const Tile& T) { return digA + ((int64_t)T.b * nrt + T.rt) * (int64_t)kOzABytes; };
+  auto srcB = [&](const Tile& T) { return digB + ((int64_t)T.b * nct + T.ct) * (int64_t)kOzBBytes; };
   if (tid == 0) {
     tc::mbar_init(&mbar_a, 1);
     tc::mbar_init(&mbar_b, 1);
@@ -422,29 +454,27 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
   const int lrow = tid & (kOzRows - 1), quarter = tid >> 7;  // TMEM lane (output row) and column quarter
-  const int64_t r = rt * kOzRows + lrow;       // row of the trailing block
-  const bool row_live = r < rest_b;
-  const int er = row_live ? rowexp[b * (d.n + d.extra) + r] : 0;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  double2* Ab = A + d.offset(b);
-  double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
-  double2* ucol = Ab + k + (k + kb + r) * n;         // TRSM: column k + kb + r of U12
-  const int nrow = (int)min((int64_t)kOzRows, rest_b - rt * kOzRows);  // live rows of the tile
-  const double2* ctile = Ab + (k + kb + rt * kOzRows) + (k + kb) * n;  // the row tile of A22
-  auto prefetch_c = [&](int64_t ct) {  // one thread: the tile's A22 columns into L2
-    const int nc = (int)min((int64_t)kOzCols, rest_cb - ct * kOzCols);
-    for (int c = 0; c < nc; ++c) tc::bulk_prefetch_l2(ctile + (ct * kOzCols + c) * n, (uint32_t)nrow * 16u);
+  // the A22 tile's columns into L2 (one thread)
+  auto prefetch_c = [&](const Tile& T) {
+    const double2* Ab = A + d.offset(T.b);
+    const int nrow = min(kOzRows, T.rest_b - T.rt * kOzRows);
+    const int nc = min(kOzCols, T.rest_cb - T.ct * kOzCols);
+    const double2* ctile = Ab + (k + T.kb + (int64_t)T.rt * kOzRows) + (k + T.kb + (int64_t)T.ct * kOzCols) * T.n;
+    for (int c = 0; c < nc; ++c) tc::bulk_prefetch_l2(ctile + (int64_t)c * T.n, (uint32_t)nrow * 16u);
   };
-  // copies and products issued / waited for (identical in every thread; for the drain)
-  int a_iss = 0, b_iss = 0, m_iss = 0, a_wt = 0, b_wt = 0, m_wt = 0;
+  // copies and products waited for, and those issued but not yet waited for (bits 1: A,
+  // 2: B, 4: products); identical in every thread
+  int a_wt = 0, b_wt = 0, m_wt = 0, pend = 0;
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(&mbar_a, kOzABytes);
-    for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, srcA + q, 16384, &mbar_a);
+    const unsigned char* sa = srcA(cur);
+    for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, sa + q, 16384, &mbar_a);
     tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
-    tc::bulk_g2s(Bs, srcB(ct0), kOzBBytes, &mbar_b);
-    if (!TRSM) prefetch_c(ct0);
+    tc::bulk_g2s(Bs, srcB(cur), kOzBBytes, &mbar_b);
+    if (!TRSM) prefetch_c(cur);
   }
-  a_iss = b_iss = 1;
+  pend = 3;
   bool failed = false;
   {
     bool ok = tc::mbar_wait(&mbar_a, 0u, kOzWaitPolls);
@@ -453,32 +483,47 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
       failed = true;
     } else {
       a_wt = b_wt = 1;
+      pend = 0;
       if (tid == 0) {
         tc::fence_after_sync();
         const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
 #pragma unroll 1
-        for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, kb);
+        for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, cur.kb);
         tc::mma_commit(&mbar_mma);
       }
-      m_iss = 1;
+      pend = 4;
     }
   }
-  for (int t = 0; t < ntile && !failed; ++t) {
-    const int64_t ct = ct0 + t;
-    const bool more = t + 1 < ntile;
-    bool ok = tc::mbar_wait(&mbar_mma, (uint32_t)(t & 1), kOzWaitPolls);
-    if (__syncthreads_or(!ok)) { failed = true; break; }
-    ++m_wt;
-    tc::fence_after_sync();
-    // the B tile is free (tile t's products are done): bring in tile t + 1's
-    if (tid == 0 && more) {
-      tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
-      tc::bulk_g2s(Bs, srcB(ct + 1), kOzBBytes, &mbar_b);
+  while (!failed) {
+    int64_t gn;
+    bool more, new_a;
+    Tile nxt = cur;
+    {
+      advance(nxt);
+      gn = next_live(g + 1, nxt);
+      more = gn < g1;
+      new_a = more && (nxt.b != cur.b || nxt.rt != cur.rt);
+      bool ok = tc::mbar_wait(&mbar_mma, (uint32_t)(m_wt & 1), kOzWaitPolls);
+      if (__syncthreads_or(!ok)) { failed = true; break; }
+      ++m_wt;
+      pend &= ~4;
+      tc::fence_after_sync();
+      // the B tile and the A tiles are free (this tile's products are done): bring in the next
+      if (tid == 0 && more) {
+        tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
+        tc::bulk_g2s(Bs, srcB(nxt), kOzBBytes, &mbar_b);
+        if (new_a) {
+          tc::mbar_arrive_expect_tx(&mbar_a, kOzABytes);
+          const unsigned char* sa = srcA(nxt);
+          for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, sa + q, 16384, &mbar_a);
+        }
+      }
     }
-    if (more) ++b_iss;
+    if (more) pend |= 2;
+    if (new_a) pend |= 1;
     if (warp == 1) {
-      const int64_t c = ct * kOzCols + lane;
-      sce[lane] = c < rest_cb ? colexp[b * (d.n + d.extra) + c] : 0;
+      const int c = cur.ct * kOzCols + lane;
+      sce[lane] = c < cur.rest_cb ? colexp[(int64_t)cur.b * (d.n + d.extra) + c] : 0;
     }
     long long vr[8], vi[8];
     ozaki_levels_to_int(trow, quarter * 8, vr, vi);
@@ -490,23 +535,35 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
       for (int q = 0; q < 8; ++q) shand[q * 32 + lane] = make_longlong2(vr[q], vi[q]);
     }
     bool okw = true;
-    if (more) okw = tc::mbar_wait(&mbar_b, (uint32_t)((t + 1) & 1), kOzWaitPolls);
+    if (more) okw = tc::mbar_wait(&mbar_b, (uint32_t)(b_wt & 1), kOzWaitPolls);
+    if (new_a && okw) okw = tc::mbar_wait(&mbar_a, (uint32_t)(a_wt & 1), kOzWaitPolls);
     // every TMEM read of this tile is done before thread 0 issues the next products
     tc::fence_before_sync();
     if (__syncthreads_or(!okw)) { failed = true; break; }
     if (more) ++b_wt;
+    if (new_a) ++a_wt;
+    pend &= ~3;
     tc::fence_after_sync();
     if (more && tid == 0) {
-      if (!TRSM) prefetch_c(ct + 1);
+      if (!TRSM) prefetch_c(nxt);
       const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
 #pragma unroll 1
-      for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, kb);
+      for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, nxt.kb);
       tc::mma_commit(&mbar_mma);
     }
-    if (more) ++m_iss;
+    if (more) pend |= 4;
+    // this tile's geometry
+    const int64_t n = cur.n;
+    const int64_t kb = cur.kb;
+    const int r = cur.rt * kOzRows + lrow;  // row of the trailing block
+    const bool row_live = r < cur.rest_b;
+    const int er = row_live ? rowexp[(int64_t)cur.b * (d.n + d.extra) + r] : 0;
+    double2* Ab = A + d.offset(cur.b);
+    double2* crow = Ab + (k + kb + r) + (k + kb) * n;  // this thread's row of A22
+    double2* ucol = Ab + k + (k + kb + r) * n;         // TRSM: column k + kb + r of U12
     // v 2^(e_i + f_j - 46) as a double by integer operations, one FP64 subtraction per real entry
     if (!(handoff && warp == 0)) {
-      const int64_t cbase = ct * kOzCols + quarter * 8;
+      const int cbase = cur.ct * kOzCols + quarter * 8;
       // warp 0's entries q0 .. q0 + nx - 1 (column quarter 0): three each for warps 4 and 8, two
       // for warp 12
       const bool recv = handoff && (warp & 3) == 0;
@@ -515,14 +572,14 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
       long long xr[3], xi[3];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const bool live = row_live && cbase + q < rest_cb;
-        cv[q] = (live && !TRSM) ? crow[(cbase + q) * n] : make_double2(0.0, 0.0);
+        const bool live = row_live && cbase + q < cur.rest_cb;
+        cv[q] = (live && !TRSM) ? crow[(int64_t)(cbase + q) * n] : make_double2(0.0, 0.0);
       }
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         if (j < nx) {
-          const int64_t c = ct * kOzCols + q0 + j;
-          xv[j] = (row_live && c < rest_cb) ? crow[c * n] : make_double2(0.0, 0.0);
+          const int c = cur.ct * kOzCols + q0 + j;
+          xv[j] = (row_live && c < cur.rest_cb) ? crow[(int64_t)c * n] : make_double2(0.0, 0.0);
           const longlong2 w = shand[(q0 + j) * 32 + lane];
           xr[j] = w.x;
           xi[j] = w.y;
@@ -530,8 +587,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int64_t c = cbase + q;
-        const bool live = row_live && c < rest_cb;
+        const int c = cbase + q;
+        const bool live = row_live && c < cur.rest_cb;
         const int sc = er + sce[quarter * 8 + q] - 46;
         const double sr = scaled_i64(vr[q], sc), si = scaled_i64(vi[q], sc);
         if (TRSM) {
@@ -539,28 +596,31 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
         } else {
           cv[q].x -= sr;
           cv[q].y -= si;
-          if (live) crow[c * n] = cv[q];
+          if (live) crow[(int64_t)c * n] = cv[q];
         }
       }
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         if (j < nx) {
-          const int64_t c = ct * kOzCols + q0 + j;
+          const int c = cur.ct * kOzCols + q0 + j;
           const int sc = er + sce[q0 + j] - 46;
           xv[j].x -= scaled_i64(xr[j], sc);
           xv[j].y -= scaled_i64(xi[j], sc);
-          if (row_live && c < rest_cb) crow[c * n] = xv[j];
+          if (row_live && c < cur.rest_cb) crow[(int64_t)c * n] = xv[j];
         }
       }
     }
+    if (!more) break;
+    g = gn;
+    cur = nxt;
   }
   if (failed) {
     // reported by the host as a timeout; drain the products and copies in flight (bounded)
     // before the tensor memory and shared memory are released
     if (tid == 0) atomicExch(timeout_flag, 1);
-    if (m_wt < m_iss) tc::mbar_wait(&mbar_mma, (uint32_t)(m_wt & 1), kOzWaitPolls);
-    if (a_wt < a_iss) tc::mbar_wait(&mbar_a, 0u, kOzWaitPolls);
-    if (b_wt < b_iss) tc::mbar_wait(&mbar_b, (uint32_t)(b_wt & 1), kOzWaitPolls);
+    if (pend & 4) tc::mbar_wait(&mbar_mma, (uint32_t)(m_wt & 1), kOzWaitPolls);
+    if (pend & 1) tc::mbar_wait(&mbar_a, (uint32_t)(a_wt & 1), kOzWaitPolls);
+    if (pend & 2) tc::mbar_wait(&mbar_b, (uint32_t)(b_wt & 1), kOzWaitPolls);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -573,6 +633,19 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
 // row and column exponents (n + extra per matrix, indexed b (n + extra) + row or column)
 static int64_t oz_row_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzRows - 1) / kOzRows; }
 static int64_t oz_col_tiles(const BatchDesc& d) { return (d.n + d.extra + kOzCols - 1) / kOzCols; }
+
+// the persistent GEMM kernel's grid: one CTA per SM (at most one per tile)
+template <bool TRSM>
+static unsigned oz_grid(int64_t ntiles) {
+  static const int sms = [] {
+    int dev = 0, v = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v;
+  }();
+  cudaFuncSetAttribute(ozaki_gemm_kernel<TRSM>, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem);
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, sms));
+}
 
 size_t ozaki_workspace_bytes(int64_t n, int64_t batch, int64_t extra) {
   const int64_t w = n + extra;
@@ -594,23 +667,9 @@ void ozaki_trailing_update(cudaStream_t st, LaunchCounter lc, const BatchDesc& d
   dim3 gs((unsigned)(row_ctas + col_ctas), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_ozaki_split",
             ozaki_split_kernel<<<gs, 256, 0, st>>>(d, A, k, kb, rest, nrt, nct, row_ctas, digA, digB, rowexp, colexp));
-  const size_t smem = kOzSmem;
-  cudaFuncSetAttribute(ozaki_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  // column tiles per CTA: the launch-shape table's value as the upper bound, halved while the
-  // grid would fill fewer than two waves of CTAs (one CTA per SM)
-  static const int sms = [] {
-    int dev = 0, v = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    return v;
-  }();
-  int group = lc.tile(d.n).oz_group;
-  group = group < 1 ? 1 : (group > kOzGroupMax ? kOzGroupMax : group);
-  while (group > 1 && nrt * ((nct + group - 1) / group) * d.batch < 2 * (int64_t)sms) group /= 2;
-  dim3 gg((unsigned)nrt, (unsigned)((nct + group - 1) / group), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_gemm_ozaki",
-            ozaki_gemm_kernel<false><<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp,
-                                                                 colexp, timeout_flag, group));
+            ozaki_gemm_kernel<false><<<oz_grid<false>(d.batch * nrt * nct), kOzThreads, kOzSmem, st>>>(
+                d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp, timeout_flag));
 }
 
 void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* A, int64_t k, void* ws,
@@ -627,12 +686,9 @@ void ozaki_trsm(cudaStream_t st, LaunchCounter lc, const BatchDesc& d, double2* 
   dim3 gs((unsigned)(row_ctas + 1), (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_trsm_ozaki_prep",
             ozaki_trsm_prep_kernel<<<gs, 256, 0, st>>>(d, A, k, rest, nrt, row_ctas, digA, digB, rowexp, colexp));
-  const size_t smem = kOzSmem;
-  cudaFuncSetAttribute(ozaki_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 gg((unsigned)nrt, 1u, (unsigned)d.batch);
   MH_LAUNCH(lc, st, "lu_trsm_ozaki",
-            ozaki_gemm_kernel<true><<<gg, kOzThreads, smem, st>>>(d, A, k, kb, rest, nrt, nct, digA, digB, rowexp,
-                                                                colexp, timeout_flag, 1));
+            ozaki_gemm_kernel<true><<<oz_grid<true>(d.batch * nrt), kOzThreads, kOzSmem, st>>>(
+                d, A, k, kb, rest, nrt, nct, digA, digB, rowexp, colexp, timeout_flag));
 }
 
 }  // namespace mh
