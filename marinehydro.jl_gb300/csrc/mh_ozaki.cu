@@ -371,10 +371,10 @@ __device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long 
 // (28 KB).  Per tile t, with t' the CTA's next tile:
 //   1. wait for tile t's products; thread 0 starts the bulk copies of t''s B tile and, when
 //      t' starts another row tile, of its A tiles (both buffers are free once t's MMAs are
-//      done);
+//      done); every thread prefetches its entries of t''s A22 tile into L2;
 //   2. every thread reads its lane's accumulators for its 8 columns and forms the integers v;
-//   3. once every thread has read the TMEM (and t''s tiles have arrived), thread 0 prefetches
-//      t''s A22 entries into L2 and issues its 56 MMAs, while the other threads subtract t's
+//   3. once every thread has read the TMEM (and t''s tiles have arrived), thread 0 issues t''s
+//      56 MMAs, while the other threads subtract t's
 //      products from their A22 entries (doubles built from v by integer operations, one FP64
 //      subtraction per real entry) and store them; warps 4, 8 and 12 also take warp 0's
 //      entries (handed over in shared memory).  The FP64 work of one tile runs under the
@@ -455,13 +455,17 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
   const uint32_t tmem = tmem_base;
   const int lrow = tid & (kOzRows - 1), quarter = tid >> 7;  // TMEM lane (output row) and column quarter
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  // the A22 tile's columns into L2 (one thread)
+  // this thread's 8 entries of a tile of A22 into L2 (plain per-thread prefetches: a warp's 32
+  // rows of one column are 512 contiguous bytes)
   auto prefetch_c = [&](const Tile& T) {
-    const double2* Ab = A + d.offset(T.b);
-    const int nrow = min(kOzRows, T.rest_b - T.rt * kOzRows);
-    const int nc = min(kOzCols, T.rest_cb - T.ct * kOzCols);
-    const double2* ctile = Ab + (k + T.kb + (int64_t)T.rt * kOzRows) + (k + T.kb + (int64_t)T.ct * kOzCols) * T.n;
-    for (int c = 0; c < nc; ++c) tc::bulk_prefetch_l2(ctile + (int64_t)c * T.n, (uint32_t)nrow * 16u);
+    const int rr = T.rt * kOzRows + lrow;
+    if (rr >= T.rest_b) return;
+    const double2* cr = A + d.offset(T.b) + (k + T.kb + rr) + (k + T.kb) * (int64_t)T.n;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int c = T.ct * kOzCols + quarter * 8 + q;
+      if (c < T.rest_cb) asm volatile("prefetch.global.L2 [%0];" ::"l"(cr + (int64_t)c * T.n));
+    }
   };
   // copies and products waited for, and those issued but not yet waited for (bits 1: A,
   // 2: B, 4: products); identical in every thread
@@ -472,8 +476,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     for (int q = 0; q < kOzABytes; q += 16384) tc::bulk_g2s(As + q, sa + q, 16384, &mbar_a);
     tc::mbar_arrive_expect_tx(&mbar_b, kOzBBytes);
     tc::bulk_g2s(Bs, srcB(cur), kOzBBytes, &mbar_b);
-    if (!TRSM) prefetch_c(cur);
   }
+  if (!TRSM) prefetch_c(cur);
   pend = 3;
   bool failed = false;
   {
@@ -521,6 +525,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     }
     if (more) pend |= 2;
     if (new_a) pend |= 1;
+    if (!TRSM && more) prefetch_c(nxt);
     if (warp == 1) {
       const int c = cur.ct * kOzCols + lane;
       sce[lane] = c < cur.rest_cb ? colexp[(int64_t)cur.b * (d.n + d.extra) + c] : 0;
@@ -545,7 +550,6 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     pend &= ~3;
     tc::fence_after_sync();
     if (more && tid == 0) {
-      if (!TRSM) prefetch_c(nxt);
       const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
 #pragma unroll 1
       for (int p = 0; p < kOzDigits; ++p) ozaki_issue_digit(tmem, a0, b0, p, nxt.kb);

@@ -233,10 +233,5 @@ __device__ __forceinline__ void tmem_ld8x2(const uint32_t (&taddr)[2], float (&v
     for (int q = 0; q < 8; ++q) v[g][q] = __uint_as_float(r[g][q]);
 }
 
-// L2 prefetch of `bytes` (multiple of 16) of global memory at a 16-byte aligned address
-__device__ __forceinline__ void bulk_prefetch_l2(const void* src_gmem, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
-}
-
 }  // namespace tc
 }  // namespace mh
