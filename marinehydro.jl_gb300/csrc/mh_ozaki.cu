@@ -395,17 +395,17 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
   __shared__ int sce[kOzCols];  // column exponents of the current tile
   __shared__ longlong2 shand[8 * 32];  // warp 0's integers, handed to warps 4, 8 and 12
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t ntiles = d.batch * nrt * nct;
-  const int64_t g0 = blockIdx.x * ntiles / gridDim.x, g1 = (blockIdx.x + 1) * ntiles / gridDim.x;
-  // tile g: matrix b, row tile rt, column tile ct, and its geometry (a grouped batch: the
-  // matrix's own order, panel width and trailing sizes; tiles past them are skipped)
+  // The launch's tiles are enumerated matrix by matrix (only those inside each matrix's
+  // trailing block: a grouped batch's matrices have orders of their own), row tiles by
+  // column tiles within a matrix, and cut into gridDim.x equal contiguous slices.
   struct Tile {  // (32-bit fields: matrix orders and tile counts stay far below 2^31)
-    int b, rt, ct, n, rest_b, rest_cb, kb;
+    int b, rt, ct, n, rest_b, rest_cb, kb, nr, nc;
   };
-  // the geometry of tile (T.b, T.rt, T.ct); false for a tile past its matrix's trailing block
+  // the geometry of matrix T.b at this panel step; false when its trailing block is empty
   auto fill = [&](Tile& T) -> bool {
     const int64_t nb = d.order(T.b);
     T.n = (int)nb;
+    T.nr = T.nc = 0;
     if (TRSM ? k + kNB_oz > nb : k + kb0 >= nb) return false;
     T.kb = (int)((k + kb0 < nb) ? kb0 : nb - k);  // 32, or 16 inside a two-level panel
     // output rows: trailing rows of A22, or (TRSM) the columns of A12; output columns: the
@@ -413,32 +413,69 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     // launch's `rest`), or the 32 rows of U12
     T.rest_b = (int)(TRSM ? nb + d.extra - k - T.kb : nb - k - T.kb);
     T.rest_cb = (int)(TRSM ? T.kb : min(rest, nb + d.extra - k - T.kb));
-    return T.rt * kOzRows < T.rest_b && T.ct * kOzCols < T.rest_cb;
+    if (T.rest_b <= 0 || T.rest_cb <= 0) return false;
+    T.nr = (T.rest_b + kOzRows - 1) / kOzRows;
+    T.nc = (T.rest_cb + kOzCols - 1) / kOzCols;
+    return true;
   };
-  // the first live tile at or after tile g (whose indices T holds) in the slice; the indices
-  // advance by counting (no divisions)
-  auto next_live = [&](int64_t g, Tile& T) {
-    while (g < g1 && !fill(T)) {
-      ++g;
-      if (++T.ct == (int)nct) {
-        T.ct = 0;
-        if (++T.rt == (int)nrt) { T.rt = 0; ++T.b; }
-      }
-    }
-    return g;
-  };
+  // the tile after T in the enumeration (no divisions)
   auto advance = [&](Tile& T) {
-    if (++T.ct == (int)nct) {
-      T.ct = 0;
-      if (++T.rt == (int)nrt) { T.rt = 0; ++T.b; }
-    }
+    if (++T.ct < T.nc) return;
+    T.ct = 0;
+    if (++T.rt < T.nr) return;
+    T.rt = 0;
+    do {
+      ++T.b;
+    } while (T.b < d.batch && !fill(T));
   };
+  // warp 0 counts every matrix's tiles and locates the first tile of this CTA's slice
+  __shared__ int s_slice[3];
+  if (warp == 0) {
+    long long tot = 0;
+    for (int64_t b0 = 0; b0 < d.batch; b0 += 32) {
+      Tile T;
+      T.b = (int)(b0 + lane);
+      int cnt = (b0 + lane < d.batch && fill(T)) ? T.nr * T.nc : 0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+      tot += cnt;
+    }
+    const long long l0 = blockIdx.x * tot / gridDim.x, l1 = (blockIdx.x + 1) * tot / gridDim.x;
+    long long base = 0;
+    int fb = -1, fj = 0;
+    for (int64_t b0 = 0; b0 < d.batch && fb < 0 && l1 > l0; b0 += 32) {
+      Tile T;
+      T.b = (int)(b0 + lane);
+      const int cnt = (b0 + lane < d.batch && fill(T)) ? T.nr * T.nc : 0;
+      int incl = cnt;  // inclusive prefix sum over the lanes
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+      }
+      const int chunk = __shfl_sync(0xffffffffu, incl, 31);
+      if (base + chunk > l0) {  // matrix b0 + first holds tile l0: its tiles are [base + incl - cnt, base + incl)
+        const unsigned hit = __ballot_sync(0xffffffffu, cnt > 0 && base + incl > l0);
+        const int first = __ffs(hit) - 1;
+        fb = (int)b0 + first;
+        fj = (int)(l0 - base - __shfl_sync(0xffffffffu, incl - cnt, first));
+      }
+      base += chunk;
+    }
+    if (lane == 0) {
+      s_slice[0] = fb;
+      s_slice[1] = fj;
+      s_slice[2] = (int)(l1 - l0);
+    }
+  }
+  __syncthreads();
+  int left = s_slice[2];  // tiles of the slice not yet finished
+  if (left <= 0 || s_slice[0] < 0) return;  // nothing here: leave before any tensor-memory allocation
   Tile cur;
-  cur.ct = (int)(g0 % nct);
-  cur.rt = (int)((g0 / nct) % nrt);
-  cur.b = (int)(g0 / (nct * nrt));
-  int64_t g = next_live(g0, cur);
-  if (g >= g1) return;  // nothing here: leave before any barrier or tensor-memory allocation
+  cur.b = s_slice[0];
+  fill(cur);
+  cur.rt = s_slice[1] / cur.nc;
+  cur.ct = s_slice[1] - cur.rt * cur.nc;
   unsigned char* As = osm;
   unsigned char* Bs = osm + kOzABytes;
   auto srcA = [&](const Tile& T) { return digA + ((int64_t)T.b * nrt + T.rt) * (int64_t)kOzABytes; };
@@ -499,13 +536,11 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
     }
   }
   while (!failed) {
-    int64_t gn;
     bool more, new_a;
     Tile nxt = cur;
     {
-      advance(nxt);
-      gn = next_live(g + 1, nxt);
-      more = gn < g1;
+      more = left > 1;
+      if (more) advance(nxt);
       new_a = more && (nxt.b != cur.b || nxt.rt != cur.rt);
       bool ok = tc::mbar_wait(&mbar_mma, (uint32_t)(m_wt & 1), kOzWaitPolls);
       if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -615,7 +650,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) ozaki_gemm_kernel(BatchDesc d, 
       }
     }
     if (!more) break;
-    g = gn;
+    --left;
     cur = nxt;
   }
   if (failed) {
