@@ -250,11 +250,12 @@ int mh_batch_release(mh_context* ctx);
    the launch shapes of the batched LU that depend on the matrix order n.  Entry q
    covers n <= n_max[q] (ascending; the last entry covers every larger n) with four
    choices, each 1..8:
-     choices[4q+0]  32-column tiles per CTA of the FP64 tensor-core update (MH_PREC_FP64_TC)
+     choices[4q+0]  reserved (the FP64 tensor-core update, MH_PREC_FP64_TC, is a persistent
+                    kernel over equal slices of its tiles; the value is kept and ignored)
      choices[4q+1]  128-column tiles per CTA of the BF16x3 FP32 update (MH_PREC_MIXED)
      choices[4q+2]  largest thread-block cluster of the FP64 LU panel
      choices[4q+3]  largest thread-block cluster of the FP32 LU panel
-   n_entries = 0 restores the defaults (4, 4, 8, 8).  The table applies to every later
+   n_entries = 0 restores the defaults (8, 4, 8, 8).  The table applies to every later
    factorization of the context, including the captured batch graph (a changed table
    re-captures it).  The shapes change only the schedule: each output entry is computed
    by the same arithmetic. */
@@ -263,7 +264,7 @@ int mh_tile_table_set(mh_context* ctx, int64_t n_entries, const int64_t* n_max, 
 int mh_tile_table_get(mh_context* ctx, int64_t capacity, int64_t* n_max, int32_t* choices, int64_t* n_entries);
 /* The project's autotuner: for each order sizes[q] (ascending, 32..12000) times the
    batched factorization of `batch` random complex matrices in `precision` with every
-   candidate launch shape -- panel cluster bound 8, 4, 2 and, for the tensor-core updates,
+   candidate launch shape -- panel cluster bound 8, 4, 2 and, for the BF16x3 update,
    1, 2, 4 or 8 column tiles per CTA -- (smallest of `reps` timed runs after a warm-up,
    CUDA events on the context's stream) and installs the fastest per order bucket
    (bounds at the geometric means of neighbouring sizes).  A shape replaces the default

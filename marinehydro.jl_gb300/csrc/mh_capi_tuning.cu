@@ -91,29 +91,22 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
   if (reps < 1 || reps > 20) return fail(ctx, MH_ERR_ARG, "autotune reps must be 1..20 (got %d)", reps);
   MH_TRY(set_device(ctx));
   const TileTable saved = ctx->tiles;
-  // candidates: the cluster bound of the panel and, for the tensor-core updates, the
-  // column tiles per CTA; the first candidate is the default shape
+  // candidates: the cluster bound of the panel and, for the BF16x3 update, the column tiles
+  // per CTA; the first candidate is the default shape
   std::vector<TileChoice> cands;
   const int caps[3] = {8, 4, 2};
-  const int groups_tc[4] = {8, 4, 2, 1}, groups_bx[4] = {4, 1, 2, 8};  // the defaults first
-  const int* groups = precision == MH_PREC_FP64_TC ? groups_tc : groups_bx;
+  const int groups[4] = {4, 1, 2, 8};  // BF16x3 column tiles per CTA, the default first
   for (int cap : caps) {
-    if (precision == MH_PREC_FP64) {
+    if (precision != MH_PREC_MIXED) {  // FP64 and FP64-TC: the panel's cluster bound only
       TileChoice c;
       c.cluster_f64 = cap;
       cands.push_back(c);
       continue;
     }
     for (int gi = 0; gi < 4; ++gi) {
-      const int gr = groups[gi];
       TileChoice c;
-      if (precision == MH_PREC_MIXED) {
-        c.bx_group = gr;
-        c.cluster_f32 = cap;
-      } else {
-        c.oz_group = gr;
-        c.cluster_f64 = cap;
-      }
+      c.bx_group = groups[gi];
+      c.cluster_f32 = cap;
       cands.push_back(c);
     }
   }
@@ -156,7 +149,6 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
         c.bx_group = cands[ci].bx_group;
         c.cluster_f32 = cands[ci].cluster_f32;
       } else {
-        c.oz_group = precision == MH_PREC_FP64_TC ? cands[ci].oz_group : c.oz_group;
         c.cluster_f64 = cands[ci].cluster_f64;
       }
       ctx->tiles.n_entries = 1;
@@ -182,7 +174,6 @@ int mh_autotune(mh_context* ctx, int precision, int64_t n_sizes, const int64_t* 
         best_c.bx_group = cands[0].bx_group;
         best_c.cluster_f32 = cands[0].cluster_f32;
       } else {
-        if (precision == MH_PREC_FP64_TC) best_c.oz_group = cands[0].oz_group;
         best_c.cluster_f64 = cands[0].cluster_f64;
       }
     }

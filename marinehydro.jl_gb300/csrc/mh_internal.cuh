@@ -54,7 +54,7 @@ struct Profiler;
 // bucket by mh_autotune (or set with mh_tile_table_set).  The defaults are the
 // hand-picked shapes the table starts from.
 struct TileChoice {
-  int oz_group = 8;     // 32-column tiles per CTA of the Ozaki (FP64 tensor-core) update, 1..8 (at most)
+  int oz_group = 8;     // reserved: the Ozaki (FP64 tensor-core) update is a persistent kernel
   int bx_group = 4;     // 128-column tiles per CTA of the BF16x3 (FP32) update, 1..8
   int cluster_f64 = 8;  // largest thread-block cluster of the FP64 LU panel, 1..8
   int cluster_f32 = 8;  // largest thread-block cluster of the FP32 LU panel, 1..8

@@ -5,8 +5,9 @@
 
 For each precision (fp64, mixed, fp64_tc) and matrix order, mh_autotune times the
 factorization of `batch` random complex matrices with every candidate shape (panel
-cluster bound 8 / 4 / 2; 1 / 2 / 4 / 8 column tiles per CTA of the tensor-core
-updates) and keeps the fastest per order bucket.  The defaults are the settings of
+cluster bound 8 / 4 / 2; 1 / 2 / 4 / 8 column tiles per CTA of the BF16x3 update; the
+FP64 tensor-core update is a persistent kernel and has no shape to tune) and keeps the
+fastest per order bucket.  The defaults are the settings of
 the table shipped in this directory (tile_table_gb300.json, made on a GB300).  Load
 a table with marinehydro_gb300.load_tile_table(path).  Needs a CUDA device.
 """
