@@ -246,10 +246,10 @@ WU_FLOPS_PER_UNORDERED_PAIR = 214
 # ncu figures of the dominant kernels (small cases of the same kernels; the capture command
 # of each is kept with its summary under profiles/)
 NCU = {
-    "lu_gemm_ozaki": {"tensor_pipe_active": 0.244, "fp64_pipe_active": 0.273, "alu_pipe_active": 0.312,
-                      "dram_bytes_per_trailing_entry": 51.0,
+    "lu_gemm_ozaki": {"tensor_pipe_active": 0.295, "fp64_pipe_active": 0.322, "alu_pipe_active": 0.438,
+                      "dram_bytes_per_trailing_entry": 30.0,
                       "capture": "one launch of the 8-frequency sweep (trailing block 1328 x 1328, 8 matrices, "
-                                 "968 CTAs); C read and written (32 B per entry) plus the digit tiles"},
+                                 "persistent grid of 152 CTAs); C read and written plus the digit tiles"},
     "assemble_wave_wu": {"fp64_pipe_active": 0.686, "alu_pipe_active": 0.288,
                          "dram_bytes_per_unordered_pair": 398e6 / 4.0e6},
     "lu_gemm_f64": {"fp64_pipe_active": 0.977, "dram_bytes_per_launch": 1.236e9},
