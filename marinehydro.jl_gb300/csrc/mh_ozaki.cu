@@ -11,10 +11,11 @@
 // and every T_d is an integer of magnitude at most (d + 1) 2^20 < 2^23, so the tensor cores
 // accumulate it exactly in FP32 (K = 32, d + 1 <= 7 digit pairs, 2 real products per
 // complex term).  Terms with p + q > 6 are dropped: they are below 2^-55 of the row/column
-// scale product, the size of FP64 rounding.  The T_d are combined exactly in 64-bit integers
-// (d = 0..3 and 4..6 separately), rounded once to a 53-bit integer, scaled by the power of
-// two and subtracted from A22 -- one FP64 operation per real element instead of the 128 FMAs
-// of the FP64 update.  (Eight base-128 digits need 36 digit products for the same 55 bits;
+// scale product, the size of FP64 rounding.  T_0..T_3 are combined exactly in 64-bit integers,
+// T_4..T_6 (which only need to be right to a fraction of the last unit) in FP32, and the sum
+// is rounded to a 53-bit integer within 0.76 of the exact value, scaled by the power of two
+// and subtracted from A22 -- one FP64 operation per real element instead of the 128 FMAs of
+// the FP64 update.  (Eight base-128 digits need 36 digit products for the same 55 bits;
 // seven base-256 digits need 28.)
 //
 // Kernels per panel step (all batched over the matrices of the sweep):
@@ -25,8 +26,8 @@
 //     q .. 6 form one (32 (7 - q)) x 32 operand;
 //   ozaki_gemm: a persistent kernel, one CTA of 512 threads per SM walking a slice of the
 //     128 x 32 output tiles: the 14 A digit tiles of the current row tile (112 KB) and one B
-//     tile (28 KB) arrive in shared memory by TMA bulk
-//     copies.  Per column tile and digit p of L21, one tcgen05.mma with N = 32 (7 - p)
+//     tile (28 KB) arrive in shared memory by TMA bulk copies.  Per column tile and digit p
+//     of L21, one tcgen05.mma with N = 32 (7 - p)
 //     multiplies X_p by the stacked Y_0 .. Y_{6-p} and accumulates X_p Y_q into the TMEM
 //     columns of T_{p+q} (Re: 32 d, Im: 224 + 32 d), so 56 MMAs (7 digits x 2 K-steps x 4
 //     real products) cover the 28 digit pairs.  (16-column tiles, whose two accumulator sets
@@ -39,6 +40,8 @@
 //     accumulators of a tile fill 448 of the 512 TMEM columns, so the TMEM reads of a tile
 //     come first); four warps per SM sub-partition keep its FP64 pipe busy, and each tile of
 //     A22 is prefetched into L2 one tile ahead.
+//   The triangular solve of a panel step (U12 = L11^-1 A12) runs as the same product with
+//   ozaki_trsm_prep cutting the operands and ozaki_gemm<true> assigning the products.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
