@@ -367,7 +367,7 @@ __device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long 
 }
 
 // A persistent kernel: one CTA of 512 threads per SM walks a contiguous slice of the launch's
-// tiles (matrix, 128-row tile, 32-column tile; column tiles innermost).  Four threads per
+// live tiles (matrix, 128-row tile, 32-column tile; column tiles innermost).  Four threads per
 // output row (warps w, w + 4, w + 8, w + 12 share the TMEM lanes 32 (w % 4) .. and take 8 of
 // the 32 columns each), so that four warps per SM sub-partition keep its FP64 pipe busy.
 // Shared memory: the 14 A digit tiles of the current row tile (112 KB) and one B tile
@@ -377,11 +377,11 @@ __device__ __forceinline__ void ozaki_levels_to_int(uint32_t trow, int c0, long 
 //      done); every thread prefetches its entries of t''s A22 tile into L2;
 //   2. every thread reads its lane's accumulators for its 8 columns and forms the integers v;
 //   3. once every thread has read the TMEM (and t''s tiles have arrived), thread 0 issues t''s
-//      56 MMAs, while the other threads subtract t's
-//      products from their A22 entries (doubles built from v by integer operations, one FP64
-//      subtraction per real entry) and store them; warps 4, 8 and 12 also take warp 0's
-//      entries (handed over in shared memory).  The FP64 work of one tile runs under the
-//      tensor work of the next, and a new row tile's A digits load under the epilogue.
+//      56 MMAs, while the other threads subtract t's products from their A22 entries (doubles
+//      built from v by integer operations, one FP64 subtraction per real entry) and store
+//      them; warps 4, 8 and 12 also take warp 0's entries (handed over in shared memory).
+//      The FP64 work of one tile runs under the tensor work of the next, and a new row
+//      tile's A digits load under the epilogue.
 // TRSM: the tiles are (matrix, 128-row tile) with one column tile, whose products are
 // assigned into U12.
 template <bool TRSM>
